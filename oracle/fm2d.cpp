@@ -1,0 +1,580 @@
+// ORACLE (test infrastructure only): CPU restatement of Rawlinson's fm2d fast
+// marching code in Cartesian form as shipped with MCTomo
+// (fm2d/fm2dray_cartesian.f90 modrays/gridder/bsplrefine/srtimes and
+// fm2d/fm2d_ttime.f90 travel/fouds1/fouds2/addtree/downtree/updtree/bilinear).
+// Used as the parity checker for the GPU 2D eikonal kernel. Never linked into
+// the product.
+//
+// Parity status: unpinned by reference execution (Fortran, no compiler on this
+// image); pinned by homogeneous-medium known answers and line-by-line
+// restatement. Arithmetic order follows the Fortran expressions; build with
+// -ffp-contract=off.
+//
+// Ray path tracing (rpaths, fm2dray_cartesian.f90:801-1455) is not restated
+// here: it only runs for group-velocity data (uar == 0).
+#include <cmath>
+#include <vector>
+#include <cstdlib>
+#include "oracle.h"
+
+namespace {
+
+struct FM2D {
+  // grid of nodes currently being marched (coarse or refined)
+  int nnx, nnz;
+  double gox, goz, dnx, dnz;
+  int fom;
+  // refined-box bounds (1-based, coarse node units)
+  int vnl, vnr, vnt, vnb;
+  int ld;                   // leading dimension (rows) of veln/ttn/nsts
+  std::vector<double> veln, ttn;
+  std::vector<int> nsts;
+  std::vector<int> btgx, btgz;  // heap backpointers (1-based slots)
+  int ntr;
+
+  double &V(int iz, int ix) { return veln[(size_t)(ix - 1) * ld + (iz - 1)]; }
+  double &T(int iz, int ix) { return ttn[(size_t)(ix - 1) * ld + (iz - 1)]; }
+  int &S(int iz, int ix) { return nsts[(size_t)(ix - 1) * ld + (iz - 1)]; }
+
+  // fm2d_ttime.f90:527-566 addtree
+  void addtree(int iz, int ix) {
+    ntr = ntr + 1;
+    if ((size_t)ntr >= btgx.size()) { btgx.resize(ntr * 2 + 8); btgz.resize(ntr * 2 + 8); }
+    S(iz, ix) = ntr;
+    btgx[ntr] = ix; btgz[ntr] = iz;
+    int tpc = ntr, tpp = tpc / 2;
+    while (tpp > 0) {
+      if (T(iz, ix) < T(btgz[tpp], btgx[tpp])) {
+        S(iz, ix) = tpp;
+        S(btgz[tpp], btgx[tpp]) = tpc;
+        std::swap(btgx[tpc], btgx[tpp]); std::swap(btgz[tpc], btgz[tpp]);
+        tpc = tpp; tpp = tpc / 2;
+      } else {
+        tpp = 0;
+      }
+    }
+  }
+
+  // fm2d_ttime.f90:576-640 downtree
+  void downtree() {
+    if (ntr == 1) { ntr = ntr - 1; return; }
+    S(btgz[ntr], btgx[ntr]) = 1;
+    btgx[1] = btgx[ntr]; btgz[1] = btgz[ntr];
+    ntr = ntr - 1;
+    int tpp = 1, tpc = 2 * tpp;
+    while (tpc < ntr) {
+      double rd1 = T(btgz[tpc], btgx[tpc]);
+      double rd2 = T(btgz[tpc + 1], btgx[tpc + 1]);
+      if (rd1 > rd2) tpc = tpc + 1;
+      rd1 = T(btgz[tpc], btgx[tpc]);
+      rd2 = T(btgz[tpp], btgx[tpp]);
+      if (rd1 < rd2) {
+        S(btgz[tpp], btgx[tpp]) = tpc;
+        S(btgz[tpc], btgx[tpc]) = tpp;
+        std::swap(btgx[tpc], btgx[tpp]); std::swap(btgz[tpc], btgz[tpp]);
+        tpp = tpc; tpc = 2 * tpp;
+      } else {
+        tpc = ntr + 1;
+      }
+    }
+    if (tpc == ntr) {
+      double rd1 = T(btgz[tpc], btgx[tpc]);
+      double rd2 = T(btgz[tpp], btgx[tpp]);
+      if (rd1 < rd2) {
+        S(btgz[tpp], btgx[tpp]) = tpc;
+        S(btgz[tpc], btgx[tpc]) = tpp;
+        std::swap(btgx[tpc], btgx[tpp]); std::swap(btgz[tpc], btgz[tpp]);
+      }
+    }
+  }
+
+  // fm2d_ttime.f90:650-672 updtree
+  void updtree(int iz, int ix) {
+    int tpc = S(iz, ix), tpp = tpc / 2;
+    while (tpp > 0) {
+      if (T(iz, ix) < T(btgz[tpp], btgx[tpp])) {
+        S(iz, ix) = tpp;
+        S(btgz[tpp], btgx[tpp]) = tpc;
+        std::swap(btgx[tpc], btgx[tpp]); std::swap(btgz[tpc], btgz[tpp]);
+        tpc = tpp; tpp = tpc / 2;
+      } else {
+        tpp = 0;
+      }
+    }
+  }
+
+  // fm2d_ttime.f90:248-332 fouds1 (first-order upwind)
+  void fouds1(int iz, int ix) {
+    int tsw1 = 0;
+    double travm = 0.0;
+    double slown = 1.0 / V(iz, ix);
+    for (int j = ix - 1; j <= ix + 1; j += 2) {
+      for (int k = iz - 1; k <= iz + 1; k += 2) {
+        if (j >= 1 && j <= nnx && k >= 1 && k <= nnz) {
+          int swsol = 0;
+          double a = 0, b = 0, c = 0, tref = 0;
+          if (S(iz, j) == 0) {
+            swsol = 1;
+            if (S(k, ix) == 0) {
+              double u = dnx, v = dnz;
+              double em = T(k, ix) - T(iz, j);
+              a = u * u + v * v;
+              b = -(2.0 * (u * u) * em);
+              c = (u * u) * (em * em - (v * v) * (slown * slown));
+              tref = T(iz, j);
+            } else {
+              a = 1.0; b = 0.0;
+              c = -((slown * slown) * (dnx * dnx));
+              tref = T(iz, j);
+            }
+          } else if (S(k, ix) == 0) {
+            swsol = 1;
+            a = 1.0; b = 0.0;
+            double sd = slown * dnz;
+            c = -(sd * sd);
+            tref = T(k, ix);
+          }
+          if (swsol == 1) {
+            double rd1 = b * b - 4.0 * a * c;
+            if (rd1 < 0.0) rd1 = 0.0;
+            double tdsh = (-b + std::sqrt(rd1)) / (2.0 * a);
+            double trav = tref + tdsh;
+            if (tsw1 == 1) travm = std::fmin(trav, travm);
+            else { travm = trav; tsw1 = 1; }
+          }
+        }
+      }
+    }
+    T(iz, ix) = travm;
+  }
+
+  // fm2d_ttime.f90:342-518 fouds2 (mixed-order upwind)
+  void fouds2(int iz, int ix) {
+    int tsw1 = 0;
+    double travm = 0.0;
+    double slown = 1.0 / V(iz, ix);
+    for (int j = ix - 1; j <= ix + 1; j += 2) {
+      if (!(j >= 1 && j <= nnx)) continue;
+      int swj = -1, j2;
+      if (j == ix - 1) {
+        j2 = j - 1;
+        if (j2 >= 1) { if (S(iz, j2) == 0) swj = 0; }
+      } else {
+        j2 = j + 1;
+        if (j2 <= nnx) { if (S(iz, j2) == 0) swj = 0; }
+      }
+      if (S(iz, j) == 0 && swj == 0) {
+        swj = -1;
+        if (T(iz, j) > T(iz, j2)) swj = 0;
+      } else {
+        swj = -1;
+      }
+      for (int k = iz - 1; k <= iz + 1; k += 2) {
+        if (!(k >= 1 && k <= nnz)) continue;
+        int swk = -1, k2;
+        if (k == iz - 1) {
+          k2 = k - 1;
+          if (k2 >= 1) { if (S(k2, ix) == 0) swk = 0; }
+        } else {
+          k2 = k + 1;
+          if (k2 <= nnz) { if (S(k2, ix) == 0) swk = 0; }
+        }
+        if (S(k, ix) == 0 && swk == 0) {
+          swk = -1;
+          if (T(k, ix) > T(k2, ix)) swk = 0;
+        } else {
+          swk = -1;
+        }
+        int swsol = 0;
+        double a = 0, b = 0, c = 0, tref = 0, tdiv = 1.0;
+        if (swj == 0) {
+          swsol = 1;
+          if (swk == 0) {
+            double u = 2.0 * dnx, v = 2.0 * dnz;
+            double em = 4.0 * T(iz, j) - T(iz, j2) - 4.0 * T(k, ix);
+            em = em + T(k2, ix);
+            a = v * v + u * u;
+            b = 2.0 * em * (u * u);
+            c = (u * u) * (em * em - (slown * slown) * (v * v));
+            tref = 4.0 * T(iz, j) - T(iz, j2);
+            tdiv = 3.0;
+          } else if (S(k, ix) == 0) {
+            double u = dnz, v = 2.0 * dnx;
+            double em = 3.0 * T(k, ix) - 4.0 * T(iz, j) + T(iz, j2);
+            a = v * v + 9.0 * (u * u);
+            b = 6.0 * em * (u * u);
+            c = (u * u) * (em * em - (slown * slown) * (v * v));
+            tref = T(k, ix);
+            tdiv = 1.0;
+          } else {
+            double u = 2.0 * dnx;
+            a = 1.0; b = 0.0;
+            c = -((u * u) * (slown * slown));
+            tref = 4.0 * T(iz, j) - T(iz, j2);
+            tdiv = 3.0;
+          }
+        } else if (S(iz, j) == 0) {
+          swsol = 1;
+          if (swk == 0) {
+            double u = dnx, v = 2.0 * dnz;
+            double em = 3.0 * T(iz, j) - 4.0 * T(k, ix) + T(k2, ix);
+            a = v * v + 9.0 * (u * u);
+            b = 6.0 * em * (u * u);
+            c = (u * u) * (em * em - (v * v) * (slown * slown));
+            tref = T(iz, j);
+            tdiv = 1.0;
+          } else if (S(k, ix) == 0) {
+            double u = dnx, v = dnz;
+            double em = T(k, ix) - T(iz, j);
+            a = u * u + v * v;
+            b = -(2.0 * (u * u) * em);
+            c = (u * u) * (em * em - (v * v) * (slown * slown));
+            tref = T(iz, j);
+            tdiv = 1.0;
+          } else {
+            a = 1.0; b = 0.0;
+            c = -((slown * slown) * (dnx * dnx));
+            tref = T(iz, j);
+            tdiv = 1.0;
+          }
+        } else {
+          if (swk == 0) {
+            swsol = 1;
+            double u = 2.0 * dnz;
+            a = 1.0; b = 0.0;
+            c = -((u * u) * (slown * slown));
+            tref = 4.0 * T(k, ix) - T(k2, ix);
+            tdiv = 3.0;
+          } else if (S(k, ix) == 0) {
+            swsol = 1;
+            a = 1.0; b = 0.0;
+            c = -((slown * slown) * (dnz * dnz));
+            tref = T(k, ix);
+            tdiv = 1.0;
+          }
+        }
+        if (swsol == 1) {
+          double rd1 = b * b - 4.0 * a * c;
+          if (rd1 < 0.0) rd1 = 0.0;
+          double tdsh = (-b + std::sqrt(rd1)) / (2.0 * a);
+          double trav = (tref + tdsh) / tdiv;
+          if (tsw1 == 1) travm = std::fmin(trav, travm);
+          else { travm = trav; tsw1 = 1; }
+        }
+      }
+    }
+    T(iz, ix) = travm;
+  }
+
+  void fouds(int iz, int ix) { if (fom == 0) fouds1(iz, ix); else fouds2(iz, ix); }
+
+  // fm2d_ttime.f90:682-711 bilinear
+  double bilinear(const double nv[2][2], double dsx, double dsz) {
+    double biv = 0.0;
+    for (int i = 1; i <= 2; ++i)
+      for (int j = 1; j <= 2; ++j) {
+        double produ = (1.0 - std::fabs(((double)(i - 1) * dnx - dsx) / dnx)) *
+                       (1.0 - std::fabs(((double)(j - 1) * dnz - dsz) / dnz));
+        biv = biv + nv[i - 1][j - 1] * produ;
+      }
+    return biv;
+  }
+
+  // fm2d_ttime.f90:41-238 travel. Returns -1 if the source is outside.
+  int travel(double scx, double scz, int urg) {
+    int isx = (int)((scx - gox) / dnx) + 1;
+    int isz = (int)((scz - goz) / dnz) + 1;
+    if (isx < 1 || isx > nnx || isz < 1 || isz > nnz) return -1;
+    if (isx == nnx) isx = isx - 1;
+    if (isz == nnz) isz = isz - 1;
+    if (urg != 2) std::fill(nsts.begin(), nsts.end(), -1);
+    ntr = 0;
+    if (urg == 2) {
+      for (int i = 1; i <= nnx; ++i)
+        for (int j = 1; j <= nnz; ++j)
+          if (S(j, i) > 0) addtree(j, i);
+    } else {
+      std::fill(nsts.begin(), nsts.end(), -1);
+      double vss[2][2];
+      for (int i = 1; i <= 2; ++i)
+        for (int j = 1; j <= 2; ++j) vss[i - 1][j - 1] = V(isz - 1 + j, isx - 1 + i);
+      double dsx = (scx - gox) - (double)(isx - 1) * dnx;
+      double dsz = (scz - goz) - (double)(isz - 1) * dnz;
+      double vsrc = bilinear(vss, dsx, dsz);
+      for (int i = 1; i <= 2; ++i)
+        for (int j = 1; j <= 2; ++j) {
+          double ex = dsx - (double)(i - 1) * dnx;
+          double ez = dsz - (double)(j - 1) * dnz;
+          double ds = std::sqrt(ex * ex + ez * ez);
+          T(isz - 1 + j, isx - 1 + i) = 2.0 * ds / (vss[i - 1][j - 1] + vsrc);
+          addtree(isz - 1 + j, isx - 1 + i);
+        }
+    }
+    while (ntr > 0) {
+      if (urg == 1) {
+        int ix = btgx[1], iz = btgz[1];
+        int swrg = 0;
+        if (ix == 1) { if (vnl != 1) swrg = 1; }
+        // vnr/vnb are coarse node indices compared with the refined grid
+        // size, exactly as the reference's module variables are at this point
+        if (ix == nnx) { if (vnr != nnx) swrg = 1; }
+        if (iz == 1) { if (vnt != 1) swrg = 1; }
+        if (iz == nnz) { if (vnb != nnz) swrg = 1; }
+        if (swrg == 1) { S(iz, ix) = 0; break; }
+      }
+      int ix = btgx[1], iz = btgz[1];
+      S(iz, ix) = 0;
+      downtree();
+      for (int i = ix - 1; i <= ix + 1; i += 2) {
+        if (i >= 1 && i <= nnx) {
+          if (S(iz, i) == -1) { fouds(iz, i); addtree(iz, i); }
+          else if (S(iz, i) > 0) { fouds(iz, i); updtree(iz, i); }
+        }
+      }
+      for (int i = iz - 1; i <= iz + 1; i += 2) {
+        if (i >= 1 && i <= nnz) {
+          if (S(i, ix) == -1) { fouds(i, ix); addtree(i, ix); }
+          else if (S(i, ix) > 0) { fouds(i, ix); updtree(i, ix); }
+        }
+      }
+    }
+    return 0;
+  }
+
+};
+
+}  // namespace
+
+extern "C" {
+
+// modrays (fm2dray_cartesian.f90:67-480) for uar=1 (no ray paths).
+// velvin: (nvz+2, nvx+2) column-major padded vertex grid. srs: (nrc*nsrc)
+// path-exists flags, source-major (pn = (i-1)*nrc + j). ttime: (nrc, nsrc)
+// column-major, written only where srs==1. tfield (optional, may be NULL):
+// (nnz, nnx, nsrc) final coarse travel-time fields.
+// Returns 0, or -1 for a source/receiver outside the grid (the reference
+// stops the program there).
+int orc_modrays(int nsrc, const double *scx, const double *scz, int nrc,
+                const double *rcx, const double *rcz, const int *srs, int nvx,
+                int nvz, double goxd, double gozd, double dvxd, double dvzd,
+                const double *velvin, int gdx, int gdz, int asgr, int sgdl,
+                int sgs, int fom, double snb, double *ttime, double *tfield) {
+  (void)snb;  // narrow-band capacity only; heap here grows as needed
+  // gridder (fm2dray_cartesian.f90:491-600)
+  int ldv = nvz + 2;
+  auto velv = [&](int i, int j) { return velvin[(size_t)j * ldv + i]; };  // velv(i,j), i=0..nvz+1
+  int nnx = (nvx - 1) * gdx + 1, nnz = (nvz - 1) * gdz + 1;
+  double dvx = dvxd, dvz = dvzd, gox = goxd, goz = gozd;
+  double dnx = dvx / gdx, dnz = dvz / gdz;
+  std::vector<double> velc((size_t)nnx * nnz);
+  {
+    std::vector<double> ui((gdx + 1) * 4), vi((gdz + 1) * 4);
+    for (int i = 1; i <= gdx + 1; ++i) {
+      double u = gdx; u = (double)(i - 1) / u;
+      double om = 1.0 - u;
+      ui[(i - 1) * 4 + 0] = om * om * om / 6.0;
+      ui[(i - 1) * 4 + 1] = (4.0 - 6.0 * (u * u) + 3.0 * (u * u * u)) / 6.0;
+      ui[(i - 1) * 4 + 2] = (1.0 + 3.0 * u + 3.0 * (u * u) - 3.0 * (u * u * u)) / 6.0;
+      ui[(i - 1) * 4 + 3] = (u * u * u) / 6.0;
+    }
+    for (int i = 1; i <= gdz + 1; ++i) {
+      double u = gdz; u = (double)(i - 1) / u;
+      double om = 1.0 - u;
+      vi[(i - 1) * 4 + 0] = om * om * om / 6.0;
+      vi[(i - 1) * 4 + 1] = (4.0 - 6.0 * (u * u) + 3.0 * (u * u * u)) / 6.0;
+      vi[(i - 1) * 4 + 2] = (1.0 + 3.0 * u + 3.0 * (u * u) - 3.0 * (u * u * u)) / 6.0;
+      vi[(i - 1) * 4 + 3] = (u * u * u) / 6.0;
+    }
+    for (int i = 1; i <= nvz - 1; ++i) {
+      int conz = (i == nvz - 1) ? gdz + 1 : gdz;
+      for (int j = 1; j <= nvx - 1; ++j) {
+        int conx = (j == nvx - 1) ? gdx + 1 : gdx;
+        for (int l = 1; l <= conz; ++l) {
+          int stz = gdz * (i - 1) + l;
+          for (int m = 1; m <= conx; ++m) {
+            int stx = gdx * (j - 1) + m;
+            double sumi = 0.0;
+            for (int i1 = 1; i1 <= 4; ++i1) {
+              double sumj = 0.0;
+              for (int j1 = 1; j1 <= 4; ++j1)
+                sumj = sumj + ui[(m - 1) * 4 + j1 - 1] * velv(i - 2 + i1, j - 2 + j1);
+              sumi = sumi + vi[(l - 1) * 4 + i1 - 1] * sumj;
+            }
+            velc[(size_t)(stx - 1) * nnz + (stz - 1)] = sumi;
+          }
+        }
+      }
+    }
+  }
+
+  FM2D f;
+  f.fom = fom;
+  int nrx_max = 2 * sgs * sgdl + 1;
+  int ld = std::max(nnz, nrx_max), cols = std::max(nnx, nrx_max);
+  f.ld = ld;
+  f.veln.assign((size_t)ld * cols, 0.0);
+  f.ttn.assign((size_t)ld * cols, 0.0);
+  f.nsts.assign((size_t)ld * cols, -1);
+  f.btgx.resize(ld * cols + 8); f.btgz.resize(ld * cols + 8);
+  auto load_coarse = [&]() {
+    f.nnx = nnx; f.nnz = nnz; f.gox = gox; f.goz = goz; f.dnx = dnx; f.dnz = dnz;
+    for (int i = 1; i <= nnx; ++i)
+      for (int k = 1; k <= nnz; ++k) f.V(k, i) = velc[(size_t)(i - 1) * nnz + (k - 1)];
+  };
+  load_coarse();
+
+  for (int i = 1; i <= nsrc; ++i) {
+    int any = 0;
+    for (int j = 0; j < nrc; ++j) any += srs[(size_t)(i - 1) * nrc + j];
+    if (any == 0 && i != 1) continue;
+    double x = scx[i - 1], z = scz[i - 1];
+    int isx = (int)((x - gox) / dnx) + 1;
+    int isz = (int)((z - goz) / dnz) + 1;
+    if (isx < 1 || isx > nnx || isz < 1 || isz > nnz) return -1;
+    if (isx == nnx) isx = isx - 1;
+    if (isz == nnz) isz = isz - 1;
+    f.vnl = std::max(isx - sgs, 1); f.vnr = std::min(isx + sgs, nnx);
+    f.vnt = std::max(isz - sgs, 1); f.vnb = std::min(isz + sgs, nnz);
+    if (asgr == 1) {
+      // refined source grid (fm2dray_cartesian.f90:292-415)
+      int nrnx = (f.vnr - f.vnl) * sgdl + 1, nrnz = (f.vnb - f.vnt) * sgdl + 1;
+      double drnx = dvx / (double)(gdx * sgdl), drnz = dvz / (double)(gdz * sgdl);
+      double gorx = gox + dnx * (double)(f.vnl - 1), gorz = goz + dnz * (double)(f.vnt - 1);
+      f.nnx = nrnx; f.nnz = nrnz; f.dnx = drnx; f.dnz = drnz; f.gox = gorx; f.goz = gorz;
+      // bsplrefine (fm2dray_cartesian.f90:608-674)
+      {
+        int nrxr = gdx * sgdl, nrzr = gdz * sgdl;
+        std::vector<double> ui((nrxr + 1) * (nrzr + 1) * 4), vi((nrxr + 1) * (nrzr + 1) * 4);
+        auto UI = [&](int j, int ii, int q) -> double & { return ui[((size_t)(ii - 1) * (nrxr + 1) + (j - 1)) * 4 + q - 1]; };
+        auto VI = [&](int j, int ii, int q) -> double & { return vi[((size_t)(ii - 1) * (nrxr + 1) + (j - 1)) * 4 + q - 1]; };
+        for (int ii = 1; ii <= nrzr + 1; ++ii) {
+          double v = nrzr; v = (double)(ii - 1) / v;
+          for (int j = 1; j <= nrxr + 1; ++j) {
+            double u = nrxr; u = (double)(j - 1) / u;
+            double om = 1.0 - u, ov = 1.0 - v;
+            UI(j, ii, 1) = om * om * om / 6.0;
+            UI(j, ii, 2) = (4.0 - 6.0 * (u * u) + 3.0 * (u * u * u)) / 6.0;
+            UI(j, ii, 3) = (1.0 + 3.0 * u + 3.0 * (u * u) - 3.0 * (u * u * u)) / 6.0;
+            UI(j, ii, 4) = (u * u * u) / 6.0;
+            VI(j, ii, 1) = ov * ov * ov / 6.0;
+            VI(j, ii, 2) = (4.0 - 6.0 * (v * v) + 3.0 * (v * v * v)) / 6.0;
+            VI(j, ii, 3) = (1.0 + 3.0 * v + 3.0 * (v * v) - 3.0 * (v * v * v)) / 6.0;
+            VI(j, ii, 4) = (v * v * v) / 6.0;
+          }
+        }
+        int origx = (f.vnl - 1) * sgdl + 1, origz = (f.vnt - 1) * sgdl + 1;
+        for (int ii = 1; ii <= nvz - 1; ++ii) {
+          int conz = (ii == nvz - 1) ? nrzr + 1 : nrzr;
+          for (int j = 1; j <= nvx - 1; ++j) {
+            int conx = (j == nvx - 1) ? nrxr + 1 : nrxr;
+            for (int k = 1; k <= conz; ++k) {
+              int st1 = gdz * (ii - 1) + (k - 1) / sgdl + 1;
+              if (st1 < f.vnt || st1 > f.vnb) continue;
+              st1 = nrzr * (ii - 1) + k;
+              for (int l = 1; l <= conx; ++l) {
+                int st2 = gdx * (j - 1) + (l - 1) / sgdl + 1;
+                if (st2 < f.vnl || st2 > f.vnr) continue;
+                st2 = nrxr * (j - 1) + l;
+                double sum[4];
+                for (int i1 = 1; i1 <= 4; ++i1) {
+                  sum[i1 - 1] = 0.0;
+                  for (int j1 = 1; j1 <= 4; ++j1)
+                    sum[i1 - 1] = sum[i1 - 1] + UI(l, k, j1) * velv(ii - 2 + i1, j - 2 + j1);
+                  sum[i1 - 1] = VI(l, k, i1) * sum[i1 - 1];
+                }
+                int idm1 = st1 - origz + 1, idm2 = st2 - origx + 1;
+                if (idm1 < 1 || idm1 > f.nnz) continue;
+                if (idm2 < 1 || idm2 > f.nnx) continue;
+                f.V(idm1, idm2) = sum[0] + sum[1] + sum[2] + sum[3];
+              }
+            }
+          }
+        }
+      }
+      if (f.travel(x, z, 1) != 0) return -1;
+      // map refined grid onto coarse grid
+      std::vector<double> ttnr((size_t)nrnz * nrnx);
+      std::vector<int> nstsr((size_t)nrnz * nrnx);
+      for (int l = 1; l <= nrnx; ++l)
+        for (int k = 1; k <= nrnz; ++k) {
+          ttnr[(size_t)(l - 1) * nrnz + k - 1] = f.T(k, l);
+          nstsr[(size_t)(l - 1) * nrnz + k - 1] = f.S(k, l);
+        }
+      std::fill(f.nsts.begin(), f.nsts.end(), -1);
+      for (int k = 1; k <= nrnz; k += sgdl) {
+        int idm1 = f.vnt + (k - 1) / sgdl;
+        for (int l = 1; l <= nrnx; l += sgdl) {
+          int idm2 = f.vnl + (l - 1) / sgdl;
+          f.S(idm1, idm2) = nstsr[(size_t)(l - 1) * nrnz + k - 1];
+          if (f.S(idm1, idm2) >= 0) f.T(idm1, idm2) = ttnr[(size_t)(l - 1) * nrnz + k - 1];
+        }
+      }
+      load_coarse();
+      // narrow band repair
+      for (int k = 1; k <= nnx; ++k)
+        for (int l = 1; l <= nnz; ++l)
+          if (f.S(l, k) == 0) {
+            if (l - 1 >= 1) { if (f.S(l - 1, k) == -1) f.S(l, k) = 1; }
+            if (l + 1 <= nnz) { if (f.S(l + 1, k) == -1) f.S(l, k) = 1; }
+            if (k - 1 >= 1) { if (f.S(l, k - 1) == -1) f.S(l, k) = 1; }
+            if (k + 1 <= nnx) { if (f.S(l, k + 1) == -1) f.S(l, k) = 1; }
+          }
+      if (f.travel(x, z, 2) != 0) return -1;
+    } else {
+      if (f.travel(x, z, 0) != 0) return -1;
+    }
+    if (tfield) {
+      for (int ix = 1; ix <= nnx; ++ix)
+        for (int iz = 1; iz <= nnz; ++iz)
+          tfield[(size_t)(i - 1) * nnx * nnz + (size_t)(ix - 1) * nnz + iz - 1] = f.T(iz, ix);
+    }
+    // srtimes (fm2dray_cartesian.f90:682-797)
+    for (int r = 1; r <= nrc; ++r) {
+      if (srs[(size_t)(i - 1) * nrc + r - 1] == 0) continue;
+      int irx = (int)std::floor((rcx[r - 1] - gox) / dnx) + 1;
+      int irz = (int)std::floor((rcz[r - 1] - goz) / dnz) + 1;
+      int sw = 0;
+      if (irx < 1 || irx > nnx || irz < 1 || irz > nnz) return -1;
+      if (irx == nnx) irx = irx - 1;
+      if (irz == nnz) irz = irz - 1;
+      int jsx = (int)std::floor((x - gox) / dnx) + 1;
+      int jsz = (int)std::floor((z - goz) / dnz) + 1;
+      double dpl = dnx, rd1 = dnz;
+      if (rd1 < dpl) dpl = rd1;
+      double sred = (x - rcx[r - 1]) * (x - rcx[r - 1]);
+      sred = sred + (z - rcz[r - 1]) * (z - rcz[r - 1]);
+      sred = std::sqrt(sred);
+      if (sred < dpl) sw = 1;
+      if (jsx == irx && jsz == irz) sw = 1;
+      double trr;
+      if (sw == 1) {
+        double vss[2][2];
+        for (int k = 1; k <= 2; ++k)
+          for (int l = 1; l <= 2; ++l) vss[k - 1][l - 1] = f.V(jsz - 1 + l, jsx - 1 + k);
+        double drx = (x - gox) - (double)(jsx - 1) * dnx;
+        double drz = (z - goz) - (double)(jsz - 1) * dnz;
+        double vels = f.bilinear(vss, drx, drz);
+        for (int k = 1; k <= 2; ++k)
+          for (int l = 1; l <= 2; ++l) vss[k - 1][l - 1] = f.V(irz - 1 + l, irx - 1 + k);
+        drx = (rcx[r - 1] - gox) - (double)(irx - 1) * dnx;
+        drz = (rcz[r - 1] - goz) - (double)(irz - 1) * dnz;
+        double velr = f.bilinear(vss, drx, drz);
+        trr = 2.0 * sred / (vels + velr);
+      } else {
+        double drx = (rcx[r - 1] - gox) - (double)(irx - 1) * dnx;
+        double drz = (rcz[r - 1] - goz) - (double)(irz - 1) * dnz;
+        trr = 0.0;
+        for (int k = 1; k <= 2; ++k)
+          for (int l = 1; l <= 2; ++l) {
+            double produ = (1.0 - std::fabs(((double)(l - 1) * dnz - drz) / dnz)) *
+                           (1.0 - std::fabs(((double)(k - 1) * dnx - drx) / dnx));
+            trr = trr + f.T(irz - 1 + l, irx - 1 + k) * produ;
+          }
+      }
+      ttime[(size_t)(i - 1) * nrc + r - 1] = trr;
+    }
+  }
+  return 0;
+}
+
+}  // extern "C"

@@ -1,0 +1,173 @@
+// ORACLE (test infrastructure only): CPU restatement of the reference's
+// model checks, column layering and misfit / log-likelihood reductions, used
+// as the parity checker for the GPU reduction and layering kernels. Never
+// linked into the product.
+//
+// Parity status: unpinned by reference execution (Fortran); these are short
+// sums restated line by line from:
+//   check_model       src/likelihood_surf.F90:631-646
+//   convert_to_layer  src/likelihood_surf.F90:523-629
+//   surf_likelihood   src/likelihood_surf.F90:354-404 (after the forward)
+//   surf_noise_likelihood src/likelihood_surf.F90:56-99
+//   body_likelihood   src/likelihood_body.F90:176-195,284-333
+//   body_noise_likelihood src/likelihood_body.F90:38-80
+//   2D body_likelihood mcmc2d/likelihood_dd.F90:468-499 (datatype 0)
+//   vs2vp / vp2rho    src/utils.f90:90-135
+#include <cmath>
+#include "oracle.h"
+
+namespace {
+const double PI2 = (double)6.283185f;  // REAL*8 parameter set from a REAL*4 literal
+}
+
+extern "C" {
+
+// Returns 1 when some column has a deeper node slower than its top node.
+int orc_check_model(const double *vs, int nz, int ny, int nx) {
+  for (int i = 0; i < nx; ++i)
+    for (int j = 0; j < ny; ++j) {
+      const double *col = vs + ((size_t)i * ny + j) * nz;
+      for (int k = 1; k < nz; ++k)
+        if (col[k] < col[0]) return 1;
+    }
+  return 0;
+}
+
+// One column (vp, vs, rho of length nz) to a layer stack. Returns nlayers.
+// thick already divided by scaling (water depth unscaled), no vbnd.
+int orc_convert_to_layer(const double *vp, const double *vs, const double *rho,
+                         int nz, double dz, double scaling, double water_depth,
+                         double *alpha, double *beta, double *rho_k,
+                         double *thick) {
+  const double EPS = 1.0E-10;
+  int nl;
+  if (water_depth > EPS) {
+    nl = 1; alpha[0] = (double)1.5f; beta[0] = 0; rho_k[0] = 1; thick[0] = water_depth;
+  } else {
+    nl = 0;
+  }
+  double last_vp = vp[0], last_vs = vs[0], last_rho = rho[0];
+  int last_k = 1;
+  for (int k = 2; k <= nz; ++k) {
+    if (std::fabs(vs[k - 1] - last_vs) > EPS) {
+      nl = nl + 1;
+      alpha[nl - 1] = last_vp; beta[nl - 1] = last_vs; rho_k[nl - 1] = last_rho;
+      thick[nl - 1] = (double)(k - last_k) * dz;
+      last_vp = vp[k - 1]; last_vs = vs[k - 1]; last_rho = rho[k - 1];
+      last_k = k;
+    }
+  }
+  nl = nl + 1;
+  if (last_k != nz) {
+    alpha[nl - 1] = vp[nz - 1]; beta[nl - 1] = vs[nz - 1]; rho_k[nl - 1] = rho[nz - 1];
+    thick[nl - 1] = (double)(nz - last_k) * dz;
+    thick[nl - 1] = 0;
+  } else {
+    alpha[nl - 1] = vp[nz - 1]; beta[nl - 1] = vs[nz - 1]; rho_k[nl - 1] = rho[nz - 1];
+    thick[nl - 1] = 0;
+  }
+  for (int i = 0; i < nl; ++i) thick[i] = thick[i] / scaling;
+  if (water_depth > 0) thick[0] = water_depth;
+  return nl;
+}
+
+// Surface-wave misfit. phase_time: (nrev, nsrc, np); dat_ttime: (npairs, 3, np)
+// with column 1 the observed time and column 2 the data sigma; raystat:
+// (npairs, 2, np); srdist (npairs, np). sigdep != 0: sigma = n0*srdist + n1.
+// sigma_out (npairs, np) receives the final sigma. out[0..2] = like, misfit,
+// unweighted misfit. Returns -1 if a used sigma is below 1e-10.
+int orc_surf_misfit(int nsrc, int nrev, int np, const double *phase_time,
+                    const double *dat_ttime, const int *raystat,
+                    const double *srdist, int sigdep, const double *n0,
+                    const double *n1, int nrays, double *sigma_out,
+                    double *out) {
+  const double EPS = 1.0E-10;
+  const int npairs = nsrc * nrev;
+  for (int i = 0; i < np; ++i) {
+    for (int r = 0; r < npairs; ++r) {
+      double s;
+      if (sigdep != 0) {
+        s = (raystat[(size_t)i * npairs * 2 + r] == 1)
+                ? n0[i] * srdist[(size_t)i * npairs + r] + n1[i] : 1.0;
+      } else {
+        s = dat_ttime[(size_t)i * npairs * 3 + npairs + r];
+      }
+      sigma_out[(size_t)i * npairs + r] = s;
+    }
+  }
+  double like = 0, misfit = 0, umisfit = 0;
+  int status = 0;
+  for (int i = 0; i < np; ++i) {
+    int nrr = 0;
+    for (int j = 0; j < nsrc; ++j)
+      for (int k = 0; k < nrev; ++k) {
+        nrr = nrr + 1;
+        size_t si = (size_t)i * npairs + nrr - 1;
+        if (raystat[(size_t)i * npairs * 2 + nrr - 1] == 1) {
+          if (sigma_out[si] < EPS) status = -1;
+          double r = phase_time[((size_t)i * nsrc + j) * nrev + k] -
+                     dat_ttime[(size_t)i * npairs * 3 + nrr - 1];
+          like = like + (r * r) / (2 * (sigma_out[si] * sigma_out[si]));
+          misfit = misfit + (r * r) / (sigma_out[si] * sigma_out[si]);
+          umisfit = umisfit + r * r;
+        } else {
+          sigma_out[si] = 1.0;
+        }
+      }
+  }
+  double slog = 0;
+  for (int i = 0; i < np; ++i)
+    for (int r = 0; r < npairs; ++r) slog = slog + std::log(sigma_out[(size_t)i * npairs + r]);
+  like = like + slog + (double)((float)nrays / 2.0f) * std::log(PI2);
+  out[0] = like; out[1] = misfit; out[2] = umisfit;
+  return status;
+}
+
+// Body-wave misfit: residual adds the event origin time t0[j] (locations(4,j)).
+int orc_body_misfit(int nsrc, int nrev, int np, const double *phase_time,
+                    const double *t0, const double *dat_ttime,
+                    const int *raystat, const double *srdist, int sigdep,
+                    const double *n0, const double *n1, int nrays,
+                    double *sigma_out, double *out) {
+  const double EPS = 2.2250738585072014e-308 * 10;  // tiny(0d0)*10
+  const int npairs = nsrc * nrev;
+  for (int i = 0; i < np; ++i)
+    for (int r = 0; r < npairs; ++r) {
+      double s = (sigdep != 0) ? n0[i] * srdist[(size_t)i * npairs + r] + n1[i]
+                               : dat_ttime[(size_t)i * npairs * 3 + npairs + r];
+      sigma_out[(size_t)i * npairs + r] = s;
+    }
+  double like = 0, misfit = 0, umisfit = 0;
+  int status = 0;
+  for (int i = 0; i < np; ++i) {
+    int nrr = 0;
+    for (int j = 0; j < nsrc; ++j)
+      for (int k = 0; k < nrev; ++k) {
+        nrr = nrr + 1;
+        size_t si = (size_t)i * npairs + nrr - 1;
+        if (raystat[(size_t)i * npairs * 2 + nrr - 1] == 1) {
+          if (sigma_out[si] < EPS) status = -1;
+          double r = phase_time[((size_t)i * nsrc + j) * nrev + k] + t0[j] -
+                     dat_ttime[(size_t)i * npairs * 3 + nrr - 1];
+          like = like + (r * r) / (2 * (sigma_out[si] * sigma_out[si]));
+          misfit = misfit + (r * r) / (sigma_out[si] * sigma_out[si]);
+          umisfit = umisfit + r * r;
+        } else {
+          sigma_out[si] = 1.0;
+        }
+      }
+  }
+  double slog = 0;
+  for (int i = 0; i < np; ++i)
+    for (int r = 0; r < npairs; ++r) slog = slog + std::log(sigma_out[(size_t)i * npairs + r]);
+  like = like + slog + (double)((float)nrays / 2.0f) * std::log(PI2);
+  out[0] = like; out[1] = misfit; out[2] = umisfit;
+  return status;
+}
+
+// src/utils.f90:98-135 vs2vp_3d / vp2rho_3d: vp = vs*1.730, rho = 1.74*vp**0.25
+// (both constants are REAL*4 literals widened to double).
+double orc_vs2vp(double vs) { return vs * (double)1.730f; }
+double orc_vp2rho(double vp) { return (double)1.74f * std::pow(vp, 0.25); }
+
+}  // extern "C"
