@@ -1,0 +1,13 @@
+"""GB300 (sm_103a) forward-modelling hot path of MCTomo's rjMCMC.
+
+The compute runs in ``libmctomo_gpu.so`` (hand-written CUDA, C ABI in
+include/mctomo.h). This package is the Python mirror of the reference's
+forward-modelling call surface (kdtree_to_grid, surfdisp96 / surfmodes,
+modrays, fastMarching3D and the likelihood reductions).
+"""
+from ._lib import MctError, lib, LIB_PATH  # noqa: F401
+from .forward import (  # noqa: F401
+    kdtree_to_grid, surfdisp96, surfdisp_mmodes, surfmodes, surfdisp_batch,
+)
+
+__version__ = "0.1.0"

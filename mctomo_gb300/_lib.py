@@ -1,0 +1,81 @@
+"""ctypes binding of libmctomo_gpu.so (the C ABI in include/mctomo.h).
+
+The library is built in-tree by ``mctomo_gb300.build``. There is no CPU
+fallback: if the shared library is missing or fails to load, every call
+raises ``MctError``.
+"""
+import ctypes
+import os
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "libmctomo_gpu.so")
+
+MCT_OK = 0
+MCT_MODEL_INVALID = 1
+ERRORS = {
+    -1: "MCT_ERR_ARG", -2: "MCT_ERR_CUDA", -3: "MCT_ERR_NOMEM", -4: "MCT_ERR_OUTSIDE",
+    -5: "MCT_ERR_UNSUPPORTED", -6: "MCT_ERR_TIMEOUT", -7: "MCT_ERR_INTERNAL",
+}
+
+P = ctypes.c_void_p
+I = ctypes.c_int
+D = ctypes.c_double
+ULLP = ctypes.POINTER(ctypes.c_ulonglong)
+
+# name -> (restype, argtypes); must list every symbol declared in include/mctomo.h
+SIGNATURES = {
+    "mct_version": (ctypes.c_char_p, []),
+    "mct_last_error": (ctypes.c_char_p, []),
+    "mct_kdtree_to_grid": (I, [I, I, P, P, I, I, I, P, P, P, P, P, P, P]),
+    "mct_grid_nearest_batch_device": (I, [I, I, I, P, P, P, I, I, I, P, P, P, P, P, P, P, P]),
+    "mct_surfdisp96": (I, [P, P, P, P, I, I, I, I, I, I, P, D, P, P, P]),
+    "mct_surfdisp_mmodes": (I, [P, P, P, P, I, I, I, I, I, I, P, D, P, P, P]),
+    "mct_surfmodes": (I, [P, P, P, P, I, P, I, I, I, D, P, P, P]),
+    "mct_surfdisp_batch": (I, [I, I, P, P, P, P, P, I, P, I, I, I, D, I, I, P, P, P, P]),
+    "mct_surfdisp_batch_device": (I, [I, I, P, P, P, P, P, I, P, I, I, I, D, I, I, P, P, P, P, P]),
+}
+
+
+class MctError(RuntimeError):
+    """A negative status from the library (or the library is unavailable)."""
+
+    def __init__(self, name, code, msg=""):
+        self.code = code
+        super().__init__("%s failed: %s (%s) %s" % (name, code, ERRORS.get(code, "?"), msg))
+
+
+_lib = None
+
+
+def lib():
+    """Load (once) and return the bound library."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    if not os.path.exists(LIB_PATH):
+        raise MctError("load", -2, "libmctomo_gpu.so not built at %s; run mctomo_gb300.build.build()" % LIB_PATH)
+    try:
+        handle = ctypes.CDLL(LIB_PATH)
+    except OSError as e:  # pragma: no cover - depends on the host
+        raise MctError("load", -2, str(e))
+    for name, (res, args) in SIGNATURES.items():
+        fn = getattr(handle, name)
+        fn.restype = res
+        fn.argtypes = args
+    _lib = handle
+    return _lib
+
+
+def check(name, rc):
+    """Raise on a negative status; return the status otherwise (0 or 1)."""
+    if rc < 0:
+        msg = lib().mct_last_error().decode(errors="replace")
+        raise MctError(name, rc, msg)
+    return rc
+
+
+def ptr(a):
+    """Pointer to a numpy array's data (None passes NULL)."""
+    if a is None:
+        return None
+    return ctypes.c_void_p(a.ctypes.data)

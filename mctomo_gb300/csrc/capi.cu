@@ -1,0 +1,299 @@
+// C-ABI entry points of libmctomo_gpu.so (declared in include/mctomo.h).
+// Host-pointer calls stage their inputs into a grow-only device workspace on
+// the library's own stream and wait for the result; _device calls launch on
+// the caller's stream.
+#include "mct_common.cuh"
+#include <cstring>
+#include <string>
+#include <vector>
+#include <algorithm>
+
+static thread_local std::string g_last_error;
+
+void mct_set_error(const char *what, const char *why, const char *file, int line) {
+  char buf[512];
+  snprintf(buf, sizeof(buf), "%s: %s (%s:%d)", what, why, file, line);
+  g_last_error = buf;
+}
+
+namespace {
+
+std::mutex g_mu;
+cudaStream_t g_stream = nullptr;
+DevBuf g_ws;
+
+int ensure_stream() {
+  if (!g_stream) MCT_CUDA_TRY(cudaStreamCreateWithFlags(&g_stream, cudaStreamNonBlocking));
+  return MCT_OK;
+}
+
+int arg_error(const char *msg) {
+  g_last_error = msg;
+  return MCT_ERR_ARG;
+}
+
+int sync_and_check(cudaStream_t s, const int *d_status) {
+  MCT_CUDA_TRY(cudaStreamSynchronize(s));
+  if (d_status) {
+    int st = 0;
+    MCT_CUDA_TRY(cudaMemcpy(&st, d_status, sizeof(int), cudaMemcpyDeviceToHost));
+    if (st != 0) { g_last_error = "device kernel reported an internal error"; return st; }
+  }
+  return MCT_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+const char *mct_version(void) { return "mctomo-gb300 0.1 (sm_103a)"; }
+
+const char *mct_last_error(void) { return g_last_error.c_str(); }
+
+// ---------------------------------------------------------------------------
+// Gridding
+// ---------------------------------------------------------------------------
+int mct_grid_nearest_batch_device(int d, int nchains, int ncell_max, const int *ncells,
+                                  const double *points, const double *params, int nx, int ny,
+                                  int nz, const double *grid_lo, const double *grid_step,
+                                  const int *box, int *sites_id, double *vp, double *vs,
+                                  double *rho, void *stream) {
+  if ((d != 2 && d != 3) || nchains < 1 || ncell_max < 1 || nx < 1 || ny < 1 || (d == 3 && nz < 1))
+    return arg_error("mct_grid_nearest_batch_device: bad sizes");
+  if (ncell_max > 12800) return arg_error("mct_grid_nearest_batch_device: ncell_max > 12800");
+  // scratch owned per call site: allocate on the caller's stream ordering
+  long nodes = (long)nx * ny * (d == 3 ? nz : 1);
+  size_t kd = kd_scratch_bytes(ncell_max);
+  size_t bytes = carve_size({sizeof(int) * (size_t)nchains, sizeof(int) * (size_t)nchains * nodes,
+                             kd * nchains, sizeof(int)});
+  cudaStream_t s = static_cast<cudaStream_t>(stream);
+  void *scratch = nullptr;
+  MCT_CUDA_TRY(cudaMallocAsync(&scratch, bytes, s));
+  Carve cv(scratch);
+  GridJob job{};
+  job.d = d; job.nx = nx; job.ny = ny; job.nz = d == 3 ? nz : 1;
+  job.xmin = grid_lo[0]; job.ymin = grid_lo[1]; job.zmin = d == 3 ? grid_lo[2] : 0.0;
+  job.dx = grid_step[0]; job.dy = grid_step[1]; job.dz = d == 3 ? grid_step[2] : 0.0;
+  job.nchains = nchains; job.ncell_max = ncell_max; job.ncells = ncells;
+  job.points = points; job.params = params; job.box = box;
+  job.sites_id = sites_id; job.vp = vp; job.vs = vs; job.rho = rho;
+  job.tie_count = cv.take<int>(nchains);
+  job.tie_nodes = cv.take<int>((size_t)nchains * nodes);
+  job.kd_scratch = cv.take<char>(kd * nchains);
+  job.status = cv.take<int>(1);
+  MCT_CUDA_TRY(cudaMemsetAsync(job.status, 0, sizeof(int), s));
+  int rc = launch_grid_nearest(job, s);
+  cudaFreeAsync(scratch, s);
+  return rc;
+}
+
+int mct_kdtree_to_grid(int d, int n, const double *points, const double *params, int nx, int ny,
+                       int nz, const double *grid_lo, const double *grid_step, const int *box,
+                       int *sites_id, double *vp, double *vs, double *rho) {
+  if ((d != 2 && d != 3) || n < 1 || nx < 1 || ny < 1 || (d == 3 && nz < 1))
+    return arg_error("mct_kdtree_to_grid: bad sizes");
+  if (n > 12800) return arg_error("mct_kdtree_to_grid: more than 12800 nuclei");
+  const int nzz = d == 3 ? nz : 1;
+  int b[6] = {1, nx, 1, ny, 1, nzz};
+  if (box) {
+    for (int i = 0; i < 6; ++i) b[i] = box[i];
+    if (d == 2) { b[4] = 1; b[5] = 1; }
+    if (b[0] < 1 || b[1] > nx || b[2] < 1 || b[3] > ny || b[4] < 1 || b[5] > nzz ||
+        b[0] > b[1] || b[2] > b[3] || b[4] > b[5])
+      return arg_error("mct_kdtree_to_grid: box outside the grid");
+  }
+  std::lock_guard<std::mutex> lk(g_mu);
+  int rc = ensure_stream(); if (rc) return rc;
+  size_t nodes = (size_t)nx * ny * nzz;
+  size_t kd = kd_scratch_bytes(n);
+  size_t bytes = carve_size({sizeof(double) * d * n, sizeof(double) * 3 * n, sizeof(int), sizeof(int) * 6,
+                             sizeof(int) * nodes, sizeof(double) * nodes * 3, sizeof(int), sizeof(int) * nodes,
+                             kd, sizeof(int)});
+  rc = g_ws.reserve(bytes); if (rc) return rc;
+  Carve cv(g_ws.p);
+  double *d_pts = cv.take<double>((size_t)d * n);
+  double *d_par = cv.take<double>((size_t)3 * n);
+  int *d_n = cv.take<int>(1);
+  int *d_box = cv.take<int>(6);
+  int *d_sites = cv.take<int>(nodes);
+  double *d_vel = cv.take<double>(nodes * 3);
+  GridJob job{};
+  job.tie_count = cv.take<int>(1);
+  job.tie_nodes = cv.take<int>(nodes);
+  job.kd_scratch = cv.take<char>(kd);
+  job.status = cv.take<int>(1);
+  cudaStream_t s = g_stream;
+  MCT_CUDA_TRY(cudaMemcpyAsync(d_pts, points, sizeof(double) * d * n, cudaMemcpyHostToDevice, s));
+  MCT_CUDA_TRY(cudaMemcpyAsync(d_par, params, sizeof(double) * 3 * n, cudaMemcpyHostToDevice, s));
+  MCT_CUDA_TRY(cudaMemcpyAsync(d_n, &n, sizeof(int), cudaMemcpyHostToDevice, s));
+  MCT_CUDA_TRY(cudaMemcpyAsync(d_box, b, sizeof(int) * 6, cudaMemcpyHostToDevice, s));
+  MCT_CUDA_TRY(cudaMemsetAsync(job.status, 0, sizeof(int), s));
+  // nodes outside the box keep the caller's values
+  MCT_CUDA_TRY(cudaMemcpyAsync(d_sites, sites_id, sizeof(int) * nodes, cudaMemcpyHostToDevice, s));
+  if (vp) {
+    MCT_CUDA_TRY(cudaMemcpyAsync(d_vel, vp, sizeof(double) * nodes, cudaMemcpyHostToDevice, s));
+    MCT_CUDA_TRY(cudaMemcpyAsync(d_vel + nodes, vs, sizeof(double) * nodes, cudaMemcpyHostToDevice, s));
+    MCT_CUDA_TRY(cudaMemcpyAsync(d_vel + 2 * nodes, rho, sizeof(double) * nodes, cudaMemcpyHostToDevice, s));
+  }
+  job.d = d; job.nx = nx; job.ny = ny; job.nz = nzz;
+  job.xmin = grid_lo[0]; job.ymin = grid_lo[1]; job.zmin = d == 3 ? grid_lo[2] : 0.0;
+  job.dx = grid_step[0]; job.dy = grid_step[1]; job.dz = d == 3 ? grid_step[2] : 0.0;
+  job.nchains = 1; job.ncell_max = n; job.ncells = d_n;
+  job.points = d_pts; job.params = d_par; job.box = d_box;
+  job.sites_id = d_sites;
+  job.vp = vp ? d_vel : nullptr; job.vs = vp ? d_vel + nodes : nullptr; job.rho = vp ? d_vel + 2 * nodes : nullptr;
+  rc = launch_grid_nearest(job, s); if (rc) return rc;
+  MCT_CUDA_TRY(cudaMemcpyAsync(sites_id, d_sites, sizeof(int) * nodes, cudaMemcpyDeviceToHost, s));
+  if (vp) {
+    MCT_CUDA_TRY(cudaMemcpyAsync(vp, d_vel, sizeof(double) * nodes, cudaMemcpyDeviceToHost, s));
+    MCT_CUDA_TRY(cudaMemcpyAsync(vs, d_vel + nodes, sizeof(double) * nodes, cudaMemcpyDeviceToHost, s));
+    MCT_CUDA_TRY(cudaMemcpyAsync(rho, d_vel + 2 * nodes, sizeof(double) * nodes, cudaMemcpyDeviceToHost, s));
+  }
+  return sync_and_check(s, job.status);
+}
+
+// ---------------------------------------------------------------------------
+// Dispersion
+// ---------------------------------------------------------------------------
+static int disp_args_ok(int ncol, int nl_max, int np, int iwave, int mode, int igr, double dphase) {
+  if (ncol < 0 || nl_max < 1 || nl_max > 200) return 0;
+  if (np < 1 || np > 60 || mode < 1 || mode > 20) return 0;
+  if (iwave != 1 && iwave != 2) return 0;
+  if (igr < 0) return 0;
+  if (!(dphase != 0.0) || (float)dphase == 0.0f) return 0;
+  return 1;
+}
+
+int mct_surfdisp_batch_device(int ncol, int nl_max, const int *nl, const float *thk, const float *vp,
+                              const float *vs, const float *rho, int np, const double *periods,
+                              int iwave, int mode, int igr, double dphase, int multimode,
+                              int precision, double *cp, double *cg, int *ierr,
+                              unsigned long long *ndltar, void *stream) {
+  if (!disp_args_ok(ncol, nl_max, np, iwave, mode, igr, dphase))
+    return arg_error("mct_surfdisp_batch_device: bad arguments");
+  if (!multimode && mode != 1) return arg_error("surfdisp96 computes one mode; use multimode");
+  DispJob job{};
+  job.ncol = ncol; job.nl_max = nl_max; job.nl = nl;
+  job.thk = thk; job.vp = vp; job.vs = vs; job.rho = rho;
+  job.np = np; job.periods = periods; job.iwave = iwave; job.mode = mode; job.igr = igr;
+  job.dphase = dphase; job.multimode = multimode; job.precision = precision ? 1 : 0;
+  job.cp = cp; job.cg = cg; job.ierr = ierr; job.ndltar = ndltar;
+  return launch_surfdisp(job, static_cast<cudaStream_t>(stream));
+}
+
+int mct_surfdisp_batch(int ncol, int nl_max, const int *nl, const float *thk, const float *vp,
+                       const float *vs, const float *rho, int np, const double *periods, int iwave,
+                       int mode, int igr, double dphase, int multimode, int precision, double *cp,
+                       double *cg, int *ierr, unsigned long long *ndltar) {
+  if (!disp_args_ok(ncol, nl_max, np, iwave, mode, igr, dphase))
+    return arg_error("mct_surfdisp_batch: bad arguments");
+  if (!multimode && mode != 1) return arg_error("surfdisp96 computes one mode; use multimode");
+  if (ncol == 0) return MCT_OK;
+  std::lock_guard<std::mutex> lk(g_mu);
+  int rc = ensure_stream(); if (rc) return rc;
+  size_t lay = (size_t)ncol * nl_max;
+  size_t outn = (size_t)ncol * mode * np;
+  size_t bytes = carve_size({sizeof(int) * ncol, 4 * sizeof(float) * lay, sizeof(double) * np,
+                             2 * sizeof(double) * outn, sizeof(int) * ncol, 2 * sizeof(unsigned long long)});
+  rc = g_ws.reserve(bytes); if (rc) return rc;
+  Carve cv(g_ws.p);
+  int *d_nl = cv.take<int>(ncol);
+  float *d_lay = cv.take<float>(4 * lay);
+  double *d_per = cv.take<double>(np);
+  double *d_out = cv.take<double>(2 * outn);
+  int *d_ierr = cv.take<int>(ncol);
+  unsigned long long *d_cnt = cv.take<unsigned long long>(2);
+  cudaStream_t s = g_stream;
+  MCT_CUDA_TRY(cudaMemcpyAsync(d_nl, nl, sizeof(int) * ncol, cudaMemcpyHostToDevice, s));
+  MCT_CUDA_TRY(cudaMemcpyAsync(d_lay, thk, sizeof(float) * lay, cudaMemcpyHostToDevice, s));
+  MCT_CUDA_TRY(cudaMemcpyAsync(d_lay + lay, vp, sizeof(float) * lay, cudaMemcpyHostToDevice, s));
+  MCT_CUDA_TRY(cudaMemcpyAsync(d_lay + 2 * lay, vs, sizeof(float) * lay, cudaMemcpyHostToDevice, s));
+  MCT_CUDA_TRY(cudaMemcpyAsync(d_lay + 3 * lay, rho, sizeof(float) * lay, cudaMemcpyHostToDevice, s));
+  MCT_CUDA_TRY(cudaMemcpyAsync(d_per, periods, sizeof(double) * np, cudaMemcpyHostToDevice, s));
+  MCT_CUDA_TRY(cudaMemsetAsync(d_cnt, 0, 2 * sizeof(unsigned long long), s));
+  DispJob job{};
+  job.ncol = ncol; job.nl_max = nl_max; job.nl = d_nl;
+  job.thk = d_lay; job.vp = d_lay + lay; job.vs = d_lay + 2 * lay; job.rho = d_lay + 3 * lay;
+  job.np = np; job.periods = d_per; job.iwave = iwave; job.mode = mode; job.igr = igr;
+  job.dphase = dphase; job.multimode = multimode; job.precision = precision ? 1 : 0;
+  job.cp = d_out; job.cg = d_out + outn; job.ierr = d_ierr; job.ndltar = d_cnt;
+  rc = launch_surfdisp(job, s); if (rc) return rc;
+  MCT_CUDA_TRY(cudaMemcpyAsync(cp, d_out, sizeof(double) * outn, cudaMemcpyDeviceToHost, s));
+  MCT_CUDA_TRY(cudaMemcpyAsync(cg, d_out + outn, sizeof(double) * outn, cudaMemcpyDeviceToHost, s));
+  MCT_CUDA_TRY(cudaMemcpyAsync(ierr, d_ierr, sizeof(int) * ncol, cudaMemcpyDeviceToHost, s));
+  unsigned long long cnt[2];
+  MCT_CUDA_TRY(cudaMemcpyAsync(cnt, d_cnt, sizeof(cnt), cudaMemcpyDeviceToHost, s));
+  rc = sync_and_check(s, nullptr);
+  if (ndltar) { ndltar[0] = cnt[0]; ndltar[1] = cnt[1]; }
+  return rc;
+}
+
+static int surfdisp_single(const float *thkm, const float *vpm, const float *vsm, const float *rhom,
+                           int nlayer, int iflsph, int iwave, int mode, int igr, int kmax,
+                           const double *t, double dphase, double *cp, double *cg, int *ierr,
+                           int multimode) {
+  if (iflsph != 0) { g_last_error = "spherical-earth flattening (iflsph=1) is not supported"; return MCT_ERR_UNSUPPORTED; }
+  if (nlayer < 1 || nlayer > 200) return arg_error("surfdisp96: nlayer out of range");
+  int nl = nlayer;
+  int rc = mct_surfdisp_batch(1, nlayer, &nl, thkm, vpm, vsm, rhom, kmax, t, iwave, mode, igr, dphase,
+                              multimode, 0, cp, cg, ierr, nullptr);
+  return rc;
+}
+
+int mct_surfdisp96(const float *thkm, const float *vpm, const float *vsm, const float *rhom,
+                   int nlayer, int iflsph, int iwave, int mode, int igr, int kmax, const double *t,
+                   double dphase, double *cp, double *cg, int *ierr) {
+  if (mode != 1) return arg_error("surfdisp96: mode must be 1 (use mct_surfdisp_mmodes)");
+  return surfdisp_single(thkm, vpm, vsm, rhom, nlayer, iflsph, iwave, mode, igr, kmax, t, dphase,
+                         cp, cg, ierr, 0);
+}
+
+int mct_surfdisp_mmodes(const float *thkm, const float *vpm, const float *vsm, const float *rhom,
+                        int nlayer, int iflsph, int iwave, int mode, int igr, int kmax,
+                        const double *t, double dphase, double *cp, double *cg, int *ierr) {
+  return surfdisp_single(thkm, vpm, vsm, rhom, nlayer, iflsph, iwave, mode, igr, kmax, t, dphase,
+                         cp, cg, ierr, 1);
+}
+
+// setup_grt's low-velocity-layer count (surfmodes.f90:320-450, nlvls1) that
+// decides between surfdisp96 and the generalized R/T solver.
+static int count_lvl(const double *vp, const double *vs, int nl, int modetype) {
+  const double eps = (double)1e-6f;
+  int ifs = 0;
+  for (int i = 0; i < nl; ++i) if (!(std::fabs(vs[i]) > eps)) ifs++;
+  int n = 0;
+  if (ifs > 0 && modetype == 1) {
+    double vss1 = vs[ifs < nl ? ifs : nl - 1];
+    for (int i = 1; i < nl - 1; ++i) if (i + 1 > ifs && vs[i] < vss1) n++;
+    return n;
+  }
+  double vs1 = (modetype == 1) ? vs[0] : vs[ifs < nl ? ifs : nl - 1];
+  for (int i = 1; i < nl - 1; ++i) {
+    if (vp[i] < vp[i + 1] && vp[i] < vp[i - 1]) {
+      if (ifs == 0) { if (vs[i] < vs1) n++; }
+      else if (vs[i] > 0.) { if (vs[i] < vs1) n++; }
+    }
+  }
+  return n;
+}
+
+int mct_surfmodes(const double *thick, const double *vp, const double *vs, const double *rho,
+                  int nlayers, const double *freqs, int np, int modetype, int phase_group,
+                  double dc, double *phase, double *group, int *ierr) {
+  if (nlayers < 1 || nlayers > 200 || np < 1 || np > 60) return arg_error("mct_surfmodes: sizes");
+  if (modetype != 0 && modetype != 1) return arg_error("mct_surfmodes: modetype must be 0 or 1");
+  if (count_lvl(vp, vs, nlayers, modetype) > 0) {
+    g_last_error = "column has a low-velocity layer (generalized R/T path)";
+    return MCT_ERR_UNSUPPORTED;
+  }
+  std::vector<float> t4(nlayers), a4(nlayers), b4(nlayers), r4(nlayers);
+  std::vector<double> per(np);
+  for (int i = 0; i < nlayers; ++i) {
+    t4[i] = (float)thick[i]; a4[i] = (float)vp[i]; b4[i] = (float)vs[i]; r4[i] = (float)rho[i];
+  }
+  for (int i = 0; i < np; ++i) per[i] = 1.0 / freqs[i];
+  return mct_surfdisp96(t4.data(), a4.data(), b4.data(), r4.data(), nlayers, 0, modetype == 1 ? 2 : 1,
+                        1, phase_group, np, per.data(), dc, phase, group, ierr);
+}
+
+}  // extern "C"
