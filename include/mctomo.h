@@ -109,6 +109,113 @@ int mct_surfdisp_batch_device(int ncol, int nl_max, const int *nl,
                               int precision, double *cp, double *cg, int *ierr,
                               unsigned long long *ndltar, void *stream);
 
+
+/* ------------------------------------------------------------------------
+ * 2D first-arrival travel times, replaces fm2d's modrays
+ * (fm2d/fm2dray_cartesian.f90:67-480) with its Cartesian argument list:
+ * sources (scx, scz)[nsrc], receivers (rcx, rcz)[nrc], srsin (nrc*nsrc, 2)
+ * column-major (column 1: path exists, source-major), velvin the padded
+ * vertex grid (nvz+2, nvx+2) column-major, grid dicing gdx/gdz, source-grid
+ * refinement asgr with level sgdl and extent sgs, fom 0 first / 1 mixed
+ * order. ttime (nrc, nsrc) is written where a path exists. tfield (optional)
+ * receives the final (nnz, nnx) field per source. Only uar = 1 (no ray paths)
+ * and wrgf = 0 are supported; earth and snb are accepted and unused, as in
+ * the Cartesian reference. MCT_ERR_OUTSIDE when a source or receiver lies
+ * outside the grid (the reference stops the program).
+ * ---------------------------------------------------------------------- */
+int mct_modrays(int nsrc, const double *scx, const double *scz, int nrc,
+                const double *rcx, const double *rcz, const int *srsin,
+                int wrgf, int nvx, int nvz, double goxd, double gozd,
+                double dvxd, double dvzd, const double *velvin, int gdx,
+                int gdz, int asgr, int sgdl, int sgs, double earth, int fom,
+                double snb, double *ttime, int uar, int *crazyray,
+                double *tfield);
+
+/* Many velocity maps (e.g. every period of every chain) sharing the
+ * stations: velv [nmaps][(nvx+2)*(nvz+2)], srs [srs_nmaps][nsrc][nrc] path
+ * flags (map m uses set m % srs_nmaps), ttime [nmaps][nsrc][nrc], tfield
+ * optional [nmaps][nsrc][nnx*nnz]. */
+int mct_modrays_batch(int nmaps, int nsrc, const double *scx,
+                      const double *scz, int nrc, const double *rcx,
+                      const double *rcz, int srs_nmaps, const int *srs,
+                      int nvx, int nvz, double goxd, double gozd, double dvxd,
+                      double dvzd, const double *velv, int gdx, int gdz,
+                      int asgr, int sgdl, int sgs, int fom, double *ttime,
+                      double *tfield);
+
+
+/* ------------------------------------------------------------------------
+ * Surface-wave likelihood with device-resident chains, replaces
+ * likelihood() case 2 (src/likelihood.f90:57-93) -> surf_likelihood
+ * (src/likelihood_surf.F90:110-410) and the kdtree_to_grid call before it.
+ * ---------------------------------------------------------------------- */
+typedef struct {
+  int nx, ny, nz;                    /* T_GRID (src/settings.f90:20-28) */
+  double xmin, ymin, zmin, dx, dy, dz;
+  double scaling, water_depth;
+} mct_grid;
+
+#define MCT_LAW_EXPLICIT 0   /* vp, vs, rho taken from the nucleus parameters */
+#define MCT_LAW_REFERENCE 1  /* vp = 1.73 vs, rho = 1.74 vp^0.25 (src/utils.f90:98-135) */
+#define MCT_LAW_FIXED_RHO 2  /* vp = 1.73 vs, rho = rho_value */
+
+typedef struct {
+  int raylov;          /* 1 Rayleigh, 0 Love (T_LIKE_SET%raylov) */
+  int phase_group;     /* 0 phase velocity (1 needs ray paths: unsupported) */
+  double dphase;       /* dPhaseVel */
+  int gridx, gridy, sgref, sgdic, sgext, order;   /* fm2d settings */
+  int sigdep;          /* 0 data sigma, else sigma = n0*time + n1 */
+  int material_law;    /* MCT_LAW_* */
+  double rho_value;
+  int precision;       /* dispersion root search: 0 FP64, 1 FP32 bracketing */
+} mct_surf_settings;
+
+typedef struct {
+  int nsrc, nrev, np;
+  const double *src;      /* (2, nsrc) station x, y */
+  const double *rev;      /* (2, nrev) */
+  const double *freqs;    /* (np) frequencies, Hz */
+  const int *raystat;     /* (nsrc*nrev, np): 1 where a path is observed */
+  const double *ttime;    /* (nsrc*nrev, np) observed times */
+  const double *sigma;    /* (nsrc*nrev, np) data sigma, or NULL */
+  int nrays;
+} mct_surf_data;
+
+typedef struct mct_surf_ctx mct_surf_ctx;
+
+/* Allocates nslots device-resident chain slots of at most ncell_max nuclei. */
+int mct_surf_create(const mct_grid *grid, const mct_surf_settings *settings,
+                    const mct_surf_data *data, int nslots, int ncell_max,
+                    mct_surf_ctx **ctx);
+int mct_surf_destroy(mct_surf_ctx *ctx);
+
+/* Evaluates one proposal per listed chain against its slot's committed
+ * state. points / params: [nchains][ncell_max][3] (x, y, z) and
+ * (vp, vs, rho); n0 / n1: [nchains][np] noise hyper-parameters. out:
+ * [nchains][4] = like (-log L, DBL_MAX when the model is rejected), misfit,
+ * unweighted misfit, status (0 valid; bit 1 check_model, bit 2 dispersion
+ * failure, bit 8 zero sigma). Host pointers, synchronous. */
+int mct_surf_forward(mct_surf_ctx *ctx, int nchains, const int *slots,
+                     const int *ncells, const double *points,
+                     const double *params, const double *n0,
+                     const double *n1, double *out);
+/* Accept (1) or reject (0) each proposal of the last forward. */
+int mct_surf_commit(mct_surf_ctx *ctx, const int *accept);
+/* Device-pointer forms, asynchronous on stream (NULL = the context's stream),
+ * free of host synchronisation so they can be captured in a CUDA graph. */
+int mct_surf_forward_device(mct_surf_ctx *ctx, int nchains, const int *slots,
+                            const int *ncells, const double *points,
+                            const double *params, const double *n0,
+                            const double *n1, double *out, void *stream);
+int mct_surf_commit_device(mct_surf_ctx *ctx, const int *accept,
+                           void *stream);
+/* Last forward's travel times (np, nsrc, nrev) = phaseTime(k,j,i) and phase
+ * maps (np, nx, ny) for batch position index; either pointer may be NULL. */
+int mct_surf_phase_time(mct_surf_ctx *ctx, int index, double *phase_time,
+                        double *phase_vel);
+/* The context's CUDA stream. */
+int mct_surf_stream(mct_surf_ctx *ctx, void **stream);
+
 #ifdef __cplusplus
 }
 #endif

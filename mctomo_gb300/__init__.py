@@ -6,8 +6,9 @@ forward-modelling call surface (kdtree_to_grid, surfdisp96 / surfmodes,
 modrays, fastMarching3D and the likelihood reductions).
 """
 from ._lib import MctError, lib, LIB_PATH  # noqa: F401
+from .surface import SurfaceLikelihood  # noqa: F401
 from .forward import (  # noqa: F401
-    kdtree_to_grid, surfdisp96, surfdisp_mmodes, surfmodes, surfdisp_batch,
+    kdtree_to_grid, surfdisp96, surfdisp_mmodes, surfmodes, surfdisp_batch, modrays, modrays_batch,
 )
 
 __version__ = "0.1.0"

@@ -3,6 +3,7 @@
 // the library's own stream and wait for the result; _device calls launch on
 // the caller's stream.
 #include "mct_common.cuh"
+#include "fm2d.cuh"
 #include <cstring>
 #include <string>
 #include <vector>
@@ -296,4 +297,98 @@ int mct_surfmodes(const double *thick, const double *vp, const double *vs, const
                         1, phase_group, np, per.data(), dc, phase, group, ierr);
 }
 
+
+// ---------------------------------------------------------------------------
+// 2D travel times (fm2d modrays)
+// ---------------------------------------------------------------------------
+int mct_modrays_batch(int nmaps, int nsrc, const double *scx, const double *scz, int nrc,
+                      const double *rcx, const double *rcz, int srs_nmaps, const int *srs, int nvx,
+                      int nvz, double goxd, double gozd, double dvxd, double dvzd,
+                      const double *velv, int gdx, int gdz, int asgr, int sgdl, int sgs, int fom,
+                      double *ttime, double *tfield) {
+  if (nmaps < 1 || nsrc < 1 || nrc < 1 || nvx < 2 || nvz < 2 || gdx < 1 || gdz < 1 ||
+      srs_nmaps < 1 || (asgr == 1 && (sgdl < 1 || sgs < 1)) || (fom != 0 && fom != 1) ||
+      !(dvxd > 0) || !(dvzd > 0))
+    return arg_error("mct_modrays_batch: bad arguments");
+  Fm2dJob job{};
+  job.nmaps = nmaps; job.nvx = nvx; job.nvz = nvz;
+  job.goxd = goxd; job.gozd = gozd; job.dvxd = dvxd; job.dvzd = dvzd;
+  job.gdx = gdx; job.gdz = gdz; job.asgr = asgr; job.sgdl = sgdl; job.sgs = sgs; job.fom = fom;
+  job.nsrc = nsrc; job.nrc = nrc; job.srs_nmaps = srs_nmaps;
+  Fm2dPlan plan;
+  int rc = fm2d_plan(job, &plan);
+  if (rc) return arg_error("mct_modrays_batch: grid too large for the shared-memory solver");
+  // active solves: a source with no paths is skipped unless it is the first
+  // (fm2dray_cartesian.f90:213-215)
+  std::vector<int2> solves;
+  for (int m = 0; m < nmaps; ++m) {
+    const int *f = srs + (size_t)(m % srs_nmaps) * nsrc * nrc;
+    for (int i = 0; i < nsrc; ++i) {
+      int any = 0;
+      for (int j = 0; j < nrc; ++j) any |= f[(size_t)i * nrc + j];
+      if (any || i == 0) solves.push_back(make_int2(m, i));
+    }
+  }
+  const int nnx = (nvx - 1) * gdx + 1, nnz = (nvz - 1) * gdz + 1;
+  const size_t nv = (size_t)(nvx + 2) * (nvz + 2);
+  const size_t ns = solves.size();
+  std::lock_guard<std::mutex> lk(g_mu);
+  rc = ensure_stream(); if (rc) return rc;
+  size_t bytes = carve_size({sizeof(double) * nv * nmaps, sizeof(double) * (size_t)nnx * nnz * nmaps,
+                             sizeof(double) * (size_t)plan.nref_max * ns, sizeof(double) * (size_t)plan.map_tmp_max * ns,
+                             sizeof(short) * (size_t)plan.map_tmp_max * ns, sizeof(double) * 2 * (nsrc + nrc),
+                             sizeof(int) * (size_t)srs_nmaps * nsrc * nrc, sizeof(int2) * ns,
+                             sizeof(double) * (size_t)nmaps * nsrc * nrc,
+                             tfield ? sizeof(double) * (size_t)nmaps * nsrc * nnx * nnz : 0, sizeof(int)});
+  rc = g_ws.reserve(bytes); if (rc) return rc;
+  Carve cv(g_ws.p);
+  double *d_velv = cv.take<double>(nv * nmaps);
+  job.veln = cv.take<double>((size_t)nnx * nnz * nmaps);
+  job.vref = cv.take<double>((size_t)plan.nref_max * ns);
+  job.map_tmp_t = cv.take<double>((size_t)plan.map_tmp_max * ns);
+  job.map_tmp_s = cv.take<short>((size_t)plan.map_tmp_max * ns);
+  double *d_xy = cv.take<double>(2 * (nsrc + nrc));
+  int *d_srs = cv.take<int>((size_t)srs_nmaps * nsrc * nrc);
+  int2 *d_solves = cv.take<int2>(ns);
+  double *d_tt = cv.take<double>((size_t)nmaps * nsrc * nrc);
+  double *d_tf = tfield ? cv.take<double>((size_t)nmaps * nsrc * nnx * nnz) : nullptr;
+  int *d_status = cv.take<int>(1);
+  cudaStream_t s = g_stream;
+  MCT_CUDA_TRY(cudaMemcpyAsync(d_velv, velv, sizeof(double) * nv * nmaps, cudaMemcpyHostToDevice, s));
+  MCT_CUDA_TRY(cudaMemcpyAsync(d_xy, scx, sizeof(double) * nsrc, cudaMemcpyHostToDevice, s));
+  MCT_CUDA_TRY(cudaMemcpyAsync(d_xy + nsrc, scz, sizeof(double) * nsrc, cudaMemcpyHostToDevice, s));
+  MCT_CUDA_TRY(cudaMemcpyAsync(d_xy + 2 * nsrc, rcx, sizeof(double) * nrc, cudaMemcpyHostToDevice, s));
+  MCT_CUDA_TRY(cudaMemcpyAsync(d_xy + 2 * nsrc + nrc, rcz, sizeof(double) * nrc, cudaMemcpyHostToDevice, s));
+  MCT_CUDA_TRY(cudaMemcpyAsync(d_srs, srs, sizeof(int) * (size_t)srs_nmaps * nsrc * nrc, cudaMemcpyHostToDevice, s));
+  MCT_CUDA_TRY(cudaMemcpyAsync(d_solves, solves.data(), sizeof(int2) * ns, cudaMemcpyHostToDevice, s));
+  // paths that are not computed keep the caller's values
+  MCT_CUDA_TRY(cudaMemcpyAsync(d_tt, ttime, sizeof(double) * (size_t)nmaps * nsrc * nrc, cudaMemcpyHostToDevice, s));
+  MCT_CUDA_TRY(cudaMemsetAsync(d_status, 0, sizeof(int), s));
+  job.velv = d_velv;
+  job.scx = d_xy; job.scz = d_xy + nsrc; job.rcx = d_xy + 2 * nsrc; job.rcz = d_xy + 2 * nsrc + nrc;
+  job.srs = d_srs; job.nsolve = (int)ns; job.solves = d_solves;
+  job.ttime = d_tt; job.tfield = d_tf; job.status = d_status;
+  job.nodes_max = plan.nodes_max; job.nref_max = plan.nref_max; job.map_tmp_max = plan.map_tmp_max;
+  rc = launch_fm2d(job, plan, s); if (rc) return rc;
+  MCT_CUDA_TRY(cudaMemcpyAsync(ttime, d_tt, sizeof(double) * (size_t)nmaps * nsrc * nrc, cudaMemcpyDeviceToHost, s));
+  if (tfield)
+    MCT_CUDA_TRY(cudaMemcpyAsync(tfield, d_tf, sizeof(double) * (size_t)nmaps * nsrc * nnx * nnz, cudaMemcpyDeviceToHost, s));
+  rc = sync_and_check(s, d_status);
+  return rc;
+}
+
+int mct_modrays(int nsrc, const double *scx, const double *scz, int nrc, const double *rcx,
+                const double *rcz, const int *srsin, int wrgf, int nvx, int nvz, double goxd,
+                double gozd, double dvxd, double dvzd, const double *velvin, int gdx, int gdz,
+                int asgr, int sgdl, int sgs, double earth, int fom, double snb, double *ttime,
+                int uar, int *crazyray, double *tfield) {
+  (void)earth; (void)snb;
+  if (wrgf != 0) { g_last_error = "writing ray geometries to file (wrgf) is not supported"; return MCT_ERR_UNSUPPORTED; }
+  if (uar == 0) { g_last_error = "ray paths (uar=0, group velocity) are not supported"; return MCT_ERR_UNSUPPORTED; }
+  if (crazyray) *crazyray = 0;
+  return mct_modrays_batch(1, nsrc, scx, scz, nrc, rcx, rcz, 1, srsin, nvx, nvz, goxd, gozd, dvxd,
+                           dvzd, velvin, gdx, gdz, asgr, sgdl, sgs, fom, ttime, tfield);
+}
+
 }  // extern "C"
+

@@ -1,0 +1,610 @@
+// 2D first-arrival travel times: the GPU replacement of fm2d's modrays
+// (fm2d/fm2dray_cartesian.f90:67-480) with gridder (491-600), bsplrefine
+// (608-674), srtimes (682-797) and the fast marching core travel / fouds1 /
+// fouds2 / addtree / downtree / updtree (fm2d/fm2d_ttime.f90:41-680).
+//
+// fm2d's mixed-order scheme (fouds2) consults only "alive" neighbours, so its
+// result depends on the order in which the narrow band is accepted. To give
+// the reference's travel times rather than a different discretisation, each
+// solve runs the reference's own marching order: one warp per (velocity map,
+// source), the narrow band kept in the reference's binary heap in shared
+// memory (lane 0 performs the sifts in the reference's sequence, so ties break
+// identically), and the up-to-four neighbour updates of each accepted node
+// computed by four lanes at once (they read only accepted nodes and are
+// independent). The refined source grid with its early exit at the box edge,
+// the refined-to-coarse mapping and the narrow-band repair follow modrays.
+// Arithmetic follows the Fortran expression order; the file is built with
+// -fmad=false so nothing is fused.
+#include "mct_common.cuh"
+#include "fm2d.cuh"
+
+namespace {
+
+constexpr int WARPS_PER_BLOCK_MAX = 4;
+
+struct Grid2 {
+  int nnx, nnz, ld;
+  double gox, goz, dnx, dnz;
+};
+
+struct WarpState {
+  double *T;          // [ld * cols]
+  short *S;           // node status: -1 far, 0 alive, >0 heap position
+  unsigned short *H;  // heap, 1-based: H[p] = linear node index (iz-1) + ld*(ix-1)
+  int ntr;
+};
+
+__device__ __forceinline__ int lin(const Grid2 &g, int iz, int ix) { return (iz - 1) + g.ld * (ix - 1); }
+
+// ---- binary heap (fm2d_ttime.f90:527-680), lane 0 only --------------------
+__device__ void addtree(WarpState &w, const Grid2 &g, int iz, int ix) {
+  w.ntr = w.ntr + 1;
+  int me = lin(g, iz, ix);
+  w.S[me] = (short)w.ntr;
+  w.H[w.ntr] = (unsigned short)me;
+  int tpc = w.ntr, tpp = tpc / 2;
+  double tme = w.T[me];
+  while (tpp > 0) {
+    int pn = w.H[tpp];
+    if (tme < w.T[pn]) {
+      w.S[me] = (short)tpp;
+      w.S[pn] = (short)tpc;
+      w.H[tpc] = (unsigned short)pn;
+      w.H[tpp] = (unsigned short)me;
+      tpc = tpp; tpp = tpc / 2;
+    } else {
+      tpp = 0;
+    }
+  }
+}
+
+__device__ void downtree(WarpState &w) {
+  if (w.ntr == 1) { w.ntr = w.ntr - 1; return; }
+  int last = w.H[w.ntr];
+  w.S[last] = 1;
+  w.H[1] = (unsigned short)last;
+  w.ntr = w.ntr - 1;
+  int tpp = 1, tpc = 2 * tpp;
+  const int ntr = w.ntr;
+  while (tpc < ntr) {
+    double rd1 = w.T[w.H[tpc]];
+    double rd2 = w.T[w.H[tpc + 1]];
+    if (rd1 > rd2) tpc = tpc + 1;
+    int cn = w.H[tpc], pn = w.H[tpp];
+    if (w.T[cn] < w.T[pn]) {
+      w.S[pn] = (short)tpc;
+      w.S[cn] = (short)tpp;
+      w.H[tpc] = (unsigned short)pn;
+      w.H[tpp] = (unsigned short)cn;
+      tpp = tpc; tpc = 2 * tpp;
+    } else {
+      tpc = ntr + 1;
+    }
+  }
+  if (tpc == ntr) {
+    int cn = w.H[tpc], pn = w.H[tpp];
+    if (w.T[cn] < w.T[pn]) {
+      w.S[pn] = (short)tpc;
+      w.S[cn] = (short)tpp;
+      w.H[tpc] = (unsigned short)pn;
+      w.H[tpp] = (unsigned short)cn;
+    }
+  }
+}
+
+__device__ void updtree(WarpState &w, const Grid2 &g, int iz, int ix) {
+  int me = lin(g, iz, ix);
+  int tpc = w.S[me], tpp = tpc / 2;
+  double tme = w.T[me];
+  while (tpp > 0) {
+    int pn = w.H[tpp];
+    if (tme < w.T[pn]) {
+      w.S[me] = (short)tpp;
+      w.S[pn] = (short)tpc;
+      w.H[tpc] = (unsigned short)pn;
+      w.H[tpp] = (unsigned short)me;
+      tpc = tpp; tpp = tpc / 2;
+    } else {
+      tpp = 0;
+    }
+  }
+}
+
+// ---- upwind updates --------------------------------------------------------
+__device__ __forceinline__ double quad_root(double a, double b, double c) {
+  double rd1 = b * b - 4.0 * a * c;
+  if (rd1 < 0.0) rd1 = 0.0;
+  return (-b + sqrt(rd1)) / (2.0 * a);
+}
+
+// fm2d_ttime.f90:248-332
+__device__ double fouds1(const WarpState &w, const Grid2 &g, const double *V, int iz, int ix) {
+  int tsw1 = 0;
+  double travm = 0.0;
+  double slown = 1.0 / V[lin(g, iz, ix)];
+  for (int j = ix - 1; j <= ix + 1; j += 2)
+    for (int k = iz - 1; k <= iz + 1; k += 2) {
+      if (!(j >= 1 && j <= g.nnx && k >= 1 && k <= g.nnz)) continue;
+      int swsol = 0;
+      double a = 0, b = 0, c = 0, tref = 0;
+      if (w.S[lin(g, iz, j)] == 0) {
+        swsol = 1;
+        if (w.S[lin(g, k, ix)] == 0) {
+          double u = g.dnx, v = g.dnz;
+          double em = w.T[lin(g, k, ix)] - w.T[lin(g, iz, j)];
+          a = u * u + v * v;
+          b = -(2.0 * (u * u) * em);
+          c = (u * u) * (em * em - (v * v) * (slown * slown));
+          tref = w.T[lin(g, iz, j)];
+        } else {
+          a = 1.0; b = 0.0;
+          c = -((slown * slown) * (g.dnx * g.dnx));
+          tref = w.T[lin(g, iz, j)];
+        }
+      } else if (w.S[lin(g, k, ix)] == 0) {
+        swsol = 1;
+        a = 1.0; b = 0.0;
+        double sd = slown * g.dnz;
+        c = -(sd * sd);
+        tref = w.T[lin(g, k, ix)];
+      }
+      if (swsol == 1) {
+        double trav = tref + quad_root(a, b, c);
+        if (tsw1 == 1) travm = fmin(trav, travm);
+        else { travm = trav; tsw1 = 1; }
+      }
+    }
+  return travm;
+}
+
+// fm2d_ttime.f90:342-518
+__device__ double fouds2(const WarpState &w, const Grid2 &g, const double *V, int iz, int ix) {
+  int tsw1 = 0;
+  double travm = 0.0;
+  double slown = 1.0 / V[lin(g, iz, ix)];
+  for (int j = ix - 1; j <= ix + 1; j += 2) {
+    if (!(j >= 1 && j <= g.nnx)) continue;
+    int swj = -1, j2;
+    if (j == ix - 1) { j2 = j - 1; if (j2 >= 1) { if (w.S[lin(g, iz, j2)] == 0) swj = 0; } }
+    else { j2 = j + 1; if (j2 <= g.nnx) { if (w.S[lin(g, iz, j2)] == 0) swj = 0; } }
+    const bool jalive = w.S[lin(g, iz, j)] == 0;
+    if (jalive && swj == 0) { swj = -1; if (w.T[lin(g, iz, j)] > w.T[lin(g, iz, j2)]) swj = 0; }
+    else swj = -1;
+    for (int k = iz - 1; k <= iz + 1; k += 2) {
+      if (!(k >= 1 && k <= g.nnz)) continue;
+      int swk = -1, k2;
+      if (k == iz - 1) { k2 = k - 1; if (k2 >= 1) { if (w.S[lin(g, k2, ix)] == 0) swk = 0; } }
+      else { k2 = k + 1; if (k2 <= g.nnz) { if (w.S[lin(g, k2, ix)] == 0) swk = 0; } }
+      const bool kalive = w.S[lin(g, k, ix)] == 0;
+      if (kalive && swk == 0) { swk = -1; if (w.T[lin(g, k, ix)] > w.T[lin(g, k2, ix)]) swk = 0; }
+      else swk = -1;
+      int swsol = 0;
+      double a = 0, b = 0, c = 0, tref = 0, tdiv = 1.0;
+      if (swj == 0) {
+        swsol = 1;
+        if (swk == 0) {
+          double u = 2.0 * g.dnx, v = 2.0 * g.dnz;
+          double em = 4.0 * w.T[lin(g, iz, j)] - w.T[lin(g, iz, j2)] - 4.0 * w.T[lin(g, k, ix)];
+          em = em + w.T[lin(g, k2, ix)];
+          a = v * v + u * u;
+          b = 2.0 * em * (u * u);
+          c = (u * u) * (em * em - (slown * slown) * (v * v));
+          tref = 4.0 * w.T[lin(g, iz, j)] - w.T[lin(g, iz, j2)];
+          tdiv = 3.0;
+        } else if (kalive) {
+          double u = g.dnz, v = 2.0 * g.dnx;
+          double em = 3.0 * w.T[lin(g, k, ix)] - 4.0 * w.T[lin(g, iz, j)] + w.T[lin(g, iz, j2)];
+          a = v * v + 9.0 * (u * u);
+          b = 6.0 * em * (u * u);
+          c = (u * u) * (em * em - (slown * slown) * (v * v));
+          tref = w.T[lin(g, k, ix)];
+          tdiv = 1.0;
+        } else {
+          double u = 2.0 * g.dnx;
+          a = 1.0; b = 0.0;
+          c = -((u * u) * (slown * slown));
+          tref = 4.0 * w.T[lin(g, iz, j)] - w.T[lin(g, iz, j2)];
+          tdiv = 3.0;
+        }
+      } else if (jalive) {
+        swsol = 1;
+        if (swk == 0) {
+          double u = g.dnx, v = 2.0 * g.dnz;
+          double em = 3.0 * w.T[lin(g, iz, j)] - 4.0 * w.T[lin(g, k, ix)] + w.T[lin(g, k2, ix)];
+          a = v * v + 9.0 * (u * u);
+          b = 6.0 * em * (u * u);
+          c = (u * u) * (em * em - (v * v) * (slown * slown));
+          tref = w.T[lin(g, iz, j)];
+          tdiv = 1.0;
+        } else if (kalive) {
+          double u = g.dnx, v = g.dnz;
+          double em = w.T[lin(g, k, ix)] - w.T[lin(g, iz, j)];
+          a = u * u + v * v;
+          b = -(2.0 * (u * u) * em);
+          c = (u * u) * (em * em - (v * v) * (slown * slown));
+          tref = w.T[lin(g, iz, j)];
+          tdiv = 1.0;
+        } else {
+          a = 1.0; b = 0.0;
+          c = -((slown * slown) * (g.dnx * g.dnx));
+          tref = w.T[lin(g, iz, j)];
+          tdiv = 1.0;
+        }
+      } else {
+        if (swk == 0) {
+          swsol = 1;
+          double u = 2.0 * g.dnz;
+          a = 1.0; b = 0.0;
+          c = -((u * u) * (slown * slown));
+          tref = 4.0 * w.T[lin(g, k, ix)] - w.T[lin(g, k2, ix)];
+          tdiv = 3.0;
+        } else if (kalive) {
+          swsol = 1;
+          a = 1.0; b = 0.0;
+          c = -((slown * slown) * (g.dnz * g.dnz));
+          tref = w.T[lin(g, k, ix)];
+          tdiv = 1.0;
+        }
+      }
+      if (swsol == 1) {
+        double trav = (tref + quad_root(a, b, c)) / tdiv;
+        if (tsw1 == 1) travm = fmin(trav, travm);
+        else { travm = trav; tsw1 = 1; }
+      }
+    }
+  }
+  return travm;
+}
+
+// fm2d_ttime.f90:682-711 bilinear
+__device__ __forceinline__ double bilinear(const double nv[2][2], double dsx, double dsz, double dnx, double dnz) {
+  double biv = 0.0;
+  for (int i = 1; i <= 2; ++i)
+    for (int j = 1; j <= 2; ++j) {
+      double produ = (1.0 - fabs(((double)(i - 1) * dnx - dsx) / dnx)) *
+                     (1.0 - fabs(((double)(j - 1) * dnz - dsz) / dnz));
+      biv = biv + nv[i - 1][j - 1] * produ;
+    }
+  return biv;
+}
+
+// The marching loop of travel (fm2d_ttime.f90:137-237), whole warp.
+// urg == 1 adds the refined-box exit test; vnr/vnb are compared with the
+// current (refined) grid size exactly as the reference's module variables
+// are at that point.
+__device__ void march(WarpState &w, const Grid2 &g, const double *V, int fom, int urg, int vnl,
+                      int vnr, int vnt, int vnb) {
+  const int lane = threadIdx.x & 31;
+  for (;;) {
+    int ix = 0, iz = 0, go = 0;
+    if (lane == 0) {
+      if (w.ntr > 0) {
+        int top = w.H[1];
+        iz = top % g.ld + 1; ix = top / g.ld + 1;
+        go = 1;
+        if (urg == 1) {
+          int swrg = 0;
+          if (ix == 1 && vnl != 1) swrg = 1;
+          if (ix == g.nnx && vnr != g.nnx) swrg = 1;
+          if (iz == 1 && vnt != 1) swrg = 1;
+          if (iz == g.nnz && vnb != g.nnz) swrg = 1;
+          if (swrg) { w.S[lin(g, iz, ix)] = 0; go = 0; }
+        }
+        if (go) {
+          w.S[lin(g, iz, ix)] = 0;
+          downtree(w);
+        }
+      }
+    }
+    go = __shfl_sync(0xffffffffu, go, 0);
+    if (!go) break;
+    ix = __shfl_sync(0xffffffffu, ix, 0);
+    iz = __shfl_sync(0xffffffffu, iz, 0);
+    __syncwarp();
+    // neighbours in the reference's order: x-1, x+1, z-1, z+1
+    int nz_ = iz, nx_ = ix;
+    bool valid = false;
+    if (lane < 4) {
+      if (lane == 0) { nx_ = ix - 1; valid = nx_ >= 1; }
+      else if (lane == 1) { nx_ = ix + 1; valid = nx_ <= g.nnx; }
+      else if (lane == 2) { nz_ = iz - 1; valid = nz_ >= 1; }
+      else { nz_ = iz + 1; valid = nz_ <= g.nnz; }
+    }
+    int st = 0;
+    if (valid) {
+      st = w.S[lin(g, nz_, nx_)];
+      if (st != 0) {
+        double t = fom == 0 ? fouds1(w, g, V, nz_, nx_) : fouds2(w, g, V, nz_, nx_);
+        w.T[lin(g, nz_, nx_)] = t;
+      }
+    }
+    int code = valid ? (st == -1 ? 1 : (st > 0 ? 2 : 0)) : 0;
+    int c0 = __shfl_sync(0xffffffffu, code, 0), c1 = __shfl_sync(0xffffffffu, code, 1);
+    int c2 = __shfl_sync(0xffffffffu, code, 2), c3 = __shfl_sync(0xffffffffu, code, 3);
+    __syncwarp();
+    if (lane == 0) {
+      if (c0 == 1) addtree(w, g, iz, ix - 1); else if (c0 == 2) updtree(w, g, iz, ix - 1);
+      if (c1 == 1) addtree(w, g, iz, ix + 1); else if (c1 == 2) updtree(w, g, iz, ix + 1);
+      if (c2 == 1) addtree(w, g, iz - 1, ix); else if (c2 == 2) updtree(w, g, iz - 1, ix);
+      if (c3 == 1) addtree(w, g, iz + 1, ix); else if (c3 == 2) updtree(w, g, iz + 1, ix);
+    }
+    __syncwarp();
+  }
+  __syncwarp();
+}
+
+// Source initialisation of travel (fm2d_ttime.f90:95-127), lane 0.
+__device__ void init_source(WarpState &w, const Grid2 &g, const double *V, double scx, double scz) {
+  int isx = (int)((scx - g.gox) / g.dnx) + 1;
+  int isz = (int)((scz - g.goz) / g.dnz) + 1;
+  if (isx == g.nnx) isx = isx - 1;
+  if (isz == g.nnz) isz = isz - 1;
+  double vss[2][2];
+  for (int i = 1; i <= 2; ++i)
+    for (int j = 1; j <= 2; ++j) vss[i - 1][j - 1] = V[lin(g, isz - 1 + j, isx - 1 + i)];
+  double dsx = (scx - g.gox) - (double)(isx - 1) * g.dnx;
+  double dsz = (scz - g.goz) - (double)(isz - 1) * g.dnz;
+  double vsrc = bilinear(vss, dsx, dsz, g.dnx, g.dnz);
+  w.ntr = 0;
+  for (int i = 1; i <= 2; ++i)
+    for (int j = 1; j <= 2; ++j) {
+      double ex = dsx - (double)(i - 1) * g.dnx;
+      double ez = dsz - (double)(j - 1) * g.dnz;
+      double ds = sqrt(ex * ex + ez * ez);
+      w.T[lin(g, isz - 1 + j, isx - 1 + i)] = 2.0 * ds / (vss[i - 1][j - 1] + vsrc);
+      addtree(w, g, isz - 1 + j, isx - 1 + i);
+    }
+}
+
+__device__ __forceinline__ double bsw(int q, double u) {
+  double om = 1.0 - u;
+  switch (q) {
+    case 0: return om * om * om / 6.0;
+    case 1: return (4.0 - 6.0 * (u * u) + 3.0 * (u * u * u)) / 6.0;
+    case 2: return (1.0 + 3.0 * u + 3.0 * (u * u) - 3.0 * (u * u * u)) / 6.0;
+    default: return (u * u * u) / 6.0;
+  }
+}
+
+// gridder (fm2dray_cartesian.f90:491-600): one block per map.
+__global__ void gridder_kernel(Fm2dJob job) {
+  const int map = blockIdx.x;
+  const int nnx = (job.nvx - 1) * job.gdx + 1, nnz = (job.nvz - 1) * job.gdz + 1;
+  const int ldv = job.nvz + 2;
+  const double *velv = job.velv + (size_t)map * (job.nvx + 2) * ldv;
+  double *veln = job.veln + (size_t)map * nnx * nnz;
+  for (int node = threadIdx.x; node < nnx * nnz; node += blockDim.x) {
+    int stz = node % nnz + 1, stx = node / nnz + 1;
+    // invert stz = gdz*(i-1)+l (l in 1..gdz, or gdz+1 in the last cell)
+    int i = (stz - 1) / job.gdz + 1; if (i > job.nvz - 1) i = job.nvz - 1;
+    int l = stz - job.gdz * (i - 1);
+    int j = (stx - 1) / job.gdx + 1; if (j > job.nvx - 1) j = job.nvx - 1;
+    int m = stx - job.gdx * (j - 1);
+    double u = (double)(m - 1) / (double)job.gdx;
+    double v = (double)(l - 1) / (double)job.gdz;
+    double sumi = 0.0;
+    for (int i1 = 1; i1 <= 4; ++i1) {
+      double sumj = 0.0;
+      for (int j1 = 1; j1 <= 4; ++j1)
+        sumj = sumj + bsw(j1 - 1, u) * velv[(size_t)(j - 2 + j1) * ldv + (i - 2 + i1)];
+      sumi = sumi + bsw(i1 - 1, v) * sumj;
+    }
+    veln[(size_t)(stx - 1) * nnz + (stz - 1)] = sumi;
+  }
+}
+
+__global__ void __launch_bounds__(32 * WARPS_PER_BLOCK_MAX)
+fm2d_solve_kernel(Fm2dJob job, int warp_bytes) {
+  extern __shared__ __align__(16) unsigned char smem[];
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int solve = blockIdx.x * (blockDim.x >> 5) + warp;
+  if (solve >= job.nsolve) return;
+  const int map = job.solves[solve].x, src = job.solves[solve].y;
+  unsigned char *base = smem + (size_t)warp * warp_bytes;
+  const int nodes_max = job.nodes_max;
+  WarpState w;
+  w.T = reinterpret_cast<double *>(base);
+  w.S = reinterpret_cast<short *>(base + sizeof(double) * nodes_max);
+  w.H = reinterpret_cast<unsigned short *>(base + (sizeof(double) + sizeof(short)) * nodes_max);
+  w.ntr = 0;
+  const int nnx = (job.nvx - 1) * job.gdx + 1, nnz = (job.nvz - 1) * job.gdz + 1;
+  const double dvx = job.dvxd, dvz = job.dvzd;
+  Grid2 gc{nnx, nnz, nnz, job.goxd, job.gozd, dvx / job.gdx, dvz / job.gdz};
+  const double *Vc = job.veln + (size_t)map * nnx * nnz;
+  const double x = job.scx[src], z = job.scz[src];
+  int isx = (int)((x - gc.gox) / gc.dnx) + 1;
+  int isz = (int)((z - gc.goz) / gc.dnz) + 1;
+  if (isx < 1 || isx > nnx || isz < 1 || isz > nnz) {
+    if (lane == 0) atomicExch(job.status, MCT_ERR_OUTSIDE);
+    return;
+  }
+  if (isx == nnx) isx = isx - 1;
+  if (isz == nnz) isz = isz - 1;
+  const int sgs = job.sgs, sgdl = job.sgdl;
+  const int vnl = max(isx - sgs, 1), vnr = min(isx + sgs, nnx);
+  const int vnt = max(isz - sgs, 1), vnb = min(isz + sgs, nnz);
+  if (job.asgr == 1) {
+    const int nrnx = (vnr - vnl) * sgdl + 1, nrnz = (vnb - vnt) * sgdl + 1;
+    Grid2 gr{nrnx, nrnz, nrnz, gc.gox + gc.dnx * (double)(vnl - 1), gc.goz + gc.dnz * (double)(vnt - 1),
+             dvx / (double)(job.gdx * sgdl), dvz / (double)(job.gdz * sgdl)};
+    double *Vr = job.vref + (size_t)solve * job.nref_max;
+    // bsplrefine (fm2dray_cartesian.f90:608-674)
+    {
+      const int nrxr = job.gdx * sgdl, nrzr = job.gdz * sgdl;
+      const int origx = (vnl - 1) * sgdl + 1, origz = (vnt - 1) * sgdl + 1;
+      const int ldv = job.nvz + 2;
+      const double *velv = job.velv + (size_t)map * (job.nvx + 2) * ldv;
+      for (int node = lane; node < nrnx * nrnz; node += 32) {
+        int idm1 = node % nrnz + 1, idm2 = node / nrnz + 1;
+        int st1 = idm1 + origz - 1, st2 = idm2 + origx - 1;
+        int i = (st1 - 1) / nrzr + 1; if (i > job.nvz - 1) i = job.nvz - 1;
+        int k = st1 - nrzr * (i - 1);
+        int j = (st2 - 1) / nrxr + 1; if (j > job.nvx - 1) j = job.nvx - 1;
+        int l = st2 - nrxr * (j - 1);
+        int c1 = job.gdz * (i - 1) + (k - 1) / sgdl + 1;
+        int c2 = job.gdx * (j - 1) + (l - 1) / sgdl + 1;
+        if (c1 < vnt || c1 > vnb || c2 < vnl || c2 > vnr) { Vr[node] = 0.0; continue; }
+        double u = (double)(l - 1) / (double)nrxr;
+        double v = (double)(k - 1) / (double)nrzr;
+        double sum[4];
+        for (int i1 = 1; i1 <= 4; ++i1) {
+          sum[i1 - 1] = 0.0;
+          for (int j1 = 1; j1 <= 4; ++j1)
+            sum[i1 - 1] = sum[i1 - 1] + bsw(j1 - 1, u) * velv[(size_t)(j - 2 + j1) * ldv + (i - 2 + i1)];
+          sum[i1 - 1] = bsw(i1 - 1, v) * sum[i1 - 1];
+        }
+        Vr[node] = sum[0] + sum[1] + sum[2] + sum[3];
+      }
+    }
+    for (int q = lane; q < nrnx * nrnz; q += 32) w.S[q] = -1;
+    __syncwarp();
+    if (lane == 0) init_source(w, gr, Vr, x, z);
+    __syncwarp();
+    march(w, gr, Vr, job.fom, 1, vnl, vnr, vnt, vnb);
+    // map refined onto coarse: gather the mapped refined nodes first
+    const int mx = (nrnx - 1) / sgdl + 1, mz = (nrnz - 1) / sgdl + 1;   // = vnr-vnl+1, vnb-vnt+1
+    double *tmpT = job.map_tmp_t + (size_t)solve * job.map_tmp_max;
+    short *tmpS = job.map_tmp_s + (size_t)solve * job.map_tmp_max;
+    for (int q = lane; q < mx * mz; q += 32) {
+      int a = q % mz, b = q / mz;
+      int k = a * sgdl + 1, l = b * sgdl + 1;
+      int r = lin(gr, k, l);
+      tmpT[q] = w.T[r];
+      tmpS[q] = w.S[r];
+    }
+    __syncwarp();
+    for (int q = lane; q < nnx * nnz; q += 32) w.S[q] = -1;
+    __syncwarp();
+    for (int q = lane; q < mx * mz; q += 32) {
+      int a = q % mz, b = q / mz;
+      int c = lin(gc, vnt + a, vnl + b);
+      short s = tmpS[q];
+      w.S[c] = s;
+      if (s >= 0) w.T[c] = tmpT[q];
+    }
+    __syncwarp();
+    // narrow band repair (fm2dray_cartesian.f90:384-405); order-independent
+    for (int q = lane; q < nnx * nnz; q += 32) {
+      int l = q % nnz + 1, k = q / nnz + 1;
+      if (w.S[q] == 0) {
+        bool far = (l - 1 >= 1 && w.S[lin(gc, l - 1, k)] == -1) || (l + 1 <= nnz && w.S[lin(gc, l + 1, k)] == -1) ||
+                   (k - 1 >= 1 && w.S[lin(gc, l, k - 1)] == -1) || (k + 1 <= nnx && w.S[lin(gc, l, k + 1)] == -1);
+        if (far) w.S[q] = 1;
+      }
+    }
+    __syncwarp();
+    // travel(urg=2): heap from all nodes marked close, i outer, j inner
+    if (lane == 0) {
+      w.ntr = 0;
+      for (int i = 1; i <= nnx; ++i)
+        for (int j = 1; j <= nnz; ++j)
+          if (w.S[lin(gc, j, i)] > 0) addtree(w, gc, j, i);
+    }
+    __syncwarp();
+    march(w, gc, Vc, job.fom, 2, vnl, vnr, vnt, vnb);
+  } else {
+    for (int q = lane; q < nnx * nnz; q += 32) w.S[q] = -1;
+    __syncwarp();
+    if (lane == 0) init_source(w, gc, Vc, x, z);
+    __syncwarp();
+    march(w, gc, Vc, job.fom, 0, vnl, vnr, vnt, vnb);
+  }
+  // optional travel-time field
+  if (job.tfield) {
+    double *tf = job.tfield + ((size_t)map * job.nsrc + src) * nnx * nnz;
+    for (int q = lane; q < nnx * nnz; q += 32) tf[q] = w.T[q];
+  }
+  // srtimes (fm2dray_cartesian.f90:682-797), one receiver per lane
+  const int *srs = job.srs + (size_t)(map % job.srs_nmaps) * job.nsrc * job.nrc + (size_t)src * job.nrc;
+  double *tt = job.ttime + ((size_t)map * job.nsrc + src) * job.nrc;
+  for (int r = lane; r < job.nrc; r += 32) {
+    if (srs[r] == 0) continue;
+    const double rx = job.rcx[r], rz = job.rcz[r];
+    int irx = (int)floor((rx - gc.gox) / gc.dnx) + 1;
+    int irz = (int)floor((rz - gc.goz) / gc.dnz) + 1;
+    if (irx < 1 || irx > nnx || irz < 1 || irz > nnz) { atomicExch(job.status, MCT_ERR_OUTSIDE); continue; }
+    if (irx == nnx) irx = irx - 1;
+    if (irz == nnz) irz = irz - 1;
+    int jsx = (int)floor((x - gc.gox) / gc.dnx) + 1;
+    int jsz = (int)floor((z - gc.goz) / gc.dnz) + 1;
+    double dpl = gc.dnx, rd1 = gc.dnz;
+    if (rd1 < dpl) dpl = rd1;
+    double sred = (x - rx) * (x - rx);
+    sred = sred + (z - rz) * (z - rz);
+    sred = sqrt(sred);
+    int sw = 0;
+    if (sred < dpl) sw = 1;
+    if (jsx == irx && jsz == irz) sw = 1;
+    double trr;
+    if (sw == 1) {
+      // source and receiver velocities (the source cell is not clamped,
+      // as in the reference; callers keep sources off the max edges)
+      int jx = min(jsx, nnx - 1), jz = min(jsz, nnz - 1);
+      double vss[2][2];
+      for (int k = 1; k <= 2; ++k)
+        for (int l = 1; l <= 2; ++l) vss[k - 1][l - 1] = Vc[lin(gc, jz - 1 + l, jx - 1 + k)];
+      double drx = (x - gc.gox) - (double)(jsx - 1) * gc.dnx;
+      double drz = (z - gc.goz) - (double)(jsz - 1) * gc.dnz;
+      double vels = bilinear(vss, drx, drz, gc.dnx, gc.dnz);
+      for (int k = 1; k <= 2; ++k)
+        for (int l = 1; l <= 2; ++l) vss[k - 1][l - 1] = Vc[lin(gc, irz - 1 + l, irx - 1 + k)];
+      drx = (rx - gc.gox) - (double)(irx - 1) * gc.dnx;
+      drz = (rz - gc.goz) - (double)(irz - 1) * gc.dnz;
+      double velr = bilinear(vss, drx, drz, gc.dnx, gc.dnz);
+      trr = 2.0 * sred / (vels + velr);
+    } else {
+      double drx = (rx - gc.gox) - (double)(irx - 1) * gc.dnx;
+      double drz = (rz - gc.goz) - (double)(irz - 1) * gc.dnz;
+      trr = 0.0;
+      for (int k = 1; k <= 2; ++k)
+        for (int l = 1; l <= 2; ++l) {
+          double produ = (1.0 - fabs(((double)(l - 1) * gc.dnz - drz) / gc.dnz)) *
+                         (1.0 - fabs(((double)(k - 1) * gc.dnx - drx) / gc.dnx));
+          trr = trr + w.T[lin(gc, irz - 1 + l, irx - 1 + k)] * produ;
+        }
+    }
+    tt[r] = trr;
+  }
+}
+
+}  // namespace
+
+int fm2d_plan(const Fm2dJob &job, Fm2dPlan *plan) {
+  const int nnx = (job.nvx - 1) * job.gdx + 1, nnz = (job.nvz - 1) * job.gdz + 1;
+  int nodes = nnx * nnz;
+  int nref = 0, tmp = 0;
+  if (job.asgr == 1) {
+    int nr = 2 * job.sgs * job.sgdl + 1;
+    nref = nr * nr;
+    tmp = (2 * job.sgs + 1) * (2 * job.sgs + 1);
+  }
+  int nodes_max = nodes > nref ? nodes : nref;
+  if (nodes_max > 32000) return MCT_ERR_ARG;   // int16 heap positions / node ids
+  int wb = nodes_max * (int)(sizeof(double) + sizeof(short) + sizeof(unsigned short)) + 64;
+  wb = (wb + 15) & ~15;
+  int wpb = (227 * 1024) / wb;
+  if (wpb < 1) return MCT_ERR_ARG;
+  if (wpb > WARPS_PER_BLOCK_MAX) wpb = WARPS_PER_BLOCK_MAX;
+  plan->nodes_max = nodes_max;
+  plan->nref_max = nref;
+  plan->map_tmp_max = tmp;
+  plan->warp_bytes = wb;
+  plan->warps_per_block = wpb;
+  return MCT_OK;
+}
+
+int launch_fm2d(const Fm2dJob &job, const Fm2dPlan &plan, cudaStream_t s) {
+  static bool attr = false;
+  if (!attr) {
+    cudaFuncSetAttribute(fm2d_solve_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, 227 * 1024);
+    attr = true;
+  }
+  gridder_kernel<<<job.nmaps, 256, 0, s>>>(job);
+  MCT_CUDA_TRY(cudaGetLastError());
+  if (job.nsolve == 0) return MCT_OK;
+  int wpb = plan.warps_per_block;
+  int blocks = (job.nsolve + wpb - 1) / wpb;
+  fm2d_solve_kernel<<<blocks, 32 * wpb, (size_t)plan.warp_bytes * wpb, s>>>(job, plan.warp_bytes);
+  MCT_CUDA_TRY(cudaGetLastError());
+  return MCT_OK;
+}

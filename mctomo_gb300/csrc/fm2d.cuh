@@ -1,0 +1,33 @@
+// fm2d job description shared by the fm2d kernels and the C ABI.
+#pragma once
+#include <cuda_runtime.h>
+
+struct Fm2dJob {
+  int nmaps;                 // velocity maps (e.g. chains x periods)
+  int nvx, nvz;              // B-spline vertex grid
+  double goxd, gozd, dvxd, dvzd;
+  int gdx, gdz, asgr, sgdl, sgs, fom;
+  const double *velv;        // [nmaps][nvx+2][nvz+2] padded vertex grids (Fortran (nvz+2,nvx+2))
+  double *veln;              // [nmaps][nnx][nnz] scratch: B-spline node velocities
+  double *vref;              // [nsolve][nref_max] scratch: refined source-box velocities
+  double *map_tmp_t;         // [nsolve][map_tmp_max] scratch
+  short *map_tmp_s;          // [nsolve][map_tmp_max] scratch
+  int nsrc, nrc;
+  const double *scx, *scz, *rcx, *rcz;
+  const int *srs;            // [srs_nmaps][nsrc][nrc] path flags
+  int srs_nmaps;             // map m uses srs set (m % srs_nmaps)
+  int nsolve;
+  const int2 *solves;        // [nsolve] (map, 0-based source)
+  double *ttime;             // [nmaps][nsrc][nrc]
+  double *tfield;            // optional [nmaps][nsrc][nnx][nnz]
+  int *status;
+  // from fm2d_plan
+  int nodes_max, nref_max, map_tmp_max;
+};
+
+struct Fm2dPlan {
+  int nodes_max, nref_max, map_tmp_max, warp_bytes, warps_per_block;
+};
+
+int fm2d_plan(const Fm2dJob &job, Fm2dPlan *plan);
+int launch_fm2d(const Fm2dJob &job, const Fm2dPlan &plan, cudaStream_t s);

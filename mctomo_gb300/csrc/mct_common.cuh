@@ -79,6 +79,7 @@ int launch_grid_nearest(const GridJob &job, cudaStream_t s);
 // Dispersion: surfdisp96 per column.
 struct DispJob {
   int ncol;
+  const int *ncol_dev;   // optional device-side column count (<= ncol)
   int nl_max;            // stride of the layer arrays
   const int *nl;         // [ncol]
   const float *thk, *vp, *vs, *rho;  // [ncol][nl_max] REAL*4 model

@@ -1,0 +1,264 @@
+// Surface-wave likelihood context: device-resident chain slots and the C ABI
+// around surf_forward / surf_commit (surf_pipeline.cu).
+#include "mct_common.cuh"
+#include "surf_pipeline.cuh"
+#include <vector>
+#include <cstring>
+#include <string>
+
+struct mct_surf_ctx {
+  SurfBatch b{};          // device pointers and sizes (inputs re-pointed per call)
+  SurfPlan plan{};
+  int nslots = 0;
+  cudaStream_t stream = nullptr;
+  void *mem = nullptr;    // one allocation for everything
+  // device staging for host-pointer calls
+  int *d_slots = nullptr, *d_ncells = nullptr, *d_accept = nullptr;
+  double *d_points = nullptr, *d_params = nullptr, *d_n0 = nullptr, *d_n1 = nullptr, *d_out = nullptr;
+  int last_nchains = 0;
+};
+
+namespace {
+std::string &err() { static thread_local std::string e; return e; }
+}
+
+extern "C" {
+
+int mct_surf_create(const mct_grid *g, const mct_surf_settings *st, const mct_surf_data *dat, int nslots,
+                    int ncell_max, mct_surf_ctx **out) {
+  if (!g || !st || !dat || !out || nslots < 1 || ncell_max < 1 || ncell_max > 12800) return MCT_ERR_ARG;
+  if (g->nx < 2 || g->ny < 2 || g->nz < 1 || !(g->dx > 0) || !(g->dy > 0) || !(g->dz > 0) || !(g->scaling > 0))
+    return MCT_ERR_ARG;
+  if (st->phase_group != 0) return MCT_ERR_UNSUPPORTED;   // group velocity needs ray paths
+  if (st->raylov != 0 && st->raylov != 1) return MCT_ERR_ARG;
+  if (dat->np < 1 || dat->np > 60 || dat->nsrc < 1 || dat->nrev < 1) return MCT_ERR_ARG;
+  if (!(st->dphase != 0.0)) return MCT_ERR_ARG;
+  *out = nullptr;
+  mct_surf_ctx *c = new mct_surf_ctx();
+  SurfBatch &b = c->b;
+  b.nx = g->nx; b.ny = g->ny; b.nz = g->nz;
+  b.xmin = g->xmin; b.ymin = g->ymin; b.zmin = g->zmin; b.dx = g->dx; b.dy = g->dy; b.dz = g->dz;
+  b.scaling = g->scaling; b.water_depth = g->water_depth;
+  b.law = st->material_law; b.rho_value = st->rho_value;
+  b.iwave = st->raylov == 1 ? 2 : 1; b.precision = st->precision; b.dphase = st->dphase;
+  b.sigdep = st->sigdep;
+  b.np = dat->np; b.nsrc = dat->nsrc; b.nrev = dat->nrev; b.nrays = dat->nrays;
+  b.ncell_max = ncell_max;
+  b.nl_max = g->nz + 1;
+  c->nslots = nslots;
+  const int np = dat->np, nsrc = dat->nsrc, nrev = dat->nrev, npairs = nsrc * nrev;
+  const size_t nodes = (size_t)g->nx * g->ny * g->nz;
+  const size_t ncol = (size_t)g->nx * g->ny;
+  const size_t maps = (size_t)np * ncol;
+  const size_t nvv = (size_t)(g->nx + 2) * (g->ny + 2);
+  // fm2d plan and solve list for one chain (active sources per period)
+  Fm2dJob &fj = c->plan.fm2d;
+  fj.nvx = g->nx; fj.nvz = g->ny; fj.goxd = g->xmin; fj.gozd = g->ymin; fj.dvxd = g->dx; fj.dvzd = g->dy;
+  fj.gdx = st->gridx; fj.gdz = st->gridy; fj.asgr = st->sgref; fj.sgdl = st->sgdic; fj.sgs = st->sgext;
+  fj.fom = st->order; fj.nsrc = nsrc; fj.nrc = nrev; fj.srs_nmaps = np;
+  if (fj.gdx < 1 || fj.gdz < 1 || (fj.asgr == 1 && (fj.sgdl < 1 || fj.sgs < 1))) { delete c; return MCT_ERR_ARG; }
+  int rc = fm2d_plan(fj, &c->plan.fm2d_plan);
+  if (rc) { delete c; return MCT_ERR_ARG; }
+  std::vector<int2> one;
+  for (int p = 0; p < np; ++p)
+    for (int i = 0; i < nsrc; ++i) {
+      int any = 0;
+      for (int j = 0; j < nrev; ++j) any |= dat->raystat[(size_t)p * npairs + (size_t)i * nrev + j] == 1;
+      if (any || i == 0) one.push_back(make_int2(p, i));
+    }
+  const int spc = (int)one.size();
+  c->plan.nsolve_per_chain = spc;
+  std::vector<int2> all((size_t)spc * nslots);
+  for (int ch = 0; ch < nslots; ++ch)
+    for (int k = 0; k < spc; ++k) all[(size_t)ch * spc + k] = make_int2(ch * np + one[k].x, one[k].y);
+  const Fm2dPlan &fp = c->plan.fm2d_plan;
+  const size_t nsolve = all.size();
+  const int nn = (g->nx - 1) * fj.gdx + 1, nz2 = (g->ny - 1) * fj.gdz + 1;
+  size_t kd = kd_scratch_bytes(ncell_max);
+  std::vector<size_t> sz = {
+      sizeof(double) * np, sizeof(int) * np * npairs, sizeof(double) * np * npairs, sizeof(double) * np * npairs,
+      sizeof(double) * 2 * (nsrc + nrev), sizeof(int) * np * npairs, sizeof(int2) * nsolve,
+      sizeof(double) * (size_t)fp.nref_max * nsolve, sizeof(double) * (size_t)fp.map_tmp_max * nsolve,
+      sizeof(short) * (size_t)fp.map_tmp_max * nsolve, sizeof(double) * (size_t)nn * nz2 * np * nslots,
+      // batch working state
+      sizeof(double) * (size_t)nslots * ncell_max * 3, sizeof(int) * (size_t)nslots * nodes,
+      sizeof(double) * (size_t)nslots * nodes * 3, sizeof(int) * nslots, sizeof(int) * (size_t)nslots * nodes,
+      kd * nslots, sizeof(int) * 2, sizeof(int) * nslots, sizeof(int), sizeof(int2) * nslots * ncol,
+      sizeof(int) * nslots * ncol, sizeof(float) * 4 * (size_t)nslots * ncol * b.nl_max,
+      sizeof(double) * 2 * (size_t)nslots * ncol * np, sizeof(int) * nslots * ncol, sizeof(unsigned long long) * 2,
+      sizeof(double) * (size_t)nslots * maps, sizeof(double) * (size_t)nslots * np * nvv,
+      sizeof(double) * (size_t)nslots * np * npairs,
+      // committed state
+      sizeof(int) * nslots, sizeof(double) * (size_t)nslots * nodes * 3, sizeof(double) * (size_t)nslots * maps,
+      // staging
+      sizeof(int) * nslots * 3, sizeof(double) * (size_t)nslots * ncell_max * 6, sizeof(double) * 2 * nslots * np,
+      sizeof(double) * 4 * nslots};
+  size_t total = 0;
+  for (size_t s : sz) total = ((total + 255) & ~size_t(255)) + s;
+  total += 256;
+  if (cudaMalloc(&c->mem, total) != cudaSuccess) { err() = "cudaMalloc failed"; delete c; return MCT_ERR_NOMEM; }
+  if (cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking) != cudaSuccess) {
+    cudaFree(c->mem); delete c; return MCT_ERR_CUDA;
+  }
+  Carve cv(c->mem);
+  double *per = cv.take<double>(np);
+  int *rays = cv.take<int>((size_t)np * npairs);
+  double *dtime = cv.take<double>((size_t)np * npairs);
+  double *dsig = cv.take<double>((size_t)np * npairs);
+  double *xy = cv.take<double>(2 * (nsrc + nrev));
+  int *srs = cv.take<int>((size_t)np * npairs);
+  int2 *solves = cv.take<int2>(nsolve);
+  fj.vref = cv.take<double>((size_t)fp.nref_max * nsolve);
+  fj.map_tmp_t = cv.take<double>((size_t)fp.map_tmp_max * nsolve);
+  fj.map_tmp_s = cv.take<short>((size_t)fp.map_tmp_max * nsolve);
+  fj.veln = cv.take<double>((size_t)nn * nz2 * np * nslots);
+  b.params = cv.take<double>((size_t)nslots * ncell_max * 3);
+  b.sites = cv.take<int>((size_t)nslots * nodes);
+  b.vp = cv.take<double>((size_t)nslots * nodes * 3);
+  b.vs = b.vp + (size_t)nslots * nodes; b.rho = b.vs + (size_t)nslots * nodes;
+  b.tie_count = cv.take<int>(nslots);
+  b.tie_nodes = cv.take<int>((size_t)nslots * nodes);
+  b.kd_scratch = cv.take<char>(kd * nslots);
+  b.dev_status = cv.take<int>(2);
+  b.status = cv.take<int>(nslots);
+  b.list_count = cv.take<int>(1);
+  b.list = cv.take<int2>((size_t)nslots * ncol);
+  b.lnl = cv.take<int>((size_t)nslots * ncol);
+  b.lthk = cv.take<float>((size_t)4 * nslots * ncol * b.nl_max);
+  b.lvp = b.lthk + (size_t)nslots * ncol * b.nl_max; b.lvs = b.lvp + (size_t)nslots * ncol * b.nl_max;
+  b.lrho = b.lvs + (size_t)nslots * ncol * b.nl_max;
+  b.lcp = cv.take<double>((size_t)2 * nslots * ncol * np);
+  b.lcg = b.lcp + (size_t)nslots * ncol * np;
+  b.lierr = cv.take<int>((size_t)nslots * ncol);
+  b.ndltar = cv.take<unsigned long long>(2);
+  b.pvel = cv.take<double>((size_t)nslots * maps);
+  b.velv = cv.take<double>((size_t)nslots * np * nvv);
+  b.ttime = cv.take<double>((size_t)nslots * np * npairs);
+  b.committed = cv.take<int>(nslots);
+  b.cvp = cv.take<double>((size_t)nslots * nodes * 3);
+  b.cvs = b.cvp + (size_t)nslots * nodes; b.crho = b.cvs + (size_t)nslots * nodes;
+  b.cpvel = cv.take<double>((size_t)nslots * maps);
+  c->d_slots = cv.take<int>((size_t)nslots * 3);
+  c->d_ncells = c->d_slots + nslots; c->d_accept = c->d_ncells + nslots;
+  c->d_points = cv.take<double>((size_t)nslots * ncell_max * 6);
+  c->d_params = c->d_points + (size_t)nslots * ncell_max * 3;
+  c->d_n0 = cv.take<double>((size_t)2 * nslots * np);
+  c->d_n1 = c->d_n0 + (size_t)nslots * np;
+  c->d_out = cv.take<double>((size_t)4 * nslots);
+  // static data
+  std::vector<double> hper(np);
+  for (int p = 0; p < np; ++p) hper[p] = 1.0 / dat->freqs[p];   // dble(1/freqs), surfmodes.f90:82
+  std::vector<double> hxy(2 * (nsrc + nrev));
+  for (int i = 0; i < nsrc; ++i) { hxy[i] = dat->src[2 * i]; hxy[nsrc + i] = dat->src[2 * i + 1]; }
+  for (int i = 0; i < nrev; ++i) { hxy[2 * nsrc + i] = dat->rev[2 * i]; hxy[2 * nsrc + nrev + i] = dat->rev[2 * i + 1]; }
+  std::vector<int> hr((size_t)np * npairs);
+  for (size_t q = 0; q < hr.size(); ++q) hr[q] = dat->raystat[q] == 1 ? 1 : 0;
+  std::vector<double> hs((size_t)np * npairs, 1.0);
+  if (dat->sigma) for (size_t q = 0; q < hs.size(); ++q) hs[q] = dat->sigma[q];
+  cudaMemcpy(per, hper.data(), sizeof(double) * np, cudaMemcpyHostToDevice);
+  cudaMemcpy(rays, dat->raystat, sizeof(int) * np * npairs, cudaMemcpyHostToDevice);
+  cudaMemcpy(srs, hr.data(), sizeof(int) * np * npairs, cudaMemcpyHostToDevice);
+  cudaMemcpy(dtime, dat->ttime, sizeof(double) * np * npairs, cudaMemcpyHostToDevice);
+  cudaMemcpy(dsig, hs.data(), sizeof(double) * np * npairs, cudaMemcpyHostToDevice);
+  cudaMemcpy(xy, hxy.data(), sizeof(double) * hxy.size(), cudaMemcpyHostToDevice);
+  cudaMemcpy(solves, all.data(), sizeof(int2) * nsolve, cudaMemcpyHostToDevice);
+  cudaMemset(b.committed, 0, sizeof(int) * nslots);
+  cudaMemset(b.ttime, 0, sizeof(double) * (size_t)nslots * np * npairs);
+  if (cudaGetLastError() != cudaSuccess || cudaDeviceSynchronize() != cudaSuccess) {
+    cudaFree(c->mem); cudaStreamDestroy(c->stream); delete c; return MCT_ERR_CUDA;
+  }
+  b.periods = per; b.raystat = rays; b.dtime = dtime; b.dsigma = dsig;
+  fj.scx = xy; fj.scz = xy + nsrc; fj.rcx = xy + 2 * nsrc; fj.rcz = xy + 2 * nsrc + nrev;
+  fj.srs = srs; fj.solves = solves;
+  fj.nodes_max = fp.nodes_max; fj.nref_max = fp.nref_max; fj.map_tmp_max = fp.map_tmp_max;
+  *out = c;
+  return MCT_OK;
+}
+
+int mct_surf_destroy(mct_surf_ctx *c) {
+  if (!c) return MCT_OK;
+  cudaStreamSynchronize(c->stream);
+  cudaFree(c->mem);
+  cudaStreamDestroy(c->stream);
+  delete c;
+  return MCT_OK;
+}
+
+int mct_surf_forward_device(mct_surf_ctx *c, int nchains, const int *slots, const int *ncells,
+                            const double *points, const double *params, const double *n0,
+                            const double *n1, double *out, void *stream) {
+  if (!c || nchains < 1 || nchains > c->nslots) return MCT_ERR_ARG;
+  SurfBatch &b = c->b;
+  b.nchains = nchains; b.slots = slots; b.ncells = ncells; b.points = points; b.params_in = params;
+  b.n0 = n0; b.n1 = n1; b.out = out;
+  c->last_nchains = nchains;
+  cudaStream_t s = stream ? static_cast<cudaStream_t>(stream) : c->stream;
+  return surf_forward(b, c->plan, s);
+}
+
+int mct_surf_commit_device(mct_surf_ctx *c, const int *accept, void *stream) {
+  if (!c || c->last_nchains < 1) return MCT_ERR_ARG;
+  cudaStream_t s = stream ? static_cast<cudaStream_t>(stream) : c->stream;
+  return surf_commit(c->b, accept, s);
+}
+
+int mct_surf_forward(mct_surf_ctx *c, int nchains, const int *slots, const int *ncells, const double *points,
+                     const double *params, const double *n0, const double *n1, double *out) {
+  if (!c || nchains < 1 || nchains > c->nslots) return MCT_ERR_ARG;
+  for (int i = 0; i < nchains; ++i) {
+    if (slots[i] < 0 || slots[i] >= c->nslots) return MCT_ERR_ARG;
+    for (int j = 0; j < i; ++j) if (slots[j] == slots[i]) return MCT_ERR_ARG;
+    if (ncells[i] < 1 || ncells[i] > c->b.ncell_max) return MCT_ERR_ARG;
+  }
+  cudaStream_t s = c->stream;
+  const int np = c->b.np;
+  const size_t pc = (size_t)nchains * c->b.ncell_max * 3;
+  MCT_CUDA_TRY(cudaMemcpyAsync(c->d_slots, slots, sizeof(int) * nchains, cudaMemcpyHostToDevice, s));
+  MCT_CUDA_TRY(cudaMemcpyAsync(c->d_ncells, ncells, sizeof(int) * nchains, cudaMemcpyHostToDevice, s));
+  MCT_CUDA_TRY(cudaMemcpyAsync(c->d_points, points, sizeof(double) * pc, cudaMemcpyHostToDevice, s));
+  MCT_CUDA_TRY(cudaMemcpyAsync(c->d_params, params, sizeof(double) * pc, cudaMemcpyHostToDevice, s));
+  MCT_CUDA_TRY(cudaMemcpyAsync(c->d_n0, n0, sizeof(double) * nchains * np, cudaMemcpyHostToDevice, s));
+  MCT_CUDA_TRY(cudaMemcpyAsync(c->d_n1, n1, sizeof(double) * nchains * np, cudaMemcpyHostToDevice, s));
+  MCT_CUDA_TRY(cudaMemsetAsync(c->b.dev_status, 0, sizeof(int) * 2, s));
+  int rc = mct_surf_forward_device(c, nchains, c->d_slots, c->d_ncells, c->d_points, c->d_params, c->d_n0,
+                                   c->d_n1, c->d_out, s);
+  if (rc) return rc;
+  MCT_CUDA_TRY(cudaMemcpyAsync(out, c->d_out, sizeof(double) * 4 * nchains, cudaMemcpyDeviceToHost, s));
+  int dst[2];
+  MCT_CUDA_TRY(cudaMemcpyAsync(dst, c->b.dev_status, sizeof(int) * 2, cudaMemcpyDeviceToHost, s));
+  MCT_CUDA_TRY(cudaStreamSynchronize(s));
+  if (dst[0]) return dst[0];
+  return MCT_OK;
+}
+
+int mct_surf_commit(mct_surf_ctx *c, const int *accept) {
+  if (!c || c->last_nchains < 1) return MCT_ERR_ARG;
+  cudaStream_t s = c->stream;
+  MCT_CUDA_TRY(cudaMemcpyAsync(c->d_accept, accept, sizeof(int) * c->last_nchains, cudaMemcpyHostToDevice, s));
+  int rc = mct_surf_commit_device(c, c->d_accept, s);
+  if (rc) return rc;
+  MCT_CUDA_TRY(cudaStreamSynchronize(s));
+  return MCT_OK;
+}
+
+int mct_surf_phase_time(mct_surf_ctx *c, int index, double *phase_time, double *phase_vel) {
+  if (!c || index < 0 || index >= c->last_nchains) return MCT_ERR_ARG;
+  const SurfBatch &b = c->b;
+  const size_t npairs = (size_t)b.nsrc * b.nrev;
+  MCT_CUDA_TRY(cudaStreamSynchronize(c->stream));
+  if (phase_time)
+    MCT_CUDA_TRY(cudaMemcpy(phase_time, b.ttime + (size_t)index * b.np * npairs, sizeof(double) * b.np * npairs,
+                            cudaMemcpyDeviceToHost));
+  if (phase_vel)
+    MCT_CUDA_TRY(cudaMemcpy(phase_vel, b.pvel + (size_t)index * b.np * b.nx * b.ny,
+                            sizeof(double) * b.np * b.nx * b.ny, cudaMemcpyDeviceToHost));
+  return MCT_OK;
+}
+
+int mct_surf_stream(mct_surf_ctx *c, void **stream) {
+  if (!c || !stream) return MCT_ERR_ARG;
+  *stream = c->stream;
+  return MCT_OK;
+}
+
+}  // extern "C"

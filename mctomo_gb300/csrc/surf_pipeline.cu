@@ -1,0 +1,257 @@
+// Batched surface-wave likelihood with device-resident chain state: the GPU
+// replacement of likelihood() case 2 (src/likelihood.f90:57-93) ->
+// surf_likelihood (src/likelihood_surf.F90:110-410), together with the
+// kdtree_to_grid call the sampler makes before it.
+//
+// One forward evaluates a proposal for each of many chains:
+//   1. nearest-nucleus gridding of every chain's Voronoi model;
+//   2. material laws vs -> vp (1.73 vs) and vp -> rho (1.74 vp^0.25) or a
+//      fixed density (src/likelihood.f90:75-76, src/utils.f90:98-135);
+//   3. check_model (likelihood_surf.F90:631-646);
+//   4. the columns whose (vp, vs, rho) differ from the chain's committed
+//      state are layered (convert_to_layer, :523-629) and get new dispersion
+//      curves (surfmodes/surfdisp96); the rest reuse the committed curves.
+//      This replaces the CGAL bounding box (:155-170) with an exact
+//      changed-column mask: the curves are identical;
+//   5. phase-velocity maps padded by edge copies (:259-264) feed fm2d for
+//      every (period, source) (:295-320);
+//   6. sigma and the misfit / -log L reductions (:356-404).
+// commit() makes a proposal the chain's state (the sampler's accept);
+// otherwise the next forward starts again from the committed state (reject).
+#include "mct_common.cuh"
+#include "fm2d.cuh"
+#include "surf_pipeline.cuh"
+#include <cfloat>
+#include <vector>
+#include <algorithm>
+
+namespace {
+
+__global__ void material_kernel(int nchains, int ncell_max, const int *ncells, const double *params_in,
+                                double *params_out, int law, double rho_value) {
+  const int c = blockIdx.y;
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < ncell_max; i += gridDim.x * blockDim.x) {
+    size_t o = ((size_t)c * ncell_max + i) * 3;
+    if (i >= ncells[c]) { params_out[o] = params_out[o + 1] = params_out[o + 2] = 1.0; continue; }
+    double vs = params_in[o + 1];
+    double vp, rho;
+    if (law == MCT_LAW_EXPLICIT) {
+      vp = params_in[o]; rho = params_in[o + 2];
+    } else {
+      vp = vs * (double)1.730f;                           // vs2vp_3d
+      rho = (law == MCT_LAW_REFERENCE) ? (double)1.74f * pow(vp, 0.25) : rho_value;   // vp2rho_3d
+    }
+    params_out[o] = vp; params_out[o + 1] = vs; params_out[o + 2] = rho;
+  }
+}
+
+// check_model + changed-column list. One thread per (chain, column).
+__global__ void columns_kernel(SurfBatch b) {
+  const int c = blockIdx.y;
+  const int ncol = b.nx * b.ny;
+  const int slot = b.slots[c];
+  const size_t nodes = (size_t)ncol * b.nz;
+  for (int col = blockIdx.x * blockDim.x + threadIdx.x; col < ncol; col += gridDim.x * blockDim.x) {
+    const size_t o = (size_t)c * nodes + (size_t)col * b.nz;
+    const double *vs = b.vs + o, *vp = b.vp + o, *rho = b.rho + o;
+    bool bad = false;
+    for (int k = 1; k < b.nz; ++k) if (vs[k] < vs[0]) bad = true;
+    if (bad) atomicOr(&b.status[c], 1);
+    bool changed = !b.committed[slot];
+    if (!changed) {
+      const size_t co = (size_t)slot * nodes + (size_t)col * b.nz;
+      for (int k = 0; k < b.nz && !changed; ++k)
+        changed = vs[k] != b.cvs[co + k] || vp[k] != b.cvp[co + k] || rho[k] != b.crho[co + k];
+    }
+    if (changed) {
+      int pos = atomicAdd(b.list_count, 1);
+      b.list[pos] = make_int2(c, col);
+    }
+  }
+}
+
+// convert_to_layer (likelihood_surf.F90:523-629) for listed columns, cast to
+// REAL*4 as surfmodes does (surfmodes.f90:81).
+__global__ void layer_kernel(SurfBatch b) {
+  const int q = blockIdx.x * blockDim.x + threadIdx.x;
+  if (q >= *b.list_count) return;
+  const int2 e = b.list[q];
+  const size_t nodes = (size_t)b.nx * b.ny * b.nz;
+  const size_t o = (size_t)e.x * nodes + (size_t)e.y * b.nz;
+  const double *vp = b.vp + o, *vs = b.vs + o, *rho = b.rho + o;
+  const double EPS = 1.0E-10;
+  float *thk = b.lthk + (size_t)q * b.nl_max, *a = b.lvp + (size_t)q * b.nl_max;
+  float *bb = b.lvs + (size_t)q * b.nl_max, *r = b.lrho + (size_t)q * b.nl_max;
+  int nl = 0;
+  double wd = b.water_depth;
+  if (wd > EPS) { nl = 1; a[0] = (float)(double)1.5f; bb[0] = 0.f; r[0] = 1.f; thk[0] = (float)wd; }
+  double last_vp = vp[0], last_vs = vs[0], last_rho = rho[0];
+  int last_k = 1;
+  for (int k = 2; k <= b.nz; ++k) {
+    if (fabs(vs[k - 1] - last_vs) > EPS) {
+      nl = nl + 1;
+      a[nl - 1] = (float)last_vp; bb[nl - 1] = (float)last_vs; r[nl - 1] = (float)last_rho;
+      thk[nl - 1] = (float)(((double)(k - last_k) * b.dz) / b.scaling);
+      last_vp = vp[k - 1]; last_vs = vs[k - 1]; last_rho = rho[k - 1];
+      last_k = k;
+    }
+  }
+  nl = nl + 1;
+  a[nl - 1] = (float)vp[b.nz - 1]; bb[nl - 1] = (float)vs[b.nz - 1]; r[nl - 1] = (float)rho[b.nz - 1];
+  thk[nl - 1] = 0.f;
+  if (wd > 0) thk[0] = (float)wd;
+  b.lnl[q] = nl;
+}
+
+// Proposal phase maps: committed maps updated with the recomputed columns.
+// pvel layout [chain][period][nx][ny] (Fortran (ny,nx) per period).
+__global__ void scatter_kernel(SurfBatch b) {
+  const int q = blockIdx.x * blockDim.x + threadIdx.x;
+  if (q >= *b.list_count) return;
+  const int2 e = b.list[q];
+  const int ncol = b.nx * b.ny;
+  if (b.lierr[q]) atomicOr(&b.status[e.x], 2);
+  for (int p = 0; p < b.np; ++p)
+    b.pvel[((size_t)e.x * b.np + p) * ncol + e.y] = b.lcp[(size_t)q * b.np + p];
+}
+
+// Padded fm2d vertex grids (likelihood_surf.F90:259-264): interior = phase
+// map, edges copied from the nearest interior node.
+__global__ void pad_kernel(SurfBatch b) {
+  const int map = blockIdx.y;        // chain * np + period
+  const int nvx = b.nx + 2, nvz = b.ny + 2;
+  const double *pv = b.pvel + (size_t)map * b.nx * b.ny;
+  double *v = b.velv + (size_t)map * nvx * nvz;
+  for (int q = blockIdx.x * blockDim.x + threadIdx.x; q < nvx * nvz; q += gridDim.x * blockDim.x) {
+    int jj = q % nvz, ii = q / nvz;            // 0-based padded row (y) and column (x)
+    int j = min(max(jj, 1), b.ny) - 1, i = min(max(ii, 1), b.nx) - 1;
+    v[q] = pv[(size_t)i * b.ny + j];
+  }
+}
+
+// sigma and the misfit / -log L (likelihood_surf.F90:356-404), one block per
+// chain, FP64 block reduction.
+__global__ void misfit_kernel(SurfBatch b) {
+  const int c = blockIdx.x;
+  const int npairs = b.nsrc * b.nrev;
+  const double *pt = b.ttime + (size_t)c * b.np * npairs;   // [p][src][rev] = phaseTime(k,j,p)
+  double like = 0, mis = 0, umis = 0, slog = 0;
+  for (int q = threadIdx.x; q < b.np * npairs; q += blockDim.x) {
+    int p = q / npairs, r = q % npairs;
+    double sig;
+    bool used = b.raystat[(size_t)p * npairs + r] == 1;
+    if (b.sigdep != 0) sig = used ? b.n0[(size_t)c * b.np + p] * pt[q] + b.n1[(size_t)c * b.np + p] : 1.0;
+    else sig = used ? b.dsigma[(size_t)p * npairs + r] : 1.0;
+    if (used) {
+      if (sig < 1.0E-10) atomicOr(&b.status[c], 8);
+      double res = pt[q] - b.dtime[(size_t)p * npairs + r];
+      double r2 = res * res;
+      like += r2 / (2 * (sig * sig));
+      mis += r2 / (sig * sig);
+      umis += r2;
+    }
+    slog += log(sig);
+  }
+  __shared__ double red[4][256];
+  red[0][threadIdx.x] = like; red[1][threadIdx.x] = mis; red[2][threadIdx.x] = umis; red[3][threadIdx.x] = slog;
+  __syncthreads();
+  for (int s = blockDim.x / 2; s > 0; s >>= 1) {
+    if (threadIdx.x < s)
+      for (int k = 0; k < 4; ++k) red[k][threadIdx.x] += red[k][threadIdx.x + s];
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) {
+    const double PI2 = (double)6.283185f;
+    double L = red[0][0] + red[3][0] + (double)((float)b.nrays / 2.0f) * log(PI2);
+    int st = b.status[c];
+    b.out[(size_t)c * 4 + 0] = st ? DBL_MAX : L;
+    b.out[(size_t)c * 4 + 1] = red[1][0];
+    b.out[(size_t)c * 4 + 2] = red[2][0];
+    b.out[(size_t)c * 4 + 3] = (double)st;
+  }
+}
+
+// Copy a chain's proposal into its slot's committed state.
+__global__ void commit_kernel(SurfBatch b, const int *accept) {
+  const int c = blockIdx.y;
+  if (!accept[c] || b.status[c]) return;
+  const int slot = b.slots[c];
+  const size_t nodes = (size_t)b.nx * b.ny * b.nz;
+  const size_t maps = (size_t)b.np * b.nx * b.ny;
+  for (size_t q = blockIdx.x * blockDim.x + threadIdx.x; q < nodes; q += (size_t)gridDim.x * blockDim.x) {
+    b.cvp[(size_t)slot * nodes + q] = b.vp[(size_t)c * nodes + q];
+    b.cvs[(size_t)slot * nodes + q] = b.vs[(size_t)c * nodes + q];
+    b.crho[(size_t)slot * nodes + q] = b.rho[(size_t)c * nodes + q];
+  }
+  for (size_t q = blockIdx.x * blockDim.x + threadIdx.x; q < maps; q += (size_t)gridDim.x * blockDim.x)
+    b.cpvel[(size_t)slot * maps + q] = b.pvel[(size_t)c * maps + q];
+  if (blockIdx.x == 0 && threadIdx.x == 0) b.committed[slot] = 1;
+}
+
+__global__ void gather_committed_maps(SurfBatch b) {
+  const int c = blockIdx.y;
+  const int slot = b.slots[c];
+  const size_t maps = (size_t)b.np * b.nx * b.ny;
+  for (size_t q = blockIdx.x * blockDim.x + threadIdx.x; q < maps; q += (size_t)gridDim.x * blockDim.x)
+    b.pvel[(size_t)c * maps + q] = b.committed[slot] ? b.cpvel[(size_t)slot * maps + q] : 0.0;
+}
+
+}  // namespace
+
+int surf_forward(SurfBatch &b, const SurfPlan &plan, cudaStream_t s) {
+  const int nch = b.nchains;
+  const int ncol = b.nx * b.ny;
+  MCT_CUDA_TRY(cudaMemsetAsync(b.status, 0, sizeof(int) * nch, s));
+  MCT_CUDA_TRY(cudaMemsetAsync(b.list_count, 0, sizeof(int), s));
+  MCT_CUDA_TRY(cudaMemsetAsync(b.dev_status, 0, sizeof(int) * 2, s));
+  // 1-2: material laws then gridding
+  material_kernel<<<dim3((b.ncell_max + 127) / 128, nch), 128, 0, s>>>(nch, b.ncell_max, b.ncells, b.params_in,
+                                                                         b.params, b.law, b.rho_value);
+  MCT_CUDA_TRY(cudaGetLastError());
+  GridJob gj{};
+  gj.d = 3; gj.nx = b.nx; gj.ny = b.ny; gj.nz = b.nz;
+  gj.xmin = b.xmin; gj.ymin = b.ymin; gj.zmin = b.zmin; gj.dx = b.dx; gj.dy = b.dy; gj.dz = b.dz;
+  gj.nchains = nch; gj.ncell_max = b.ncell_max; gj.ncells = b.ncells;
+  gj.points = b.points; gj.params = b.params; gj.box = nullptr;
+  gj.sites_id = b.sites; gj.vp = b.vp; gj.vs = b.vs; gj.rho = b.rho;
+  gj.tie_count = b.tie_count; gj.tie_nodes = b.tie_nodes; gj.kd_scratch = b.kd_scratch; gj.status = b.dev_status;
+  int rc = launch_grid_nearest(gj, s); if (rc) return rc;
+  // 3-4: model check, changed columns, layering, dispersion, scatter
+  columns_kernel<<<dim3((ncol + 127) / 128, nch), 128, 0, s>>>(b);
+  MCT_CUDA_TRY(cudaGetLastError());
+  const int maxlist = nch * ncol;
+  layer_kernel<<<(maxlist + 127) / 128, 128, 0, s>>>(b);
+  MCT_CUDA_TRY(cudaGetLastError());
+  DispJob dj{};
+  dj.ncol = maxlist; dj.ncol_dev = b.list_count; dj.nl_max = b.nl_max; dj.nl = b.lnl;
+  dj.thk = b.lthk; dj.vp = b.lvp; dj.vs = b.lvs; dj.rho = b.lrho;
+  dj.np = b.np; dj.periods = b.periods; dj.iwave = b.iwave; dj.mode = 1; dj.igr = 0;
+  dj.dphase = b.dphase; dj.multimode = 0; dj.precision = b.precision;
+  dj.cp = b.lcp; dj.cg = b.lcg; dj.ierr = b.lierr; dj.ndltar = b.ndltar;
+  rc = launch_surfdisp(dj, s); if (rc) return rc;
+  gather_committed_maps<<<dim3(64, nch), 256, 0, s>>>(b);
+  MCT_CUDA_TRY(cudaGetLastError());
+  scatter_kernel<<<(maxlist + 127) / 128, 128, 0, s>>>(b);
+  MCT_CUDA_TRY(cudaGetLastError());
+  // 5: padded maps and fm2d
+  pad_kernel<<<dim3(8, nch * b.np), 256, 0, s>>>(b);
+  MCT_CUDA_TRY(cudaGetLastError());
+  Fm2dJob fj = plan.fm2d;
+  fj.nmaps = nch * b.np;
+  fj.velv = b.velv;
+  fj.nsolve = plan.nsolve_per_chain * nch;
+  fj.ttime = b.ttime;
+  fj.tfield = nullptr;
+  fj.status = b.dev_status;
+  rc = launch_fm2d(fj, plan.fm2d_plan, s); if (rc) return rc;
+  // 6: misfit
+  misfit_kernel<<<nch, 256, 0, s>>>(b);
+  MCT_CUDA_TRY(cudaGetLastError());
+  return MCT_OK;
+}
+
+int surf_commit(SurfBatch &b, const int *accept_dev, cudaStream_t s) {
+  commit_kernel<<<dim3(64, b.nchains), 256, 0, s>>>(b, accept_dev);
+  MCT_CUDA_TRY(cudaGetLastError());
+  return MCT_OK;
+}

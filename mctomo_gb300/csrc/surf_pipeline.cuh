@@ -1,0 +1,55 @@
+// Device-side description of one batched surface-wave forward.
+#pragma once
+#include <cuda_runtime.h>
+#include "fm2d.cuh"
+
+#include "../../include/mctomo.h"
+
+struct SurfBatch {
+  // grid and settings
+  int nx, ny, nz;
+  double xmin, ymin, zmin, dx, dy, dz, scaling, water_depth;
+  int law; double rho_value;
+  int iwave, precision; double dphase;
+  int sigdep;
+  int np, nsrc, nrev, nrays;
+  const double *periods;     // [np]
+  const int *raystat;        // [np][nsrc*nrev]
+  const double *dtime;       // [np][nsrc*nrev]
+  const double *dsigma;      // [np][nsrc*nrev]
+  // inputs (device)
+  int nchains, ncell_max;
+  const int *slots;          // [nchains]
+  const int *ncells;         // [nchains]
+  const double *points;      // [nchains][ncell_max][3]
+  const double *params_in;   // [nchains][ncell_max][3]
+  const double *n0, *n1;     // [nchains][np]
+  double *out;               // [nchains][4]: like, misfit, unweighted misfit, status
+  // working state for the batch
+  double *params;            // [nchains][ncell_max][3] after material laws
+  int *sites;                // [nchains][nodes]
+  double *vp, *vs, *rho;     // [nchains][nodes]
+  int *tie_count, *tie_nodes; void *kd_scratch; int *dev_status;
+  int *status;               // [nchains]
+  int *list_count; int2 *list;   // changed columns
+  int nl_max;
+  int *lnl; float *lthk, *lvp, *lvs, *lrho;   // [nchains*ncol][nl_max]
+  double *lcp, *lcg; int *lierr;               // [nchains*ncol][np]
+  unsigned long long *ndltar;
+  double *pvel;              // [nchains][np][nx][ny]
+  double *velv;              // [nchains*np][(nx+2)*(ny+2)]
+  double *ttime;             // [nchains*np][nsrc][nrev]
+  // committed per-slot state
+  int *committed;            // [nslots]
+  double *cvp, *cvs, *crho;  // [nslots][nodes]
+  double *cpvel;             // [nslots][np][nx][ny]
+};
+
+struct SurfPlan {
+  Fm2dJob fm2d;              // static parts (stations, settings, scratch, solve list)
+  Fm2dPlan fm2d_plan;
+  int nsolve_per_chain;
+};
+
+int surf_forward(SurfBatch &b, const SurfPlan &plan, cudaStream_t s);
+int surf_commit(SurfBatch &b, const int *accept_dev, cudaStream_t s);

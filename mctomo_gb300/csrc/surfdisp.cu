@@ -386,6 +386,7 @@ __device__ float gtsolh(float a, float b) {
 __global__ void __launch_bounds__(128) surfdisp_kernel(DispJob job) {
   const int col = blockIdx.x * blockDim.x + threadIdx.x;
   if (col >= job.ncol) return;
+  if (job.ncol_dev && col >= *job.ncol_dev) return;
   const int nl = job.nl[col];
   const int kmax = job.np, mode = job.mode, igr = job.igr;
   const bool mm_ = job.multimode != 0;

@@ -102,3 +102,52 @@ def surfdisp_batch(nl, thk, vp, vs, rho, periods, iwave, igr, dphase, mode=1, mu
                                   int(precision), ptr(cp), ptr(cg), ptr(ierr), cnt)
     check("mct_surfdisp_batch", rc)
     return cp, cg, ierr, (cnt[0], cnt[1])
+
+
+def modrays(src, rev, srs, nvx, nvz, goxd, gozd, dvxd, dvzd, velv, gdx=1, gdz=1, asgr=1, sgdl=4,
+            sgs=8, fom=1, snb=0.5, earth=6371.0, ttime=None, tfield=False):
+    """fm2d modrays (fm2d/fm2dray_cartesian.f90:67-480) for travel times only
+    (uar = 1). src: (nsrc, 2), rev: (nrc, 2), srs: (nsrc, nrc) path flags,
+    velv: (nvx+2, nvz+2) C-order = Fortran (nvz+2, nvx+2). Returns ttime
+    (nsrc, nrc) (C order = Fortran (nrc, nsrc)) and optionally the fields
+    (nsrc, nnx, nnz)."""
+    src = _f64(src); rev = _f64(rev)
+    nsrc, nrc = src.shape[0], rev.shape[0]
+    srsin = np.zeros(2 * nsrc * nrc, np.int32)
+    srsin[:nsrc * nrc] = np.asarray(srs, np.int32).reshape(-1)
+    velv = _f64(velv)
+    assert velv.shape == (nvx + 2, nvz + 2)
+    if ttime is None:
+        ttime = np.zeros((nsrc, nrc))
+    nnx = (nvx - 1) * gdx + 1
+    nnz = (nvz - 1) * gdz + 1
+    tf = np.zeros((nsrc, nnx, nnz)) if tfield else None
+    cr = ctypes.c_int(0)
+    sx, sz = np.ascontiguousarray(src[:, 0]), np.ascontiguousarray(src[:, 1])
+    rx, rz = np.ascontiguousarray(rev[:, 0]), np.ascontiguousarray(rev[:, 1])
+    rc = lib().mct_modrays(nsrc, ptr(sx), ptr(sz), nrc, ptr(rx), ptr(rz), ptr(srsin), 0, nvx, nvz,
+                           goxd, gozd, dvxd, dvzd, ptr(velv), gdx, gdz, asgr, sgdl, sgs, earth, fom,
+                           snb, ptr(ttime), 1, ctypes.byref(cr), ptr(tf))
+    check("mct_modrays", rc)
+    return (ttime, tf) if tfield else ttime
+
+
+def modrays_batch(src, rev, srs, nvx, nvz, goxd, gozd, dvxd, dvzd, velv, gdx=1, gdz=1, asgr=1,
+                  sgdl=4, sgs=8, fom=1, ttime=None):
+    """Many velocity maps with shared stations. velv: (nmaps, nvx+2, nvz+2);
+    srs: (srs_nmaps, nsrc, nrc). Returns ttime (nmaps, nsrc, nrc)."""
+    src = _f64(src); rev = _f64(rev); velv = _f64(velv)
+    srs = np.ascontiguousarray(srs, np.int32)
+    if srs.ndim == 2:
+        srs = srs[None]
+    nmaps = velv.shape[0]
+    nsrc, nrc = src.shape[0], rev.shape[0]
+    if ttime is None:
+        ttime = np.zeros((nmaps, nsrc, nrc))
+    sx, sz = np.ascontiguousarray(src[:, 0]), np.ascontiguousarray(src[:, 1])
+    rx, rz = np.ascontiguousarray(rev[:, 0]), np.ascontiguousarray(rev[:, 1])
+    rc = lib().mct_modrays_batch(nmaps, nsrc, ptr(sx), ptr(sz), nrc, ptr(rx), ptr(rz), srs.shape[0],
+                                 ptr(srs), nvx, nvz, goxd, gozd, dvxd, dvzd, ptr(velv), gdx, gdz, asgr,
+                                 sgdl, sgs, fom, ptr(ttime), None)
+    check("mct_modrays_batch", rc)
+    return ttime

@@ -55,3 +55,64 @@ def layered_columns(rng, ncol, nl_range=(12, 40), h_range=(0.05, 0.5), vs_range=
     vp = (vs * np.float32(1.73)).astype(np.float32)
     rho = (np.float32(1.74) * vp.astype(np.float64) ** 0.25).astype(np.float32)
     return nl, thk, vp, vs, rho
+
+
+def surface_workload(rng, nx=41, ny=41, nz=31, extent=(40.0, 40.0, 6.0), nstations=50, nperiods=20,
+                     pmin=0.5, pmax=5.0):
+    """The batched surface-wave configuration: grid, settings and data dicts
+    for SurfaceLikelihood. Stations at seeded uniform positions, every
+    station pair once (upper triangle: nsta*(nsta-1)/2 paths per period),
+    Rayleigh fundamental-mode phase velocity at log-spaced periods. Observed
+    times are straight-ray times at 1.5 km/s with 2% noise; sigma = 2% of the
+    time (sigdep with n0 = 0.02, n1 = 0)."""
+    grid = dict(nx=nx, ny=ny, nz=nz, xmin=0.0, ymin=0.0, zmin=0.0,
+                dx=extent[0] / (nx - 1), dy=extent[1] / (ny - 1), dz=extent[2] / (nz - 1),
+                scaling=1.0, water_depth=0.0)
+    settings = dict(raylov=1, phase_group=0, dphase=1e-3, gridx=1, gridy=1, sgref=1, sgdic=4, sgext=8,
+                    order=1, sigdep=1, material_law=2, rho_value=2.0, precision=1)
+    margin = 0.05 * np.array(extent[:2])
+    st = margin + (np.array(extent[:2]) - 2 * margin) * rng.random((nstations, 2))
+    periods = np.geomspace(pmin, pmax, nperiods)
+    freqs = 1.0 / periods
+    srs = np.triu(np.ones((nstations, nstations), np.int32), 1).reshape(-1)
+    raystat = np.tile(srs, (nperiods, 1))
+    dist = np.hypot(st[:, None, 0] - st[None, :, 0], st[:, None, 1] - st[None, :, 1]).reshape(-1)
+    tt = dist / 1.5
+    ttime = np.tile(tt, (nperiods, 1)) * (1 + 0.02 * rng.standard_normal((nperiods, tt.size)))
+    data = dict(src=st, rev=st, freqs=freqs, raystat=raystat, ttime=ttime, sigma=None,
+                nrays=int(raystat.sum()))
+    return grid, settings, data
+
+
+def surface_chain_models(rng, nchains, ncell_max, grid, ncell_range=(10, 400), vs_range=(0.3, 2.5)):
+    """One Voronoi model per chain with an uneven cell count, Vs sorted by
+    nucleus depth (so every model passes check_model). Returns ncells,
+    points (nchains, ncell_max, 3), params (nchains, ncell_max, 3)."""
+    lo = np.array([grid["xmin"], grid["ymin"], grid["zmin"]])
+    hi = lo + np.array([grid["dx"] * (grid["nx"] - 1), grid["dy"] * (grid["ny"] - 1), grid["dz"] * (grid["nz"] - 1)])
+    ncells = rng.integers(ncell_range[0], ncell_range[1] + 1, nchains).astype(np.int32)
+    points = np.zeros((nchains, ncell_max, 3))
+    params = np.zeros((nchains, ncell_max, 3))
+    for c in range(nchains):
+        p, q = voronoi_model_3d(rng, int(ncells[c]), lo, hi, vs_range, rho_value=2.0)
+        points[c, :ncells[c]] = p
+        params[c, :ncells[c]] = q
+    return ncells, points, params
+
+
+def perturb_chain_models(rng, ncells, points, params, grid, vs_range=(0.3, 2.5)):
+    """A move proposal per chain: one nucleus is displaced in depth order
+    (keeping Vs sorted by depth), so each proposal changes one Voronoi cell."""
+    lo = np.array([grid["xmin"], grid["ymin"], grid["zmin"]])
+    ext = np.array([grid["dx"] * (grid["nx"] - 1), grid["dy"] * (grid["ny"] - 1), grid["dz"] * (grid["nz"] - 1)])
+    points = points.copy(); params = params.copy()
+    for c in range(len(ncells)):
+        n = int(ncells[c])
+        i = rng.integers(n)
+        newp = np.clip(points[c, i] + rng.normal(0, 0.05, 3) * ext, lo, lo + ext)
+        points[c, i] = newp
+        order = np.argsort(points[c, :n, 2])
+        vs = np.sort(params[c, :n, 1])
+        params[c, order, 1] = vs
+        params[c, :n, 0] = params[c, :n, 1] * np.float64(np.float32(1.73))
+    return points, params

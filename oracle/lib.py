@@ -4,7 +4,7 @@ import os
 import subprocess
 
 HERE = os.path.dirname(os.path.abspath(__file__))
-SOURCES = ["kdgrid.cpp", "surfdisp.cpp", "fm2d.cpp", "sfmm3d.cpp", "likelihood.cpp"]
+SOURCES = ["kdgrid.cpp", "surfdisp.cpp", "fm2d.cpp", "sfmm3d.cpp", "likelihood.cpp", "surf_pipeline.cpp"]
 LIB = os.path.join(HERE, "liboracle.so")
 REF_LIB = os.path.join(HERE, "_ref", "libfmm_ref.so")
 
@@ -22,7 +22,7 @@ def build(force=False):
         mt = os.path.getmtime(LIB)
         if all(os.path.getmtime(s) <= mt for s in srcs + [os.path.join(HERE, "oracle.h")]):
             return LIB
-    cmd = ["g++", "-O2", "-std=c++17", "-ffp-contract=off", "-fno-fast-math",
+    cmd = ["g++", "-O2", "-std=c++17", "-ffp-contract=off", "-fno-fast-math", "-fopenmp",
            "-fPIC", "-shared", "-o", LIB] + srcs
     subprocess.check_call(cmd, cwd=HERE)
     return LIB
@@ -65,6 +65,8 @@ def load():
             "orc_convert_to_layer": (_I, [_P, _P, _P, _I, _D, _D, _D, _P, _P, _P, _P]),
             "orc_surf_misfit": (_I, [_I, _I, _I, _P, _P, _P, _P, _I, _P, _P, _I, _P, _P]),
             "orc_body_misfit": (_I, [_I, _I, _I, _P, _P, _P, _P, _P, _I, _P, _P, _I, _P, _P]),
+            "orc_surf_likelihood": (_I, [_P, _P, _P, _D, _D, _I, _P, _P, _I, _P, _I, _P, _I, _P,
+                                         _P, _P, _P, _I, _P, _P, _P, _P, _P, _P]),
             "orc_vs2vp": (_D, [_D]),
             "orc_vp2rho": (_D, [_D]),
         }

@@ -58,6 +58,12 @@ int orc_body_misfit(int nsrc, int nrev, int np, const double *phase_time,
                     const int *raystat, const double *srdist, int sigdep,
                     const double *n0, const double *n1, int nrays,
                     double *sigma_out, double *out);
+int orc_surf_likelihood(const int *gi, const double *gd, const int *iset, double dphase,
+                        double rho_value, int n, const double *points, const double *params,
+                        int np, const double *freqs, int nsrc, const double *src, int nrev,
+                        const double *rev, const int *raystat, const double *ttime,
+                        const double *sigma, int nrays, const double *n0, const double *n1,
+                        const int *col_mask, double *pvel_io, double *phase_time, double *out);
 double orc_vs2vp(double vs);
 double orc_vp2rho(double vp);
 

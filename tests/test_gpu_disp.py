@@ -70,7 +70,7 @@ def test_fp32_bracketing_gives_the_fp64_roots(gpulib):
     b = surfdisp_batch(nl, thk, vp, vs, rho, per, 2, 0, 0.001, precision=1)
     np.testing.assert_array_equal(a[2], b[2])
     np.testing.assert_array_equal(a[0], b[0])
-    assert b[3][0] < a[3][0] / 3   # most period-equation evaluations moved to FP32
+    assert b[3][0] < a[3][0] * 0.7   # the bracketing scans moved to FP32
 
 
 def test_mmodes_and_single_column_entry_points(orc, gpulib):

@@ -1,0 +1,102 @@
+"""GPU parity: fm2d travel times (modrays) vs the CPU restatement.
+
+The GPU runs the reference's own marching order and heap, and the same
+FP64 operations without FMA, so the travel times are expected to agree to
+the last bit; the stated tolerance is 1e-9 s (far inside the 1e-4 s bound).
+"""
+import ctypes
+
+import numpy as np
+import pytest
+
+from mctomo_gb300 import modrays, modrays_batch
+
+pytestmark = pytest.mark.gpu
+P = lambda a: None if a is None else a.ctypes.data_as(ctypes.c_void_p)  # noqa: E731
+TOL = 1e-9
+
+
+def voronoi_velv(rng, nvx, nvz, dx, dz, ncell, vrange):
+    pts = rng.uniform(0, 1, (ncell, 2)) * [(nvx - 1) * dx, (nvz - 1) * dz]
+    vals = rng.uniform(*vrange, ncell)
+    X, Z = np.meshgrid(np.arange(nvx) * dx, np.arange(nvz) * dz, indexing="ij")
+    d = (X[..., None] - pts[:, 0]) ** 2 + (Z[..., None] - pts[:, 1]) ** 2
+    vel = vals[np.argmin(d, -1)]           # (nvx, nvz)
+    ext = np.zeros((nvx + 2, nvz + 2))
+    ext[1:-1, 1:-1] = vel
+    ext[0] = ext[1]; ext[-1] = ext[-2]; ext[:, 0] = ext[:, 1]; ext[:, -1] = ext[:, -2]
+    return ext
+
+
+def oracle_modrays(orc, src, rev, srs, nvx, nvz, gox, goz, dx, dz, velv, gdx, gdz, asgr, sgdl, sgs, fom):
+    nsrc, nrc = len(src), len(rev)
+    tt = np.zeros((nsrc, nrc))
+    sx, sz = np.ascontiguousarray(src[:, 0]), np.ascontiguousarray(src[:, 1])
+    rx, rz = np.ascontiguousarray(rev[:, 0]), np.ascontiguousarray(rev[:, 1])
+    rc = orc.orc_modrays(nsrc, P(sx), P(sz), nrc, P(rx), P(rz), P(np.ascontiguousarray(srs, np.int32)),
+                         nvx, nvz, gox, goz, dx, dz, P(np.ascontiguousarray(velv)), gdx, gdz, asgr, sgdl,
+                         sgs, fom, 0.5, P(tt), None)
+    assert rc == 0
+    return tt
+
+
+def stations_perimeter(n, L):
+    s = np.linspace(0, 4 * L, n, endpoint=False) + 0.37
+    pts = []
+    for v in s:
+        if v < L: pts.append((v, 0.05))
+        elif v < 2 * L: pts.append((L - 0.05, v - L))
+        elif v < 3 * L: pts.append((3 * L - v, L - 0.05))
+        else: pts.append((0.05, 4 * L - v))
+    return np.array(pts)
+
+
+@pytest.mark.parametrize("asgr,fom,sgdl,sgs", [(1, 1, 5, 10), (1, 0, 4, 8), (0, 1, 4, 8), (0, 0, 4, 8)])
+def test_modrays_2d_config_shape_matches_oracle(orc, gpulib, asgr, fom, sgdl, sgs):
+    # 10 x 10 km, 51 x 51 grid, 16 stations on the perimeter, all pairs
+    rng = np.random.default_rng(asgr * 10 + fom)
+    nvx = nvz = 51
+    dx = dz = 0.2
+    velv = voronoi_velv(rng, nvx, nvz, dx, dz, 20, (2.0, 4.0))
+    st = stations_perimeter(16, 10.0)
+    srs = 1 - np.eye(16, dtype=np.int32)
+    got = modrays(st, st, srs, nvx, nvz, 0.0, 0.0, dx, dz, velv, asgr=asgr, sgdl=sgdl, sgs=sgs, fom=fom)
+    exp = oracle_modrays(orc, st, st, srs, nvx, nvz, 0.0, 0.0, dx, dz, velv.T.copy().T if False else velv,
+                         1, 1, asgr, sgdl, sgs, fom)
+    m = srs == 1
+    assert np.max(np.abs(got[m] - exp[m])) <= TOL
+
+
+def test_modrays_batch_surface_shape_matches_oracle(orc, gpulib):
+    # 41 x 41 phase-velocity maps, 12 stations, upper-triangle paths
+    rng = np.random.default_rng(4)
+    nvx = nvz = 41
+    dx = dz = 1.0
+    nmaps = 6
+    velv = np.stack([voronoi_velv(rng, nvx, nvz, dx, dz, 30, (0.4, 2.2)) for _ in range(nmaps)])
+    st = rng.uniform(1.0, 39.0, (12, 2))
+    srs = np.triu(np.ones((12, 12), np.int32), 1)
+    got = modrays_batch(st, st, srs, nvx, nvz, 0.0, 0.0, dx, dz, velv, sgdl=4, sgs=8)
+    for mp in range(nmaps):
+        exp = oracle_modrays(orc, st, st, srs, nvx, nvz, 0.0, 0.0, dx, dz, velv[mp], 1, 1, 1, 4, 8, 1)
+        m = srs == 1
+        assert np.max(np.abs(got[mp][m] - exp[m])) <= TOL
+
+
+def test_modrays_homogeneous_close_to_straight_line(gpulib):
+    nvx = nvz = 41
+    velv = np.full((nvx + 2, nvz + 2), 3.0)
+    src = np.array([[3.3, 4.1]])
+    rev = np.array([[8.7, 1.2], [1.1, 9.3], [9.6, 9.6]])
+    tt = modrays(src, rev, np.ones((1, 3), np.int32), nvx, nvz, 0.0, 0.0, 0.25, 0.25, velv)
+    exact = np.hypot(rev[:, 0] - 3.3, rev[:, 1] - 4.1) / 3.0
+    assert np.all(np.abs(tt[0] - exact) / exact < 0.01)
+
+
+def test_modrays_source_outside_is_an_error(gpulib):
+    from mctomo_gb300 import MctError
+    velv = np.full((43, 43), 3.0)
+    with pytest.raises(MctError) as ei:
+        modrays(np.array([[50.0, 1.0]]), np.array([[1.0, 1.0]]), np.ones((1, 1), np.int32), 41, 41, 0., 0.,
+                0.25, 0.25, velv)
+    assert ei.value.code == -4
