@@ -1,0 +1,377 @@
+"""Benchmark: batched 3D surface-wave rjMCMC forward evaluations on one GB300.
+
+Workload (the batched surface-wave configuration): 64 chains, grid
+41 x 41 x 31 over 40 x 40 x 6 km, per-chain Voronoi cell counts uniform on
+[10, 400], Vs uniform on [0.3, 2.5] km/s, Vp = 1.73 Vs, density 2.0 g/cc,
+20 Rayleigh fundamental-mode phase-velocity periods log-spaced 0.5-5 s,
+50 stations, 1,225 paths per period, sigma = 2% of the travel time. Every
+step evaluates one move proposal per chain (one Voronoi nucleus displaced),
+then commits it, so each proposal's dispersion work is the columns its cell
+change touches, as in the reference.
+
+value  = proposal evaluations / s with the proposals already resident in HBM
+         (device API, CUDA-event timed).
+e2e    = the same through the host API (mct_surf_forward / mct_surf_commit):
+         pinned host buffers copied in and results copied out every step.
+plain  = one chain per call through the host API (the per-proposal drop-in).
+
+--impl reference times the CPU restatement of the reference's path (oracle/)
+on the host cores on a bounded sample of the same workload.
+"""
+import argparse
+import ctypes
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+NCHAINS = 64
+NCELL_MAX = 400
+SEED = 20261203
+METRIC = "forward evals/s & p99 latency: served batch vs plain, 1 GB300, ttime err<=1e-4"
+CONFIG = {"workload": "batched 3D surface-wave rjMCMC: 64 chains, 41x41x31 grid over 40x40x6 km, "
+                      "10-400 Voronoi cells/chain, 20 Rayleigh phase periods 0.5-5 s, 50 stations, "
+                      "1225 paths/period, move proposals committed each step",
+          "chains": NCHAINS, "grid": [41, 41, 31], "periods": 20, "stations": 50,
+          "paths_per_period": 1225, "dispersion_root_search": "FP32 bracketing + FP64 polish",
+          "fm2d": "reference marching order, FP64", "l2": "flushed (512 MB write) between steps"}
+
+
+def log(*a):
+    print(*a, file=sys.stderr, flush=True)
+
+
+def dist_env():
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    return ws, rank
+
+
+class Clocks:
+    """nvidia-smi sampling of SM clocks and throttle reasons during the timed region."""
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu=0):
+        self.gpu = gpu
+        self.proc = None
+        self.lines = []
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.gpu), "--query-gpu=" + self.FIELDS,
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except OSError:
+            self.proc = None
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def stop(self):
+        if not self.proc:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        sm, smax, reasons, power = [], [], set(), []
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            f = [x.strip() for x in ln.split(",")]
+            if len(f) < 9:
+                continue
+            try:
+                sm.append(float(f[1])); smax.append(float(f[2])); power.append(float(f[3]))
+            except ValueError:
+                continue
+            for nm, v in zip(names, f[5:9]):
+                if v.lower().startswith("active"):
+                    reasons.add(nm)
+        return {"sm_mhz": statistics.median(sm) if sm else None,
+                "sm_max_mhz": max(smax) if smax else None,
+                "power_w_max": max(power) if power else None,
+                "samples": len(sm), "reasons": sorted(reasons)}
+
+
+def make_workload(steps_total):
+    from mctomo_gb300 import synthetic
+    rng = np.random.default_rng(SEED)
+    grid, settings, data = synthetic.surface_workload(rng)
+    ncells, pts, par = synthetic.surface_chain_models(rng, NCHAINS, NCELL_MAX, grid)
+    props = []
+    cur_p, cur_q = pts, par
+    for _ in range(steps_total):
+        cur_p, cur_q = synthetic.perturb_chain_models(rng, ncells, cur_p, cur_q, grid)
+        props.append((cur_p, cur_q))
+    npd = len(data["freqs"])
+    n0 = np.full((NCHAINS, npd), 0.02)
+    n1 = np.zeros((NCHAINS, npd))
+    return grid, settings, data, ncells, (pts, par), props, n0, n1
+
+
+def peaks():
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            return json.load(f)["hbm_gbs"], "measured"
+    except (OSError, KeyError, ValueError):
+        return 6800.0, "fallback"
+
+
+def run_gpu(args):
+    import torch
+    from mctomo_gb300 import SurfaceLikelihood, lib
+    from mctomo_gb300._lib import check
+    ws, rank = dist_env()
+    if ws > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl")
+        torch.cuda.set_device(int(os.environ.get("LOCAL_RANK", "0")))
+    dev = torch.device("cuda")
+    K, W = args.steps, args.warmup
+    grid, settings, data, ncells, init, props, n0, n1 = make_workload(K + W + 1)
+    lk = SurfaceLikelihood(grid, settings, data, nslots=NCHAINS, ncell_max=NCELL_MAX)
+    L = lib()
+    slots = np.arange(NCHAINS, dtype=np.int32)
+    # initial state (every column computed), committed
+    lk.forward(slots, ncells, init[0], init[1], n0, n1)
+    lk.commit(np.ones(NCHAINS, np.int32))
+    # device-resident proposals
+    stream_p = ctypes.c_void_p()
+    check("mct_surf_stream", L.mct_surf_stream(lk.h, ctypes.byref(stream_p)))
+    ext = torch.cuda.ExternalStream(stream_p.value)
+    d_slots = torch.from_numpy(slots).to(dev)
+    d_ncells = torch.from_numpy(ncells).to(dev)
+    d_n0 = torch.from_numpy(n0).to(dev)
+    d_n1 = torch.from_numpy(n1).to(dev)
+    d_acc = torch.ones(NCHAINS, dtype=torch.int32, device=dev)
+    d_out = torch.zeros((NCHAINS, 4), dtype=torch.float64, device=dev)
+    d_pts = [torch.from_numpy(p).to(dev) for p, _ in props]
+    d_par = [torch.from_numpy(q).to(dev) for _, q in props]
+    flush = torch.empty(512 * 1024 * 1024, dtype=torch.uint8, device=dev)
+    torch.cuda.synchronize()
+
+    def dstep(i):
+        rc = L.mct_surf_forward_device(lk.h, NCHAINS, d_slots.data_ptr(), d_ncells.data_ptr(),
+                                       d_pts[i].data_ptr(), d_par[i].data_ptr(), d_n0.data_ptr(),
+                                       d_n1.data_ptr(), d_out.data_ptr(), None)
+        check("mct_surf_forward_device", rc)
+        check("mct_surf_commit_device", L.mct_surf_commit_device(lk.h, d_acc.data_ptr(), None))
+
+    for i in range(W):
+        dstep(i)
+    torch.cuda.synchronize()
+    if ws > 1:
+        torch.distributed.barrier()
+    check("mct_surf_profile_start", L.mct_surf_profile_start(lk.h, K))
+    clocks = Clocks(int(os.environ.get("LOCAL_RANK", "0")))
+    clocks.start()
+    step_ms = []
+    with torch.cuda.stream(ext):
+        for i in range(W, W + K):
+            flush.fill_(i & 0xff)
+            e0 = torch.cuda.Event(enable_timing=True); e1 = torch.cuda.Event(enable_timing=True)
+            e0.record(ext)
+            dstep(i)
+            e1.record(ext)
+            step_ms.append((e0, e1))
+    torch.cuda.synchronize()
+    cl = clocks.stop()
+    times = [a.elapsed_time(b) for a, b in step_ms]
+    total_ms = sum(times)
+    stage = (ctypes.c_double * 4)()
+    nsteps = ctypes.c_int()
+    launches = ctypes.c_longlong()
+    check("mct_surf_profile_read", L.mct_surf_profile_read(lk.h, stage, ctypes.byref(nsteps), ctypes.byref(launches)))
+    check("mct_surf_profile_start", L.mct_surf_profile_start(lk.h, 0))
+    out = d_out.cpu().numpy()
+    if ws > 1:
+        t = torch.tensor([total_ms], device=dev)
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        total_ms = float(t.item())
+    value = NCHAINS * K * ws / (total_ms / 1e3)
+
+    # end to end through the host API, pinned host buffers
+    pin = lambda a: torch.from_numpy(np.ascontiguousarray(a)).pin_memory().numpy()  # noqa: E731
+    hp = [(pin(p), pin(q)) for p, q in props]
+    e2e_ms = []
+    lk.forward(slots, ncells, hp[0][0], hp[0][1], n0, n1)
+    lk.commit(np.ones(NCHAINS, np.int32))
+    for i in range(W, W + K):
+        flush.fill_(i & 0xff)
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        o = lk.forward(slots, ncells, hp[i][0], hp[i][1], n0, n1)
+        lk.commit(np.ones(NCHAINS, np.int32))
+        e2e_ms.append((time.perf_counter() - t0) * 1e3)
+    e2e_value = NCHAINS * len(e2e_ms) * ws / (sum(e2e_ms) / 1e3)
+    h2d = NCHAINS * NCELL_MAX * 3 * 8 * 2 + NCHAINS * (4 + 4) + 2 * NCHAINS * n0.shape[1] * 8 + NCHAINS * 4
+    d2h = NCHAINS * 4 * 8
+
+    # plain drop-in: one chain per call
+    plain_ms = []
+    nplain = min(64, NCHAINS)
+    for c in range(nplain):
+        t0 = time.perf_counter()
+        lk.forward(slots[c:c + 1], ncells[c:c + 1], hp[W + K][0][c:c + 1], hp[W + K][1][c:c + 1],
+                   n0[c:c + 1], n1[c:c + 1])
+        lk.commit(np.ones(1, np.int32))
+        plain_ms.append((time.perf_counter() - t0) * 1e3)
+    plain_value = len(plain_ms) / (sum(plain_ms) / 1e3)
+
+    # roofline of the dominant stage (fm2d travel times): algorithmic bytes =
+    # for every (chain, period, source) solve, each node of the 41x41 grid read
+    # (velocity) and written (travel time) once in FP64 = 16 B/node/solve
+    stage_ms = [stage[k] / max(nsteps.value, 1) for k in range(4)]
+    names = ["gridding", "layering+dispersion", "fm2d travel times", "misfit"]
+    dom = int(np.argmax(stage_ms))
+    nsolve = NCHAINS * sum(1 for p in range(20) for s in range(50)
+                           if (np.asarray(data["raystat"][p]).reshape(50, 50)[s].any() or s == 0))
+    alg_bytes = {2: nsolve * 41 * 41 * 16.0,
+                 0: NCHAINS * (41 * 41 * 31 * (4 + 24)) + NCHAINS * 400 * 48.0,
+                 1: 0.0, 3: NCHAINS * 20 * 1225 * 24.0}[dom]
+    peak, peak_kind = peaks()
+    achieved = alg_bytes / (stage_ms[dom] / 1e3) / 1e9 if alg_bytes else 0.0
+    line = {
+        "metric": METRIC, "value": round(value, 3), "unit": "proposal evals/s", "n_gpus": ws,
+        "steps": K, "warmup": W, "ms_per_step": round(total_ms / K, 4), "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f64 (fm2d, dispersion polish), f32 (dispersion bracketing)",
+        "data": "synthetic (seeded, shapes of the configuration)", "config": CONFIG,
+        "e2e": {"value": round(e2e_value, 3), "unit": "proposal evals/s", "h2d_bytes_per_step": h2d,
+                "d2h_bytes_per_step": d2h},
+        "plain": {"value": round(plain_value, 3), "unit": "proposal evals/s", "p50_ms": round(float(np.percentile(plain_ms, 50)), 3),
+                  "p99_ms": round(float(np.percentile(plain_ms, 99)), 3)},
+        "batched_latency_ms": {"p50": round(float(np.percentile(times, 50)), 3),
+                               "p99": round(float(np.percentile(times, 99)), 3)},
+        "stage_ms_per_step": {n: round(v, 4) for n, v in zip(names, stage_ms)},
+        "roofline": {"kernel": names[dom], "bound": "hbm", "achieved": round(achieved, 3), "peak": peak,
+                     "peak_kind": peak_kind, "unit": "GB/s", "frac": round(achieved / peak, 6),
+                     "traffic": None},
+        "gpu_launches": int(launches.value),
+        "clocks": cl,
+        "valid_models": int((out[:, 3] == 0).sum()),
+    }
+    if rank == 0 and not args.no_cpu:
+        line["cpu_baseline"] = cpu_baseline(grid, settings, data, ncells, init, props, n0, n1, args)
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+    lk.close()
+    if ws > 1:
+        torch.distributed.destroy_process_group()
+
+
+def cpu_sample(grid, settings, data, ncells, init, props, n0, n1, nprop, threads):
+    """Times the oracle's restatement of the reference path on nprop proposals
+    (one chain each), each against its chain's committed state: only the
+    columns whose model changed get new dispersion curves, as the reference's
+    CGAL box arranges. The timed call includes the chain's kd-tree gridding."""
+    os.environ["OMP_NUM_THREADS"] = str(threads)
+    import oracle
+    orc = oracle.load()
+    P = lambda a: None if a is None else a.ctypes.data_as(ctypes.c_void_p)  # noqa: E731
+    f = lambda a, t=np.float64: np.ascontiguousarray(a, t)  # noqa: E731
+    gi = np.array([grid["nx"], grid["ny"], grid["nz"]], np.int32)
+    gd = np.array([grid[k] for k in ("xmin", "ymin", "zmin", "dx", "dy", "dz", "scaling", "water_depth")])
+    iset = np.array([settings[k] for k in ("raylov", "gridx", "gridy", "sgref", "sgdic", "sgext", "order",
+                                           "sigdep", "material_law")], np.int32)
+    npd = len(data["freqs"])
+    nsta = len(data["src"])
+    freqs, src, raystat, ttime = f(data["freqs"]), f(data["src"]), f(data["raystat"], np.int32), f(data["ttime"])
+    shape = (grid["nx"], grid["ny"], grid["nz"])
+
+    def vs_grid(p, q, n):
+        sid = np.zeros(shape, np.int32)
+        a, b, c = np.zeros(shape), np.zeros(shape), np.zeros(shape)
+        orc.orc_kdtree_to_grid(3, n, P(f(p[:n])), P(f(q[:n])), *shape, grid["xmin"], grid["ymin"], grid["zmin"],
+                               grid["dx"], grid["dy"], grid["dz"], 1, shape[0], 1, shape[1], 1, shape[2],
+                               P(sid), P(a), P(b), P(c))
+        return b
+
+    def like(p, q, n, c, mask, pv):
+        out = np.zeros(4)
+        orc.orc_surf_likelihood(P(gi), P(gd), P(iset), settings["dphase"], settings["rho_value"], n,
+                                P(f(p[:n])), P(f(q[:n])), npd, P(freqs), nsta, P(src), nsta, P(src), P(raystat),
+                                P(ttime), None, data["nrays"], P(f(n0[c])), P(f(n1[c])), P(mask), P(pv), None, P(out))
+        return out
+
+    t_total = 0.0
+    for k in range(nprop):
+        c = k % len(ncells)
+        n = int(ncells[c])
+        pv = np.zeros((npd, grid["nx"], grid["ny"]))
+        like(init[0][c], init[1][c], n, c, None, pv)          # committed state (untimed)
+        p1, q1 = props[0][0][c], props[0][1][c]
+        mask = f((vs_grid(init[0][c], init[1][c], n) != vs_grid(p1, q1, n)).any(axis=2).reshape(-1), np.int32)
+        t0 = time.perf_counter()
+        like(p1, q1, n, c, mask, pv)
+        t_total += time.perf_counter() - t0
+    return nprop / t_total
+
+
+def cpu_baseline(grid, settings, data, ncells, init, props, n0, n1, args):
+    threads = os.cpu_count() or 1
+    nprop = args.cpu_sample
+    v = cpu_sample(grid, settings, data, ncells, init, props, n0, n1, nprop, threads)
+    return {"value": round(v, 4), "unit": "proposal evals/s", "cores": threads, "kind": "port",
+            "sample": "%d move proposals of the same workload (one chain each, changed columns only), "
+                      "C++ restatement of the reference's Fortran path with OpenMP over columns and periods"
+                      % nprop}
+
+
+def run_reference(args):
+    ws, rank = dist_env()
+    if rank != 0:
+        return
+    grid, settings, data, ncells, init, props, n0, n1 = make_workload(2)
+    threads = os.cpu_count() or 1
+    vals = []
+    for _ in range(args.warmup):
+        cpu_sample(grid, settings, data, ncells, init, props, n0, n1, 1, threads)
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        vals.append(cpu_sample(grid, settings, data, ncells, init, props, n0, n1, args.cpu_sample, threads))
+    dt = time.perf_counter() - t0
+    value = statistics.mean(vals)
+    line = {"impl": "reference", "metric": METRIC, "value": round(value, 4), "unit": "proposal evals/s",
+            "n_gpus": ws, "steps": args.steps, "warmup": args.warmup,
+            "ms_per_step": round(dt / args.steps * 1e3, 3), "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded, shapes of the configuration)",
+            "config": CONFIG,
+            "cpu_baseline": {"value": round(value, 4), "unit": "proposal evals/s", "cores": threads, "kind": "port",
+                             "sample": "%d move proposals per step, C++ restatement of the reference path"
+                                       % args.cpu_sample},
+            "e2e": {"value": round(value, 4), "unit": "proposal evals/s", "h2d_bytes_per_step": 0,
+                    "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--cpu-sample", type=int, default=8)
+    ap.add_argument("--no-cpu", action="store_true")
+    args = ap.parse_args()
+    if args.impl == "reference":
+        run_reference(args)
+    else:
+        run_gpu(args)
+
+
+if __name__ == "__main__":
+    main()

@@ -134,14 +134,16 @@ int mct_modrays(int nsrc, const double *scx, const double *scz, int nrc,
 /* Many velocity maps (e.g. every period of every chain) sharing the
  * stations: velv [nmaps][(nvx+2)*(nvz+2)], srs [srs_nmaps][nsrc][nrc] path
  * flags (map m uses set m % srs_nmaps), ttime [nmaps][nsrc][nrc], tfield
- * optional [nmaps][nsrc][nnx*nnz]. */
+ * optional [nmaps][nsrc][nnx*nnz]. precision 0 evaluates the upwind updates
+ * in FP64 as the reference; 1 solves each update's quadratic in FP32 on
+ * times shifted to a neighbouring accepted time (times stay FP64). */
 int mct_modrays_batch(int nmaps, int nsrc, const double *scx,
                       const double *scz, int nrc, const double *rcx,
                       const double *rcz, int srs_nmaps, const int *srs,
                       int nvx, int nvz, double goxd, double gozd, double dvxd,
                       double dvzd, const double *velv, int gdx, int gdz,
                       int asgr, int sgdl, int sgs, int fom, double *ttime,
-                      double *tfield);
+                      double *tfield, int precision);
 
 
 /* ------------------------------------------------------------------------
@@ -168,6 +170,7 @@ typedef struct {
   int material_law;    /* MCT_LAW_* */
   double rho_value;
   int precision;       /* dispersion root search: 0 FP64, 1 FP32 bracketing */
+  int tt_precision;    /* fm2d upwind updates: 0 FP64, 1 FP32 quadratic */
 } mct_surf_settings;
 
 typedef struct {
@@ -213,6 +216,13 @@ int mct_surf_commit_device(mct_surf_ctx *ctx, const int *accept,
  * maps (np, nx, ny) for batch position index; either pointer may be NULL. */
 int mct_surf_phase_time(mct_surf_ctx *ctx, int index, double *phase_time,
                         double *phase_vel);
+/* Stage timing of the next max_steps forwards (CUDA events, no host
+ * synchronisation in the forward), and its read-back: stage_ms[4] = summed
+ * milliseconds of gridding, layering + dispersion, fm2d, misfit; launches =
+ * kernels launched by forwards and commits since the start. */
+int mct_surf_profile_start(mct_surf_ctx *ctx, int max_steps);
+int mct_surf_profile_read(mct_surf_ctx *ctx, double *stage_ms, int *steps,
+                          long long *launches);
 /* The context's CUDA stream. */
 int mct_surf_stream(mct_surf_ctx *ctx, void **stream);
 

@@ -34,7 +34,7 @@ SIGNATURES = {
     "mct_surfdisp_batch": (I, [I, I, P, P, P, P, P, I, P, I, I, I, D, I, I, P, P, P, P]),
     "mct_surfdisp_batch_device": (I, [I, I, P, P, P, P, P, I, P, I, I, I, D, I, I, P, P, P, P, P]),
     "mct_modrays": (I, [I, P, P, I, P, P, P, I, I, I, D, D, D, D, P, I, I, I, I, I, D, I, D, P, I, P, P]),
-    "mct_modrays_batch": (I, [I, I, P, P, I, P, P, I, P, I, I, D, D, D, D, P, I, I, I, I, I, I, P, P]),
+    "mct_modrays_batch": (I, [I, I, P, P, I, P, P, I, P, I, I, D, D, D, D, P, I, I, I, I, I, I, P, P, I]),
     "mct_surf_create": (I, [P, P, P, I, I, P]),
     "mct_surf_destroy": (I, [P]),
     "mct_surf_forward": (I, [P, I, P, P, P, P, P, P, P]),
@@ -43,6 +43,8 @@ SIGNATURES = {
     "mct_surf_commit_device": (I, [P, P, P]),
     "mct_surf_phase_time": (I, [P, I, P, P]),
     "mct_surf_stream": (I, [P, P]),
+    "mct_surf_profile_start": (I, [P, I]),
+    "mct_surf_profile_read": (I, [P, P, P, P]),
 }
 
 

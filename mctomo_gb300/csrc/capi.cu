@@ -22,6 +22,9 @@ namespace {
 std::mutex g_mu;
 cudaStream_t g_stream = nullptr;
 DevBuf g_ws;
+int g_trace_solve = -1;
+std::vector<int> g_trace_i;
+std::vector<double> g_trace_t;
 
 int ensure_stream() {
   if (!g_stream) MCT_CUDA_TRY(cudaStreamCreateWithFlags(&g_stream, cudaStreamNonBlocking));
@@ -305,7 +308,7 @@ int mct_modrays_batch(int nmaps, int nsrc, const double *scx, const double *scz,
                       const double *rcx, const double *rcz, int srs_nmaps, const int *srs, int nvx,
                       int nvz, double goxd, double gozd, double dvxd, double dvzd,
                       const double *velv, int gdx, int gdz, int asgr, int sgdl, int sgs, int fom,
-                      double *ttime, double *tfield) {
+                      double *ttime, double *tfield, int precision) {
   if (nmaps < 1 || nsrc < 1 || nrc < 1 || nvx < 2 || nvz < 2 || gdx < 1 || gdz < 1 ||
       srs_nmaps < 1 || (asgr == 1 && (sgdl < 1 || sgs < 1)) || (fom != 0 && fom != 1) ||
       !(dvxd > 0) || !(dvzd > 0))
@@ -369,7 +372,23 @@ int mct_modrays_batch(int nmaps, int nsrc, const double *scx, const double *scz,
   job.srs = d_srs; job.nsolve = (int)ns; job.solves = d_solves;
   job.ttime = d_tt; job.tfield = d_tf; job.status = d_status;
   job.nodes_max = plan.nodes_max; job.nref_max = plan.nref_max; job.map_tmp_max = plan.map_tmp_max;
+  job.precision = precision ? 1 : 0;
+  int *d_ti = nullptr; double *d_trt = nullptr;
+  if (g_trace_solve >= 0) {
+    job.trace_solve = g_trace_solve; job.trace_max = 20000;
+    MCT_CUDA_TRY(cudaMalloc(&d_ti, sizeof(int) * 3 * job.trace_max));
+    MCT_CUDA_TRY(cudaMalloc(&d_trt, sizeof(double) * job.trace_max));
+    MCT_CUDA_TRY(cudaMemset(d_ti, 0xff, sizeof(int) * 3 * job.trace_max));
+    job.trace_i = d_ti; job.trace_t = d_trt;
+  }
   rc = launch_fm2d(job, plan, s); if (rc) return rc;
+  if (d_ti) {
+    MCT_CUDA_TRY(cudaStreamSynchronize(s));
+    g_trace_i.resize(3 * job.trace_max); g_trace_t.resize(job.trace_max);
+    MCT_CUDA_TRY(cudaMemcpy(g_trace_i.data(), d_ti, sizeof(int) * 3 * job.trace_max, cudaMemcpyDeviceToHost));
+    MCT_CUDA_TRY(cudaMemcpy(g_trace_t.data(), d_trt, sizeof(double) * job.trace_max, cudaMemcpyDeviceToHost));
+    cudaFree(d_ti); cudaFree(d_trt);
+  }
   MCT_CUDA_TRY(cudaMemcpyAsync(ttime, d_tt, sizeof(double) * (size_t)nmaps * nsrc * nrc, cudaMemcpyDeviceToHost, s));
   if (tfield)
     MCT_CUDA_TRY(cudaMemcpyAsync(tfield, d_tf, sizeof(double) * (size_t)nmaps * nsrc * nnx * nnz, cudaMemcpyDeviceToHost, s));
@@ -387,8 +406,19 @@ int mct_modrays(int nsrc, const double *scx, const double *scz, int nrc, const d
   if (uar == 0) { g_last_error = "ray paths (uar=0, group velocity) are not supported"; return MCT_ERR_UNSUPPORTED; }
   if (crazyray) *crazyray = 0;
   return mct_modrays_batch(1, nsrc, scx, scz, nrc, rcx, rcz, 1, srsin, nvx, nvz, goxd, gozd, dvxd,
-                           dvzd, velvin, gdx, gdz, asgr, sgdl, sgs, fom, ttime, tfield);
+                           dvzd, velvin, gdx, gdz, asgr, sgdl, sgs, fom, ttime, tfield, 0);
 }
+
+
+// Diagnostics (not part of the public header): record the marching order of
+// one solve of the next mct_modrays_batch call.
+int mct_debug_fm2d_trace(int solve, int *idx_out, double *t_out, int max) {
+  if (solve >= -1 && idx_out == nullptr) { g_trace_solve = solve; return MCT_OK; }
+  int n = std::min<int>(max, (int)g_trace_t.size());
+  for (int i = 0; i < n; ++i) { idx_out[3 * i] = g_trace_i[3 * i]; idx_out[3 * i + 1] = g_trace_i[3 * i + 1]; idx_out[3 * i + 2] = g_trace_i[3 * i + 2]; t_out[i] = g_trace_t[i]; }
+  return n;
+}
+
 
 }  // extern "C"
 

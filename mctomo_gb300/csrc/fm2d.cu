@@ -36,6 +36,12 @@ struct WarpState {
 
 __device__ __forceinline__ int lin(const Grid2 &g, int iz, int ix) { return (iz - 1) + g.ld * (ix - 1); }
 
+// Travel times are finite and non-negative, so their IEEE bit patterns order
+// exactly like the values: the heap compares them on the integer pipe.
+__device__ __forceinline__ long long tkey(const double *T, int node) {
+  return __double_as_longlong(T[node]);
+}
+
 // ---- binary heap (fm2d_ttime.f90:527-680), lane 0 only --------------------
 __device__ void addtree(WarpState &w, const Grid2 &g, int iz, int ix) {
   w.ntr = w.ntr + 1;
@@ -43,10 +49,10 @@ __device__ void addtree(WarpState &w, const Grid2 &g, int iz, int ix) {
   w.S[me] = (short)w.ntr;
   w.H[w.ntr] = (unsigned short)me;
   int tpc = w.ntr, tpp = tpc / 2;
-  double tme = w.T[me];
+  long long tme = tkey(w.T, me);
   while (tpp > 0) {
     int pn = w.H[tpp];
-    if (tme < w.T[pn]) {
+    if (tme < tkey(w.T, pn)) {
       w.S[me] = (short)tpp;
       w.S[pn] = (short)tpc;
       w.H[tpc] = (unsigned short)pn;
@@ -67,11 +73,11 @@ __device__ void downtree(WarpState &w) {
   int tpp = 1, tpc = 2 * tpp;
   const int ntr = w.ntr;
   while (tpc < ntr) {
-    double rd1 = w.T[w.H[tpc]];
-    double rd2 = w.T[w.H[tpc + 1]];
+    long long rd1 = tkey(w.T, w.H[tpc]);
+    long long rd2 = tkey(w.T, w.H[tpc + 1]);
     if (rd1 > rd2) tpc = tpc + 1;
     int cn = w.H[tpc], pn = w.H[tpp];
-    if (w.T[cn] < w.T[pn]) {
+    if (tkey(w.T, cn) < tkey(w.T, pn)) {
       w.S[pn] = (short)tpc;
       w.S[cn] = (short)tpp;
       w.H[tpc] = (unsigned short)pn;
@@ -83,7 +89,7 @@ __device__ void downtree(WarpState &w) {
   }
   if (tpc == ntr) {
     int cn = w.H[tpc], pn = w.H[tpp];
-    if (w.T[cn] < w.T[pn]) {
+    if (tkey(w.T, cn) < tkey(w.T, pn)) {
       w.S[pn] = (short)tpc;
       w.S[cn] = (short)tpp;
       w.H[tpc] = (unsigned short)pn;
@@ -95,10 +101,10 @@ __device__ void downtree(WarpState &w) {
 __device__ void updtree(WarpState &w, const Grid2 &g, int iz, int ix) {
   int me = lin(g, iz, ix);
   int tpc = w.S[me], tpp = tpc / 2;
-  double tme = w.T[me];
+  long long tme = tkey(w.T, me);
   while (tpp > 0) {
     int pn = w.H[tpp];
-    if (tme < w.T[pn]) {
+    if (tme < tkey(w.T, pn)) {
       w.S[me] = (short)tpp;
       w.S[pn] = (short)tpc;
       w.H[tpc] = (unsigned short)pn;
@@ -256,6 +262,151 @@ __device__ double fouds2(const WarpState &w, const Grid2 &g, const double *V, in
   return travm;
 }
 
+
+// Mixed-precision variants (precision == 1): the same stencils and case
+// selection, with the quadratic solved in FP32 on travel times shifted by a
+// nearby accepted time `base` (one FP64 subtraction per neighbour and one
+// FP64 addition for the result). Every stencil is shift-invariant: em is a
+// difference and tref's coefficients sum to tdiv, so
+// trav = base + (tref' + tdsh) / tdiv with tref' the shifted tref.
+__device__ __forceinline__ float quad_rootf(float a, float b, float c) {
+  float rd1 = b * b - 4.0f * a * c;
+  if (rd1 < 0.0f) rd1 = 0.0f;
+  return (-b + sqrtf(rd1)) / (2.0f * a);
+}
+
+__device__ double fouds1_mixed(const WarpState &w, const Grid2 &g, const double *V, int iz, int ix) {
+  int tsw1 = 0;
+  float travm = 0.f;
+  const float slown = (float)(1.0 / V[lin(g, iz, ix)]);
+  const float dnx = (float)g.dnx, dnz = (float)g.dnz;
+  double base = -1.0;
+  for (int j = ix - 1; j <= ix + 1; j += 2)
+    for (int k = iz - 1; k <= iz + 1; k += 2) {
+      if (!(j >= 1 && j <= g.nnx && k >= 1 && k <= g.nnz)) continue;
+      const bool ja = w.S[lin(g, iz, j)] == 0, ka = w.S[lin(g, k, ix)] == 0;
+      if (!ja && !ka) continue;
+      if (base < 0) base = ja ? w.T[lin(g, iz, j)] : w.T[lin(g, k, ix)];
+      float a, b, c, tref;
+      if (ja) {
+        float tj = (float)(w.T[lin(g, iz, j)] - base);
+        if (ka) {
+          float tk = (float)(w.T[lin(g, k, ix)] - base);
+          float em = tk - tj;
+          a = dnx * dnx + dnz * dnz;
+          b = -(2.0f * (dnx * dnx) * em);
+          c = (dnx * dnx) * (em * em - (dnz * dnz) * (slown * slown));
+        } else {
+          a = 1.f; b = 0.f; c = -((slown * slown) * (dnx * dnx));
+        }
+        tref = tj;
+      } else {
+        a = 1.f; b = 0.f;
+        float sd = slown * dnz;
+        c = -(sd * sd);
+        tref = (float)(w.T[lin(g, k, ix)] - base);
+      }
+      float trav = tref + quad_rootf(a, b, c);
+      if (tsw1 == 1) travm = fminf(trav, travm);
+      else { travm = trav; tsw1 = 1; }
+    }
+  return base + (double)travm;
+}
+
+__device__ double fouds2_mixed(const WarpState &w, const Grid2 &g, const double *V, int iz, int ix) {
+  int tsw1 = 0;
+  float travm = 0.f;
+  const float slown = (float)(1.0 / V[lin(g, iz, ix)]);
+  const float dnx = (float)g.dnx, dnz = (float)g.dnz;
+  double base = -1.0;
+  for (int j = ix - 1; j <= ix + 1; j += 2) {
+    if (!(j >= 1 && j <= g.nnx)) continue;
+    int swj = -1, j2;
+    if (j == ix - 1) { j2 = j - 1; if (j2 >= 1) { if (w.S[lin(g, iz, j2)] == 0) swj = 0; } }
+    else { j2 = j + 1; if (j2 <= g.nnx) { if (w.S[lin(g, iz, j2)] == 0) swj = 0; } }
+    const bool jalive = w.S[lin(g, iz, j)] == 0;
+    if (jalive && swj == 0) { swj = -1; if (tkey(w.T, lin(g, iz, j)) > tkey(w.T, lin(g, iz, j2))) swj = 0; }
+    else swj = -1;
+    if (jalive && base < 0) base = w.T[lin(g, iz, j)];
+    for (int k = iz - 1; k <= iz + 1; k += 2) {
+      if (!(k >= 1 && k <= g.nnz)) continue;
+      int swk = -1, k2;
+      if (k == iz - 1) { k2 = k - 1; if (k2 >= 1) { if (w.S[lin(g, k2, ix)] == 0) swk = 0; } }
+      else { k2 = k + 1; if (k2 <= g.nnz) { if (w.S[lin(g, k2, ix)] == 0) swk = 0; } }
+      const bool kalive = w.S[lin(g, k, ix)] == 0;
+      if (kalive && swk == 0) { swk = -1; if (tkey(w.T, lin(g, k, ix)) > tkey(w.T, lin(g, k2, ix))) swk = 0; }
+      else swk = -1;
+      if (!jalive && !kalive) continue;
+      if (base < 0) base = w.T[lin(g, k, ix)];
+      auto sh = [&](int node) { return (float)(w.T[node] - base); };
+      int swsol = 0;
+      float a = 0, b = 0, c = 0, tref = 0, tdiv = 1.f;
+      if (swj == 0) {
+        swsol = 1;
+        float tj = sh(lin(g, iz, j)), tj2 = sh(lin(g, iz, j2));
+        if (swk == 0) {
+          float u = 2.f * dnx, v = 2.f * dnz;
+          float tk = sh(lin(g, k, ix)), tk2 = sh(lin(g, k2, ix));
+          float em = 4.f * tj - tj2 - 4.f * tk;
+          em = em + tk2;
+          a = v * v + u * u; b = 2.f * em * (u * u);
+          c = (u * u) * (em * em - (slown * slown) * (v * v));
+          tref = 4.f * tj - tj2; tdiv = 3.f;
+        } else if (kalive) {
+          float u = dnz, v = 2.f * dnx;
+          float tk = sh(lin(g, k, ix));
+          float em = 3.f * tk - 4.f * tj + tj2;
+          a = v * v + 9.f * (u * u); b = 6.f * em * (u * u);
+          c = (u * u) * (em * em - (slown * slown) * (v * v));
+          tref = tk; tdiv = 1.f;
+        } else {
+          float u = 2.f * dnx;
+          a = 1.f; b = 0.f; c = -((u * u) * (slown * slown));
+          tref = 4.f * tj - tj2; tdiv = 3.f;
+        }
+      } else if (jalive) {
+        swsol = 1;
+        float tj = sh(lin(g, iz, j));
+        if (swk == 0) {
+          float u = dnx, v = 2.f * dnz;
+          float tk = sh(lin(g, k, ix)), tk2 = sh(lin(g, k2, ix));
+          float em = 3.f * tj - 4.f * tk + tk2;
+          a = v * v + 9.f * (u * u); b = 6.f * em * (u * u);
+          c = (u * u) * (em * em - (v * v) * (slown * slown));
+          tref = tj; tdiv = 1.f;
+        } else if (kalive) {
+          float tk = sh(lin(g, k, ix));
+          float em = tk - tj;
+          a = dnx * dnx + dnz * dnz; b = -(2.f * (dnx * dnx) * em);
+          c = (dnx * dnx) * (em * em - (dnz * dnz) * (slown * slown));
+          tref = tj; tdiv = 1.f;
+        } else {
+          a = 1.f; b = 0.f; c = -((slown * slown) * (dnx * dnx));
+          tref = tj; tdiv = 1.f;
+        }
+      } else {
+        if (swk == 0) {
+          swsol = 1;
+          float u = 2.f * dnz;
+          float tk = sh(lin(g, k, ix)), tk2 = sh(lin(g, k2, ix));
+          a = 1.f; b = 0.f; c = -((u * u) * (slown * slown));
+          tref = 4.f * tk - tk2; tdiv = 3.f;
+        } else if (kalive) {
+          swsol = 1;
+          a = 1.f; b = 0.f; c = -((slown * slown) * (dnz * dnz));
+          tref = sh(lin(g, k, ix)); tdiv = 1.f;
+        }
+      }
+      if (swsol == 1) {
+        float trav = (tref + quad_rootf(a, b, c)) / tdiv;
+        if (tsw1 == 1) travm = fminf(trav, travm);
+        else { travm = trav; tsw1 = 1; }
+      }
+    }
+  }
+  return base + (double)travm;
+}
+
 // fm2d_ttime.f90:682-711 bilinear
 __device__ __forceinline__ double bilinear(const double nv[2][2], double dsx, double dsz, double dnx, double dnz) {
   double biv = 0.0;
@@ -272,8 +423,10 @@ __device__ __forceinline__ double bilinear(const double nv[2][2], double dsx, do
 // urg == 1 adds the refined-box exit test; vnr/vnb are compared with the
 // current (refined) grid size exactly as the reference's module variables
 // are at that point.
-__device__ void march(WarpState &w, const Grid2 &g, const double *V, int fom, int urg, int vnl,
-                      int vnr, int vnt, int vnb) {
+struct Trace { int *ti; double *tt; int max; int n; };
+
+__device__ void march(WarpState &w, const Grid2 &g, const double *V, int fom, int prec, int urg, int vnl,
+                      int vnr, int vnt, int vnb, Trace *tr = nullptr) {
   const int lane = threadIdx.x & 31;
   for (;;) {
     int ix = 0, iz = 0, go = 0;
@@ -291,6 +444,10 @@ __device__ void march(WarpState &w, const Grid2 &g, const double *V, int fom, in
           if (swrg) { w.S[lin(g, iz, ix)] = 0; go = 0; }
         }
         if (go) {
+          if (tr && tr->n < tr->max) {
+            tr->ti[3 * tr->n] = urg; tr->ti[3 * tr->n + 1] = lin(g, iz, ix); tr->ti[3 * tr->n + 2] = w.ntr;
+            tr->tt[tr->n] = w.T[lin(g, iz, ix)]; tr->n++;
+          }
           w.S[lin(g, iz, ix)] = 0;
           downtree(w);
         }
@@ -310,23 +467,37 @@ __device__ void march(WarpState &w, const Grid2 &g, const double *V, int fom, in
       else if (lane == 2) { nz_ = iz - 1; valid = nz_ >= 1; }
       else { nz_ = iz + 1; valid = nz_ <= g.nnz; }
     }
+    // New times are computed in registers (each reads only accepted nodes),
+    // then written and sifted one neighbour at a time in the reference's
+    // order: a sift compares against the other close nodes' current times, so
+    // the writes must not run ahead of the sifts.
     int st = 0;
+    double tnew = 0.0;
     if (valid) {
       st = w.S[lin(g, nz_, nx_)];
       if (st != 0) {
-        double t = fom == 0 ? fouds1(w, g, V, nz_, nx_) : fouds2(w, g, V, nz_, nx_);
-        w.T[lin(g, nz_, nx_)] = t;
+        if (prec == 0) tnew = fom == 0 ? fouds1(w, g, V, nz_, nx_) : fouds2(w, g, V, nz_, nx_);
+        else tnew = fom == 0 ? fouds1_mixed(w, g, V, nz_, nx_) : fouds2_mixed(w, g, V, nz_, nx_);
       }
     }
     int code = valid ? (st == -1 ? 1 : (st > 0 ? 2 : 0)) : 0;
-    int c0 = __shfl_sync(0xffffffffu, code, 0), c1 = __shfl_sync(0xffffffffu, code, 1);
-    int c2 = __shfl_sync(0xffffffffu, code, 2), c3 = __shfl_sync(0xffffffffu, code, 3);
+    int cd[4];
+    double tn[4];
+#pragma unroll
+    for (int q = 0; q < 4; ++q) {
+      cd[q] = __shfl_sync(0xffffffffu, code, q);
+      tn[q] = __shfl_sync(0xffffffffu, tnew, q);
+    }
     __syncwarp();
     if (lane == 0) {
-      if (c0 == 1) addtree(w, g, iz, ix - 1); else if (c0 == 2) updtree(w, g, iz, ix - 1);
-      if (c1 == 1) addtree(w, g, iz, ix + 1); else if (c1 == 2) updtree(w, g, iz, ix + 1);
-      if (c2 == 1) addtree(w, g, iz - 1, ix); else if (c2 == 2) updtree(w, g, iz - 1, ix);
-      if (c3 == 1) addtree(w, g, iz + 1, ix); else if (c3 == 2) updtree(w, g, iz + 1, ix);
+      const int qz[4] = {iz, iz, iz - 1, iz + 1}, qx[4] = {ix - 1, ix + 1, ix, ix};
+#pragma unroll
+      for (int q = 0; q < 4; ++q) {
+        if (cd[q] == 0) continue;
+        w.T[lin(g, qz[q], qx[q])] = tn[q];
+        if (cd[q] == 1) addtree(w, g, qz[q], qx[q]);
+        else updtree(w, g, qz[q], qx[q]);
+      }
     }
     __syncwarp();
   }
@@ -412,6 +583,8 @@ fm2d_solve_kernel(Fm2dJob job, int warp_bytes) {
   Grid2 gc{nnx, nnz, nnz, job.goxd, job.gozd, dvx / job.gdx, dvz / job.gdz};
   const double *Vc = job.veln + (size_t)map * nnx * nnz;
   const double x = job.scx[src], z = job.scz[src];
+  Trace trace{job.trace_i, job.trace_t, job.trace_max, 0};
+  Trace *tr = (job.trace_i && solve == job.trace_solve && lane == 0) ? &trace : nullptr;
   int isx = (int)((x - gc.gox) / gc.dnx) + 1;
   int isz = (int)((z - gc.goz) / gc.dnz) + 1;
   if (isx < 1 || isx > nnx || isz < 1 || isz > nnz) {
@@ -460,7 +633,7 @@ fm2d_solve_kernel(Fm2dJob job, int warp_bytes) {
     __syncwarp();
     if (lane == 0) init_source(w, gr, Vr, x, z);
     __syncwarp();
-    march(w, gr, Vr, job.fom, 1, vnl, vnr, vnt, vnb);
+    march(w, gr, Vr, job.fom, job.precision, 1, vnl, vnr, vnt, vnb, tr);
     // map refined onto coarse: gather the mapped refined nodes first
     const int mx = (nrnx - 1) / sgdl + 1, mz = (nrnz - 1) / sgdl + 1;   // = vnr-vnl+1, vnb-vnt+1
     double *tmpT = job.map_tmp_t + (size_t)solve * job.map_tmp_max;
@@ -501,13 +674,13 @@ fm2d_solve_kernel(Fm2dJob job, int warp_bytes) {
           if (w.S[lin(gc, j, i)] > 0) addtree(w, gc, j, i);
     }
     __syncwarp();
-    march(w, gc, Vc, job.fom, 2, vnl, vnr, vnt, vnb);
+    march(w, gc, Vc, job.fom, job.precision, 2, vnl, vnr, vnt, vnb, tr);
   } else {
     for (int q = lane; q < nnx * nnz; q += 32) w.S[q] = -1;
     __syncwarp();
     if (lane == 0) init_source(w, gc, Vc, x, z);
     __syncwarp();
-    march(w, gc, Vc, job.fom, 0, vnl, vnr, vnt, vnb);
+    march(w, gc, Vc, job.fom, job.precision, 0, vnl, vnr, vnt, vnb, tr);
   }
   // optional travel-time field
   if (job.tfield) {

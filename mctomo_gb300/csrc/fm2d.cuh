@@ -7,6 +7,7 @@ struct Fm2dJob {
   int nvx, nvz;              // B-spline vertex grid
   double goxd, gozd, dvxd, dvzd;
   int gdx, gdz, asgr, sgdl, sgs, fom;
+  int precision;             // 0 FP64 as the reference, 1 FP32 local solves on FP64 times
   const double *velv;        // [nmaps][nvx+2][nvz+2] padded vertex grids (Fortran (nvz+2,nvx+2))
   double *veln;              // [nmaps][nnx][nnz] scratch: B-spline node velocities
   double *vref;              // [nsolve][nref_max] scratch: refined source-box velocities
@@ -21,6 +22,8 @@ struct Fm2dJob {
   double *ttime;             // [nmaps][nsrc][nrc]
   double *tfield;            // optional [nmaps][nsrc][nnx][nnz]
   int *status;
+  // optional pop trace of one solve (debugging): [stage, node, ntr] ints and times
+  int trace_solve; int *trace_i; double *trace_t; int trace_max;
   // from fm2d_plan
   int nodes_max, nref_max, map_tmp_max;
 };

@@ -16,6 +16,7 @@ struct mct_surf_ctx {
   int *d_slots = nullptr, *d_ncells = nullptr, *d_accept = nullptr;
   double *d_points = nullptr, *d_params = nullptr, *d_n0 = nullptr, *d_n1 = nullptr, *d_out = nullptr;
   int last_nchains = 0;
+  SurfProfile prof;
 };
 
 namespace {
@@ -56,6 +57,7 @@ int mct_surf_create(const mct_grid *g, const mct_surf_settings *st, const mct_su
   fj.nvx = g->nx; fj.nvz = g->ny; fj.goxd = g->xmin; fj.gozd = g->ymin; fj.dvxd = g->dx; fj.dvzd = g->dy;
   fj.gdx = st->gridx; fj.gdz = st->gridy; fj.asgr = st->sgref; fj.sgdl = st->sgdic; fj.sgs = st->sgext;
   fj.fom = st->order; fj.nsrc = nsrc; fj.nrc = nrev; fj.srs_nmaps = np;
+  fj.precision = st->tt_precision ? 1 : 0;
   if (fj.gdx < 1 || fj.gdz < 1 || (fj.asgr == 1 && (fj.sgdl < 1 || fj.sgs < 1))) { delete c; return MCT_ERR_ARG; }
   int rc = fm2d_plan(fj, &c->plan.fm2d_plan);
   if (rc) { delete c; return MCT_ERR_ARG; }
@@ -178,6 +180,10 @@ int mct_surf_create(const mct_grid *g, const mct_surf_settings *st, const mct_su
 int mct_surf_destroy(mct_surf_ctx *c) {
   if (!c) return MCT_OK;
   cudaStreamSynchronize(c->stream);
+  if (c->prof.ev) {
+    for (int i = 0; i < 5 * c->prof.max_steps; ++i) cudaEventDestroy(c->prof.ev[i]);
+    delete[] c->prof.ev;
+  }
   cudaFree(c->mem);
   cudaStreamDestroy(c->stream);
   delete c;
@@ -193,12 +199,13 @@ int mct_surf_forward_device(mct_surf_ctx *c, int nchains, const int *slots, cons
   b.n0 = n0; b.n1 = n1; b.out = out;
   c->last_nchains = nchains;
   cudaStream_t s = stream ? static_cast<cudaStream_t>(stream) : c->stream;
-  return surf_forward(b, c->plan, s);
+  return surf_forward(b, c->plan, s, &c->prof);
 }
 
 int mct_surf_commit_device(mct_surf_ctx *c, const int *accept, void *stream) {
   if (!c || c->last_nchains < 1) return MCT_ERR_ARG;
   cudaStream_t s = stream ? static_cast<cudaStream_t>(stream) : c->stream;
+  c->prof.launches += 1;
   return surf_commit(c->b, accept, s);
 }
 
@@ -252,6 +259,39 @@ int mct_surf_phase_time(mct_surf_ctx *c, int index, double *phase_time, double *
   if (phase_vel)
     MCT_CUDA_TRY(cudaMemcpy(phase_vel, b.pvel + (size_t)index * b.np * b.nx * b.ny,
                             sizeof(double) * b.np * b.nx * b.ny, cudaMemcpyDeviceToHost));
+  return MCT_OK;
+}
+
+int mct_surf_profile_start(mct_surf_ctx *c, int max_steps) {
+  if (!c || max_steps < 0) return MCT_ERR_ARG;
+  SurfProfile &p = c->prof;
+  if (p.ev) {
+    for (int i = 0; i < 5 * p.max_steps; ++i) cudaEventDestroy(p.ev[i]);
+    delete[] p.ev;
+    p.ev = nullptr;
+  }
+  p.enabled = max_steps > 0; p.max_steps = max_steps; p.step = 0; p.launches = 0;
+  if (max_steps > 0) {
+    p.ev = new cudaEvent_t[5 * max_steps];
+    for (int i = 0; i < 5 * max_steps; ++i) MCT_CUDA_TRY(cudaEventCreate(&p.ev[i]));
+  }
+  return MCT_OK;
+}
+
+int mct_surf_profile_read(mct_surf_ctx *c, double *stage_ms, int *steps, long long *launches) {
+  if (!c) return MCT_ERR_ARG;
+  SurfProfile &p = c->prof;
+  for (int k = 0; k < 4; ++k) stage_ms[k] = 0.0;
+  for (int i = 0; i < p.step; ++i) {
+    MCT_CUDA_TRY(cudaEventSynchronize(p.ev[5 * i + 4]));
+    for (int k = 0; k < 4; ++k) {
+      float ms = 0.f;
+      MCT_CUDA_TRY(cudaEventElapsedTime(&ms, p.ev[5 * i + k], p.ev[5 * i + k + 1]));
+      stage_ms[k] += ms;
+    }
+  }
+  if (steps) *steps = p.step;
+  if (launches) *launches = p.launches;
   return MCT_OK;
 }
 

@@ -198,8 +198,12 @@ __global__ void gather_committed_maps(SurfBatch b) {
 
 }  // namespace
 
-int surf_forward(SurfBatch &b, const SurfPlan &plan, cudaStream_t s) {
+int surf_forward(SurfBatch &b, const SurfPlan &plan, cudaStream_t s, SurfProfile *prof) {
   const int nch = b.nchains;
+  cudaEvent_t *ev = nullptr;
+  if (prof && prof->enabled && prof->step < prof->max_steps) ev = prof->ev + 5 * prof->step++;
+  if (ev) MCT_CUDA_TRY(cudaEventRecord(ev[0], s));
+  if (prof) prof->launches += 12;
   const int ncol = b.nx * b.ny;
   MCT_CUDA_TRY(cudaMemsetAsync(b.status, 0, sizeof(int) * nch, s));
   MCT_CUDA_TRY(cudaMemsetAsync(b.list_count, 0, sizeof(int), s));
@@ -216,6 +220,7 @@ int surf_forward(SurfBatch &b, const SurfPlan &plan, cudaStream_t s) {
   gj.sites_id = b.sites; gj.vp = b.vp; gj.vs = b.vs; gj.rho = b.rho;
   gj.tie_count = b.tie_count; gj.tie_nodes = b.tie_nodes; gj.kd_scratch = b.kd_scratch; gj.status = b.dev_status;
   int rc = launch_grid_nearest(gj, s); if (rc) return rc;
+  if (ev) MCT_CUDA_TRY(cudaEventRecord(ev[1], s));
   // 3-4: model check, changed columns, layering, dispersion, scatter
   columns_kernel<<<dim3((ncol + 127) / 128, nch), 128, 0, s>>>(b);
   MCT_CUDA_TRY(cudaGetLastError());
@@ -233,6 +238,7 @@ int surf_forward(SurfBatch &b, const SurfPlan &plan, cudaStream_t s) {
   MCT_CUDA_TRY(cudaGetLastError());
   scatter_kernel<<<(maxlist + 127) / 128, 128, 0, s>>>(b);
   MCT_CUDA_TRY(cudaGetLastError());
+  if (ev) MCT_CUDA_TRY(cudaEventRecord(ev[2], s));
   // 5: padded maps and fm2d
   pad_kernel<<<dim3(8, nch * b.np), 256, 0, s>>>(b);
   MCT_CUDA_TRY(cudaGetLastError());
@@ -244,9 +250,11 @@ int surf_forward(SurfBatch &b, const SurfPlan &plan, cudaStream_t s) {
   fj.tfield = nullptr;
   fj.status = b.dev_status;
   rc = launch_fm2d(fj, plan.fm2d_plan, s); if (rc) return rc;
+  if (ev) MCT_CUDA_TRY(cudaEventRecord(ev[3], s));
   // 6: misfit
   misfit_kernel<<<nch, 256, 0, s>>>(b);
   MCT_CUDA_TRY(cudaGetLastError());
+  if (ev) MCT_CUDA_TRY(cudaEventRecord(ev[4], s));
   return MCT_OK;
 }
 

@@ -45,11 +45,19 @@ struct SurfBatch {
   double *cpvel;             // [nslots][np][nx][ny]
 };
 
+// Optional per-stage timing: events recorded around the stages of each
+// forward (no host synchronisation), read back after the timed region.
+struct SurfProfile {
+  int enabled = 0, max_steps = 0, step = 0;
+  cudaEvent_t *ev = nullptr;        // [max_steps][5]
+  long long launches = 0;           // kernels launched by forwards
+};
+
 struct SurfPlan {
   Fm2dJob fm2d;              // static parts (stations, settings, scratch, solve list)
   Fm2dPlan fm2d_plan;
   int nsolve_per_chain;
 };
 
-int surf_forward(SurfBatch &b, const SurfPlan &plan, cudaStream_t s);
+int surf_forward(SurfBatch &b, const SurfPlan &plan, cudaStream_t s, SurfProfile *prof = nullptr);
 int surf_commit(SurfBatch &b, const int *accept_dev, cudaStream_t s);

@@ -133,7 +133,7 @@ def modrays(src, rev, srs, nvx, nvz, goxd, gozd, dvxd, dvzd, velv, gdx=1, gdz=1,
 
 
 def modrays_batch(src, rev, srs, nvx, nvz, goxd, gozd, dvxd, dvzd, velv, gdx=1, gdz=1, asgr=1,
-                  sgdl=4, sgs=8, fom=1, ttime=None):
+                  sgdl=4, sgs=8, fom=1, ttime=None, precision=0):
     """Many velocity maps with shared stations. velv: (nmaps, nvx+2, nvz+2);
     srs: (srs_nmaps, nsrc, nrc). Returns ttime (nmaps, nsrc, nrc)."""
     src = _f64(src); rev = _f64(rev); velv = _f64(velv)
@@ -148,6 +148,6 @@ def modrays_batch(src, rev, srs, nvx, nvz, goxd, gozd, dvxd, dvzd, velv, gdx=1, 
     rx, rz = np.ascontiguousarray(rev[:, 0]), np.ascontiguousarray(rev[:, 1])
     rc = lib().mct_modrays_batch(nmaps, nsrc, ptr(sx), ptr(sz), nrc, ptr(rx), ptr(rz), srs.shape[0],
                                  ptr(srs), nvx, nvz, goxd, gozd, dvxd, dvzd, ptr(velv), gdx, gdz, asgr,
-                                 sgdl, sgs, fom, ptr(ttime), None)
+                                 sgdl, sgs, fom, ptr(ttime), None, int(precision))
     check("mct_modrays_batch", rc)
     return ttime

@@ -69,7 +69,7 @@ def surface_workload(rng, nx=41, ny=41, nz=31, extent=(40.0, 40.0, 6.0), nstatio
                 dx=extent[0] / (nx - 1), dy=extent[1] / (ny - 1), dz=extent[2] / (nz - 1),
                 scaling=1.0, water_depth=0.0)
     settings = dict(raylov=1, phase_group=0, dphase=1e-3, gridx=1, gridy=1, sgref=1, sgdic=4, sgext=8,
-                    order=1, sigdep=1, material_law=2, rho_value=2.0, precision=1)
+                    order=1, sigdep=1, material_law=2, rho_value=2.0, precision=1, tt_precision=0)
     margin = 0.05 * np.array(extent[:2])
     st = margin + (np.array(extent[:2]) - 2 * margin) * rng.random((nstations, 2))
     periods = np.geomspace(pmin, pmax, nperiods)

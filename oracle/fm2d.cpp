@@ -19,6 +19,10 @@
 
 namespace {
 
+int g_trace_src = -1, g_trace_n = 0, g_trace_max = 0, g_cur_src = -1;
+int *g_trace_i = nullptr;
+double *g_trace_t = nullptr;
+
 struct FM2D {
   // grid of nodes currently being marched (coarse or refined)
   int nnx, nnz;
@@ -323,6 +327,10 @@ struct FM2D {
         if (swrg == 1) { S(iz, ix) = 0; break; }
       }
       int ix = btgx[1], iz = btgz[1];
+      if (g_cur_src == g_trace_src && g_trace_n < g_trace_max) {
+        g_trace_i[3 * g_trace_n] = urg; g_trace_i[3 * g_trace_n + 1] = (iz - 1) + nnz * (ix - 1);
+        g_trace_i[3 * g_trace_n + 2] = ntr; g_trace_t[g_trace_n] = T(iz, ix); g_trace_n++;
+      }
       S(iz, ix) = 0;
       downtree();
       for (int i = ix - 1; i <= ix + 1; i += 2) {
@@ -346,6 +354,14 @@ struct FM2D {
 }  // namespace
 
 extern "C" {
+
+// Test hook: record the marching order (stage, node, heap size, time) of one
+// source of the next orc_modrays call.
+int orc_fm2d_trace(int src, int *idx, double *t, int max) {
+  g_trace_src = src; g_trace_i = idx; g_trace_t = t; g_trace_max = max; g_trace_n = 0;
+  return 0;
+}
+int orc_fm2d_trace_count(void) { return g_trace_n; }
 
 // modrays (fm2dray_cartesian.f90:67-480) for uar=1 (no ray paths).
 // velvin: (nvz+2, nvx+2) column-major padded vertex grid. srs: (nrc*nsrc)
@@ -428,6 +444,7 @@ int orc_modrays(int nsrc, const double *scx, const double *scz, int nrc,
     for (int j = 0; j < nrc; ++j) any += srs[(size_t)(i - 1) * nrc + j];
     if (any == 0 && i != 1) continue;
     double x = scx[i - 1], z = scz[i - 1];
+    g_cur_src = i - 1;
     int isx = (int)((x - gox) / dnx) + 1;
     int isz = (int)((z - goz) / dnz) + 1;
     if (isx < 1 || isx > nnx || isz < 1 || isz > nnz) return -1;

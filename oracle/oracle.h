@@ -38,6 +38,8 @@ int orc_modrays(int nsrc, const double *scx, const double *scz, int nrc,
                 const double *velvin, int gdx, int gdz, int asgr, int sgdl,
                 int sgs, int fom, double snb, double *ttime, double *tfield);
 
+int orc_fm2d_trace(int src, int *idx, double *t, int max);
+int orc_fm2d_trace_count(void);
 int orc_fast_marching3d(int nx, int ny, int nz, double dx, double dy, double dz,
                         double xmin, double ymin, double zmin, const double *vel,
                         const double *src, const double *rev, int nrev,

@@ -14,6 +14,7 @@ from mctomo_gb300 import modrays, modrays_batch
 pytestmark = pytest.mark.gpu
 P = lambda a: None if a is None else a.ctypes.data_as(ctypes.c_void_p)  # noqa: E731
 TOL = 1e-9
+TT_MIXED_TOL = 1e-4
 
 
 def voronoi_velv(rng, nvx, nvz, dx, dz, ncell, vrange):
@@ -40,14 +41,21 @@ def oracle_modrays(orc, src, rev, srs, nvx, nvz, gox, goz, dx, dz, velv, gdx, gd
     return tt
 
 
-def stations_perimeter(n, L):
-    s = np.linspace(0, 4 * L, n, endpoint=False) + 0.37
+def stations_perimeter(n, L, inset=0.5):
+    """n stations equally spaced on a square inset from the domain edges.
+    A source within one refined cell of a maximum edge makes the reference's
+    refined pass stop before any refined node maps back onto the coarse grid,
+    and the reference then reports stale memory as travel times; stations are
+    kept away from the edges so the comparison is meaningful."""
+    a, b = inset, L - inset
+    side = b - a
+    s = np.linspace(0, 4 * side, n, endpoint=False) + 0.37
     pts = []
     for v in s:
-        if v < L: pts.append((v, 0.05))
-        elif v < 2 * L: pts.append((L - 0.05, v - L))
-        elif v < 3 * L: pts.append((3 * L - v, L - 0.05))
-        else: pts.append((0.05, 4 * L - v))
+        if v < side: pts.append((a + v, a))
+        elif v < 2 * side: pts.append((b, a + v - side))
+        elif v < 3 * side: pts.append((b - (v - 2 * side), b))
+        else: pts.append((a, b - (v - 3 * side)))
     return np.array(pts)
 
 
@@ -61,8 +69,7 @@ def test_modrays_2d_config_shape_matches_oracle(orc, gpulib, asgr, fom, sgdl, sg
     st = stations_perimeter(16, 10.0)
     srs = 1 - np.eye(16, dtype=np.int32)
     got = modrays(st, st, srs, nvx, nvz, 0.0, 0.0, dx, dz, velv, asgr=asgr, sgdl=sgdl, sgs=sgs, fom=fom)
-    exp = oracle_modrays(orc, st, st, srs, nvx, nvz, 0.0, 0.0, dx, dz, velv.T.copy().T if False else velv,
-                         1, 1, asgr, sgdl, sgs, fom)
+    exp = oracle_modrays(orc, st, st, srs, nvx, nvz, 0.0, 0.0, dx, dz, velv, 1, 1, asgr, sgdl, sgs, fom)
     m = srs == 1
     assert np.max(np.abs(got[m] - exp[m])) <= TOL
 
@@ -74,7 +81,7 @@ def test_modrays_batch_surface_shape_matches_oracle(orc, gpulib):
     dx = dz = 1.0
     nmaps = 6
     velv = np.stack([voronoi_velv(rng, nvx, nvz, dx, dz, 30, (0.4, 2.2)) for _ in range(nmaps)])
-    st = rng.uniform(1.0, 39.0, (12, 2))
+    st = rng.uniform(2.0, 38.0, (12, 2))
     srs = np.triu(np.ones((12, 12), np.int32), 1)
     got = modrays_batch(st, st, srs, nvx, nvz, 0.0, 0.0, dx, dz, velv, sgdl=4, sgs=8)
     for mp in range(nmaps):
@@ -100,3 +107,16 @@ def test_modrays_source_outside_is_an_error(gpulib):
         modrays(np.array([[50.0, 1.0]]), np.array([[1.0, 1.0]]), np.ones((1, 1), np.int32), 41, 41, 0., 0.,
                 0.25, 0.25, velv)
     assert ei.value.code == -4
+
+
+def test_modrays_mixed_precision_within_tolerance(orc, gpulib):
+    # FP32 quadratic solves on FP64 times: within the 1e-4 s travel-time bound
+    rng = np.random.default_rng(8)
+    nvx = nvz = 41
+    velv = np.stack([voronoi_velv(rng, nvx, nvz, 1.0, 1.0, 40, (0.4, 2.2)) for _ in range(4)])
+    st = rng.uniform(2.0, 38.0, (20, 2))
+    srs = np.triu(np.ones((20, 20), np.int32), 1)
+    exact = modrays_batch(st, st, srs, nvx, nvz, 0.0, 0.0, 1.0, 1.0, velv, sgdl=4, sgs=8, precision=0)
+    mixed = modrays_batch(st, st, srs, nvx, nvz, 0.0, 0.0, 1.0, 1.0, velv, sgdl=4, sgs=8, precision=1)
+    m = np.broadcast_to(srs == 1, exact.shape)
+    assert np.max(np.abs(mixed[m] - exact[m])) <= TT_MIXED_TOL

@@ -58,6 +58,7 @@ def check_chain(orc, lk, idx, grid, settings, data, n, pts, par, n0, n1, out):
 def test_surface_batch_matches_oracle(orc, gpulib, precision):
     rng, grid, settings, data, ncells, pts, par = small_case(1)
     settings["precision"] = precision
+    settings["tt_precision"] = 0
     lk = SurfaceLikelihood(grid, settings, data, nslots=4, ncell_max=pts.shape[1])
     npd = len(data["freqs"])
     n0 = np.full((4, npd), 0.02); n1 = np.full((4, npd), 0.01)
@@ -112,4 +113,22 @@ def test_surface_rejects_models_failing_check_model(gpulib):
     out = lk.forward(np.arange(2), ncells, pts, par, np.full((2, npd), 0.02), np.zeros((2, npd)))
     assert int(out[0, 3]) & 1 and out[0, 0] > 1e300
     assert int(out[1, 3]) == 0
+    lk.close()
+
+
+def test_surface_mixed_precision_travel_times_within_tolerance(orc, gpulib):
+    rng, grid, settings, data, ncells, pts, par = small_case(5)
+    settings["precision"] = 1
+    settings["tt_precision"] = 1
+    lk = SurfaceLikelihood(grid, settings, data, nslots=4, ncell_max=pts.shape[1])
+    npd = len(data["freqs"])
+    n0 = np.full((4, npd), 0.02); n1 = np.full((4, npd), 0.01)
+    out = lk.forward(np.arange(4), ncells, pts, par, n0, n1)
+    for c in range(4):
+        eo, ept, epv = oracle_like(orc, grid, settings, data, ncells[c], pts[c], par[c], n0[c], n1[c])
+        pt, pv = lk.phase_time(c)
+        m = np.asarray(data["raystat"]).reshape(pt.shape) == 1
+        assert np.max(np.abs(pt[m] - ept[m])) <= TT_TOL
+        if eo[3] == 0:
+            np.testing.assert_allclose(out[c, :3], eo[:3], rtol=1e-3)
     lk.close()
