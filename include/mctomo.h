@@ -226,6 +226,34 @@ int mct_surf_profile_read(mct_surf_ctx *ctx, double *stage_ms, int *steps,
 /* The context's CUDA stream. */
 int mct_surf_stream(mct_surf_ctx *ctx, void **stream);
 
+
+/* ------------------------------------------------------------------------
+ * 3D first-arrival travel times, replaces the reference's C entry point
+ * fastMarching3D (fastmarching/fastMarching.cpp:26-30) with the same
+ * arguments: grid nx,ny,nz with spacing dx,dy,dz and origin xmin,ymin,zmin;
+ * vel (nx,ny,nz) C order (= Fortran (nz,ny,nx)); src[3]; rev (nrev,3);
+ * order 0 first order / 1 mixed second order; ttime[nrev]; tfield (optional)
+ * the final field in vel's layout. Solved on the GPU by a tile-based fast
+ * iterative method on the reference's update operator (times within 1e-4 s
+ * of the reference).
+ * ---------------------------------------------------------------------- */
+int mct_fast_marching3d(int nx, int ny, int nz, double dx, double dy,
+                        double dz, double xmin, double ymin, double zmin,
+                        const double *vel, const double *src,
+                        const double *rev, int nrev, int order, double *ttime,
+                        double *tfield);
+
+/* Many solves at once: ngrids velocity grids vel[ngrids][nx][ny][nz], solve
+ * i runs on grid solve_grid[i] from src[i][3]; the nrev receivers rev[nrev][3]
+ * are shared; ttime[nsolve][nrev]; tfield optional [nsolve][nx][ny][nz];
+ * passes (optional) receives the number of tile passes run. */
+int mct_eikonal3d_batch(int nsolve, int nx, int ny, int nz, double dx,
+                        double dy, double dz, double xmin, double ymin,
+                        double zmin, int ngrids, const double *vel,
+                        const int *solve_grid, const double *src, int nrev,
+                        const double *rev, int order, double *ttime,
+                        double *tfield, int *passes);
+
 #ifdef __cplusplus
 }
 #endif

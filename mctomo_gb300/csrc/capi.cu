@@ -4,6 +4,7 @@
 // the caller's stream.
 #include "mct_common.cuh"
 #include "fm2d.cuh"
+#include "eikonal3d.cuh"
 #include <cstring>
 #include <string>
 #include <vector>
@@ -419,6 +420,82 @@ int mct_debug_fm2d_trace(int solve, int *idx_out, double *t_out, int max) {
   return n;
 }
 
+
+
+// ---------------------------------------------------------------------------
+// 3D travel times (fastMarching3D)
+// ---------------------------------------------------------------------------
+int mct_eikonal3d_batch(int nsolve, int nx, int ny, int nz, double dx, double dy, double dz, double xmin,
+                        double ymin, double zmin, int ngrids, const double *vel, const int *solve_grid,
+                        const double *src, int nrev, const double *rev, int order, double *ttime,
+                        double *tfield, int *passes) {
+  if (nsolve < 1 || nx < 2 || ny < 2 || nz < 2 || ngrids < 1 || nrev < 0 || !(dx > 0) || !(dy > 0) ||
+      !(dz > 0) || (order != 0 && order != 1))
+    return arg_error("mct_eikonal3d_batch: bad arguments");
+  const size_t nn = (size_t)nx * ny * nz;
+  double vmin = 1e300;
+  for (size_t q = 0; q < nn * ngrids; ++q)
+    if (vel[q] >= 2.220446049250313e-11 && vel[q] < vmin) vmin = vel[q];
+  if (!(vmin < 1e300)) return arg_error("mct_eikonal3d_batch: no positive velocity");
+  for (int sI = 0; sI < nsolve; ++sI)
+    if (solve_grid[sI] < 0 || solve_grid[sI] >= ngrids) return arg_error("mct_eikonal3d_batch: bad grid index");
+  const double diag = sqrt(((nx - 1) * dx) * ((nx - 1) * dx) + ((ny - 1) * dy) * ((ny - 1) * dy) +
+                           ((nz - 1) * dz) * ((nz - 1) * dz));
+  std::lock_guard<std::mutex> lk(g_mu);
+  int rc = ensure_stream(); if (rc) return rc;
+  Eik3Job job{};
+  job.nsolve = nsolve; job.nx = nx; job.ny = ny; job.nz = nz; job.dx = dx; job.dy = dy; job.dz = dz;
+  job.ngrids = ngrids; job.order = order; job.nrev = nrev; job.rev_per_solve = 0;
+  job.shift = eik3_shift_for(4.0 * diag / vmin);
+  const size_t ntile = eik3_tiles(job);
+  size_t bytes = carve_size({sizeof(double) * nn * ngrids, sizeof(float) * nn * ngrids, sizeof(int) * nsolve,
+                             sizeof(double) * 3 * nsolve, sizeof(int) * nn * nsolve, ntile * nsolve,
+                             sizeof(int) * ntile * nsolve, sizeof(int), sizeof(double) * 3 * (nrev + 1),
+                             sizeof(double) * (size_t)nsolve * (nrev + 1),
+                             tfield ? sizeof(double) * nn * nsolve : 0});
+  rc = g_ws.reserve(bytes); if (rc) return rc;
+  Carve cv(g_ws.p);
+  double *d_vel = cv.take<double>(nn * ngrids);
+  job.slow = cv.take<float>(nn * ngrids);
+  int *d_sg = cv.take<int>(nsolve);
+  double *d_src = cv.take<double>(3 * (size_t)nsolve);
+  job.T = cv.take<int>(nn * nsolve);
+  job.flags = cv.take<unsigned char>(ntile * nsolve);
+  job.list = cv.take<int>(ntile * nsolve);
+  job.count = cv.take<int>(1);
+  double *d_rev = cv.take<double>(3 * (size_t)(nrev + 1));
+  double *d_tt = cv.take<double>((size_t)nsolve * (nrev + 1));
+  double *d_tf = tfield ? cv.take<double>(nn * nsolve) : nullptr;
+  std::vector<double> hsrc(3 * (size_t)nsolve), hrev(3 * (size_t)nrev);
+  for (int q = 0; q < nsolve; ++q) {
+    hsrc[3 * q] = src[3 * q] - xmin; hsrc[3 * q + 1] = src[3 * q + 1] - ymin; hsrc[3 * q + 2] = src[3 * q + 2] - zmin;
+  }
+  for (int q = 0; q < nrev; ++q) {
+    hrev[3 * q] = rev[3 * q] - xmin; hrev[3 * q + 1] = rev[3 * q + 1] - ymin; hrev[3 * q + 2] = rev[3 * q + 2] - zmin;
+  }
+  cudaStream_t s = g_stream;
+  MCT_CUDA_TRY(cudaMemcpyAsync(d_vel, vel, sizeof(double) * nn * ngrids, cudaMemcpyHostToDevice, s));
+  MCT_CUDA_TRY(cudaMemcpyAsync(d_sg, solve_grid, sizeof(int) * nsolve, cudaMemcpyHostToDevice, s));
+  MCT_CUDA_TRY(cudaMemcpyAsync(d_src, hsrc.data(), sizeof(double) * 3 * nsolve, cudaMemcpyHostToDevice, s));
+  if (nrev) MCT_CUDA_TRY(cudaMemcpyAsync(d_rev, hrev.data(), sizeof(double) * 3 * nrev, cudaMemcpyHostToDevice, s));
+  job.vel = d_vel; job.solve_grid = d_sg; job.src = d_src; job.rev = d_rev; job.ttime = d_tt;
+  int np_ = 0;
+  rc = launch_eik3(job, s, 100000, &np_, d_tf);
+  if (rc) return rc;
+  if (nrev) MCT_CUDA_TRY(cudaMemcpyAsync(ttime, d_tt, sizeof(double) * nsolve * nrev, cudaMemcpyDeviceToHost, s));
+  if (tfield) MCT_CUDA_TRY(cudaMemcpyAsync(tfield, d_tf, sizeof(double) * nn * nsolve, cudaMemcpyDeviceToHost, s));
+  rc = sync_and_check(s, nullptr);
+  if (passes) *passes = np_;
+  return rc;
+}
+
+int mct_fast_marching3d(int nx, int ny, int nz, double dx, double dy, double dz, double xmin, double ymin,
+                        double zmin, const double *vel, const double *src, const double *rev, int nrev, int order,
+                        double *ttime, double *tfield) {
+  const int g = 0;
+  return mct_eikonal3d_batch(1, nx, ny, nz, dx, dy, dz, xmin, ymin, zmin, 1, vel, &g, src, nrev, rev, order == 1 ? 1 : 0,
+                             ttime, tfield, nullptr);
+}
 
 }  // extern "C"
 

@@ -1,0 +1,379 @@
+// 3D first-arrival travel times: the GPU replacement of the reference's
+// fastMarching3D (fastmarching/fastMarching.cpp:26-129), an SFMM over
+// fmm/fmm.hpp:92-158 with the first-order solveEikonal and the mixed
+// second-order highAccuracySolveEikonal updates
+// (fmm/eikonalsolver.hpp:50-145,292-368), 8-corner source initialisation
+// (fmm/solver.hpp:72-92) and trilinear receiver read-out
+// (ndgridmap/ndgridmap.hpp:462-490).
+//
+// The reference's heap march is one sequential chain of ~10^6 dependent
+// steps. Here the same local update is iterated to convergence on tiles: a
+// tile-based fast iterative method. Every (solve, 8x8x8 tile) with pending
+// change is one CTA; the tile and a two-node halo are relaxed in shared
+// memory until they settle, changed values are written back, and the tiles
+// across any face whose outer two layers changed are queued for the next
+// pass. A node's time only ever decreases, so the iteration ends at a fixed
+// point of the reference's update operator; for the first-order scheme that
+// is the discrete solution the heap march computes.
+//
+// Times are stored as int32 fixed point in units of 2^-shift s (shift chosen
+// per call so the largest possible time fits), so comparisons and the final
+// additions are integer operations; each local quadratic is solved in FP32
+// on times taken relative to its smallest neighbour. No FP64 arithmetic runs
+// in the iteration (FP64 throughput is scarce on this GPU); the accumulated
+// rounding stays far below the 1e-4 s travel-time bound.
+#include "mct_common.cuh"
+#include "eikonal3d.cuh"
+#include <climits>
+
+namespace {
+
+constexpr int TX = 8, TY = 8, TZ = 8, HALO = 2;
+constexpr int SX = TX + 2 * HALO, SY = TY + 2 * HALO, SZ = TZ + 2 * HALO;
+constexpr int NLOCAL = 12;           // local relaxation sweeps per visit
+constexpr int TINF = INT_MAX;
+
+struct Dims {
+  int nx, ny, nz, tnx, tny, tnz;
+};
+
+__device__ __forceinline__ Dims dims(const Eik3Job &j) {
+  return Dims{j.nx, j.ny, j.nz, (j.nx + TX - 1) / TX, (j.ny + TY - 1) / TY, (j.nz + TZ - 1) / TZ};
+}
+
+// node index with z fastest (the reference's vel[nx][ny][nz] layout)
+__device__ __forceinline__ size_t nidx(const Dims &d, int i, int j, int k) {
+  return (size_t)k + (size_t)d.nz * ((size_t)j + (size_t)d.ny * i);
+}
+
+// FP32 slowness per velocity grid; obstacles (velocity below the
+// reference's COMP_MARGIN, cell.h isOccupied) are marked negative.
+__global__ void slowness_kernel(const double *vel, float *slow, size_t n) {
+  for (size_t q = blockIdx.x * (size_t)blockDim.x + threadIdx.x; q < n; q += (size_t)gridDim.x * blockDim.x) {
+    double v = vel[q];
+    slow[q] = v < 2.220446049250313e-11 ? -1.f : (float)(1.0 / v);
+  }
+}
+
+__global__ void fill_kernel(int *T, size_t n) {
+  for (size_t q = blockIdx.x * (size_t)blockDim.x + threadIdx.x; q < n; q += (size_t)gridDim.x * blockDim.x)
+    T[q] = TINF;
+}
+
+// Trilinear interpolation with the reference's weights and max-face clamp
+// (ndgridmap.hpp getVel/getTime), point relative to the grid origin.
+template <class F>
+__device__ double trilinear(const Dims &d, const double h[3], const double p[3], F value) {
+  int pc[3];
+  int dimsz[3] = {d.nx, d.ny, d.nz};
+  for (int q = 0; q < 3; ++q) {
+    int c = (int)(p[q] / h[q]);
+    if (c < 0) c = 0; else if (c >= dimsz[q]) c = dimsz[q] - 1;
+    pc[q] = c;
+  }
+  double acc = 0;
+  for (int v = 0; v < 8; ++v) {
+    int vc[3];
+    for (int q = 0; q < 3; ++q) {
+      int vi = (v >> (3 - q - 1)) & 1;
+      vc[q] = pc[q] + vi;
+      if (vc[q] >= dimsz[q]) vc[q] = dimsz[q] - 1;
+    }
+    double w = 1.0;
+    for (int q = 0; q < 3; ++q) {
+      double di = (double)(unsigned)(vc[q] - pc[q]);
+      double s = p[q] - h[q] * (double)(unsigned)pc[q];
+      double wj = fabs(di * h[q] - h[q] + s);
+      w = w * wj / h[q];
+    }
+    acc = acc + w * value(vc[0], vc[1], vc[2]);
+  }
+  return acc;
+}
+
+// Source initialisation (solver.hpp:72-92) and seeding of the first tiles.
+__global__ void init_kernel(Eik3Job job) {
+  const int s = blockIdx.x * blockDim.x + threadIdx.x;
+  if (s >= job.nsolve) return;
+  const Dims d = dims(job);
+  const double h[3] = {job.dx, job.dy, job.dz};
+  const double *vel = job.vel + (size_t)job.solve_grid[s] * d.nx * d.ny * d.nz;
+  int *T = job.T + (size_t)s * d.nx * d.ny * d.nz;
+  const double sp[3] = {job.src[3 * s], job.src[3 * s + 1], job.src[3 * s + 2]};
+  auto vget = [&](int i, int j, int k) { return vel[nidx(d, i, j, k)]; };
+  double v = trilinear(d, h, sp, vget);
+  int pc[3];
+  int dimsz[3] = {d.nx, d.ny, d.nz};
+  for (int q = 0; q < 3; ++q) {
+    int c = (int)(sp[q] / h[q]);
+    if (c < 0) c = 0; else if (c >= dimsz[q]) c = dimsz[q] - 1;
+    pc[q] = c;
+  }
+  const double scale = ldexp(1.0, job.shift);
+  for (int vtx = 0; vtx < 8; ++vtx) {
+    int vc[3];
+    for (int q = 0; q < 3; ++q) {
+      vc[q] = pc[q] + ((vtx >> (3 - q - 1)) & 1);
+      if (vc[q] >= dimsz[q]) vc[q] = dimsz[q] - 1;
+    }
+    double dist = 0;
+    for (int q = 0; q < 3; ++q) {
+      double pk = (double)(unsigned)vc[q] * h[q];
+      double xi = (pk - sp[q]) * (pk - sp[q]);
+      dist = dist + xi;
+    }
+    dist = sqrt(dist);
+    double t = dist * 2 / (v + vget(vc[0], vc[1], vc[2]));
+    long long f = llrint(t * scale);
+    T[nidx(d, vc[0], vc[1], vc[2])] = (int)min(f, (long long)TINF - 1);
+    int tile = (vc[0] / TX) + d.tnx * ((vc[1] / TY) + d.tny * (vc[2] / TZ));
+    job.flags[(size_t)s * d.tnx * d.tny * d.tnz + tile] = 1;
+  }
+}
+
+// Builds the list of (solve, tile) pairs flagged for the next pass.
+__global__ void compact_kernel(Eik3Job job, int *list, int *count) {
+  const Dims d = dims(job);
+  const size_t ntile = (size_t)d.tnx * d.tny * d.tnz;
+  const size_t total = ntile * job.nsolve;
+  for (size_t q = blockIdx.x * (size_t)blockDim.x + threadIdx.x; q < total; q += (size_t)gridDim.x * blockDim.x) {
+    if (job.flags[q]) {
+      job.flags[q] = 0;
+      int pos = atomicAdd(count, 1);
+      list[pos] = (int)q;
+    }
+  }
+}
+
+struct Nb {
+  int t1, t2;    // first and second neighbour times (fixed point, TINF if absent)
+};
+
+// One relaxation of node (x,y,z) of the shared tile; returns the candidate
+// (fixed point) or TINF when no update applies. Mirrors solveEikonal /
+// highAccuracySolveEikonal, including their acceptance rules.
+__device__ __forceinline__ int relax(const int *sT, int x, int y, int z, float slow, const float hh[3],
+                                     int order, float inv_scale, float scale) {
+  const int sidx = z + SZ * (y + SY * x);
+  const int cur = sT[sidx];
+  const int stride[3] = {SY * SZ, SZ, 1};     // x, y, z (shared tile is z fastest)
+  int t1[3], t2[3], dm[3];
+  int cnt = 0;
+  for (int dim = 0; dim < 3; ++dim) {
+    const int st = stride[dim];
+    // neighbours -1 and +1 (absent outside the grid are TINF in the halo)
+    int a = sT[sidx - st], b = sT[sidx + st];
+    if (order == 0) {
+      int m = min(a, b);     // getMinValueInDim: (v0 < v1) ? v0 : v1
+      if (m != TINF && m < cur) { t1[cnt] = m; t2[cnt] = TINF; dm[cnt] = dim; cnt++; }
+    } else {
+      int minT = TINF, minT2 = TINF;
+      if (a != TINF && a < minT) {
+        minT = a; minT2 = TINF;
+        int a2 = sT[sidx - 2 * st];
+        if (a2 != TINF && a2 <= a) minT2 = a2;
+      }
+      if (b != TINF && b < minT) {
+        minT = b; minT2 = TINF;
+        int b2 = sT[sidx + 2 * st];
+        if (b2 != TINF && b2 <= b) minT2 = b2;
+      }
+      if (minT != TINF && minT < cur) { t1[cnt] = minT; t2[cnt] = minT2; dm[cnt] = dim; cnt++; }
+    }
+  }
+  if (cnt == 0) return TINF;
+  // stable insertion sort by t1 (std::sort of <= 3 elements)
+  for (int i = 1; i < cnt; ++i) {
+    int v = t1[i], v2 = t2[i], dd = dm[i], j = i;
+    while (j > 0 && v < t1[j - 1]) { t1[j] = t1[j - 1]; t2[j] = t2[j - 1]; dm[j] = dm[j - 1]; --j; }
+    t1[j] = v; t2[j] = v2; dm[j] = dd;
+  }
+  const int base = t1[0];
+  float r1[3], r2[3];
+  for (int i = 0; i < cnt; ++i) {
+    r1[i] = (float)(t1[i] - base) * inv_scale;
+    r2[i] = t2[i] == TINF ? 0.f : (float)((long long)t2[i] - base) * inv_scale;
+  }
+  auto solve_n = [&](int n, bool second) -> float {
+    if (n == 1) return r1[0] + hh[dm[0]] * slow;
+    float A = 0.f, B = 0.f, C = -(slow * slow);
+    for (int q = 0; q < n; ++q) {
+      float h = hh[dm[q]];
+      if (second && t2[q] != TINF) {
+        float alpha = 2.25f / (h * h);
+        float t = (4.f * r1[q] - r2[q]) / 3.f;
+        C += t * t * alpha; B += -2.f * t * alpha; A += alpha;
+      } else {
+        float alpha = 1.f / (h * h);
+        C += r1[q] * r1[q] * alpha; B += -2.f * r1[q] * alpha; A += alpha;
+      }
+    }
+    float quad = B * B - 4.f * A * C;
+    if (quad < 0.f) return INFINITY;
+    return (-B + sqrtf(quad)) / (2.f * A);
+  };
+  auto to_fixed = [&](float rel) -> long long { return (long long)base + llrintf(rel * scale); };
+  long long res = TINF;
+  if (order == 0) {
+    for (int i = 1; i <= cnt; ++i) {
+      float c = solve_n(i, false);
+      if (isinf(c)) { res = TINF; if (i == cnt) break; continue; }
+      res = to_fixed(c);
+      if (i == cnt || res - (long long)t1[i] < 1) break;
+    }
+  } else {
+    for (int i = cnt; i >= 1; --i) {
+      float c = solve_n(i, true);
+      if (!isinf(c)) {
+        long long f = to_fixed(c);
+        if (f - (long long)t1[i - 1] > 0) { res = f; break; }
+      }
+    }
+  }
+  if (res >= TINF) return TINF;
+  return (int)res;
+}
+
+__global__ void __launch_bounds__(512) tile_kernel(Eik3Job job, const int *list) {
+  __shared__ int sT[SX * SY * SZ];
+  __shared__ float sS[TX * TY * TZ];
+  __shared__ int s_face[6];
+  const Dims d = dims(job);
+  const int ntile = d.tnx * d.tny * d.tnz;
+  const int e = list[blockIdx.x];
+  const int s = e / ntile, tile = e % ntile;
+  const int tx = tile % d.tnx, ty = (tile / d.tnx) % d.tny, tz = tile / (d.tnx * d.tny);
+  const int x0 = tx * TX, y0 = ty * TY, z0 = tz * TZ;
+  const size_t nn = (size_t)d.nx * d.ny * d.nz;
+  int *T = job.T + (size_t)s * nn;
+  const float *slw = job.slow + (size_t)job.solve_grid[s] * nn;
+  // load tile + halo
+  for (int q = threadIdx.x; q < SX * SY * SZ; q += blockDim.x) {
+    int z = q % SZ, y = (q / SZ) % SY, x = q / (SZ * SY);
+    int gi = x0 + x - HALO, gj = y0 + y - HALO, gk = z0 + z - HALO;
+    sT[q] = (gi >= 0 && gi < d.nx && gj >= 0 && gj < d.ny && gk >= 0 && gk < d.nz) ? T[nidx(d, gi, gj, gk)] : TINF;
+  }
+  const int lz = threadIdx.x % TZ, ly = (threadIdx.x / TZ) % TY, lx = threadIdx.x / (TZ * TY);
+  const int gi = x0 + lx, gj = y0 + ly, gk = z0 + lz;
+  const bool inside = gi < d.nx && gj < d.ny && gk < d.nz;
+  float slow = 0.f;
+  bool obstacle = true;
+  if (inside) {
+    slow = slw[nidx(d, gi, gj, gk)];
+    obstacle = slow < 0.f;
+  }
+  if (threadIdx.x < 6) s_face[threadIdx.x] = 0;
+  __syncthreads();
+  const int me = (lz + HALO) + SZ * ((ly + HALO) + SY * (lx + HALO));
+  const int orig = sT[me];
+  const float hh[3] = {(float)job.dx, (float)job.dy, (float)job.dz};
+  const float scale = ldexpf(1.f, job.shift), inv_scale = ldexpf(1.f, -job.shift);
+  int last_change = 0;
+  for (int it = 0; it < NLOCAL; ++it) {
+    int mine = 0;
+    if (inside && !obstacle) {
+      int c = relax(sT, lx + HALO, ly + HALO, lz + HALO, slow, hh, job.order, inv_scale, scale);
+      if (c < sT[me]) { sT[me] = c; mine = 1; }
+    }
+    last_change = __syncthreads_or(mine);
+    if (!last_change) break;
+  }
+  const int fin = sT[me];
+  if (inside && fin < orig) {
+    T[nidx(d, gi, gj, gk)] = fin;
+    if (lx < 2) s_face[0] = 1;
+    if (lx >= TX - 2) s_face[1] = 1;
+    if (ly < 2) s_face[2] = 1;
+    if (ly >= TY - 2) s_face[3] = 1;
+    if (lz < 2) s_face[4] = 1;
+    if (lz >= TZ - 2) s_face[5] = 1;
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    unsigned char *fl = job.flags + (size_t)s * ntile;
+    if (last_change) fl[tile] = 1;     // not settled within the visit: revisit
+    if (s_face[0] && tx > 0) fl[tile - 1] = 1;
+    if (s_face[1] && tx < d.tnx - 1) fl[tile + 1] = 1;
+    if (s_face[2] && ty > 0) fl[tile - d.tnx] = 1;
+    if (s_face[3] && ty < d.tny - 1) fl[tile + d.tnx] = 1;
+    if (s_face[4] && tz > 0) fl[tile - d.tnx * d.tny] = 1;
+    if (s_face[5] && tz < d.tnz - 1) fl[tile + d.tnx * d.tny] = 1;
+  }
+}
+
+// Receiver read-out (ndgridmap.hpp:462-490) per (solve, receiver).
+__global__ void readout_kernel(Eik3Job job) {
+  const int s = blockIdx.y;
+  const Dims d = dims(job);
+  const size_t nn = (size_t)d.nx * d.ny * d.nz;
+  const int *T = job.T + (size_t)s * nn;
+  const double h[3] = {job.dx, job.dy, job.dz};
+  const double inv = ldexp(1.0, -job.shift);
+  const int rs = job.rev_per_solve ? s : 0;
+  for (int r = blockIdx.x * blockDim.x + threadIdx.x; r < job.nrev; r += gridDim.x * blockDim.x) {
+    const double *p = job.rev + ((size_t)rs * job.nrev + r) * 3;
+    double pt[3] = {p[0], p[1], p[2]};
+    auto tget = [&](int i, int j, int k) {
+      int t = T[nidx(d, i, j, k)];
+      return t == TINF ? (double)INFINITY : (double)t * inv;
+    };
+    job.ttime[(size_t)s * job.nrev + r] = trilinear(d, h, pt, tget);
+  }
+}
+
+__global__ void field_kernel(Eik3Job job, double *tfield) {
+  const int s = blockIdx.y;
+  const size_t nn = (size_t)job.nx * job.ny * job.nz;
+  const double inv = ldexp(1.0, -job.shift);
+  for (size_t q = blockIdx.x * (size_t)blockDim.x + threadIdx.x; q < nn; q += (size_t)gridDim.x * blockDim.x) {
+    int t = job.T[(size_t)s * nn + q];
+    tfield[(size_t)s * nn + q] = t == TINF ? (double)INFINITY : (double)t * inv;
+  }
+}
+
+}  // namespace
+
+size_t eik3_tiles(const Eik3Job &j) {
+  return (size_t)((j.nx + TX - 1) / TX) * ((j.ny + TY - 1) / TY) * ((j.nz + TZ - 1) / TZ);
+}
+
+int eik3_shift_for(double tmax_bound) {
+  int shift = 30;
+  while (shift > 4 && ldexp(tmax_bound, shift) > 2.0e9) --shift;
+  return shift;
+}
+
+int launch_eik3(Eik3Job &job, cudaStream_t s, int max_passes, int *passes_out, double *tfield) {
+  const size_t nn = (size_t)job.nx * job.ny * job.nz;
+  const size_t ntile = eik3_tiles(job);
+  slowness_kernel<<<1024, 256, 0, s>>>(job.vel, job.slow, nn * job.ngrids);
+  MCT_CUDA_TRY(cudaGetLastError());
+  fill_kernel<<<1024, 256, 0, s>>>(job.T, nn * job.nsolve);
+  MCT_CUDA_TRY(cudaGetLastError());
+  MCT_CUDA_TRY(cudaMemsetAsync(job.flags, 0, ntile * job.nsolve, s));
+  init_kernel<<<(job.nsolve + 127) / 128, 128, 0, s>>>(job);
+  MCT_CUDA_TRY(cudaGetLastError());
+  int passes = 0;
+  for (;;) {
+    MCT_CUDA_TRY(cudaMemsetAsync(job.count, 0, sizeof(int), s));
+    compact_kernel<<<1024, 256, 0, s>>>(job, job.list, job.count);
+    MCT_CUDA_TRY(cudaGetLastError());
+    int n = 0;
+    MCT_CUDA_TRY(cudaMemcpyAsync(&n, job.count, sizeof(int), cudaMemcpyDeviceToHost, s));
+    MCT_CUDA_TRY(cudaStreamSynchronize(s));
+    if (n == 0) break;
+    if (++passes > max_passes) return MCT_ERR_TIMEOUT;
+    tile_kernel<<<n, 512, 0, s>>>(job, job.list);
+    MCT_CUDA_TRY(cudaGetLastError());
+  }
+  if (passes_out) *passes_out = passes;
+  if (job.nrev > 0) {
+    readout_kernel<<<dim3((job.nrev + 127) / 128, job.nsolve), 128, 0, s>>>(job);
+    MCT_CUDA_TRY(cudaGetLastError());
+  }
+  if (tfield) {
+    field_kernel<<<dim3(256, job.nsolve), 256, 0, s>>>(job, tfield);
+    MCT_CUDA_TRY(cudaGetLastError());
+  }
+  return MCT_OK;
+}

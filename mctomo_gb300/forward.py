@@ -151,3 +151,39 @@ def modrays_batch(src, rev, srs, nvx, nvz, goxd, gozd, dvxd, dvzd, velv, gdx=1, 
                                  sgdl, sgs, fom, ptr(ttime), None, int(precision))
     check("mct_modrays_batch", rc)
     return ttime
+
+
+def fast_marching3d(vel, h, lo, src, rev, order=1, tfield=False):
+    """fastMarching3D (fastmarching/fastMarching.cpp:26-129). vel: (nx, ny, nz)
+    C order; h = (dx, dy, dz); lo = (xmin, ymin, zmin); src (3,); rev (nrev, 3).
+    Returns ttime (nrev,) and optionally the field (nx, ny, nz)."""
+    vel = _f64(vel)
+    nx, ny, nz = vel.shape
+    src = _f64(src); rev = _f64(rev).reshape(-1, 3)
+    tt = np.zeros(rev.shape[0])
+    tf = np.zeros_like(vel) if tfield else None
+    rc = lib().mct_fast_marching3d(nx, ny, nz, float(h[0]), float(h[1]), float(h[2]), float(lo[0]), float(lo[1]),
+                                   float(lo[2]), ptr(vel), ptr(src), ptr(rev), rev.shape[0], int(order), ptr(tt),
+                                   ptr(tf))
+    check("mct_fast_marching3d", rc)
+    return (tt, tf) if tfield else tt
+
+
+def eikonal3d_batch(vels, h, lo, solve_grid, srcs, rev, order=1, tfield=False):
+    """Many 3D solves: vels (ngrids, nx, ny, nz), solve_grid (nsolve,),
+    srcs (nsolve, 3), shared receivers rev (nrev, 3). Returns ttime
+    (nsolve, nrev), the optional fields and the number of tile passes."""
+    vels = _f64(vels)
+    ng, nx, ny, nz = vels.shape
+    solve_grid = np.ascontiguousarray(solve_grid, np.int32)
+    srcs = _f64(srcs).reshape(-1, 3)
+    rev = _f64(rev).reshape(-1, 3)
+    ns = srcs.shape[0]
+    tt = np.zeros((ns, rev.shape[0]))
+    tf = np.zeros((ns, nx, ny, nz)) if tfield else None
+    passes = ctypes.c_int(0)
+    rc = lib().mct_eikonal3d_batch(ns, nx, ny, nz, float(h[0]), float(h[1]), float(h[2]), float(lo[0]),
+                                   float(lo[1]), float(lo[2]), ng, ptr(vels), ptr(solve_grid), ptr(srcs),
+                                   rev.shape[0], ptr(rev), int(order), ptr(tt), ptr(tf), ctypes.byref(passes))
+    check("mct_eikonal3d_batch", rc)
+    return tt, tf, passes.value

@@ -1,0 +1,80 @@
+"""GPU parity: 3D travel times (tile-based fast iterative method on the
+reference's update operator) vs the reference's own fastMarching3D as
+restated by the oracle (bit-exact to the compiled reference).
+
+Tolerance: 1e-4 s on receiver times (the benchmark spec's bound). The FP32 local
+solves with fixed-point times add ~1e-6 s; the remaining difference is the
+iteration's fixed point against the heap march (nil for the first-order
+scheme up to rounding, small for the mixed second-order scheme)."""
+import ctypes
+
+import numpy as np
+import pytest
+
+from mctomo_gb300 import eikonal3d_batch, fast_marching3d
+
+pytestmark = pytest.mark.gpu
+P = lambda a: None if a is None else a.ctypes.data_as(ctypes.c_void_p)  # noqa: E731
+TOL = 1e-4
+
+
+def oracle_fmm(orc, vel, h, lo, src, rev, order):
+    nx, ny, nz = vel.shape
+    tt = np.zeros(len(rev)); tf = np.zeros_like(vel)
+    rc = orc.orc_fast_marching3d(nx, ny, nz, *h, *lo, P(np.ascontiguousarray(vel)), P(np.ascontiguousarray(src)),
+                                 P(np.ascontiguousarray(rev)), len(rev), order, P(tt), P(tf))
+    assert rc == 0
+    return tt, tf
+
+
+def layered_voronoi(rng, shape, h, ncell, vrange):
+    nx, ny, nz = shape
+    pts = rng.uniform(0, 1, (ncell, 3)) * (np.array(shape) - 1) * h
+    vals = np.sort(rng.uniform(*vrange, ncell))[np.argsort(np.argsort(pts[:, 2]))]
+    X, Y, Z = np.meshgrid(np.arange(nx) * h[0], np.arange(ny) * h[1], np.arange(nz) * h[2], indexing="ij")
+    d = (X[..., None] - pts[:, 0]) ** 2 + (Y[..., None] - pts[:, 1]) ** 2 + (Z[..., None] - pts[:, 2]) ** 2
+    return vals[np.argmin(d, -1)]
+
+
+@pytest.mark.parametrize("order", [0, 1])
+def test_fast_marching3d_matches_reference(orc, gpulib, order):
+    rng = np.random.default_rng(10 + order)
+    shape = (41, 37, 21)
+    h = np.array([0.5, 0.5, 0.5]); lo = np.array([-5.0, 2.0, 0.0])
+    vel = layered_voronoi(rng, shape, h, 60, (3.0, 7.5))
+    ext = (np.array(shape) - 1) * h
+    for trial in range(3):
+        src = lo + ext * rng.uniform(0.05, 0.95, 3)
+        rev = lo + ext * rng.uniform(0.02, 0.98, (40, 3))
+        rev[:, 2] = lo[2] + 0.0   # stations at the surface
+        got, gf = fast_marching3d(vel, h, lo, src, rev, order=order, tfield=True)
+        exp, ef = oracle_fmm(orc, vel, h, lo, src, rev, order)
+        assert np.max(np.abs(got - exp)) <= TOL, np.max(np.abs(got - exp))
+        assert np.max(np.abs(gf - ef)) <= 10 * TOL
+
+
+def test_eikonal3d_homogeneous_first_order(orc, gpulib):
+    vel = np.full((30, 30, 20), 4.0)
+    h = (0.5, 0.5, 0.5); lo = (0.0, 0.0, 0.0)
+    src = np.array([7.3, 6.1, 4.2])
+    rev = np.array([[1.0, 1.0, 0.0], [14.0, 14.0, 9.0], [3.3, 12.2, 5.5]])
+    got = fast_marching3d(vel, h, lo, src, rev, order=0)
+    exp, _ = oracle_fmm(orc, vel, np.array(h), np.array(lo), src, rev, 0)
+    assert np.max(np.abs(got - exp)) <= TOL
+
+
+def test_eikonal3d_batch_many_sources_and_grids(orc, gpulib):
+    rng = np.random.default_rng(3)
+    shape = (33, 29, 17)
+    h = np.array([0.5, 0.5, 0.5]); lo = np.zeros(3)
+    vels = np.stack([layered_voronoi(rng, shape, h, 40, (3.0, 7.5)) for _ in range(2)])
+    vels[1] = vels[1] / 1.73
+    ext = (np.array(shape) - 1) * h
+    srcs = ext * rng.uniform(0.05, 0.95, (6, 3)); srcs[:, 2] = 0.0
+    grid_of = np.array([0, 1, 0, 1, 0, 1])
+    rev = ext * rng.uniform(0.02, 0.98, (25, 3))
+    got, _, passes = eikonal3d_batch(vels, h, lo, grid_of, srcs, rev, order=1)
+    assert passes > 0
+    for i in range(6):
+        exp, _ = oracle_fmm(orc, vels[grid_of[i]], h, lo, srcs[i], rev, 1)
+        assert np.max(np.abs(got[i] - exp)) <= TOL
