@@ -136,7 +136,8 @@ int mct_modrays(int nsrc, const double *scx, const double *scz, int nrc,
  * flags (map m uses set m % srs_nmaps), ttime [nmaps][nsrc][nrc], tfield
  * optional [nmaps][nsrc][nnx*nnz]. precision 0 evaluates the upwind updates
  * in FP64 as the reference; 1 solves each update's quadratic in FP32 on
- * times shifted to a neighbouring accepted time (times stay FP64). */
+ * times shifted to a neighbouring accepted time (times stay FP64); 2 does the
+ * same with int32 fixed-point times (half the shared memory per solve). */
 int mct_modrays_batch(int nmaps, int nsrc, const double *scx,
                       const double *scz, int nrc, const double *rcx,
                       const double *rcz, int srs_nmaps, const int *srs,
@@ -170,7 +171,7 @@ typedef struct {
   int material_law;    /* MCT_LAW_* */
   double rho_value;
   int precision;       /* dispersion root search: 0 FP64, 1 FP32 bracketing */
-  int tt_precision;    /* fm2d upwind updates: 0 FP64, 1 FP32 quadratic */
+  int tt_precision;    /* fm2d updates: 0 FP64, 1 FP32 quadratic, 2 FP32 + fixed-point times */
 } mct_surf_settings;
 
 typedef struct {

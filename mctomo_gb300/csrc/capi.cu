@@ -319,6 +319,7 @@ int mct_modrays_batch(int nmaps, int nsrc, const double *scx, const double *scz,
   job.goxd = goxd; job.gozd = gozd; job.dvxd = dvxd; job.dvzd = dvzd;
   job.gdx = gdx; job.gdz = gdz; job.asgr = asgr; job.sgdl = sgdl; job.sgs = sgs; job.fom = fom;
   job.nsrc = nsrc; job.nrc = nrc; job.srs_nmaps = srs_nmaps;
+  job.precision = (precision >= 0 && precision <= 2) ? precision : 0;
   Fm2dPlan plan;
   int rc = fm2d_plan(job, &plan);
   if (rc) return arg_error("mct_modrays_batch: grid too large for the shared-memory solver");
@@ -343,7 +344,8 @@ int mct_modrays_batch(int nmaps, int nsrc, const double *scx, const double *scz,
                              sizeof(short) * (size_t)plan.map_tmp_max * ns, sizeof(double) * 2 * (nsrc + nrc),
                              sizeof(int) * (size_t)srs_nmaps * nsrc * nrc, sizeof(int2) * ns,
                              sizeof(double) * (size_t)nmaps * nsrc * nrc,
-                             tfield ? sizeof(double) * (size_t)nmaps * nsrc * nnx * nnz : 0, sizeof(int)});
+                             tfield ? sizeof(double) * (size_t)nmaps * nsrc * nnx * nnz : 0, sizeof(int),
+                             sizeof(int)});
   rc = g_ws.reserve(bytes); if (rc) return rc;
   Carve cv(g_ws.p);
   double *d_velv = cv.take<double>(nv * nmaps);
@@ -357,6 +359,7 @@ int mct_modrays_batch(int nmaps, int nsrc, const double *scx, const double *scz,
   double *d_tt = cv.take<double>((size_t)nmaps * nsrc * nrc);
   double *d_tf = tfield ? cv.take<double>((size_t)nmaps * nsrc * nnx * nnz) : nullptr;
   int *d_status = cv.take<int>(1);
+  job.vmin_bits = cv.take<int>(1);
   cudaStream_t s = g_stream;
   MCT_CUDA_TRY(cudaMemcpyAsync(d_velv, velv, sizeof(double) * nv * nmaps, cudaMemcpyHostToDevice, s));
   MCT_CUDA_TRY(cudaMemcpyAsync(d_xy, scx, sizeof(double) * nsrc, cudaMemcpyHostToDevice, s));
@@ -373,7 +376,7 @@ int mct_modrays_batch(int nmaps, int nsrc, const double *scx, const double *scz,
   job.srs = d_srs; job.nsolve = (int)ns; job.solves = d_solves;
   job.ttime = d_tt; job.tfield = d_tf; job.status = d_status;
   job.nodes_max = plan.nodes_max; job.nref_max = plan.nref_max; job.map_tmp_max = plan.map_tmp_max;
-  job.precision = precision ? 1 : 0;
+  job.precision = (precision >= 0 && precision <= 2) ? precision : 0;
   int *d_ti = nullptr; double *d_trt = nullptr;
   if (g_trace_solve >= 0) {
     job.trace_solve = g_trace_solve; job.trace_max = 20000;

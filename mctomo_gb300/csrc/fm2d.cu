@@ -17,46 +17,56 @@
 // -fmad=false so nothing is fused.
 #include "mct_common.cuh"
 #include "fm2d.cuh"
+#include <climits>
 
 namespace {
 
-constexpr int WARPS_PER_BLOCK_MAX = 4;
+constexpr int WARPS_PER_BLOCK_MAX = 8;
 
 struct Grid2 {
   int nnx, nnz, ld;
   double gox, goz, dnx, dnz;
 };
 
-struct WarpState {
-  double *T;          // [ld * cols]
+// Per-solve shared-memory state. TT is double (FP64 times, precision 0 and 1)
+// or int (fixed-point times in units of 2^-shift s, precision 2).
+template <class TT> struct WarpStateT {
+  TT *T;              // [ld * cols]
   short *S;           // node status: -1 far, 0 alive, >0 heap position
-  unsigned short *H;  // heap, 1-based: H[p] = linear node index (iz-1) + ld*(ix-1)
+  unsigned short *H;  // heap, 1-based: H[p] = packed node ((ix-1) << 8) | (iz-1)
   int ntr;
+  int ld;
 };
+using WarpState = WarpStateT<double>;
 
 __device__ __forceinline__ int lin(const Grid2 &g, int iz, int ix) { return (iz - 1) + g.ld * (ix - 1); }
+__device__ __forceinline__ unsigned short pack(int iz, int ix) { return (unsigned short)(((ix - 1) << 8) | (iz - 1)); }
+template <class TT> __device__ __forceinline__ int plin(const WarpStateT<TT> &w, int p) { return (p & 255) + w.ld * (p >> 8); }
 
-// Travel times are finite and non-negative, so their IEEE bit patterns order
-// exactly like the values: the heap compares them on the integer pipe.
-__device__ __forceinline__ long long tkey(const double *T, int node) {
-  return __double_as_longlong(T[node]);
-}
+// Travel times are finite and non-negative, so the IEEE bit patterns of the
+// FP64 times order exactly like the values: the heap compares them on the
+// integer pipe. Fixed-point times compare directly.
+__device__ __forceinline__ long long tkey(const double *T, int node) { return __double_as_longlong(T[node]); }
+__device__ __forceinline__ int tkey(const int *T, int node) { return T[node]; }
 
 // ---- binary heap (fm2d_ttime.f90:527-680), lane 0 only --------------------
-__device__ void addtree(WarpState &w, const Grid2 &g, int iz, int ix) {
+template <class TT>
+__device__ void addtree(WarpStateT<TT> &w, const Grid2 &g, int iz, int ix) {
   w.ntr = w.ntr + 1;
-  int me = lin(g, iz, ix);
+  const int me = lin(g, iz, ix);
+  const unsigned short pm = pack(iz, ix);
   w.S[me] = (short)w.ntr;
-  w.H[w.ntr] = (unsigned short)me;
+  w.H[w.ntr] = pm;
   int tpc = w.ntr, tpp = tpc / 2;
-  long long tme = tkey(w.T, me);
+  const auto tme = tkey(w.T, me);
   while (tpp > 0) {
-    int pn = w.H[tpp];
+    const int pp = w.H[tpp];
+    const int pn = plin(w, pp);
     if (tme < tkey(w.T, pn)) {
       w.S[me] = (short)tpp;
       w.S[pn] = (short)tpc;
-      w.H[tpc] = (unsigned short)pn;
-      w.H[tpp] = (unsigned short)me;
+      w.H[tpc] = (unsigned short)pp;
+      w.H[tpp] = pm;
       tpc = tpp; tpp = tpc / 2;
     } else {
       tpp = 0;
@@ -64,51 +74,57 @@ __device__ void addtree(WarpState &w, const Grid2 &g, int iz, int ix) {
   }
 }
 
-__device__ void downtree(WarpState &w) {
+template <class TT>
+__device__ void downtree(WarpStateT<TT> &w) {
   if (w.ntr == 1) { w.ntr = w.ntr - 1; return; }
-  int last = w.H[w.ntr];
-  w.S[last] = 1;
-  w.H[1] = (unsigned short)last;
+  const int lastp = w.H[w.ntr];
+  w.S[plin(w, lastp)] = 1;
+  w.H[1] = (unsigned short)lastp;
   w.ntr = w.ntr - 1;
   int tpp = 1, tpc = 2 * tpp;
   const int ntr = w.ntr;
   while (tpc < ntr) {
-    long long rd1 = tkey(w.T, w.H[tpc]);
-    long long rd2 = tkey(w.T, w.H[tpc + 1]);
+    const auto rd1 = tkey(w.T, plin(w, w.H[tpc]));
+    const auto rd2 = tkey(w.T, plin(w, w.H[tpc + 1]));
     if (rd1 > rd2) tpc = tpc + 1;
-    int cn = w.H[tpc], pn = w.H[tpp];
+    const int cp = w.H[tpc], pp = w.H[tpp];
+    const int cn = plin(w, cp), pn = plin(w, pp);
     if (tkey(w.T, cn) < tkey(w.T, pn)) {
       w.S[pn] = (short)tpc;
       w.S[cn] = (short)tpp;
-      w.H[tpc] = (unsigned short)pn;
-      w.H[tpp] = (unsigned short)cn;
+      w.H[tpc] = (unsigned short)pp;
+      w.H[tpp] = (unsigned short)cp;
       tpp = tpc; tpc = 2 * tpp;
     } else {
       tpc = ntr + 1;
     }
   }
   if (tpc == ntr) {
-    int cn = w.H[tpc], pn = w.H[tpp];
+    const int cp = w.H[tpc], pp = w.H[tpp];
+    const int cn = plin(w, cp), pn = plin(w, pp);
     if (tkey(w.T, cn) < tkey(w.T, pn)) {
       w.S[pn] = (short)tpc;
       w.S[cn] = (short)tpp;
-      w.H[tpc] = (unsigned short)pn;
-      w.H[tpp] = (unsigned short)cn;
+      w.H[tpc] = (unsigned short)pp;
+      w.H[tpp] = (unsigned short)cp;
     }
   }
 }
 
-__device__ void updtree(WarpState &w, const Grid2 &g, int iz, int ix) {
-  int me = lin(g, iz, ix);
+template <class TT>
+__device__ void updtree(WarpStateT<TT> &w, const Grid2 &g, int iz, int ix) {
+  const int me = lin(g, iz, ix);
+  const unsigned short pm = pack(iz, ix);
   int tpc = w.S[me], tpp = tpc / 2;
-  long long tme = tkey(w.T, me);
+  const auto tme = tkey(w.T, me);
   while (tpp > 0) {
-    int pn = w.H[tpp];
+    const int pp = w.H[tpp];
+    const int pn = plin(w, pp);
     if (tme < tkey(w.T, pn)) {
       w.S[me] = (short)tpp;
       w.S[pn] = (short)tpc;
-      w.H[tpc] = (unsigned short)pn;
-      w.H[tpp] = (unsigned short)me;
+      w.H[tpc] = (unsigned short)pp;
+      w.H[tpp] = pm;
       tpc = tpp; tpp = tpc / 2;
     } else {
       tpp = 0;
@@ -407,6 +423,107 @@ __device__ double fouds2_mixed(const WarpState &w, const Grid2 &g, const double 
   return base + (double)travm;
 }
 
+
+// Fixed-point variant (precision == 2): times are int32 in units of
+// 2^-shift s, each update's quadratic is solved in FP32 on the neighbours'
+// times relative to a nearby accepted time, and the result is rounded back to
+// the fixed-point grid. The stencils and case selection are fouds1/fouds2's.
+struct Fx { float scale, inv; };
+
+__device__ int fouds_fx(const WarpStateT<int> &w, const Grid2 &g, const double *V, int iz, int ix, int fom,
+                        const Fx &fx) {
+  int tsw1 = 0;
+  float travm = 0.f;
+  const float slown = (float)(1.0 / V[lin(g, iz, ix)]);
+  const float dnx = (float)g.dnx, dnz = (float)g.dnz;
+  int base = -1;
+  auto S = [&](int z, int x) { return w.S[lin(g, z, x)]; };
+  auto sh = [&](int z, int x) { return (float)(w.T[lin(g, z, x)] - base) * fx.inv; };
+  for (int j = ix - 1; j <= ix + 1; j += 2) {
+    if (!(j >= 1 && j <= g.nnx)) continue;
+    int swj = -1, j2 = j;
+    const bool jalive = S(iz, j) == 0;
+    if (fom == 1) {
+      if (j == ix - 1) { j2 = j - 1; if (j2 >= 1) { if (S(iz, j2) == 0) swj = 0; } }
+      else { j2 = j + 1; if (j2 <= g.nnx) { if (S(iz, j2) == 0) swj = 0; } }
+      if (jalive && swj == 0) { swj = -1; if (w.T[lin(g, iz, j)] > w.T[lin(g, iz, j2)]) swj = 0; }
+      else swj = -1;
+    }
+    if (jalive && base < 0) base = w.T[lin(g, iz, j)];
+    for (int k = iz - 1; k <= iz + 1; k += 2) {
+      if (!(k >= 1 && k <= g.nnz)) continue;
+      int swk = -1, k2 = k;
+      const bool kalive = S(k, ix) == 0;
+      if (fom == 1) {
+        if (k == iz - 1) { k2 = k - 1; if (k2 >= 1) { if (S(k2, ix) == 0) swk = 0; } }
+        else { k2 = k + 1; if (k2 <= g.nnz) { if (S(k2, ix) == 0) swk = 0; } }
+        if (kalive && swk == 0) { swk = -1; if (w.T[lin(g, k, ix)] > w.T[lin(g, k2, ix)]) swk = 0; }
+        else swk = -1;
+      }
+      if (!jalive && !kalive) continue;
+      if (base < 0) base = w.T[lin(g, k, ix)];
+      float a = 0, b = 0, c = 0, tref = 0, tdiv = 1.f;
+      if (swj == 0) {
+        float tj = sh(iz, j), tj2 = sh(iz, j2);
+        if (swk == 0) {
+          float u = 2.f * dnx, v = 2.f * dnz;
+          float tk = sh(k, ix), tk2 = sh(k2, ix);
+          float em = 4.f * tj - tj2 - 4.f * tk;
+          em = em + tk2;
+          a = v * v + u * u; b = 2.f * em * (u * u);
+          c = (u * u) * (em * em - (slown * slown) * (v * v));
+          tref = 4.f * tj - tj2; tdiv = 3.f;
+        } else if (kalive) {
+          float u = dnz, v = 2.f * dnx;
+          float tk = sh(k, ix);
+          float em = 3.f * tk - 4.f * tj + tj2;
+          a = v * v + 9.f * (u * u); b = 6.f * em * (u * u);
+          c = (u * u) * (em * em - (slown * slown) * (v * v));
+          tref = tk;
+        } else {
+          float u = 2.f * dnx;
+          a = 1.f; c = -((u * u) * (slown * slown));
+          tref = 4.f * tj - tj2; tdiv = 3.f;
+        }
+      } else if (jalive) {
+        float tj = sh(iz, j);
+        if (swk == 0) {
+          float u = dnx, v = 2.f * dnz;
+          float tk = sh(k, ix), tk2 = sh(k2, ix);
+          float em = 3.f * tj - 4.f * tk + tk2;
+          a = v * v + 9.f * (u * u); b = 6.f * em * (u * u);
+          c = (u * u) * (em * em - (v * v) * (slown * slown));
+          tref = tj;
+        } else if (kalive) {
+          float tk = sh(k, ix);
+          float em = tk - tj;
+          a = dnx * dnx + dnz * dnz; b = -(2.f * (dnx * dnx) * em);
+          c = (dnx * dnx) * (em * em - (dnz * dnz) * (slown * slown));
+          tref = tj;
+        } else {
+          a = 1.f; c = -((slown * slown) * (dnx * dnx));
+          tref = tj;
+        }
+      } else {
+        if (swk == 0) {
+          float u = 2.f * dnz;
+          float tk = sh(k, ix), tk2 = sh(k2, ix);
+          a = 1.f; c = -((u * u) * (slown * slown));
+          tref = 4.f * tk - tk2; tdiv = 3.f;
+        } else {
+          a = 1.f; c = -((slown * slown) * (dnz * dnz));
+          tref = sh(k, ix);
+        }
+      }
+      float trav = (tref + quad_rootf(a, b, c)) / tdiv;
+      if (tsw1 == 1) travm = fminf(trav, travm);
+      else { travm = trav; tsw1 = 1; }
+    }
+  }
+  long long r = (long long)base + llrintf(travm * fx.scale);
+  return (int)min(max(r, 0LL), (long long)INT_MAX - 1);
+}
+
 // fm2d_ttime.f90:682-711 bilinear
 __device__ __forceinline__ double bilinear(const double nv[2][2], double dsx, double dsz, double dnx, double dnz) {
   double biv = 0.0;
@@ -425,15 +542,16 @@ __device__ __forceinline__ double bilinear(const double nv[2][2], double dsx, do
 // are at that point.
 struct Trace { int *ti; double *tt; int max; int n; };
 
-__device__ void march(WarpState &w, const Grid2 &g, const double *V, int fom, int prec, int urg, int vnl,
-                      int vnr, int vnt, int vnb, Trace *tr = nullptr) {
+template <class TT>
+__device__ void march(WarpStateT<TT> &w, const Grid2 &g, const double *V, int fom, int prec, int urg, int vnl,
+                      int vnr, int vnt, int vnb, const Fx &fx, Trace *tr = nullptr) {
   const int lane = threadIdx.x & 31;
   for (;;) {
     int ix = 0, iz = 0, go = 0;
     if (lane == 0) {
       if (w.ntr > 0) {
         int top = w.H[1];
-        iz = top % g.ld + 1; ix = top / g.ld + 1;
+        iz = (top & 255) + 1; ix = (top >> 8) + 1;
         go = 1;
         if (urg == 1) {
           int swrg = 0;
@@ -446,7 +564,7 @@ __device__ void march(WarpState &w, const Grid2 &g, const double *V, int fom, in
         if (go) {
           if (tr && tr->n < tr->max) {
             tr->ti[3 * tr->n] = urg; tr->ti[3 * tr->n + 1] = lin(g, iz, ix); tr->ti[3 * tr->n + 2] = w.ntr;
-            tr->tt[tr->n] = w.T[lin(g, iz, ix)]; tr->n++;
+            tr->tt[tr->n] = (double)w.T[lin(g, iz, ix)]; tr->n++;
           }
           w.S[lin(g, iz, ix)] = 0;
           downtree(w);
@@ -472,17 +590,21 @@ __device__ void march(WarpState &w, const Grid2 &g, const double *V, int fom, in
     // order: a sift compares against the other close nodes' current times, so
     // the writes must not run ahead of the sifts.
     int st = 0;
-    double tnew = 0.0;
+    TT tnew = 0;
     if (valid) {
       st = w.S[lin(g, nz_, nx_)];
       if (st != 0) {
-        if (prec == 0) tnew = fom == 0 ? fouds1(w, g, V, nz_, nx_) : fouds2(w, g, V, nz_, nx_);
-        else tnew = fom == 0 ? fouds1_mixed(w, g, V, nz_, nx_) : fouds2_mixed(w, g, V, nz_, nx_);
+        if constexpr (sizeof(TT) == sizeof(double)) {
+          if (prec == 0) tnew = fom == 0 ? fouds1(w, g, V, nz_, nx_) : fouds2(w, g, V, nz_, nx_);
+          else tnew = fom == 0 ? fouds1_mixed(w, g, V, nz_, nx_) : fouds2_mixed(w, g, V, nz_, nx_);
+        } else {
+          tnew = fouds_fx(w, g, V, nz_, nx_, fom, fx);
+        }
       }
     }
     int code = valid ? (st == -1 ? 1 : (st > 0 ? 2 : 0)) : 0;
     int cd[4];
-    double tn[4];
+    TT tn[4];
 #pragma unroll
     for (int q = 0; q < 4; ++q) {
       cd[q] = __shfl_sync(0xffffffffu, code, q);
@@ -505,7 +627,8 @@ __device__ void march(WarpState &w, const Grid2 &g, const double *V, int fom, in
 }
 
 // Source initialisation of travel (fm2d_ttime.f90:95-127), lane 0.
-__device__ void init_source(WarpState &w, const Grid2 &g, const double *V, double scx, double scz) {
+template <class TT>
+__device__ void init_source(WarpStateT<TT> &w, const Grid2 &g, const double *V, double scx, double scz, const Fx &fx) {
   int isx = (int)((scx - g.gox) / g.dnx) + 1;
   int isz = (int)((scz - g.goz) / g.dnz) + 1;
   if (isx == g.nnx) isx = isx - 1;
@@ -522,7 +645,9 @@ __device__ void init_source(WarpState &w, const Grid2 &g, const double *V, doubl
       double ex = dsx - (double)(i - 1) * g.dnx;
       double ez = dsz - (double)(j - 1) * g.dnz;
       double ds = sqrt(ex * ex + ez * ez);
-      w.T[lin(g, isz - 1 + j, isx - 1 + i)] = 2.0 * ds / (vss[i - 1][j - 1] + vsrc);
+      const double t0 = 2.0 * ds / (vss[i - 1][j - 1] + vsrc);
+      if constexpr (sizeof(TT) == sizeof(double)) w.T[lin(g, isz - 1 + j, isx - 1 + i)] = t0;
+      else w.T[lin(g, isz - 1 + j, isx - 1 + i)] = (int)min(llrint(t0 * (double)fx.scale), (long long)INT_MAX - 1);
       addtree(w, g, isz - 1 + j, isx - 1 + i);
     }
 }
@@ -537,6 +662,8 @@ __device__ __forceinline__ double bsw(int q, double u) {
   }
 }
 
+__global__ void set_int_kernel(int *p, int v) { *p = v; }
+
 // gridder (fm2dray_cartesian.f90:491-600): one block per map.
 __global__ void gridder_kernel(Fm2dJob job) {
   const int map = blockIdx.x;
@@ -544,6 +671,11 @@ __global__ void gridder_kernel(Fm2dJob job) {
   const int ldv = job.nvz + 2;
   const double *velv = job.velv + (size_t)map * (job.nvx + 2) * ldv;
   double *veln = job.veln + (size_t)map * nnx * nnz;
+  if (job.vmin_bits) {
+    float vm = 3.0e38f;
+    for (int q = threadIdx.x; q < (job.nvx + 2) * ldv; q += blockDim.x) vm = fminf(vm, (float)velv[q] * 0.999f);
+    if (vm > 0.f) atomicMin(job.vmin_bits, __float_as_int(vm));
+  }
   for (int node = threadIdx.x; node < nnx * nnz; node += blockDim.x) {
     int stz = node % nnz + 1, stx = node / nnz + 1;
     // invert stz = gdz*(i-1)+l (l in 1..gdz, or gdz+1 in the last cell)
@@ -564,6 +696,7 @@ __global__ void gridder_kernel(Fm2dJob job) {
   }
 }
 
+template <class TT>
 __global__ void __launch_bounds__(32 * WARPS_PER_BLOCK_MAX)
 fm2d_solve_kernel(Fm2dJob job, int warp_bytes) {
   extern __shared__ __align__(16) unsigned char smem[];
@@ -573,11 +706,24 @@ fm2d_solve_kernel(Fm2dJob job, int warp_bytes) {
   const int map = job.solves[solve].x, src = job.solves[solve].y;
   unsigned char *base = smem + (size_t)warp * warp_bytes;
   const int nodes_max = job.nodes_max;
-  WarpState w;
-  w.T = reinterpret_cast<double *>(base);
-  w.S = reinterpret_cast<short *>(base + sizeof(double) * nodes_max);
-  w.H = reinterpret_cast<unsigned short *>(base + (sizeof(double) + sizeof(short)) * nodes_max);
+  WarpStateT<TT> w;
+  w.T = reinterpret_cast<TT *>(base);
+  w.S = reinterpret_cast<short *>(base + sizeof(TT) * nodes_max);
+  w.H = reinterpret_cast<unsigned short *>(base + (sizeof(TT) + sizeof(short)) * nodes_max);
   w.ntr = 0;
+  // fixed-point scale: the largest time is below 3 x diagonal / slowest
+  // velocity; keep it under 2^31 units
+  Fx fx{1.f, 1.f};
+  if constexpr (sizeof(TT) != sizeof(double)) {
+    const float vmin = __int_as_float(*job.vmin_bits);
+    const double ext = sqrt(((job.nvx - 1) * job.dvxd) * ((job.nvx - 1) * job.dvxd) +
+                            ((job.nvz - 1) * job.dvzd) * ((job.nvz - 1) * job.dvzd));
+    const double tmax = 3.0 * ext / (double)vmin;
+    int shift = 30;
+    while (shift > 4 && ldexp(tmax, shift) > 2.0e9) --shift;
+    fx.scale = ldexpf(1.f, shift); fx.inv = ldexpf(1.f, -shift);
+  }
+  const float inv_scale = fx.inv;
   const int nnx = (job.nvx - 1) * job.gdx + 1, nnz = (job.nvz - 1) * job.gdz + 1;
   const double dvx = job.dvxd, dvz = job.dvzd;
   Grid2 gc{nnx, nnz, nnz, job.goxd, job.gozd, dvx / job.gdx, dvz / job.gdz};
@@ -630,10 +776,11 @@ fm2d_solve_kernel(Fm2dJob job, int warp_bytes) {
       }
     }
     for (int q = lane; q < nrnx * nrnz; q += 32) w.S[q] = -1;
+    w.ld = gr.ld;
     __syncwarp();
-    if (lane == 0) init_source(w, gr, Vr, x, z);
+    if (lane == 0) init_source(w, gr, Vr, x, z, fx);
     __syncwarp();
-    march(w, gr, Vr, job.fom, job.precision, 1, vnl, vnr, vnt, vnb, tr);
+    march(w, gr, Vr, job.fom, job.precision, 1, vnl, vnr, vnt, vnb, fx, tr);
     // map refined onto coarse: gather the mapped refined nodes first
     const int mx = (nrnx - 1) / sgdl + 1, mz = (nrnz - 1) / sgdl + 1;   // = vnr-vnl+1, vnb-vnt+1
     double *tmpT = job.map_tmp_t + (size_t)solve * job.map_tmp_max;
@@ -642,7 +789,7 @@ fm2d_solve_kernel(Fm2dJob job, int warp_bytes) {
       int a = q % mz, b = q / mz;
       int k = a * sgdl + 1, l = b * sgdl + 1;
       int r = lin(gr, k, l);
-      tmpT[q] = w.T[r];
+      tmpT[q] = (double)w.T[r];
       tmpS[q] = w.S[r];
     }
     __syncwarp();
@@ -653,7 +800,7 @@ fm2d_solve_kernel(Fm2dJob job, int warp_bytes) {
       int c = lin(gc, vnt + a, vnl + b);
       short s = tmpS[q];
       w.S[c] = s;
-      if (s >= 0) w.T[c] = tmpT[q];
+      if (s >= 0) w.T[c] = (TT)tmpT[q];
     }
     __syncwarp();
     // narrow band repair (fm2dray_cartesian.f90:384-405); order-independent
@@ -667,6 +814,7 @@ fm2d_solve_kernel(Fm2dJob job, int warp_bytes) {
     }
     __syncwarp();
     // travel(urg=2): heap from all nodes marked close, i outer, j inner
+    w.ld = gc.ld;
     if (lane == 0) {
       w.ntr = 0;
       for (int i = 1; i <= nnx; ++i)
@@ -674,18 +822,20 @@ fm2d_solve_kernel(Fm2dJob job, int warp_bytes) {
           if (w.S[lin(gc, j, i)] > 0) addtree(w, gc, j, i);
     }
     __syncwarp();
-    march(w, gc, Vc, job.fom, job.precision, 2, vnl, vnr, vnt, vnb, tr);
+    march(w, gc, Vc, job.fom, job.precision, 2, vnl, vnr, vnt, vnb, fx, tr);
   } else {
     for (int q = lane; q < nnx * nnz; q += 32) w.S[q] = -1;
+    w.ld = gc.ld;
     __syncwarp();
-    if (lane == 0) init_source(w, gc, Vc, x, z);
+    if (lane == 0) init_source(w, gc, Vc, x, z, fx);
     __syncwarp();
-    march(w, gc, Vc, job.fom, job.precision, 0, vnl, vnr, vnt, vnb, tr);
+    march(w, gc, Vc, job.fom, job.precision, 0, vnl, vnr, vnt, vnb, fx, tr);
   }
   // optional travel-time field
   if (job.tfield) {
     double *tf = job.tfield + ((size_t)map * job.nsrc + src) * nnx * nnz;
-    for (int q = lane; q < nnx * nnz; q += 32) tf[q] = w.T[q];
+    for (int q = lane; q < nnx * nnz; q += 32)
+      tf[q] = sizeof(TT) == sizeof(double) ? (double)w.T[q] : (double)w.T[q] * (double)inv_scale;
   }
   // srtimes (fm2dray_cartesian.f90:682-797), one receiver per lane
   const int *srs = job.srs + (size_t)(map % job.srs_nmaps) * job.nsrc * job.nrc + (size_t)src * job.nrc;
@@ -733,7 +883,9 @@ fm2d_solve_kernel(Fm2dJob job, int warp_bytes) {
         for (int l = 1; l <= 2; ++l) {
           double produ = (1.0 - fabs(((double)(l - 1) * gc.dnz - drz) / gc.dnz)) *
                          (1.0 - fabs(((double)(k - 1) * gc.dnx - drx) / gc.dnx));
-          trr = trr + w.T[lin(gc, irz - 1 + l, irx - 1 + k)] * produ;
+          const double tv = sizeof(TT) == sizeof(double) ? (double)w.T[lin(gc, irz - 1 + l, irx - 1 + k)]
+                                                         : (double)w.T[lin(gc, irz - 1 + l, irx - 1 + k)] * (double)inv_scale;
+          trr = trr + tv * produ;
         }
     }
     tt[r] = trr;
@@ -753,7 +905,9 @@ int fm2d_plan(const Fm2dJob &job, Fm2dPlan *plan) {
   }
   int nodes_max = nodes > nref ? nodes : nref;
   if (nodes_max > 32000) return MCT_ERR_ARG;   // int16 heap positions / node ids
-  int wb = nodes_max * (int)(sizeof(double) + sizeof(short) + sizeof(unsigned short)) + 64;
+  if (nnx > 256 || nnz > 256 || (job.asgr == 1 && 2 * job.sgs * job.sgdl + 1 > 256)) return MCT_ERR_ARG;
+  const int tbytes = job.precision == 2 ? (int)sizeof(int) : (int)sizeof(double);
+  int wb = nodes_max * (tbytes + (int)sizeof(short) + (int)sizeof(unsigned short)) + 64;
   wb = (wb + 15) & ~15;
   int wpb = (227 * 1024) / wb;
   if (wpb < 1) return MCT_ERR_ARG;
@@ -769,15 +923,24 @@ int fm2d_plan(const Fm2dJob &job, Fm2dPlan *plan) {
 int launch_fm2d(const Fm2dJob &job, const Fm2dPlan &plan, cudaStream_t s) {
   static bool attr = false;
   if (!attr) {
-    cudaFuncSetAttribute(fm2d_solve_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, 227 * 1024);
+    cudaFuncSetAttribute(fm2d_solve_kernel<double>, cudaFuncAttributeMaxDynamicSharedMemorySize, 227 * 1024);
+    cudaFuncSetAttribute(fm2d_solve_kernel<int>, cudaFuncAttributeMaxDynamicSharedMemorySize, 227 * 1024);
     attr = true;
+  }
+  if (job.precision == 2) {
+    if (!job.vmin_bits) return MCT_ERR_ARG;
+    set_int_kernel<<<1, 1, 0, s>>>(job.vmin_bits, 0x7f7fffff);   // FLT_MAX bits
+    MCT_CUDA_TRY(cudaGetLastError());
   }
   gridder_kernel<<<job.nmaps, 256, 0, s>>>(job);
   MCT_CUDA_TRY(cudaGetLastError());
   if (job.nsolve == 0) return MCT_OK;
   int wpb = plan.warps_per_block;
   int blocks = (job.nsolve + wpb - 1) / wpb;
-  fm2d_solve_kernel<<<blocks, 32 * wpb, (size_t)plan.warp_bytes * wpb, s>>>(job, plan.warp_bytes);
+  if (job.precision == 2)
+    fm2d_solve_kernel<int><<<blocks, 32 * wpb, (size_t)plan.warp_bytes * wpb, s>>>(job, plan.warp_bytes);
+  else
+    fm2d_solve_kernel<double><<<blocks, 32 * wpb, (size_t)plan.warp_bytes * wpb, s>>>(job, plan.warp_bytes);
   MCT_CUDA_TRY(cudaGetLastError());
   return MCT_OK;
 }

@@ -7,7 +7,8 @@ struct Fm2dJob {
   int nvx, nvz;              // B-spline vertex grid
   double goxd, gozd, dvxd, dvzd;
   int gdx, gdz, asgr, sgdl, sgs, fom;
-  int precision;             // 0 FP64 as the reference, 1 FP32 local solves on FP64 times
+  int precision;             // 0 FP64 as the reference, 1 FP32 quadratic on FP64 times, 2 FP32 on fixed-point times
+  int *vmin_bits;            // scratch (precision 2): smallest vertex velocity, float bits
   const double *velv;        // [nmaps][nvx+2][nvz+2] padded vertex grids (Fortran (nvz+2,nvx+2))
   double *veln;              // [nmaps][nnx][nnz] scratch: B-spline node velocities
   double *vref;              // [nsolve][nref_max] scratch: refined source-box velocities

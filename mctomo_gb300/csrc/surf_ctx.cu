@@ -57,7 +57,7 @@ int mct_surf_create(const mct_grid *g, const mct_surf_settings *st, const mct_su
   fj.nvx = g->nx; fj.nvz = g->ny; fj.goxd = g->xmin; fj.gozd = g->ymin; fj.dvxd = g->dx; fj.dvzd = g->dy;
   fj.gdx = st->gridx; fj.gdz = st->gridy; fj.asgr = st->sgref; fj.sgdl = st->sgdic; fj.sgs = st->sgext;
   fj.fom = st->order; fj.nsrc = nsrc; fj.nrc = nrev; fj.srs_nmaps = np;
-  fj.precision = st->tt_precision ? 1 : 0;
+  fj.precision = (st->tt_precision >= 0 && st->tt_precision <= 2) ? st->tt_precision : 0;
   if (fj.gdx < 1 || fj.gdz < 1 || (fj.asgr == 1 && (fj.sgdl < 1 || fj.sgs < 1))) { delete c; return MCT_ERR_ARG; }
   int rc = fm2d_plan(fj, &c->plan.fm2d_plan);
   if (rc) { delete c; return MCT_ERR_ARG; }
@@ -94,7 +94,7 @@ int mct_surf_create(const mct_grid *g, const mct_surf_settings *st, const mct_su
       sizeof(int) * nslots, sizeof(double) * (size_t)nslots * nodes * 3, sizeof(double) * (size_t)nslots * maps,
       // staging
       sizeof(int) * nslots * 3, sizeof(double) * (size_t)nslots * ncell_max * 6, sizeof(double) * 2 * nslots * np,
-      sizeof(double) * 4 * nslots};
+      sizeof(double) * 4 * nslots, sizeof(int)};
   size_t total = 0;
   for (size_t s : sz) total = ((total + 255) & ~size_t(255)) + s;
   total += 256;
@@ -147,6 +147,7 @@ int mct_surf_create(const mct_grid *g, const mct_surf_settings *st, const mct_su
   c->d_n0 = cv.take<double>((size_t)2 * nslots * np);
   c->d_n1 = c->d_n0 + (size_t)nslots * np;
   c->d_out = cv.take<double>((size_t)4 * nslots);
+  fj.vmin_bits = cv.take<int>(1);
   // static data
   std::vector<double> hper(np);
   for (int p = 0; p < np; ++p) hper[p] = 1.0 / dat->freqs[p];   // dble(1/freqs), surfmodes.f90:82

@@ -109,14 +109,16 @@ def test_modrays_source_outside_is_an_error(gpulib):
     assert ei.value.code == -4
 
 
-def test_modrays_mixed_precision_within_tolerance(orc, gpulib):
-    # FP32 quadratic solves on FP64 times: within the 1e-4 s travel-time bound
+@pytest.mark.parametrize("precision", [1, 2])
+def test_modrays_mixed_precision_within_tolerance(orc, gpulib, precision):
+    # FP32 quadratic solves on FP64 (1) or fixed-point (2) times: within the
+    # 1e-4 s travel-time bound of the FP64 path
     rng = np.random.default_rng(8)
     nvx = nvz = 41
     velv = np.stack([voronoi_velv(rng, nvx, nvz, 1.0, 1.0, 40, (0.4, 2.2)) for _ in range(4)])
     st = rng.uniform(2.0, 38.0, (20, 2))
     srs = np.triu(np.ones((20, 20), np.int32), 1)
     exact = modrays_batch(st, st, srs, nvx, nvz, 0.0, 0.0, 1.0, 1.0, velv, sgdl=4, sgs=8, precision=0)
-    mixed = modrays_batch(st, st, srs, nvx, nvz, 0.0, 0.0, 1.0, 1.0, velv, sgdl=4, sgs=8, precision=1)
+    mixed = modrays_batch(st, st, srs, nvx, nvz, 0.0, 0.0, 1.0, 1.0, velv, sgdl=4, sgs=8, precision=precision)
     m = np.broadcast_to(srs == 1, exact.shape)
     assert np.max(np.abs(mixed[m] - exact[m])) <= TT_MIXED_TOL

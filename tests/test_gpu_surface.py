@@ -116,10 +116,11 @@ def test_surface_rejects_models_failing_check_model(gpulib):
     lk.close()
 
 
-def test_surface_mixed_precision_travel_times_within_tolerance(orc, gpulib):
+@pytest.mark.parametrize("tt_precision", [1, 2])
+def test_surface_mixed_precision_travel_times_within_tolerance(orc, gpulib, tt_precision):
     rng, grid, settings, data, ncells, pts, par = small_case(5)
     settings["precision"] = 1
-    settings["tt_precision"] = 1
+    settings["tt_precision"] = tt_precision
     lk = SurfaceLikelihood(grid, settings, data, nslots=4, ncell_max=pts.shape[1])
     npd = len(data["freqs"])
     n0 = np.full((4, npd), 0.02); n1 = np.full((4, npd), 0.01)
