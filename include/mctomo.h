@@ -255,6 +255,48 @@ int mct_eikonal3d_batch(int nsolve, int nx, int ny, int nz, double dx,
                         const double *rev, int order, double *ttime,
                         double *tfield, int *passes);
 
+
+/* ------------------------------------------------------------------------
+ * Body-wave (P and S) likelihood for many chains, replaces likelihood()
+ * cases 0/1 (src/likelihood.f90:57-93) -> body_likelihood
+ * (src/likelihood_body.F90:151-337) and the kdtree_to_grid call before it.
+ * Events are the sources, stations the receivers; solves run from the
+ * stations when events outnumber them (reciprocity), as the reference does.
+ * ---------------------------------------------------------------------- */
+typedef struct {
+  int order;     /* 0 first order, 1 mixed second order */
+  int np;        /* 1: P only (datatype 0), 2: P and S (datatype 1) */
+  int sigdep;    /* 0 data sigma, else sigma = n0*time + n1 */
+} mct_body_settings;
+
+typedef struct {
+  int nsrc, nrev, np;
+  const double *rev;      /* (3, nrev) station x, y, z */
+  const int *raystat;     /* (nsrc*nrev, np): 1 where a pick exists */
+  const double *ttime;    /* (nsrc*nrev, np) observed arrival times */
+  const double *sigma;    /* (nsrc*nrev, np) data sigma, or NULL */
+  int nrays;
+} mct_body_data;
+
+typedef struct mct_body_ctx mct_body_ctx;
+
+int mct_body_create(const mct_grid *grid, const mct_body_settings *settings,
+                    const mct_body_data *data, int nslots, int ncell_max,
+                    mct_body_ctx **ctx);
+int mct_body_destroy(mct_body_ctx *ctx);
+/* points/params [nchains][ncell_max][3] ((x,y,z) and (vp,vs,rho)),
+ * locations [nchains][nsrc][4] event (x, y, z, origin time) (RTI%locations),
+ * n0/n1 [nchains][np]; out [nchains][4] = like, misfit, unweighted misfit,
+ * status. Host pointers, synchronous. */
+int mct_body_forward(mct_body_ctx *ctx, int nchains, const int *ncells,
+                     const double *points, const double *params,
+                     const double *locations, const double *n0,
+                     const double *n1, double *out);
+/* Last forward's travel times (np, nsrc, nrev) = phaseTime(k,j,i) for batch
+ * position index, and the number of tile passes the solves took. */
+int mct_body_phase_time(mct_body_ctx *ctx, int index, double *phase_time,
+                        int *passes);
+
 #ifdef __cplusplus
 }
 #endif

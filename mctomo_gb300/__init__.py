@@ -7,6 +7,7 @@ modrays, fastMarching3D and the likelihood reductions).
 """
 from ._lib import MctError, lib, LIB_PATH  # noqa: F401
 from .surface import SurfaceLikelihood  # noqa: F401
+from .body import BodyLikelihood  # noqa: F401
 from .forward import (  # noqa: F401
     kdtree_to_grid, surfdisp96, surfdisp_mmodes, surfmodes, surfdisp_batch, modrays, modrays_batch, fast_marching3d, eikonal3d_batch,
 )

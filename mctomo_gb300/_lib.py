@@ -37,6 +37,10 @@ SIGNATURES = {
     "mct_modrays_batch": (I, [I, I, P, P, I, P, P, I, P, I, I, D, D, D, D, P, I, I, I, I, I, I, P, P, I]),
     "mct_fast_marching3d": (I, [I, I, I, D, D, D, D, D, D, P, P, P, I, I, P, P]),
     "mct_eikonal3d_batch": (I, [I, I, I, I, D, D, D, D, D, D, I, P, P, P, I, P, I, P, P, P]),
+    "mct_body_create": (I, [P, P, P, I, I, P]),
+    "mct_body_destroy": (I, [P]),
+    "mct_body_forward": (I, [P, I, P, P, P, P, P, P, P]),
+    "mct_body_phase_time": (I, [P, I, P, P]),
     "mct_surf_create": (I, [P, P, P, I, I, P]),
     "mct_surf_destroy": (I, [P]),
     "mct_surf_forward": (I, [P, I, P, P, P, P, P, P, P]),

@@ -1,0 +1,77 @@
+"""Body-wave (P, S) likelihood for many chains (C ABI mct_body_*).
+
+Mirrors the reference's likelihood() for datatypes 0/1
+(src/likelihood.f90:57-93 -> src/likelihood_body.F90:151-337).
+"""
+import ctypes
+
+import numpy as np
+
+from ._lib import check, lib, ptr
+from .surface import Grid
+
+
+class BodySettings(ctypes.Structure):
+    _fields_ = [("order", ctypes.c_int), ("np", ctypes.c_int), ("sigdep", ctypes.c_int)]
+
+
+class BodyData(ctypes.Structure):
+    _fields_ = [("nsrc", ctypes.c_int), ("nrev", ctypes.c_int), ("np", ctypes.c_int),
+                ("rev", ctypes.c_void_p), ("raystat", ctypes.c_void_p), ("ttime", ctypes.c_void_p),
+                ("sigma", ctypes.c_void_p), ("nrays", ctypes.c_int)]
+
+
+class BodyLikelihood:
+    """grid: dict as for SurfaceLikelihood; settings: order, np, sigdep;
+    data: nsrc, rev (nrev, 3), raystat (np, nsrc*nrev), ttime (np, nsrc*nrev),
+    optional sigma."""
+
+    def __init__(self, grid, settings, data, nslots, ncell_max):
+        g = Grid(**grid)
+        s = BodySettings(**settings)
+        self.np = settings["np"]
+        self.nsrc = int(data["nsrc"])
+        rev = np.ascontiguousarray(data["rev"], np.float64)
+        rays = np.ascontiguousarray(data["raystat"], np.int32)
+        tt = np.ascontiguousarray(data["ttime"], np.float64)
+        sig = data.get("sigma")
+        sig = None if sig is None else np.ascontiguousarray(sig, np.float64)
+        self._keep = (rev, rays, tt, sig)
+        self.nrev = rev.shape[0]
+        d = BodyData(self.nsrc, self.nrev, self.np, rev.ctypes.data, rays.ctypes.data, tt.ctypes.data,
+                     None if sig is None else sig.ctypes.data, int(data.get("nrays", int((rays == 1).sum()))))
+        self.ncell_max = ncell_max
+        h = ctypes.c_void_p()
+        check("mct_body_create", lib().mct_body_create(ctypes.byref(g), ctypes.byref(s), ctypes.byref(d),
+                                                       nslots, ncell_max, ctypes.byref(h)))
+        self.h = h
+
+    def close(self):
+        if self.h:
+            lib().mct_body_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def forward(self, ncells, points, params, locations, n0, n1):
+        ncells = np.ascontiguousarray(ncells, np.int32)
+        nch = ncells.size
+        points = np.ascontiguousarray(points, np.float64)
+        params = np.ascontiguousarray(params, np.float64)
+        locations = np.ascontiguousarray(locations, np.float64).reshape(nch, self.nsrc, 4)
+        n0 = np.ascontiguousarray(n0, np.float64).reshape(nch, self.np)
+        n1 = np.ascontiguousarray(n1, np.float64).reshape(nch, self.np)
+        out = np.zeros((nch, 4))
+        check("mct_body_forward", lib().mct_body_forward(self.h, nch, ptr(ncells), ptr(points), ptr(params),
+                                                         ptr(locations), ptr(n0), ptr(n1), ptr(out)))
+        return out
+
+    def phase_time(self, index):
+        pt = np.zeros((self.np, self.nsrc, self.nrev))
+        passes = ctypes.c_int()
+        check("mct_body_phase_time", lib().mct_body_phase_time(self.h, index, ptr(pt), ctypes.byref(passes)))
+        return pt, passes.value

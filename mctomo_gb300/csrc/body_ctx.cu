@@ -1,0 +1,292 @@
+// Batched body-wave (P and S) likelihood: the GPU replacement of
+// likelihood() cases 0/1 (src/likelihood.f90:57-93) -> body_likelihood
+// (src/likelihood_body.F90:151-337), with the kdtree_to_grid call the
+// sampler makes before it.
+//
+// Per forward and chain: nearest-nucleus gridding of vp and vs; one 3D
+// travel-time solve per station and phase when there are more events than
+// stations (reciprocity, likelihood_body.F90:226-250), otherwise one per
+// event; trilinear times at the other end of every path; then sigma and the
+// misfit / -log L with the events' origin times (:284-333). The z axis is
+// scaled by the grid's scaling factor as the reference's call does
+// (dz/scaling, zmin/scaling).
+#include "mct_common.cuh"
+#include "eikonal3d.cuh"
+#include "../../include/mctomo.h"
+#include <vector>
+#include <cfloat>
+#include <cmath>
+
+namespace {
+
+__global__ void body_material_kernel(int ncell_max, const int *ncells, const double *in, double *out) {
+  const int c = blockIdx.y;
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < ncell_max; i += gridDim.x * blockDim.x) {
+    size_t o = ((size_t)c * ncell_max + i) * 3;
+    bool live = i < ncells[c];
+    out[o] = live ? in[o] : 1.0; out[o + 1] = live ? in[o + 1] : 1.0; out[o + 2] = live ? in[o + 2] : 1.0;
+  }
+}
+
+// Solve sources and receiver sets for every (chain, phase, station|event).
+__global__ void body_geometry_kernel(int nchains, int nph, int nsrc, int nrev, int from_rev, const double *rev,
+                                     const double *loc, double xmin, double ymin, double zmin_s, int nslots,
+                                     double *src_out, int *grid_out, double *recv_out, int *recv_set) {
+  const int per_chain = nph * (from_rev ? nrev : nsrc);
+  const int total = nchains * per_chain;
+  for (int q = blockIdx.x * blockDim.x + threadIdx.x; q < total; q += gridDim.x * blockDim.x) {
+    int c = q / per_chain, r = q % per_chain;
+    int ph = r / (from_rev ? nrev : nsrc), e = r % (from_rev ? nrev : nsrc);
+    const double *p = from_rev ? rev + 3 * e : loc + ((size_t)c * nsrc + e) * 4;
+    src_out[3 * q] = p[0] - xmin; src_out[3 * q + 1] = p[1] - ymin; src_out[3 * q + 2] = p[2] - zmin_s;
+    grid_out[q] = ph == 0 ? c : nslots + c;      // vp grids, then vs grids
+    recv_set[q] = c;
+  }
+  // receiver sets: per chain, the other end of every path
+  const int nrecv = from_rev ? nsrc : nrev;
+  for (int q = blockIdx.x * blockDim.x + threadIdx.x; q < nchains * nrecv; q += gridDim.x * blockDim.x) {
+    int c = q / nrecv, k = q % nrecv;
+    const double *p = from_rev ? loc + ((size_t)c * nsrc + k) * 4 : rev + 3 * k;
+    recv_out[3 * q] = p[0] - xmin; recv_out[3 * q + 1] = p[1] - ymin; recv_out[3 * q + 2] = p[2] - zmin_s;
+  }
+}
+
+struct BodyDev {
+  int nsrc, nrev, np, nrays, sigdep, from_rev;
+  const int *raystat; const double *dtime, *dsigma;
+};
+
+// misfit with origin times (likelihood_body.F90:284-333), one block per chain
+__global__ void body_misfit_kernel(BodyDev d, int nchains, const double *tt, const double *loc, const double *n0,
+                                   const double *n1, double *ptime, double *out) {
+  const int c = blockIdx.x;
+  const int npairs = d.nsrc * d.nrev;
+  const int nsol = d.from_rev ? d.nrev : d.nsrc, nrecv = d.from_rev ? d.nsrc : d.nrev;
+  double like = 0, mis = 0, umis = 0, slog = 0;
+  int bad = 0;
+  for (int q = threadIdx.x; q < d.np * npairs; q += blockDim.x) {
+    int p = q / npairs, r = q % npairs;
+    int j = r / d.nrev, k = r % d.nrev;             // source j, receiver k (nrr = k + (j-1)*nrev)
+    int sol = d.from_rev ? k : j, end = d.from_rev ? j : k;
+    double t = tt[(((size_t)c * d.np + p) * nsol + sol) * nrecv + end];   // phaseTime(k,j,p)
+    ptime[((size_t)c * d.np + p) * npairs + r] = t;
+    bool used = d.raystat[(size_t)p * npairs + r] == 1;
+    double sig = used ? (d.sigdep ? n0[(size_t)c * d.np + p] * t + n1[(size_t)c * d.np + p]
+                                  : d.dsigma[(size_t)p * npairs + r]) : 1.0;
+    if (used) {
+      if (sig < 2.2250738585072014e-307) bad = 1;
+      double res = t + loc[((size_t)c * d.nsrc + j) * 4 + 3] - d.dtime[(size_t)p * npairs + r];
+      double r2 = res * res;
+      like += r2 / (2 * (sig * sig));
+      mis += r2 / (sig * sig);
+      umis += r2;
+    }
+    slog += log(sig);
+  }
+  __shared__ double red[4][256];
+  __shared__ int sbad;
+  if (threadIdx.x == 0) sbad = 0;
+  __syncthreads();
+  if (bad) sbad = 1;
+  red[0][threadIdx.x] = like; red[1][threadIdx.x] = mis; red[2][threadIdx.x] = umis; red[3][threadIdx.x] = slog;
+  __syncthreads();
+  for (int s = blockDim.x / 2; s > 0; s >>= 1) {
+    if (threadIdx.x < s)
+      for (int k = 0; k < 4; ++k) red[k][threadIdx.x] += red[k][threadIdx.x + s];
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) {
+    const double PI2 = (double)6.283185f;
+    double L = red[0][0] + red[3][0] + (double)((float)d.nrays / 2.0f) * log(PI2);
+    out[(size_t)c * 4 + 0] = sbad ? DBL_MAX : L;
+    out[(size_t)c * 4 + 1] = red[1][0];
+    out[(size_t)c * 4 + 2] = red[2][0];
+    out[(size_t)c * 4 + 3] = sbad ? 8.0 : 0.0;
+  }
+}
+
+}  // namespace
+
+struct mct_body_ctx {
+  mct_grid g{};
+  int order = 0, np = 1, sigdep = 1, nslots = 0, ncell_max = 0;
+  BodyDev dev{};
+  cudaStream_t stream = nullptr;
+  void *mem = nullptr;
+  // device buffers
+  int *ncells = nullptr; double *points = nullptr, *params_in = nullptr, *params = nullptr, *loc = nullptr;
+  double *n0 = nullptr, *n1 = nullptr, *out = nullptr, *rev = nullptr;
+  int *sites = nullptr; double *vel = nullptr; float *slow = nullptr;
+  int *tie_count = nullptr, *tie_nodes = nullptr; void *kd = nullptr; int *gstatus = nullptr;
+  double *esrc = nullptr, *erecv = nullptr, *ett = nullptr, *ptime = nullptr;
+  int *egrid = nullptr, *eset = nullptr, *T = nullptr, *list = nullptr, *count = nullptr;
+  unsigned char *flags = nullptr;
+  int last_nchains = 0, last_passes = 0;
+};
+
+extern "C" {
+
+int mct_body_create(const mct_grid *g, const mct_body_settings *st, const mct_body_data *dat, int nslots,
+                    int ncell_max, mct_body_ctx **out) {
+  if (!g || !st || !dat || !out || nslots < 1 || ncell_max < 1 || ncell_max > 12800) return MCT_ERR_ARG;
+  if (g->nx < 2 || g->ny < 2 || g->nz < 2 || !(g->dx > 0) || !(g->dy > 0) || !(g->dz > 0) || !(g->scaling > 0))
+    return MCT_ERR_ARG;
+  if (st->np != 1 && st->np != 2) return MCT_ERR_ARG;
+  if (st->order != 0 && st->order != 1) return MCT_ERR_ARG;
+  if (dat->nsrc < 1 || dat->nrev < 1 || dat->np != st->np) return MCT_ERR_ARG;
+  *out = nullptr;
+  mct_body_ctx *c = new mct_body_ctx();
+  c->g = *g; c->order = st->order; c->np = st->np; c->sigdep = st->sigdep; c->nslots = nslots; c->ncell_max = ncell_max;
+  const int nsrc = dat->nsrc, nrev = dat->nrev, np = dat->np, npairs = nsrc * nrev;
+  const int from_rev = nsrc > nrev ? 1 : 0;   // likelihood_body.F90:204,226
+  const int nsol = from_rev ? nrev : nsrc, nrecv = from_rev ? nsrc : nrev;
+  const size_t nn = (size_t)g->nx * g->ny * g->nz;
+  const size_t nsolve = (size_t)nslots * np * nsol;
+  Eik3Job tmp{}; tmp.nx = g->nx; tmp.ny = g->ny; tmp.nz = g->nz;
+  const size_t ntile = eik3_tiles(tmp);
+  const size_t kd = kd_scratch_bytes(ncell_max);
+  std::vector<size_t> sz = {
+      sizeof(int) * nslots, sizeof(double) * (size_t)nslots * ncell_max * 3 * 3, sizeof(double) * (size_t)nslots * nsrc * 4,
+      sizeof(double) * 2 * (size_t)nslots * np, sizeof(double) * 4 * nslots, sizeof(double) * 3 * nrev,
+      sizeof(int) * (size_t)nslots * nn, sizeof(double) * 2 * (size_t)nslots * nn, sizeof(float) * 2 * (size_t)nslots * nn,
+      sizeof(int) * nslots, sizeof(int) * (size_t)nslots * nn, kd * nslots, sizeof(int) * 2,
+      sizeof(double) * 3 * nsolve, sizeof(double) * 3 * (size_t)nslots * nrecv, sizeof(double) * nsolve * nrecv,
+      sizeof(double) * (size_t)nslots * np * npairs, sizeof(int) * nsolve, sizeof(int) * nsolve,
+      sizeof(int) * nsolve * nn, ntile * nsolve, sizeof(int) * ntile * nsolve, sizeof(int),
+      sizeof(int) * np * npairs, sizeof(double) * 2 * np * npairs};
+  size_t total = 0;
+  for (size_t s : sz) total = ((total + 255) & ~size_t(255)) + s;
+  total += 256;
+  if (cudaMalloc(&c->mem, total) != cudaSuccess) { delete c; return MCT_ERR_NOMEM; }
+  if (cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking) != cudaSuccess) {
+    cudaFree(c->mem); delete c; return MCT_ERR_CUDA;
+  }
+  Carve cv(c->mem);
+  c->ncells = cv.take<int>(nslots);
+  c->points = cv.take<double>((size_t)nslots * ncell_max * 9);
+  c->params_in = c->points + (size_t)nslots * ncell_max * 3;
+  c->params = c->params_in + (size_t)nslots * ncell_max * 3;
+  c->loc = cv.take<double>((size_t)nslots * nsrc * 4);
+  c->n0 = cv.take<double>((size_t)2 * nslots * np); c->n1 = c->n0 + (size_t)nslots * np;
+  c->out = cv.take<double>((size_t)4 * nslots);
+  c->rev = cv.take<double>((size_t)3 * nrev);
+  c->sites = cv.take<int>((size_t)nslots * nn);
+  c->vel = cv.take<double>((size_t)2 * nslots * nn);
+  c->slow = cv.take<float>((size_t)2 * nslots * nn);
+  c->tie_count = cv.take<int>(nslots);
+  c->tie_nodes = cv.take<int>((size_t)nslots * nn);
+  c->kd = cv.take<char>(kd * nslots);
+  c->gstatus = cv.take<int>(2);
+  c->esrc = cv.take<double>(3 * nsolve);
+  c->erecv = cv.take<double>((size_t)3 * nslots * nrecv);
+  c->ett = cv.take<double>(nsolve * nrecv);
+  c->ptime = cv.take<double>((size_t)nslots * np * npairs);
+  c->egrid = cv.take<int>(nsolve);
+  c->eset = cv.take<int>(nsolve);
+  c->T = cv.take<int>(nsolve * nn);
+  c->flags = cv.take<unsigned char>(ntile * nsolve);
+  c->list = cv.take<int>(ntile * nsolve);
+  c->count = cv.take<int>(1);
+  int *rays = cv.take<int>((size_t)np * npairs);
+  double *dt = cv.take<double>((size_t)2 * np * npairs);
+  std::vector<double> hs((size_t)np * npairs, 1.0);
+  if (dat->sigma) for (size_t q = 0; q < hs.size(); ++q) hs[q] = dat->sigma[q];
+  cudaMemcpy(c->rev, dat->rev, sizeof(double) * 3 * nrev, cudaMemcpyHostToDevice);
+  cudaMemcpy(rays, dat->raystat, sizeof(int) * np * npairs, cudaMemcpyHostToDevice);
+  cudaMemcpy(dt, dat->ttime, sizeof(double) * np * npairs, cudaMemcpyHostToDevice);
+  cudaMemcpy(dt + (size_t)np * npairs, hs.data(), sizeof(double) * np * npairs, cudaMemcpyHostToDevice);
+  if (cudaDeviceSynchronize() != cudaSuccess) { cudaFree(c->mem); cudaStreamDestroy(c->stream); delete c; return MCT_ERR_CUDA; }
+  c->dev = BodyDev{nsrc, nrev, np, dat->nrays, st->sigdep, from_rev, rays, dt, dt + (size_t)np * npairs};
+  *out = c;
+  return MCT_OK;
+}
+
+int mct_body_destroy(mct_body_ctx *c) {
+  if (!c) return MCT_OK;
+  cudaStreamSynchronize(c->stream);
+  cudaFree(c->mem);
+  cudaStreamDestroy(c->stream);
+  delete c;
+  return MCT_OK;
+}
+
+int mct_body_forward(mct_body_ctx *c, int nchains, const int *ncells, const double *points, const double *params,
+                     const double *locations, const double *n0, const double *n1, double *out) {
+  if (!c || nchains < 1 || nchains > c->nslots) return MCT_ERR_ARG;
+  for (int i = 0; i < nchains; ++i) if (ncells[i] < 1 || ncells[i] > c->ncell_max) return MCT_ERR_ARG;
+  const mct_grid &g = c->g;
+  const BodyDev &d = c->dev;
+  cudaStream_t s = c->stream;
+  const size_t nn = (size_t)g.nx * g.ny * g.nz;
+  const size_t pc = (size_t)nchains * c->ncell_max * 3;
+  MCT_CUDA_TRY(cudaMemcpyAsync(c->ncells, ncells, sizeof(int) * nchains, cudaMemcpyHostToDevice, s));
+  MCT_CUDA_TRY(cudaMemcpyAsync(c->points, points, sizeof(double) * pc, cudaMemcpyHostToDevice, s));
+  MCT_CUDA_TRY(cudaMemcpyAsync(c->params_in, params, sizeof(double) * pc, cudaMemcpyHostToDevice, s));
+  MCT_CUDA_TRY(cudaMemcpyAsync(c->loc, locations, sizeof(double) * nchains * d.nsrc * 4, cudaMemcpyHostToDevice, s));
+  MCT_CUDA_TRY(cudaMemcpyAsync(c->n0, n0, sizeof(double) * nchains * d.np, cudaMemcpyHostToDevice, s));
+  MCT_CUDA_TRY(cudaMemcpyAsync(c->n1, n1, sizeof(double) * nchains * d.np, cudaMemcpyHostToDevice, s));
+  MCT_CUDA_TRY(cudaMemsetAsync(c->gstatus, 0, sizeof(int) * 2, s));
+  body_material_kernel<<<dim3((c->ncell_max + 127) / 128, nchains), 128, 0, s>>>(c->ncell_max, c->ncells,
+                                                                                   c->params_in, c->params);
+  MCT_CUDA_TRY(cudaGetLastError());
+  // gridding: vp into grids [0, nslots), vs into [nslots, 2 nslots)
+  GridJob gj{};
+  gj.d = 3; gj.nx = g.nx; gj.ny = g.ny; gj.nz = g.nz;
+  gj.xmin = g.xmin; gj.ymin = g.ymin; gj.zmin = g.zmin; gj.dx = g.dx; gj.dy = g.dy; gj.dz = g.dz;
+  gj.nchains = nchains; gj.ncell_max = c->ncell_max; gj.ncells = c->ncells;
+  gj.points = c->points; gj.params = c->params; gj.box = nullptr;
+  gj.sites_id = c->sites; gj.vp = c->vel; gj.vs = c->vel + (size_t)c->nslots * nn;
+  gj.rho = reinterpret_cast<double *>(c->slow);   // density is not used by the body path: scratch target
+  gj.tie_count = c->tie_count; gj.tie_nodes = c->tie_nodes; gj.kd_scratch = c->kd; gj.status = c->gstatus;
+  int rc = launch_grid_nearest(gj, s); if (rc) return rc;
+  // solves
+  const int nsol = d.from_rev ? d.nrev : d.nsrc, nrecv = d.from_rev ? d.nsrc : d.nrev;
+  const int nsolve = nchains * d.np * nsol;
+  body_geometry_kernel<<<64, 256, 0, s>>>(nchains, d.np, d.nsrc, d.nrev, d.from_rev, c->rev, c->loc, g.xmin, g.ymin,
+                                           g.zmin / g.scaling, c->nslots, c->esrc, c->egrid, c->erecv, c->eset);
+  MCT_CUDA_TRY(cudaGetLastError());
+  // velocity bound for the fixed-point scale (smallest nucleus velocity)
+  std::vector<double> hp(pc);
+  MCT_CUDA_TRY(cudaMemcpyAsync(hp.data(), c->params, sizeof(double) * pc, cudaMemcpyDeviceToHost, s));
+  MCT_CUDA_TRY(cudaStreamSynchronize(s));
+  double vmin = 1e300;
+  for (int ch = 0; ch < nchains; ++ch)
+    for (int i = 0; i < ncells[ch]; ++i) {
+      const double *q = &hp[((size_t)ch * c->ncell_max + i) * 3];
+      if (q[0] > 0 && q[0] < vmin) vmin = q[0];
+      if (d.np > 1 && q[1] > 0 && q[1] < vmin) vmin = q[1];
+    }
+  const double dzs = g.dz / g.scaling;
+  const double diag = sqrt(((g.nx - 1) * g.dx) * ((g.nx - 1) * g.dx) + ((g.ny - 1) * g.dy) * ((g.ny - 1) * g.dy) +
+                           ((g.nz - 1) * dzs) * ((g.nz - 1) * dzs));
+  Eik3Job job{};
+  job.nsolve = nsolve; job.nx = g.nx; job.ny = g.ny; job.nz = g.nz; job.dx = g.dx; job.dy = g.dy; job.dz = dzs;
+  job.vel = c->vel; job.slow = c->slow; job.ngrids = 2 * c->nslots; job.solve_grid = c->egrid; job.src = c->esrc;
+  job.order = c->order; job.shift = eik3_shift_for(4.0 * diag / vmin);
+  job.T = c->T; job.flags = c->flags; job.list = c->list; job.count = c->count;
+  job.nrev = nrecv; job.rev = c->erecv; job.rev_per_solve = 1; job.solve_rev = c->eset; job.ttime = c->ett;
+  int passes = 0;
+  rc = launch_eik3(job, s, 100000, &passes, nullptr); if (rc) return rc;
+  c->last_passes = passes;
+  body_misfit_kernel<<<nchains, 256, 0, s>>>(d, nchains, c->ett, c->loc, c->n0, c->n1, c->ptime, c->out);
+  MCT_CUDA_TRY(cudaGetLastError());
+  MCT_CUDA_TRY(cudaMemcpyAsync(out, c->out, sizeof(double) * 4 * nchains, cudaMemcpyDeviceToHost, s));
+  int gst[2];
+  MCT_CUDA_TRY(cudaMemcpyAsync(gst, c->gstatus, sizeof(int) * 2, cudaMemcpyDeviceToHost, s));
+  MCT_CUDA_TRY(cudaStreamSynchronize(s));
+  c->last_nchains = nchains;
+  if (gst[0]) return gst[0];
+  return MCT_OK;
+}
+
+int mct_body_phase_time(mct_body_ctx *c, int index, double *phase_time, int *passes) {
+  if (!c || index < 0 || index >= c->last_nchains) return MCT_ERR_ARG;
+  const size_t n = (size_t)c->dev.np * c->dev.nsrc * c->dev.nrev;
+  MCT_CUDA_TRY(cudaStreamSynchronize(c->stream));
+  if (phase_time) MCT_CUDA_TRY(cudaMemcpy(phase_time, c->ptime + (size_t)index * n, sizeof(double) * n,
+                                          cudaMemcpyDeviceToHost));
+  if (passes) *passes = c->last_passes;
+  return MCT_OK;
+}
+
+}  // extern "C"

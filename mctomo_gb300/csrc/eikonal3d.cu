@@ -309,7 +309,7 @@ __global__ void readout_kernel(Eik3Job job) {
   const int *T = job.T + (size_t)s * nn;
   const double h[3] = {job.dx, job.dy, job.dz};
   const double inv = ldexp(1.0, -job.shift);
-  const int rs = job.rev_per_solve ? s : 0;
+  const int rs = job.solve_rev ? job.solve_rev[s] : (job.rev_per_solve ? s : 0);
   for (int r = blockIdx.x * blockDim.x + threadIdx.x; r < job.nrev; r += gridDim.x * blockDim.x) {
     const double *p = job.rev + ((size_t)rs * job.nrev + r) * 3;
     double pt[3] = {p[0], p[1], p[2]};

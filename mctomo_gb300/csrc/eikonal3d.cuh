@@ -18,8 +18,9 @@ struct Eik3Job {
   unsigned char *flags;           // [nsolve][tiles] scratch
   int *list, *count;              // scratch: active (solve, tile) list
   int nrev;                       // receivers per solve
-  const double *rev;              // [rev_per_solve ? nsolve : 1][nrev][3] relative to the origin
-  int rev_per_solve;
+  const double *rev;              // [sets][nrev][3] relative to the origin
+  int rev_per_solve;              // 1: set = solve index (unless solve_rev given)
+  const int *solve_rev;           // optional [nsolve]: receiver set of each solve
   double *ttime;                  // [nsolve][nrev]
 };
 

@@ -116,3 +116,30 @@ def perturb_chain_models(rng, ncells, points, params, grid, vs_range=(0.3, 2.5))
         params[c, order, 1] = vs
         params[c, :n, 0] = params[c, :n, 1] * np.float64(np.float32(1.73))
     return points, params
+
+
+def body_workload(rng, nx=101, ny=101, nz=51, extent=(50.0, 50.0, 25.0), nevents=200, nstations=60, np_=2):
+    """The 3D body-wave configuration: events at seeded uniform positions at
+    1-20 km depth with origin times uniform on [0, 1] s, stations at the
+    surface kept off the grid's maximum x/y faces (where the reference's
+    trilinear read-out multiplies times), P and S picks for every pair, noise
+    sigma 0.03 s (P) / 0.06 s (S). Observed times are straight-ray times at
+    6 / 3.5 km/s plus noise and origin time. Returns grid, settings, data,
+    event locations (nevents, 4)."""
+    grid = dict(nx=nx, ny=ny, nz=nz, xmin=0.0, ymin=0.0, zmin=0.0,
+                dx=extent[0] / (nx - 1), dy=extent[1] / (ny - 1), dz=extent[2] / (nz - 1),
+                scaling=1.0, water_depth=0.0)
+    ev = np.column_stack([rng.uniform(0.02, 0.98, nevents) * extent[0], rng.uniform(0.02, 0.98, nevents) * extent[1],
+                          rng.uniform(1.0, 20.0, nevents), rng.uniform(0.0, 1.0, nevents)])
+    sta = np.column_stack([rng.uniform(0.02, 0.95, nstations) * extent[0],
+                           rng.uniform(0.02, 0.95, nstations) * extent[1], np.zeros(nstations)])
+    dist = np.sqrt(((ev[:, None, :3] - sta[None, :, :]) ** 2).sum(-1)).reshape(-1)   # (src j, rev k)
+    sig = np.array([0.03, 0.06])[:np_]
+    vel = np.array([6.0, 3.5])[:np_]
+    t0 = np.repeat(ev[:, 3], nstations)
+    ttime = np.stack([dist / vel[p] + t0 + sig[p] * rng.standard_normal(dist.size) for p in range(np_)])
+    raystat = np.ones((np_, dist.size), np.int32)
+    settings = dict(order=1, np=np_, sigdep=0)
+    sigma = np.stack([np.full(dist.size, sig[p]) for p in range(np_)])
+    data = dict(nsrc=nevents, rev=sta, raystat=raystat, ttime=ttime, sigma=sigma, nrays=int(raystat.sum()))
+    return grid, settings, data, ev
