@@ -42,7 +42,7 @@ CONFIG = {"workload": "batched 3D surface-wave rjMCMC: 64 chains, 41x41x31 grid 
                       "1225 paths/period, move proposals committed each step",
           "chains": NCHAINS, "grid": [41, 41, 31], "periods": 20, "stations": 50,
           "paths_per_period": 1225, "dispersion_root_search": "FP32 bracketing + FP64 polish",
-          "fm2d": "reference marching order, FP32 updates on fixed-point times",
+          "fm2d": "reference marching order, double-float (FP32 pair) updates",
           "l2": "flushed (512 MB write) between steps"}
 
 
@@ -250,7 +250,7 @@ def run_gpu(args):
     line = {
         "metric": METRIC, "value": round(value, 3), "unit": "proposal evals/s", "n_gpus": ws,
         "steps": K, "warmup": W, "ms_per_step": round(total_ms / K, 4), "higher_is_better": True,
-        "scaling": "weak", "vs_baseline": None, "dtype": "f64 dispersion polish; f32 dispersion bracketing and fm2d updates on int32 fixed-point times",
+        "scaling": "weak", "vs_baseline": None, "dtype": "f64 dispersion polish; f32 dispersion bracketing; double-float (f32 pairs) fm2d",
         "data": "synthetic (seeded, shapes of the configuration)", "config": CONFIG,
         "e2e": {"value": round(e2e_value, 3), "unit": "proposal evals/s", "h2d_bytes_per_step": h2d,
                 "d2h_bytes_per_step": d2h},
@@ -368,7 +368,7 @@ def main():
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--cpu-sample", type=int, default=8)
     ap.add_argument("--no-cpu", action="store_true")
-    ap.add_argument("--tt-precision", type=int, default=2)
+    ap.add_argument("--tt-precision", type=int, default=1)
     args = ap.parse_args()
     if args.impl == "reference":
         run_reference(args)

@@ -18,6 +18,7 @@
 #include "mct_common.cuh"
 #include "fm2d.cuh"
 #include <climits>
+#include <type_traits>
 
 namespace {
 
@@ -46,8 +47,10 @@ template <class TT> __device__ __forceinline__ int plin(const WarpStateT<TT> &w,
 // Travel times are finite and non-negative, so the IEEE bit patterns of the
 // FP64 times order exactly like the values: the heap compares them on the
 // integer pipe. Fixed-point times compare directly.
-__device__ __forceinline__ long long tkey(const double *T, int node) { return __double_as_longlong(T[node]); }
-__device__ __forceinline__ int tkey(const int *T, int node) { return T[node]; }
+__device__ __forceinline__ bool tlt(double a, double b) { return __double_as_longlong(a) < __double_as_longlong(b); }
+__device__ __forceinline__ bool tlt(int a, int b) { return a < b; }
+// double-float times (hi, lo) are normalised, so they order lexicographically
+__device__ __forceinline__ bool tlt(float2 a, float2 b) { return a.x < b.x || (a.x == b.x && a.y < b.y); }
 
 // ---- binary heap (fm2d_ttime.f90:527-680), lane 0 only --------------------
 template <class TT>
@@ -58,11 +61,11 @@ __device__ void addtree(WarpStateT<TT> &w, const Grid2 &g, int iz, int ix) {
   w.S[me] = (short)w.ntr;
   w.H[w.ntr] = pm;
   int tpc = w.ntr, tpp = tpc / 2;
-  const auto tme = tkey(w.T, me);
+  const TT tme = w.T[me];
   while (tpp > 0) {
     const int pp = w.H[tpp];
     const int pn = plin(w, pp);
-    if (tme < tkey(w.T, pn)) {
+    if (tlt(tme, w.T[pn])) {
       w.S[me] = (short)tpp;
       w.S[pn] = (short)tpc;
       w.H[tpc] = (unsigned short)pp;
@@ -84,12 +87,12 @@ __device__ void downtree(WarpStateT<TT> &w) {
   int tpp = 1, tpc = 2 * tpp;
   const int ntr = w.ntr;
   while (tpc < ntr) {
-    const auto rd1 = tkey(w.T, plin(w, w.H[tpc]));
-    const auto rd2 = tkey(w.T, plin(w, w.H[tpc + 1]));
-    if (rd1 > rd2) tpc = tpc + 1;
+    const TT rd1 = w.T[plin(w, w.H[tpc])];
+    const TT rd2 = w.T[plin(w, w.H[tpc + 1])];
+    if (tlt(rd2, rd1)) tpc = tpc + 1;
     const int cp = w.H[tpc], pp = w.H[tpp];
     const int cn = plin(w, cp), pn = plin(w, pp);
-    if (tkey(w.T, cn) < tkey(w.T, pn)) {
+    if (tlt(w.T[cn], w.T[pn])) {
       w.S[pn] = (short)tpc;
       w.S[cn] = (short)tpp;
       w.H[tpc] = (unsigned short)pp;
@@ -102,7 +105,7 @@ __device__ void downtree(WarpStateT<TT> &w) {
   if (tpc == ntr) {
     const int cp = w.H[tpc], pp = w.H[tpp];
     const int cn = plin(w, cp), pn = plin(w, pp);
-    if (tkey(w.T, cn) < tkey(w.T, pn)) {
+    if (tlt(w.T[cn], w.T[pn])) {
       w.S[pn] = (short)tpc;
       w.S[cn] = (short)tpp;
       w.H[tpc] = (unsigned short)pp;
@@ -116,11 +119,11 @@ __device__ void updtree(WarpStateT<TT> &w, const Grid2 &g, int iz, int ix) {
   const int me = lin(g, iz, ix);
   const unsigned short pm = pack(iz, ix);
   int tpc = w.S[me], tpp = tpc / 2;
-  const auto tme = tkey(w.T, me);
+  const TT tme = w.T[me];
   while (tpp > 0) {
     const int pp = w.H[tpp];
     const int pn = plin(w, pp);
-    if (tme < tkey(w.T, pn)) {
+    if (tlt(tme, w.T[pn])) {
       w.S[me] = (short)tpp;
       w.S[pn] = (short)tpc;
       w.H[tpc] = (unsigned short)pp;
@@ -279,156 +282,189 @@ __device__ double fouds2(const WarpState &w, const Grid2 &g, const double *V, in
 }
 
 
-// Mixed-precision variants (precision == 1): the same stencils and case
-// selection, with the quadratic solved in FP32 on travel times shifted by a
-// nearby accepted time `base` (one FP64 subtraction per neighbour and one
-// FP64 addition for the result). Every stencil is shift-invariant: em is a
-// difference and tref's coefficients sum to tdiv, so
-// trav = base + (tref' + tdsh) / tdiv with tref' the shifted tref.
+
+// Double-float variant (precision == 1): times are unevaluated sums of two
+// FP32 numbers (hi + lo, |lo| <= ulp(hi)/2) and every operation of the
+// reference's update is carried out in that format with error-free
+// transformations (Knuth's two-sum, Dekker's two-product via fmaf, Newton
+// steps for division and square root), giving about 2^-48 relative precision
+// on the FP32 pipe. Results agree with the FP64 reference to ~1e-13 s, so the
+// acceptance order only differs on ties closer than that.
+struct DF { float hi, lo; };
+__device__ __forceinline__ DF df(float a) { return DF{a, 0.f}; }
+__device__ __forceinline__ DF df_from(double d) { float h = (float)d; return DF{h, (float)(d - (double)h)}; }
+__device__ __forceinline__ double df_to(DF a) { return (double)a.hi + (double)a.lo; }
+__device__ __forceinline__ DF two_sum(float a, float b) {
+  float s = a + b, bb = s - a;
+  return DF{s, (a - (s - bb)) + (b - bb)};
+}
+__device__ __forceinline__ DF quick_two_sum(float a, float b) {
+  float s = a + b;
+  return DF{s, b - (s - a)};
+}
+__device__ __forceinline__ DF dadd(DF a, DF b) {
+  DF s = two_sum(a.hi, b.hi), t = two_sum(a.lo, b.lo);
+  s.lo += t.hi;
+  s = quick_two_sum(s.hi, s.lo);
+  s.lo += t.lo;
+  return quick_two_sum(s.hi, s.lo);
+}
+__device__ __forceinline__ DF dneg(DF a) { return DF{-a.hi, -a.lo}; }
+__device__ __forceinline__ DF dsub(DF a, DF b) { return dadd(a, dneg(b)); }
+__device__ __forceinline__ DF dmul(DF a, DF b) {
+  float p = a.hi * b.hi;
+  float e = fmaf(a.hi, b.hi, -p);
+  e += a.hi * b.lo + a.lo * b.hi;
+  return quick_two_sum(p, e);
+}
+__device__ __forceinline__ DF dmulf(DF a, float f) {
+  float p = a.hi * f;
+  float e = fmaf(a.hi, f, -p);
+  e += a.lo * f;
+  return quick_two_sum(p, e);
+}
+__device__ __forceinline__ DF ddiv(DF a, DF b) {
+  float q1 = a.hi / b.hi;
+  DF r = dsub(a, dmulf(b, q1));
+  float q2 = r.hi / b.hi;
+  r = dsub(r, dmulf(b, q2));
+  float q3 = r.hi / b.hi;
+  return dadd(quick_two_sum(q1, q2), df(q3));
+}
+__device__ __forceinline__ DF dsqrt(DF a) {
+  if (!(a.hi > 0.f)) return df(0.f);
+  float y = sqrtf(a.hi);
+  float p = y * y, e = fmaf(y, y, -p);
+  DF rem = dsub(a, DF{p, e});
+  return quick_two_sum(y, rem.hi / (2.f * y));
+}
+__device__ __forceinline__ bool dlt(DF a, DF b) { return a.hi < b.hi || (a.hi == b.hi && a.lo < b.lo); }
+__device__ __forceinline__ DF dmin(DF a, DF b) { return dlt(b, a) ? b : a; }
+__device__ __forceinline__ DF f2df(float2 v) { return DF{v.x, v.y}; }
+
+__device__ __forceinline__ DF quad_root_df(DF a, DF b, DF c) {
+  DF rd1 = dsub(dmul(b, b), dmul(dmulf(a, 4.f), c));
+  if (rd1.hi < 0.f) rd1 = df(0.f);
+  return ddiv(dadd(dneg(b), dsqrt(rd1)), dmulf(a, 2.f));
+}
+
+// fouds1 / fouds2 (fm2d_ttime.f90:248-518) in double-float.
+__device__ float2 fouds_df(const WarpStateT<float2> &w, const Grid2 &g, const double *V, int iz, int ix, int fom) {
+  int tsw1 = 0;
+  DF travm = df(0.f);
+  const DF slown = ddiv(df(1.f), df_from(V[lin(g, iz, ix)]));
+  const DF s2 = dmul(slown, slown);
+  const DF dnx = df_from(g.dnx), dnz = df_from(g.dnz);
+  auto S = [&](int z, int x) { return w.S[lin(g, z, x)]; };
+  auto Tv = [&](int z, int x) { return f2df(w.T[lin(g, z, x)]); };
+  for (int j = ix - 1; j <= ix + 1; j += 2) {
+    if (!(j >= 1 && j <= g.nnx)) continue;
+    int swj = -1, j2 = j;
+    const bool jalive = S(iz, j) == 0;
+    if (fom == 1) {
+      if (j == ix - 1) { j2 = j - 1; if (j2 >= 1) { if (S(iz, j2) == 0) swj = 0; } }
+      else { j2 = j + 1; if (j2 <= g.nnx) { if (S(iz, j2) == 0) swj = 0; } }
+      if (jalive && swj == 0) { swj = -1; if (dlt(Tv(iz, j2), Tv(iz, j))) swj = 0; }
+      else swj = -1;
+    }
+    for (int k = iz - 1; k <= iz + 1; k += 2) {
+      if (!(k >= 1 && k <= g.nnz)) continue;
+      int swk = -1, k2 = k;
+      const bool kalive = S(k, ix) == 0;
+      if (fom == 1) {
+        if (k == iz - 1) { k2 = k - 1; if (k2 >= 1) { if (S(k2, ix) == 0) swk = 0; } }
+        else { k2 = k + 1; if (k2 <= g.nnz) { if (S(k2, ix) == 0) swk = 0; } }
+        if (kalive && swk == 0) { swk = -1; if (dlt(Tv(k2, ix), Tv(k, ix))) swk = 0; }
+        else swk = -1;
+      }
+      if (!jalive && !kalive) continue;
+      DF a = df(0.f), b = df(0.f), c = df(0.f), tref = df(0.f);
+      float tdiv = 1.f;
+      if (swj == 0) {
+        DF tj = Tv(iz, j), tj2 = Tv(iz, j2);
+        if (swk == 0) {
+          DF u = dmulf(dnx, 2.f), v = dmulf(dnz, 2.f);
+          DF em = dsub(dsub(dmulf(tj, 4.f), tj2), dmulf(Tv(k, ix), 4.f));
+          em = dadd(em, Tv(k2, ix));
+          DF uu = dmul(u, u), vv = dmul(v, v);
+          a = dadd(vv, uu); b = dmul(dmulf(em, 2.f), uu);
+          c = dmul(uu, dsub(dmul(em, em), dmul(s2, vv)));
+          tref = dsub(dmulf(tj, 4.f), tj2); tdiv = 3.f;
+        } else if (kalive) {
+          DF u = dnz, v = dmulf(dnx, 2.f);
+          DF em = dadd(dsub(dmulf(Tv(k, ix), 3.f), dmulf(tj, 4.f)), tj2);
+          DF uu = dmul(u, u), vv = dmul(v, v);
+          a = dadd(vv, dmulf(uu, 9.f)); b = dmul(dmulf(em, 6.f), uu);
+          c = dmul(uu, dsub(dmul(em, em), dmul(s2, vv)));
+          tref = Tv(k, ix);
+        } else {
+          DF u = dmulf(dnx, 2.f);
+          a = df(1.f); c = dneg(dmul(dmul(u, u), s2));
+          tref = dsub(dmulf(tj, 4.f), tj2); tdiv = 3.f;
+        }
+      } else if (jalive) {
+        DF tj = Tv(iz, j);
+        if (swk == 0) {
+          DF u = dnx, v = dmulf(dnz, 2.f);
+          DF em = dadd(dsub(dmulf(tj, 3.f), dmulf(Tv(k, ix), 4.f)), Tv(k2, ix));
+          DF uu = dmul(u, u), vv = dmul(v, v);
+          a = dadd(vv, dmulf(uu, 9.f)); b = dmul(dmulf(em, 6.f), uu);
+          c = dmul(uu, dsub(dmul(em, em), dmul(vv, s2)));
+          tref = tj;
+        } else if (kalive) {
+          DF em = dsub(Tv(k, ix), tj);
+          DF uu = dmul(dnx, dnx), vv = dmul(dnz, dnz);
+          a = dadd(uu, vv); b = dneg(dmul(dmulf(uu, 2.f), em));
+          c = dmul(uu, dsub(dmul(em, em), dmul(vv, s2)));
+          tref = tj;
+        } else {
+          a = df(1.f); c = dneg(dmul(s2, dmul(dnx, dnx)));
+          tref = tj;
+        }
+      } else {
+        if (swk == 0) {
+          DF u = dmulf(dnz, 2.f);
+          a = df(1.f); c = dneg(dmul(dmul(u, u), s2));
+          tref = dsub(dmulf(Tv(k, ix), 4.f), Tv(k2, ix)); tdiv = 3.f;
+        } else {
+          a = df(1.f);
+          if (fom == 1) c = dneg(dmul(s2, dmul(dnz, dnz)));
+          else { DF sd = dmul(slown, dnz); c = dneg(dmul(sd, sd)); }
+          tref = Tv(k, ix);
+        }
+      }
+      DF trav = dadd(tref, quad_root_df(a, b, c));
+      if (tdiv != 1.f) trav = ddiv(trav, df(tdiv));
+      if (tsw1 == 1) travm = dmin(trav, travm);
+      else { travm = trav; tsw1 = 1; }
+    }
+  }
+  return make_float2(travm.hi, travm.lo);
+}
+
 __device__ __forceinline__ float quad_rootf(float a, float b, float c) {
   float rd1 = b * b - 4.0f * a * c;
   if (rd1 < 0.0f) rd1 = 0.0f;
   return (-b + sqrtf(rd1)) / (2.0f * a);
 }
 
-__device__ double fouds1_mixed(const WarpState &w, const Grid2 &g, const double *V, int iz, int ix) {
-  int tsw1 = 0;
-  float travm = 0.f;
-  const float slown = (float)(1.0 / V[lin(g, iz, ix)]);
-  const float dnx = (float)g.dnx, dnz = (float)g.dnz;
-  double base = -1.0;
-  for (int j = ix - 1; j <= ix + 1; j += 2)
-    for (int k = iz - 1; k <= iz + 1; k += 2) {
-      if (!(j >= 1 && j <= g.nnx && k >= 1 && k <= g.nnz)) continue;
-      const bool ja = w.S[lin(g, iz, j)] == 0, ka = w.S[lin(g, k, ix)] == 0;
-      if (!ja && !ka) continue;
-      if (base < 0) base = ja ? w.T[lin(g, iz, j)] : w.T[lin(g, k, ix)];
-      float a, b, c, tref;
-      if (ja) {
-        float tj = (float)(w.T[lin(g, iz, j)] - base);
-        if (ka) {
-          float tk = (float)(w.T[lin(g, k, ix)] - base);
-          float em = tk - tj;
-          a = dnx * dnx + dnz * dnz;
-          b = -(2.0f * (dnx * dnx) * em);
-          c = (dnx * dnx) * (em * em - (dnz * dnz) * (slown * slown));
-        } else {
-          a = 1.f; b = 0.f; c = -((slown * slown) * (dnx * dnx));
-        }
-        tref = tj;
-      } else {
-        a = 1.f; b = 0.f;
-        float sd = slown * dnz;
-        c = -(sd * sd);
-        tref = (float)(w.T[lin(g, k, ix)] - base);
-      }
-      float trav = tref + quad_rootf(a, b, c);
-      if (tsw1 == 1) travm = fminf(trav, travm);
-      else { travm = trav; tsw1 = 1; }
-    }
-  return base + (double)travm;
-}
-
-__device__ double fouds2_mixed(const WarpState &w, const Grid2 &g, const double *V, int iz, int ix) {
-  int tsw1 = 0;
-  float travm = 0.f;
-  const float slown = (float)(1.0 / V[lin(g, iz, ix)]);
-  const float dnx = (float)g.dnx, dnz = (float)g.dnz;
-  double base = -1.0;
-  for (int j = ix - 1; j <= ix + 1; j += 2) {
-    if (!(j >= 1 && j <= g.nnx)) continue;
-    int swj = -1, j2;
-    if (j == ix - 1) { j2 = j - 1; if (j2 >= 1) { if (w.S[lin(g, iz, j2)] == 0) swj = 0; } }
-    else { j2 = j + 1; if (j2 <= g.nnx) { if (w.S[lin(g, iz, j2)] == 0) swj = 0; } }
-    const bool jalive = w.S[lin(g, iz, j)] == 0;
-    if (jalive && swj == 0) { swj = -1; if (tkey(w.T, lin(g, iz, j)) > tkey(w.T, lin(g, iz, j2))) swj = 0; }
-    else swj = -1;
-    if (jalive && base < 0) base = w.T[lin(g, iz, j)];
-    for (int k = iz - 1; k <= iz + 1; k += 2) {
-      if (!(k >= 1 && k <= g.nnz)) continue;
-      int swk = -1, k2;
-      if (k == iz - 1) { k2 = k - 1; if (k2 >= 1) { if (w.S[lin(g, k2, ix)] == 0) swk = 0; } }
-      else { k2 = k + 1; if (k2 <= g.nnz) { if (w.S[lin(g, k2, ix)] == 0) swk = 0; } }
-      const bool kalive = w.S[lin(g, k, ix)] == 0;
-      if (kalive && swk == 0) { swk = -1; if (tkey(w.T, lin(g, k, ix)) > tkey(w.T, lin(g, k2, ix))) swk = 0; }
-      else swk = -1;
-      if (!jalive && !kalive) continue;
-      if (base < 0) base = w.T[lin(g, k, ix)];
-      auto sh = [&](int node) { return (float)(w.T[node] - base); };
-      int swsol = 0;
-      float a = 0, b = 0, c = 0, tref = 0, tdiv = 1.f;
-      if (swj == 0) {
-        swsol = 1;
-        float tj = sh(lin(g, iz, j)), tj2 = sh(lin(g, iz, j2));
-        if (swk == 0) {
-          float u = 2.f * dnx, v = 2.f * dnz;
-          float tk = sh(lin(g, k, ix)), tk2 = sh(lin(g, k2, ix));
-          float em = 4.f * tj - tj2 - 4.f * tk;
-          em = em + tk2;
-          a = v * v + u * u; b = 2.f * em * (u * u);
-          c = (u * u) * (em * em - (slown * slown) * (v * v));
-          tref = 4.f * tj - tj2; tdiv = 3.f;
-        } else if (kalive) {
-          float u = dnz, v = 2.f * dnx;
-          float tk = sh(lin(g, k, ix));
-          float em = 3.f * tk - 4.f * tj + tj2;
-          a = v * v + 9.f * (u * u); b = 6.f * em * (u * u);
-          c = (u * u) * (em * em - (slown * slown) * (v * v));
-          tref = tk; tdiv = 1.f;
-        } else {
-          float u = 2.f * dnx;
-          a = 1.f; b = 0.f; c = -((u * u) * (slown * slown));
-          tref = 4.f * tj - tj2; tdiv = 3.f;
-        }
-      } else if (jalive) {
-        swsol = 1;
-        float tj = sh(lin(g, iz, j));
-        if (swk == 0) {
-          float u = dnx, v = 2.f * dnz;
-          float tk = sh(lin(g, k, ix)), tk2 = sh(lin(g, k2, ix));
-          float em = 3.f * tj - 4.f * tk + tk2;
-          a = v * v + 9.f * (u * u); b = 6.f * em * (u * u);
-          c = (u * u) * (em * em - (v * v) * (slown * slown));
-          tref = tj; tdiv = 1.f;
-        } else if (kalive) {
-          float tk = sh(lin(g, k, ix));
-          float em = tk - tj;
-          a = dnx * dnx + dnz * dnz; b = -(2.f * (dnx * dnx) * em);
-          c = (dnx * dnx) * (em * em - (dnz * dnz) * (slown * slown));
-          tref = tj; tdiv = 1.f;
-        } else {
-          a = 1.f; b = 0.f; c = -((slown * slown) * (dnx * dnx));
-          tref = tj; tdiv = 1.f;
-        }
-      } else {
-        if (swk == 0) {
-          swsol = 1;
-          float u = 2.f * dnz;
-          float tk = sh(lin(g, k, ix)), tk2 = sh(lin(g, k2, ix));
-          a = 1.f; b = 0.f; c = -((u * u) * (slown * slown));
-          tref = 4.f * tk - tk2; tdiv = 3.f;
-        } else if (kalive) {
-          swsol = 1;
-          a = 1.f; b = 0.f; c = -((slown * slown) * (dnz * dnz));
-          tref = sh(lin(g, k, ix)); tdiv = 1.f;
-        }
-      }
-      if (swsol == 1) {
-        float trav = (tref + quad_rootf(a, b, c)) / tdiv;
-        if (tsw1 == 1) travm = fminf(trav, travm);
-        else { travm = trav; tsw1 = 1; }
-      }
-    }
-  }
-  return base + (double)travm;
-}
-
-
 // Fixed-point variant (precision == 2): times are int32 in units of
 // 2^-shift s, each update's quadratic is solved in FP32 on the neighbours'
 // times relative to a nearby accepted time, and the result is rounded back to
 // the fixed-point grid. The stencils and case selection are fouds1/fouds2's.
 struct Fx { float scale, inv; };
+
+template <class TT> __device__ __forceinline__ TT from_double(double t, const Fx &fx);
+template <> __device__ __forceinline__ double from_double<double>(double t, const Fx &) { return t; }
+template <> __device__ __forceinline__ float2 from_double<float2>(double t, const Fx &) {
+  float h = (float)t; return make_float2(h, (float)(t - (double)h));
+}
+template <> __device__ __forceinline__ int from_double<int>(double t, const Fx &fx) {
+  return (int)min(llrint(t * (double)fx.scale), (long long)INT_MAX - 1);
+}
+__device__ __forceinline__ double to_double(double t, const Fx &) { return t; }
+__device__ __forceinline__ double to_double(float2 t, const Fx &) { return (double)t.x + (double)t.y; }
+__device__ __forceinline__ double to_double(int t, const Fx &fx) { return (double)t * (double)fx.inv; }
 
 __device__ int fouds_fx(const WarpStateT<int> &w, const Grid2 &g, const double *V, int iz, int ix, int fom,
                         const Fx &fx) {
@@ -446,7 +482,7 @@ __device__ int fouds_fx(const WarpStateT<int> &w, const Grid2 &g, const double *
     if (fom == 1) {
       if (j == ix - 1) { j2 = j - 1; if (j2 >= 1) { if (S(iz, j2) == 0) swj = 0; } }
       else { j2 = j + 1; if (j2 <= g.nnx) { if (S(iz, j2) == 0) swj = 0; } }
-      if (jalive && swj == 0) { swj = -1; if (w.T[lin(g, iz, j)] > w.T[lin(g, iz, j2)]) swj = 0; }
+      if (jalive && swj == 0) { swj = -1; if (tlt(w.T[lin(g, iz, j2)], w.T[lin(g, iz, j)])) swj = 0; }
       else swj = -1;
     }
     if (jalive && base < 0) base = w.T[lin(g, iz, j)];
@@ -524,6 +560,26 @@ __device__ int fouds_fx(const WarpStateT<int> &w, const Grid2 &g, const double *
   return (int)min(max(r, 0LL), (long long)INT_MAX - 1);
 }
 
+__device__ __forceinline__ double shfl_time(double v, int src) { return __shfl_sync(0xffffffffu, v, src); }
+__device__ __forceinline__ int shfl_time(int v, int src) { return __shfl_sync(0xffffffffu, v, src); }
+__device__ __forceinline__ float2 shfl_time(float2 v, int src) {
+  return make_float2(__shfl_sync(0xffffffffu, v.x, src), __shfl_sync(0xffffffffu, v.y, src));
+}
+
+// Exact 8-byte round trip of a time through the mapping scratch.
+__device__ __forceinline__ double bit_store(double t) { return t; }
+__device__ __forceinline__ double bit_store(int t) { return (double)t; }
+__device__ __forceinline__ double bit_store(float2 t) {
+  return __longlong_as_double(((long long)__float_as_uint(t.y) << 32) | __float_as_uint(t.x));
+}
+template <class TT> __device__ __forceinline__ TT bit_load(double v);
+template <> __device__ __forceinline__ double bit_load<double>(double v) { return v; }
+template <> __device__ __forceinline__ int bit_load<int>(double v) { return (int)v; }
+template <> __device__ __forceinline__ float2 bit_load<float2>(double v) {
+  unsigned long long b = (unsigned long long)__double_as_longlong(v);
+  return make_float2(__uint_as_float((unsigned)(b & 0xffffffffu)), __uint_as_float((unsigned)(b >> 32)));
+}
+
 // fm2d_ttime.f90:682-711 bilinear
 __device__ __forceinline__ double bilinear(const double nv[2][2], double dsx, double dsz, double dnx, double dnz) {
   double biv = 0.0;
@@ -564,7 +620,7 @@ __device__ void march(WarpStateT<TT> &w, const Grid2 &g, const double *V, int fo
         if (go) {
           if (tr && tr->n < tr->max) {
             tr->ti[3 * tr->n] = urg; tr->ti[3 * tr->n + 1] = lin(g, iz, ix); tr->ti[3 * tr->n + 2] = w.ntr;
-            tr->tt[tr->n] = (double)w.T[lin(g, iz, ix)]; tr->n++;
+            tr->tt[tr->n] = to_double(w.T[lin(g, iz, ix)], fx); tr->n++;
           }
           w.S[lin(g, iz, ix)] = 0;
           downtree(w);
@@ -590,13 +646,14 @@ __device__ void march(WarpStateT<TT> &w, const Grid2 &g, const double *V, int fo
     // order: a sift compares against the other close nodes' current times, so
     // the writes must not run ahead of the sifts.
     int st = 0;
-    TT tnew = 0;
+    TT tnew = TT();
     if (valid) {
       st = w.S[lin(g, nz_, nx_)];
       if (st != 0) {
-        if constexpr (sizeof(TT) == sizeof(double)) {
-          if (prec == 0) tnew = fom == 0 ? fouds1(w, g, V, nz_, nx_) : fouds2(w, g, V, nz_, nx_);
-          else tnew = fom == 0 ? fouds1_mixed(w, g, V, nz_, nx_) : fouds2_mixed(w, g, V, nz_, nx_);
+        if constexpr (std::is_same<TT, double>::value) {
+          tnew = fom == 0 ? fouds1(w, g, V, nz_, nx_) : fouds2(w, g, V, nz_, nx_);
+        } else if constexpr (std::is_same<TT, float2>::value) {
+          tnew = fouds_df(w, g, V, nz_, nx_, fom);
         } else {
           tnew = fouds_fx(w, g, V, nz_, nx_, fom, fx);
         }
@@ -608,7 +665,7 @@ __device__ void march(WarpStateT<TT> &w, const Grid2 &g, const double *V, int fo
 #pragma unroll
     for (int q = 0; q < 4; ++q) {
       cd[q] = __shfl_sync(0xffffffffu, code, q);
-      tn[q] = __shfl_sync(0xffffffffu, tnew, q);
+      tn[q] = shfl_time(tnew, q);
     }
     __syncwarp();
     if (lane == 0) {
@@ -646,8 +703,7 @@ __device__ void init_source(WarpStateT<TT> &w, const Grid2 &g, const double *V, 
       double ez = dsz - (double)(j - 1) * g.dnz;
       double ds = sqrt(ex * ex + ez * ez);
       const double t0 = 2.0 * ds / (vss[i - 1][j - 1] + vsrc);
-      if constexpr (sizeof(TT) == sizeof(double)) w.T[lin(g, isz - 1 + j, isx - 1 + i)] = t0;
-      else w.T[lin(g, isz - 1 + j, isx - 1 + i)] = (int)min(llrint(t0 * (double)fx.scale), (long long)INT_MAX - 1);
+      w.T[lin(g, isz - 1 + j, isx - 1 + i)] = from_double<TT>(t0, fx);
       addtree(w, g, isz - 1 + j, isx - 1 + i);
     }
 }
@@ -714,7 +770,7 @@ fm2d_solve_kernel(Fm2dJob job, int warp_bytes) {
   // fixed-point scale: the largest time is below 3 x diagonal / slowest
   // velocity; keep it under 2^31 units
   Fx fx{1.f, 1.f};
-  if constexpr (sizeof(TT) != sizeof(double)) {
+  if constexpr (std::is_same<TT, int>::value) {
     const float vmin = __int_as_float(*job.vmin_bits);
     const double ext = sqrt(((job.nvx - 1) * job.dvxd) * ((job.nvx - 1) * job.dvxd) +
                             ((job.nvz - 1) * job.dvzd) * ((job.nvz - 1) * job.dvzd));
@@ -723,7 +779,6 @@ fm2d_solve_kernel(Fm2dJob job, int warp_bytes) {
     while (shift > 4 && ldexp(tmax, shift) > 2.0e9) --shift;
     fx.scale = ldexpf(1.f, shift); fx.inv = ldexpf(1.f, -shift);
   }
-  const float inv_scale = fx.inv;
   const int nnx = (job.nvx - 1) * job.gdx + 1, nnz = (job.nvz - 1) * job.gdz + 1;
   const double dvx = job.dvxd, dvz = job.dvzd;
   Grid2 gc{nnx, nnz, nnz, job.goxd, job.gozd, dvx / job.gdx, dvz / job.gdz};
@@ -789,7 +844,7 @@ fm2d_solve_kernel(Fm2dJob job, int warp_bytes) {
       int a = q % mz, b = q / mz;
       int k = a * sgdl + 1, l = b * sgdl + 1;
       int r = lin(gr, k, l);
-      tmpT[q] = (double)w.T[r];
+      tmpT[q] = bit_store(w.T[r]);
       tmpS[q] = w.S[r];
     }
     __syncwarp();
@@ -800,7 +855,7 @@ fm2d_solve_kernel(Fm2dJob job, int warp_bytes) {
       int c = lin(gc, vnt + a, vnl + b);
       short s = tmpS[q];
       w.S[c] = s;
-      if (s >= 0) w.T[c] = (TT)tmpT[q];
+      if (s >= 0) w.T[c] = bit_load<TT>(tmpT[q]);
     }
     __syncwarp();
     // narrow band repair (fm2dray_cartesian.f90:384-405); order-independent
@@ -834,8 +889,7 @@ fm2d_solve_kernel(Fm2dJob job, int warp_bytes) {
   // optional travel-time field
   if (job.tfield) {
     double *tf = job.tfield + ((size_t)map * job.nsrc + src) * nnx * nnz;
-    for (int q = lane; q < nnx * nnz; q += 32)
-      tf[q] = sizeof(TT) == sizeof(double) ? (double)w.T[q] : (double)w.T[q] * (double)inv_scale;
+    for (int q = lane; q < nnx * nnz; q += 32) tf[q] = to_double(w.T[q], fx);
   }
   // srtimes (fm2dray_cartesian.f90:682-797), one receiver per lane
   const int *srs = job.srs + (size_t)(map % job.srs_nmaps) * job.nsrc * job.nrc + (size_t)src * job.nrc;
@@ -883,8 +937,7 @@ fm2d_solve_kernel(Fm2dJob job, int warp_bytes) {
         for (int l = 1; l <= 2; ++l) {
           double produ = (1.0 - fabs(((double)(l - 1) * gc.dnz - drz) / gc.dnz)) *
                          (1.0 - fabs(((double)(k - 1) * gc.dnx - drx) / gc.dnx));
-          const double tv = sizeof(TT) == sizeof(double) ? (double)w.T[lin(gc, irz - 1 + l, irx - 1 + k)]
-                                                         : (double)w.T[lin(gc, irz - 1 + l, irx - 1 + k)] * (double)inv_scale;
+          const double tv = to_double(w.T[lin(gc, irz - 1 + l, irx - 1 + k)], fx);
           trr = trr + tv * produ;
         }
     }
@@ -925,6 +978,7 @@ int launch_fm2d(const Fm2dJob &job, const Fm2dPlan &plan, cudaStream_t s) {
   if (!attr) {
     cudaFuncSetAttribute(fm2d_solve_kernel<double>, cudaFuncAttributeMaxDynamicSharedMemorySize, 227 * 1024);
     cudaFuncSetAttribute(fm2d_solve_kernel<int>, cudaFuncAttributeMaxDynamicSharedMemorySize, 227 * 1024);
+    cudaFuncSetAttribute(fm2d_solve_kernel<float2>, cudaFuncAttributeMaxDynamicSharedMemorySize, 227 * 1024);
     attr = true;
   }
   if (job.precision == 2) {
@@ -939,6 +993,8 @@ int launch_fm2d(const Fm2dJob &job, const Fm2dPlan &plan, cudaStream_t s) {
   int blocks = (job.nsolve + wpb - 1) / wpb;
   if (job.precision == 2)
     fm2d_solve_kernel<int><<<blocks, 32 * wpb, (size_t)plan.warp_bytes * wpb, s>>>(job, plan.warp_bytes);
+  else if (job.precision == 1)
+    fm2d_solve_kernel<float2><<<blocks, 32 * wpb, (size_t)plan.warp_bytes * wpb, s>>>(job, plan.warp_bytes);
   else
     fm2d_solve_kernel<double><<<blocks, 32 * wpb, (size_t)plan.warp_bytes * wpb, s>>>(job, plan.warp_bytes);
   MCT_CUDA_TRY(cudaGetLastError());

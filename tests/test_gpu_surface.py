@@ -117,7 +117,7 @@ def test_surface_rejects_models_failing_check_model(gpulib):
 
 
 @pytest.mark.parametrize("tt_precision", [1, 2])
-def test_surface_mixed_precision_travel_times_within_tolerance(orc, gpulib, tt_precision):
+def test_surface_reduced_precision_travel_times(orc, gpulib, tt_precision):
     rng, grid, settings, data, ncells, pts, par = small_case(5)
     settings["precision"] = 1
     settings["tt_precision"] = tt_precision
@@ -130,7 +130,10 @@ def test_surface_mixed_precision_travel_times_within_tolerance(orc, gpulib, tt_p
         pt, pv = lk.phase_time(c)
         m = np.asarray(data["raystat"]).reshape(pt.shape) == 1
         err = np.abs(pt[m] - ept[m])
-        assert np.quantile(err, 0.99) <= TT_TOL and err.max() <= 5e-2
+        if tt_precision == 1:      # double-float: within the bound on every path
+            assert err.max() <= TT_TOL
+        else:                      # fixed point: approximate mode
+            assert np.quantile(err, 0.99) <= TT_TOL and err.max() <= 5e-2
         if eo[3] == 0:
             np.testing.assert_allclose(out[c, :3], eo[:3], rtol=1e-2)
     lk.close()
