@@ -59,6 +59,24 @@ int mct_grid_nearest_batch_device(int d, int nchains, int ncell_max,
                                   const int *box, int *sites_id, double *vp,
                                   double *vs, double *rho, void *stream);
 
+/* Same as mct_grid_nearest_batch_device, same arguments and results, but it
+ * allocates no device memory: its scratch is a fixed array of
+ * MCT_GRID_NOALLOC_SCRATCH_BYTES per device inside the library. No counterpart
+ * in the reference (which grids on the host); it serves callers that may not
+ * allocate while they run (pre-reserved device memory, proposals enqueued
+ * ahead on one stream). A call needing more scratch than the array holds
+ * (about 4 B per node per chain plus the kd-tree storage) returns
+ * MCT_ERR_ARG. The first call on a device does a one-time address lookup;
+ * make it before any stream capture. All calls on a device share the array:
+ * calls that overlap in time race and must be ordered by the caller. */
+#define MCT_GRID_NOALLOC_SCRATCH_BYTES (32u * 1024u * 1024u)
+int mct_grid_nearest_batch_device_noalloc(int d, int nchains, int ncell_max,
+                                          const int *ncells, const double *points,
+                                          const double *params, int nx, int ny, int nz,
+                                          const double *grid_lo, const double *grid_step,
+                                          const int *box, int *sites_id, double *vp,
+                                          double *vs, double *rho, void *stream);
+
 /* ------------------------------------------------------------------------
  * Surface-wave dispersion of one layered column, replaces surfdisp96
  * (surfmodes/surfdisp96.f:52-382) with its argument list: REAL*4 model
