@@ -10,8 +10,8 @@
 // source), the narrow band kept in the reference's binary heap in shared
 // memory (lane 0 performs the sifts in the reference's sequence, so ties break
 // identically), and the up-to-four neighbour updates of each accepted node
-// computed by four lanes at once (they read only accepted nodes and are
-// independent). The refined source grid with its early exit at the box edge,
+// computed by 16 lanes at once, one stencil combination each (they read only
+// accepted nodes and are independent). The refined source grid with its early exit at the box edge,
 // the refined-to-coarse mapping and the narrow-band repair follow modrays.
 // Arithmetic follows the Fortran expression order; the file is built with
 // -fmad=false so nothing is fused.
@@ -135,153 +135,12 @@ __device__ void updtree(WarpStateT<TT> &w, const Grid2 &g, int iz, int ix) {
   }
 }
 
-// ---- upwind updates --------------------------------------------------------
+// ---- upwind arithmetic ------------------------------------------------------
 __device__ __forceinline__ double quad_root(double a, double b, double c) {
   double rd1 = b * b - 4.0 * a * c;
   if (rd1 < 0.0) rd1 = 0.0;
   return (-b + sqrt(rd1)) / (2.0 * a);
 }
-
-// fm2d_ttime.f90:248-332
-__device__ double fouds1(const WarpState &w, const Grid2 &g, const double *V, int iz, int ix) {
-  int tsw1 = 0;
-  double travm = 0.0;
-  double slown = 1.0 / V[lin(g, iz, ix)];
-  for (int j = ix - 1; j <= ix + 1; j += 2)
-    for (int k = iz - 1; k <= iz + 1; k += 2) {
-      if (!(j >= 1 && j <= g.nnx && k >= 1 && k <= g.nnz)) continue;
-      int swsol = 0;
-      double a = 0, b = 0, c = 0, tref = 0;
-      if (w.S[lin(g, iz, j)] == 0) {
-        swsol = 1;
-        if (w.S[lin(g, k, ix)] == 0) {
-          double u = g.dnx, v = g.dnz;
-          double em = w.T[lin(g, k, ix)] - w.T[lin(g, iz, j)];
-          a = u * u + v * v;
-          b = -(2.0 * (u * u) * em);
-          c = (u * u) * (em * em - (v * v) * (slown * slown));
-          tref = w.T[lin(g, iz, j)];
-        } else {
-          a = 1.0; b = 0.0;
-          c = -((slown * slown) * (g.dnx * g.dnx));
-          tref = w.T[lin(g, iz, j)];
-        }
-      } else if (w.S[lin(g, k, ix)] == 0) {
-        swsol = 1;
-        a = 1.0; b = 0.0;
-        double sd = slown * g.dnz;
-        c = -(sd * sd);
-        tref = w.T[lin(g, k, ix)];
-      }
-      if (swsol == 1) {
-        double trav = tref + quad_root(a, b, c);
-        if (tsw1 == 1) travm = fmin(trav, travm);
-        else { travm = trav; tsw1 = 1; }
-      }
-    }
-  return travm;
-}
-
-// fm2d_ttime.f90:342-518
-__device__ double fouds2(const WarpState &w, const Grid2 &g, const double *V, int iz, int ix) {
-  int tsw1 = 0;
-  double travm = 0.0;
-  double slown = 1.0 / V[lin(g, iz, ix)];
-  for (int j = ix - 1; j <= ix + 1; j += 2) {
-    if (!(j >= 1 && j <= g.nnx)) continue;
-    int swj = -1, j2;
-    if (j == ix - 1) { j2 = j - 1; if (j2 >= 1) { if (w.S[lin(g, iz, j2)] == 0) swj = 0; } }
-    else { j2 = j + 1; if (j2 <= g.nnx) { if (w.S[lin(g, iz, j2)] == 0) swj = 0; } }
-    const bool jalive = w.S[lin(g, iz, j)] == 0;
-    if (jalive && swj == 0) { swj = -1; if (w.T[lin(g, iz, j)] > w.T[lin(g, iz, j2)]) swj = 0; }
-    else swj = -1;
-    for (int k = iz - 1; k <= iz + 1; k += 2) {
-      if (!(k >= 1 && k <= g.nnz)) continue;
-      int swk = -1, k2;
-      if (k == iz - 1) { k2 = k - 1; if (k2 >= 1) { if (w.S[lin(g, k2, ix)] == 0) swk = 0; } }
-      else { k2 = k + 1; if (k2 <= g.nnz) { if (w.S[lin(g, k2, ix)] == 0) swk = 0; } }
-      const bool kalive = w.S[lin(g, k, ix)] == 0;
-      if (kalive && swk == 0) { swk = -1; if (w.T[lin(g, k, ix)] > w.T[lin(g, k2, ix)]) swk = 0; }
-      else swk = -1;
-      int swsol = 0;
-      double a = 0, b = 0, c = 0, tref = 0, tdiv = 1.0;
-      if (swj == 0) {
-        swsol = 1;
-        if (swk == 0) {
-          double u = 2.0 * g.dnx, v = 2.0 * g.dnz;
-          double em = 4.0 * w.T[lin(g, iz, j)] - w.T[lin(g, iz, j2)] - 4.0 * w.T[lin(g, k, ix)];
-          em = em + w.T[lin(g, k2, ix)];
-          a = v * v + u * u;
-          b = 2.0 * em * (u * u);
-          c = (u * u) * (em * em - (slown * slown) * (v * v));
-          tref = 4.0 * w.T[lin(g, iz, j)] - w.T[lin(g, iz, j2)];
-          tdiv = 3.0;
-        } else if (kalive) {
-          double u = g.dnz, v = 2.0 * g.dnx;
-          double em = 3.0 * w.T[lin(g, k, ix)] - 4.0 * w.T[lin(g, iz, j)] + w.T[lin(g, iz, j2)];
-          a = v * v + 9.0 * (u * u);
-          b = 6.0 * em * (u * u);
-          c = (u * u) * (em * em - (slown * slown) * (v * v));
-          tref = w.T[lin(g, k, ix)];
-          tdiv = 1.0;
-        } else {
-          double u = 2.0 * g.dnx;
-          a = 1.0; b = 0.0;
-          c = -((u * u) * (slown * slown));
-          tref = 4.0 * w.T[lin(g, iz, j)] - w.T[lin(g, iz, j2)];
-          tdiv = 3.0;
-        }
-      } else if (jalive) {
-        swsol = 1;
-        if (swk == 0) {
-          double u = g.dnx, v = 2.0 * g.dnz;
-          double em = 3.0 * w.T[lin(g, iz, j)] - 4.0 * w.T[lin(g, k, ix)] + w.T[lin(g, k2, ix)];
-          a = v * v + 9.0 * (u * u);
-          b = 6.0 * em * (u * u);
-          c = (u * u) * (em * em - (v * v) * (slown * slown));
-          tref = w.T[lin(g, iz, j)];
-          tdiv = 1.0;
-        } else if (kalive) {
-          double u = g.dnx, v = g.dnz;
-          double em = w.T[lin(g, k, ix)] - w.T[lin(g, iz, j)];
-          a = u * u + v * v;
-          b = -(2.0 * (u * u) * em);
-          c = (u * u) * (em * em - (v * v) * (slown * slown));
-          tref = w.T[lin(g, iz, j)];
-          tdiv = 1.0;
-        } else {
-          a = 1.0; b = 0.0;
-          c = -((slown * slown) * (g.dnx * g.dnx));
-          tref = w.T[lin(g, iz, j)];
-          tdiv = 1.0;
-        }
-      } else {
-        if (swk == 0) {
-          swsol = 1;
-          double u = 2.0 * g.dnz;
-          a = 1.0; b = 0.0;
-          c = -((u * u) * (slown * slown));
-          tref = 4.0 * w.T[lin(g, k, ix)] - w.T[lin(g, k2, ix)];
-          tdiv = 3.0;
-        } else if (kalive) {
-          swsol = 1;
-          a = 1.0; b = 0.0;
-          c = -((slown * slown) * (g.dnz * g.dnz));
-          tref = w.T[lin(g, k, ix)];
-          tdiv = 1.0;
-        }
-      }
-      if (swsol == 1) {
-        double trav = (tref + quad_root(a, b, c)) / tdiv;
-        if (tsw1 == 1) travm = fmin(trav, travm);
-        else { travm = trav; tsw1 = 1; }
-      }
-    }
-  }
-  return travm;
-}
-
-
 
 // Double-float variant (precision == 1): times are unevaluated sums of two
 // FP32 numbers (hi + lo, |lo| <= ulp(hi)/2) and every operation of the
@@ -348,100 +207,6 @@ __device__ __forceinline__ DF quad_root_df(DF a, DF b, DF c) {
   return ddiv(dadd(dneg(b), dsqrt(rd1)), dmulf(a, 2.f));
 }
 
-// fouds1 / fouds2 (fm2d_ttime.f90:248-518) in double-float.
-__device__ float2 fouds_df(const WarpStateT<float2> &w, const Grid2 &g, const double *V, int iz, int ix, int fom) {
-  int tsw1 = 0;
-  DF travm = df(0.f);
-  const DF slown = ddiv(df(1.f), df_from(V[lin(g, iz, ix)]));
-  const DF s2 = dmul(slown, slown);
-  const DF dnx = df_from(g.dnx), dnz = df_from(g.dnz);
-  auto S = [&](int z, int x) { return w.S[lin(g, z, x)]; };
-  auto Tv = [&](int z, int x) { return f2df(w.T[lin(g, z, x)]); };
-  for (int j = ix - 1; j <= ix + 1; j += 2) {
-    if (!(j >= 1 && j <= g.nnx)) continue;
-    int swj = -1, j2 = j;
-    const bool jalive = S(iz, j) == 0;
-    if (fom == 1) {
-      if (j == ix - 1) { j2 = j - 1; if (j2 >= 1) { if (S(iz, j2) == 0) swj = 0; } }
-      else { j2 = j + 1; if (j2 <= g.nnx) { if (S(iz, j2) == 0) swj = 0; } }
-      if (jalive && swj == 0) { swj = -1; if (dlt(Tv(iz, j2), Tv(iz, j))) swj = 0; }
-      else swj = -1;
-    }
-    for (int k = iz - 1; k <= iz + 1; k += 2) {
-      if (!(k >= 1 && k <= g.nnz)) continue;
-      int swk = -1, k2 = k;
-      const bool kalive = S(k, ix) == 0;
-      if (fom == 1) {
-        if (k == iz - 1) { k2 = k - 1; if (k2 >= 1) { if (S(k2, ix) == 0) swk = 0; } }
-        else { k2 = k + 1; if (k2 <= g.nnz) { if (S(k2, ix) == 0) swk = 0; } }
-        if (kalive && swk == 0) { swk = -1; if (dlt(Tv(k2, ix), Tv(k, ix))) swk = 0; }
-        else swk = -1;
-      }
-      if (!jalive && !kalive) continue;
-      DF a = df(0.f), b = df(0.f), c = df(0.f), tref = df(0.f);
-      float tdiv = 1.f;
-      if (swj == 0) {
-        DF tj = Tv(iz, j), tj2 = Tv(iz, j2);
-        if (swk == 0) {
-          DF u = dmulf(dnx, 2.f), v = dmulf(dnz, 2.f);
-          DF em = dsub(dsub(dmulf(tj, 4.f), tj2), dmulf(Tv(k, ix), 4.f));
-          em = dadd(em, Tv(k2, ix));
-          DF uu = dmul(u, u), vv = dmul(v, v);
-          a = dadd(vv, uu); b = dmul(dmulf(em, 2.f), uu);
-          c = dmul(uu, dsub(dmul(em, em), dmul(s2, vv)));
-          tref = dsub(dmulf(tj, 4.f), tj2); tdiv = 3.f;
-        } else if (kalive) {
-          DF u = dnz, v = dmulf(dnx, 2.f);
-          DF em = dadd(dsub(dmulf(Tv(k, ix), 3.f), dmulf(tj, 4.f)), tj2);
-          DF uu = dmul(u, u), vv = dmul(v, v);
-          a = dadd(vv, dmulf(uu, 9.f)); b = dmul(dmulf(em, 6.f), uu);
-          c = dmul(uu, dsub(dmul(em, em), dmul(s2, vv)));
-          tref = Tv(k, ix);
-        } else {
-          DF u = dmulf(dnx, 2.f);
-          a = df(1.f); c = dneg(dmul(dmul(u, u), s2));
-          tref = dsub(dmulf(tj, 4.f), tj2); tdiv = 3.f;
-        }
-      } else if (jalive) {
-        DF tj = Tv(iz, j);
-        if (swk == 0) {
-          DF u = dnx, v = dmulf(dnz, 2.f);
-          DF em = dadd(dsub(dmulf(tj, 3.f), dmulf(Tv(k, ix), 4.f)), Tv(k2, ix));
-          DF uu = dmul(u, u), vv = dmul(v, v);
-          a = dadd(vv, dmulf(uu, 9.f)); b = dmul(dmulf(em, 6.f), uu);
-          c = dmul(uu, dsub(dmul(em, em), dmul(vv, s2)));
-          tref = tj;
-        } else if (kalive) {
-          DF em = dsub(Tv(k, ix), tj);
-          DF uu = dmul(dnx, dnx), vv = dmul(dnz, dnz);
-          a = dadd(uu, vv); b = dneg(dmul(dmulf(uu, 2.f), em));
-          c = dmul(uu, dsub(dmul(em, em), dmul(vv, s2)));
-          tref = tj;
-        } else {
-          a = df(1.f); c = dneg(dmul(s2, dmul(dnx, dnx)));
-          tref = tj;
-        }
-      } else {
-        if (swk == 0) {
-          DF u = dmulf(dnz, 2.f);
-          a = df(1.f); c = dneg(dmul(dmul(u, u), s2));
-          tref = dsub(dmulf(Tv(k, ix), 4.f), Tv(k2, ix)); tdiv = 3.f;
-        } else {
-          a = df(1.f);
-          if (fom == 1) c = dneg(dmul(s2, dmul(dnz, dnz)));
-          else { DF sd = dmul(slown, dnz); c = dneg(dmul(sd, sd)); }
-          tref = Tv(k, ix);
-        }
-      }
-      DF trav = dadd(tref, quad_root_df(a, b, c));
-      if (tdiv != 1.f) trav = ddiv(trav, df(tdiv));
-      if (tsw1 == 1) travm = dmin(trav, travm);
-      else { travm = trav; tsw1 = 1; }
-    }
-  }
-  return make_float2(travm.hi, travm.lo);
-}
-
 __device__ __forceinline__ float quad_rootf(float a, float b, float c) {
   float rd1 = b * b - 4.0f * a * c;
   if (rd1 < 0.0f) rd1 = 0.0f;
@@ -466,99 +231,194 @@ __device__ __forceinline__ double to_double(double t, const Fx &) { return t; }
 __device__ __forceinline__ double to_double(float2 t, const Fx &) { return (double)t.x + (double)t.y; }
 __device__ __forceinline__ double to_double(int t, const Fx &fx) { return (double)t * (double)fx.inv; }
 
-__device__ int fouds_fx(const WarpStateT<int> &w, const Grid2 &g, const double *V, int iz, int ix, int fom,
-                        const Fx &fx) {
-  int tsw1 = 0;
-  float travm = 0.f;
-  const float slown = (float)(1.0 / V[lin(g, iz, ix)]);
-  const float dnx = (float)g.dnx, dnz = (float)g.dnz;
-  int base = -1;
-  auto S = [&](int z, int x) { return w.S[lin(g, z, x)]; };
-  auto sh = [&](int z, int x) { return (float)(w.T[lin(g, z, x)] - base) * fx.inv; };
-  for (int j = ix - 1; j <= ix + 1; j += 2) {
-    if (!(j >= 1 && j <= g.nnx)) continue;
-    int swj = -1, j2 = j;
-    const bool jalive = S(iz, j) == 0;
-    if (fom == 1) {
-      if (j == ix - 1) { j2 = j - 1; if (j2 >= 1) { if (S(iz, j2) == 0) swj = 0; } }
-      else { j2 = j + 1; if (j2 <= g.nnx) { if (S(iz, j2) == 0) swj = 0; } }
-      if (jalive && swj == 0) { swj = -1; if (tlt(w.T[lin(g, iz, j2)], w.T[lin(g, iz, j)])) swj = 0; }
-      else swj = -1;
+// ---- upwind updates (fm2d_ttime.f90:248-518) ------------------------------
+// fouds1 / fouds2 give the node being updated the minimum, over its four
+// (x-neighbour j, z-neighbour k) combinations, of the solution of that
+// combination's local stencil. The combinations are independent of each other
+// and of the order of evaluation, so a warp evaluates the 16 combinations of
+// an accepted node's four neighbours at once (one per lane) and takes the
+// minimum over each group of four lanes: the minimum of the same candidate
+// values, hence the reference's result.
+//
+// Per combination, X = 2 if the x term is second order (j and the next node
+// j2 beyond it are accepted and T(j2) < T(j)), 1 if only j is accepted, 0
+// otherwise; Z likewise along z (second order only with fom = 1). Every
+// two-term case of fouds1/fouds2 solves
+//     a = vv + m*uu,  b = (kb*em)*uu,  c = uu*(em*em - s^2*vv)
+// with (uu, vv, m, kb, em, tref, tdiv) set per case, and every one-term case
+// a = 1, b = 0, c = -(uu*s^2); the operand order below is the reference's
+// (scaling by 2 and negation are exact, so (2*em)*uu with em = Tj - Tk is
+// bit-identical to the reference's -(2*uu*em) with em = Tk - Tj).
+struct Stencil {
+  int X, Z;                 // order of the x and z terms (0, 1, 2)
+  int lj, lj2, lk, lk2;     // nodes j, j2 (along x) and k, k2 (along z)
+};
+
+// Combination cmb (0..3) of node (iz, ix): j = ix -/+ 1, k = iz -/+ 1.
+// Returns false when the reference skips it (j or k off the grid, neither
+// accepted).
+template <class TT>
+__device__ __forceinline__ bool combo_stencil(const WarpStateT<TT> &w, const Grid2 &g, int iz, int ix, int cmb,
+                                              int fom, Stencil &s) {
+  const int dj = cmb < 2 ? -1 : 1, dk = (cmb & 1) ? 1 : -1;
+  const int j = ix + dj, k = iz + dk;
+  if (j < 1 || j > g.nnx || k < 1 || k > g.nnz) return false;
+  s.lj = lin(g, iz, j); s.lk = lin(g, k, ix);
+  s.lj2 = s.lj; s.lk2 = s.lk;
+  const bool jal = w.S[s.lj] == 0, kal = w.S[s.lk] == 0;
+  if (!jal && !kal) return false;
+  s.X = jal ? 1 : 0; s.Z = kal ? 1 : 0;
+  if (fom == 1) {
+    const int j2 = j + dj, k2 = k + dk;
+    if (jal && j2 >= 1 && j2 <= g.nnx) {
+      const int l2 = lin(g, iz, j2);
+      if (w.S[l2] == 0 && tlt(w.T[l2], w.T[s.lj])) { s.X = 2; s.lj2 = l2; }
     }
-    if (jalive && base < 0) base = w.T[lin(g, iz, j)];
-    for (int k = iz - 1; k <= iz + 1; k += 2) {
-      if (!(k >= 1 && k <= g.nnz)) continue;
-      int swk = -1, k2 = k;
-      const bool kalive = S(k, ix) == 0;
-      if (fom == 1) {
-        if (k == iz - 1) { k2 = k - 1; if (k2 >= 1) { if (S(k2, ix) == 0) swk = 0; } }
-        else { k2 = k + 1; if (k2 <= g.nnz) { if (S(k2, ix) == 0) swk = 0; } }
-        if (kalive && swk == 0) { swk = -1; if (w.T[lin(g, k, ix)] > w.T[lin(g, k2, ix)]) swk = 0; }
-        else swk = -1;
-      }
-      if (!jalive && !kalive) continue;
-      if (base < 0) base = w.T[lin(g, k, ix)];
-      float a = 0, b = 0, c = 0, tref = 0, tdiv = 1.f;
-      if (swj == 0) {
-        float tj = sh(iz, j), tj2 = sh(iz, j2);
-        if (swk == 0) {
-          float u = 2.f * dnx, v = 2.f * dnz;
-          float tk = sh(k, ix), tk2 = sh(k2, ix);
-          float em = 4.f * tj - tj2 - 4.f * tk;
-          em = em + tk2;
-          a = v * v + u * u; b = 2.f * em * (u * u);
-          c = (u * u) * (em * em - (slown * slown) * (v * v));
-          tref = 4.f * tj - tj2; tdiv = 3.f;
-        } else if (kalive) {
-          float u = dnz, v = 2.f * dnx;
-          float tk = sh(k, ix);
-          float em = 3.f * tk - 4.f * tj + tj2;
-          a = v * v + 9.f * (u * u); b = 6.f * em * (u * u);
-          c = (u * u) * (em * em - (slown * slown) * (v * v));
-          tref = tk;
-        } else {
-          float u = 2.f * dnx;
-          a = 1.f; c = -((u * u) * (slown * slown));
-          tref = 4.f * tj - tj2; tdiv = 3.f;
-        }
-      } else if (jalive) {
-        float tj = sh(iz, j);
-        if (swk == 0) {
-          float u = dnx, v = 2.f * dnz;
-          float tk = sh(k, ix), tk2 = sh(k2, ix);
-          float em = 3.f * tj - 4.f * tk + tk2;
-          a = v * v + 9.f * (u * u); b = 6.f * em * (u * u);
-          c = (u * u) * (em * em - (v * v) * (slown * slown));
-          tref = tj;
-        } else if (kalive) {
-          float tk = sh(k, ix);
-          float em = tk - tj;
-          a = dnx * dnx + dnz * dnz; b = -(2.f * (dnx * dnx) * em);
-          c = (dnx * dnx) * (em * em - (dnz * dnz) * (slown * slown));
-          tref = tj;
-        } else {
-          a = 1.f; c = -((slown * slown) * (dnx * dnx));
-          tref = tj;
-        }
-      } else {
-        if (swk == 0) {
-          float u = 2.f * dnz;
-          float tk = sh(k, ix), tk2 = sh(k2, ix);
-          a = 1.f; c = -((u * u) * (slown * slown));
-          tref = 4.f * tk - tk2; tdiv = 3.f;
-        } else {
-          a = 1.f; c = -((slown * slown) * (dnz * dnz));
-          tref = sh(k, ix);
-        }
-      }
-      float trav = (tref + quad_rootf(a, b, c)) / tdiv;
-      if (tsw1 == 1) travm = fminf(trav, travm);
-      else { travm = trav; tsw1 = 1; }
+    if (kal && k2 >= 1 && k2 <= g.nnz) {
+      const int l2 = lin(g, k2, ix);
+      if (w.S[l2] == 0 && tlt(w.T[l2], w.T[s.lk])) { s.Z = 2; s.lk2 = l2; }
     }
   }
-  long long r = (long long)base + llrintf(travm * fx.scale);
+  return true;
+}
+
+
+// FP64, the reference's arithmetic (precision 0).
+__device__ double combo_time(const WarpStateT<double> &w, const Grid2 &g, const Stencil &s, double vnode, int fom,
+                             const Fx &) {
+  const double slown = 1.0 / vnode;
+  const double ss = slown * slown;
+  const double u2x = 2.0 * g.dnx, u2z = 2.0 * g.dnz;
+  const double hx1 = g.dnx * g.dnx, hz1 = g.dnz * g.dnz, hx2 = u2x * u2x, hz2 = u2z * u2z;
+  const double Tj = w.T[s.lj], Tk = w.T[s.lk];
+  double a = 1.0, b = 0.0, c, tref, tdiv = 1.0;
+  if (s.X && s.Z) {
+    double uu, vv, m = 1.0, kb = 2.0, em;
+    if (s.X == 2 && s.Z == 2) {
+      tref = 4.0 * Tj - w.T[s.lj2];
+      em = (tref - 4.0 * Tk) + w.T[s.lk2];
+      uu = hx2; vv = hz2; tdiv = 3.0;
+    } else if (s.X == 2) {
+      em = (3.0 * Tk - 4.0 * Tj) + w.T[s.lj2];
+      uu = hz1; vv = hx2; m = 9.0; kb = 6.0; tref = Tk;
+    } else if (s.Z == 2) {
+      em = (3.0 * Tj - 4.0 * Tk) + w.T[s.lk2];
+      uu = hx1; vv = hz2; m = 9.0; kb = 6.0; tref = Tj;
+    } else {
+      em = Tj - Tk;
+      uu = hx1; vv = hz1; tref = Tj;
+    }
+    a = vv + m * uu;
+    b = (kb * em) * uu;
+    c = uu * (em * em - ss * vv);
+  } else if (s.X) {
+    if (s.X == 2) { tref = 4.0 * Tj - w.T[s.lj2]; c = -(hx2 * ss); tdiv = 3.0; }
+    else { tref = Tj; c = -(ss * hx1); }
+  } else {
+    if (s.Z == 2) { tref = 4.0 * Tk - w.T[s.lk2]; c = -(hz2 * ss); tdiv = 3.0; }
+    else if (fom == 1) { tref = Tk; c = -(ss * hz1); }
+    else { const double sd = slown * g.dnz; tref = Tk; c = -(sd * sd); }
+  }
+  return (tref + quad_root(a, b, c)) / tdiv;
+}
+
+// Double-float (precision 1): the same cases in FP32-pair arithmetic.
+__device__ float2 combo_time(const WarpStateT<float2> &w, const Grid2 &g, const Stencil &s, double vnode, int fom,
+                             const Fx &) {
+  const DF slown = ddiv(df(1.f), df_from(vnode));
+  const DF ss = dmul(slown, slown);
+  const DF dnx = df_from(g.dnx), dnz = df_from(g.dnz);
+  const DF u2x = dmulf(dnx, 2.f), u2z = dmulf(dnz, 2.f);
+  const DF Tj = f2df(w.T[s.lj]), Tk = f2df(w.T[s.lk]);
+  DF a = df(1.f), b = df(0.f), c, tref;
+  float tdiv = 1.f;
+  if (s.X && s.Z) {
+    DF uu, vv, em;
+    float m = 1.f, kb = 2.f;
+    if (s.X == 2 && s.Z == 2) {
+      tref = dsub(dmulf(Tj, 4.f), f2df(w.T[s.lj2]));
+      em = dadd(dsub(tref, dmulf(Tk, 4.f)), f2df(w.T[s.lk2]));
+      uu = dmul(u2x, u2x); vv = dmul(u2z, u2z); tdiv = 3.f;
+    } else if (s.X == 2) {
+      em = dadd(dsub(dmulf(Tk, 3.f), dmulf(Tj, 4.f)), f2df(w.T[s.lj2]));
+      uu = dmul(dnz, dnz); vv = dmul(u2x, u2x); m = 9.f; kb = 6.f; tref = Tk;
+    } else if (s.Z == 2) {
+      em = dadd(dsub(dmulf(Tj, 3.f), dmulf(Tk, 4.f)), f2df(w.T[s.lk2]));
+      uu = dmul(dnx, dnx); vv = dmul(u2z, u2z); m = 9.f; kb = 6.f; tref = Tj;
+    } else {
+      em = dsub(Tj, Tk);
+      uu = dmul(dnx, dnx); vv = dmul(dnz, dnz); tref = Tj;
+    }
+    a = dadd(vv, dmulf(uu, m));
+    b = dmul(dmulf(em, kb), uu);
+    c = dmul(uu, dsub(dmul(em, em), dmul(ss, vv)));
+  } else if (s.X) {
+    if (s.X == 2) { tref = dsub(dmulf(Tj, 4.f), f2df(w.T[s.lj2])); c = dneg(dmul(dmul(u2x, u2x), ss)); tdiv = 3.f; }
+    else { tref = Tj; c = dneg(dmul(ss, dmul(dnx, dnx))); }
+  } else {
+    if (s.Z == 2) { tref = dsub(dmulf(Tk, 4.f), f2df(w.T[s.lk2])); c = dneg(dmul(dmul(u2z, u2z), ss)); tdiv = 3.f; }
+    else if (fom == 1) { tref = Tk; c = dneg(dmul(ss, dmul(dnz, dnz))); }
+    else { const DF sd = dmul(slown, dnz); tref = Tk; c = dneg(dmul(sd, sd)); }
+  }
+  const DF trav = ddiv(dadd(tref, quad_root_df(a, b, c)), df(tdiv));
+  return make_float2(trav.hi, trav.lo);
+}
+
+// Fixed point (precision 2): the same cases in FP32 on times taken relative
+// to the combination's first accepted neighbour, rounded back to the
+// fixed-point grid.
+__device__ int combo_time(const WarpStateT<int> &w, const Grid2 &g, const Stencil &s, double vnode, int fom,
+                          const Fx &fx) {
+  const float slown = (float)(1.0 / vnode);
+  const float ss = slown * slown;
+  const float dnx = (float)g.dnx, dnz = (float)g.dnz;
+  const float u2x = 2.f * dnx, u2z = 2.f * dnz;
+  const int base = s.X ? w.T[s.lj] : w.T[s.lk];
+  auto sh = [&](int l) { return (float)(w.T[l] - base) * fx.inv; };
+  const float Tj = sh(s.lj), Tk = sh(s.lk);
+  float a = 1.f, b = 0.f, c, tref, tdiv = 1.f;
+  if (s.X && s.Z) {
+    float uu, vv, m = 1.f, kb = 2.f, em;
+    if (s.X == 2 && s.Z == 2) {
+      tref = 4.f * Tj - sh(s.lj2);
+      em = (tref - 4.f * Tk) + sh(s.lk2);
+      uu = u2x * u2x; vv = u2z * u2z; tdiv = 3.f;
+    } else if (s.X == 2) {
+      em = (3.f * Tk - 4.f * Tj) + sh(s.lj2);
+      uu = dnz * dnz; vv = u2x * u2x; m = 9.f; kb = 6.f; tref = Tk;
+    } else if (s.Z == 2) {
+      em = (3.f * Tj - 4.f * Tk) + sh(s.lk2);
+      uu = dnx * dnx; vv = u2z * u2z; m = 9.f; kb = 6.f; tref = Tj;
+    } else {
+      em = Tj - Tk;
+      uu = dnx * dnx; vv = dnz * dnz; tref = Tj;
+    }
+    a = vv + m * uu;
+    b = (kb * em) * uu;
+    c = uu * (em * em - ss * vv);
+  } else if (s.X) {
+    if (s.X == 2) { tref = 4.f * Tj - sh(s.lj2); c = -((u2x * u2x) * ss); tdiv = 3.f; }
+    else { tref = Tj; c = -(ss * (dnx * dnx)); }
+  } else {
+    if (s.Z == 2) { tref = 4.f * Tk - sh(s.lk2); c = -((u2z * u2z) * ss); tdiv = 3.f; }
+    else if (fom == 1) { tref = Tk; c = -(ss * (dnz * dnz)); }
+    else { const float sd = slown * dnz; tref = Tk; c = -(sd * sd); }
+  }
+  const float trav = (tref + quad_rootf(a, b, c)) / tdiv;
+  long long r = (long long)base + llrintf(trav * fx.scale);
   return (int)min(max(r, 0LL), (long long)INT_MAX - 1);
 }
+
+// "no candidate" value for the group minimum, above every time
+__device__ __forceinline__ double time_inf(double) { return __longlong_as_double(0x7ff0000000000000LL); }
+__device__ __forceinline__ float2 time_inf(float2) { return make_float2(__int_as_float(0x7f800000), 0.f); }
+__device__ __forceinline__ int time_inf(int) { return INT_MAX; }
+__device__ __forceinline__ double shfl_xor_time(double v, int m) { return __shfl_xor_sync(0xffffffffu, v, m); }
+__device__ __forceinline__ int shfl_xor_time(int v, int m) { return __shfl_xor_sync(0xffffffffu, v, m); }
+__device__ __forceinline__ float2 shfl_xor_time(float2 v, int m) {
+  return make_float2(__shfl_xor_sync(0xffffffffu, v.x, m), __shfl_xor_sync(0xffffffffu, v.y, m));
+}
+
 
 __device__ __forceinline__ double shfl_time(double v, int src) { return __shfl_sync(0xffffffffu, v, src); }
 __device__ __forceinline__ int shfl_time(int v, int src) { return __shfl_sync(0xffffffffu, v, src); }
@@ -632,50 +492,58 @@ __device__ void march(WarpStateT<TT> &w, const Grid2 &g, const double *V, int fo
     ix = __shfl_sync(0xffffffffu, ix, 0);
     iz = __shfl_sync(0xffffffffu, iz, 0);
     __syncwarp();
-    // neighbours in the reference's order: x-1, x+1, z-1, z+1
+    // lanes 0-15: neighbour q = lane / 4 in the reference's order (x-1, x+1,
+    // z-1, z+1), stencil combination lane % 4. New times are computed in
+    // registers (each reads only accepted nodes), then written and sifted one
+    // neighbour at a time in the reference's order: a sift compares against
+    // the other close nodes' current times, so the writes must not run ahead
+    // of the sifts.
+    const int q = (lane >> 2) & 3, cmb = lane & 3;
     int nz_ = iz, nx_ = ix;
     bool valid = false;
-    if (lane < 4) {
-      if (lane == 0) { nx_ = ix - 1; valid = nx_ >= 1; }
-      else if (lane == 1) { nx_ = ix + 1; valid = nx_ <= g.nnx; }
-      else if (lane == 2) { nz_ = iz - 1; valid = nz_ >= 1; }
+    if (lane < 16) {
+      if (q == 0) { nx_ = ix - 1; valid = nx_ >= 1; }
+      else if (q == 1) { nx_ = ix + 1; valid = nx_ <= g.nnx; }
+      else if (q == 2) { nz_ = iz - 1; valid = nz_ >= 1; }
       else { nz_ = iz + 1; valid = nz_ <= g.nnz; }
     }
-    // New times are computed in registers (each reads only accepted nodes),
-    // then written and sifted one neighbour at a time in the reference's
-    // order: a sift compares against the other close nodes' current times, so
-    // the writes must not run ahead of the sifts.
     int st = 0;
-    TT tnew = TT();
+    bool have = false;
+    TT cand = time_inf(TT());
     if (valid) {
-      st = w.S[lin(g, nz_, nx_)];
-      if (st != 0) {
-        if constexpr (std::is_same<TT, double>::value) {
-          tnew = fom == 0 ? fouds1(w, g, V, nz_, nx_) : fouds2(w, g, V, nz_, nx_);
-        } else if constexpr (std::is_same<TT, float2>::value) {
-          tnew = fouds_df(w, g, V, nz_, nx_, fom);
-        } else {
-          tnew = fouds_fx(w, g, V, nz_, nx_, fom, fx);
-        }
+      const int ln = lin(g, nz_, nx_);
+      st = w.S[ln];
+      Stencil sc;
+      if (st != 0 && combo_stencil(w, g, nz_, nx_, cmb, fom, sc)) {
+        have = true;
+        cand = combo_time(w, g, sc, V[ln], fom, fx);
       }
     }
-    int code = valid ? (st == -1 ? 1 : (st > 0 ? 2 : 0)) : 0;
+    const unsigned hb = __ballot_sync(0xffffffffu, have);
+#pragma unroll
+    for (int m = 1; m <= 2; m <<= 1) {
+      const TT o = shfl_xor_time(cand, m);
+      if (tlt(o, cand)) cand = o;
+    }
+    // a node with no usable combination gets 0, the reference's initial travm
+    if (((hb >> (lane & ~3)) & 0xFu) == 0u) cand = TT();
+    const int code = valid ? (st == -1 ? 1 : (st > 0 ? 2 : 0)) : 0;
     int cd[4];
     TT tn[4];
 #pragma unroll
-    for (int q = 0; q < 4; ++q) {
-      cd[q] = __shfl_sync(0xffffffffu, code, q);
-      tn[q] = shfl_time(tnew, q);
+    for (int k = 0; k < 4; ++k) {
+      cd[k] = __shfl_sync(0xffffffffu, code, 4 * k);
+      tn[k] = shfl_time(cand, 4 * k);
     }
     __syncwarp();
     if (lane == 0) {
       const int qz[4] = {iz, iz, iz - 1, iz + 1}, qx[4] = {ix - 1, ix + 1, ix, ix};
 #pragma unroll
-      for (int q = 0; q < 4; ++q) {
-        if (cd[q] == 0) continue;
-        w.T[lin(g, qz[q], qx[q])] = tn[q];
-        if (cd[q] == 1) addtree(w, g, qz[q], qx[q]);
-        else updtree(w, g, qz[q], qx[q]);
+      for (int k = 0; k < 4; ++k) {
+        if (cd[k] == 0) continue;
+        w.T[lin(g, qz[k], qx[k])] = tn[k];
+        if (cd[k] == 1) addtree(w, g, qz[k], qx[k]);
+        else updtree(w, g, qz[k], qx[k]);
       }
     }
     __syncwarp();

@@ -1,0 +1,67 @@
+"""Small fixed cases of the hot kernels, for profilers.
+
+    python -m mctomo_gb300.profcase fm2d [--precision P] [--maps M] [--repeat R]
+    python -m mctomo_gb300.profcase eik3 [--order O]
+
+fm2d: M Voronoi phase maps of 41 x 41 vertices (1 km spacing), 50 stations
+between 2 and 38 km, every station pair once, source refinement 4 x over
+8 cells (the surface-wave likelihood's fm2d settings); R calls of
+mct_modrays_batch. eik3: 8 velocity grids of 101 x 101 x 51 nodes (0.5 km),
+120 solves. Each case prints one line and exits 0.
+"""
+import argparse
+import time
+
+import numpy as np
+
+from . import forward, synthetic
+
+
+def fm2d(precision=1, maps=16, repeat=2):
+    rng = np.random.default_rng(0)
+    nvx = nvz = 41
+    st = rng.uniform(2.0, 38.0, (50, 2))
+    srs = np.triu(np.ones((50, 50), np.int32), 1)
+    velv = synthetic.voronoi_phase_maps(rng, maps, nvx, nvz, 1.0, 1.0)
+    for _ in range(repeat):
+        t0 = time.perf_counter()
+        tt = forward.modrays_batch(st, st, srs, nvx, nvz, 0.0, 0.0, 1.0, 1.0, velv, sgdl=4, sgs=8,
+                                   precision=precision)
+        dt = time.perf_counter() - t0
+    print(f"fm2d precision={precision} maps={maps} solves={maps * 49} last_call_s={dt:.4f} t01={tt[0, 0, 1]:.6f}")
+
+
+def eik3(order=0):
+    rng = np.random.default_rng(1)
+    nx, ny, nz = 101, 101, 51
+    h = (0.5, 0.5, 0.5)
+    lo = (0.0, 0.0, 0.0)
+    z = np.arange(nz) * h[2]
+    vels = np.stack([np.broadcast_to(3.0 + 0.08 * z * (1 + 0.1 * g), (nx, ny, nz)).copy() *
+                     (1 + 0.05 * rng.standard_normal((nx, ny, nz))) for g in range(8)])
+    nsolve = 120
+    grid = (np.arange(nsolve) % 8).astype(np.int32)
+    srcs = rng.uniform([2, 2, 1], [48, 48, 20], (nsolve, 3))
+    rev = rng.uniform([2, 2, 0], [48, 48, 0.5], (60, 3))
+    t0 = time.perf_counter()
+    tt, _, passes = forward.eikonal3d_batch(vels, h, lo, grid, srcs, rev, order=order)
+    dt = time.perf_counter() - t0
+    print(f"eik3 order={order} solves={nsolve} passes={passes} call_s={dt:.4f} t00={tt[0, 0]:.6f}")
+
+
+def main(argv=None):
+    ap = argparse.ArgumentParser(description=__doc__, formatter_class=argparse.RawDescriptionHelpFormatter)
+    ap.add_argument("case", choices=["fm2d", "eik3"])
+    ap.add_argument("--precision", type=int, default=1)
+    ap.add_argument("--maps", type=int, default=16)
+    ap.add_argument("--repeat", type=int, default=2)
+    ap.add_argument("--order", type=int, default=0)
+    a = ap.parse_args(argv)
+    if a.case == "fm2d":
+        fm2d(a.precision, a.maps, a.repeat)
+    else:
+        eik3(a.order)
+
+
+if __name__ == "__main__":
+    main()

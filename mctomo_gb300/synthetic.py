@@ -119,8 +119,9 @@ def perturb_chain_models(rng, ncells, points, params, grid, vs_range=(0.3, 2.5))
 
 
 def body_workload(rng, nx=101, ny=101, nz=51, extent=(50.0, 50.0, 25.0), nevents=200, nstations=60, np_=2):
-    """The 3D body-wave configuration: events at seeded uniform positions at
-    1-20 km depth with origin times uniform on [0, 1] s, stations at the
+    """The 3D body-wave configuration: events at seeded uniform positions
+    inside the grid, at 4-80 % of its depth (1-20 km for the default 25 km),
+    with origin times uniform on [0, 1] s, stations at the
     surface kept off the grid's maximum x/y faces (where the reference's
     trilinear read-out multiplies times), P and S picks for every pair, noise
     sigma 0.03 s (P) / 0.06 s (S). Observed times are straight-ray times at
@@ -130,7 +131,7 @@ def body_workload(rng, nx=101, ny=101, nz=51, extent=(50.0, 50.0, 25.0), nevents
                 dx=extent[0] / (nx - 1), dy=extent[1] / (ny - 1), dz=extent[2] / (nz - 1),
                 scaling=1.0, water_depth=0.0)
     ev = np.column_stack([rng.uniform(0.02, 0.98, nevents) * extent[0], rng.uniform(0.02, 0.98, nevents) * extent[1],
-                          rng.uniform(1.0, 20.0, nevents), rng.uniform(0.0, 1.0, nevents)])
+                          rng.uniform(0.04, 0.8, nevents) * extent[2], rng.uniform(0.0, 1.0, nevents)])
     sta = np.column_stack([rng.uniform(0.02, 0.95, nstations) * extent[0],
                            rng.uniform(0.02, 0.95, nstations) * extent[1], np.zeros(nstations)])
     dist = np.sqrt(((ev[:, None, :3] - sta[None, :, :]) ** 2).sum(-1)).reshape(-1)   # (src j, rev k)
@@ -143,3 +144,19 @@ def body_workload(rng, nx=101, ny=101, nz=51, extent=(50.0, 50.0, 25.0), nevents
     sigma = np.stack([np.full(dist.size, sig[p]) for p in range(np_)])
     data = dict(nsrc=nevents, rev=sta, raystat=raystat, ttime=ttime, sigma=sigma, nrays=int(raystat.sum()))
     return grid, settings, data, ev
+
+
+def voronoi_phase_maps(rng, nmaps, nvx, nvz, dx, dz, ncell=50, vrange=(0.4, 2.2)):
+    """Piecewise-constant 2D phase-velocity maps (Voronoi cells of uniform
+    random velocity), padded by one vertex on each side by edge copy, the
+    layout modrays takes: (nmaps, nvx+2, nvz+2)."""
+    out = np.zeros((nmaps, nvx + 2, nvz + 2))
+    X, Z = np.meshgrid(np.arange(nvx) * dx, np.arange(nvz) * dz, indexing="ij")
+    for m in range(nmaps):
+        pts = rng.uniform(0, 1, (ncell, 2)) * [(nvx - 1) * dx, (nvz - 1) * dz]
+        vals = rng.uniform(vrange[0], vrange[1], ncell)
+        d = (X[..., None] - pts[:, 0]) ** 2 + (Z[..., None] - pts[:, 1]) ** 2
+        out[m, 1:-1, 1:-1] = vals[np.argmin(d, -1)]
+        out[m, 0] = out[m, 1]; out[m, -1] = out[m, -2]
+        out[m, :, 0] = out[m, :, 1]; out[m, :, -1] = out[m, :, -2]
+    return out
