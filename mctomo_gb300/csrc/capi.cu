@@ -340,6 +340,7 @@ int mct_modrays_batch(int nmaps, int nsrc, const double *scx, const double *scz,
   std::lock_guard<std::mutex> lk(g_mu);
   rc = ensure_stream(); if (rc) return rc;
   size_t bytes = carve_size({sizeof(double) * nv * nmaps, sizeof(double) * (size_t)nnx * nnz * nmaps,
+                             sizeof(double) * (size_t)nnx * nnz * nmaps,
                              sizeof(double) * (size_t)plan.nref_max * ns, sizeof(double) * (size_t)plan.map_tmp_max * ns,
                              sizeof(short) * (size_t)plan.map_tmp_max * ns, sizeof(double) * 2 * (nsrc + nrc),
                              sizeof(int) * (size_t)srs_nmaps * nsrc * nrc, sizeof(int2) * ns,
@@ -350,7 +351,8 @@ int mct_modrays_batch(int nmaps, int nsrc, const double *scx, const double *scz,
   Carve cv(g_ws.p);
   double *d_velv = cv.take<double>(nv * nmaps);
   job.veln = cv.take<double>((size_t)nnx * nnz * nmaps);
-  job.vref = cv.take<double>((size_t)plan.nref_max * ns);
+  job.slon = cv.take<double>((size_t)nnx * nnz * nmaps);
+  job.sref = cv.take<double>((size_t)plan.nref_max * ns);
   job.map_tmp_t = cv.take<double>((size_t)plan.map_tmp_max * ns);
   job.map_tmp_s = cv.take<short>((size_t)plan.map_tmp_max * ns);
   double *d_xy = cv.take<double>(2 * (nsrc + nrc));

@@ -19,6 +19,8 @@
 #include "fm2d.cuh"
 #include <climits>
 #include <type_traits>
+#include <utility>
+#include <vector>
 
 namespace {
 
@@ -53,86 +55,90 @@ __device__ __forceinline__ bool tlt(int a, int b) { return a < b; }
 __device__ __forceinline__ bool tlt(float2 a, float2 b) { return a.x < b.x || (a.x == b.x && a.y < b.y); }
 
 // ---- binary heap (fm2d_ttime.f90:527-680), lane 0 only --------------------
+// The reference swaps the moving node with its parent (addtree, updtree) or
+// its smaller child (downtree) level by level. Moving a hole instead and
+// writing the node once at its final position visits the same positions with
+// the same comparisons (the moving node's time is fixed during a sift), so
+// the heap ends in the identical state; the moving node's time stays in a
+// register and the two child ids are read with one 32-bit load.
 template <class TT>
-__device__ void addtree(WarpStateT<TT> &w, const Grid2 &g, int iz, int ix) {
-  w.ntr = w.ntr + 1;
-  const int me = lin(g, iz, ix);
-  const unsigned short pm = pack(iz, ix);
-  w.S[me] = (short)w.ntr;
-  w.H[w.ntr] = pm;
-  int tpc = w.ntr, tpp = tpc / 2;
-  const TT tme = w.T[me];
+__device__ __forceinline__ void sift_up(WarpStateT<TT> &w, int me, unsigned short pm, int pos, TT tme) {
+  int tpc = pos, tpp = tpc >> 1;
   while (tpp > 0) {
     const int pp = w.H[tpp];
     const int pn = plin(w, pp);
-    if (tlt(tme, w.T[pn])) {
-      w.S[me] = (short)tpp;
-      w.S[pn] = (short)tpc;
-      w.H[tpc] = (unsigned short)pp;
-      w.H[tpp] = pm;
-      tpc = tpp; tpp = tpc / 2;
-    } else {
-      tpp = 0;
-    }
+    if (!tlt(tme, w.T[pn])) break;
+    w.H[tpc] = (unsigned short)pp;
+    w.S[pn] = (short)tpc;
+    tpc = tpp; tpp = tpc >> 1;
   }
+  w.H[tpc] = pm;
+  w.S[me] = (short)tpc;
 }
 
+// addtree: a far node joins the heap with time tme (already stored in T)
+template <class TT>
+__device__ __forceinline__ void addtree(WarpStateT<TT> &w, const Grid2 &g, int iz, int ix, TT tme) {
+  w.ntr = w.ntr + 1;
+  sift_up(w, lin(g, iz, ix), pack(iz, ix), w.ntr, tme);
+}
+template <class TT>
+__device__ __forceinline__ void addtree(WarpStateT<TT> &w, const Grid2 &g, int iz, int ix) {
+  addtree(w, g, iz, ix, w.T[lin(g, iz, ix)]);
+}
+
+// updtree: a close node's time decreased to tme
+template <class TT>
+__device__ __forceinline__ void updtree(WarpStateT<TT> &w, const Grid2 &g, int iz, int ix, TT tme) {
+  const int me = lin(g, iz, ix);
+  sift_up(w, me, pack(iz, ix), w.S[me], tme);
+}
+
+// downtree: remove the root (already marked alive by the caller)
 template <class TT>
 __device__ void downtree(WarpStateT<TT> &w) {
-  if (w.ntr == 1) { w.ntr = w.ntr - 1; return; }
+  if (w.ntr == 1) { w.ntr = 0; return; }
   const int lastp = w.H[w.ntr];
-  w.S[plin(w, lastp)] = 1;
-  w.H[1] = (unsigned short)lastp;
+  const int ln = plin(w, lastp);
   w.ntr = w.ntr - 1;
-  int tpp = 1, tpc = 2 * tpp;
   const int ntr = w.ntr;
-  while (tpc < ntr) {
-    const TT rd1 = w.T[plin(w, w.H[tpc])];
-    const TT rd2 = w.T[plin(w, w.H[tpc + 1])];
-    if (tlt(rd2, rd1)) tpc = tpc + 1;
-    const int cp = w.H[tpc], pp = w.H[tpp];
-    const int cn = plin(w, cp), pn = plin(w, pp);
-    if (tlt(w.T[cn], w.T[pn])) {
-      w.S[pn] = (short)tpc;
-      w.S[cn] = (short)tpp;
-      w.H[tpc] = (unsigned short)pp;
-      w.H[tpp] = (unsigned short)cp;
-      tpp = tpc; tpc = 2 * tpp;
-    } else {
-      tpc = ntr + 1;
+  const TT key = w.T[ln];
+  int hole = 1, c = 2;
+  while (c < ntr) {
+    const unsigned pair = reinterpret_cast<const unsigned *>(w.H)[c >> 1];   // H[c], H[c+1]
+    const int p1 = (int)(pair & 0xffffu), p2 = (int)(pair >> 16);
+    const int n1 = plin(w, p1), n2 = plin(w, p2);
+    const TT k1 = w.T[n1], k2 = w.T[n2];
+    const bool right = tlt(k2, k1);
+    const int cp = right ? p2 : p1, cn = right ? n2 : n1, cc = c + (right ? 1 : 0);
+    if (!tlt(right ? k2 : k1, key)) { c = ntr + 1; break; }
+    w.H[hole] = (unsigned short)cp;
+    w.S[cn] = (short)hole;
+    hole = cc; c = 2 * hole;
+  }
+  if (c == ntr) {
+    const int cp = w.H[c];
+    const int cn = plin(w, cp);
+    if (tlt(w.T[cn], key)) {
+      w.H[hole] = (unsigned short)cp;
+      w.S[cn] = (short)hole;
+      hole = c;
     }
   }
-  if (tpc == ntr) {
-    const int cp = w.H[tpc], pp = w.H[tpp];
-    const int cn = plin(w, cp), pn = plin(w, pp);
-    if (tlt(w.T[cn], w.T[pn])) {
-      w.S[pn] = (short)tpc;
-      w.S[cn] = (short)tpp;
-      w.H[tpc] = (unsigned short)pp;
-      w.H[tpp] = (unsigned short)cp;
-    }
-  }
+  w.H[hole] = (unsigned short)lastp;
+  w.S[ln] = (short)hole;
 }
 
-template <class TT>
-__device__ void updtree(WarpStateT<TT> &w, const Grid2 &g, int iz, int ix) {
-  const int me = lin(g, iz, ix);
-  const unsigned short pm = pack(iz, ix);
-  int tpc = w.S[me], tpp = tpc / 2;
-  const TT tme = w.T[me];
-  while (tpp > 0) {
-    const int pp = w.H[tpp];
-    const int pn = plin(w, pp);
-    if (tlt(tme, w.T[pn])) {
-      w.S[me] = (short)tpp;
-      w.S[pn] = (short)tpc;
-      w.H[tpc] = (unsigned short)pp;
-      w.H[tpp] = pm;
-      tpc = tpp; tpp = tpc / 2;
-    } else {
-      tpp = 0;
-    }
-  }
+// Shared-memory layout of one solve: T [n], S [n], H [n + 2] (1-based heap),
+// each array starting on a 16-byte boundary.
+__host__ __device__ __forceinline__ int align16(int b) { return (b + 15) & ~15; }
+struct SolveLayout { int offS, offH, bytes; };
+__host__ __device__ __forceinline__ SolveLayout solve_layout(int tbytes, int n) {
+  SolveLayout L;
+  L.offS = align16(tbytes * n);
+  L.offH = L.offS + align16(2 * n);
+  L.bytes = L.offH + align16(2 * (n + 2));
+  return L;
 }
 
 // ---- upwind arithmetic ------------------------------------------------------
@@ -145,14 +151,14 @@ __device__ __forceinline__ double quad_root(double a, double b, double c) {
 // Double-float variant (precision == 1): times are unevaluated sums of two
 // FP32 numbers (hi + lo, |lo| <= ulp(hi)/2) and every operation of the
 // reference's update is carried out in that format with error-free
-// transformations (Knuth's two-sum, Dekker's two-product via fmaf, Newton
-// steps for division and square root), giving about 2^-48 relative precision
-// on the FP32 pipe. Results agree with the FP64 reference to ~1e-13 s, so the
+// transformations (Knuth's two-sum, the two-product via fmaf, division and
+// square root from a hardware reciprocal / reciprocal-square-root estimate
+// refined by exact remainders), giving about 2^-46 relative precision on the
+// FP32 pipe. Results agree with the FP64 reference to ~1e-12 s, so the
 // acceptance order only differs on ties closer than that.
 struct DF { float hi, lo; };
 __device__ __forceinline__ DF df(float a) { return DF{a, 0.f}; }
 __device__ __forceinline__ DF df_from(double d) { float h = (float)d; return DF{h, (float)(d - (double)h)}; }
-__device__ __forceinline__ double df_to(DF a) { return (double)a.hi + (double)a.lo; }
 __device__ __forceinline__ DF two_sum(float a, float b) {
   float s = a + b, bb = s - a;
   return DF{s, (a - (s - bb)) + (b - bb)};
@@ -171,34 +177,41 @@ __device__ __forceinline__ DF dadd(DF a, DF b) {
 __device__ __forceinline__ DF dneg(DF a) { return DF{-a.hi, -a.lo}; }
 __device__ __forceinline__ DF dsub(DF a, DF b) { return dadd(a, dneg(b)); }
 __device__ __forceinline__ DF dmul(DF a, DF b) {
-  float p = a.hi * b.hi;
+  const float p = a.hi * b.hi;
   float e = fmaf(a.hi, b.hi, -p);
-  e += a.hi * b.lo + a.lo * b.hi;
+  e = fmaf(a.hi, b.lo, e);
+  e = fmaf(a.lo, b.hi, e);
   return quick_two_sum(p, e);
 }
 __device__ __forceinline__ DF dmulf(DF a, float f) {
-  float p = a.hi * f;
+  const float p = a.hi * f;
   float e = fmaf(a.hi, f, -p);
-  e += a.lo * f;
+  e = fmaf(a.lo, f, e);
   return quick_two_sum(p, e);
 }
+// a / b: quotient digits from an approximate reciprocal of b.hi (relative
+// error ~2^-22), each followed by the exact remainder a - b*q; three digits
+// reach double-float accuracy.
 __device__ __forceinline__ DF ddiv(DF a, DF b) {
-  float q1 = a.hi / b.hi;
-  DF r = dsub(a, dmulf(b, q1));
-  float q2 = r.hi / b.hi;
-  r = dsub(r, dmulf(b, q2));
-  float q3 = r.hi / b.hi;
+  const float r = __fdividef(1.f, b.hi);
+  const float q1 = a.hi * r;
+  DF rem = dsub(a, dmulf(b, q1));
+  const float q2 = rem.hi * r;
+  rem = dsub(rem, dmulf(b, q2));
+  const float q3 = rem.hi * r;
   return dadd(quick_two_sum(q1, q2), df(q3));
 }
+// sqrt(a): the correctly rounded FP32 root of a.hi plus one correction
+// (a - y^2) / (2y) from the exact remainder, the halved reciprocal square
+// root standing in for 1 / (2y).
 __device__ __forceinline__ DF dsqrt(DF a) {
   if (!(a.hi > 0.f)) return df(0.f);
-  float y = sqrtf(a.hi);
-  float p = y * y, e = fmaf(y, y, -p);
-  DF rem = dsub(a, DF{p, e});
-  return quick_two_sum(y, rem.hi / (2.f * y));
+  const float y = sqrtf(a.hi);
+  const float h = 0.5f * rsqrtf(a.hi);
+  const float p = y * y, e = fmaf(y, y, -p);
+  const DF rem = dsub(a, DF{p, e});
+  return quick_two_sum(y, rem.hi * h);
 }
-__device__ __forceinline__ bool dlt(DF a, DF b) { return a.hi < b.hi || (a.hi == b.hi && a.lo < b.lo); }
-__device__ __forceinline__ DF dmin(DF a, DF b) { return dlt(b, a) ? b : a; }
 __device__ __forceinline__ DF f2df(float2 v) { return DF{v.x, v.y}; }
 
 __device__ __forceinline__ DF quad_root_df(DF a, DF b, DF c) {
@@ -210,7 +223,7 @@ __device__ __forceinline__ DF quad_root_df(DF a, DF b, DF c) {
 __device__ __forceinline__ float quad_rootf(float a, float b, float c) {
   float rd1 = b * b - 4.0f * a * c;
   if (rd1 < 0.0f) rd1 = 0.0f;
-  return (-b + sqrtf(rd1)) / (2.0f * a);
+  return __fdividef(-b + sqrtf(rd1), 2.0f * a);
 }
 
 // Fixed-point variant (precision == 2): times are int32 in units of
@@ -283,10 +296,10 @@ __device__ __forceinline__ bool combo_stencil(const WarpStateT<TT> &w, const Gri
 }
 
 
-// FP64, the reference's arithmetic (precision 0).
-__device__ double combo_time(const WarpStateT<double> &w, const Grid2 &g, const Stencil &s, double vnode, int fom,
+// FP64, the reference's arithmetic (precision 0). slown is the node's
+// slowness 1/V, precomputed per node with the reference's division.
+__device__ double combo_time(const WarpStateT<double> &w, const Grid2 &g, const Stencil &s, double slown, int fom,
                              const Fx &) {
-  const double slown = 1.0 / vnode;
   const double ss = slown * slown;
   const double u2x = 2.0 * g.dnx, u2z = 2.0 * g.dnz;
   const double hx1 = g.dnx * g.dnx, hz1 = g.dnz * g.dnz, hx2 = u2x * u2x, hz2 = u2z * u2z;
@@ -323,9 +336,9 @@ __device__ double combo_time(const WarpStateT<double> &w, const Grid2 &g, const 
 }
 
 // Double-float (precision 1): the same cases in FP32-pair arithmetic.
-__device__ float2 combo_time(const WarpStateT<float2> &w, const Grid2 &g, const Stencil &s, double vnode, int fom,
+__device__ float2 combo_time(const WarpStateT<float2> &w, const Grid2 &g, const Stencil &s, double sl, int fom,
                              const Fx &) {
-  const DF slown = ddiv(df(1.f), df_from(vnode));
+  const DF slown = df_from(sl);
   const DF ss = dmul(slown, slown);
   const DF dnx = df_from(g.dnx), dnz = df_from(g.dnz);
   const DF u2x = dmulf(dnx, 2.f), u2z = dmulf(dnz, 2.f);
@@ -360,16 +373,17 @@ __device__ float2 combo_time(const WarpStateT<float2> &w, const Grid2 &g, const 
     else if (fom == 1) { tref = Tk; c = dneg(dmul(ss, dmul(dnz, dnz))); }
     else { const DF sd = dmul(slown, dnz); tref = Tk; c = dneg(dmul(sd, sd)); }
   }
-  const DF trav = ddiv(dadd(tref, quad_root_df(a, b, c)), df(tdiv));
+  DF trav = dadd(tref, quad_root_df(a, b, c));
+  if (tdiv != 1.f) trav = dmul(trav, df_from(1.0 / 3.0));
   return make_float2(trav.hi, trav.lo);
 }
 
 // Fixed point (precision 2): the same cases in FP32 on times taken relative
 // to the combination's first accepted neighbour, rounded back to the
 // fixed-point grid.
-__device__ int combo_time(const WarpStateT<int> &w, const Grid2 &g, const Stencil &s, double vnode, int fom,
+__device__ int combo_time(const WarpStateT<int> &w, const Grid2 &g, const Stencil &s, double sl, int fom,
                           const Fx &fx) {
-  const float slown = (float)(1.0 / vnode);
+  const float slown = (float)sl;
   const float ss = slown * slown;
   const float dnx = (float)g.dnx, dnz = (float)g.dnz;
   const float u2x = 2.f * dnx, u2z = 2.f * dnz;
@@ -404,7 +418,7 @@ __device__ int combo_time(const WarpStateT<int> &w, const Grid2 &g, const Stenci
     else if (fom == 1) { tref = Tk; c = -(ss * (dnz * dnz)); }
     else { const float sd = slown * dnz; tref = Tk; c = -(sd * sd); }
   }
-  const float trav = (tref + quad_rootf(a, b, c)) / tdiv;
+  const float trav = __fdividef(tref + quad_rootf(a, b, c), tdiv);
   long long r = (long long)base + llrintf(trav * fx.scale);
   return (int)min(max(r, 0LL), (long long)INT_MAX - 1);
 }
@@ -459,64 +473,63 @@ __device__ __forceinline__ double bilinear(const double nv[2][2], double dsx, do
 struct Trace { int *ti; double *tt; int max; int n; };
 
 template <class TT>
-__device__ void march(WarpStateT<TT> &w, const Grid2 &g, const double *V, int fom, int prec, int urg, int vnl,
-                      int vnr, int vnt, int vnb, const Fx &fx, Trace *tr = nullptr) {
+__device__ void march(WarpStateT<TT> &w, const Grid2 &g, const double *SL, int fom, int urg, int vnl, int vnr,
+                      int vnt, int vnb, const Fx &fx, Trace *tr = nullptr) {
   const int lane = threadIdx.x & 31;
+  // lanes 16-31 work on neighbour q = (lane - 16) / 4 of the accepted node,
+  // in the reference's order (x-1, x+1, z-1, z+1), stencil combination lane % 4
+  const int q = (lane >> 2) & 3, cmb = lane & 3;
+  const int dqx = q == 0 ? -1 : (q == 1 ? 1 : 0), dqz = q == 2 ? -1 : (q == 3 ? 1 : 0);
+  // slowness of this lane's neighbour of the node predicted to be accepted
+  // next, loaded while lane 0 sifts (a global-memory load off the critical path)
+  int pred = -1;
+  double sl_pred = 0.0;
   for (;;) {
-    int ix = 0, iz = 0, go = 0;
-    if (lane == 0) {
-      if (w.ntr > 0) {
-        int top = w.H[1];
-        iz = (top & 255) + 1; ix = (top >> 8) + 1;
-        go = 1;
-        if (urg == 1) {
-          int swrg = 0;
-          if (ix == 1 && vnl != 1) swrg = 1;
-          if (ix == g.nnx && vnr != g.nnx) swrg = 1;
-          if (iz == 1 && vnt != 1) swrg = 1;
-          if (iz == g.nnz && vnb != g.nnz) swrg = 1;
-          if (swrg) { w.S[lin(g, iz, ix)] = 0; go = 0; }
+    int pk = -1;   // accepted node ((ix-1) << 8) | (iz-1), or -1 to stop
+    if (lane == 0 && w.ntr > 0) {
+      const int top = w.H[1];
+      const int iz = (top & 255) + 1, ix = (top >> 8) + 1;
+      bool go = true;
+      if (urg == 1) {
+        int swrg = 0;
+        if (ix == 1 && vnl != 1) swrg = 1;
+        if (ix == g.nnx && vnr != g.nnx) swrg = 1;
+        if (iz == 1 && vnt != 1) swrg = 1;
+        if (iz == g.nnz && vnb != g.nnz) swrg = 1;
+        if (swrg) { w.S[lin(g, iz, ix)] = 0; go = false; }
+      }
+      if (go) {
+        if (tr && tr->n < tr->max) {
+          tr->ti[3 * tr->n] = urg; tr->ti[3 * tr->n + 1] = lin(g, iz, ix); tr->ti[3 * tr->n + 2] = w.ntr;
+          tr->tt[tr->n] = to_double(w.T[lin(g, iz, ix)], fx); tr->n++;
         }
-        if (go) {
-          if (tr && tr->n < tr->max) {
-            tr->ti[3 * tr->n] = urg; tr->ti[3 * tr->n + 1] = lin(g, iz, ix); tr->ti[3 * tr->n + 2] = w.ntr;
-            tr->tt[tr->n] = to_double(w.T[lin(g, iz, ix)], fx); tr->n++;
-          }
-          w.S[lin(g, iz, ix)] = 0;
-          downtree(w);
-        }
+        w.S[lin(g, iz, ix)] = 0;
+        downtree(w);
+        pk = top;
       }
     }
-    go = __shfl_sync(0xffffffffu, go, 0);
-    if (!go) break;
-    ix = __shfl_sync(0xffffffffu, ix, 0);
-    iz = __shfl_sync(0xffffffffu, iz, 0);
+    pk = __shfl_sync(0xffffffffu, pk, 0);
+    if (pk < 0) break;
     __syncwarp();
-    // lanes 0-15: neighbour q = lane / 4 in the reference's order (x-1, x+1,
-    // z-1, z+1), stencil combination lane % 4. New times are computed in
-    // registers (each reads only accepted nodes), then written and sifted one
-    // neighbour at a time in the reference's order: a sift compares against
-    // the other close nodes' current times, so the writes must not run ahead
-    // of the sifts.
-    const int q = (lane >> 2) & 3, cmb = lane & 3;
-    int nz_ = iz, nx_ = ix;
-    bool valid = false;
-    if (lane < 16) {
-      if (q == 0) { nx_ = ix - 1; valid = nx_ >= 1; }
-      else if (q == 1) { nx_ = ix + 1; valid = nx_ <= g.nnx; }
-      else if (q == 2) { nz_ = iz - 1; valid = nz_ >= 1; }
-      else { nz_ = iz + 1; valid = nz_ <= g.nnz; }
-    }
+    const int iz = (pk & 255) + 1, ix = (pk >> 8) + 1;
+    // New times are computed in registers (each reads only accepted nodes),
+    // then written and sifted by lane 0 one neighbour at a time in the
+    // reference's order: a sift compares against the other close nodes'
+    // current times, so the writes must not run ahead of the sifts.
     int st = 0;
-    bool have = false;
+    bool valid = false, have = false;
     TT cand = time_inf(TT());
-    if (valid) {
-      const int ln = lin(g, nz_, nx_);
-      st = w.S[ln];
-      Stencil sc;
-      if (st != 0 && combo_stencil(w, g, nz_, nx_, cmb, fom, sc)) {
-        have = true;
-        cand = combo_time(w, g, sc, V[ln], fom, fx);
+    if (lane >= 16) {
+      const int nx_ = ix + dqx, nz_ = iz + dqz;
+      valid = nx_ >= 1 && nx_ <= g.nnx && nz_ >= 1 && nz_ <= g.nnz;
+      if (valid) {
+        const int ln = lin(g, nz_, nx_);
+        st = w.S[ln];
+        Stencil sc;
+        if (st != 0 && combo_stencil(w, g, nz_, nx_, cmb, fom, sc)) {
+          have = true;
+          cand = combo_time(w, g, sc, pk == pred ? sl_pred : SL[ln], fom, fx);
+        }
       }
     }
     const unsigned hb = __ballot_sync(0xffffffffu, have);
@@ -532,18 +545,38 @@ __device__ void march(WarpStateT<TT> &w, const Grid2 &g, const double *V, int fo
     TT tn[4];
 #pragma unroll
     for (int k = 0; k < 4; ++k) {
-      cd[k] = __shfl_sync(0xffffffffu, code, 4 * k);
-      tn[k] = shfl_time(cand, 4 * k);
+      cd[k] = __shfl_sync(0xffffffffu, code, 16 + 4 * k);
+      tn[k] = shfl_time(cand, 16 + 4 * k);
+    }
+    const int qz[4] = {iz, iz, iz - 1, iz + 1}, qx[4] = {ix - 1, ix + 1, ix, ix};
+    // the next root: the current one unless a sifted neighbour is strictly
+    // earlier (the sifts below move such a node to the top)
+    int nxt = -1;
+    if (lane == 0) {
+      int r = w.ntr > 0 ? w.H[1] : -1;
+      TT rk = r >= 0 ? w.T[plin(w, r)] : TT();
+#pragma unroll
+      for (int k = 0; k < 4; ++k) {
+        if (cd[k] == 0) continue;
+        const int pq = (int)pack(qz[k], qx[k]);
+        if (r < 0 || pq == r || tlt(tn[k], rk)) { r = pq; rk = tn[k]; }
+      }
+      nxt = r;
+    }
+    nxt = __shfl_sync(0xffffffffu, nxt, 0);
+    if (lane >= 16 && nxt >= 0) {
+      const int nx_ = (nxt >> 8) + 1 + dqx, nz_ = (nxt & 255) + 1 + dqz;
+      pred = nxt;
+      if (nx_ >= 1 && nx_ <= g.nnx && nz_ >= 1 && nz_ <= g.nnz) sl_pred = SL[lin(g, nz_, nx_)];
     }
     __syncwarp();
     if (lane == 0) {
-      const int qz[4] = {iz, iz, iz - 1, iz + 1}, qx[4] = {ix - 1, ix + 1, ix, ix};
 #pragma unroll
       for (int k = 0; k < 4; ++k) {
         if (cd[k] == 0) continue;
         w.T[lin(g, qz[k], qx[k])] = tn[k];
-        if (cd[k] == 1) addtree(w, g, qz[k], qx[k]);
-        else updtree(w, g, qz[k], qx[k]);
+        if (cd[k] == 1) addtree(w, g, qz[k], qx[k], tn[k]);
+        else updtree(w, g, qz[k], qx[k], tn[k]);
       }
     }
     __syncwarp();
@@ -551,16 +584,17 @@ __device__ void march(WarpStateT<TT> &w, const Grid2 &g, const double *V, int fo
   __syncwarp();
 }
 
-// Source initialisation of travel (fm2d_ttime.f90:95-127), lane 0.
-template <class TT>
-__device__ void init_source(WarpStateT<TT> &w, const Grid2 &g, const double *V, double scx, double scz, const Fx &fx) {
+// Source initialisation of travel (fm2d_ttime.f90:95-127), lane 0. vel(iz, ix)
+// gives the node velocities of the grid g.
+template <class TT, class Vel>
+__device__ void init_source(WarpStateT<TT> &w, const Grid2 &g, Vel vel, double scx, double scz, const Fx &fx) {
   int isx = (int)((scx - g.gox) / g.dnx) + 1;
   int isz = (int)((scz - g.goz) / g.dnz) + 1;
   if (isx == g.nnx) isx = isx - 1;
   if (isz == g.nnz) isz = isz - 1;
   double vss[2][2];
   for (int i = 1; i <= 2; ++i)
-    for (int j = 1; j <= 2; ++j) vss[i - 1][j - 1] = V[lin(g, isz - 1 + j, isx - 1 + i)];
+    for (int j = 1; j <= 2; ++j) vss[i - 1][j - 1] = vel(isz - 1 + j, isx - 1 + i);
   double dsx = (scx - g.gox) - (double)(isx - 1) * g.dnx;
   double dsz = (scz - g.goz) - (double)(isz - 1) * g.dnz;
   double vsrc = bilinear(vss, dsx, dsz, g.dnx, g.dnz);
@@ -617,26 +651,67 @@ __global__ void gridder_kernel(Fm2dJob job) {
       sumi = sumi + bsw(i1 - 1, v) * sumj;
     }
     veln[(size_t)(stx - 1) * nnz + (stz - 1)] = sumi;
+    job.slon[(size_t)map * nnx * nnz + (size_t)(stx - 1) * nnz + (stz - 1)] = 1.0 / sumi;
   }
 }
 
+// bsplrefine (fm2dray_cartesian.f90:608-674): the cubic B-spline velocity of
+// refined node (idm1, idm2) (1-based z, x) of the source box whose corner is
+// refined node (origz, origx) of the whole grid; 0 outside the coarse box
+// [vnl, vnr] x [vnt, vnb].
+struct RefineBox {
+  const double *velv;   // this map's padded vertex grid
+  int ldv, origx, origz, nrxr, nrzr, vnl, vnr, vnt, vnb;
+};
+__device__ double refined_velocity(const Fm2dJob &job, const RefineBox &rb, int idm1, int idm2) {
+  const int sgdl = job.sgdl;
+  int st1 = idm1 + rb.origz - 1, st2 = idm2 + rb.origx - 1;
+  int i = (st1 - 1) / rb.nrzr + 1; if (i > job.nvz - 1) i = job.nvz - 1;
+  int k = st1 - rb.nrzr * (i - 1);
+  int j = (st2 - 1) / rb.nrxr + 1; if (j > job.nvx - 1) j = job.nvx - 1;
+  int l = st2 - rb.nrxr * (j - 1);
+  int c1 = job.gdz * (i - 1) + (k - 1) / sgdl + 1;
+  int c2 = job.gdx * (j - 1) + (l - 1) / sgdl + 1;
+  if (c1 < rb.vnt || c1 > rb.vnb || c2 < rb.vnl || c2 > rb.vnr) return 0.0;
+  double u = (double)(l - 1) / (double)rb.nrxr;
+  double v = (double)(k - 1) / (double)rb.nrzr;
+  double sum[4];
+  for (int i1 = 1; i1 <= 4; ++i1) {
+    sum[i1 - 1] = 0.0;
+    for (int j1 = 1; j1 <= 4; ++j1)
+      sum[i1 - 1] = sum[i1 - 1] + bsw(j1 - 1, u) * rb.velv[(size_t)(j - 2 + j1) * rb.ldv + (i - 2 + i1)];
+    sum[i1 - 1] = bsw(i1 - 1, v) * sum[i1 - 1];
+  }
+  return sum[0] + sum[1] + sum[2] + sum[3];
+}
+
+// Per-solve geometry shared by the two kernels (modrays' source cell and
+// refined box, fm2dray_cartesian.f90:283-330).
+struct SolveGeom {
+  int map, src;
+  double x, z;
+  int isx, isz, vnl, vnr, vnt, vnb;
+  Grid2 gc;
+};
+__device__ __forceinline__ bool solve_geom(const Fm2dJob &job, int solve, SolveGeom &s) {
+  s.map = job.solves[solve].x; s.src = job.solves[solve].y;
+  const int nnx = (job.nvx - 1) * job.gdx + 1, nnz = (job.nvz - 1) * job.gdz + 1;
+  s.gc = Grid2{nnx, nnz, nnz, job.goxd, job.gozd, job.dvxd / job.gdx, job.dvzd / job.gdz};
+  s.x = job.scx[s.src]; s.z = job.scz[s.src];
+  s.isx = (int)((s.x - s.gc.gox) / s.gc.dnx) + 1;
+  s.isz = (int)((s.z - s.gc.goz) / s.gc.dnz) + 1;
+  if (s.isx < 1 || s.isx > nnx || s.isz < 1 || s.isz > nnz) return false;
+  if (s.isx == nnx) s.isx = s.isx - 1;
+  if (s.isz == nnz) s.isz = s.isz - 1;
+  s.vnl = max(s.isx - job.sgs, 1); s.vnr = min(s.isx + job.sgs, nnx);
+  s.vnt = max(s.isz - job.sgs, 1); s.vnb = min(s.isz + job.sgs, nnz);
+  return true;
+}
+
+// Fixed-point scale (precision 2): the largest time is below 3 x diagonal /
+// slowest velocity; keep it under 2^31 units.
 template <class TT>
-__global__ void __launch_bounds__(32 * WARPS_PER_BLOCK_MAX)
-fm2d_solve_kernel(Fm2dJob job, int warp_bytes) {
-  extern __shared__ __align__(16) unsigned char smem[];
-  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  const int solve = blockIdx.x * (blockDim.x >> 5) + warp;
-  if (solve >= job.nsolve) return;
-  const int map = job.solves[solve].x, src = job.solves[solve].y;
-  unsigned char *base = smem + (size_t)warp * warp_bytes;
-  const int nodes_max = job.nodes_max;
-  WarpStateT<TT> w;
-  w.T = reinterpret_cast<TT *>(base);
-  w.S = reinterpret_cast<short *>(base + sizeof(TT) * nodes_max);
-  w.H = reinterpret_cast<unsigned short *>(base + (sizeof(TT) + sizeof(short)) * nodes_max);
-  w.ntr = 0;
-  // fixed-point scale: the largest time is below 3 x diagonal / slowest
-  // velocity; keep it under 2^31 units
+__device__ __forceinline__ Fx time_scale(const Fm2dJob &job) {
   Fx fx{1.f, 1.f};
   if constexpr (std::is_same<TT, int>::value) {
     const float vmin = __int_as_float(*job.vmin_bits);
@@ -647,77 +722,110 @@ fm2d_solve_kernel(Fm2dJob job, int warp_bytes) {
     while (shift > 4 && ldexp(tmax, shift) > 2.0e9) --shift;
     fx.scale = ldexpf(1.f, shift); fx.inv = ldexpf(1.f, -shift);
   }
-  const int nnx = (job.nvx - 1) * job.gdx + 1, nnz = (job.nvz - 1) * job.gdz + 1;
-  const double dvx = job.dvxd, dvz = job.dvzd;
-  Grid2 gc{nnx, nnz, nnz, job.goxd, job.gozd, dvx / job.gdx, dvz / job.gdz};
-  const double *Vc = job.veln + (size_t)map * nnx * nnz;
-  const double x = job.scx[src], z = job.scz[src];
-  Trace trace{job.trace_i, job.trace_t, job.trace_max, 0};
+  return fx;
+}
+
+template <class TT>
+__device__ __forceinline__ WarpStateT<TT> warp_state(unsigned char *base, int nodes) {
+  WarpStateT<TT> w;
+  const SolveLayout lay = solve_layout((int)sizeof(TT), nodes);
+  w.T = reinterpret_cast<TT *>(base);
+  w.S = reinterpret_cast<short *>(base + lay.offS);
+  w.H = reinterpret_cast<unsigned short *>(base + lay.offH);
+  w.ntr = 0;
+  w.ld = 1;
+  return w;
+}
+
+// Stage 1, source-grid refinement (asgr = 1): one warp per solve marches the
+// refined source box (travel with urg = 1) and leaves the times and states
+// of the box nodes that coincide with coarse nodes in the mapping scratch.
+// The refined box has up to (2*sgs*sgdl+1)^2 nodes, more than the coarse grid
+// usually has, so this stage runs with its own (smaller) warps per block.
+template <class TT>
+__global__ void __launch_bounds__(32 * WARPS_PER_BLOCK_MAX)
+fm2d_refined_kernel(Fm2dJob job, int warp_bytes) {
+  extern __shared__ __align__(16) unsigned char smem[];
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int solve = blockIdx.x * (blockDim.x >> 5) + warp;
+  if (solve >= job.nsolve) return;
+  SolveGeom sg;
+  if (!solve_geom(job, solve, sg)) return;   // reported by the coarse stage
+  WarpStateT<TT> w = warp_state<TT>(smem + (size_t)warp * warp_bytes, job.nref_max);
+  const Fx fx = time_scale<TT>(job);
+  const int sgdl = job.sgdl;
+  const int vnl = sg.vnl, vnr = sg.vnr, vnt = sg.vnt, vnb = sg.vnb;
+  const Grid2 &gc = sg.gc;
+  const int nrnx = (vnr - vnl) * sgdl + 1, nrnz = (vnb - vnt) * sgdl + 1;
+  Grid2 gr{nrnx, nrnz, nrnz, gc.gox + gc.dnx * (double)(vnl - 1), gc.goz + gc.dnz * (double)(vnt - 1),
+           job.dvxd / (double)(job.gdx * sgdl), job.dvzd / (double)(job.gdz * sgdl)};
+  Trace trace{job.trace_i, job.trace_t, job.trace_max / 2, 0};
   Trace *tr = (job.trace_i && solve == job.trace_solve && lane == 0) ? &trace : nullptr;
-  int isx = (int)((x - gc.gox) / gc.dnx) + 1;
-  int isz = (int)((z - gc.goz) / gc.dnz) + 1;
-  if (isx < 1 || isx > nnx || isz < 1 || isz > nnz) {
+  // refined slowness (1 / bsplrefine velocity; +inf outside the box, as
+  // the reference's 1/0 there)
+  double *Sr = job.sref + (size_t)solve * job.nref_max;
+  const int ldv = job.nvz + 2;
+  const RefineBox rb{job.velv + (size_t)sg.map * (job.nvx + 2) * ldv, ldv, (vnl - 1) * sgdl + 1,
+                     (vnt - 1) * sgdl + 1, job.gdx * sgdl, job.gdz * sgdl, vnl, vnr, vnt, vnb};
+  for (int node = lane; node < nrnx * nrnz; node += 32)
+    Sr[node] = 1.0 / refined_velocity(job, rb, node % nrnz + 1, node / nrnz + 1);
+  for (int q = lane; q < nrnx * nrnz; q += 32) w.S[q] = -1;
+  w.ld = gr.ld;
+  __syncwarp();
+  if (lane == 0)
+    init_source(w, gr, [&](int zz, int xx) { return refined_velocity(job, rb, zz, xx); }, sg.x, sg.z, fx);
+  __syncwarp();
+  march(w, gr, Sr, job.fom, 1, vnl, vnr, vnt, vnb, fx, tr);
+  // the refined nodes that map onto coarse nodes (fm2dray_cartesian.f90:365-383)
+  const int mx = (nrnx - 1) / sgdl + 1, mz = (nrnz - 1) / sgdl + 1;   // = vnr-vnl+1, vnb-vnt+1
+  double *tmpT = job.map_tmp_t + (size_t)solve * job.map_tmp_max;
+  short *tmpS = job.map_tmp_s + (size_t)solve * job.map_tmp_max;
+  for (int q = lane; q < mx * mz; q += 32) {
+    int a = q % mz, b = q / mz;
+    int k = a * sgdl + 1, l = b * sgdl + 1;
+    int r = lin(gr, k, l);
+    tmpT[q] = bit_store(w.T[r]);
+    tmpS[q] = w.S[r];
+  }
+}
+
+// Stage 2, the coarse grid: the refined box's times and states mapped in, the
+// narrow band repaired and re-heaped, travel with urg = 2 (or, without
+// refinement, the point source and travel with urg = 0); then the optional
+// time field and srtimes.
+template <class TT>
+__global__ void __launch_bounds__(32 * WARPS_PER_BLOCK_MAX)
+fm2d_coarse_kernel(Fm2dJob job, int warp_bytes) {
+  extern __shared__ __align__(16) unsigned char smem[];
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int solve = blockIdx.x * (blockDim.x >> 5) + warp;
+  if (solve >= job.nsolve) return;
+  SolveGeom sg;
+  if (!solve_geom(job, solve, sg)) {
     if (lane == 0) atomicExch(job.status, MCT_ERR_OUTSIDE);
     return;
   }
-  if (isx == nnx) isx = isx - 1;
-  if (isz == nnz) isz = isz - 1;
-  const int sgs = job.sgs, sgdl = job.sgdl;
-  const int vnl = max(isx - sgs, 1), vnr = min(isx + sgs, nnx);
-  const int vnt = max(isz - sgs, 1), vnb = min(isz + sgs, nnz);
+  const Grid2 gc = sg.gc;
+  const int nnx = gc.nnx, nnz = gc.nnz;
+  WarpStateT<TT> w = warp_state<TT>(smem + (size_t)warp * warp_bytes, nnx * nnz);
+  const Fx fx = time_scale<TT>(job);
+  const int map = sg.map, src = sg.src;
+  const double x = sg.x, z = sg.z;
+  const int sgdl = job.sgdl;
+  const int vnl = sg.vnl, vnr = sg.vnr, vnt = sg.vnt, vnb = sg.vnb;
+  const double *Vc = job.veln + (size_t)map * nnx * nnz;
+  const double *SLc = job.slon + (size_t)map * nnx * nnz;
+  Trace trace{job.trace_i ? job.trace_i + 3 * (job.trace_max / 2) : nullptr,
+              job.trace_t ? job.trace_t + job.trace_max / 2 : nullptr, job.trace_max / 2, 0};
+  Trace *tr = (job.trace_i && solve == job.trace_solve && lane == 0) ? &trace : nullptr;
+  w.ld = gc.ld;
+  for (int q = lane; q < nnx * nnz; q += 32) w.S[q] = -1;
+  __syncwarp();
   if (job.asgr == 1) {
     const int nrnx = (vnr - vnl) * sgdl + 1, nrnz = (vnb - vnt) * sgdl + 1;
-    Grid2 gr{nrnx, nrnz, nrnz, gc.gox + gc.dnx * (double)(vnl - 1), gc.goz + gc.dnz * (double)(vnt - 1),
-             dvx / (double)(job.gdx * sgdl), dvz / (double)(job.gdz * sgdl)};
-    double *Vr = job.vref + (size_t)solve * job.nref_max;
-    // bsplrefine (fm2dray_cartesian.f90:608-674)
-    {
-      const int nrxr = job.gdx * sgdl, nrzr = job.gdz * sgdl;
-      const int origx = (vnl - 1) * sgdl + 1, origz = (vnt - 1) * sgdl + 1;
-      const int ldv = job.nvz + 2;
-      const double *velv = job.velv + (size_t)map * (job.nvx + 2) * ldv;
-      for (int node = lane; node < nrnx * nrnz; node += 32) {
-        int idm1 = node % nrnz + 1, idm2 = node / nrnz + 1;
-        int st1 = idm1 + origz - 1, st2 = idm2 + origx - 1;
-        int i = (st1 - 1) / nrzr + 1; if (i > job.nvz - 1) i = job.nvz - 1;
-        int k = st1 - nrzr * (i - 1);
-        int j = (st2 - 1) / nrxr + 1; if (j > job.nvx - 1) j = job.nvx - 1;
-        int l = st2 - nrxr * (j - 1);
-        int c1 = job.gdz * (i - 1) + (k - 1) / sgdl + 1;
-        int c2 = job.gdx * (j - 1) + (l - 1) / sgdl + 1;
-        if (c1 < vnt || c1 > vnb || c2 < vnl || c2 > vnr) { Vr[node] = 0.0; continue; }
-        double u = (double)(l - 1) / (double)nrxr;
-        double v = (double)(k - 1) / (double)nrzr;
-        double sum[4];
-        for (int i1 = 1; i1 <= 4; ++i1) {
-          sum[i1 - 1] = 0.0;
-          for (int j1 = 1; j1 <= 4; ++j1)
-            sum[i1 - 1] = sum[i1 - 1] + bsw(j1 - 1, u) * velv[(size_t)(j - 2 + j1) * ldv + (i - 2 + i1)];
-          sum[i1 - 1] = bsw(i1 - 1, v) * sum[i1 - 1];
-        }
-        Vr[node] = sum[0] + sum[1] + sum[2] + sum[3];
-      }
-    }
-    for (int q = lane; q < nrnx * nrnz; q += 32) w.S[q] = -1;
-    w.ld = gr.ld;
-    __syncwarp();
-    if (lane == 0) init_source(w, gr, Vr, x, z, fx);
-    __syncwarp();
-    march(w, gr, Vr, job.fom, job.precision, 1, vnl, vnr, vnt, vnb, fx, tr);
-    // map refined onto coarse: gather the mapped refined nodes first
-    const int mx = (nrnx - 1) / sgdl + 1, mz = (nrnz - 1) / sgdl + 1;   // = vnr-vnl+1, vnb-vnt+1
-    double *tmpT = job.map_tmp_t + (size_t)solve * job.map_tmp_max;
-    short *tmpS = job.map_tmp_s + (size_t)solve * job.map_tmp_max;
-    for (int q = lane; q < mx * mz; q += 32) {
-      int a = q % mz, b = q / mz;
-      int k = a * sgdl + 1, l = b * sgdl + 1;
-      int r = lin(gr, k, l);
-      tmpT[q] = bit_store(w.T[r]);
-      tmpS[q] = w.S[r];
-    }
-    __syncwarp();
-    for (int q = lane; q < nnx * nnz; q += 32) w.S[q] = -1;
-    __syncwarp();
+    const int mx = (nrnx - 1) / sgdl + 1, mz = (nrnz - 1) / sgdl + 1;
+    const double *tmpT = job.map_tmp_t + (size_t)solve * job.map_tmp_max;
+    const short *tmpS = job.map_tmp_s + (size_t)solve * job.map_tmp_max;
     for (int q = lane; q < mx * mz; q += 32) {
       int a = q % mz, b = q / mz;
       int c = lin(gc, vnt + a, vnl + b);
@@ -737,7 +845,6 @@ fm2d_solve_kernel(Fm2dJob job, int warp_bytes) {
     }
     __syncwarp();
     // travel(urg=2): heap from all nodes marked close, i outer, j inner
-    w.ld = gc.ld;
     if (lane == 0) {
       w.ntr = 0;
       for (int i = 1; i <= nnx; ++i)
@@ -745,14 +852,11 @@ fm2d_solve_kernel(Fm2dJob job, int warp_bytes) {
           if (w.S[lin(gc, j, i)] > 0) addtree(w, gc, j, i);
     }
     __syncwarp();
-    march(w, gc, Vc, job.fom, job.precision, 2, vnl, vnr, vnt, vnb, fx, tr);
+    march(w, gc, SLc, job.fom, 2, vnl, vnr, vnt, vnb, fx, tr);
   } else {
-    for (int q = lane; q < nnx * nnz; q += 32) w.S[q] = -1;
-    w.ld = gc.ld;
+    if (lane == 0) init_source(w, gc, [&](int zz, int xx) { return Vc[lin(gc, zz, xx)]; }, x, z, fx);
     __syncwarp();
-    if (lane == 0) init_source(w, gc, Vc, x, z, fx);
-    __syncwarp();
-    march(w, gc, Vc, job.fom, job.precision, 0, vnl, vnr, vnt, vnb, fx, tr);
+    march(w, gc, SLc, job.fom, 0, vnl, vnr, vnt, vnb, fx, tr);
   }
   // optional travel-time field
   if (job.tfield) {
@@ -815,6 +919,31 @@ fm2d_solve_kernel(Fm2dJob job, int warp_bytes) {
 
 }  // namespace
 
+namespace {
+// Warps (solves) per block for kernel k with a per-warp shared-memory
+// footprint of wb bytes: the block size that keeps the most solves resident
+// per SM (shared memory, registers and the block limit all counted by the
+// occupancy calculator). Remembered per (kernel, footprint).
+template <class K>
+int warps_for(K k, int wb) {
+  static std::mutex mu;
+  static std::vector<std::pair<std::pair<const void *, int>, int>> memo;
+  std::lock_guard<std::mutex> lk(mu);
+  for (auto &m : memo)
+    if (m.first.first == (const void *)k && m.first.second == wb) return m.second;
+  int best = 0, best_warps = 0;
+  for (int wpb = 1; wpb <= WARPS_PER_BLOCK_MAX; ++wpb) {
+    const size_t bytes = (size_t)wpb * wb;
+    if (bytes > 227 * 1024) break;
+    int nb = 0;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, k, 32 * wpb, bytes) != cudaSuccess) continue;
+    if (nb * wpb > best_warps) { best_warps = nb * wpb; best = wpb; }
+  }
+  memo.push_back({{(const void *)k, wb}, best});
+  return best;
+}
+}  // namespace
+
 int fm2d_plan(const Fm2dJob &job, Fm2dPlan *plan) {
   const int nnx = (job.nvx - 1) * job.gdx + 1, nnz = (job.nvz - 1) * job.gdz + 1;
   int nodes = nnx * nnz;
@@ -828,27 +957,41 @@ int fm2d_plan(const Fm2dJob &job, Fm2dPlan *plan) {
   if (nodes_max > 32000) return MCT_ERR_ARG;   // int16 heap positions / node ids
   if (nnx > 256 || nnz > 256 || (job.asgr == 1 && 2 * job.sgs * job.sgdl + 1 > 256)) return MCT_ERR_ARG;
   const int tbytes = job.precision == 2 ? (int)sizeof(int) : (int)sizeof(double);
-  int wb = nodes_max * (tbytes + (int)sizeof(short) + (int)sizeof(unsigned short)) + 64;
-  wb = (wb + 15) & ~15;
-  int wpb = (227 * 1024) / wb;
-  if (wpb < 1) return MCT_ERR_ARG;
-  if (wpb > WARPS_PER_BLOCK_MAX) wpb = WARPS_PER_BLOCK_MAX;
   plan->nodes_max = nodes_max;
   plan->nref_max = nref;
   plan->map_tmp_max = tmp;
-  plan->warp_bytes = wb;
-  plan->warps_per_block = wpb;
+  plan->warp_bytes = solve_layout(tbytes, nodes).bytes;
+  plan->ref_warp_bytes = nref > 0 ? solve_layout(tbytes, nref).bytes : 0;
+  if (plan->warp_bytes > 227 * 1024 || plan->ref_warp_bytes > 227 * 1024) return MCT_ERR_ARG;
   return MCT_OK;
 }
 
-int launch_fm2d(const Fm2dJob &job, const Fm2dPlan &plan, cudaStream_t s) {
+namespace {
+template <class TT>
+int launch_solves(const Fm2dJob &job, const Fm2dPlan &plan, cudaStream_t s) {
   static bool attr = false;
   if (!attr) {
-    cudaFuncSetAttribute(fm2d_solve_kernel<double>, cudaFuncAttributeMaxDynamicSharedMemorySize, 227 * 1024);
-    cudaFuncSetAttribute(fm2d_solve_kernel<int>, cudaFuncAttributeMaxDynamicSharedMemorySize, 227 * 1024);
-    cudaFuncSetAttribute(fm2d_solve_kernel<float2>, cudaFuncAttributeMaxDynamicSharedMemorySize, 227 * 1024);
+    cudaFuncSetAttribute(fm2d_refined_kernel<TT>, cudaFuncAttributeMaxDynamicSharedMemorySize, 227 * 1024);
+    cudaFuncSetAttribute(fm2d_coarse_kernel<TT>, cudaFuncAttributeMaxDynamicSharedMemorySize, 227 * 1024);
     attr = true;
   }
+  if (job.asgr == 1) {
+    const int wpb = warps_for(fm2d_refined_kernel<TT>, plan.ref_warp_bytes);
+    if (wpb < 1) return MCT_ERR_ARG;
+    const int blocks = (job.nsolve + wpb - 1) / wpb;
+    fm2d_refined_kernel<TT><<<blocks, 32 * wpb, (size_t)plan.ref_warp_bytes * wpb, s>>>(job, plan.ref_warp_bytes);
+    MCT_CUDA_TRY(cudaGetLastError());
+  }
+  const int wpb = warps_for(fm2d_coarse_kernel<TT>, plan.warp_bytes);
+  if (wpb < 1) return MCT_ERR_ARG;
+  const int blocks = (job.nsolve + wpb - 1) / wpb;
+  fm2d_coarse_kernel<TT><<<blocks, 32 * wpb, (size_t)plan.warp_bytes * wpb, s>>>(job, plan.warp_bytes);
+  MCT_CUDA_TRY(cudaGetLastError());
+  return MCT_OK;
+}
+}  // namespace
+
+int launch_fm2d(const Fm2dJob &job, const Fm2dPlan &plan, cudaStream_t s) {
   if (job.precision == 2) {
     if (!job.vmin_bits) return MCT_ERR_ARG;
     set_int_kernel<<<1, 1, 0, s>>>(job.vmin_bits, 0x7f7fffff);   // FLT_MAX bits
@@ -857,14 +1000,7 @@ int launch_fm2d(const Fm2dJob &job, const Fm2dPlan &plan, cudaStream_t s) {
   gridder_kernel<<<job.nmaps, 256, 0, s>>>(job);
   MCT_CUDA_TRY(cudaGetLastError());
   if (job.nsolve == 0) return MCT_OK;
-  int wpb = plan.warps_per_block;
-  int blocks = (job.nsolve + wpb - 1) / wpb;
-  if (job.precision == 2)
-    fm2d_solve_kernel<int><<<blocks, 32 * wpb, (size_t)plan.warp_bytes * wpb, s>>>(job, plan.warp_bytes);
-  else if (job.precision == 1)
-    fm2d_solve_kernel<float2><<<blocks, 32 * wpb, (size_t)plan.warp_bytes * wpb, s>>>(job, plan.warp_bytes);
-  else
-    fm2d_solve_kernel<double><<<blocks, 32 * wpb, (size_t)plan.warp_bytes * wpb, s>>>(job, plan.warp_bytes);
-  MCT_CUDA_TRY(cudaGetLastError());
-  return MCT_OK;
+  if (job.precision == 2) return launch_solves<int>(job, plan, s);
+  if (job.precision == 1) return launch_solves<float2>(job, plan, s);
+  return launch_solves<double>(job, plan, s);
 }

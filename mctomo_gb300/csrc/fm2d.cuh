@@ -7,11 +7,12 @@ struct Fm2dJob {
   int nvx, nvz;              // B-spline vertex grid
   double goxd, gozd, dvxd, dvzd;
   int gdx, gdz, asgr, sgdl, sgs, fom;
-  int precision;             // 0 FP64 as the reference, 1 FP32 quadratic on FP64 times, 2 FP32 on fixed-point times
+  int precision;             // 0 FP64 as the reference, 1 double-float (FP32 pairs), 2 FP32 on fixed-point times
   int *vmin_bits;            // scratch (precision 2): smallest vertex velocity, float bits
   const double *velv;        // [nmaps][nvx+2][nvz+2] padded vertex grids (Fortran (nvz+2,nvx+2))
   double *veln;              // [nmaps][nnx][nnz] scratch: B-spline node velocities
-  double *vref;              // [nsolve][nref_max] scratch: refined source-box velocities
+  double *slon;              // [nmaps][nnx][nnz] scratch: their slownesses (1 / veln)
+  double *sref;              // [nsolve][nref_max] scratch: refined source-box slownesses
   double *map_tmp_t;         // [nsolve][map_tmp_max] scratch
   short *map_tmp_s;          // [nsolve][map_tmp_max] scratch
   int nsrc, nrc;
@@ -30,7 +31,9 @@ struct Fm2dJob {
 };
 
 struct Fm2dPlan {
-  int nodes_max, nref_max, map_tmp_max, warp_bytes, warps_per_block;
+  int nodes_max, nref_max, map_tmp_max;
+  int warp_bytes;       // shared memory per solve, coarse-grid stage
+  int ref_warp_bytes;   // shared memory per solve, refined source-box stage (asgr = 1)
 };
 
 int fm2d_plan(const Fm2dJob &job, Fm2dPlan *plan);

@@ -82,6 +82,7 @@ int mct_surf_create(const mct_grid *g, const mct_surf_settings *st, const mct_su
       sizeof(double) * 2 * (nsrc + nrev), sizeof(int) * np * npairs, sizeof(int2) * nsolve,
       sizeof(double) * (size_t)fp.nref_max * nsolve, sizeof(double) * (size_t)fp.map_tmp_max * nsolve,
       sizeof(short) * (size_t)fp.map_tmp_max * nsolve, sizeof(double) * (size_t)nn * nz2 * np * nslots,
+      sizeof(double) * (size_t)nn * nz2 * np * nslots,
       // batch working state
       sizeof(double) * (size_t)nslots * ncell_max * 3, sizeof(int) * (size_t)nslots * nodes,
       sizeof(double) * (size_t)nslots * nodes * 3, sizeof(int) * nslots, sizeof(int) * (size_t)nslots * nodes,
@@ -110,10 +111,11 @@ int mct_surf_create(const mct_grid *g, const mct_surf_settings *st, const mct_su
   double *xy = cv.take<double>(2 * (nsrc + nrev));
   int *srs = cv.take<int>((size_t)np * npairs);
   int2 *solves = cv.take<int2>(nsolve);
-  fj.vref = cv.take<double>((size_t)fp.nref_max * nsolve);
+  fj.sref = cv.take<double>((size_t)fp.nref_max * nsolve);
   fj.map_tmp_t = cv.take<double>((size_t)fp.map_tmp_max * nsolve);
   fj.map_tmp_s = cv.take<short>((size_t)fp.map_tmp_max * nsolve);
   fj.veln = cv.take<double>((size_t)nn * nz2 * np * nslots);
+  fj.slon = cv.take<double>((size_t)nn * nz2 * np * nslots);
   b.params = cv.take<double>((size_t)nslots * ncell_max * 3);
   b.sites = cv.take<int>((size_t)nslots * nodes);
   b.vp = cv.take<double>((size_t)nslots * nodes * 3);
