@@ -342,7 +342,8 @@ int mct_modrays_batch(int nmaps, int nsrc, const double *scx, const double *scz,
   size_t bytes = carve_size({sizeof(double) * nv * nmaps, sizeof(double) * (size_t)nnx * nnz * nmaps,
                              sizeof(double) * (size_t)nnx * nnz * nmaps,
                              sizeof(double) * (size_t)plan.nref_max * ns, sizeof(double) * (size_t)plan.map_tmp_max * ns,
-                             sizeof(short) * (size_t)plan.map_tmp_max * ns, sizeof(double) * 2 * (nsrc + nrc),
+                             sizeof(short) * (size_t)plan.map_tmp_max * ns, sizeof(int) * (ns + 1),
+                             sizeof(double) * 2 * (nsrc + nrc),
                              sizeof(int) * (size_t)srs_nmaps * nsrc * nrc, sizeof(int2) * ns,
                              sizeof(double) * (size_t)nmaps * nsrc * nrc,
                              tfield ? sizeof(double) * (size_t)nmaps * nsrc * nnx * nnz : 0, sizeof(int),
@@ -355,6 +356,8 @@ int mct_modrays_batch(int nmaps, int nsrc, const double *scx, const double *scz,
   job.sref = cv.take<double>((size_t)plan.nref_max * ns);
   job.map_tmp_t = cv.take<double>((size_t)plan.map_tmp_max * ns);
   job.map_tmp_s = cv.take<short>((size_t)plan.map_tmp_max * ns);
+  job.ovf_list = cv.take<int>(ns + 1);
+  job.ovf_count = job.ovf_list + ns;
   double *d_xy = cv.take<double>(2 * (nsrc + nrc));
   int *d_srs = cv.take<int>((size_t)srs_nmaps * nsrc * nrc);
   int2 *d_solves = cv.take<int2>(ns);

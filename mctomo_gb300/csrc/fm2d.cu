@@ -39,6 +39,8 @@ template <class TT> struct WarpStateT {
   unsigned short *H;  // heap, 1-based: H[p] = packed node ((ix-1) << 8) | (iz-1)
   int ntr;
   int ld;
+  int cap;            // heap capacity (entries)
+  bool overflow;      // a node did not fit: the solve is abandoned and redone
 };
 using WarpState = WarpStateT<double>;
 
@@ -79,6 +81,7 @@ __device__ __forceinline__ void sift_up(WarpStateT<TT> &w, int me, unsigned shor
 // addtree: a far node joins the heap with time tme (already stored in T)
 template <class TT>
 __device__ __forceinline__ void addtree(WarpStateT<TT> &w, const Grid2 &g, int iz, int ix, TT tme) {
+  if (w.ntr >= w.cap) { w.overflow = true; return; }
   w.ntr = w.ntr + 1;
   sift_up(w, lin(g, iz, ix), pack(iz, ix), w.ntr, tme);
 }
@@ -129,17 +132,23 @@ __device__ void downtree(WarpStateT<TT> &w) {
   w.S[ln] = (short)hole;
 }
 
-// Shared-memory layout of one solve: T [n], S [n], H [n + 2] (1-based heap),
-// each array starting on a 16-byte boundary.
+// Shared-memory layout of one solve: T [n], S [n], H [cap + 2] (1-based
+// heap of at most cap entries), each array starting on a 16-byte boundary.
 __host__ __device__ __forceinline__ int align16(int b) { return (b + 15) & ~15; }
 struct SolveLayout { int offS, offH, bytes; };
-__host__ __device__ __forceinline__ SolveLayout solve_layout(int tbytes, int n) {
+__host__ __device__ __forceinline__ SolveLayout solve_layout(int tbytes, int n, int cap) {
   SolveLayout L;
   L.offS = align16(tbytes * n);
   L.offH = L.offS + align16(2 * n);
-  L.bytes = L.offH + align16(2 * (n + 2));
+  L.bytes = L.offH + align16(2 * (cap + 2));
   return L;
 }
+// Heap capacity of the refined source-box stage. The heap holds the narrow
+// band, a closed front around the source (a few hundred nodes on the largest
+// box), so a capacity well below the node count frees shared memory for more
+// resident solves; a solve whose band outgrows it is redone with a full-size
+// heap (see the overflow pass below).
+constexpr int REFINED_HEAP_CAP = 1024;
 
 // ---- upwind arithmetic ------------------------------------------------------
 __device__ __forceinline__ double quad_root(double a, double b, double c) {
@@ -214,17 +223,7 @@ __device__ __forceinline__ DF dsqrt(DF a) {
 }
 __device__ __forceinline__ DF f2df(float2 v) { return DF{v.x, v.y}; }
 
-__device__ __forceinline__ DF quad_root_df(DF a, DF b, DF c) {
-  DF rd1 = dsub(dmul(b, b), dmul(dmulf(a, 4.f), c));
-  if (rd1.hi < 0.f) rd1 = df(0.f);
-  return ddiv(dadd(dneg(b), dsqrt(rd1)), dmulf(a, 2.f));
-}
 
-__device__ __forceinline__ float quad_rootf(float a, float b, float c) {
-  float rd1 = b * b - 4.0f * a * c;
-  if (rd1 < 0.0f) rd1 = 0.0f;
-  return __fdividef(-b + sqrtf(rd1), 2.0f * a);
-}
 
 // Fixed-point variant (precision == 2): times are int32 in units of
 // 2^-shift s, each update's quadratic is solved in FP32 on the neighbours'
@@ -296,10 +295,47 @@ __device__ __forceinline__ bool combo_stencil(const WarpStateT<TT> &w, const Gri
 }
 
 
+// Per-march constants of the reduced-precision updates. Every two-term case
+// is a W^2 + 2 B W + c = 0 with a = vv + m uu fixed by the grid spacing, so a
+// and 1/a are computed once per march for the four cases (X, Z) = (2, 2),
+// (2, 1), (1, 2), (1, 1); the root is then (-B + sqrt(B^2 - a c)) / a with
+// no division. A one-term case (alpha T - R)^2 / h^2 = s^2 has the root
+// T = (R + h s) / alpha, again without a division or a square root.
+template <class TT> struct UpdConst {
+  __device__ void init(const Grid2 &) {}
+};
+template <> struct UpdConst<float2> {
+  DF dnx, dnz, hx1, hz1, a[4], ia[4];
+  __device__ void init(const Grid2 &g) {
+    dnx = df_from(g.dnx); dnz = df_from(g.dnz);
+    hx1 = dmul(dnx, dnx); hz1 = dmul(dnz, dnz);
+    const DF hx2 = dmulf(hx1, 4.f), hz2 = dmulf(hz1, 4.f);
+    a[0] = dadd(hz2, hx2);
+    a[1] = dadd(hx2, dmulf(hz1, 9.f));
+    a[2] = dadd(hz2, dmulf(hx1, 9.f));
+    a[3] = dadd(hz1, hx1);
+#pragma unroll
+    for (int i = 0; i < 4; ++i) ia[i] = ddiv(df(1.f), a[i]);
+  }
+};
+template <> struct UpdConst<int> {
+  float dnx, dnz, a[4], ia[4];
+  __device__ void init(const Grid2 &g) {
+    dnx = (float)g.dnx; dnz = (float)g.dnz;
+    const float hx1 = dnx * dnx, hz1 = dnz * dnz;
+    a[0] = 4.f * hz1 + 4.f * hx1;
+    a[1] = 4.f * hx1 + 9.f * hz1;
+    a[2] = 4.f * hz1 + 9.f * hx1;
+    a[3] = hz1 + hx1;
+#pragma unroll
+    for (int i = 0; i < 4; ++i) ia[i] = 1.f / a[i];
+  }
+};
+
 // FP64, the reference's arithmetic (precision 0). slown is the node's
 // slowness 1/V, precomputed per node with the reference's division.
 __device__ double combo_time(const WarpStateT<double> &w, const Grid2 &g, const Stencil &s, double slown, int fom,
-                             const Fx &) {
+                             const Fx &, const UpdConst<double> &) {
   const double ss = slown * slown;
   const double u2x = 2.0 * g.dnx, u2z = 2.0 * g.dnz;
   const double hx1 = g.dnx * g.dnx, hz1 = g.dnz * g.dnz, hx2 = u2x * u2x, hz2 = u2z * u2z;
@@ -335,90 +371,96 @@ __device__ double combo_time(const WarpStateT<double> &w, const Grid2 &g, const 
   return (tref + quad_root(a, b, c)) / tdiv;
 }
 
-// Double-float (precision 1): the same cases in FP32-pair arithmetic.
-__device__ float2 combo_time(const WarpStateT<float2> &w, const Grid2 &g, const Stencil &s, double sl, int fom,
-                             const Fx &) {
+// Double-float (precision 1): the same cases and stencils in FP32-pair
+// arithmetic, with the division-free roots above.
+__device__ float2 combo_time(const WarpStateT<float2> &w, const Grid2 &, const Stencil &s, double sl, int,
+                             const Fx &, const UpdConst<float2> &K) {
   const DF slown = df_from(sl);
-  const DF ss = dmul(slown, slown);
-  const DF dnx = df_from(g.dnx), dnz = df_from(g.dnz);
-  const DF u2x = dmulf(dnx, 2.f), u2z = dmulf(dnz, 2.f);
   const DF Tj = f2df(w.T[s.lj]), Tk = f2df(w.T[s.lk]);
-  DF a = df(1.f), b = df(0.f), c, tref;
-  float tdiv = 1.f;
+  DF trav;
+  bool third = false;
   if (s.X && s.Z) {
-    DF uu, vv, em;
-    float m = 1.f, kb = 2.f;
+    DF uu, vv, em, tref, A, IA;
+    float k = 1.f;
     if (s.X == 2 && s.Z == 2) {
       tref = dsub(dmulf(Tj, 4.f), f2df(w.T[s.lj2]));
       em = dadd(dsub(tref, dmulf(Tk, 4.f)), f2df(w.T[s.lk2]));
-      uu = dmul(u2x, u2x); vv = dmul(u2z, u2z); tdiv = 3.f;
+      uu = dmulf(K.hx1, 4.f); vv = dmulf(K.hz1, 4.f); A = K.a[0]; IA = K.ia[0]; third = true;
     } else if (s.X == 2) {
       em = dadd(dsub(dmulf(Tk, 3.f), dmulf(Tj, 4.f)), f2df(w.T[s.lj2]));
-      uu = dmul(dnz, dnz); vv = dmul(u2x, u2x); m = 9.f; kb = 6.f; tref = Tk;
+      uu = K.hz1; vv = dmulf(K.hx1, 4.f); k = 3.f; A = K.a[1]; IA = K.ia[1]; tref = Tk;
     } else if (s.Z == 2) {
       em = dadd(dsub(dmulf(Tj, 3.f), dmulf(Tk, 4.f)), f2df(w.T[s.lk2]));
-      uu = dmul(dnx, dnx); vv = dmul(u2z, u2z); m = 9.f; kb = 6.f; tref = Tj;
+      uu = K.hx1; vv = dmulf(K.hz1, 4.f); k = 3.f; A = K.a[2]; IA = K.ia[2]; tref = Tj;
     } else {
       em = dsub(Tj, Tk);
-      uu = dmul(dnx, dnx); vv = dmul(dnz, dnz); tref = Tj;
+      uu = K.hx1; vv = K.hz1; A = K.a[3]; IA = K.ia[3]; tref = Tj;
     }
-    a = dadd(vv, dmulf(uu, m));
-    b = dmul(dmulf(em, kb), uu);
-    c = dmul(uu, dsub(dmul(em, em), dmul(ss, vv)));
-  } else if (s.X) {
-    if (s.X == 2) { tref = dsub(dmulf(Tj, 4.f), f2df(w.T[s.lj2])); c = dneg(dmul(dmul(u2x, u2x), ss)); tdiv = 3.f; }
-    else { tref = Tj; c = dneg(dmul(ss, dmul(dnx, dnx))); }
+    const DF B = dmulf(dmul(em, uu), k);
+    const DF c = dmul(uu, dsub(dmul(em, em), dmul(dmul(slown, slown), vv)));
+    DF disc = dsub(dmul(B, B), dmul(A, c));
+    if (disc.hi < 0.f) disc = df(0.f);
+    trav = dadd(tref, dmul(dsub(dsqrt(disc), B), IA));
   } else {
-    if (s.Z == 2) { tref = dsub(dmulf(Tk, 4.f), f2df(w.T[s.lk2])); c = dneg(dmul(dmul(u2z, u2z), ss)); tdiv = 3.f; }
-    else if (fom == 1) { tref = Tk; c = dneg(dmul(ss, dmul(dnz, dnz))); }
-    else { const DF sd = dmul(slown, dnz); tref = Tk; c = dneg(dmul(sd, sd)); }
+    DF tref, h;
+    if (s.X) {
+      if (s.X == 2) { tref = dsub(dmulf(Tj, 4.f), f2df(w.T[s.lj2])); h = dmulf(K.dnx, 2.f); third = true; }
+      else { tref = Tj; h = K.dnx; }
+    } else {
+      if (s.Z == 2) { tref = dsub(dmulf(Tk, 4.f), f2df(w.T[s.lk2])); h = dmulf(K.dnz, 2.f); third = true; }
+      else { tref = Tk; h = K.dnz; }
+    }
+    trav = dadd(tref, dmul(h, slown));
   }
-  DF trav = dadd(tref, quad_root_df(a, b, c));
-  if (tdiv != 1.f) trav = dmul(trav, df_from(1.0 / 3.0));
+  if (third) trav = dmul(trav, df_from(1.0 / 3.0));
   return make_float2(trav.hi, trav.lo);
 }
 
 // Fixed point (precision 2): the same cases in FP32 on times taken relative
 // to the combination's first accepted neighbour, rounded back to the
 // fixed-point grid.
-__device__ int combo_time(const WarpStateT<int> &w, const Grid2 &g, const Stencil &s, double sl, int fom,
-                          const Fx &fx) {
+__device__ int combo_time(const WarpStateT<int> &w, const Grid2 &, const Stencil &s, double sl, int,
+                          const Fx &fx, const UpdConst<int> &K) {
   const float slown = (float)sl;
-  const float ss = slown * slown;
-  const float dnx = (float)g.dnx, dnz = (float)g.dnz;
-  const float u2x = 2.f * dnx, u2z = 2.f * dnz;
   const int base = s.X ? w.T[s.lj] : w.T[s.lk];
   auto sh = [&](int l) { return (float)(w.T[l] - base) * fx.inv; };
   const float Tj = sh(s.lj), Tk = sh(s.lk);
-  float a = 1.f, b = 0.f, c, tref, tdiv = 1.f;
+  float trav;
+  bool third = false;
   if (s.X && s.Z) {
-    float uu, vv, m = 1.f, kb = 2.f, em;
+    float uu, vv, em, tref, A, IA, k = 1.f;
+    const float hx1 = K.dnx * K.dnx, hz1 = K.dnz * K.dnz;
     if (s.X == 2 && s.Z == 2) {
       tref = 4.f * Tj - sh(s.lj2);
       em = (tref - 4.f * Tk) + sh(s.lk2);
-      uu = u2x * u2x; vv = u2z * u2z; tdiv = 3.f;
+      uu = 4.f * hx1; vv = 4.f * hz1; A = K.a[0]; IA = K.ia[0]; third = true;
     } else if (s.X == 2) {
       em = (3.f * Tk - 4.f * Tj) + sh(s.lj2);
-      uu = dnz * dnz; vv = u2x * u2x; m = 9.f; kb = 6.f; tref = Tk;
+      uu = hz1; vv = 4.f * hx1; k = 3.f; A = K.a[1]; IA = K.ia[1]; tref = Tk;
     } else if (s.Z == 2) {
       em = (3.f * Tj - 4.f * Tk) + sh(s.lk2);
-      uu = dnx * dnx; vv = u2z * u2z; m = 9.f; kb = 6.f; tref = Tj;
+      uu = hx1; vv = 4.f * hz1; k = 3.f; A = K.a[2]; IA = K.ia[2]; tref = Tj;
     } else {
       em = Tj - Tk;
-      uu = dnx * dnx; vv = dnz * dnz; tref = Tj;
+      uu = hx1; vv = hz1; A = K.a[3]; IA = K.ia[3]; tref = Tj;
     }
-    a = vv + m * uu;
-    b = (kb * em) * uu;
-    c = uu * (em * em - ss * vv);
-  } else if (s.X) {
-    if (s.X == 2) { tref = 4.f * Tj - sh(s.lj2); c = -((u2x * u2x) * ss); tdiv = 3.f; }
-    else { tref = Tj; c = -(ss * (dnx * dnx)); }
+    const float B = k * (em * uu);
+    const float c = uu * (em * em - (slown * slown) * vv);
+    float disc = B * B - A * c;
+    if (disc < 0.f) disc = 0.f;
+    trav = tref + (sqrtf(disc) - B) * IA;
   } else {
-    if (s.Z == 2) { tref = 4.f * Tk - sh(s.lk2); c = -((u2z * u2z) * ss); tdiv = 3.f; }
-    else if (fom == 1) { tref = Tk; c = -(ss * (dnz * dnz)); }
-    else { const float sd = slown * dnz; tref = Tk; c = -(sd * sd); }
+    float tref, h;
+    if (s.X) {
+      if (s.X == 2) { tref = 4.f * Tj - sh(s.lj2); h = 2.f * K.dnx; third = true; }
+      else { tref = Tj; h = K.dnx; }
+    } else {
+      if (s.Z == 2) { tref = 4.f * Tk - sh(s.lk2); h = 2.f * K.dnz; third = true; }
+      else { tref = Tk; h = K.dnz; }
+    }
+    trav = tref + h * slown;
   }
-  const float trav = __fdividef(tref + quad_rootf(a, b, c), tdiv);
+  if (third) trav = trav * (1.f / 3.f);
   long long r = (long long)base + llrintf(trav * fx.scale);
   return (int)min(max(r, 0LL), (long long)INT_MAX - 1);
 }
@@ -484,9 +526,11 @@ __device__ void march(WarpStateT<TT> &w, const Grid2 &g, const double *SL, int f
   // next, loaded while lane 0 sifts (a global-memory load off the critical path)
   int pred = -1;
   double sl_pred = 0.0;
+  UpdConst<TT> K;
+  K.init(g);
   for (;;) {
     int pk = -1;   // accepted node ((ix-1) << 8) | (iz-1), or -1 to stop
-    if (lane == 0 && w.ntr > 0) {
+    if (lane == 0 && w.ntr > 0 && !w.overflow) {
       const int top = w.H[1];
       const int iz = (top & 255) + 1, ix = (top >> 8) + 1;
       bool go = true;
@@ -528,7 +572,7 @@ __device__ void march(WarpStateT<TT> &w, const Grid2 &g, const double *SL, int f
         Stencil sc;
         if (st != 0 && combo_stencil(w, g, nz_, nx_, cmb, fom, sc)) {
           have = true;
-          cand = combo_time(w, g, sc, pk == pred ? sl_pred : SL[ln], fom, fx);
+          cand = combo_time(w, g, sc, pk == pred ? sl_pred : SL[ln], fom, fx, K);
         }
       }
     }
@@ -726,9 +770,11 @@ __device__ __forceinline__ Fx time_scale(const Fm2dJob &job) {
 }
 
 template <class TT>
-__device__ __forceinline__ WarpStateT<TT> warp_state(unsigned char *base, int nodes) {
+__device__ __forceinline__ WarpStateT<TT> warp_state(unsigned char *base, int nodes, int cap) {
   WarpStateT<TT> w;
-  const SolveLayout lay = solve_layout((int)sizeof(TT), nodes);
+  const SolveLayout lay = solve_layout((int)sizeof(TT), nodes, cap);
+  w.cap = cap;
+  w.overflow = false;
   w.T = reinterpret_cast<TT *>(base);
   w.S = reinterpret_cast<short *>(base + lay.offS);
   w.H = reinterpret_cast<unsigned short *>(base + lay.offH);
@@ -742,16 +788,23 @@ __device__ __forceinline__ WarpStateT<TT> warp_state(unsigned char *base, int no
 // of the box nodes that coincide with coarse nodes in the mapping scratch.
 // The refined box has up to (2*sgs*sgdl+1)^2 nodes, more than the coarse grid
 // usually has, so this stage runs with its own (smaller) warps per block.
+// First pass: every solve with a heap of REFINED_HEAP_CAP entries, solves
+// whose band outgrows it listed in job.ovf_list. Overflow pass (redo = 1): the
+// listed solves again with a heap as large as the box.
 template <class TT>
 __global__ void __launch_bounds__(32 * WARPS_PER_BLOCK_MAX)
-fm2d_refined_kernel(Fm2dJob job, int warp_bytes) {
+fm2d_refined_kernel(Fm2dJob job, int warp_bytes, int heap_cap, int redo) {
   extern __shared__ __align__(16) unsigned char smem[];
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  const int solve = blockIdx.x * (blockDim.x >> 5) + warp;
+  int solve = blockIdx.x * (blockDim.x >> 5) + warp;
+  if (redo) {
+    if (solve >= *job.ovf_count) return;
+    solve = job.ovf_list[solve];
+  }
   if (solve >= job.nsolve) return;
   SolveGeom sg;
   if (!solve_geom(job, solve, sg)) return;   // reported by the coarse stage
-  WarpStateT<TT> w = warp_state<TT>(smem + (size_t)warp * warp_bytes, job.nref_max);
+  WarpStateT<TT> w = warp_state<TT>(smem + (size_t)warp * warp_bytes, job.nref_max, heap_cap);
   const Fx fx = time_scale<TT>(job);
   const int sgdl = job.sgdl;
   const int vnl = sg.vnl, vnr = sg.vnr, vnt = sg.vnt, vnb = sg.vnb;
@@ -776,6 +829,10 @@ fm2d_refined_kernel(Fm2dJob job, int warp_bytes) {
     init_source(w, gr, [&](int zz, int xx) { return refined_velocity(job, rb, zz, xx); }, sg.x, sg.z, fx);
   __syncwarp();
   march(w, gr, Sr, job.fom, 1, vnl, vnr, vnt, vnb, fx, tr);
+  if (__shfl_sync(0xffffffffu, (int)w.overflow, 0)) {
+    if (lane == 0) job.ovf_list[atomicAdd(job.ovf_count, 1)] = solve;
+    return;
+  }
   // the refined nodes that map onto coarse nodes (fm2dray_cartesian.f90:365-383)
   const int mx = (nrnx - 1) / sgdl + 1, mz = (nrnz - 1) / sgdl + 1;   // = vnr-vnl+1, vnb-vnt+1
   double *tmpT = job.map_tmp_t + (size_t)solve * job.map_tmp_max;
@@ -807,7 +864,7 @@ fm2d_coarse_kernel(Fm2dJob job, int warp_bytes) {
   }
   const Grid2 gc = sg.gc;
   const int nnx = gc.nnx, nnz = gc.nnz;
-  WarpStateT<TT> w = warp_state<TT>(smem + (size_t)warp * warp_bytes, nnx * nnz);
+  WarpStateT<TT> w = warp_state<TT>(smem + (size_t)warp * warp_bytes, nnx * nnz, nnx * nnz);
   const Fx fx = time_scale<TT>(job);
   const int map = sg.map, src = sg.src;
   const double x = sg.x, z = sg.z;
@@ -944,6 +1001,18 @@ int warps_for(K k, int wb) {
 }
 }  // namespace
 
+namespace {
+int g_ref_heap_cap = REFINED_HEAP_CAP;
+}  // namespace
+
+// Test hook (not part of the C ABI): the refined-stage heap capacity used by
+// plans made after the call; cap < 4 restores the default. Small capacities
+// force the overflow pass.
+extern "C" int mct_debug_fm2d_heap_cap(int cap) {
+  g_ref_heap_cap = cap < 4 ? REFINED_HEAP_CAP : cap;
+  return MCT_OK;
+}
+
 int fm2d_plan(const Fm2dJob &job, Fm2dPlan *plan) {
   const int nnx = (job.nvx - 1) * job.gdx + 1, nnz = (job.nvz - 1) * job.gdz + 1;
   int nodes = nnx * nnz;
@@ -960,9 +1029,11 @@ int fm2d_plan(const Fm2dJob &job, Fm2dPlan *plan) {
   plan->nodes_max = nodes_max;
   plan->nref_max = nref;
   plan->map_tmp_max = tmp;
-  plan->warp_bytes = solve_layout(tbytes, nodes).bytes;
-  plan->ref_warp_bytes = nref > 0 ? solve_layout(tbytes, nref).bytes : 0;
-  if (plan->warp_bytes > 227 * 1024 || plan->ref_warp_bytes > 227 * 1024) return MCT_ERR_ARG;
+  plan->warp_bytes = solve_layout(tbytes, nodes, nodes).bytes;
+  plan->ref_heap_cap = nref < g_ref_heap_cap ? nref : g_ref_heap_cap;
+  plan->ref_warp_bytes = nref > 0 ? solve_layout(tbytes, nref, plan->ref_heap_cap).bytes : 0;
+  plan->ref_full_warp_bytes = nref > 0 ? solve_layout(tbytes, nref, nref).bytes : 0;
+  if (plan->warp_bytes > 227 * 1024 || plan->ref_full_warp_bytes > 227 * 1024) return MCT_ERR_ARG;
   return MCT_OK;
 }
 
@@ -976,11 +1047,23 @@ int launch_solves(const Fm2dJob &job, const Fm2dPlan &plan, cudaStream_t s) {
     attr = true;
   }
   if (job.asgr == 1) {
-    const int wpb = warps_for(fm2d_refined_kernel<TT>, plan.ref_warp_bytes);
+    if (!job.ovf_list || !job.ovf_count) return MCT_ERR_ARG;
+    MCT_CUDA_TRY(cudaMemsetAsync(job.ovf_count, 0, sizeof(int), s));
+    int wpb = warps_for(fm2d_refined_kernel<TT>, plan.ref_warp_bytes);
     if (wpb < 1) return MCT_ERR_ARG;
-    const int blocks = (job.nsolve + wpb - 1) / wpb;
-    fm2d_refined_kernel<TT><<<blocks, 32 * wpb, (size_t)plan.ref_warp_bytes * wpb, s>>>(job, plan.ref_warp_bytes);
+    int blocks = (job.nsolve + wpb - 1) / wpb;
+    fm2d_refined_kernel<TT><<<blocks, 32 * wpb, (size_t)plan.ref_warp_bytes * wpb, s>>>(
+        job, plan.ref_warp_bytes, plan.ref_heap_cap, 0);
     MCT_CUDA_TRY(cudaGetLastError());
+    if (plan.ref_heap_cap < job.nref_max) {
+      // overflow pass: blocks beyond the device-side count exit at once
+      wpb = warps_for(fm2d_refined_kernel<TT>, plan.ref_full_warp_bytes);
+      if (wpb < 1) return MCT_ERR_ARG;
+      blocks = (job.nsolve + wpb - 1) / wpb;
+      fm2d_refined_kernel<TT><<<blocks, 32 * wpb, (size_t)plan.ref_full_warp_bytes * wpb, s>>>(
+          job, plan.ref_full_warp_bytes, job.nref_max, 1);
+      MCT_CUDA_TRY(cudaGetLastError());
+    }
   }
   const int wpb = warps_for(fm2d_coarse_kernel<TT>, plan.warp_bytes);
   if (wpb < 1) return MCT_ERR_ARG;

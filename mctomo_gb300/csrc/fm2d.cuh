@@ -15,6 +15,8 @@ struct Fm2dJob {
   double *sref;              // [nsolve][nref_max] scratch: refined source-box slownesses
   double *map_tmp_t;         // [nsolve][map_tmp_max] scratch
   short *map_tmp_s;          // [nsolve][map_tmp_max] scratch
+  int *ovf_list;             // [nsolve] scratch: solves whose refined-box heap overflowed
+  int *ovf_count;            // [1] scratch: their number
   int nsrc, nrc;
   const double *scx, *scz, *rcx, *rcz;
   const int *srs;            // [srs_nmaps][nsrc][nrc] path flags
@@ -32,8 +34,10 @@ struct Fm2dJob {
 
 struct Fm2dPlan {
   int nodes_max, nref_max, map_tmp_max;
-  int warp_bytes;       // shared memory per solve, coarse-grid stage
-  int ref_warp_bytes;   // shared memory per solve, refined source-box stage (asgr = 1)
+  int warp_bytes;            // shared memory per solve, coarse-grid stage
+  int ref_heap_cap;          // heap entries of the refined source-box stage (asgr = 1)
+  int ref_warp_bytes;        // shared memory per solve of that stage
+  int ref_full_warp_bytes;   // the same with a heap as large as the box (overflow pass)
 };
 
 int fm2d_plan(const Fm2dJob &job, Fm2dPlan *plan);

@@ -81,7 +81,8 @@ int mct_surf_create(const mct_grid *g, const mct_surf_settings *st, const mct_su
       sizeof(double) * np, sizeof(int) * np * npairs, sizeof(double) * np * npairs, sizeof(double) * np * npairs,
       sizeof(double) * 2 * (nsrc + nrev), sizeof(int) * np * npairs, sizeof(int2) * nsolve,
       sizeof(double) * (size_t)fp.nref_max * nsolve, sizeof(double) * (size_t)fp.map_tmp_max * nsolve,
-      sizeof(short) * (size_t)fp.map_tmp_max * nsolve, sizeof(double) * (size_t)nn * nz2 * np * nslots,
+      sizeof(short) * (size_t)fp.map_tmp_max * nsolve, sizeof(int) * (nsolve + 1),
+      sizeof(double) * (size_t)nn * nz2 * np * nslots,
       sizeof(double) * (size_t)nn * nz2 * np * nslots,
       // batch working state
       sizeof(double) * (size_t)nslots * ncell_max * 3, sizeof(int) * (size_t)nslots * nodes,
@@ -114,6 +115,8 @@ int mct_surf_create(const mct_grid *g, const mct_surf_settings *st, const mct_su
   fj.sref = cv.take<double>((size_t)fp.nref_max * nsolve);
   fj.map_tmp_t = cv.take<double>((size_t)fp.map_tmp_max * nsolve);
   fj.map_tmp_s = cv.take<short>((size_t)fp.map_tmp_max * nsolve);
+  fj.ovf_list = cv.take<int>(nsolve + 1);
+  fj.ovf_count = fj.ovf_list + nsolve;
   fj.veln = cv.take<double>((size_t)nn * nz2 * np * nslots);
   fj.slon = cv.take<double>((size_t)nn * nz2 * np * nslots);
   b.params = cv.take<double>((size_t)nslots * ncell_max * 3);

@@ -90,6 +90,30 @@ def test_modrays_batch_surface_shape_matches_oracle(orc, gpulib):
         assert np.max(np.abs(got[mp][m] - exp[m])) <= TOL
 
 
+@pytest.mark.parametrize("cap", [16, 64])
+def test_modrays_heap_overflow_pass_matches_oracle(orc, gpulib, cap):
+    # a refined-stage heap far smaller than the narrow band: nearly every
+    # solve overflows the first pass and is redone with a full heap
+    rng = np.random.default_rng(5)
+    nvx = nvz = 41
+    nmaps = 3
+    velv = np.stack([voronoi_velv(rng, nvx, nvz, 1.0, 1.0, 30, (0.4, 2.2)) for _ in range(nmaps)])
+    st = rng.uniform(2.0, 38.0, (10, 2))
+    srs = np.triu(np.ones((10, 10), np.int32), 1)
+    base = modrays_batch(st, st, srs, nvx, nvz, 0.0, 0.0, 1.0, 1.0, velv, sgdl=4, sgs=8, precision=1)
+    gpulib.mct_debug_fm2d_heap_cap(cap)
+    try:
+        got = modrays_batch(st, st, srs, nvx, nvz, 0.0, 0.0, 1.0, 1.0, velv, sgdl=4, sgs=8)
+        got_df = modrays_batch(st, st, srs, nvx, nvz, 0.0, 0.0, 1.0, 1.0, velv, sgdl=4, sgs=8, precision=1)
+    finally:
+        gpulib.mct_debug_fm2d_heap_cap(0)
+    m = srs == 1
+    for mp in range(nmaps):
+        exp = oracle_modrays(orc, st, st, srs, nvx, nvz, 0.0, 0.0, 1.0, 1.0, velv[mp], 1, 1, 1, 4, 8, 1)
+        assert np.max(np.abs(got[mp][m] - exp[m])) <= TOL
+    np.testing.assert_array_equal(got_df, base)
+
+
 def test_modrays_homogeneous_close_to_straight_line(gpulib):
     nvx = nvz = 41
     velv = np.full((nvx + 2, nvz + 2), 3.0)
