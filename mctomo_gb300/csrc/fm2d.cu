@@ -97,7 +97,9 @@ __device__ __forceinline__ void updtree(WarpStateT<TT> &w, const Grid2 &g, int i
   sift_up(w, me, pack(iz, ix), w.S[me], tme);
 }
 
-// downtree: remove the root (already marked alive by the caller)
+// downtree: remove the root (already marked alive by the caller). The ids
+// of both possible next-level child pairs are fetched (one 64-bit load)
+// while the current children's times are compared.
 template <class TT>
 __device__ void downtree(WarpStateT<TT> &w) {
   if (w.ntr == 1) { w.ntr = 0; return; }
@@ -107,17 +109,21 @@ __device__ void downtree(WarpStateT<TT> &w) {
   const int ntr = w.ntr;
   const TT key = w.T[ln];
   int hole = 1, c = 2;
+  unsigned pair = c < ntr ? reinterpret_cast<const unsigned *>(w.H)[1] : 0u;   // H[2], H[3]
   while (c < ntr) {
-    const unsigned pair = reinterpret_cast<const unsigned *>(w.H)[c >> 1];   // H[c], H[c+1]
     const int p1 = (int)(pair & 0xffffu), p2 = (int)(pair >> 16);
     const int n1 = plin(w, p1), n2 = plin(w, p2);
     const TT k1 = w.T[n1], k2 = w.T[n2];
+    // H[2c], H[2c+1] (children of c) and H[2c+2], H[2c+3] (children of c+1)
+    const unsigned long long quad =
+        2 * c < ntr ? reinterpret_cast<const unsigned long long *>(w.H)[c >> 1] : 0ull;
     const bool right = tlt(k2, k1);
     const int cp = right ? p2 : p1, cn = right ? n2 : n1, cc = c + (right ? 1 : 0);
     if (!tlt(right ? k2 : k1, key)) { c = ntr + 1; break; }
     w.H[hole] = (unsigned short)cp;
     w.S[cn] = (short)hole;
     hole = cc; c = 2 * hole;
+    pair = right ? (unsigned)(quad >> 32) : (unsigned)quad;
   }
   if (c == ntr) {
     const int cp = w.H[c];
@@ -214,12 +220,14 @@ __device__ __forceinline__ DF ddiv(DF a, DF b) {
 // (a - y^2) / (2y) from the exact remainder, the halved reciprocal square
 // root standing in for 1 / (2y).
 __device__ __forceinline__ DF dsqrt(DF a) {
-  if (!(a.hi > 0.f)) return df(0.f);
-  const float y = sqrtf(a.hi);
-  const float h = 0.5f * rsqrtf(a.hi);
+  const bool pos = a.hi > 0.f;
+  const float x = pos ? a.hi : 1.f;
+  const float y = sqrtf(x);
+  const float h = 0.5f * rsqrtf(x);
   const float p = y * y, e = fmaf(y, y, -p);
-  const DF rem = dsub(a, DF{p, e});
-  return quick_two_sum(y, rem.hi * h);
+  const DF rem = dsub(pos ? a : df(1.f), DF{p, e});
+  const DF r = quick_two_sum(y, rem.hi * h);
+  return pos ? r : df(0.f);
 }
 __device__ __forceinline__ DF f2df(float2 v) { return DF{v.x, v.y}; }
 
@@ -294,6 +302,23 @@ __device__ __forceinline__ bool combo_stencil(const WarpStateT<TT> &w, const Gri
   return true;
 }
 
+
+// Node slowness as each mode consumes it: FP64 (precision 0), an FP32 pair
+// (precision 1) or FP32 (precision 2), stored in the same 8-byte slots.
+template <class TT> struct SlowOf { using type = double; };
+template <> struct SlowOf<float2> { using type = float2; };
+template <> struct SlowOf<int> { using type = float; };
+template <class TT> using SlowT = typename SlowOf<TT>::type;
+__device__ __forceinline__ void store_slowness(double *base, size_t i, double s, int precision) {
+  if (precision == 1) {
+    const float h = (float)s;
+    reinterpret_cast<float2 *>(base)[i] = make_float2(h, (float)(s - (double)h));
+  } else if (precision == 2) {
+    reinterpret_cast<float *>(base)[i] = (float)s;
+  } else {
+    base[i] = s;
+  }
+}
 
 // Per-march constants of the reduced-precision updates. Every two-term case
 // is a W^2 + 2 B W + c = 0 with a = vv + m uu fixed by the grid spacing, so a
@@ -372,56 +397,47 @@ __device__ double combo_time(const WarpStateT<double> &w, const Grid2 &g, const 
 }
 
 // Double-float (precision 1): the same cases and stencils in FP32-pair
-// arithmetic, with the division-free roots above.
-__device__ float2 combo_time(const WarpStateT<float2> &w, const Grid2 &, const Stencil &s, double sl, int,
+// arithmetic, written as one branch-free formula so that the 16 lanes do not
+// serialise over the cases. With R = 4 T1 - T2 (second order, alpha = 3) or
+// R = T1 (first order, alpha = 1) per axis, the pivot axis p is x unless x is
+// unused or x is second order and z first order; W = alpha_p T - R_p solves
+//   a W^2 + 2 B W + c = 0,  B = k e uu,  c = uu (e^2 - s^2 vv),  e = k R_p - R_q,
+// k = alpha_q / alpha_p (0 for one term, whose a = vv = 1), uu and vv the
+// squared stencil spacings of p and q; T = (R_p + W) / alpha_p.
+__device__ float2 combo_time(const WarpStateT<float2> &w, const Grid2 &, const Stencil &s, float2 sl, int,
                              const Fx &, const UpdConst<float2> &K) {
-  const DF slown = df_from(sl);
+  const DF slown = f2df(sl);
   const DF Tj = f2df(w.T[s.lj]), Tk = f2df(w.T[s.lk]);
-  DF trav;
-  bool third = false;
-  if (s.X && s.Z) {
-    DF uu, vv, em, tref, A, IA;
-    float k = 1.f;
-    if (s.X == 2 && s.Z == 2) {
-      tref = dsub(dmulf(Tj, 4.f), f2df(w.T[s.lj2]));
-      em = dadd(dsub(tref, dmulf(Tk, 4.f)), f2df(w.T[s.lk2]));
-      uu = dmulf(K.hx1, 4.f); vv = dmulf(K.hz1, 4.f); A = K.a[0]; IA = K.ia[0]; third = true;
-    } else if (s.X == 2) {
-      em = dadd(dsub(dmulf(Tk, 3.f), dmulf(Tj, 4.f)), f2df(w.T[s.lj2]));
-      uu = K.hz1; vv = dmulf(K.hx1, 4.f); k = 3.f; A = K.a[1]; IA = K.ia[1]; tref = Tk;
-    } else if (s.Z == 2) {
-      em = dadd(dsub(dmulf(Tj, 3.f), dmulf(Tk, 4.f)), f2df(w.T[s.lk2]));
-      uu = K.hx1; vv = dmulf(K.hz1, 4.f); k = 3.f; A = K.a[2]; IA = K.ia[2]; tref = Tj;
-    } else {
-      em = dsub(Tj, Tk);
-      uu = K.hx1; vv = K.hz1; A = K.a[3]; IA = K.ia[3]; tref = Tj;
-    }
-    const DF B = dmulf(dmul(em, uu), k);
-    const DF c = dmul(uu, dsub(dmul(em, em), dmul(dmul(slown, slown), vv)));
-    DF disc = dsub(dmul(B, B), dmul(A, c));
-    if (disc.hi < 0.f) disc = df(0.f);
-    trav = dadd(tref, dmul(dsub(dsqrt(disc), B), IA));
-  } else {
-    DF tref, h;
-    if (s.X) {
-      if (s.X == 2) { tref = dsub(dmulf(Tj, 4.f), f2df(w.T[s.lj2])); h = dmulf(K.dnx, 2.f); third = true; }
-      else { tref = Tj; h = K.dnx; }
-    } else {
-      if (s.Z == 2) { tref = dsub(dmulf(Tk, 4.f), f2df(w.T[s.lk2])); h = dmulf(K.dnz, 2.f); third = true; }
-      else { tref = Tk; h = K.dnz; }
-    }
-    trav = dadd(tref, dmul(h, slown));
-  }
-  if (third) trav = dmul(trav, df_from(1.0 / 3.0));
+  const DF Rx2 = dsub(dmulf(Tj, 4.f), f2df(w.T[s.lj2]));
+  const DF Rz2 = dsub(dmulf(Tk, 4.f), f2df(w.T[s.lk2]));
+  const DF Rx = s.X == 2 ? Rx2 : Tj, Rz = s.Z == 2 ? Rz2 : Tk;
+  const bool two = s.X != 0 && s.Z != 0;
+  const bool pz = s.X == 0 || (s.X == 2 && s.Z == 1);
+  const int op = pz ? s.Z : s.X;
+  const DF Rp = pz ? Rz : Rx, Rq = pz ? Rx : Rz;
+  const DF hx = s.X == 2 ? dmulf(K.hx1, 4.f) : K.hx1, hz = s.Z == 2 ? dmulf(K.hz1, 4.f) : K.hz1;
+  const DF uu = pz ? hz : hx;
+  const DF vv = two ? (pz ? hx : hz) : df(1.f);
+  const float k = two ? (s.X == s.Z ? 1.f : 3.f) : 0.f;
+  const int ci = (s.X == 2) ? (s.Z == 2 ? 0 : 1) : (s.Z == 2 ? 2 : 3);
+  const DF A = !two ? df(1.f) : ci == 0 ? K.a[0] : ci == 1 ? K.a[1] : ci == 2 ? K.a[2] : K.a[3];
+  const DF IA = !two ? df(1.f) : ci == 0 ? K.ia[0] : ci == 1 ? K.ia[1] : ci == 2 ? K.ia[2] : K.ia[3];
+  const DF e = two ? dsub(dmulf(Rp, k), Rq) : df(0.f);
+  const DF B = dmulf(dmul(e, uu), k);
+  const DF c = dmul(uu, dsub(dmul(e, e), dmul(dmul(slown, slown), vv)));
+  DF disc = dsub(dmul(B, B), dmul(A, c));
+  if (disc.hi < 0.f) disc = df(0.f);
+  DF trav = dadd(Rp, dmul(dsub(dsqrt(disc), B), IA));
+  trav = dmul(trav, op == 2 ? df_from(1.0 / 3.0) : df(1.f));
   return make_float2(trav.hi, trav.lo);
 }
 
 // Fixed point (precision 2): the same cases in FP32 on times taken relative
 // to the combination's first accepted neighbour, rounded back to the
 // fixed-point grid.
-__device__ int combo_time(const WarpStateT<int> &w, const Grid2 &, const Stencil &s, double sl, int,
+__device__ int combo_time(const WarpStateT<int> &w, const Grid2 &, const Stencil &s, float sl, int,
                           const Fx &fx, const UpdConst<int> &K) {
-  const float slown = (float)sl;
+  const float slown = sl;
   const int base = s.X ? w.T[s.lj] : w.T[s.lk];
   auto sh = [&](int l) { return (float)(w.T[l] - base) * fx.inv; };
   const float Tj = sh(s.lj), Tk = sh(s.lk);
@@ -515,7 +531,7 @@ __device__ __forceinline__ double bilinear(const double nv[2][2], double dsx, do
 struct Trace { int *ti; double *tt; int max; int n; };
 
 template <class TT>
-__device__ void march(WarpStateT<TT> &w, const Grid2 &g, const double *SL, int fom, int urg, int vnl, int vnr,
+__device__ void march(WarpStateT<TT> &w, const Grid2 &g, const SlowT<TT> *SL, int fom, int urg, int vnl, int vnr,
                       int vnt, int vnb, const Fx &fx, Trace *tr = nullptr) {
   const int lane = threadIdx.x & 31;
   // lanes 16-31 work on neighbour q = (lane - 16) / 4 of the accepted node,
@@ -525,7 +541,7 @@ __device__ void march(WarpStateT<TT> &w, const Grid2 &g, const double *SL, int f
   // slowness of this lane's neighbour of the node predicted to be accepted
   // next, loaded while lane 0 sifts (a global-memory load off the critical path)
   int pred = -1;
-  double sl_pred = 0.0;
+  SlowT<TT> sl_pred = SlowT<TT>();
   UpdConst<TT> K;
   K.init(g);
   for (;;) {
@@ -695,7 +711,8 @@ __global__ void gridder_kernel(Fm2dJob job) {
       sumi = sumi + bsw(i1 - 1, v) * sumj;
     }
     veln[(size_t)(stx - 1) * nnz + (stz - 1)] = sumi;
-    job.slon[(size_t)map * nnx * nnz + (size_t)(stx - 1) * nnz + (stz - 1)] = 1.0 / sumi;
+    store_slowness(job.slon, (size_t)map * nnx * nnz + (size_t)(stx - 1) * nnz + (stz - 1), 1.0 / sumi,
+                   job.precision);
   }
 }
 
@@ -817,18 +834,19 @@ fm2d_refined_kernel(Fm2dJob job, int warp_bytes, int heap_cap, int redo) {
   // refined slowness (1 / bsplrefine velocity; +inf outside the box, as
   // the reference's 1/0 there)
   double *Sr = job.sref + (size_t)solve * job.nref_max;
+  const SlowT<TT> *SLr = reinterpret_cast<const SlowT<TT> *>(Sr);
   const int ldv = job.nvz + 2;
   const RefineBox rb{job.velv + (size_t)sg.map * (job.nvx + 2) * ldv, ldv, (vnl - 1) * sgdl + 1,
                      (vnt - 1) * sgdl + 1, job.gdx * sgdl, job.gdz * sgdl, vnl, vnr, vnt, vnb};
   for (int node = lane; node < nrnx * nrnz; node += 32)
-    Sr[node] = 1.0 / refined_velocity(job, rb, node % nrnz + 1, node / nrnz + 1);
+    store_slowness(Sr, node, 1.0 / refined_velocity(job, rb, node % nrnz + 1, node / nrnz + 1), job.precision);
   for (int q = lane; q < nrnx * nrnz; q += 32) w.S[q] = -1;
   w.ld = gr.ld;
   __syncwarp();
   if (lane == 0)
     init_source(w, gr, [&](int zz, int xx) { return refined_velocity(job, rb, zz, xx); }, sg.x, sg.z, fx);
   __syncwarp();
-  march(w, gr, Sr, job.fom, 1, vnl, vnr, vnt, vnb, fx, tr);
+  march(w, gr, SLr, job.fom, 1, vnl, vnr, vnt, vnb, fx, tr);
   if (__shfl_sync(0xffffffffu, (int)w.overflow, 0)) {
     if (lane == 0) job.ovf_list[atomicAdd(job.ovf_count, 1)] = solve;
     return;
@@ -871,7 +889,7 @@ fm2d_coarse_kernel(Fm2dJob job, int warp_bytes) {
   const int sgdl = job.sgdl;
   const int vnl = sg.vnl, vnr = sg.vnr, vnt = sg.vnt, vnb = sg.vnb;
   const double *Vc = job.veln + (size_t)map * nnx * nnz;
-  const double *SLc = job.slon + (size_t)map * nnx * nnz;
+  const SlowT<TT> *SLc = reinterpret_cast<const SlowT<TT> *>(job.slon) + (size_t)map * nnx * nnz;
   Trace trace{job.trace_i ? job.trace_i + 3 * (job.trace_max / 2) : nullptr,
               job.trace_t ? job.trace_t + job.trace_max / 2 : nullptr, job.trace_max / 2, 0};
   Trace *tr = (job.trace_i && solve == job.trace_solve && lane == 0) ? &trace : nullptr;
