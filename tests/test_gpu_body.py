@@ -11,7 +11,7 @@ from mctomo_gb300 import BodyLikelihood, synthetic
 
 pytestmark = pytest.mark.gpu
 P = lambda a: None if a is None else a.ctypes.data_as(ctypes.c_void_p)  # noqa: E731
-TT_TOL = {0: 1e-4, 1: 2e-2}   # per order, see test_gpu_eik3
+TT_TOL = {0: 1e-4, 1: 5e-2}   # per order, see test_gpu_eik3
 
 
 def oracle_body(orc, grid, settings, data, ev, n, pts, par, n0, n1):
