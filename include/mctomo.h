@@ -231,6 +231,15 @@ int mct_surf_forward_device(mct_surf_ctx *ctx, int nchains, const int *slots,
                             const double *n1, double *out, void *stream);
 int mct_surf_commit_device(mct_surf_ctx *ctx, const int *accept,
                            void *stream);
+/* Noise-only likelihood, replaces surf_noise_likelihood
+ * (src/likelihood_surf.F90:56-99): each listed slot's committed travel times
+ * re-reduced with new noise parameters n0, n1 (nchains x np), sigma = n0 *
+ * travel time + n1 for every path; no forward solve. out as mct_surf_forward
+ * (unweighted misfit included); status bit 8 for a zero sigma (the
+ * reference's fatal error), bit 16 for a slot with nothing committed; the
+ * call then returns MCT_MODEL_INVALID. */
+int mct_surf_noise_likelihood(mct_surf_ctx *ctx, int nchains, const int *slots,
+                              const double *n0, const double *n1, double *out);
 /* Last forward's travel times (np, nsrc, nrev) = phaseTime(k,j,i) and phase
  * maps (np, nx, ny) for batch position index; either pointer may be NULL. */
 int mct_surf_phase_time(mct_surf_ctx *ctx, int index, double *phase_time,
@@ -310,6 +319,15 @@ int mct_body_forward(mct_body_ctx *ctx, int nchains, const int *ncells,
                      const double *points, const double *params,
                      const double *locations, const double *n0,
                      const double *n1, double *out);
+/* Noise-only likelihood, replaces body_noise_likelihood
+ * (src/likelihood_body.F90:38-80): the last forward's travel times of batch
+ * positions 0..nchains-1 re-reduced with new noise parameters n0, n1
+ * (nchains x np) and origin times (locations, nchains x nsrc x 4, the 4th
+ * entry used); sigma = n0 * travel time + n1 for every pair. out as
+ * mct_body_forward. */
+int mct_body_noise_likelihood(mct_body_ctx *ctx, int nchains,
+                              const double *locations, const double *n0,
+                              const double *n1, double *out);
 /* Last forward's travel times (np, nsrc, nrev) = phaseTime(k,j,i) for batch
  * position index, and the number of tile passes the solves took. */
 int mct_body_phase_time(mct_body_ctx *ctx, int index, double *phase_time,

@@ -42,6 +42,7 @@ SIGNATURES = {
     "mct_body_destroy": (I, [P]),
     "mct_body_forward": (I, [P, I, P, P, P, P, P, P, P]),
     "mct_body_phase_time": (I, [P, I, P, P]),
+    "mct_body_noise_likelihood": (I, [P, I, P, P, P, P]),
     "mct_surf_create": (I, [P, P, P, I, I, P]),
     "mct_surf_destroy": (I, [P]),
     "mct_surf_forward": (I, [P, I, P, P, P, P, P, P, P]),
@@ -49,6 +50,7 @@ SIGNATURES = {
     "mct_surf_forward_device": (I, [P, I, P, P, P, P, P, P, P, P]),
     "mct_surf_commit_device": (I, [P, P, P]),
     "mct_surf_phase_time": (I, [P, I, P, P]),
+    "mct_surf_noise_likelihood": (I, [P, I, P, P, P, P]),
     "mct_surf_stream": (I, [P, P]),
     "mct_surf_profile_start": (I, [P, I]),
     "mct_surf_profile_read": (I, [P, P, P, P]),

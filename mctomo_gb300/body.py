@@ -70,6 +70,20 @@ class BodyLikelihood:
                                                          ptr(locations), ptr(n0), ptr(n1), ptr(out)))
         return out
 
+    def noise_likelihood(self, locations, n0, n1):
+        """body_noise_likelihood: the last forward's travel times of batch
+        positions 0..nchains-1 re-reduced with new noise parameters n0/n1
+        (nchains, np) and origin times (locations[..., 3]); no forward."""
+        n0 = np.ascontiguousarray(n0, np.float64)
+        nch = n0.shape[0]
+        n0 = n0.reshape(nch, self.np)
+        n1 = np.ascontiguousarray(n1, np.float64).reshape(nch, self.np)
+        locations = np.ascontiguousarray(locations, np.float64).reshape(nch, self.nsrc, 4)
+        out = np.zeros((nch, 4))
+        check("mct_body_noise_likelihood",
+              lib().mct_body_noise_likelihood(self.h, nch, ptr(locations), ptr(n0), ptr(n1), ptr(out)))
+        return out
+
     def phase_time(self, index):
         pt = np.zeros((self.np, self.nsrc, self.nrev))
         passes = ctypes.c_int()

@@ -107,6 +107,46 @@ __global__ void body_misfit_kernel(BodyDev d, int nchains, const double *tt, con
 
 }  // namespace
 
+// body_noise_likelihood (src/likelihood_body.F90:38-80): the last forward's
+// phase times re-reduced with new noise parameters and origin times,
+// sigma = n0 * phase time + n1 for every pair, unused pairs with sigma = 1.
+__global__ void body_noise_kernel(BodyDev d, const double *ptime, const double *loc, const double *n0,
+                                  const double *n1, double *out) {
+  const int c = blockIdx.x;
+  const int npairs = d.nsrc * d.nrev;
+  double like = 0, mis = 0, umis = 0, slog = 0;
+  for (int q = threadIdx.x; q < d.np * npairs; q += blockDim.x) {
+    const int p = q / npairs, r = q % npairs;
+    const int j = r / d.nrev;
+    const double t = ptime[((size_t)c * d.np + p) * npairs + r];
+    const bool used = d.raystat[(size_t)p * npairs + r] == 1;
+    const double sig = used ? n0[(size_t)c * d.np + p] * t + n1[(size_t)c * d.np + p] : 1.0;
+    if (used) {
+      const double res = t + loc[((size_t)c * d.nsrc + j) * 4 + 3] - d.dtime[(size_t)p * npairs + r];
+      const double r2 = res * res;
+      like += r2 / (2 * (sig * sig));
+      mis += r2 / (sig * sig);
+      umis += r2;
+    }
+    slog += log(sig);
+  }
+  __shared__ double red[4][256];
+  red[0][threadIdx.x] = like; red[1][threadIdx.x] = mis; red[2][threadIdx.x] = umis; red[3][threadIdx.x] = slog;
+  __syncthreads();
+  for (int st = blockDim.x / 2; st > 0; st >>= 1) {
+    if (threadIdx.x < st)
+      for (int k = 0; k < 4; ++k) red[k][threadIdx.x] += red[k][threadIdx.x + st];
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) {
+    const double PI2 = (double)6.283185f;
+    out[(size_t)c * 4 + 0] = red[0][0] + red[3][0] + (double)((float)d.nrays / 2.0f) * log(PI2);
+    out[(size_t)c * 4 + 1] = red[1][0];
+    out[(size_t)c * 4 + 2] = red[2][0];
+    out[(size_t)c * 4 + 3] = 0.0;
+  }
+}
+
 struct mct_body_ctx {
   mct_grid g{};
   int order = 0, np = 1, sigdep = 1, nslots = 0, ncell_max = 0;
@@ -276,6 +316,21 @@ int mct_body_forward(mct_body_ctx *c, int nchains, const int *ncells, const doub
   MCT_CUDA_TRY(cudaStreamSynchronize(s));
   c->last_nchains = nchains;
   if (gst[0]) return gst[0];
+  return MCT_OK;
+}
+
+int mct_body_noise_likelihood(mct_body_ctx *c, int nchains, const double *locations, const double *n0,
+                              const double *n1, double *out) {
+  if (!c || nchains < 1 || nchains > c->last_nchains || !locations || !n0 || !n1 || !out) return MCT_ERR_ARG;
+  cudaStream_t s = c->stream;
+  const BodyDev &d = c->dev;
+  MCT_CUDA_TRY(cudaMemcpyAsync(c->loc, locations, sizeof(double) * nchains * d.nsrc * 4, cudaMemcpyHostToDevice, s));
+  MCT_CUDA_TRY(cudaMemcpyAsync(c->n0, n0, sizeof(double) * nchains * d.np, cudaMemcpyHostToDevice, s));
+  MCT_CUDA_TRY(cudaMemcpyAsync(c->n1, n1, sizeof(double) * nchains * d.np, cudaMemcpyHostToDevice, s));
+  body_noise_kernel<<<nchains, 256, 0, s>>>(d, c->ptime, c->loc, c->n0, c->n1, c->out);
+  MCT_CUDA_TRY(cudaGetLastError());
+  MCT_CUDA_TRY(cudaMemcpyAsync(out, c->out, sizeof(double) * 4 * nchains, cudaMemcpyDeviceToHost, s));
+  MCT_CUDA_TRY(cudaStreamSynchronize(s));
   return MCT_OK;
 }
 

@@ -94,6 +94,7 @@ int mct_surf_create(const mct_grid *g, const mct_surf_settings *st, const mct_su
       sizeof(double) * (size_t)nslots * np * npairs,
       // committed state
       sizeof(int) * nslots, sizeof(double) * (size_t)nslots * nodes * 3, sizeof(double) * (size_t)nslots * maps,
+      sizeof(double) * (size_t)nslots * np * npairs,
       // staging
       sizeof(int) * nslots * 3, sizeof(double) * (size_t)nslots * ncell_max * 6, sizeof(double) * 2 * nslots * np,
       sizeof(double) * 4 * nslots, sizeof(int)};
@@ -145,6 +146,7 @@ int mct_surf_create(const mct_grid *g, const mct_surf_settings *st, const mct_su
   b.cvp = cv.take<double>((size_t)nslots * nodes * 3);
   b.cvs = b.cvp + (size_t)nslots * nodes; b.crho = b.cvs + (size_t)nslots * nodes;
   b.cpvel = cv.take<double>((size_t)nslots * maps);
+  b.cttime = cv.take<double>((size_t)nslots * np * npairs);
   c->d_slots = cv.take<int>((size_t)nslots * 3);
   c->d_ncells = c->d_slots + nslots; c->d_accept = c->d_ncells + nslots;
   c->d_points = cv.take<double>((size_t)nslots * ncell_max * 6);
@@ -172,6 +174,7 @@ int mct_surf_create(const mct_grid *g, const mct_surf_settings *st, const mct_su
   cudaMemcpy(solves, all.data(), sizeof(int2) * nsolve, cudaMemcpyHostToDevice);
   cudaMemset(b.committed, 0, sizeof(int) * nslots);
   cudaMemset(b.ttime, 0, sizeof(double) * (size_t)nslots * np * npairs);
+  cudaMemset(b.cttime, 0, sizeof(double) * (size_t)nslots * np * npairs);
   if (cudaGetLastError() != cudaSuccess || cudaDeviceSynchronize() != cudaSuccess) {
     cudaFree(c->mem); cudaStreamDestroy(c->stream); delete c; return MCT_ERR_CUDA;
   }
@@ -251,6 +254,26 @@ int mct_surf_commit(mct_surf_ctx *c, const int *accept) {
   int rc = mct_surf_commit_device(c, c->d_accept, s);
   if (rc) return rc;
   MCT_CUDA_TRY(cudaStreamSynchronize(s));
+  return MCT_OK;
+}
+
+int mct_surf_noise_likelihood(mct_surf_ctx *c, int nchains, const int *slots, const double *n0, const double *n1,
+                              double *out) {
+  if (!c || nchains < 1 || nchains > c->nslots || !slots || !n0 || !n1 || !out) return MCT_ERR_ARG;
+  for (int i = 0; i < nchains; ++i)
+    if (slots[i] < 0 || slots[i] >= c->nslots) return MCT_ERR_ARG;
+  cudaStream_t s = c->stream;
+  const int np = c->b.np;
+  // staging shared with forwards: calls on one context are ordered on its stream
+  MCT_CUDA_TRY(cudaMemcpyAsync(c->d_slots, slots, sizeof(int) * nchains, cudaMemcpyHostToDevice, s));
+  MCT_CUDA_TRY(cudaMemcpyAsync(c->d_n0, n0, sizeof(double) * nchains * np, cudaMemcpyHostToDevice, s));
+  MCT_CUDA_TRY(cudaMemcpyAsync(c->d_n1, n1, sizeof(double) * nchains * np, cudaMemcpyHostToDevice, s));
+  int rc = surf_noise(c->b, nchains, c->d_slots, c->d_n0, c->d_n1, c->d_out, s);
+  if (rc) return rc;
+  MCT_CUDA_TRY(cudaMemcpyAsync(out, c->d_out, sizeof(double) * 4 * nchains, cudaMemcpyDeviceToHost, s));
+  MCT_CUDA_TRY(cudaStreamSynchronize(s));
+  for (int i = 0; i < nchains; ++i)
+    if (out[4 * i + 3] != 0.0) return MCT_MODEL_INVALID;
   return MCT_OK;
 }
 

@@ -185,7 +185,61 @@ __global__ void commit_kernel(SurfBatch b, const int *accept) {
   }
   for (size_t q = blockIdx.x * blockDim.x + threadIdx.x; q < maps; q += (size_t)gridDim.x * blockDim.x)
     b.cpvel[(size_t)slot * maps + q] = b.pvel[(size_t)c * maps + q];
+  const size_t nt = (size_t)b.np * b.nsrc * b.nrev;
+  for (size_t q = blockIdx.x * blockDim.x + threadIdx.x; q < nt; q += (size_t)gridDim.x * blockDim.x)
+    b.cttime[(size_t)slot * nt + q] = b.ttime[(size_t)c * nt + q];
   if (blockIdx.x == 0 && threadIdx.x == 0) b.committed[slot] = 1;
+}
+
+// surf_noise_likelihood (src/likelihood_surf.F90:56-99): the committed phase
+// times re-reduced with new noise parameters, sigma = n0 * srdist + n1 with
+// srdist the phase time, for every pair; unused pairs count with sigma = 1.
+// A sigma below 1e-10 is the reference's fatal 'noise level is 0' (status 8).
+__global__ void noise_kernel(SurfBatch b, const int *slots, const double *n0, const double *n1, double *out) {
+  const int c = blockIdx.x;
+  const int slot = slots[c];
+  const int npairs = b.nsrc * b.nrev;
+  const double *pt = b.cttime + (size_t)slot * b.np * npairs;
+  double like = 0, mis = 0, umis = 0, slog = 0;
+  int bad = 0;
+  for (int q = threadIdx.x; q < b.np * npairs; q += blockDim.x) {
+    const int p = q / npairs, r = q % npairs;
+    const bool used = b.raystat[(size_t)p * npairs + r] == 1;
+    double sig = n0[(size_t)c * b.np + p] * pt[q] + n1[(size_t)c * b.np + p];
+    if (used) {
+      if (sig == 0.0) bad = 1;
+      const double res = pt[q] - b.dtime[(size_t)p * npairs + r];
+      const double r2 = res * res;
+      like += r2 / (2 * (sig * sig));
+      mis += r2 / (sig * sig);
+      umis += r2;
+    } else {
+      sig = 1.0;
+    }
+    if (sig < 1.0E-10) bad = 1;
+    slog += log(sig);
+  }
+  __shared__ double red[4][256];
+  __shared__ int sbad;
+  if (threadIdx.x == 0) sbad = 0;
+  __syncthreads();
+  if (bad) sbad = 1;
+  red[0][threadIdx.x] = like; red[1][threadIdx.x] = mis; red[2][threadIdx.x] = umis; red[3][threadIdx.x] = slog;
+  __syncthreads();
+  for (int st = blockDim.x / 2; st > 0; st >>= 1) {
+    if (threadIdx.x < st)
+      for (int k = 0; k < 4; ++k) red[k][threadIdx.x] += red[k][threadIdx.x + st];
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) {
+    const double PI2 = (double)6.283185f;
+    const double L = red[0][0] + red[3][0] + (double)((float)b.nrays / 2.0f) * log(PI2);
+    const int stt = (sbad ? 8 : 0) | (b.committed[slot] ? 0 : 16);
+    out[(size_t)c * 4 + 0] = stt ? DBL_MAX : L;
+    out[(size_t)c * 4 + 1] = red[1][0];
+    out[(size_t)c * 4 + 2] = red[2][0];
+    out[(size_t)c * 4 + 3] = (double)stt;
+  }
 }
 
 __global__ void gather_committed_maps(SurfBatch b) {
@@ -255,6 +309,13 @@ int surf_forward(SurfBatch &b, const SurfPlan &plan, cudaStream_t s, SurfProfile
   misfit_kernel<<<nch, 256, 0, s>>>(b);
   MCT_CUDA_TRY(cudaGetLastError());
   if (ev) MCT_CUDA_TRY(cudaEventRecord(ev[4], s));
+  return MCT_OK;
+}
+
+int surf_noise(const SurfBatch &b, int nchains, const int *slots, const double *n0, const double *n1, double *out,
+               cudaStream_t s) {
+  noise_kernel<<<nchains, 256, 0, s>>>(b, slots, n0, n1, out);
+  MCT_CUDA_TRY(cudaGetLastError());
   return MCT_OK;
 }
 

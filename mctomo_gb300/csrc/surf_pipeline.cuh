@@ -43,6 +43,7 @@ struct SurfBatch {
   int *committed;            // [nslots]
   double *cvp, *cvs, *crho;  // [nslots][nodes]
   double *cpvel;             // [nslots][np][nx][ny]
+  double *cttime;            // [nslots][np][nsrc][nrev] committed phase times
 };
 
 // Optional per-stage timing: events recorded around the stages of each
@@ -61,3 +62,6 @@ struct SurfPlan {
 
 int surf_forward(SurfBatch &b, const SurfPlan &plan, cudaStream_t s, SurfProfile *prof = nullptr);
 int surf_commit(SurfBatch &b, const int *accept_dev, cudaStream_t s);
+// Noise-only likelihood of committed slots (no forward solve).
+int surf_noise(const SurfBatch &b, int nchains, const int *slots, const double *n0, const double *n1, double *out,
+               cudaStream_t s);

@@ -96,6 +96,19 @@ class SurfaceLikelihood:
         accept = np.ascontiguousarray(accept, np.int32)
         check("mct_surf_commit", lib().mct_surf_commit(self.h, ptr(accept)))
 
+    def noise_likelihood(self, slots, n0, n1):
+        """surf_noise_likelihood: the committed travel times of each slot
+        re-reduced with new noise parameters n0/n1 (nchains, np); no forward.
+        Returns out (nchains, 4) as forward."""
+        slots = np.ascontiguousarray(slots, np.int32)
+        nch = slots.size
+        n0 = np.ascontiguousarray(n0, np.float64).reshape(nch, self.np)
+        n1 = np.ascontiguousarray(n1, np.float64).reshape(nch, self.np)
+        out = np.zeros((nch, 4))
+        check("mct_surf_noise_likelihood",
+              lib().mct_surf_noise_likelihood(self.h, nch, ptr(slots), ptr(n0), ptr(n1), ptr(out)))
+        return out
+
     def phase_time(self, index):
         """Last forward's travel times (np, nsrc, nrev) and phase maps (np, nx, ny)."""
         pt = np.zeros((self.np, self.nsrc, self.nrev))

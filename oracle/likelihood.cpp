@@ -71,7 +71,10 @@ int orc_convert_to_layer(const double *vp, const double *vs, const double *rho,
   return nl;
 }
 
-// Surface-wave misfit. phase_time: (nrev, nsrc, np); dat_ttime: (npairs, 3, np)
+// Surface-wave misfit (src/likelihood_surf.F90:356-404; with sigdep != 0 and
+// srdist = phase_time it is also surf_noise_likelihood, :56-99, whose sigma
+// of unused paths is reset to 1 the same way).
+// phase_time: (nrev, nsrc, np); dat_ttime: (npairs, 3, np)
 // with column 1 the observed time and column 2 the data sigma; raystat:
 // (npairs, 2, np); srdist (npairs, np). sigdep != 0: sigma = n0*srdist + n1.
 // sigma_out (npairs, np) receives the final sigma. out[0..2] = like, misfit,
@@ -123,7 +126,9 @@ int orc_surf_misfit(int nsrc, int nrev, int np, const double *phase_time,
   return status;
 }
 
-// Body-wave misfit: residual adds the event origin time t0[j] (locations(4,j)).
+// Body-wave misfit (src/likelihood_body.F90:284-333; with sigdep != 0 and
+// srdist = phase_time also body_noise_likelihood, :38-80): residual adds the
+// event origin time t0[j] (locations(4,j)).
 int orc_body_misfit(int nsrc, int nrev, int np, const double *phase_time,
                     const double *t0, const double *dat_ttime,
                     const int *raystat, const double *srdist, int sigdep,
