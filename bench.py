@@ -108,6 +108,19 @@ class Clocks:
                 "samples": len(sm), "reasons": sorted(reasons)}
 
 
+def job_rate(units_per_rank, elapsed_ms, ws, device=None):
+    """Whole-job throughput over ws replica ranks: the units all ranks
+    processed over the slowest rank's time (all-reduce MAX of the elapsed
+    time). Returns (rate per second, max elapsed ms)."""
+    if ws > 1:
+        import torch
+        import torch.distributed as dist
+        t = torch.tensor([float(elapsed_ms)], dtype=torch.float64, device=device)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        elapsed_ms = float(t.item())
+    return units_per_rank * ws / (elapsed_ms / 1e3), elapsed_ms
+
+
 def make_workload(steps_total):
     from mctomo_gb300 import synthetic
     rng = np.random.default_rng(SEED)
@@ -200,11 +213,7 @@ def run_gpu(args):
     check("mct_surf_profile_read", L.mct_surf_profile_read(lk.h, stage, ctypes.byref(nsteps), ctypes.byref(launches)))
     check("mct_surf_profile_start", L.mct_surf_profile_start(lk.h, 0))
     out = d_out.cpu().numpy()
-    if ws > 1:
-        t = torch.tensor([total_ms], device=dev)
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        total_ms = float(t.item())
-    value = NCHAINS * K * ws / (total_ms / 1e3)
+    value, total_ms = job_rate(NCHAINS * K, total_ms, ws, dev)
 
     # end to end through the host API, pinned host buffers
     pin = lambda a: torch.from_numpy(np.ascontiguousarray(a)).pin_memory().numpy()  # noqa: E731
@@ -219,7 +228,7 @@ def run_gpu(args):
         o = lk.forward(slots, ncells, hp[i][0], hp[i][1], n0, n1)
         lk.commit(np.ones(NCHAINS, np.int32))
         e2e_ms.append((time.perf_counter() - t0) * 1e3)
-    e2e_value = NCHAINS * len(e2e_ms) * ws / (sum(e2e_ms) / 1e3)
+    e2e_value, _ = job_rate(NCHAINS * len(e2e_ms), sum(e2e_ms), ws, dev)
     h2d = NCHAINS * NCELL_MAX * 3 * 8 * 2 + NCHAINS * (4 + 4) + 2 * NCHAINS * n0.shape[1] * 8 + NCHAINS * 4
     d2h = NCHAINS * 4 * 8
 
@@ -232,7 +241,7 @@ def run_gpu(args):
                    n0[c:c + 1], n1[c:c + 1])
         lk.commit(np.ones(1, np.int32))
         plain_ms.append((time.perf_counter() - t0) * 1e3)
-    plain_value = len(plain_ms) / (sum(plain_ms) / 1e3)
+    plain_value, _ = job_rate(len(plain_ms), sum(plain_ms), ws, dev)
 
     # roofline of the dominant stage (fm2d travel times): algorithmic bytes =
     # for every (chain, period, source) solve, each node of the 41x41 grid read
