@@ -33,6 +33,7 @@ import numpy as np
 ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, ROOT)
 
+FM2D_DRAM_BYTES_PER_FORWARD = 2.19e9
 NCHAINS = 64
 NCELL_MAX = 400
 SEED = 20261203
@@ -256,6 +257,10 @@ def run_gpu(args):
                  1: 0.0, 3: NCHAINS * 20 * 1225 * 24.0}[dom]
     peak, peak_kind = peaks()
     achieved = alg_bytes / (stage_ms[dom] / 1e3) / 1e9 if alg_bytes else 0.0
+    # DRAM bytes (read + write) of the fm2d launches of one forward of this
+    # workload, measured with ncu (dram__bytes_read.sum, dram__bytes_write.sum,
+    # one pass) on the double-float path
+    traffic = FM2D_DRAM_BYTES_PER_FORWARD if dom == 2 and args.tt_precision == 1 else None
     line = {
         "metric": METRIC, "value": round(value, 3), "unit": "proposal evals/s", "n_gpus": ws,
         "steps": K, "warmup": W, "ms_per_step": round(total_ms / K, 4), "higher_is_better": True,
@@ -270,7 +275,7 @@ def run_gpu(args):
         "stage_ms_per_step": {n: round(v, 4) for n, v in zip(names, stage_ms)},
         "roofline": {"kernel": names[dom], "bound": "hbm", "achieved": round(achieved, 3), "peak": peak,
                      "peak_kind": peak_kind, "unit": "GB/s", "frac": round(achieved / peak, 6),
-                     "traffic": None},
+                     "traffic": traffic},
         "gpu_launches": int(launches.value),
         "clocks": cl,
         "valid_models": int((out[:, 3] == 0).sum()),
