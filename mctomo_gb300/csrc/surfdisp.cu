@@ -383,8 +383,17 @@ __device__ float gtsolh(float a, float b) {
   return c;
 }
 
-__global__ void __launch_bounds__(128) surfdisp_kernel(DispJob job) {
-  const int col = blockIdx.x * blockDim.x + threadIdx.x;
+// One warp-sized block per COLS_PER_WARP columns. The active columns of a
+// batch are the leading ones, so small blocks spread them over all SMs (and
+// their FP64 pipes) instead of packing them onto a few.
+#ifndef DISP_COLS_PER_WARP
+#define DISP_COLS_PER_WARP 32
+#endif
+constexpr int COLS_PER_WARP = DISP_COLS_PER_WARP;
+
+__global__ void __launch_bounds__(32) surfdisp_kernel(DispJob job) {
+  if ((int)threadIdx.x >= COLS_PER_WARP) return;
+  const int col = blockIdx.x * COLS_PER_WARP + threadIdx.x;
   if (col >= job.ncol) return;
   if (job.ncol_dev && col >= *job.ncol_dev) return;
   const int nl = job.nl[col];
@@ -502,8 +511,8 @@ int launch_surfdisp(const DispJob &job, cudaStream_t s) {
   if (job.ncol < 0 || job.np < 1 || job.np > NPMAX || job.mode < 1) return MCT_ERR_ARG;
   if (job.iwave != 1 && job.iwave != 2) return MCT_ERR_ARG;
   if (job.ncol == 0) return MCT_OK;
-  int blocks = (job.ncol + 127) / 128;
-  surfdisp_kernel<<<blocks, 128, 0, s>>>(job);
+  const int blocks = (job.ncol + COLS_PER_WARP - 1) / COLS_PER_WARP;
+  surfdisp_kernel<<<blocks, 32, 0, s>>>(job);
   MCT_CUDA_TRY(cudaGetLastError());
   return MCT_OK;
 }

@@ -2,12 +2,18 @@
 
     python -m mctomo_gb300.profcase fm2d [--precision P] [--maps M] [--repeat R]
     python -m mctomo_gb300.profcase eik3 [--order O]
+    python -m mctomo_gb300.profcase disp [--precision P] [--columns N]
+    python -m mctomo_gb300.profcase grid
 
 fm2d: M Voronoi phase maps of 41 x 41 vertices (1 km spacing), 50 stations
 between 2 and 38 km, every station pair once, source refinement 4 x over
 8 cells (the surface-wave likelihood's fm2d settings); R calls of
 mct_modrays_batch. eik3: 8 velocity grids of 101 x 101 x 51 nodes (0.5 km),
-120 solves. Each case prints one line and exits 0.
+120 solves. disp: N layered columns (12-40 layers, no low-velocity layers),
+20 Rayleigh fundamental-mode phase periods log-spaced 0.5-5 s, the surface
+likelihood's search increment 1e-3 km/s. grid: nearest-nucleus gridding of a
+101 x 101 x 51 grid over 50 x 50 x 25 km from 800 nuclei. Each case prints
+one line and exits 0.
 """
 import argparse
 import time
@@ -49,9 +55,33 @@ def eik3(order=0):
     print(f"eik3 order={order} solves={nsolve} passes={passes} call_s={dt:.4f} t00={tt[0, 0]:.6f}")
 
 
+def disp(precision=1, columns=4096):
+    rng = np.random.default_rng(2)
+    nl, thk, vp, vs, rho = synthetic.layered_columns(rng, columns, lvl_prob=0.0)
+    periods = np.geomspace(0.5, 5.0, 20)
+    t0 = time.perf_counter()
+    cp, _, ierr, cnt = forward.surfdisp_batch(nl, thk, vp, vs, rho, periods, 2, 0, 1e-3, precision=precision)
+    dt = time.perf_counter() - t0
+    print(f"disp precision={precision} columns={columns} call_s={dt:.4f} ierr={int((ierr != 0).sum())} "
+          f"evals_fp64={cnt[0]} evals_fp32={cnt[1]} cp00={cp[0, 0, 0]:.6f}")
+
+
+def grid():
+    rng = np.random.default_rng(3)
+    lo = np.zeros(3); hi = np.array([50.0, 50.0, 25.0])
+    shape = (101, 101, 51)
+    st = (hi - lo) / (np.array(shape) - 1)
+    pts, par = synthetic.voronoi_model_3d(rng, 800, lo, hi, (1.7, 4.3))
+    t0 = time.perf_counter()
+    sid, _, _, _ = forward.kdtree_to_grid(pts, par, *shape, lo, st)
+    dt = time.perf_counter() - t0
+    print(f"grid nodes={sid.size} nuclei=800 call_s={dt:.4f} sid0={int(sid.ravel()[0])}")
+
+
 def main(argv=None):
     ap = argparse.ArgumentParser(description=__doc__, formatter_class=argparse.RawDescriptionHelpFormatter)
-    ap.add_argument("case", choices=["fm2d", "eik3"])
+    ap.add_argument("case", choices=["fm2d", "eik3", "disp", "grid"])
+    ap.add_argument("--columns", type=int, default=4096)
     ap.add_argument("--precision", type=int, default=1)
     ap.add_argument("--maps", type=int, default=16)
     ap.add_argument("--repeat", type=int, default=2)
@@ -59,8 +89,12 @@ def main(argv=None):
     a = ap.parse_args(argv)
     if a.case == "fm2d":
         fm2d(a.precision, a.maps, a.repeat)
-    else:
+    elif a.case == "eik3":
         eik3(a.order)
+    elif a.case == "disp":
+        disp(a.precision, a.columns)
+    else:
+        grid()
 
 
 if __name__ == "__main__":
