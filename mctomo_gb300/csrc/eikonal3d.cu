@@ -145,10 +145,6 @@ __global__ void compact_kernel(Eik3Job job, int *list, int *count) {
   }
 }
 
-struct Nb {
-  int t1, t2;    // first and second neighbour times (fixed point, TINF if absent)
-};
-
 // One relaxation of node (x,y,z) of the shared tile; returns the candidate
 // (fixed point) or TINF when no update applies. Mirrors solveEikonal /
 // highAccuracySolveEikonal, including their acceptance rules.
@@ -156,55 +152,72 @@ __device__ __forceinline__ int relax(const int *sT, int x, int y, int z, float s
                                      int order, float inv_scale, float scale) {
   const int sidx = z + SZ * (y + SY * x);
   const int cur = sT[sidx];
-  const int stride[3] = {SY * SZ, SZ, 1};     // x, y, z (shared tile is z fastest)
+  // per dimension (x, y, z; the shared tile is z fastest): the smaller
+  // neighbour time t1, for second order the next time t2 beyond it, or TINF
+  // when the dimension does not take part; fixed indices keep every array
+  // in registers
   int t1[3], t2[3], dm[3];
   int cnt = 0;
+#pragma unroll
   for (int dim = 0; dim < 3; ++dim) {
-    const int st = stride[dim];
+    const int st = dim == 0 ? SY * SZ : (dim == 1 ? SZ : 1);
     // neighbours -1 and +1 (absent outside the grid are TINF in the halo)
-    int a = sT[sidx - st], b = sT[sidx + st];
+    const int a = sT[sidx - st], b = sT[sidx + st];
+    int m1 = TINF, m2 = TINF;
     if (order == 0) {
-      int m = min(a, b);     // getMinValueInDim: (v0 < v1) ? v0 : v1
-      if (m != TINF && m < cur) { t1[cnt] = m; t2[cnt] = TINF; dm[cnt] = dim; cnt++; }
+      m1 = min(a, b);     // getMinValueInDim: (v0 < v1) ? v0 : v1
     } else {
-      int minT = TINF, minT2 = TINF;
-      if (a != TINF && a < minT) {
-        minT = a; minT2 = TINF;
-        int a2 = sT[sidx - 2 * st];
-        if (a2 != TINF && a2 <= a) minT2 = a2;
+      if (a != TINF) {
+        m1 = a;
+        const int a2 = sT[sidx - 2 * st];
+        if (a2 != TINF && a2 <= a) m2 = a2;
       }
-      if (b != TINF && b < minT) {
-        minT = b; minT2 = TINF;
-        int b2 = sT[sidx + 2 * st];
-        if (b2 != TINF && b2 <= b) minT2 = b2;
+      if (b != TINF && b < m1) {
+        m1 = b; m2 = TINF;
+        const int b2 = sT[sidx + 2 * st];
+        if (b2 != TINF && b2 <= b) m2 = b2;
       }
-      if (minT != TINF && minT < cur) { t1[cnt] = minT; t2[cnt] = minT2; dm[cnt] = dim; cnt++; }
     }
+    const bool use = m1 != TINF && m1 < cur;
+    t1[dim] = use ? m1 : TINF;
+    t2[dim] = use ? m2 : TINF;
+    dm[dim] = dim;
+    cnt += use ? 1 : 0;
   }
   if (cnt == 0) return TINF;
-  // stable insertion sort by t1 (std::sort of <= 3 elements)
-  for (int i = 1; i < cnt; ++i) {
-    int v = t1[i], v2 = t2[i], dd = dm[i], j = i;
-    while (j > 0 && v < t1[j - 1]) { t1[j] = t1[j - 1]; t2[j] = t2[j - 1]; dm[j] = dm[j - 1]; --j; }
-    t1[j] = v; t2[j] = v2; dm[j] = dd;
-  }
+  // stable sort by t1 (std::sort of <= 3 elements is an insertion sort):
+  // unused dimensions hold TINF and sort last; adjacent swaps on strict
+  // inversions only keep equal times in dimension order
+  auto cswap = [&](int i, int j) {
+    if (t1[j] < t1[i]) {
+      int v = t1[i]; t1[i] = t1[j]; t1[j] = v;
+      v = t2[i]; t2[i] = t2[j]; t2[j] = v;
+      v = dm[i]; dm[i] = dm[j]; dm[j] = v;
+    }
+  };
+  cswap(0, 1); cswap(1, 2); cswap(0, 1);
   const int base = t1[0];
-  float r1[3], r2[3];
-  for (int i = 0; i < cnt; ++i) {
-    r1[i] = (float)(t1[i] - base) * inv_scale;
-    r2[i] = t2[i] == TINF ? 0.f : (float)((long long)t2[i] - base) * inv_scale;
+  float r1[3], r2[3], h[3];
+#pragma unroll
+  for (int i = 0; i < 3; ++i) {
+    // times are in [0, 2^31): differences fit in int32 (no 64-bit
+    // conversions, which would run on the FP64 pipe)
+    r1[i] = t1[i] == TINF ? 0.f : (float)(t1[i] - base) * inv_scale;
+    r2[i] = t2[i] == TINF ? 0.f : (float)(t2[i] - base) * inv_scale;
+    h[i] = dm[i] == 0 ? hh[0] : (dm[i] == 1 ? hh[1] : hh[2]);
   }
   auto solve_n = [&](int n, bool second) -> float {
-    if (n == 1) return r1[0] + hh[dm[0]] * slow;
+    if (n == 1) return r1[0] + h[0] * slow;
     float A = 0.f, B = 0.f, C = -(slow * slow);
-    for (int q = 0; q < n; ++q) {
-      float h = hh[dm[q]];
+#pragma unroll
+    for (int q = 0; q < 3; ++q) {
+      if (q >= n) continue;
       if (second && t2[q] != TINF) {
-        float alpha = 2.25f / (h * h);
+        float alpha = 2.25f / (h[q] * h[q]);
         float t = (4.f * r1[q] - r2[q]) / 3.f;
         C += t * t * alpha; B += -2.f * t * alpha; A += alpha;
       } else {
-        float alpha = 1.f / (h * h);
+        float alpha = 1.f / (h[q] * h[q]);
         C += r1[q] * r1[q] * alpha; B += -2.f * r1[q] * alpha; A += alpha;
       }
     }
@@ -212,21 +225,32 @@ __device__ __forceinline__ int relax(const int *sT, int x, int y, int z, float s
     if (quad < 0.f) return INFINITY;
     return (-B + sqrtf(quad)) / (2.f * A);
   };
-  auto to_fixed = [&](float rel) -> long long { return (long long)base + llrintf(rel * scale); };
+  auto to_fixed = [&](float rel) -> long long {
+    return (long long)base + (long long)__float2int_rn(rel * scale);   // saturates at +-2^31
+  };
   long long res = TINF;
+  bool done = false;
   if (order == 0) {
-    for (int i = 1; i <= cnt; ++i) {
-      float c = solve_n(i, false);
-      if (isinf(c)) { res = TINF; if (i == cnt) break; continue; }
+    // solveEikonal: add dimensions in increasing time while the solution
+    // stays above the next neighbour
+#pragma unroll
+    for (int i = 1; i <= 3; ++i) {
+      if (done || i > cnt) continue;
+      const float c = solve_n(i, false);
+      if (isinf(c)) { res = TINF; if (i == cnt) done = true; continue; }
       res = to_fixed(c);
-      if (i == cnt || res - (long long)t1[i] < 1) break;
+      if (i == cnt) done = true;
+      else if (res - (long long)t1[i < 3 ? i : 2] < 1) done = true;
     }
   } else {
-    for (int i = cnt; i >= 1; --i) {
-      float c = solve_n(i, true);
+    // highAccuracySolveEikonal: the largest number of dimensions first
+#pragma unroll
+    for (int i = 3; i >= 1; --i) {
+      if (done || i > cnt) continue;
+      const float c = solve_n(i, true);
       if (!isinf(c)) {
-        long long f = to_fixed(c);
-        if (f - (long long)t1[i - 1] > 0) { res = f; break; }
+        const long long f = to_fixed(c);
+        if (f - (long long)t1[i - 1] > 0) { res = f; done = true; }
       }
     }
   }
@@ -236,7 +260,6 @@ __device__ __forceinline__ int relax(const int *sT, int x, int y, int z, float s
 
 __global__ void __launch_bounds__(512) tile_kernel(Eik3Job job, const int *list) {
   __shared__ int sT[SX * SY * SZ];
-  __shared__ float sS[TX * TY * TZ];
   __shared__ int s_face[6];
   const Dims d = dims(job);
   const int ntile = d.tnx * d.tny * d.tnz;
