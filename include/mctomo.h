@@ -14,6 +14,8 @@
 #ifndef MCTOMO_H_
 #define MCTOMO_H_
 
+#include <stddef.h>
+
 #ifdef __cplusplus
 extern "C" {
 #endif
@@ -223,8 +225,8 @@ int mct_surf_forward(mct_surf_ctx *ctx, int nchains, const int *slots,
                      const double *n1, double *out);
 /* Accept (1) or reject (0) each proposal of the last forward. */
 int mct_surf_commit(mct_surf_ctx *ctx, const int *accept);
-/* Device-pointer forms, asynchronous on stream (NULL = the context's stream),
- * free of host synchronisation so they can be captured in a CUDA graph. */
+/* Device-pointer forms, asynchronous on stream (NULL = the context's stream)
+ * and free of host synchronisation. */
 int mct_surf_forward_device(mct_surf_ctx *ctx, int nchains, const int *slots,
                             const int *ncells, const double *points,
                             const double *params, const double *n0,
@@ -254,6 +256,33 @@ int mct_surf_profile_read(mct_surf_ctx *ctx, double *stage_ms, int *steps,
 /* The context's CUDA stream. */
 int mct_surf_stream(mct_surf_ctx *ctx, void **stream);
 
+/* Serving. No counterpart in the reference, whose sampler calls the
+ * likelihood synchronously; these let a host loop keep many chains resident
+ * and overlap its own work with the GPU's.
+ * mct_surf_device_bytes: the device memory a context with these arguments
+ * allocates (no allocation made), so a server can size nslots to the free
+ * memory. mct_surf_admit: claims a free slot for a new chain (its first
+ * forward computes every column); MCT_ERR_NOMEM when all are claimed.
+ * mct_surf_evict: releases a claimed slot. Slots can also be addressed
+ * directly without admit/evict. mct_surf_submit: starts the forward of
+ * mct_surf_forward and returns at once (the arrays are copied before it
+ * returns); one submitted batch per context at a time, and the blocking
+ * calls on the context return MCT_ERR_ARG until it is polled.
+ * mct_surf_poll: *done = 0 while the batch runs; when it has finished, *done
+ * = 1, out (nchains x 4) is filled as by mct_surf_forward and the batch's
+ * status is returned; mct_surf_commit then applies to it. A context is used
+ * by one host thread at a time. */
+int mct_surf_device_bytes(const mct_grid *grid, const mct_surf_settings *settings,
+                          const mct_surf_data *data, int nslots, int ncell_max,
+                          size_t *bytes);
+int mct_surf_admit(mct_surf_ctx *ctx, int *slot);
+int mct_surf_evict(mct_surf_ctx *ctx, int slot);
+int mct_surf_submit(mct_surf_ctx *ctx, int nchains, const int *slots,
+                    const int *ncells, const double *points,
+                    const double *params, const double *n0,
+                    const double *n1);
+int mct_surf_poll(mct_surf_ctx *ctx, double *out, int *done);
+
 
 /* ------------------------------------------------------------------------
  * 3D first-arrival travel times, replaces the reference's C entry point
@@ -262,8 +291,9 @@ int mct_surf_stream(mct_surf_ctx *ctx, void **stream);
  * vel (nx,ny,nz) C order (= Fortran (nz,ny,nx)); src[3]; rev (nrev,3);
  * order 0 first order / 1 mixed second order; ttime[nrev]; tfield (optional)
  * the final field in vel's layout. Solved on the GPU by a tile-based fast
- * iterative method on the reference's update operator (times within 1e-4 s
- * of the reference).
+ * iterative method on the reference's update operator: order 0 within
+ * 1e-4 s of the reference; order 1 approximate (the reference's result
+ * depends on its acceptance order; within 5e-2 s, typically 1e-3 s).
  * ---------------------------------------------------------------------- */
 int mct_fast_marching3d(int nx, int ny, int nz, double dx, double dy,
                         double dz, double xmin, double ymin, double zmin,

@@ -52,6 +52,11 @@ SIGNATURES = {
     "mct_surf_phase_time": (I, [P, I, P, P]),
     "mct_surf_noise_likelihood": (I, [P, I, P, P, P, P]),
     "mct_surf_stream": (I, [P, P]),
+    "mct_surf_device_bytes": (I, [P, P, P, I, I, P]),
+    "mct_surf_admit": (I, [P, P]),
+    "mct_surf_evict": (I, [P, I]),
+    "mct_surf_submit": (I, [P, I, P, P, P, P, P, P]),
+    "mct_surf_poll": (I, [P, P, P]),
     "mct_surf_profile_start": (I, [P, I]),
     "mct_surf_profile_read": (I, [P, P, P, P]),
 }

@@ -17,24 +17,32 @@ struct mct_surf_ctx {
   double *d_points = nullptr, *d_params = nullptr, *d_n0 = nullptr, *d_n1 = nullptr, *d_out = nullptr;
   int last_nchains = 0;
   SurfProfile prof;
+  size_t bytes = 0;       // device allocation
+  // serving: one submitted batch in flight, pinned host staging, completion event
+  int *h_ints = nullptr;              // [nslots] slots, [nslots] ncells, [2] device status
+  double *h_dbl = nullptr;            // [nslots][ncell_max][3] points, params; [nslots][np] n0, n1; [nslots][4] out
+  cudaEvent_t done = nullptr;
+  int pending = 0;
+  std::vector<char> in_use;           // slot allocator (mct_surf_admit / mct_surf_evict)
 };
 
 namespace {
 std::string &err() { static thread_local std::string e; return e; }
 }
 
-extern "C" {
+namespace {
 
-int mct_surf_create(const mct_grid *g, const mct_surf_settings *st, const mct_surf_data *dat, int nslots,
-                    int ncell_max, mct_surf_ctx **out) {
-  if (!g || !st || !dat || !out || nslots < 1 || ncell_max < 1 || ncell_max > 12800) return MCT_ERR_ARG;
+// Builds a context; with dry set, only computes its device allocation.
+int surf_create(const mct_grid *g, const mct_surf_settings *st, const mct_surf_data *dat, int nslots,
+                int ncell_max, mct_surf_ctx **out, bool dry, size_t *bytes_out) {
+  if (!g || !st || !dat || (!out && !dry) || nslots < 1 || ncell_max < 1 || ncell_max > 12800) return MCT_ERR_ARG;
   if (g->nx < 2 || g->ny < 2 || g->nz < 1 || !(g->dx > 0) || !(g->dy > 0) || !(g->dz > 0) || !(g->scaling > 0))
     return MCT_ERR_ARG;
   if (st->phase_group != 0) return MCT_ERR_UNSUPPORTED;   // group velocity needs ray paths
   if (st->raylov != 0 && st->raylov != 1) return MCT_ERR_ARG;
   if (dat->np < 1 || dat->np > 60 || dat->nsrc < 1 || dat->nrev < 1) return MCT_ERR_ARG;
   if (!(st->dphase != 0.0)) return MCT_ERR_ARG;
-  *out = nullptr;
+  if (out) *out = nullptr;
   mct_surf_ctx *c = new mct_surf_ctx();
   SurfBatch &b = c->b;
   b.nx = g->nx; b.ny = g->ny; b.nz = g->nz;
@@ -101,9 +109,23 @@ int mct_surf_create(const mct_grid *g, const mct_surf_settings *st, const mct_su
   size_t total = 0;
   for (size_t s : sz) total = ((total + 255) & ~size_t(255)) + s;
   total += 256;
+  if (dry) { *bytes_out = total; delete c; return MCT_OK; }
+  c->bytes = total;
   if (cudaMalloc(&c->mem, total) != cudaSuccess) { err() = "cudaMalloc failed"; delete c; return MCT_ERR_NOMEM; }
   if (cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking) != cudaSuccess) {
     cudaFree(c->mem); delete c; return MCT_ERR_CUDA;
+  }
+  {
+    const size_t ni = 2 * (size_t)nslots + 2;
+    const size_t nd = 2 * (size_t)nslots * ncell_max * 3 + 2 * (size_t)nslots * np + 4 * (size_t)nslots;
+    if (cudaMallocHost(&c->h_ints, sizeof(int) * ni) != cudaSuccess ||
+        cudaMallocHost(&c->h_dbl, sizeof(double) * nd) != cudaSuccess ||
+        cudaEventCreateWithFlags(&c->done, cudaEventDisableTiming) != cudaSuccess) {
+      if (c->h_ints) cudaFreeHost(c->h_ints);
+      if (c->h_dbl) cudaFreeHost(c->h_dbl);
+      cudaFree(c->mem); cudaStreamDestroy(c->stream); delete c; return MCT_ERR_NOMEM;
+    }
+    c->in_use.assign((size_t)nslots, 0);
   }
   Carve cv(c->mem);
   double *per = cv.take<double>(np);
@@ -186,9 +208,28 @@ int mct_surf_create(const mct_grid *g, const mct_surf_settings *st, const mct_su
   return MCT_OK;
 }
 
+}  // namespace
+
+extern "C" {
+
+int mct_surf_create(const mct_grid *g, const mct_surf_settings *st, const mct_surf_data *dat, int nslots,
+                    int ncell_max, mct_surf_ctx **out) {
+  if (!out) return MCT_ERR_ARG;
+  return surf_create(g, st, dat, nslots, ncell_max, out, false, nullptr);
+}
+
+int mct_surf_device_bytes(const mct_grid *g, const mct_surf_settings *st, const mct_surf_data *dat, int nslots,
+                          int ncell_max, size_t *bytes) {
+  if (!bytes) return MCT_ERR_ARG;
+  return surf_create(g, st, dat, nslots, ncell_max, nullptr, true, bytes);
+}
+
 int mct_surf_destroy(mct_surf_ctx *c) {
   if (!c) return MCT_OK;
   cudaStreamSynchronize(c->stream);
+  if (c->done) cudaEventDestroy(c->done);
+  if (c->h_ints) cudaFreeHost(c->h_ints);
+  if (c->h_dbl) cudaFreeHost(c->h_dbl);
   if (c->prof.ev) {
     for (int i = 0; i < 5 * c->prof.max_steps; ++i) cudaEventDestroy(c->prof.ev[i]);
     delete[] c->prof.ev;
@@ -220,7 +261,7 @@ int mct_surf_commit_device(mct_surf_ctx *c, const int *accept, void *stream) {
 
 int mct_surf_forward(mct_surf_ctx *c, int nchains, const int *slots, const int *ncells, const double *points,
                      const double *params, const double *n0, const double *n1, double *out) {
-  if (!c || nchains < 1 || nchains > c->nslots) return MCT_ERR_ARG;
+  if (!c || nchains < 1 || nchains > c->nslots || c->pending) return MCT_ERR_ARG;
   for (int i = 0; i < nchains; ++i) {
     if (slots[i] < 0 || slots[i] >= c->nslots) return MCT_ERR_ARG;
     for (int j = 0; j < i; ++j) if (slots[j] == slots[i]) return MCT_ERR_ARG;
@@ -248,7 +289,7 @@ int mct_surf_forward(mct_surf_ctx *c, int nchains, const int *slots, const int *
 }
 
 int mct_surf_commit(mct_surf_ctx *c, const int *accept) {
-  if (!c || c->last_nchains < 1) return MCT_ERR_ARG;
+  if (!c || c->last_nchains < 1 || c->pending) return MCT_ERR_ARG;
   cudaStream_t s = c->stream;
   MCT_CUDA_TRY(cudaMemcpyAsync(c->d_accept, accept, sizeof(int) * c->last_nchains, cudaMemcpyHostToDevice, s));
   int rc = mct_surf_commit_device(c, c->d_accept, s);
@@ -259,7 +300,7 @@ int mct_surf_commit(mct_surf_ctx *c, const int *accept) {
 
 int mct_surf_noise_likelihood(mct_surf_ctx *c, int nchains, const int *slots, const double *n0, const double *n1,
                               double *out) {
-  if (!c || nchains < 1 || nchains > c->nslots || !slots || !n0 || !n1 || !out) return MCT_ERR_ARG;
+  if (!c || nchains < 1 || nchains > c->nslots || !slots || !n0 || !n1 || !out || c->pending) return MCT_ERR_ARG;
   for (int i = 0; i < nchains; ++i)
     if (slots[i] < 0 || slots[i] >= c->nslots) return MCT_ERR_ARG;
   cudaStream_t s = c->stream;
@@ -274,6 +315,84 @@ int mct_surf_noise_likelihood(mct_surf_ctx *c, int nchains, const int *slots, co
   MCT_CUDA_TRY(cudaStreamSynchronize(s));
   for (int i = 0; i < nchains; ++i)
     if (out[4 * i + 3] != 0.0) return MCT_MODEL_INVALID;
+  return MCT_OK;
+}
+
+// Serving: the caller's arrays are copied into pinned staging before the
+// call returns, the batch runs on the context's stream, and mct_surf_poll
+// reports completion without blocking.
+int mct_surf_submit(mct_surf_ctx *c, int nchains, const int *slots, const int *ncells, const double *points,
+                    const double *params, const double *n0, const double *n1) {
+  if (!c || nchains < 1 || nchains > c->nslots || c->pending || !slots || !ncells || !points || !params || !n0 ||
+      !n1)
+    return MCT_ERR_ARG;
+  for (int i = 0; i < nchains; ++i) {
+    if (slots[i] < 0 || slots[i] >= c->nslots) return MCT_ERR_ARG;
+    for (int j = 0; j < i; ++j) if (slots[j] == slots[i]) return MCT_ERR_ARG;
+    if (ncells[i] < 1 || ncells[i] > c->b.ncell_max) return MCT_ERR_ARG;
+  }
+  cudaStream_t s = c->stream;
+  const int np = c->b.np, ns = c->nslots;
+  const size_t pc = (size_t)nchains * c->b.ncell_max * 3, pmax = (size_t)ns * c->b.ncell_max * 3;
+  int *hs = c->h_ints, *hn = c->h_ints + ns;
+  double *hp = c->h_dbl, *hq = hp + pmax, *h0 = hq + pmax, *h1 = h0 + (size_t)ns * np;
+  std::memcpy(hs, slots, sizeof(int) * nchains);
+  std::memcpy(hn, ncells, sizeof(int) * nchains);
+  std::memcpy(hp, points, sizeof(double) * pc);
+  std::memcpy(hq, params, sizeof(double) * pc);
+  std::memcpy(h0, n0, sizeof(double) * nchains * np);
+  std::memcpy(h1, n1, sizeof(double) * nchains * np);
+  MCT_CUDA_TRY(cudaMemcpyAsync(c->d_slots, hs, sizeof(int) * nchains, cudaMemcpyHostToDevice, s));
+  MCT_CUDA_TRY(cudaMemcpyAsync(c->d_ncells, hn, sizeof(int) * nchains, cudaMemcpyHostToDevice, s));
+  MCT_CUDA_TRY(cudaMemcpyAsync(c->d_points, hp, sizeof(double) * pc, cudaMemcpyHostToDevice, s));
+  MCT_CUDA_TRY(cudaMemcpyAsync(c->d_params, hq, sizeof(double) * pc, cudaMemcpyHostToDevice, s));
+  MCT_CUDA_TRY(cudaMemcpyAsync(c->d_n0, h0, sizeof(double) * nchains * np, cudaMemcpyHostToDevice, s));
+  MCT_CUDA_TRY(cudaMemcpyAsync(c->d_n1, h1, sizeof(double) * nchains * np, cudaMemcpyHostToDevice, s));
+  MCT_CUDA_TRY(cudaMemsetAsync(c->b.dev_status, 0, sizeof(int) * 2, s));
+  int rc = mct_surf_forward_device(c, nchains, c->d_slots, c->d_ncells, c->d_points, c->d_params, c->d_n0,
+                                   c->d_n1, c->d_out, s);
+  if (rc) return rc;
+  double *ho = h1 + (size_t)ns * np;
+  MCT_CUDA_TRY(cudaMemcpyAsync(ho, c->d_out, sizeof(double) * 4 * nchains, cudaMemcpyDeviceToHost, s));
+  MCT_CUDA_TRY(cudaMemcpyAsync(c->h_ints + 2 * ns, c->b.dev_status, sizeof(int) * 2, cudaMemcpyDeviceToHost, s));
+  MCT_CUDA_TRY(cudaEventRecord(c->done, s));
+  c->pending = nchains;
+  return MCT_OK;
+}
+
+int mct_surf_poll(mct_surf_ctx *c, double *out, int *done) {
+  if (!c || !out || !done || !c->pending) return MCT_ERR_ARG;
+  *done = 0;
+  const cudaError_t q = cudaEventQuery(c->done);
+  if (q == cudaErrorNotReady) return MCT_OK;
+  if (q != cudaSuccess) { mct_set_error("cudaEventQuery", cudaGetErrorString(q), __FILE__, __LINE__); return MCT_ERR_CUDA; }
+  const int ns = c->nslots, np = c->b.np, n = c->pending;
+  const double *ho = c->h_dbl + 2 * (size_t)ns * c->b.ncell_max * 3 + 2 * (size_t)ns * np;
+  std::memcpy(out, ho, sizeof(double) * 4 * n);
+  c->pending = 0;
+  *done = 1;
+  const int st = c->h_ints[2 * ns];
+  return st ? st : MCT_OK;
+}
+
+int mct_surf_admit(mct_surf_ctx *c, int *slot) {
+  if (!c || !slot) return MCT_ERR_ARG;
+  for (int i = 0; i < c->nslots; ++i) {
+    if (c->in_use[(size_t)i]) continue;
+    // a fresh chain: nothing committed, so its first forward computes every column
+    MCT_CUDA_TRY(cudaMemsetAsync(c->b.committed + i, 0, sizeof(int), c->stream));
+    c->in_use[(size_t)i] = 1;
+    *slot = i;
+    return MCT_OK;
+  }
+  mct_set_error("mct_surf_admit", "no free chain slot", __FILE__, __LINE__);
+  return MCT_ERR_NOMEM;
+}
+
+int mct_surf_evict(mct_surf_ctx *c, int slot) {
+  if (!c || slot < 0 || slot >= c->nslots || !c->in_use[(size_t)slot]) return MCT_ERR_ARG;
+  MCT_CUDA_TRY(cudaMemsetAsync(c->b.committed + slot, 0, sizeof(int), c->stream));
+  c->in_use[(size_t)slot] = 0;
   return MCT_OK;
 }
 

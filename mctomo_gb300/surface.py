@@ -37,6 +37,30 @@ class SurfData(ctypes.Structure):
                 ("nrays", ctypes.c_int)]
 
 
+def _structs(grid, settings, data):
+    g = Grid(**grid)
+    s = SurfSettings(**settings)
+    npd = len(data["freqs"])
+    arrs = {k: np.ascontiguousarray(data[k], np.float64) for k in ("src", "rev", "freqs", "ttime")}
+    arrs["raystat"] = np.ascontiguousarray(data["raystat"], np.int32)
+    sig = data.get("sigma")
+    arrs["sigma"] = None if sig is None else np.ascontiguousarray(sig, np.float64)
+    d = SurfData(len(arrs["src"]), len(arrs["rev"]), npd, arrs["src"].ctypes.data,
+                 arrs["rev"].ctypes.data, arrs["freqs"].ctypes.data, arrs["raystat"].ctypes.data,
+                 arrs["ttime"].ctypes.data, None if arrs["sigma"] is None else arrs["sigma"].ctypes.data,
+                 int(data.get("nrays", int((arrs["raystat"] == 1).sum()))))
+    return g, s, d, arrs
+
+
+def device_bytes(grid, settings, data, nslots, ncell_max):
+    """Device memory a SurfaceLikelihood with these arguments allocates."""
+    g, s, d, _keep = _structs(grid, settings, data)
+    out = ctypes.c_size_t()
+    check("mct_surf_device_bytes", lib().mct_surf_device_bytes(ctypes.byref(g), ctypes.byref(s), ctypes.byref(d),
+                                                               nslots, ncell_max, ctypes.byref(out)))
+    return out.value
+
+
 class SurfaceLikelihood:
     """grid: dict with nx, ny, nz, xmin, ymin, zmin, dx, dy, dz, scaling,
     water_depth. settings: dict of mct_surf_settings fields. data: dict with
@@ -45,18 +69,9 @@ class SurfaceLikelihood:
 
     def __init__(self, grid, settings, data, nslots, ncell_max):
         self._keep = []
-        g = Grid(**grid)
-        s = SurfSettings(**settings)
+        g, s, d, arrs = _structs(grid, settings, data)
         self.np = len(data["freqs"])
-        arrs = {k: np.ascontiguousarray(data[k], np.float64) for k in ("src", "rev", "freqs", "ttime")}
-        arrs["raystat"] = np.ascontiguousarray(data["raystat"], np.int32)
-        sig = data.get("sigma")
-        arrs["sigma"] = None if sig is None else np.ascontiguousarray(sig, np.float64)
         self._keep.append(arrs)
-        d = SurfData(len(arrs["src"]), len(arrs["rev"]), self.np, arrs["src"].ctypes.data,
-                     arrs["rev"].ctypes.data, arrs["freqs"].ctypes.data, arrs["raystat"].ctypes.data,
-                     arrs["ttime"].ctypes.data, None if arrs["sigma"] is None else arrs["sigma"].ctypes.data,
-                     int(data.get("nrays", int((arrs["raystat"] == 1).sum()))))
         self.nsrc, self.nrev = d.nsrc, d.nrev
         self.nslots, self.ncell_max = nslots, ncell_max
         self.nx, self.ny = g.nx, g.ny
@@ -91,6 +106,35 @@ class SurfaceLikelihood:
         check("mct_surf_forward", lib().mct_surf_forward(self.h, nch, ptr(slots), ptr(ncells), ptr(points),
                                                          ptr(params), ptr(n0), ptr(n1), ptr(out)))
         return out
+
+    def submit(self, slots, ncells, points, params, n0, n1):
+        """Starts forward() without waiting; poll() collects it."""
+        slots = np.ascontiguousarray(slots, np.int32)
+        nch = slots.size
+        ncells = np.ascontiguousarray(ncells, np.int32)
+        points = np.ascontiguousarray(points, np.float64)
+        params = np.ascontiguousarray(params, np.float64)
+        n0 = np.ascontiguousarray(n0, np.float64).reshape(nch, self.np)
+        n1 = np.ascontiguousarray(n1, np.float64).reshape(nch, self.np)
+        check("mct_surf_submit", lib().mct_surf_submit(self.h, nch, ptr(slots), ptr(ncells), ptr(points),
+                                                       ptr(params), ptr(n0), ptr(n1)))
+        self._pending = nch
+
+    def poll(self):
+        """(done, out): out (nchains, 4) once the submitted batch finished."""
+        out = np.zeros((self._pending, 4))
+        done = ctypes.c_int()
+        check("mct_surf_poll", lib().mct_surf_poll(self.h, ptr(out), ctypes.byref(done)))
+        return bool(done.value), (out if done.value else None)
+
+    def admit(self):
+        """Claims a free chain slot (MctError when none is free)."""
+        slot = ctypes.c_int()
+        check("mct_surf_admit", lib().mct_surf_admit(self.h, ctypes.byref(slot)))
+        return slot.value
+
+    def evict(self, slot):
+        check("mct_surf_evict", lib().mct_surf_evict(self.h, int(slot)))
 
     def commit(self, accept):
         accept = np.ascontiguousarray(accept, np.int32)
