@@ -353,6 +353,174 @@ struct FM2D {
 
 }  // namespace
 
+namespace {
+
+// ---- ray paths and group times ---------------------------------------------
+
+// Rectangular grid description shared by the ray tracer and GetVelocity.
+struct G2 { int nx, nz; double gox, goz, dx, dz; };
+
+// GetVelocity (src/likelihood_surf.F90:496-521): bilinear velocity of the
+// model grid vel (column-major (nz, nx), i.e. vel(iy, ix)) at point p.
+double get_velocity(const double *vel, const G2 &g, double px, double pz) {
+  int ix = (int)std::floor((px - g.gox) / g.dx) + 1;
+  int iy = (int)std::floor((pz - g.goz) / g.dz) + 1;
+  if (ix < 1) ix = 1;
+  if (iy < 1) iy = 1;
+  if (ix >= g.nx) ix = g.nx - 1;
+  if (iy >= g.nz) iy = g.nz - 1;
+  double dsx = px - (g.gox + (double)(ix - 1) * g.dx);
+  double dsy = pz - (g.goz + (double)(iy - 1) * g.dz);
+  double qv = 0;
+  for (int i = 1; i <= 2; ++i)
+    for (int j = 1; j <= 2; ++j) {
+      double weight = (1.0 - std::fabs((double)(i - 1) * g.dx - dsx) / g.dx) *
+                      (1.0 - std::fabs((double)(j - 1) * g.dz - dsy) / g.dz);
+      qv = qv + weight * vel[(size_t)(ix + i - 2) * g.nz + (iy + j - 2)];
+    }
+  return qv;
+}
+
+// CalGroupTime (src/likelihood_surf.F90:455-494) for one ray, and the ray's
+// length (T_RAY%length, fm2d/fm2dray_cartesian.f90:51-65).
+void group_time(const std::vector<double> &rx, const std::vector<double> &rz, const double *vel, const G2 &g,
+                double *time, double *length) {
+  *time = 0; *length = 0;
+  const size_t n = rx.size();
+  if (n < 2) return;
+  double vhead = get_velocity(vel, g, rx[0], rz[0]);
+  for (size_t k = 1; k < n; ++k) {
+    double dist = (rx[k] - rx[k - 1]) * (rx[k] - rx[k - 1]) + (rz[k] - rz[k - 1]) * (rz[k] - rz[k - 1]);
+    dist = std::sqrt(dist);
+    double vtail = get_velocity(vel, g, rx[k], rz[k]);
+    *time = *time + dist * 2 / (vhead + vtail);
+    *length = *length + dist;
+    vhead = vtail;
+  }
+}
+
+// rpaths (fm2d/fm2dray_cartesian.f90:801-1455) without Frechet derivatives,
+// one receiver: steepest descent on the final coarse field ttn (nnz, nnx),
+// or on the refined-box field ttnr / states nstsr where the ray is inside the
+// box and the four corners of its cell are accepted. Returns 1 for a ray
+// that reached the point limit (the reference's crazy ray).
+int trace_ray(double rcx, double rcz, double scx, double scz, const G2 &c, const double *ttn, int asgr,
+              const G2 &r, const double *ttnr, const int *nstsr, std::vector<double> &rx, std::vector<double> &rz) {
+  auto T = [&](int iz, int ix) { return ttn[(size_t)(ix - 1) * c.nz + (iz - 1)]; };
+  auto TR = [&](int iz, int ix) { return ttnr[(size_t)(ix - 1) * r.nz + (iz - 1)]; };
+  auto SR = [&](int iz, int ix) { return nstsr[(size_t)(ix - 1) * r.nz + (iz - 1)]; };
+  const int nnx = c.nx, nnz = c.nz, nnxr = r.nx, nnzr = r.nz;
+  const double gox = c.gox, goz = c.goz, dnx = c.dx, dnz = c.dz;
+  const double goxr = r.gox, gozr = r.goz, dnxr = r.dx, dnzr = r.dz;
+  const int maxrp = nnx * nnz;
+  int isx, isz;
+  if (asgr == 1) { isx = (int)std::floor((scx - goxr) / dnxr) + 1; isz = (int)std::floor((scz - gozr) / dnzr) + 1; }
+  else { isx = (int)std::floor((scx - gox) / dnx) + 1; isz = (int)std::floor((scz - goz) / dnz) + 1; }
+  double dpl = dnx, rd1 = dnz;
+  if (rd1 < dpl) dpl = rd1;
+  dpl = 0.5 * dpl;
+  rx.assign(1, rcx); rz.assign(1, rcz);
+  int ipx = (int)std::floor((rcx - gox) / dnx) + 1;
+  int ipz = (int)std::floor((rcz - goz) / dnz) + 1;
+  int sw = 0;
+  if (ipx < 1 || ipx >= nnx) sw = 1;
+  if (ipz < 1 || ipz >= nnz) sw = 1;
+  if (sw == 1) return -1;   // the reference stops the program
+  if (ipx == nnx) ipx = ipx - 1;
+  if (ipz == nnz) ipz = ipz - 1;
+  int nrp = 1;
+  double sred = (scx - rx[0]) * (scx - rx[0]);
+  sred = sred + (scz - rz[0]) * (scz - rz[0]);
+  sred = std::sqrt(sred);
+  if (sred < 2.0 * dpl) { rx.push_back(scx); rz.push_back(scz); nrp = 2; sw = 1; }
+  int ipxr = 0, ipzr = 0, igref = 0;
+  auto in_refined = [&](double px, double pz) {
+    ipxr = (int)std::floor((px - goxr) / dnxr) + 1;
+    ipzr = (int)std::floor((pz - gozr) / dnzr) + 1;
+    int g = 1;
+    if (ipxr < 1 || ipxr >= nnxr) g = 0;
+    if (ipzr < 1 || ipzr >= nnzr) g = 0;
+    if (g == 1) {
+      if (SR(ipzr, ipxr) != 0 || SR(ipzr + 1, ipxr) != 0) g = 0;
+      if (SR(ipzr, ipxr + 1) != 0 || SR(ipzr + 1, ipxr + 1) != 0) g = 0;
+    }
+    return g;
+  };
+  if (asgr == 1) igref = in_refined(rcx, rcz);
+  if (sw == 0) {
+    if (asgr == 1) {
+      if (igref == 1 && ipxr == isx && ipzr == isz) { rx.push_back(scx); rz.push_back(scz); nrp = 2; sw = 1; }
+    } else {
+      if (ipx == isx && ipz == isz) { rx.push_back(scx); rz.push_back(scz); nrp = 2; sw = 1; }
+    }
+  }
+  int crazy = 0;
+  for (int j = 1; j <= maxrp; ++j) {
+    if (sw == 1) break;
+    double dtx, dtz;
+    const double px = rx[(size_t)j - 1], pz = rz[(size_t)j - 1];
+    if (igref == 1) {
+      if (ipxr == 1) dtx = (TR(ipzr, ipxr + 1) - TR(ipzr, ipxr)) / dnxr;
+      else if (ipxr == nnxr) dtx = (TR(ipzr, ipxr) - TR(ipzr, ipxr - 1)) / dnxr;
+      else dtx = (TR(ipzr, ipxr + 1) - TR(ipzr, ipxr - 1)) / (2.0 * dnxr);
+      if (ipzr == 1) dtz = (TR(ipzr + 1, ipxr) - TR(ipzr, ipxr)) / dnzr;
+      else if (ipzr == nnzr) dtz = (TR(ipzr, ipxr) - TR(ipzr - 1, ipxr)) / dnzr;
+      else dtz = (TR(ipzr + 1, ipxr) - TR(ipzr - 1, ipxr)) / (2.0 * dnzr);
+    } else {
+      if (ipx == 1) dtx = (T(ipz, ipx + 1) - T(ipz, ipx)) / dnx;
+      else if (ipx == nnx) dtx = (T(ipz, ipx) - T(ipz, ipx - 1)) / dnx;
+      else dtx = (T(ipz, ipx + 1) - T(ipz, ipx - 1)) / (2.0 * dnx);
+      // the reference tests the refined index here (ipzr == nnzr); without
+      // refinement those are undefined (an unset local), and the coarse
+      // index test the code intends (ipz == nnz) is used
+      if (ipz == 1) dtz = (T(ipz + 1, ipx) - T(ipz, ipx)) / dnz;
+      else if (asgr == 1 ? ipzr == nnzr : ipz == nnz) dtz = (T(ipz, ipx) - T(ipz - 1, ipx)) / dnz;
+      else dtz = (T(ipz + 1, ipx) - T(ipz - 1, ipx)) / (2.0 * dnz);
+    }
+    rd1 = std::sqrt(dtx * dtx + dtz * dtz);
+    double nx = px - dpl * dtx / rd1;
+    double nz = pz - dpl * dtz / rd1;
+    rx.push_back(nx); rz.push_back(nz);
+    if (asgr == 1) {
+      igref = in_refined(nx, nz);
+      ipx = (int)std::floor((nx - gox) / dnx) + 1;
+      ipz = (int)std::floor((nz - goz) / dnz) + 1;
+    } else {
+      ipx = (int)std::floor((nx - gox) / dnx) + 1;
+      ipz = (int)std::floor((nz - goz) / dnz) + 1;
+      igref = 0;
+    }
+    sred = (scx - nx) * (scx - nx);
+    sred = sred + (scz - nz) * (scz - nz);
+    sred = std::sqrt(sred);
+    sw = 0;
+    if (sred < 2.0 * dpl) { rx.push_back(scx); rz.push_back(scz); nrp = j + 2; sw = 1; break; }
+    if (asgr == 1) {
+      if (igref == 1 && ipxr == isx && ipzr == isz) { rx.push_back(scx); rz.push_back(scz); nrp = j + 2; sw = 1; break; }
+    } else {
+      if (ipx == isx && ipz == isz) { rx.push_back(scx); rz.push_back(scz); nrp = j + 2; sw = 1; break; }
+    }
+    if (ipx < 1) { rx.back() = gox; ipx = 1; }
+    if (ipx >= nnx) { rx.back() = gox + (double)(nnx - 1) * dnx; ipx = nnx - 1; }
+    if (ipz < 1) { rz.back() = goz; ipz = 1; }
+    if (ipz >= nnz) { rz.back() = goz + (double)(nnz - 1) * dnz; ipz = nnz - 1; }
+    if (j == maxrp - 1 && sw == 0) { crazy = 1; sw = 1; break; }
+  }
+  rx.resize((size_t)nrp); rz.resize((size_t)nrp);
+  return crazy;
+}
+
+// What modrays returns with uar = 0 besides the phase times: per path the
+// group time along its ray (CalGroupTime on gvel, the model grid
+// (nvz, nvx)), the ray length, and the number of crazy rays.
+struct RayOut {
+  const double *gvel;
+  double *gtime, *raylen;
+  int crazy;
+};
+
+}  // namespace
+
 extern "C" {
 
 // Test hook: record the marching order (stage, node, heap size, time) of one
@@ -370,12 +538,14 @@ int orc_fm2d_trace_count(void) { return g_trace_n; }
 // (nnz, nnx, nsrc) final coarse travel-time fields.
 // Returns 0, or -1 for a source/receiver outside the grid (the reference
 // stops the program there).
-int orc_modrays(int nsrc, const double *scx, const double *scz, int nrc,
-                const double *rcx, const double *rcz, const int *srs, int nvx,
-                int nvz, double goxd, double gozd, double dvxd, double dvzd,
-                const double *velvin, int gdx, int gdz, int asgr, int sgdl,
-                int sgs, int fom, double snb, double *ttime, double *tfield) {
-  (void)snb;  // narrow-band capacity only; heap here grows as needed
+}  // extern "C"
+
+namespace {
+int modrays_impl(int nsrc, const double *scx, const double *scz, int nrc,
+                 const double *rcx, const double *rcz, const int *srs, int nvx,
+                 int nvz, double goxd, double gozd, double dvxd, double dvzd,
+                 const double *velvin, int gdx, int gdz, int asgr, int sgdl,
+                 int sgs, int fom, double *ttime, double *tfield, RayOut *ro) {
   // gridder (fm2dray_cartesian.f90:491-600)
   int ldv = nvz + 2;
   auto velv = [&](int i, int j) { return velvin[(size_t)j * ldv + i]; };  // velv(i,j), i=0..nvz+1
@@ -439,6 +609,10 @@ int orc_modrays(int nsrc, const double *scx, const double *scz, int nrc,
   };
   load_coarse();
 
+  std::vector<double> ttnr;
+  std::vector<int> nstsr;
+  G2 rgeom{0, 0, 0, 0, 1, 1};
+  if (ro) ro->crazy = 0;
   for (int i = 1; i <= nsrc; ++i) {
     int any = 0;
     for (int j = 0; j < nrc; ++j) any += srs[(size_t)(i - 1) * nrc + j];
@@ -510,12 +684,14 @@ int orc_modrays(int nsrc, const double *scx, const double *scz, int nrc,
       }
       if (f.travel(x, z, 1) != 0) return -1;
       // map refined grid onto coarse grid
-      std::vector<double> ttnr((size_t)nrnz * nrnx);
-      std::vector<int> nstsr((size_t)nrnz * nrnx);
+      ttnr.assign((size_t)nrnz * nrnx, 0.0);
+      nstsr.assign((size_t)nrnz * nrnx, -1);
+      rgeom = G2{nrnx, nrnz, gorx, gorz, drnx, drnz};
       for (int l = 1; l <= nrnx; ++l)
         for (int k = 1; k <= nrnz; ++k) {
-          ttnr[(size_t)(l - 1) * nrnz + k - 1] = f.T(k, l);
+          // far nodes hold uninitialised memory in the reference; 0 here
           nstsr[(size_t)(l - 1) * nrnz + k - 1] = f.S(k, l);
+          ttnr[(size_t)(l - 1) * nrnz + k - 1] = f.S(k, l) == -1 ? 0.0 : f.T(k, l);
         }
       std::fill(f.nsts.begin(), f.nsts.end(), -1);
       for (int k = 1; k <= nrnz; k += sgdl) {
@@ -590,7 +766,97 @@ int orc_modrays(int nsrc, const double *scx, const double *scz, int nrc,
       }
       ttime[(size_t)(i - 1) * nrc + r - 1] = trr;
     }
+    if (ro) {
+      // rpaths (modrays calls it after srtimes when uar = 0)
+      std::vector<double> ttc((size_t)nnx * nnz);
+      for (int ix = 1; ix <= nnx; ++ix)
+        for (int iz = 1; iz <= nnz; ++iz) ttc[(size_t)(ix - 1) * nnz + iz - 1] = f.T(iz, ix);
+      const G2 cg{nnx, nnz, gox, goz, dnx, dnz};
+      const G2 mg{nvx, nvz, goxd, gozd, dvxd, dvzd};
+      std::vector<double> rx, rz;
+      for (int r = 1; r <= nrc; ++r) {
+        if (srs[(size_t)(i - 1) * nrc + r - 1] == 0) continue;
+        int cz = trace_ray(rcx[r - 1], rcz[r - 1], x, z, cg, ttc.data(), asgr, rgeom, ttnr.data(), nstsr.data(),
+                           rx, rz);
+        if (cz < 0) return -1;
+        ro->crazy += cz;
+        double gt, len;
+        group_time(rx, rz, ro->gvel, mg, &gt, &len);
+        ro->gtime[(size_t)(i - 1) * nrc + r - 1] = gt;
+        ro->raylen[(size_t)(i - 1) * nrc + r - 1] = len;
+      }
+    }
   }
+  return 0;
+}
+}  // namespace
+
+extern "C" {
+
+int orc_modrays(int nsrc, const double *scx, const double *scz, int nrc,
+                const double *rcx, const double *rcz, const int *srs, int nvx,
+                int nvz, double goxd, double gozd, double dvxd, double dvzd,
+                const double *velvin, int gdx, int gdz, int asgr, int sgdl,
+                int sgs, int fom, double snb, double *ttime, double *tfield) {
+  (void)snb;  // narrow-band capacity only; heap here grows as needed
+  return modrays_impl(nsrc, scx, scz, nrc, rcx, rcz, srs, nvx, nvz, goxd, gozd, dvxd, dvzd, velvin, gdx, gdz,
+                      asgr, sgdl, sgs, fom, ttime, tfield, nullptr);
+}
+
+// modrays with uar = 0 followed by CalGroupTime: ttime as orc_modrays (phase
+// times); gvel the model-grid velocity for the group delay ((nvz, nvx)
+// column-major); gtime / raylen (nrc, nsrc) the group time and length of
+// each path's ray; *crazy the number of rays that hit the point limit.
+int orc_modrays_group(int nsrc, const double *scx, const double *scz, int nrc,
+                      const double *rcx, const double *rcz, const int *srs, int nvx,
+                      int nvz, double goxd, double gozd, double dvxd, double dvzd,
+                      const double *velvin, int gdx, int gdz, int asgr, int sgdl,
+                      int sgs, int fom, const double *gvel, double *ttime, double *gtime,
+                      double *raylen, int *crazy) {
+  RayOut ro{gvel, gtime, raylen, 0};
+  int rc = modrays_impl(nsrc, scx, scz, nrc, rcx, rcz, srs, nvx, nvz, goxd, gozd, dvxd, dvzd, velvin, gdx, gdz,
+                        asgr, sgdl, sgs, fom, ttime, nullptr, &ro);
+  *crazy = ro.crazy;
+  return rc;
+}
+
+// setup_straightRays + CalGroupTime (src/likelihood_surf.F90:412-494) for one
+// period: straight rays from each source to each receiver with points every
+// min(dx, dy)/2, group delay on vel (model grid (ny, nx) column-major).
+// dist (nrev, nsrc) always receives the source-receiver distance; time only
+// where raystat == 1 (0 elsewhere). Returns -1 if a ray point leaves the grid
+// (the reference's fatal 'Straight ray out of area').
+int orc_straight_group(int nsrc, const double *src, int nrev, const double *rev, const int *raystat, int nx,
+                       int ny, double xmin, double ymin, double dx, double dy, const double *vel, double *time,
+                       double *dist) {
+  const G2 g{nx, ny, xmin, ymin, dx, dy};
+  const double xmax = xmin + (double)(nx - 1) * dx, ymax = ymin + (double)(ny - 1) * dy;
+  const double dl = std::min(dx, dy) / 2;
+  std::vector<double> rx, rz;
+  for (int j = 1; j <= nsrc; ++j)
+    for (int k = 1; k <= nrev; ++k) {
+      const int n = k + (j - 1) * nrev;
+      const double ddx = rev[2 * (k - 1)] - src[2 * (j - 1)];
+      const double ddy = rev[2 * (k - 1) + 1] - src[2 * (j - 1) + 1];
+      const double ds = std::sqrt(ddx * ddx + ddy * ddy);
+      dist[n - 1] = ds;
+      time[n - 1] = 0;
+      if (raystat[n - 1] != 1) continue;
+      const int npts = (int)std::floor(ds / dl) + 1;
+      rx.assign((size_t)npts, 0.0); rz.assign((size_t)npts, 0.0);
+      for (int l = 1; l <= npts - 1; ++l) {
+        rx[(size_t)l - 1] = src[2 * (j - 1)] + (double)(l - 1) * dl * ddx / ds;
+        rz[(size_t)l - 1] = src[2 * (j - 1) + 1] + (double)(l - 1) * dl * ddy / ds;
+        if (rx[(size_t)l - 1] < xmin || rx[(size_t)l - 1] > xmax || rz[(size_t)l - 1] < ymin ||
+            rz[(size_t)l - 1] > ymax)
+          return -1;
+      }
+      rx[(size_t)npts - 1] = rev[2 * (k - 1)];
+      rz[(size_t)npts - 1] = rev[2 * (k - 1) + 1];
+      double t, len;
+      group_time(rx, rz, vel, g, &t, &len);
+      time[n - 1] = t;
+    }
   return 0;
 }
 

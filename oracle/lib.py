@@ -59,6 +59,9 @@ def load():
             "orc_surfmodes": (_I, [_P, _P, _P, _P, _I, _P, _I, _I, _I, _D, _P, _P, _P]),
             "orc_modrays": (_I, [_I, _P, _P, _I, _P, _P, _P, _I, _I, _D, _D, _D, _D, _P,
                                  _I, _I, _I, _I, _I, _I, _D, _P, _P]),
+            "orc_modrays_group": (_I, [_I, _P, _P, _I, _P, _P, _P, _I, _I, _D, _D, _D, _D, _P,
+                                       _I, _I, _I, _I, _I, _I, _P, _P, _P, _P, _P]),
+            "orc_straight_group": (_I, [_I, _P, _I, _P, _P, _I, _I, _D, _D, _D, _D, _P, _P, _P]),
             "orc_fm2d_trace": (_I, [_I, _P, _P, _I]),
             "orc_fm2d_trace_count": (_I, []),
             "orc_fast_marching3d": (_I, [_I, _I, _I, _D, _D, _D, _D, _D, _D, _P, _P, _P, _I,

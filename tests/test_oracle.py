@@ -147,3 +147,73 @@ def test_misfit_reduction_hand_computed(orc):
     s = 0.1
     like = (r ** 2 / (2 * s * s)).sum() + 3 * np.log(0.1) + np.log(1.0) + 1.5 * np.log(np.float64(np.float32(6.283185)))
     np.testing.assert_allclose(out, [like, (r ** 2 / s ** 2).sum(), (r ** 2).sum()], rtol=1e-12)
+
+
+def _modrays_group(orc, st, srs, nv, h, velv, gvel, asgr=1, sgdl=4, sgs=8, fom=1):
+    n = len(st)
+    sx, sz = np.ascontiguousarray(st[:, 0]), np.ascontiguousarray(st[:, 1])
+    tt = np.zeros((n, n)); gt = np.zeros((n, n)); ln = np.zeros((n, n)); cz = ctypes.c_int()
+    rc = orc.orc_modrays_group(n, P(sx), P(sz), n, P(sx), P(sz), P(np.ascontiguousarray(srs, np.int32)), nv, nv,
+                               0.0, 0.0, h, h, P(np.ascontiguousarray(velv)), 1, 1, asgr, sgdl, sgs, fom,
+                               P(np.ascontiguousarray(gvel)), P(tt), P(gt), P(ln), ctypes.byref(cz))
+    assert rc == 0
+    return tt, gt, ln, cz.value
+
+
+@pytest.mark.parametrize("asgr", [1, 0])
+def test_rays_homogeneous_group_time_is_length_over_velocity(orc, asgr):
+    # uniform phase velocity: rays are close to straight lines and the group
+    # delay along them is exactly their length over the uniform group velocity
+    nv, h = 41, 0.5
+    st = np.array([[3.1, 4.2], [17.3, 5.6], [9.9, 16.4], [15.2, 15.9]])
+    n = len(st)
+    srs = 1 - np.eye(n, dtype=np.int32)
+    velv = np.full((nv + 2, nv + 2), 2.0)
+    gvel = np.full((nv, nv), 1.6)
+    tt, gt, ln, cz = _modrays_group(orc, st, srs, nv, h, velv, gvel, asgr=asgr)
+    assert cz == 0
+    d = np.hypot(st[:, None, 0] - st[None, :, 0], st[:, None, 1] - st[None, :, 1])
+    m = srs == 1        # [source][receiver], as ttime
+    np.testing.assert_allclose(gt[m], ln[m] / 1.6, rtol=1e-12)
+    assert np.all(ln[m] >= d[m] * (1 - 1e-9))
+    if asgr == 1:
+        assert np.all(ln[m] <= d[m] * 1.02)
+    # without refinement the reference takes the gradient at the cell's
+    # lower-left node, and rays may circle the source cell before they end
+    np.testing.assert_allclose(tt[m], d[m] / 2.0, rtol=0.05)   # FMM discretisation
+
+
+def test_rays_phase_times_unchanged_by_ray_tracing(orc):
+    rng = np.random.default_rng(3)
+    nv, h = 31, 1.0
+    st = rng.uniform(3.0, 27.0, (6, 2))
+    srs = np.triu(np.ones((6, 6), np.int32), 1)
+    velv = rng.uniform(1.0, 2.0, (nv + 2, nv + 2))
+    gvel = rng.uniform(0.8, 1.6, (nv, nv))
+    tt, gt, ln, cz = _modrays_group(orc, st, srs, nv, h, velv, gvel)
+    tt0 = np.zeros((6, 6))
+    sx, sz = np.ascontiguousarray(st[:, 0]), np.ascontiguousarray(st[:, 1])
+    assert orc.orc_modrays(6, P(sx), P(sz), 6, P(sx), P(sz), P(srs), nv, nv, 0.0, 0.0, h, h, P(velv), 1, 1, 1, 4, 8,
+                           1, 0.5, P(tt0), None) == 0
+    m = srs == 1
+    np.testing.assert_array_equal(tt[m], tt0[m])
+    d = np.hypot(st[:, None, 0] - st[None, :, 0], st[:, None, 1] - st[None, :, 1])
+    assert np.all(ln[m] >= d[m] * (1 - 1e-9))
+    # group times bracketed by the extreme group velocities along the ray
+    assert np.all(gt[m] >= ln[m] / 1.6 * (1 - 1e-12)) and np.all(gt[m] <= ln[m] / 0.8 * (1 + 1e-12))
+
+
+def test_straight_rays_uniform_velocity(orc):
+    nx = ny = 21
+    src = np.array([[1.0, 1.5], [8.0, 12.5]])
+    rev = np.array([[15.0, 3.0], [2.5, 18.0], [19.0, 19.0]])
+    raystat = np.array([1, 1, 0, 1, 0, 1], np.int32)
+    vel = np.full((nx, ny), 2.5)
+    t = np.zeros(6); d = np.zeros(6)
+    rc = orc.orc_straight_group(2, P(np.ascontiguousarray(src)), 3, P(np.ascontiguousarray(rev)), P(raystat), nx, ny,
+                                0.0, 0.0, 1.0, 1.0, P(vel), P(t), P(d))
+    assert rc == 0
+    ds = np.hypot(rev[None, :, 0] - src[:, None, 0], rev[None, :, 1] - src[:, None, 1]).reshape(-1)
+    np.testing.assert_allclose(d, ds, rtol=1e-15)
+    np.testing.assert_allclose(t[raystat == 1], ds[raystat == 1] / 2.5, rtol=1e-12)
+    assert np.all(t[raystat == 0] == 0)
