@@ -180,7 +180,8 @@ def test_rays_homogeneous_group_time_is_length_over_velocity(orc, asgr):
         assert np.all(ln[m] <= d[m] * 1.02)
     # without refinement the reference takes the gradient at the cell's
     # lower-left node, and rays may circle the source cell before they end
-    np.testing.assert_allclose(tt[m], d[m] / 2.0, rtol=0.05)   # FMM discretisation
+    # FMM discretisation (first order near the source without refinement)
+    np.testing.assert_allclose(tt[m], d[m] / 2.0, rtol=0.05 if asgr == 1 else 0.1)
 
 
 def test_rays_phase_times_unchanged_by_ray_tracing(orc):
