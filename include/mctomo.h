@@ -166,6 +166,21 @@ int mct_modrays_batch(int nmaps, int nsrc, const double *scx,
                       int asgr, int sgdl, int sgs, int fom, double *ttime,
                       double *tfield, int precision);
 
+/* Group delays along ray paths: modrays with uar = 0 (ray paths traced from
+ * each receiver down the phase travel-time field, fm2d/fm2dray_cartesian.f90
+ * rpaths 801-1455) followed by CalGroupTime (src/likelihood_surf.F90:455-494)
+ * on the group-velocity maps gvel[nmaps][nvx][nvz] (Fortran (nvz, nvx), the
+ * model grid). Arguments as mct_modrays_batch; ttime receives the phase
+ * times, gtime the group times and raylen the ray lengths
+ * ([nmaps][nsrc][nrc]), crazy[nmaps] the rays that reached the point limit
+ * (the reference's crazyray; their gtime and raylen are 0). */
+int mct_modrays_group_batch(int nmaps, int nsrc, const double *scx, const double *scz, int nrc,
+                            const double *rcx, const double *rcz, int srs_nmaps, const int *srs, int nvx,
+                            int nvz, double goxd, double gozd, double dvxd, double dvzd,
+                            const double *velv, const double *gvel, int gdx, int gdz, int asgr, int sgdl,
+                            int sgs, int fom, double *ttime, double *gtime, double *raylen, int *crazy,
+                            int precision);
+
 
 /* ------------------------------------------------------------------------
  * Surface-wave likelihood with device-resident chains, replaces

@@ -9,7 +9,8 @@ from ._lib import MctError, lib, LIB_PATH  # noqa: F401
 from .surface import SurfaceLikelihood  # noqa: F401
 from .body import BodyLikelihood  # noqa: F401
 from .forward import (  # noqa: F401
-    kdtree_to_grid, surfdisp96, surfdisp_mmodes, surfmodes, surfdisp_batch, modrays, modrays_batch, fast_marching3d, eikonal3d_batch,
+    kdtree_to_grid, surfdisp96, surfdisp_mmodes, surfmodes, surfdisp_batch, modrays, modrays_batch,
+    modrays_group_batch, fast_marching3d, eikonal3d_batch,
 )
 
 __version__ = "0.1.0"

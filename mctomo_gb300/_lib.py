@@ -36,6 +36,8 @@ SIGNATURES = {
     "mct_surfdisp_batch_device": (I, [I, I, P, P, P, P, P, I, P, I, I, I, D, I, I, P, P, P, P, P]),
     "mct_modrays": (I, [I, P, P, I, P, P, P, I, I, I, D, D, D, D, P, I, I, I, I, I, D, I, D, P, I, P, P]),
     "mct_modrays_batch": (I, [I, I, P, P, I, P, P, I, P, I, I, D, D, D, D, P, I, I, I, I, I, I, P, P, I]),
+    "mct_modrays_group_batch": (I, [I, I, P, P, I, P, P, I, P, I, I, D, D, D, D, P, P, I, I, I, I, I, I, P, P, P, P,
+                                    I]),
     "mct_fast_marching3d": (I, [I, I, I, D, D, D, D, D, D, P, P, P, I, I, P, P]),
     "mct_eikonal3d_batch": (I, [I, I, I, I, D, D, D, D, D, D, I, P, P, P, I, P, I, P, P, P]),
     "mct_body_create": (I, [P, P, P, I, I, P]),

@@ -305,11 +305,18 @@ int mct_surfmodes(const double *thick, const double *vp, const double *vs, const
 // ---------------------------------------------------------------------------
 // 2D travel times (fm2d modrays)
 // ---------------------------------------------------------------------------
-int mct_modrays_batch(int nmaps, int nsrc, const double *scx, const double *scz, int nrc,
-                      const double *rcx, const double *rcz, int srs_nmaps, const int *srs, int nvx,
-                      int nvz, double goxd, double gozd, double dvxd, double dvzd,
-                      const double *velv, int gdx, int gdz, int asgr, int sgdl, int sgs, int fom,
-                      double *ttime, double *tfield, int precision) {
+}  // extern "C"
+
+namespace {
+// modrays over many maps; with gvel set (rays), also the ray-path group
+// delays and lengths of every path (modrays uar = 0 + CalGroupTime).
+int modrays_batch(int nmaps, int nsrc, const double *scx, const double *scz, int nrc,
+                  const double *rcx, const double *rcz, int srs_nmaps, const int *srs, int nvx,
+                  int nvz, double goxd, double gozd, double dvxd, double dvzd,
+                  const double *velv, int gdx, int gdz, int asgr, int sgdl, int sgs, int fom,
+                  double *ttime, double *tfield, int precision, const double *gvel, double *gtime,
+                  double *raylen, int *crazy) {
+  const bool rays = gvel != nullptr;
   if (nmaps < 1 || nsrc < 1 || nrc < 1 || nvx < 2 || nvz < 2 || gdx < 1 || gdz < 1 ||
       srs_nmaps < 1 || (asgr == 1 && (sgdl < 1 || sgs < 1)) || (fom != 0 && fom != 1) ||
       !(dvxd > 0) || !(dvzd > 0))
@@ -347,7 +354,12 @@ int mct_modrays_batch(int nmaps, int nsrc, const double *scx, const double *scz,
                              sizeof(int) * (size_t)srs_nmaps * nsrc * nrc, sizeof(int2) * ns,
                              sizeof(double) * (size_t)nmaps * nsrc * nrc,
                              tfield ? sizeof(double) * (size_t)nmaps * nsrc * nnx * nnz : 0, sizeof(int),
-                             sizeof(int)});
+                             sizeof(int),
+                             rays ? sizeof(double) * (size_t)nmaps * nvx * nvz : 0,
+                             rays ? sizeof(double) * 2 * (size_t)nmaps * nsrc * nrc : 0,
+                             rays ? sizeof(int) * (size_t)nmaps : 0,
+                             rays ? sizeof(double) * (size_t)plan.nref_max * ns : 0,
+                             rays ? sizeof(short) * (size_t)plan.nref_max * ns : 0});
   rc = g_ws.reserve(bytes); if (rc) return rc;
   Carve cv(g_ws.p);
   double *d_velv = cv.take<double>(nv * nmaps);
@@ -365,7 +377,23 @@ int mct_modrays_batch(int nmaps, int nsrc, const double *scx, const double *scz,
   double *d_tf = tfield ? cv.take<double>((size_t)nmaps * nsrc * nnx * nnz) : nullptr;
   int *d_status = cv.take<int>(1);
   job.vmin_bits = cv.take<int>(1);
+  double *d_gvel = nullptr, *d_gt = nullptr;
+  int *d_crazy = nullptr;
+  if (rays) {
+    d_gvel = cv.take<double>((size_t)nmaps * nvx * nvz);
+    d_gt = cv.take<double>(2 * (size_t)nmaps * nsrc * nrc);
+    d_crazy = cv.take<int>((size_t)nmaps);
+    job.ref_t = cv.take<double>((size_t)plan.nref_max * ns);
+    job.ref_s = cv.take<short>((size_t)plan.nref_max * ns);
+    job.rays = 1; job.gvel = d_gvel; job.gtime = d_gt; job.raylen = d_gt + (size_t)nmaps * nsrc * nrc;
+    job.crazy = d_crazy;
+  }
   cudaStream_t s = g_stream;
+  if (rays) {
+    MCT_CUDA_TRY(cudaMemcpyAsync(d_gvel, gvel, sizeof(double) * (size_t)nmaps * nvx * nvz, cudaMemcpyHostToDevice, s));
+    MCT_CUDA_TRY(cudaMemsetAsync(d_gt, 0, sizeof(double) * 2 * (size_t)nmaps * nsrc * nrc, s));
+    MCT_CUDA_TRY(cudaMemsetAsync(d_crazy, 0, sizeof(int) * (size_t)nmaps, s));
+  }
   MCT_CUDA_TRY(cudaMemcpyAsync(d_velv, velv, sizeof(double) * nv * nmaps, cudaMemcpyHostToDevice, s));
   MCT_CUDA_TRY(cudaMemcpyAsync(d_xy, scx, sizeof(double) * nsrc, cudaMemcpyHostToDevice, s));
   MCT_CUDA_TRY(cudaMemcpyAsync(d_xy + nsrc, scz, sizeof(double) * nsrc, cudaMemcpyHostToDevice, s));
@@ -401,8 +429,38 @@ int mct_modrays_batch(int nmaps, int nsrc, const double *scx, const double *scz,
   MCT_CUDA_TRY(cudaMemcpyAsync(ttime, d_tt, sizeof(double) * (size_t)nmaps * nsrc * nrc, cudaMemcpyDeviceToHost, s));
   if (tfield)
     MCT_CUDA_TRY(cudaMemcpyAsync(tfield, d_tf, sizeof(double) * (size_t)nmaps * nsrc * nnx * nnz, cudaMemcpyDeviceToHost, s));
+  if (rays) {
+    MCT_CUDA_TRY(cudaMemcpyAsync(gtime, d_gt, sizeof(double) * (size_t)nmaps * nsrc * nrc, cudaMemcpyDeviceToHost, s));
+    MCT_CUDA_TRY(cudaMemcpyAsync(raylen, d_gt + (size_t)nmaps * nsrc * nrc, sizeof(double) * (size_t)nmaps * nsrc * nrc,
+                                 cudaMemcpyDeviceToHost, s));
+    MCT_CUDA_TRY(cudaMemcpyAsync(crazy, d_crazy, sizeof(int) * (size_t)nmaps, cudaMemcpyDeviceToHost, s));
+  }
   rc = sync_and_check(s, d_status);
   return rc;
+}
+}  // namespace
+
+extern "C" {
+
+int mct_modrays_batch(int nmaps, int nsrc, const double *scx, const double *scz, int nrc,
+                      const double *rcx, const double *rcz, int srs_nmaps, const int *srs, int nvx,
+                      int nvz, double goxd, double gozd, double dvxd, double dvzd,
+                      const double *velv, int gdx, int gdz, int asgr, int sgdl, int sgs, int fom,
+                      double *ttime, double *tfield, int precision) {
+  return modrays_batch(nmaps, nsrc, scx, scz, nrc, rcx, rcz, srs_nmaps, srs, nvx, nvz, goxd, gozd, dvxd, dvzd,
+                       velv, gdx, gdz, asgr, sgdl, sgs, fom, ttime, tfield, precision, nullptr, nullptr, nullptr,
+                       nullptr);
+}
+
+int mct_modrays_group_batch(int nmaps, int nsrc, const double *scx, const double *scz, int nrc,
+                            const double *rcx, const double *rcz, int srs_nmaps, const int *srs, int nvx,
+                            int nvz, double goxd, double gozd, double dvxd, double dvzd,
+                            const double *velv, const double *gvel, int gdx, int gdz, int asgr, int sgdl,
+                            int sgs, int fom, double *ttime, double *gtime, double *raylen, int *crazy,
+                            int precision) {
+  if (!gvel || !gtime || !raylen || !crazy) return arg_error("mct_modrays_group_batch: null output");
+  return modrays_batch(nmaps, nsrc, scx, scz, nrc, rcx, rcz, srs_nmaps, srs, nvx, nvz, goxd, gozd, dvxd, dvzd,
+                       velv, gdx, gdz, asgr, sgdl, sgs, fom, ttime, nullptr, precision, gvel, gtime, raylen, crazy);
 }
 
 int mct_modrays(int nsrc, const double *scx, const double *scz, int nrc, const double *rcx,

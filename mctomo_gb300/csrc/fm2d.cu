@@ -746,6 +746,28 @@ __device__ double refined_velocity(const Fm2dJob &job, const RefineBox &rb, int 
   return sum[0] + sum[1] + sum[2] + sum[3];
 }
 
+// GetVelocity (src/likelihood_surf.F90:496-521): bilinear velocity of one
+// map of the model grid (Fortran (nvz, nvx)) at (px, pz).
+__device__ double get_velocity(const double *vel, int nx, int nz, double gox, double goz, double dx, double dz,
+                               double px, double pz) {
+  int ix = (int)floor((px - gox) / dx) + 1;
+  int iy = (int)floor((pz - goz) / dz) + 1;
+  if (ix < 1) ix = 1;
+  if (iy < 1) iy = 1;
+  if (ix >= nx) ix = nx - 1;
+  if (iy >= nz) iy = nz - 1;
+  const double dsx = px - (gox + (double)(ix - 1) * dx);
+  const double dsy = pz - (goz + (double)(iy - 1) * dz);
+  double qv = 0;
+  for (int i = 1; i <= 2; ++i)
+    for (int j = 1; j <= 2; ++j) {
+      const double weight = (1.0 - fabs((double)(i - 1) * dx - dsx) / dx) *
+                            (1.0 - fabs((double)(j - 1) * dz - dsy) / dz);
+      qv = qv + weight * vel[(size_t)(ix + i - 2) * nz + (iy + j - 2)];
+    }
+  return qv;
+}
+
 // Per-solve geometry shared by the two kernels (modrays' source cell and
 // refined box, fm2dray_cartesian.f90:283-330).
 struct SolveGeom {
@@ -861,6 +883,161 @@ fm2d_refined_kernel(Fm2dJob job, int warp_bytes, int heap_cap, int redo) {
     int r = lin(gr, k, l);
     tmpT[q] = bit_store(w.T[r]);
     tmpS[q] = w.S[r];
+  }
+  if (job.rays) {
+    // the refined field and states for the ray tracer (far nodes hold
+    // uninitialised memory in the reference; 0 here)
+    double *rt = job.ref_t + (size_t)solve * job.nref_max;
+    short *rs = job.ref_s + (size_t)solve * job.nref_max;
+    for (int q = lane; q < nrnx * nrnz; q += 32) {
+      const short st = w.S[q];
+      rs[q] = st;
+      rt[q] = st == -1 ? 0.0 : to_double(w.T[q], fx);
+    }
+  }
+}
+
+// FLOOR of a ray coordinate. Where the travel-time gradient vanishes the
+// reference's next point is NaN, and FLOOR(NaN) is -2^31 on the x86 targets
+// the reference is built for, which the boundary clamp then moves to the
+// lower grid edge; that is made explicit here.
+__device__ __forceinline__ int floor_idx(double v) { return isnan(v) ? INT_MIN : (int)floor(v); }
+
+// rpaths (fm2d/fm2dray_cartesian.f90:801-1455, without Frechet derivatives)
+// followed by CalGroupTime (src/likelihood_surf.F90:455-494) and the ray
+// length (T_RAY%length), one receiver per lane: steepest descent from the
+// receiver on the final coarse field (shared memory) or, inside the refined
+// box where the four corners of the current cell were accepted, on the
+// refined field; the group delay sums each segment's length over the mean of
+// the end points' velocities as the ray is traced. A ray that reaches the
+// point limit counts as crazy (its delay and length stay 0, as the reference
+// stores a one-point ray).
+template <class TT>
+__device__ void trace_rays(const Fm2dJob &job, const WarpStateT<TT> &w, const Fx &fx, const SolveGeom &sg, int solve,
+                           int lane) {
+  const int map = sg.map, src = sg.src;
+  const Grid2 &gc = sg.gc;
+  const int nnx = gc.nnx, nnz = gc.nnz;
+  const double gox = gc.gox, goz = gc.goz, dnx = gc.dnx, dnz = gc.dnz;
+  const int asgr = job.asgr, sgdl = job.sgdl;
+  int nnxr = 0, nnzr = 0;
+  double goxr = 0, gozr = 0, dnxr = 1, dnzr = 1;
+  const double *TR = nullptr;
+  const short *SR = nullptr;
+  if (asgr == 1) {
+    nnxr = (sg.vnr - sg.vnl) * sgdl + 1; nnzr = (sg.vnb - sg.vnt) * sgdl + 1;
+    goxr = gox + dnx * (double)(sg.vnl - 1); gozr = goz + dnz * (double)(sg.vnt - 1);
+    dnxr = job.dvxd / (double)(job.gdx * sgdl); dnzr = job.dvzd / (double)(job.gdz * sgdl);
+    TR = job.ref_t + (size_t)solve * job.nref_max;
+    SR = job.ref_s + (size_t)solve * job.nref_max;
+  }
+  auto T = [&](int iz, int ix) { return to_double(w.T[(iz - 1) + nnz * (ix - 1)], fx); };
+  auto tr = [&](int iz, int ix) { return TR[(size_t)(iz - 1) + (size_t)nnzr * (ix - 1)]; };
+  auto srf = [&](int iz, int ix) { return SR[(size_t)(iz - 1) + (size_t)nnzr * (ix - 1)]; };
+  const double scx = sg.x, scz = sg.z;
+  const double *gv = job.gvel + (size_t)map * job.nvx * job.nvz;
+  const int maxrp = nnx * nnz;
+  int isx, isz;
+  if (asgr == 1) { isx = floor_idx((scx - goxr) / dnxr) + 1; isz = floor_idx((scz - gozr) / dnzr) + 1; }
+  else { isx = floor_idx((scx - gox) / dnx) + 1; isz = floor_idx((scz - goz) / dnz) + 1; }
+  double dpl = dnx, rd1 = dnz;
+  if (rd1 < dpl) dpl = rd1;
+  dpl = 0.5 * dpl;
+  const int *srs = job.srs + (size_t)(map % job.srs_nmaps) * job.nsrc * job.nrc + (size_t)src * job.nrc;
+  const size_t o0 = ((size_t)map * job.nsrc + src) * job.nrc;
+  for (int r = lane; r < job.nrc; r += 32) {
+    if (srs[r] == 0) continue;
+    const double rcx = job.rcx[r], rcz = job.rcz[r];
+    int ipx = floor_idx((rcx - gox) / dnx) + 1;
+    int ipz = floor_idx((rcz - goz) / dnz) + 1;
+    if (ipx < 1 || ipx >= nnx || ipz < 1 || ipz >= nnz) { atomicExch(job.status, MCT_ERR_OUTSIDE); continue; }
+    // the delay and length accumulate over the ray's points as they are made
+    double px = rcx, pz = rcz;
+    double vhead = get_velocity(gv, job.nvx, job.nvz, job.goxd, job.gozd, job.dvxd, job.dvzd, px, pz);
+    double gt = 0, len = 0;
+    auto add_point = [&](double qx, double qz) {
+      double dist = (qx - px) * (qx - px) + (qz - pz) * (qz - pz);
+      dist = sqrt(dist);
+      const double vtail = get_velocity(gv, job.nvx, job.nvz, job.goxd, job.gozd, job.dvxd, job.dvzd, qx, qz);
+      gt = gt + dist * 2 / (vhead + vtail);
+      len = len + dist;
+      vhead = vtail;
+      px = qx; pz = qz;
+    };
+    int sw = 0;
+    double sred = (scx - rcx) * (scx - rcx);
+    sred = sred + (scz - rcz) * (scz - rcz);
+    sred = sqrt(sred);
+    if (sred < 2.0 * dpl) { add_point(scx, scz); sw = 1; }
+    int ipxr = 0, ipzr = 0, igref = 0;
+    auto in_refined = [&](double qx, double qz) {
+      ipxr = floor_idx((qx - goxr) / dnxr) + 1;
+      ipzr = floor_idx((qz - gozr) / dnzr) + 1;
+      int g = 1;
+      if (ipxr < 1 || ipxr >= nnxr) g = 0;
+      if (ipzr < 1 || ipzr >= nnzr) g = 0;
+      if (g == 1) {
+        if (srf(ipzr, ipxr) != 0 || srf(ipzr + 1, ipxr) != 0) g = 0;
+        if (srf(ipzr, ipxr + 1) != 0 || srf(ipzr + 1, ipxr + 1) != 0) g = 0;
+      }
+      return g;
+    };
+    if (asgr == 1) igref = in_refined(rcx, rcz);
+    if (sw == 0) {
+      if (asgr == 1) {
+        if (igref == 1 && ipxr == isx && ipzr == isz) { add_point(scx, scz); sw = 1; }
+      } else {
+        if (ipx == isx && ipz == isz) { add_point(scx, scz); sw = 1; }
+      }
+    }
+    int crazy = 0;
+    for (int j = 1; j <= maxrp; ++j) {
+      if (sw == 1) break;
+      double dtx, dtz;
+      if (igref == 1) {
+        if (ipxr == 1) dtx = (tr(ipzr, ipxr + 1) - tr(ipzr, ipxr)) / dnxr;
+        else if (ipxr == nnxr) dtx = (tr(ipzr, ipxr) - tr(ipzr, ipxr - 1)) / dnxr;
+        else dtx = (tr(ipzr, ipxr + 1) - tr(ipzr, ipxr - 1)) / (2.0 * dnxr);
+        if (ipzr == 1) dtz = (tr(ipzr + 1, ipxr) - tr(ipzr, ipxr)) / dnzr;
+        else if (ipzr == nnzr) dtz = (tr(ipzr, ipxr) - tr(ipzr - 1, ipxr)) / dnzr;
+        else dtz = (tr(ipzr + 1, ipxr) - tr(ipzr - 1, ipxr)) / (2.0 * dnzr);
+      } else {
+        if (ipx == 1) dtx = (T(ipz, ipx + 1) - T(ipz, ipx)) / dnx;
+        else if (ipx == nnx) dtx = (T(ipz, ipx) - T(ipz, ipx - 1)) / dnx;
+        else dtx = (T(ipz, ipx + 1) - T(ipz, ipx - 1)) / (2.0 * dnx);
+        // the reference tests the refined index here (ipzr == nnzr); without
+        // refinement that is an unset local, and the intended coarse test
+        // (ipz == nnz) is used
+        if (ipz == 1) dtz = (T(ipz + 1, ipx) - T(ipz, ipx)) / dnz;
+        else if (asgr == 1 ? ipzr == nnzr : ipz == nnz) dtz = (T(ipz, ipx) - T(ipz - 1, ipx)) / dnz;
+        else dtz = (T(ipz + 1, ipx) - T(ipz - 1, ipx)) / (2.0 * dnz);
+      }
+      rd1 = sqrt(dtx * dtx + dtz * dtz);
+      double nx = px - dpl * dtx / rd1;
+      double nz = pz - dpl * dtz / rd1;
+      if (asgr == 1) igref = in_refined(nx, nz);
+      else igref = 0;
+      ipx = floor_idx((nx - gox) / dnx) + 1;
+      ipz = floor_idx((nz - goz) / dnz) + 1;
+      sred = (scx - nx) * (scx - nx);
+      sred = sred + (scz - nz) * (scz - nz);
+      sred = sqrt(sred);
+      if (sred < 2.0 * dpl) { add_point(nx, nz); add_point(scx, scz); sw = 1; break; }
+      if (asgr == 1) {
+        if (igref == 1 && ipxr == isx && ipzr == isz) { add_point(nx, nz); add_point(scx, scz); sw = 1; break; }
+      } else {
+        if (ipx == isx && ipz == isz) { add_point(nx, nz); add_point(scx, scz); sw = 1; break; }
+      }
+      if (ipx < 1) { nx = gox; ipx = 1; }
+      if (ipx >= nnx) { nx = gox + (double)(nnx - 1) * dnx; ipx = nnx - 1; }
+      if (ipz < 1) { nz = goz; ipz = 1; }
+      if (ipz >= nnz) { nz = goz + (double)(nnz - 1) * dnz; ipz = nnz - 1; }
+      if (j == maxrp - 1) { crazy = 1; break; }
+      add_point(nx, nz);
+    }
+    if (crazy) { gt = 0; len = 0; atomicAdd(&job.crazy[map], 1); }
+    job.gtime[o0 + r] = gt;
+    job.raylen[o0 + r] = len;
   }
 }
 
@@ -990,6 +1167,7 @@ fm2d_coarse_kernel(Fm2dJob job, int warp_bytes) {
     }
     tt[r] = trr;
   }
+  if (job.rays) trace_rays(job, w, fx, sg, solve, lane);
 }
 
 }  // namespace

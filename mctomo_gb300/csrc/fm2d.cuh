@@ -17,6 +17,13 @@ struct Fm2dJob {
   short *map_tmp_s;          // [nsolve][map_tmp_max] scratch
   int *ovf_list;             // [nsolve] scratch: solves whose refined-box heap overflowed
   int *ovf_count;            // [1] scratch: their number
+  // ray paths and group delays (modrays with uar = 0, then CalGroupTime)
+  int rays;                  // 1: trace a ray for every path
+  const double *gvel;        // [nmaps][nvx][nvz] velocity for the delay along the ray (model grid)
+  double *gtime, *raylen;    // [nmaps][nsrc][nrc] group time and ray length
+  int *crazy;                // [nmaps] rays that reached the point limit
+  double *ref_t;             // [nsolve][nref_max] scratch: refined-box times after the refined march
+  short *ref_s;              // [nsolve][nref_max] scratch: their states
   int nsrc, nrc;
   const double *scx, *scz, *rcx, *rcz;
   const int *srs;            // [srs_nmaps][nsrc][nrc] path flags

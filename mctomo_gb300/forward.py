@@ -153,6 +153,28 @@ def modrays_batch(src, rev, srs, nvx, nvz, goxd, gozd, dvxd, dvzd, velv, gdx=1, 
     return ttime
 
 
+def modrays_group_batch(src, rev, srs, nvx, nvz, goxd, gozd, dvxd, dvzd, velv, gvel, gdx=1, gdz=1, asgr=1,
+                        sgdl=4, sgs=8, fom=1, precision=0):
+    """modrays with ray paths (uar = 0) and CalGroupTime on gvel (nmaps, nvx,
+    nvz). Returns (phase times, group times, ray lengths), each (nmaps, nsrc,
+    nrc), and the crazy-ray count per map."""
+    src = _f64(src); rev = _f64(rev); velv = _f64(velv); gvel = _f64(gvel)
+    srs = np.ascontiguousarray(srs, np.int32)
+    if srs.ndim == 2:
+        srs = srs[None]
+    nmaps = velv.shape[0]
+    nsrc, nrc = src.shape[0], rev.shape[0]
+    tt = np.zeros((nmaps, nsrc, nrc)); gt = np.zeros_like(tt); ln = np.zeros_like(tt)
+    crazy = np.zeros(nmaps, np.int32)
+    sx, sz = np.ascontiguousarray(src[:, 0]), np.ascontiguousarray(src[:, 1])
+    rx, rz = np.ascontiguousarray(rev[:, 0]), np.ascontiguousarray(rev[:, 1])
+    rc = lib().mct_modrays_group_batch(nmaps, nsrc, ptr(sx), ptr(sz), nrc, ptr(rx), ptr(rz), srs.shape[0],
+                                       ptr(srs), nvx, nvz, goxd, gozd, dvxd, dvzd, ptr(velv), ptr(gvel), gdx, gdz,
+                                       asgr, sgdl, sgs, fom, ptr(tt), ptr(gt), ptr(ln), ptr(crazy), int(precision))
+    check("mct_modrays_group_batch", rc)
+    return tt, gt, ln, crazy
+
+
 def fast_marching3d(vel, h, lo, src, rev, order=1, tfield=False):
     """fastMarching3D (fastmarching/fastMarching.cpp:26-129). vel: (nx, ny, nz)
     C order; h = (dx, dy, dz); lo = (xmin, ymin, zmin); src (3,); rev (nrev, 3).

@@ -12,6 +12,7 @@
 //
 // Ray path tracing (rpaths, fm2dray_cartesian.f90:801-1455) is not restated
 // here: it only runs for group-velocity data (uar == 0).
+#include <climits>
 #include <cmath>
 #include <vector>
 #include <cstdlib>
@@ -399,6 +400,12 @@ void group_time(const std::vector<double> &rx, const std::vector<double> &rz, co
   }
 }
 
+// FLOOR of a ray coordinate. Where the travel-time gradient vanishes the
+// reference's next point is NaN, and FLOOR(NaN) is -2^31 on the x86 targets
+// the reference is built for, which the boundary clamp then moves to the
+// lower grid edge; that is made explicit here.
+int floor_idx(double v) { return std::isnan(v) ? INT_MIN : (int)std::floor(v); }
+
 // rpaths (fm2d/fm2dray_cartesian.f90:801-1455) without Frechet derivatives,
 // one receiver: steepest descent on the final coarse field ttn (nnz, nnx),
 // or on the refined-box field ttnr / states nstsr where the ray is inside the
@@ -414,14 +421,14 @@ int trace_ray(double rcx, double rcz, double scx, double scz, const G2 &c, const
   const double goxr = r.gox, gozr = r.goz, dnxr = r.dx, dnzr = r.dz;
   const int maxrp = nnx * nnz;
   int isx, isz;
-  if (asgr == 1) { isx = (int)std::floor((scx - goxr) / dnxr) + 1; isz = (int)std::floor((scz - gozr) / dnzr) + 1; }
-  else { isx = (int)std::floor((scx - gox) / dnx) + 1; isz = (int)std::floor((scz - goz) / dnz) + 1; }
+  if (asgr == 1) { isx = floor_idx((scx - goxr) / dnxr) + 1; isz = floor_idx((scz - gozr) / dnzr) + 1; }
+  else { isx = floor_idx((scx - gox) / dnx) + 1; isz = floor_idx((scz - goz) / dnz) + 1; }
   double dpl = dnx, rd1 = dnz;
   if (rd1 < dpl) dpl = rd1;
   dpl = 0.5 * dpl;
   rx.assign(1, rcx); rz.assign(1, rcz);
-  int ipx = (int)std::floor((rcx - gox) / dnx) + 1;
-  int ipz = (int)std::floor((rcz - goz) / dnz) + 1;
+  int ipx = floor_idx((rcx - gox) / dnx) + 1;
+  int ipz = floor_idx((rcz - goz) / dnz) + 1;
   int sw = 0;
   if (ipx < 1 || ipx >= nnx) sw = 1;
   if (ipz < 1 || ipz >= nnz) sw = 1;
@@ -435,8 +442,8 @@ int trace_ray(double rcx, double rcz, double scx, double scz, const G2 &c, const
   if (sred < 2.0 * dpl) { rx.push_back(scx); rz.push_back(scz); nrp = 2; sw = 1; }
   int ipxr = 0, ipzr = 0, igref = 0;
   auto in_refined = [&](double px, double pz) {
-    ipxr = (int)std::floor((px - goxr) / dnxr) + 1;
-    ipzr = (int)std::floor((pz - gozr) / dnzr) + 1;
+    ipxr = floor_idx((px - goxr) / dnxr) + 1;
+    ipzr = floor_idx((pz - gozr) / dnzr) + 1;
     int g = 1;
     if (ipxr < 1 || ipxr >= nnxr) g = 0;
     if (ipzr < 1 || ipzr >= nnzr) g = 0;
@@ -483,11 +490,11 @@ int trace_ray(double rcx, double rcz, double scx, double scz, const G2 &c, const
     rx.push_back(nx); rz.push_back(nz);
     if (asgr == 1) {
       igref = in_refined(nx, nz);
-      ipx = (int)std::floor((nx - gox) / dnx) + 1;
-      ipz = (int)std::floor((nz - goz) / dnz) + 1;
+      ipx = floor_idx((nx - gox) / dnx) + 1;
+      ipz = floor_idx((nz - goz) / dnz) + 1;
     } else {
-      ipx = (int)std::floor((nx - gox) / dnx) + 1;
-      ipz = (int)std::floor((nz - goz) / dnz) + 1;
+      ipx = floor_idx((nx - gox) / dnx) + 1;
+      ipz = floor_idx((nz - goz) / dnz) + 1;
       igref = 0;
     }
     sred = (scx - nx) * (scx - nx);
