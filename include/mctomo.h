@@ -199,14 +199,19 @@ typedef struct {
 
 typedef struct {
   int raylov;          /* 1 Rayleigh, 0 Love (T_LIKE_SET%raylov) */
-  int phase_group;     /* 0 phase velocity (1 needs ray paths: unsupported) */
+  int phase_group;     /* 0 phase velocity; 1 group velocity: times along the
+                          rays of the phase field (rpaths + CalGroupTime),
+                          sigma uses the ray length */
   double dphase;       /* dPhaseVel */
   int gridx, gridy, sgref, sgdic, sgext, order;   /* fm2d settings */
-  int sigdep;          /* 0 data sigma, else sigma = n0*time + n1 */
+  int sigdep;          /* 0 data sigma, else sigma = n0*srdist + n1 (srdist:
+                          phase time, ray length for phase_group 1,
+                          source-receiver distance for straight rays) */
   int material_law;    /* MCT_LAW_* */
   double rho_value;
   int precision;       /* dispersion root search: 0 FP64, 1 FP32 bracketing */
-  int tt_precision;    /* fm2d updates: 0 FP64, 1 FP32 quadratic, 2 FP32 + fixed-point times */
+  int tt_precision;    /* fm2d updates: 0 FP64, 1 double-float, 2 FP32 + fixed-point times */
+  int straight;        /* isStraight: 1 = straight rays, no fast marching */
 } mct_surf_settings;
 
 typedef struct {
@@ -233,7 +238,7 @@ int mct_surf_destroy(mct_surf_ctx *ctx);
  * (vp, vs, rho); n0 / n1: [nchains][np] noise hyper-parameters. out:
  * [nchains][4] = like (-log L, DBL_MAX when the model is rejected), misfit,
  * unweighted misfit, status (0 valid; bit 1 check_model, bit 2 dispersion
- * failure, bit 8 zero sigma). Host pointers, synchronous. */
+ * failure, bit 4 crazy ray, bit 8 zero sigma). Host pointers, synchronous. */
 int mct_surf_forward(mct_surf_ctx *ctx, int nchains, const int *slots,
                      const int *ncells, const double *points,
                      const double *params, const double *n0,

@@ -2,6 +2,7 @@
 // around surf_forward / surf_commit (surf_pipeline.cu).
 #include "mct_common.cuh"
 #include "surf_pipeline.cuh"
+#include <cmath>
 #include <vector>
 #include <cstring>
 #include <string>
@@ -38,7 +39,21 @@ int surf_create(const mct_grid *g, const mct_surf_settings *st, const mct_surf_d
   if (!g || !st || !dat || (!out && !dry) || nslots < 1 || ncell_max < 1 || ncell_max > 12800) return MCT_ERR_ARG;
   if (g->nx < 2 || g->ny < 2 || g->nz < 1 || !(g->dx > 0) || !(g->dy > 0) || !(g->dz > 0) || !(g->scaling > 0))
     return MCT_ERR_ARG;
-  if (st->phase_group != 0) return MCT_ERR_UNSUPPORTED;   // group velocity needs ray paths
+  if (st->phase_group != 0 && st->phase_group != 1) return MCT_ERR_ARG;
+  if (st->straight != 0 && st->straight != 1) return MCT_ERR_ARG;
+  if (st->straight == 1) {
+    // straight rays must stay inside the model (the reference's fatal
+    // 'Straight ray out of area'); the model is a rectangle, so its stations must
+    const double xmax = g->xmin + (double)(g->nx - 1) * g->dx, ymax = g->ymin + (double)(g->ny - 1) * g->dy;
+    for (int i = 0; i < dat->nsrc; ++i)
+      if (dat->src[2 * i] < g->xmin || dat->src[2 * i] > xmax || dat->src[2 * i + 1] < g->ymin ||
+          dat->src[2 * i + 1] > ymax)
+        return MCT_ERR_OUTSIDE;
+    for (int i = 0; i < dat->nrev; ++i)
+      if (dat->rev[2 * i] < g->xmin || dat->rev[2 * i] > xmax || dat->rev[2 * i + 1] < g->ymin ||
+          dat->rev[2 * i + 1] > ymax)
+        return MCT_ERR_OUTSIDE;
+  }
   if (st->raylov != 0 && st->raylov != 1) return MCT_ERR_ARG;
   if (dat->np < 1 || dat->np > 60 || dat->nsrc < 1 || dat->nrev < 1) return MCT_ERR_ARG;
   if (!(st->dphase != 0.0)) return MCT_ERR_ARG;
@@ -51,6 +66,7 @@ int surf_create(const mct_grid *g, const mct_surf_settings *st, const mct_surf_d
   b.law = st->material_law; b.rho_value = st->rho_value;
   b.iwave = st->raylov == 1 ? 2 : 1; b.precision = st->precision; b.dphase = st->dphase;
   b.sigdep = st->sigdep;
+  b.igr = st->phase_group; b.straight = st->straight;
   b.np = dat->np; b.nsrc = dat->nsrc; b.nrev = dat->nrev; b.nrays = dat->nrays;
   b.ncell_max = ncell_max;
   b.nl_max = g->nz + 1;
@@ -105,7 +121,14 @@ int surf_create(const mct_grid *g, const mct_surf_settings *st, const mct_surf_d
       sizeof(double) * (size_t)nslots * np * npairs,
       // staging
       sizeof(int) * nslots * 3, sizeof(double) * (size_t)nslots * ncell_max * 6, sizeof(double) * 2 * nslots * np,
-      sizeof(double) * 4 * nslots, sizeof(int)};
+      sizeof(double) * 4 * nslots, sizeof(int),
+      // group velocities, rays and straight rays
+      sizeof(double) * (size_t)nslots * maps * (b.igr ? 2 : 0),
+      sizeof(double) * 2 * (size_t)nslots * np * npairs * ((b.igr || b.straight) ? 1 : 0),
+      sizeof(int) * (size_t)nslots * np, sizeof(double) * (size_t)npairs, sizeof(double) * 2 * (nsrc + nrev),
+      sizeof(double) * (size_t)nslots * np * npairs,
+      (b.igr && !b.straight) ? sizeof(double) * (size_t)fp.nref_max * nsolve : 0,
+      (b.igr && !b.straight) ? sizeof(short) * (size_t)fp.nref_max * nsolve : 0};
   size_t total = 0;
   for (size_t s : sz) total = ((total + 255) & ~size_t(255)) + s;
   total += 256;
@@ -177,6 +200,31 @@ int surf_create(const mct_grid *g, const mct_surf_settings *st, const mct_surf_d
   c->d_n1 = c->d_n0 + (size_t)nslots * np;
   c->d_out = cv.take<double>((size_t)4 * nslots);
   fj.vmin_bits = cv.take<int>(1);
+  b.gvel = cv.take<double>((size_t)nslots * maps * (b.igr ? 1 : 0));
+  b.cgvel = cv.take<double>((size_t)nslots * maps * (b.igr ? 1 : 0));
+  b.gtime = cv.take<double>((size_t)nslots * np * npairs * ((b.igr || b.straight) ? 1 : 0));
+  b.raylen = cv.take<double>((size_t)nslots * np * npairs * ((b.igr || b.straight) ? 1 : 0));
+  b.crazy = cv.take<int>((size_t)nslots * np);
+  double *sdist = cv.take<double>((size_t)npairs);
+  double *sxy = cv.take<double>(2 * (size_t)(nsrc + nrev));
+  b.csrd = cv.take<double>((size_t)nslots * np * npairs);
+  fj.ref_t = cv.take<double>((b.igr && !b.straight) ? (size_t)fp.nref_max * nsolve : 0);
+  fj.ref_s = cv.take<short>((b.igr && !b.straight) ? (size_t)fp.nref_max * nsolve : 0);
+  b.sdist = sdist;
+  c->plan.src_xy = sxy; c->plan.rev_xy = sxy + 2 * nsrc;
+  {
+    // setup_straightRays distances (likelihood_surf.F90:430-433) and the
+    // stations as [n][2]
+    std::vector<double> hd((size_t)npairs);
+    for (int j = 0; j < nsrc; ++j)
+      for (int k = 0; k < nrev; ++k) {
+        const double ddx = dat->rev[2 * k] - dat->src[2 * j], ddy = dat->rev[2 * k + 1] - dat->src[2 * j + 1];
+        hd[(size_t)j * nrev + k] = std::sqrt(ddx * ddx + ddy * ddy);
+      }
+    cudaMemcpy(sdist, hd.data(), sizeof(double) * npairs, cudaMemcpyHostToDevice);
+    cudaMemcpy(sxy, dat->src, sizeof(double) * 2 * nsrc, cudaMemcpyHostToDevice);
+    cudaMemcpy(sxy + 2 * nsrc, dat->rev, sizeof(double) * 2 * nrev, cudaMemcpyHostToDevice);
+  }
   // static data
   std::vector<double> hper(np);
   for (int p = 0; p < np; ++p) hper[p] = 1.0 / dat->freqs[p];   // dble(1/freqs), surfmodes.f90:82
@@ -197,6 +245,7 @@ int surf_create(const mct_grid *g, const mct_surf_settings *st, const mct_surf_d
   cudaMemset(b.committed, 0, sizeof(int) * nslots);
   cudaMemset(b.ttime, 0, sizeof(double) * (size_t)nslots * np * npairs);
   cudaMemset(b.cttime, 0, sizeof(double) * (size_t)nslots * np * npairs);
+  cudaMemset(b.csrd, 0, sizeof(double) * (size_t)nslots * np * npairs);
   if (cudaGetLastError() != cudaSuccess || cudaDeviceSynchronize() != cudaSuccess) {
     cudaFree(c->mem); cudaStreamDestroy(c->stream); delete c; return MCT_ERR_CUDA;
   }
@@ -401,8 +450,11 @@ int mct_surf_phase_time(mct_surf_ctx *c, int index, double *phase_time, double *
   const SurfBatch &b = c->b;
   const size_t npairs = (size_t)b.nsrc * b.nrev;
   MCT_CUDA_TRY(cudaStreamSynchronize(c->stream));
+  // the likelihood's phaseTime: group times along the rays (or straight
+  // rays) when those are used, otherwise the phase times
+  const double *lt = (b.igr || b.straight) ? b.gtime : b.ttime;
   if (phase_time)
-    MCT_CUDA_TRY(cudaMemcpy(phase_time, b.ttime + (size_t)index * b.np * npairs, sizeof(double) * b.np * npairs,
+    MCT_CUDA_TRY(cudaMemcpy(phase_time, lt + (size_t)index * b.np * npairs, sizeof(double) * b.np * npairs,
                             cudaMemcpyDeviceToHost));
   if (phase_vel)
     MCT_CUDA_TRY(cudaMemcpy(phase_vel, b.pvel + (size_t)index * b.np * b.nx * b.ny,

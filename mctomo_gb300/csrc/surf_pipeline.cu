@@ -113,6 +113,9 @@ __global__ void scatter_kernel(SurfBatch b) {
   if (b.lierr[q]) atomicOr(&b.status[e.x], 2);
   for (int p = 0; p < b.np; ++p)
     b.pvel[((size_t)e.x * b.np + p) * ncol + e.y] = b.lcp[(size_t)q * b.np + p];
+  if (b.igr)
+    for (int p = 0; p < b.np; ++p)
+      b.gvel[((size_t)e.x * b.np + p) * ncol + e.y] = b.lcg[(size_t)q * b.np + p];
 }
 
 // Padded fm2d vertex grids (likelihood_surf.F90:259-264): interior = phase
@@ -131,16 +134,29 @@ __global__ void pad_kernel(SurfBatch b) {
 
 // sigma and the misfit / -log L (likelihood_surf.F90:356-404), one block per
 // chain, FP64 block reduction.
+// The likelihood's phaseTime and srdist by mode (likelihood_surf.F90:233-329):
+// phase times and srdist = phase time; group times along the rays and
+// srdist = ray length; straight-ray times and srdist = the distance.
+__device__ __forceinline__ const double *like_times(const SurfBatch &b) {
+  return (b.igr || b.straight) ? b.gtime : b.ttime;
+}
+__device__ __forceinline__ double like_srdist(const SurfBatch &b, size_t q, int r) {
+  return b.straight ? b.sdist[r] : (b.igr ? b.raylen[q] : b.ttime[q]);
+}
+
 __global__ void misfit_kernel(SurfBatch b) {
   const int c = blockIdx.x;
   const int npairs = b.nsrc * b.nrev;
-  const double *pt = b.ttime + (size_t)c * b.np * npairs;   // [p][src][rev] = phaseTime(k,j,p)
+  const double *pt = like_times(b) + (size_t)c * b.np * npairs;   // [p][src][rev] = phaseTime(k,j,p)
+  if (b.igr && !b.straight && threadIdx.x < b.np && b.crazy[(size_t)c * b.np + threadIdx.x] > 0)
+    atomicOr(&b.status[c], 4);     // crazyray: like = huge
   double like = 0, mis = 0, umis = 0, slog = 0;
   for (int q = threadIdx.x; q < b.np * npairs; q += blockDim.x) {
     int p = q / npairs, r = q % npairs;
     double sig;
     bool used = b.raystat[(size_t)p * npairs + r] == 1;
-    if (b.sigdep != 0) sig = used ? b.n0[(size_t)c * b.np + p] * pt[q] + b.n1[(size_t)c * b.np + p] : 1.0;
+    const double srd = like_srdist(b, (size_t)c * b.np * npairs + q, r);
+    if (b.sigdep != 0) sig = used ? b.n0[(size_t)c * b.np + p] * srd + b.n1[(size_t)c * b.np + p] : 1.0;
     else sig = used ? b.dsigma[(size_t)p * npairs + r] : 1.0;
     if (used) {
       if (sig < 1.0E-10) atomicOr(&b.status[c], 8);
@@ -185,15 +201,23 @@ __global__ void commit_kernel(SurfBatch b, const int *accept) {
   }
   for (size_t q = blockIdx.x * blockDim.x + threadIdx.x; q < maps; q += (size_t)gridDim.x * blockDim.x)
     b.cpvel[(size_t)slot * maps + q] = b.pvel[(size_t)c * maps + q];
+  if (b.igr)
+    for (size_t q = blockIdx.x * blockDim.x + threadIdx.x; q < maps; q += (size_t)gridDim.x * blockDim.x)
+      b.cgvel[(size_t)slot * maps + q] = b.gvel[(size_t)c * maps + q];
   const size_t nt = (size_t)b.np * b.nsrc * b.nrev;
-  for (size_t q = blockIdx.x * blockDim.x + threadIdx.x; q < nt; q += (size_t)gridDim.x * blockDim.x)
-    b.cttime[(size_t)slot * nt + q] = b.ttime[(size_t)c * nt + q];
+  const int npairs = b.nsrc * b.nrev;
+  const double *lt = like_times(b);
+  for (size_t q = blockIdx.x * blockDim.x + threadIdx.x; q < nt; q += (size_t)gridDim.x * blockDim.x) {
+    b.cttime[(size_t)slot * nt + q] = lt[(size_t)c * nt + q];
+    b.csrd[(size_t)slot * nt + q] = like_srdist(b, (size_t)c * nt + q, (int)(q % npairs));
+  }
   if (blockIdx.x == 0 && threadIdx.x == 0) b.committed[slot] = 1;
 }
 
 // surf_noise_likelihood (src/likelihood_surf.F90:56-99): the committed phase
 // times re-reduced with new noise parameters, sigma = n0 * srdist + n1 with
-// srdist the phase time, for every pair; unused pairs count with sigma = 1.
+// the committed srdist (phase time, ray length or distance by mode), for
+// every pair; unused pairs count with sigma = 1.
 // A sigma below 1e-10 is the reference's fatal 'noise level is 0' (status 8).
 __global__ void noise_kernel(SurfBatch b, const int *slots, const double *n0, const double *n1, double *out) {
   const int c = blockIdx.x;
@@ -205,7 +229,8 @@ __global__ void noise_kernel(SurfBatch b, const int *slots, const double *n0, co
   for (int q = threadIdx.x; q < b.np * npairs; q += blockDim.x) {
     const int p = q / npairs, r = q % npairs;
     const bool used = b.raystat[(size_t)p * npairs + r] == 1;
-    double sig = n0[(size_t)c * b.np + p] * pt[q] + n1[(size_t)c * b.np + p];
+    const double srd = b.csrd[(size_t)slot * b.np * npairs + q];
+    double sig = n0[(size_t)c * b.np + p] * srd + n1[(size_t)c * b.np + p];
     if (used) {
       if (sig == 0.0) bad = 1;
       const double res = pt[q] - b.dtime[(size_t)p * npairs + r];
@@ -248,6 +273,72 @@ __global__ void gather_committed_maps(SurfBatch b) {
   const size_t maps = (size_t)b.np * b.nx * b.ny;
   for (size_t q = blockIdx.x * blockDim.x + threadIdx.x; q < maps; q += (size_t)gridDim.x * blockDim.x)
     b.pvel[(size_t)c * maps + q] = b.committed[slot] ? b.cpvel[(size_t)slot * maps + q] : 0.0;
+  if (b.igr)
+    for (size_t q = blockIdx.x * blockDim.x + threadIdx.x; q < maps; q += (size_t)gridDim.x * blockDim.x)
+      b.gvel[(size_t)c * maps + q] = b.committed[slot] ? b.cgvel[(size_t)slot * maps + q] : 0.0;
+}
+
+// setup_straightRays + CalGroupTime (likelihood_surf.F90:412-494), one thread
+// per (chain, period, path): points every min(dx, dy)/2 from the source, the
+// receiver last, delay on the group maps (phase maps for phaseGroup = 0).
+__device__ double grid_velocity(const SurfBatch &b, const double *vel, double px, double py) {
+  int ix = (int)floor((px - b.xmin) / b.dx) + 1;
+  int iy = (int)floor((py - b.ymin) / b.dy) + 1;
+  if (ix < 1) ix = 1;
+  if (iy < 1) iy = 1;
+  if (ix >= b.nx) ix = b.nx - 1;
+  if (iy >= b.ny) iy = b.ny - 1;
+  const double dsx = px - (b.xmin + (double)(ix - 1) * b.dx);
+  const double dsy = py - (b.ymin + (double)(iy - 1) * b.dy);
+  double qv = 0;
+  for (int i = 1; i <= 2; ++i)
+    for (int j = 1; j <= 2; ++j) {
+      const double weight = (1.0 - fabs((double)(i - 1) * b.dx - dsx) / b.dx) *
+                            (1.0 - fabs((double)(j - 1) * b.dy - dsy) / b.dy);
+      qv = qv + weight * vel[(size_t)(ix + i - 2) * b.ny + (iy + j - 2)];
+    }
+  return qv;
+}
+
+__global__ void straight_kernel(SurfBatch b, const double *src, const double *rev) {
+  const int npairs = b.nsrc * b.nrev;
+  const int map = blockIdx.y;                 // chain * np + period
+  const int p = map % b.np;
+  const int n = blockIdx.x * blockDim.x + threadIdx.x;
+  if (n >= npairs) return;
+  double *t = b.gtime + (size_t)map * npairs;
+  t[n] = 0;
+  if (b.raystat[(size_t)p * npairs + n] != 1) return;
+  const int j = n / b.nrev, k = n % b.nrev;
+  const double *vel = (b.igr ? b.gvel : b.pvel) + (size_t)map * b.nx * b.ny;
+  const double sx = src[2 * j], sy = src[2 * j + 1], rx = rev[2 * k], ry = rev[2 * k + 1];
+  const double ddx = rx - sx, ddy = ry - sy;
+  const double ds = sqrt(ddx * ddx + ddy * ddy);
+  const double dl = fmin(b.dx, b.dy) / 2;
+  const int npts = (int)floor(ds / dl) + 1;
+  const double xmax = b.xmin + (double)(b.nx - 1) * b.dx, ymax = b.ymin + (double)(b.ny - 1) * b.dy;
+  double px = sx, py = sy, vhead = 0, tt = 0;
+  for (int l = 1; l <= npts; ++l) {
+    double qx, qy;
+    if (l < npts) {
+      qx = sx + (double)(l - 1) * dl * ddx / ds;
+      qy = sy + (double)(l - 1) * dl * ddy / ds;
+      if (qx < b.xmin || qx > xmax || qy < b.ymin || qy > ymax) {   // 'Straight ray out of area'
+        atomicExch(&b.dev_status[0], MCT_ERR_OUTSIDE);
+        return;
+      }
+    } else {
+      qx = rx; qy = ry;
+    }
+    const double v = grid_velocity(b, vel, qx, qy);
+    if (l > 1) {
+      double dist = (qx - px) * (qx - px) + (qy - py) * (qy - py);
+      dist = sqrt(dist);
+      tt = tt + dist * 2 / (vhead + v);
+    }
+    vhead = v; px = qx; py = qy;
+  }
+  t[n] = tt;
 }
 
 }  // namespace
@@ -284,7 +375,7 @@ int surf_forward(SurfBatch &b, const SurfPlan &plan, cudaStream_t s, SurfProfile
   DispJob dj{};
   dj.ncol = maxlist; dj.ncol_dev = b.list_count; dj.nl_max = b.nl_max; dj.nl = b.lnl;
   dj.thk = b.lthk; dj.vp = b.lvp; dj.vs = b.lvs; dj.rho = b.lrho;
-  dj.np = b.np; dj.periods = b.periods; dj.iwave = b.iwave; dj.mode = 1; dj.igr = 0;
+  dj.np = b.np; dj.periods = b.periods; dj.iwave = b.iwave; dj.mode = 1; dj.igr = b.igr;
   dj.dphase = b.dphase; dj.multimode = 0; dj.precision = b.precision;
   dj.cp = b.lcp; dj.cg = b.lcg; dj.ierr = b.lierr; dj.ndltar = b.ndltar;
   rc = launch_surfdisp(dj, s); if (rc) return rc;
@@ -294,16 +385,26 @@ int surf_forward(SurfBatch &b, const SurfPlan &plan, cudaStream_t s, SurfProfile
   MCT_CUDA_TRY(cudaGetLastError());
   if (ev) MCT_CUDA_TRY(cudaEventRecord(ev[2], s));
   // 5: padded maps and fm2d
-  pad_kernel<<<dim3(8, nch * b.np), 256, 0, s>>>(b);
-  MCT_CUDA_TRY(cudaGetLastError());
-  Fm2dJob fj = plan.fm2d;
-  fj.nmaps = nch * b.np;
-  fj.velv = b.velv;
-  fj.nsolve = plan.nsolve_per_chain * nch;
-  fj.ttime = b.ttime;
-  fj.tfield = nullptr;
-  fj.status = b.dev_status;
-  rc = launch_fm2d(fj, plan.fm2d_plan, s); if (rc) return rc;
+  if (b.straight) {
+    const int npairs = b.nsrc * b.nrev;
+    straight_kernel<<<dim3((npairs + 127) / 128, nch * b.np), 128, 0, s>>>(b, plan.src_xy, plan.rev_xy);
+    MCT_CUDA_TRY(cudaGetLastError());
+  } else {
+    pad_kernel<<<dim3(8, nch * b.np), 256, 0, s>>>(b);
+    MCT_CUDA_TRY(cudaGetLastError());
+    Fm2dJob fj = plan.fm2d;
+    fj.nmaps = nch * b.np;
+    fj.velv = b.velv;
+    fj.nsolve = plan.nsolve_per_chain * nch;
+    fj.ttime = b.ttime;
+    fj.tfield = nullptr;
+    fj.status = b.dev_status;
+    if (b.igr) {
+      fj.rays = 1; fj.gvel = b.gvel; fj.gtime = b.gtime; fj.raylen = b.raylen; fj.crazy = b.crazy;
+      MCT_CUDA_TRY(cudaMemsetAsync(b.crazy, 0, sizeof(int) * (size_t)nch * b.np, s));
+    }
+    rc = launch_fm2d(fj, plan.fm2d_plan, s); if (rc) return rc;
+  }
   if (ev) MCT_CUDA_TRY(cudaEventRecord(ev[3], s));
   // 6: misfit
   misfit_kernel<<<nch, 256, 0, s>>>(b);

@@ -12,6 +12,8 @@ struct SurfBatch {
   int law; double rho_value;
   int iwave, precision; double dphase;
   int sigdep;
+  int igr;                   // 1: group velocities (phaseGroup = 1)
+  int straight;              // 1: straight rays (isStraight = 1), no fast marching
   int np, nsrc, nrev, nrays;
   const double *periods;     // [np]
   const int *raystat;        // [np][nsrc*nrev]
@@ -38,12 +40,18 @@ struct SurfBatch {
   unsigned long long *ndltar;
   double *pvel;              // [nchains][np][nx][ny]
   double *velv;              // [nchains*np][(nx+2)*(ny+2)]
-  double *ttime;             // [nchains*np][nsrc][nrev]
+  double *ttime;             // [nchains*np][nsrc][nrev] phase times (fm2d)
+  double *gvel;              // [nchains][np][nx][ny] group maps (igr)
+  double *gtime, *raylen;    // [nchains*np][nsrc][nrev] times along rays and ray lengths (igr or straight)
+  int *crazy;                // [nchains*np] rays that reached the point limit
+  const double *sdist;       // [nsrc*nrev] source-receiver distances (straight)
   // committed per-slot state
   int *committed;            // [nslots]
   double *cvp, *cvs, *crho;  // [nslots][nodes]
   double *cpvel;             // [nslots][np][nx][ny]
   double *cttime;            // [nslots][np][nsrc][nrev] committed phase times
+  double *csrd;              // [nslots][np][nsrc][nrev] their srdist (sigma = n0 srdist + n1)
+  double *cgvel;             // [nslots][np][nx][ny] committed group maps (igr)
 };
 
 // Optional per-stage timing: events recorded around the stages of each
@@ -58,6 +66,7 @@ struct SurfPlan {
   Fm2dJob fm2d;              // static parts (stations, settings, scratch, solve list)
   Fm2dPlan fm2d_plan;
   int nsolve_per_chain;
+  const double *src_xy, *rev_xy;   // [nsrc][2], [nrev][2] station coordinates (straight rays)
 };
 
 int surf_forward(SurfBatch &b, const SurfPlan &plan, cudaStream_t s, SurfProfile *prof = nullptr);

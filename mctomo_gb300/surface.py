@@ -27,7 +27,7 @@ class SurfSettings(ctypes.Structure):
                 ("gridx", ctypes.c_int), ("gridy", ctypes.c_int), ("sgref", ctypes.c_int),
                 ("sgdic", ctypes.c_int), ("sgext", ctypes.c_int), ("order", ctypes.c_int),
                 ("sigdep", ctypes.c_int), ("material_law", ctypes.c_int), ("rho_value", ctypes.c_double),
-                ("precision", ctypes.c_int), ("tt_precision", ctypes.c_int)]
+                ("precision", ctypes.c_int), ("tt_precision", ctypes.c_int), ("straight", ctypes.c_int)]
 
 
 class SurfData(ctypes.Structure):

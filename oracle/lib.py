@@ -61,6 +61,8 @@ def load():
                                  _I, _I, _I, _I, _I, _I, _D, _P, _P]),
             "orc_modrays_group": (_I, [_I, _P, _P, _I, _P, _P, _P, _I, _I, _D, _D, _D, _D, _P,
                                        _I, _I, _I, _I, _I, _I, _P, _P, _P, _P, _P]),
+            "orc_surf_likelihood_ex": (_I, [_P, _P, _P, _D, _D, _I, _P, _P, _I, _P, _I, _P, _I, _P, _P, _P, _P, _I,
+                                            _P, _P, _P, _I, _I, _P, _P, _P, _P, _P]),
             "orc_straight_group": (_I, [_I, _P, _I, _P, _P, _I, _I, _D, _D, _D, _D, _P, _P, _P]),
             "orc_fm2d_trace": (_I, [_I, _P, _P, _I]),
             "orc_fm2d_trace_count": (_I, []),

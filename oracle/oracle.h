@@ -37,6 +37,15 @@ int orc_modrays(int nsrc, const double *scx, const double *scz, int nrc,
                 int nvz, double goxd, double gozd, double dvxd, double dvzd,
                 const double *velvin, int gdx, int gdz, int asgr, int sgdl,
                 int sgs, int fom, double snb, double *ttime, double *tfield);
+int orc_modrays_group(int nsrc, const double *scx, const double *scz, int nrc,
+                      const double *rcx, const double *rcz, const int *srs, int nvx,
+                      int nvz, double goxd, double gozd, double dvxd, double dvzd,
+                      const double *velvin, int gdx, int gdz, int asgr, int sgdl,
+                      int sgs, int fom, const double *gvel, double *ttime, double *gtime,
+                      double *raylen, int *crazy);
+int orc_straight_group(int nsrc, const double *src, int nrev, const double *rev, const int *raystat, int nx,
+                       int ny, double xmin, double ymin, double dx, double dy, const double *vel, double *time,
+                       double *dist);
 
 int orc_fm2d_trace(int src, int *idx, double *t, int max);
 int orc_fm2d_trace_count(void);
