@@ -374,6 +374,117 @@ def run_reference(args):
     print(json.dumps(line), flush=True)
 
 
+BODY_CONFIG = {"workload": "batched 3D body-wave (P and S first arrivals) likelihood: 101x101x51 grid over "
+                           "50x50x25 km, 20-800 Voronoi cells/chain, 200 events at 1-20 km depth, 60 surface "
+                           "stations, 24,000 picks, solved from the stations (reciprocity), first-order eikonal",
+               "grid": [101, 101, 51], "events": 200, "stations": 60, "phases": 2,
+               "eikonal": "tile-based fast iterative method on the reference's first-order update"}
+
+
+def run_body(args):
+    """The body-wave configuration: every step is one full proposal per chain
+    (gridding, 120 3D solves, misfit) through the host API."""
+    import torch
+    from mctomo_gb300 import BodyLikelihood, synthetic
+    ws, rank = dist_env()
+    if ws > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl")
+        torch.cuda.set_device(int(os.environ.get("LOCAL_RANK", "0")))
+    dev = torch.device("cuda")
+    nch = args.chains
+    rng = np.random.default_rng(SEED + 1)
+    grid, settings, data, ev = synthetic.body_workload(rng)
+    settings["order"] = args.order
+    lo = np.zeros(3); hi = np.array([50.0, 50.0, 25.0])
+    ncell_max = 800
+    props = []
+    for _ in range(args.warmup + args.steps):
+        ncells = rng.integers(20, ncell_max + 1, nch).astype(np.int32)
+        pts = np.zeros((nch, ncell_max, 3)); par = np.zeros((nch, ncell_max, 3))
+        for c in range(nch):
+            p, q = synthetic.voronoi_model_3d(rng, int(ncells[c]), lo, hi, (3.0 / 1.73, 7.5 / 1.73))
+            q[:, 0] = q[:, 1] * 1.73
+            pts[c, :ncells[c]] = p; par[c, :ncells[c]] = q
+        props.append((ncells, pts, par))
+    locs = np.repeat(ev[None], nch, 0)
+    n0 = np.zeros((nch, 2)); n1 = np.full((nch, 2), 0.05)
+    lk = BodyLikelihood(grid, settings, data, nslots=nch, ncell_max=ncell_max)
+    for i in range(args.warmup):
+        lk.forward(*props[i], locs, n0, n1)
+    torch.cuda.synchronize()
+    if ws > 1:
+        torch.distributed.barrier()
+    clocks = Clocks(int(os.environ.get("LOCAL_RANK", "0")))
+    clocks.start()
+    ms = []
+    for i in range(args.warmup, args.warmup + args.steps):
+        t0 = time.perf_counter()
+        out = lk.forward(*props[i], locs, n0, n1)
+        ms.append((time.perf_counter() - t0) * 1e3)
+    cl = clocks.stop()
+    value, total = job_rate(nch * args.steps, sum(ms), ws, dev)
+    h2d = nch * ncell_max * 3 * 8 * 2 + nch * 4 + nch * len(ev) * 4 * 8 + 2 * nch * 2 * 8
+    line = {"metric": "body-wave forward evals/s, 1 GB300, ttime err<=1e-4 (first order)", "value": round(value, 4),
+            "unit": "proposal evals/s", "n_gpus": ws, "steps": args.steps, "warmup": args.warmup,
+            "ms_per_step": round(total / args.steps, 3), "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f32 local solves on int32 fixed-point times; f64 gridding and misfit",
+            "data": "synthetic (seeded, shapes of the configuration)",
+            "config": dict(BODY_CONFIG, chains=nch, order=args.order),
+            "e2e": {"value": round(value, 4), "unit": "proposal evals/s", "h2d_bytes_per_step": h2d,
+                    "d2h_bytes_per_step": nch * 4 * 8},
+            "note": "host API only (value = e2e): the body context has no device-pointer forward",
+            "clocks": cl, "valid_models": int((out[:, 3] == 0).sum())}
+    if rank == 0 and not args.no_cpu:
+        line["cpu_baseline"] = body_cpu_baseline(grid, settings, data, ev, props[0], args)
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+    lk.close()
+    if ws > 1:
+        torch.distributed.destroy_process_group()
+
+
+def body_cpu_baseline(grid, settings, data, ev, prop, args):
+    """The oracle's restatement of the reference's body path for one chain's
+    proposal: kd-tree gridding, then fastMarching3D from each station for P
+    and S (the reference's OpenMP loop over stations, here a thread pool over
+    all host cores), then the misfit."""
+    import concurrent.futures as cf
+    import oracle
+    orc = oracle.load()
+    P = lambda a: None if a is None else a.ctypes.data_as(ctypes.c_void_p)  # noqa: E731
+    ncells, pts, par = prop
+    n = int(ncells[0])
+    nx, ny, nz = grid["nx"], grid["ny"], grid["nz"]
+    shp = (nx, ny, nz)
+    threads = os.cpu_count() or 1
+    rev = np.asarray(data["rev"])
+    locs = np.ascontiguousarray(ev[:, :3])
+    t0 = time.perf_counter()
+    sid = np.zeros(shp, np.int32); vp = np.zeros(shp); vs = np.zeros(shp); rho = np.zeros(shp)
+    orc.orc_kdtree_to_grid(3, n, P(np.ascontiguousarray(pts[0, :n])), P(np.ascontiguousarray(par[0, :n])), nx, ny,
+                           nz, grid["xmin"], grid["ymin"], grid["zmin"], grid["dx"], grid["dy"], grid["dz"], 1, nx, 1,
+                           ny, 1, nz, P(sid), P(vp), P(vs), P(rho))
+    jobs = [(p, k) for p in range(2) for k in range(len(rev))]
+    vels = [vp, vs]
+    pt = np.zeros((2, data["nsrc"], len(rev)))
+
+    def solve(job):
+        p, k = job
+        tt = np.zeros(data["nsrc"])
+        orc.orc_fast_marching3d(nx, ny, nz, grid["dx"], grid["dy"], grid["dz"], grid["xmin"], grid["ymin"],
+                                grid["zmin"], P(vels[p]), P(np.ascontiguousarray(rev[k])), P(locs), data["nsrc"],
+                                settings["order"], P(tt), None)
+        pt[p, :, k] = tt
+
+    with cf.ThreadPoolExecutor(threads) as ex:
+        list(ex.map(solve, jobs))
+    dt = time.perf_counter() - t0
+    return {"value": round(1.0 / dt, 4), "unit": "proposal evals/s", "cores": threads, "kind": "reference",
+            "sample": "1 proposal (one chain): kd-tree gridding + 120 fastMarching3D solves (the reference's "
+                      "own C++ SFMM as restated bit-exactly) on a thread pool over all host cores"}
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -383,8 +494,16 @@ def main():
     ap.add_argument("--cpu-sample", type=int, default=8)
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--tt-precision", type=int, default=1)
+    ap.add_argument("--workload", default="surface", choices=["surface", "body"])
+    ap.add_argument("--chains", type=int, default=32, help="body workload: chains per step")
+    ap.add_argument("--order", type=int, default=0, help="body workload: eikonal order")
     args = ap.parse_args()
-    if args.impl == "reference":
+    if args.workload == "body":
+        if args.impl == "reference":
+            print(json.dumps({"impl": "reference", "unavailable": "the reference arm times the surface workload"}))
+        else:
+            run_body(args)
+    elif args.impl == "reference":
         run_reference(args)
     else:
         run_gpu(args)
