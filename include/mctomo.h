@@ -309,12 +309,28 @@ int mct_surf_poll(mct_surf_ctx *ctx, double *out, int *done);
  * fastMarching3D (fastmarching/fastMarching.cpp:26-30) with the same
  * arguments: grid nx,ny,nz with spacing dx,dy,dz and origin xmin,ymin,zmin;
  * vel (nx,ny,nz) C order (= Fortran (nz,ny,nx)); src[3]; rev (nrev,3);
- * order 0 first order / 1 mixed second order; ttime[nrev]; tfield (optional)
- * the final field in vel's layout. Solved on the GPU by a tile-based fast
- * iterative method on the reference's update operator: order 0 within
- * 1e-4 s of the reference; order 1 approximate (the reference's result
- * depends on its acceptance order; within 5e-2 s, typically 1e-3 s).
+ * order 1 mixed second order, anything else first order (as the
+ * reference); ttime[nrev]; tfield (optional) the final field in vel's
+ * layout.
+ *
+ * Two GPU solvers, chosen by a flag OR-ed into order:
+ *  MCT_EIK3_HEAP  - the reference's heap march (SFMM) itself, its pops,
+ *                   pushes and FP64 updates in the same order: results
+ *                   identical to the reference's, both orders. One group
+ *                   of 8 lanes marches each solve, so it is fast only for
+ *                   many solves at once.
+ *  MCT_EIK3_TILES - a tile-based fast iterative method on the same update
+ *                   operator (FP32 updates on fixed-point times): first
+ *                   order within 1e-4 s of the reference; the mixed second
+ *                   order only approximately (within 5e-2 s, typically
+ *                   1e-3 s), since the reference's second-order result
+ *                   depends on its acceptance order.
+ * Without a flag: the heap march for order 1, tiles for first order.
+ * An infinite accepted time (a region cut off by obstacles), where the
+ * reference asserts, returns MCT_ERR_INTERNAL from the heap march.
  * ---------------------------------------------------------------------- */
+#define MCT_EIK3_TILES 0x10
+#define MCT_EIK3_HEAP 0x20
 int mct_fast_marching3d(int nx, int ny, int nz, double dx, double dy,
                         double dz, double xmin, double ymin, double zmin,
                         const double *vel, const double *src,
@@ -324,7 +340,9 @@ int mct_fast_marching3d(int nx, int ny, int nz, double dx, double dy,
 /* Many solves at once: ngrids velocity grids vel[ngrids][nx][ny][nz], solve
  * i runs on grid solve_grid[i] from src[i][3]; the nrev receivers rev[nrev][3]
  * are shared; ttime[nsolve][nrev]; tfield optional [nsolve][nx][ny][nz];
- * passes (optional) receives the number of tile passes run. */
+ * order 0 or 1, optionally OR-ed with MCT_EIK3_TILES or MCT_EIK3_HEAP;
+ * passes (optional) receives the number of tile passes run (0 for the heap
+ * march). */
 int mct_eikonal3d_batch(int nsolve, int nx, int ny, int nz, double dx,
                         double dy, double dz, double xmin, double ymin,
                         double zmin, int ngrids, const double *vel,
@@ -344,6 +362,8 @@ typedef struct {
   int order;     /* 0 first order, 1 mixed second order */
   int np;        /* 1: P only (datatype 0), 2: P and S (datatype 1) */
   int sigdep;    /* 0 data sigma, else sigma = n0*time + n1 */
+  int solver;    /* 3D solver: 0 default (heap march for order 1, tiles for
+                    order 0), MCT_EIK3_TILES or MCT_EIK3_HEAP */
 } mct_body_settings;
 
 typedef struct {

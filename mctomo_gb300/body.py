@@ -12,7 +12,11 @@ from .surface import Grid
 
 
 class BodySettings(ctypes.Structure):
-    _fields_ = [("order", ctypes.c_int), ("np", ctypes.c_int), ("sigdep", ctypes.c_int)]
+    """order, np, sigdep as the reference's settings; solver selects the 3D
+    travel-time solver (0 default: the exact heap march for order 1, tiles
+    for order 0; EIK3_TILES or EIK3_HEAP)."""
+    _fields_ = [("order", ctypes.c_int), ("np", ctypes.c_int), ("sigdep", ctypes.c_int),
+                ("solver", ctypes.c_int)]
 
 
 class BodyData(ctypes.Structure):

@@ -15,6 +15,8 @@
 #include "../../include/mctomo.h"
 #include <vector>
 #include <cfloat>
+#include <climits>
+#include <algorithm>
 #include <cmath>
 
 namespace {
@@ -161,6 +163,10 @@ struct mct_body_ctx {
   double *esrc = nullptr, *erecv = nullptr, *ett = nullptr, *ptime = nullptr;
   int *egrid = nullptr, *eset = nullptr, *T = nullptr, *list = nullptr, *count = nullptr;
   unsigned char *flags = nullptr;
+  // 3D solver and the heap march's scratch
+  int method = EIK3_TILES;
+  double2 *hvn = nullptr; double *ht = nullptr; unsigned char *hst = nullptr; unsigned *hheap = nullptr;
+  int hchunk = 0; unsigned hcap = 0; int *herr = nullptr;
   int last_nchains = 0, last_passes = 0;
 };
 
@@ -173,6 +179,7 @@ int mct_body_create(const mct_grid *g, const mct_body_settings *st, const mct_bo
     return MCT_ERR_ARG;
   if (st->np != 1 && st->np != 2) return MCT_ERR_ARG;
   if (st->order != 0 && st->order != 1) return MCT_ERR_ARG;
+  if (st->solver != 0 && st->solver != MCT_EIK3_TILES && st->solver != MCT_EIK3_HEAP) return MCT_ERR_ARG;
   if (dat->nsrc < 1 || dat->nrev < 1 || dat->np != st->np) return MCT_ERR_ARG;
   *out = nullptr;
   mct_body_ctx *c = new mct_body_ctx();
@@ -183,7 +190,23 @@ int mct_body_create(const mct_grid *g, const mct_body_settings *st, const mct_bo
   const size_t nn = (size_t)g->nx * g->ny * g->nz;
   const size_t nsolve = (size_t)nslots * np * nsol;
   Eik3Job tmp{}; tmp.nx = g->nx; tmp.ny = g->ny; tmp.nz = g->nz;
-  const size_t ntile = eik3_tiles(tmp);
+  const int method = eik3_resolve_method(st->order, st->solver == MCT_EIK3_TILES ? EIK3_TILES
+                                                    : st->solver == MCT_EIK3_HEAP ? EIK3_HEAP : EIK3_DEFAULT);
+  const bool heap = method == EIK3_HEAP;
+  if (heap && nn >= (size_t)UINT_MAX / 2) { delete c; return MCT_ERR_ARG; }
+  c->method = method;
+  const size_t ntile = heap ? 0 : eik3_tiles(tmp);
+  const size_t nT = heap ? 0 : nsolve * nn;
+  // heap march: as many solves at once as fit in min(48 GiB, half the free
+  // memory); the rest run in further equal chunks
+  size_t hchunk = 0;
+  const unsigned hcap = eik3_heap_cap(g->nx, g->ny, g->nz);
+  if (heap) {
+    size_t fr = 0, tot = 0;
+    if (cudaMemGetInfo(&fr, &tot) != cudaSuccess) { delete c; return MCT_ERR_CUDA; }
+    const size_t budget = std::min<size_t>(48ull << 30, fr / 2);
+    hchunk = std::max<size_t>(1, std::min<size_t>(nsolve, budget / eik3_heap_bytes_per_solve(g->nx, g->ny, g->nz)));
+  }
   const size_t kd = kd_scratch_bytes(ncell_max);
   std::vector<size_t> sz = {
       sizeof(int) * nslots, sizeof(double) * (size_t)nslots * ncell_max * 3 * 3, sizeof(double) * (size_t)nslots * nsrc * 4,
@@ -192,8 +215,10 @@ int mct_body_create(const mct_grid *g, const mct_body_settings *st, const mct_bo
       sizeof(int) * nslots, sizeof(int) * (size_t)nslots * nn, kd * nslots, sizeof(int) * 2,
       sizeof(double) * 3 * nsolve, sizeof(double) * 3 * (size_t)nslots * nrecv, sizeof(double) * nsolve * nrecv,
       sizeof(double) * (size_t)nslots * np * npairs, sizeof(int) * nsolve, sizeof(int) * nsolve,
-      sizeof(int) * nsolve * nn, ntile * nsolve, sizeof(int) * ntile * nsolve, sizeof(int),
-      sizeof(int) * np * npairs, sizeof(double) * 2 * np * npairs};
+      sizeof(int) * nT, ntile * nsolve, sizeof(int) * ntile * nsolve, sizeof(int),
+      sizeof(int) * np * npairs, sizeof(double) * 2 * np * npairs,
+      heap ? sizeof(double2) * 2 * (size_t)nslots * nn : 0, sizeof(double) * hchunk * nn, hchunk * nn,
+      sizeof(unsigned) * hchunk * hcap, sizeof(int)};
   size_t total = 0;
   for (size_t s : sz) total = ((total + 255) & ~size_t(255)) + s;
   total += 256;
@@ -223,12 +248,18 @@ int mct_body_create(const mct_grid *g, const mct_body_settings *st, const mct_bo
   c->ptime = cv.take<double>((size_t)nslots * np * npairs);
   c->egrid = cv.take<int>(nsolve);
   c->eset = cv.take<int>(nsolve);
-  c->T = cv.take<int>(nsolve * nn);
+  c->T = cv.take<int>(nT);
   c->flags = cv.take<unsigned char>(ntile * nsolve);
   c->list = cv.take<int>(ntile * nsolve);
   c->count = cv.take<int>(1);
   int *rays = cv.take<int>((size_t)np * npairs);
   double *dt = cv.take<double>((size_t)2 * np * npairs);
+  c->hvn = cv.take<double2>(heap ? 2 * (size_t)nslots * nn : 0);
+  c->ht = cv.take<double>(hchunk * nn);
+  c->hst = cv.take<unsigned char>(hchunk * nn);
+  c->hheap = cv.take<unsigned>(hchunk * hcap);
+  c->herr = cv.take<int>(1);
+  c->hchunk = (int)hchunk; c->hcap = hcap;
   std::vector<double> hs((size_t)np * npairs, 1.0);
   if (dat->sigma) for (size_t q = 0; q < hs.size(); ++q) hs[q] = dat->sigma[q];
   cudaMemcpy(c->rev, dat->rev, sizeof(double) * 3 * nrev, cudaMemcpyHostToDevice);
@@ -302,8 +333,10 @@ int mct_body_forward(mct_body_ctx *c, int nchains, const int *ncells, const doub
   Eik3Job job{};
   job.nsolve = nsolve; job.nx = g.nx; job.ny = g.ny; job.nz = g.nz; job.dx = g.dx; job.dy = g.dy; job.dz = dzs;
   job.vel = c->vel; job.slow = c->slow; job.ngrids = 2 * c->nslots; job.solve_grid = c->egrid; job.src = c->esrc;
-  job.order = c->order; job.shift = eik3_shift_for(4.0 * diag / vmin);
+  job.order = c->order; job.method = c->method; job.shift = eik3_shift_for(4.0 * diag / vmin);
   job.T = c->T; job.flags = c->flags; job.list = c->list; job.count = c->count;
+  job.hvn = c->hvn; job.ht = c->ht; job.hst = c->hst; job.hheap = c->hheap;
+  job.hchunk = c->hchunk; job.hcap = c->hcap; job.herr = c->herr;
   job.nrev = nrecv; job.rev = c->erecv; job.rev_per_solve = 1; job.solve_rev = c->eset; job.ttime = c->ett;
   int passes = 0;
   rc = launch_eik3(job, s, 100000, &passes, nullptr); if (rc) return rc;

@@ -6,6 +6,7 @@
 #include "fm2d.cuh"
 #include "eikonal3d.cuh"
 #include <cstring>
+#include <climits>
 #include <string>
 #include <vector>
 #include <algorithm>
@@ -495,10 +496,15 @@ int mct_eikonal3d_batch(int nsolve, int nx, int ny, int nz, double dx, double dy
                         double ymin, double zmin, int ngrids, const double *vel, const int *solve_grid,
                         const double *src, int nrev, const double *rev, int order, double *ttime,
                         double *tfield, int *passes) {
+  const int ord = order & 0xF, mflag = order & ~0xF;
   if (nsolve < 1 || nx < 2 || ny < 2 || nz < 2 || ngrids < 1 || nrev < 0 || !(dx > 0) || !(dy > 0) ||
-      !(dz > 0) || (order != 0 && order != 1))
+      !(dz > 0) || (ord != 0 && ord != 1) ||
+      (mflag != 0 && mflag != MCT_EIK3_TILES && mflag != MCT_EIK3_HEAP))
     return arg_error("mct_eikonal3d_batch: bad arguments");
+  const int method = eik3_resolve_method(ord, mflag == MCT_EIK3_TILES ? EIK3_TILES
+                                              : mflag == MCT_EIK3_HEAP ? EIK3_HEAP : EIK3_DEFAULT);
   const size_t nn = (size_t)nx * ny * nz;
+  if (method == EIK3_HEAP && nn >= (size_t)UINT_MAX / 2) return arg_error("mct_eikonal3d_batch: grid too large");
   double vmin = 1e300;
   for (size_t q = 0; q < nn * ngrids; ++q)
     if (vel[q] >= 2.220446049250313e-11 && vel[q] < vmin) vmin = vel[q];
@@ -511,27 +517,44 @@ int mct_eikonal3d_batch(int nsolve, int nx, int ny, int nz, double dx, double dy
   int rc = ensure_stream(); if (rc) return rc;
   Eik3Job job{};
   job.nsolve = nsolve; job.nx = nx; job.ny = ny; job.nz = nz; job.dx = dx; job.dy = dy; job.dz = dz;
-  job.ngrids = ngrids; job.order = order; job.nrev = nrev; job.rev_per_solve = 0;
+  job.ngrids = ngrids; job.order = ord; job.method = method; job.nrev = nrev; job.rev_per_solve = 0;
   job.shift = eik3_shift_for(4.0 * diag / vmin);
-  const size_t ntile = eik3_tiles(job);
+  const bool heap = method == EIK3_HEAP;
+  const size_t ntile = heap ? 0 : eik3_tiles(job);
+  const size_t nT = heap ? 0 : nn * nsolve;
+  // heap march: as many solves at once as 16 GiB of scratch holds
+  const size_t per_solve = eik3_heap_bytes_per_solve(nx, ny, nz);
+  const int hchunk = heap ? (int)std::max<size_t>(1, std::min<size_t>(nsolve, (16ull << 30) / per_solve)) : 0;
+  const unsigned hcap = eik3_heap_cap(nx, ny, nz);
   size_t bytes = carve_size({sizeof(double) * nn * ngrids, sizeof(float) * nn * ngrids, sizeof(int) * nsolve,
-                             sizeof(double) * 3 * nsolve, sizeof(int) * nn * nsolve, ntile * nsolve,
+                             sizeof(double) * 3 * nsolve, sizeof(int) * nT, ntile * nsolve,
                              sizeof(int) * ntile * nsolve, sizeof(int), sizeof(double) * 3 * (nrev + 1),
                              sizeof(double) * (size_t)nsolve * (nrev + 1),
-                             tfield ? sizeof(double) * nn * nsolve : 0});
+                             tfield ? sizeof(double) * nn * nsolve : 0,
+                             heap ? sizeof(double2) * nn * ngrids : 0, heap ? sizeof(double) * nn * hchunk : 0,
+                             heap ? nn * hchunk : 0, heap ? sizeof(unsigned) * (size_t)hcap * hchunk : 0,
+                             sizeof(int)});
   rc = g_ws.reserve(bytes); if (rc) return rc;
   Carve cv(g_ws.p);
   double *d_vel = cv.take<double>(nn * ngrids);
   job.slow = cv.take<float>(nn * ngrids);
   int *d_sg = cv.take<int>(nsolve);
   double *d_src = cv.take<double>(3 * (size_t)nsolve);
-  job.T = cv.take<int>(nn * nsolve);
+  job.T = cv.take<int>(nT);
   job.flags = cv.take<unsigned char>(ntile * nsolve);
   job.list = cv.take<int>(ntile * nsolve);
   job.count = cv.take<int>(1);
   double *d_rev = cv.take<double>(3 * (size_t)(nrev + 1));
   double *d_tt = cv.take<double>((size_t)nsolve * (nrev + 1));
   double *d_tf = tfield ? cv.take<double>(nn * nsolve) : nullptr;
+  if (heap) {
+    job.hvn = cv.take<double2>(nn * ngrids);
+    job.ht = cv.take<double>(nn * hchunk);
+    job.hst = cv.take<unsigned char>(nn * hchunk);
+    job.hheap = cv.take<unsigned>((size_t)hcap * hchunk);
+    job.hchunk = hchunk; job.hcap = hcap;
+  }
+  job.herr = cv.take<int>(1);
   std::vector<double> hsrc(3 * (size_t)nsolve), hrev(3 * (size_t)nrev);
   for (int q = 0; q < nsolve; ++q) {
     hsrc[3 * q] = src[3 * q] - xmin; hsrc[3 * q + 1] = src[3 * q + 1] - ymin; hsrc[3 * q + 2] = src[3 * q + 2] - zmin;
@@ -559,7 +582,12 @@ int mct_fast_marching3d(int nx, int ny, int nz, double dx, double dy, double dz,
                         double zmin, const double *vel, const double *src, const double *rev, int nrev, int order,
                         double *ttime, double *tfield) {
   const int g = 0;
-  return mct_eikonal3d_batch(1, nx, ny, nz, dx, dy, dz, xmin, ymin, zmin, 1, vel, &g, src, nrev, rev, order == 1 ? 1 : 0,
+  // the reference: order 1 -> second order, anything else first order
+  // (fastMarching.cpp:76-80); a solver-selection flag may be added
+  const int flags = order & ~0xF;
+  const int ord = (flags == MCT_EIK3_TILES || flags == MCT_EIK3_HEAP) ? ((order & 0xF) == 1 ? 1 : 0) | flags
+                                                                       : (order == 1 ? 1 : 0);
+  return mct_eikonal3d_batch(1, nx, ny, nz, dx, dy, dz, xmin, ymin, zmin, 1, vel, &g, src, nrev, rev, ord,
                              ttime, tfield, nullptr);
 }
 

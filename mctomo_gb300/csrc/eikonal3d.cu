@@ -24,6 +24,7 @@
 // rounding stays far below the 1e-4 s travel-time bound.
 #include "mct_common.cuh"
 #include "eikonal3d.cuh"
+#include "eik3_common.cuh"
 #include <climits>
 
 namespace {
@@ -64,31 +65,7 @@ __global__ void fill_kernel(int *T, size_t n) {
 // (ndgridmap.hpp getVel/getTime), point relative to the grid origin.
 template <class F>
 __device__ double trilinear(const Dims &d, const double h[3], const double p[3], F value) {
-  int pc[3];
-  int dimsz[3] = {d.nx, d.ny, d.nz};
-  for (int q = 0; q < 3; ++q) {
-    int c = (int)(p[q] / h[q]);
-    if (c < 0) c = 0; else if (c >= dimsz[q]) c = dimsz[q] - 1;
-    pc[q] = c;
-  }
-  double acc = 0;
-  for (int v = 0; v < 8; ++v) {
-    int vc[3];
-    for (int q = 0; q < 3; ++q) {
-      int vi = (v >> (3 - q - 1)) & 1;
-      vc[q] = pc[q] + vi;
-      if (vc[q] >= dimsz[q]) vc[q] = dimsz[q] - 1;
-    }
-    double w = 1.0;
-    for (int q = 0; q < 3; ++q) {
-      double di = (double)(unsigned)(vc[q] - pc[q]);
-      double s = p[q] - h[q] * (double)(unsigned)pc[q];
-      double wj = fabs(di * h[q] - h[q] + s);
-      w = w * wj / h[q];
-    }
-    acc = acc + w * value(vc[0], vc[1], vc[2]);
-  }
-  return acc;
+  return e3_trilinear(E3Dims{d.nx, d.ny, d.nz}, h, p, value);
 }
 
 // Source initialisation (solver.hpp:72-92) and seeding of the first tiles.
@@ -367,6 +344,10 @@ int eik3_shift_for(double tmax_bound) {
 }
 
 int launch_eik3(Eik3Job &job, cudaStream_t s, int max_passes, int *passes_out, double *tfield) {
+  if (job.method == EIK3_HEAP) {
+    if (passes_out) *passes_out = 0;
+    return launch_eik3_heap(job, s, tfield);
+  }
   const size_t nn = (size_t)job.nx * job.ny * job.nz;
   const size_t ntile = eik3_tiles(job);
   slowness_kernel<<<1024, 256, 0, s>>>(job.vel, job.slow, nn * job.ngrids);

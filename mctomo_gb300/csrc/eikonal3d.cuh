@@ -1,7 +1,12 @@
-// 3D eikonal job description (tile-based fast iterative method).
+// 3D eikonal job description: tile-based fast iterative method (method 1)
+// or the exact heap march (method 2).
 #pragma once
 #include <cuda_runtime.h>
 #include <cstddef>
+
+// Method selection (the low bits of the public order argument carry the
+// order; these bits select the solver).
+enum Eik3Method { EIK3_DEFAULT = 0, EIK3_TILES = 1, EIK3_HEAP = 2 };
 
 struct Eik3Job {
   int nsolve;
@@ -13,10 +18,21 @@ struct Eik3Job {
   const int *solve_grid;          // [nsolve] velocity grid of each solve
   const double *src;              // [nsolve][3] source relative to the grid origin
   int order;                      // 0 first order, 1 mixed second order
+  int method;                     // EIK3_TILES or EIK3_HEAP (resolved, never EIK3_DEFAULT)
+  // tile iteration scratch
   int shift;                      // times stored in units of 2^-shift s
   int *T;                         // [nsolve][nx][ny][nz] scratch: fixed-point times
   unsigned char *flags;           // [nsolve][tiles] scratch
   int *list, *count;              // scratch: active (solve, tile) list
+  // heap march scratch (solves run in chunks of hchunk)
+  double *ht;                     // [hchunk][nn] arrival times
+  unsigned char *hst;             // [hchunk][nn] OPEN / NARROW / FROZEN
+  unsigned *hheap;                // [hchunk][hcap] heap of node indices
+  double2 *hvn;                   // [ngrids][nn] (velocity, -1/velocity^2)
+  int hchunk;
+  unsigned hcap;
+  int *herr;                      // [1] error bits
+  // receivers
   int nrev;                       // receivers per solve
   const double *rev;              // [sets][nrev][3] relative to the origin
   int rev_per_solve;              // 1: set = solve index (unless solve_rev given)
@@ -26,4 +42,11 @@ struct Eik3Job {
 
 size_t eik3_tiles(const Eik3Job &j);
 int eik3_shift_for(double tmax_bound);
+// Resolves EIK3_DEFAULT: the heap march for the mixed second-order scheme
+// (whose result depends on the acceptance order), tiles for first order.
+int eik3_resolve_method(int order, int method);
+// Heap-march scratch per solve (times, states, heap) and per velocity grid.
+size_t eik3_heap_bytes_per_solve(int nx, int ny, int nz);
+unsigned eik3_heap_cap(int nx, int ny, int nz);
 int launch_eik3(Eik3Job &job, cudaStream_t s, int max_passes, int *passes_out, double *tfield);
+int launch_eik3_heap(Eik3Job &job, cudaStream_t s, double *tfield);

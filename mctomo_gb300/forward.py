@@ -175,10 +175,17 @@ def modrays_group_batch(src, rev, srs, nvx, nvz, goxd, gozd, dvxd, dvzd, velv, g
     return tt, gt, ln, crazy
 
 
-def fast_marching3d(vel, h, lo, src, rev, order=1, tfield=False):
+EIK3_TILES = 0x10
+EIK3_HEAP = 0x20
+_SOLVER = {None: 0, "tiles": EIK3_TILES, "heap": EIK3_HEAP}
+
+
+def fast_marching3d(vel, h, lo, src, rev, order=1, tfield=False, solver=None):
     """fastMarching3D (fastmarching/fastMarching.cpp:26-129). vel: (nx, ny, nz)
     C order; h = (dx, dy, dz); lo = (xmin, ymin, zmin); src (3,); rev (nrev, 3).
-    Returns ttime (nrev,) and optionally the field (nx, ny, nz)."""
+    solver: None (heap march for order 1, tiles for order 0), "heap" or
+    "tiles". Returns ttime (nrev,) and optionally the field (nx, ny, nz)."""
+    order = int(order) | _SOLVER[solver]
     vel = _f64(vel)
     nx, ny, nz = vel.shape
     src = _f64(src); rev = _f64(rev).reshape(-1, 3)
@@ -191,10 +198,12 @@ def fast_marching3d(vel, h, lo, src, rev, order=1, tfield=False):
     return (tt, tf) if tfield else tt
 
 
-def eikonal3d_batch(vels, h, lo, solve_grid, srcs, rev, order=1, tfield=False):
+def eikonal3d_batch(vels, h, lo, solve_grid, srcs, rev, order=1, tfield=False, solver=None):
     """Many 3D solves: vels (ngrids, nx, ny, nz), solve_grid (nsolve,),
-    srcs (nsolve, 3), shared receivers rev (nrev, 3). Returns ttime
-    (nsolve, nrev), the optional fields and the number of tile passes."""
+    srcs (nsolve, 3), shared receivers rev (nrev, 3); solver as for
+    fast_marching3d. Returns ttime (nsolve, nrev), the optional fields and
+    the number of tile passes (0 for the heap march)."""
+    order = int(order) | _SOLVER[solver]
     vels = _f64(vels)
     ng, nx, ny, nz = vels.shape
     solve_grid = np.ascontiguousarray(solve_grid, np.int32)

@@ -10,8 +10,9 @@ import pytest
 from mctomo_gb300 import BodyLikelihood, synthetic
 
 pytestmark = pytest.mark.gpu
+EIK3_TILES, EIK3_HEAP = 0x10, 0x20
 P = lambda a: None if a is None else a.ctypes.data_as(ctypes.c_void_p)  # noqa: E731
-TT_TOL = {0: 1e-4, 1: 5e-2}   # per order, see test_gpu_eik3
+TT_TOL = {0: 1e-4, 1: 5e-2}   # tile solver, per order, see test_gpu_eik3
 
 
 def oracle_body(orc, grid, settings, data, ev, n, pts, par, n0, n1):
@@ -51,12 +52,14 @@ def body_misfit(orc, settings, data, ev, pt, n0, n1):
     return out
 
 
-@pytest.mark.parametrize("order", [0, 1])
-def test_body_batch_matches_oracle(orc, gpulib, order):
+@pytest.mark.parametrize("order,solver", [(0, 0), (1, 0), (0, EIK3_HEAP), (1, EIK3_TILES)])
+def test_body_batch_matches_oracle(orc, gpulib, order, solver):
     rng = np.random.default_rng(40 + order)
     grid, settings, data, ev = synthetic.body_workload(rng, nx=31, ny=29, nz=17, extent=(15.0, 14.0, 8.0),
                                                       nevents=24, nstations=9)
     settings["order"] = order
+    settings["solver"] = solver
+    exact = solver == EIK3_HEAP or (solver == 0 and order == 1)   # the heap march
     lo = np.zeros(3); hi = np.array([15.0, 14.0, 8.0])
     nch, ncell_max = 3, 40
     ncells = np.array([12, 25, 40], np.int32)
@@ -72,6 +75,13 @@ def test_body_batch_matches_oracle(orc, gpulib, order):
     for c in range(nch):
         eo, ept = oracle_body(orc, grid, settings, data, ev, ncells[c], pts[c], par[c], n0[c], n1[c])
         pt, passes = lk.phase_time(c)
+        if exact:
+            assert passes == 0
+            np.testing.assert_array_equal(pt, ept)
+            # identical times: the likelihood equals the reference path's up
+            # to the order of the misfit sums
+            np.testing.assert_allclose(out[c, :3], eo, rtol=1e-12)
+            continue
         assert passes > 0
         assert np.max(np.abs(pt - ept)) <= TT_TOL[order], np.max(np.abs(pt - ept))
         # the misfit reduction itself, on the GPU's own phase times

@@ -1,8 +1,12 @@
-"""GPU parity: 3D travel times (tile-based fast iterative method on the
-reference's update operator) vs the reference's own fastMarching3D as
+"""GPU parity: 3D travel times vs the reference's own fastMarching3D as
 restated by the oracle (bit-exact to the compiled reference).
 
-Tolerances: first order (order 0) 1e-4 s on receiver times, the north-star
+Heap march (the default for order 1, selectable for both orders): the
+reference's SFMM run step for step; times and fields must be identical, bit
+for bit, for every lane-group size and chunking.
+
+Tile solver (fast iterative method on the reference's update operator):
+first order (order 0) within 1e-4 s on receiver times, the north-star
 bound: the iteration's fixed point is the heap march's discrete solution and
 the FP32 local solves on fixed-point times add ~1e-6 s. Mixed second order
 (order 1) 5e-2 s: the reference's heap march feeds second-order stencils with
@@ -42,7 +46,7 @@ def layered_voronoi(rng, shape, h, ncell, vrange):
 
 
 @pytest.mark.parametrize("order", [0, 1])
-def test_fast_marching3d_matches_reference(orc, gpulib, order):
+def test_fast_marching3d_tiles_match_reference(orc, gpulib, order):
     rng = np.random.default_rng(10 + order)
     shape = (41, 37, 21)
     h = np.array([0.5, 0.5, 0.5]); lo = np.array([-5.0, 2.0, 0.0])
@@ -52,7 +56,7 @@ def test_fast_marching3d_matches_reference(orc, gpulib, order):
         src = lo + ext * rng.uniform(0.05, 0.95, 3)
         rev = lo + ext * rng.uniform(0.02, 0.98, (40, 3))
         rev[:, 2] = lo[2] + 0.0   # stations at the surface
-        got, gf = fast_marching3d(vel, h, lo, src, rev, order=order, tfield=True)
+        got, gf = fast_marching3d(vel, h, lo, src, rev, order=order, tfield=True, solver="tiles")
         exp, ef = oracle_fmm(orc, vel, h, lo, src, rev, order)
         tol = TOL if order == 0 else TOL_ORDER1
         assert np.max(np.abs(got - exp)) <= tol, np.max(np.abs(got - exp))
@@ -67,9 +71,11 @@ def test_eikonal3d_homogeneous_first_order(orc, gpulib):
     got = fast_marching3d(vel, h, lo, src, rev, order=0)
     exp, _ = oracle_fmm(orc, vel, np.array(h), np.array(lo), src, rev, 0)
     assert np.max(np.abs(got - exp)) <= TOL
+    got = fast_marching3d(vel, h, lo, src, rev, order=0, solver="heap")
+    np.testing.assert_array_equal(got, exp)
 
 
-def test_eikonal3d_batch_many_sources_and_grids(orc, gpulib):
+def test_eikonal3d_batch_tiles_many_sources_and_grids(orc, gpulib):
     rng = np.random.default_rng(3)
     shape = (33, 29, 17)
     h = np.array([0.5, 0.5, 0.5]); lo = np.zeros(3)
@@ -79,12 +85,113 @@ def test_eikonal3d_batch_many_sources_and_grids(orc, gpulib):
     srcs = ext * rng.uniform(0.05, 0.95, (6, 3)); srcs[:, 2] = 0.0
     grid_of = np.array([0, 1, 0, 1, 0, 1])
     rev = ext * rng.uniform(0.02, 0.98, (25, 3))
-    got, _, passes = eikonal3d_batch(vels, h, lo, grid_of, srcs, rev, order=1)
+    got, _, passes = eikonal3d_batch(vels, h, lo, grid_of, srcs, rev, order=1, solver="tiles")
     assert passes > 0
     for i in range(6):
         exp, _ = oracle_fmm(orc, vels[grid_of[i]], h, lo, srcs[i], rev, 1)
         assert np.max(np.abs(got[i] - exp)) <= TOL_ORDER1
-    got0, _, _ = eikonal3d_batch(vels, h, lo, grid_of, srcs, rev, order=0)
+    got0, _, _ = eikonal3d_batch(vels, h, lo, grid_of, srcs, rev, order=0, solver="tiles")
     for i in range(6):
         exp, _ = oracle_fmm(orc, vels[grid_of[i]], h, lo, srcs[i], rev, 0)
         assert np.max(np.abs(got0[i] - exp)) <= TOL
+
+
+# ---------------------------------------------------------------- heap march
+
+@pytest.mark.parametrize("order", [0, 1])
+@pytest.mark.parametrize("group", [8, 32, 16])
+def test_heap_march_bit_exact(orc, gpulib, order, group):
+    rng = np.random.default_rng(20 + order + group)
+    shape = (29, 23, 17)
+    h = np.array([0.5, 0.45, 0.4]); lo = np.array([-3.0, 1.0, 0.0])
+    vel = layered_voronoi(rng, shape, h, 50, (3.0, 7.5))
+    ext = (np.array(shape) - 1) * h
+    old = gpulib.mct_debug_eik3_heap_group(group)
+    try:
+        for trial in range(2):
+            src = lo + ext * rng.uniform(0.0, 1.0, 3)
+            rev = lo + ext * rng.uniform(0.0, 1.0, (30, 3))
+            rev[:5, 2] = lo[2]
+            rev[5] = lo + ext            # a corner on the max faces (the 8x read-out quirk)
+            got, gf = fast_marching3d(vel, h, lo, src, rev, order=order, tfield=True, solver="heap")
+            exp, ef = oracle_fmm(orc, vel, h, lo, src, rev, order)
+            np.testing.assert_array_equal(gf, ef)
+            np.testing.assert_array_equal(got, exp)
+    finally:
+        gpulib.mct_debug_eik3_heap_group(old)
+
+
+def test_heap_march_is_the_order1_default(orc, gpulib):
+    rng = np.random.default_rng(7)
+    shape = (25, 21, 19)
+    h = np.array([0.5, 0.5, 0.5]); lo = np.zeros(3)
+    vel = layered_voronoi(rng, shape, h, 30, (2.0, 6.0))
+    src = np.array([3.1, 4.7, 2.2]); rev = rng.uniform(0, 9.0, (20, 3))
+    got, passes = fast_marching3d(vel, h, lo, src, rev, order=1), None
+    exp, _ = oracle_fmm(orc, vel, h, lo, src, rev, 1)
+    np.testing.assert_array_equal(got, exp)
+
+
+def test_heap_march_source_on_nodes_and_faces(orc, gpulib):
+    # sources exactly on a node, on a max face (clamped corners pushed
+    # twice) and at the origin
+    rng = np.random.default_rng(8)
+    shape = (21, 19, 15)
+    h = np.array([0.5, 0.5, 0.5]); lo = np.zeros(3)
+    vel = layered_voronoi(rng, shape, h, 25, (3.0, 7.5))
+    ext = (np.array(shape) - 1) * h
+    rev = rng.uniform(0, 1, (15, 3)) * ext
+    for src in (np.array([2.0, 3.5, 1.5]), ext.copy(), np.array([ext[0], 1.3, ext[2]]), np.zeros(3)):
+        for order in (0, 1):
+            got, gf = fast_marching3d(vel, h, lo, src, rev, order=order, tfield=True, solver="heap")
+            exp, ef = oracle_fmm(orc, vel, h, lo, src, rev, order)
+            np.testing.assert_array_equal(gf, ef)
+            np.testing.assert_array_equal(got, exp)
+
+
+def test_heap_march_obstacle_wall_with_gap(orc, gpulib):
+    # zero-velocity nodes are obstacles (never updated); the wave goes
+    # round through a gap; behind a closed wall times stay infinite
+    rng = np.random.default_rng(9)
+    shape = (24, 20, 16)
+    h = np.array([0.5, 0.5, 0.5]); lo = np.zeros(3)
+    vel = layered_voronoi(rng, shape, h, 20, (3.0, 7.5))
+    vel[12, :, :] = 0.0
+    vel[12, 3:6, 4:8] = 4.0                       # the gap
+    src = np.array([2.2, 4.1, 3.3])
+    rev = rng.uniform(0, 1, (20, 3)) * (np.array(shape) - 1) * h
+    for order in (0, 1):
+        got, gf = fast_marching3d(vel, h, lo, src, rev, order=order, tfield=True, solver="heap")
+        exp, ef = oracle_fmm(orc, vel, h, lo, src, rev, order)
+        np.testing.assert_array_equal(gf, ef)
+        np.testing.assert_array_equal(got, exp)
+    closed = vel.copy(); closed[12] = 0.0
+    got, gf = fast_marching3d(closed, h, lo, src, rev, order=1, tfield=True, solver="heap")
+    exp, ef = oracle_fmm(orc, closed, h, lo, src, rev, 1)
+    np.testing.assert_array_equal(gf, ef)
+    assert np.isinf(gf[13:]).all()
+
+
+def test_heap_march_batch_chunks(orc, gpulib):
+    rng = np.random.default_rng(4)
+    shape = (27, 25, 13)
+    h = np.array([0.5, 0.5, 0.5]); lo = np.zeros(3)
+    vels = np.stack([layered_voronoi(rng, shape, h, 40, (3.0, 7.5)) for _ in range(3)])
+    ext = (np.array(shape) - 1) * h
+    ns = 7
+    srcs = ext * rng.uniform(0.0, 1.0, (ns, 3)); srcs[:3, 2] = 0.0
+    grid_of = rng.integers(0, 3, ns).astype(np.int32)
+    rev = ext * rng.uniform(0.0, 1.0, (18, 3))
+    got, gf, passes = eikonal3d_batch(vels, h, lo, grid_of, srcs, rev, order=1, tfield=True)
+    assert passes == 0
+    old = gpulib.mct_debug_eik3_heap_chunk(3)
+    try:
+        got3, gf3, _ = eikonal3d_batch(vels, h, lo, grid_of, srcs, rev, order=1, tfield=True)
+    finally:
+        gpulib.mct_debug_eik3_heap_chunk(old)
+    np.testing.assert_array_equal(got3, got)
+    np.testing.assert_array_equal(gf3, gf)
+    for i in range(ns):
+        exp, ef = oracle_fmm(orc, vels[grid_of[i]], h, lo, srcs[i], rev, 1)
+        np.testing.assert_array_equal(gf[i], ef)
+        np.testing.assert_array_equal(got[i], exp)
