@@ -165,8 +165,8 @@ struct mct_body_ctx {
   unsigned char *flags = nullptr;
   // 3D solver and the heap march's scratch
   int method = EIK3_TILES;
-  double2 *hvn = nullptr; double *ht = nullptr; unsigned char *hst = nullptr; unsigned *hheap = nullptr;
-  int hchunk = 0; unsigned hcap = 0; int *herr = nullptr;
+  double2 *hvn = nullptr; void *hscratch = nullptr;
+  int hchunk = 0; int *herr = nullptr;
   int last_nchains = 0, last_passes = 0;
 };
 
@@ -193,14 +193,13 @@ int mct_body_create(const mct_grid *g, const mct_body_settings *st, const mct_bo
   const int method = eik3_resolve_method(st->order, st->solver == MCT_EIK3_TILES ? EIK3_TILES
                                                     : st->solver == MCT_EIK3_HEAP ? EIK3_HEAP : EIK3_DEFAULT);
   const bool heap = method == EIK3_HEAP;
-  if (heap && nn >= (size_t)UINT_MAX / 2) { delete c; return MCT_ERR_ARG; }
+  if (heap && nn > (size_t)0x3FFFFFFF) { delete c; return MCT_ERR_ARG; }   // 30-bit node indices
   c->method = method;
   const size_t ntile = heap ? 0 : eik3_tiles(tmp);
   const size_t nT = heap ? 0 : nsolve * nn;
   // heap march: as many solves at once as fit in min(48 GiB, half the free
   // memory); the rest run in further equal chunks
   size_t hchunk = 0;
-  const unsigned hcap = eik3_heap_cap(g->nx, g->ny, g->nz);
   if (heap) {
     size_t fr = 0, tot = 0;
     if (cudaMemGetInfo(&fr, &tot) != cudaSuccess) { delete c; return MCT_ERR_CUDA; }
@@ -217,8 +216,8 @@ int mct_body_create(const mct_grid *g, const mct_body_settings *st, const mct_bo
       sizeof(double) * (size_t)nslots * np * npairs, sizeof(int) * nsolve, sizeof(int) * nsolve,
       sizeof(int) * nT, ntile * nsolve, sizeof(int) * ntile * nsolve, sizeof(int),
       sizeof(int) * np * npairs, sizeof(double) * 2 * np * npairs,
-      heap ? sizeof(double2) * 2 * (size_t)nslots * nn : 0, sizeof(double) * hchunk * nn, hchunk * nn,
-      sizeof(unsigned) * hchunk * hcap, sizeof(int)};
+      heap ? sizeof(double2) * 2 * (size_t)nslots * nn : 0,
+      eik3_heap_scratch_bytes(g->nx, g->ny, g->nz, (int)hchunk), sizeof(int)};
   size_t total = 0;
   for (size_t s : sz) total = ((total + 255) & ~size_t(255)) + s;
   total += 256;
@@ -255,11 +254,9 @@ int mct_body_create(const mct_grid *g, const mct_body_settings *st, const mct_bo
   int *rays = cv.take<int>((size_t)np * npairs);
   double *dt = cv.take<double>((size_t)2 * np * npairs);
   c->hvn = cv.take<double2>(heap ? 2 * (size_t)nslots * nn : 0);
-  c->ht = cv.take<double>(hchunk * nn);
-  c->hst = cv.take<unsigned char>(hchunk * nn);
-  c->hheap = cv.take<unsigned>(hchunk * hcap);
+  c->hscratch = cv.take<char>(eik3_heap_scratch_bytes(g->nx, g->ny, g->nz, (int)hchunk));
   c->herr = cv.take<int>(1);
-  c->hchunk = (int)hchunk; c->hcap = hcap;
+  c->hchunk = (int)hchunk;
   std::vector<double> hs((size_t)np * npairs, 1.0);
   if (dat->sigma) for (size_t q = 0; q < hs.size(); ++q) hs[q] = dat->sigma[q];
   cudaMemcpy(c->rev, dat->rev, sizeof(double) * 3 * nrev, cudaMemcpyHostToDevice);
@@ -335,8 +332,11 @@ int mct_body_forward(mct_body_ctx *c, int nchains, const int *ncells, const doub
   job.vel = c->vel; job.slow = c->slow; job.ngrids = 2 * c->nslots; job.solve_grid = c->egrid; job.src = c->esrc;
   job.order = c->order; job.method = c->method; job.shift = eik3_shift_for(4.0 * diag / vmin);
   job.T = c->T; job.flags = c->flags; job.list = c->list; job.count = c->count;
-  job.hvn = c->hvn; job.ht = c->ht; job.hst = c->hst; job.hheap = c->hheap;
-  job.hchunk = c->hchunk; job.hcap = c->hcap; job.herr = c->herr;
+  job.hvn = c->hvn; job.herr = c->herr;
+  if (c->method == EIK3_HEAP) {
+    Carve hc(c->hscratch);
+    eik3_heap_take(job, hc, c->hchunk);
+  }
   job.nrev = nrecv; job.rev = c->erecv; job.rev_per_solve = 1; job.solve_rev = c->eset; job.ttime = c->ett;
   int passes = 0;
   rc = launch_eik3(job, s, 100000, &passes, nullptr); if (rc) return rc;

@@ -504,7 +504,7 @@ int mct_eikonal3d_batch(int nsolve, int nx, int ny, int nz, double dx, double dy
   const int method = eik3_resolve_method(ord, mflag == MCT_EIK3_TILES ? EIK3_TILES
                                               : mflag == MCT_EIK3_HEAP ? EIK3_HEAP : EIK3_DEFAULT);
   const size_t nn = (size_t)nx * ny * nz;
-  if (method == EIK3_HEAP && nn >= (size_t)UINT_MAX / 2) return arg_error("mct_eikonal3d_batch: grid too large");
+  if (method == EIK3_HEAP && nn > (size_t)0x3FFFFFFF) return arg_error("mct_eikonal3d_batch: grid too large");
   double vmin = 1e300;
   for (size_t q = 0; q < nn * ngrids; ++q)
     if (vel[q] >= 2.220446049250313e-11 && vel[q] < vmin) vmin = vel[q];
@@ -525,15 +525,13 @@ int mct_eikonal3d_batch(int nsolve, int nx, int ny, int nz, double dx, double dy
   // heap march: as many solves at once as 16 GiB of scratch holds
   const size_t per_solve = eik3_heap_bytes_per_solve(nx, ny, nz);
   const int hchunk = heap ? (int)std::max<size_t>(1, std::min<size_t>(nsolve, (16ull << 30) / per_solve)) : 0;
-  const unsigned hcap = eik3_heap_cap(nx, ny, nz);
   size_t bytes = carve_size({sizeof(double) * nn * ngrids, sizeof(float) * nn * ngrids, sizeof(int) * nsolve,
                              sizeof(double) * 3 * nsolve, sizeof(int) * nT, ntile * nsolve,
                              sizeof(int) * ntile * nsolve, sizeof(int), sizeof(double) * 3 * (nrev + 1),
                              sizeof(double) * (size_t)nsolve * (nrev + 1),
                              tfield ? sizeof(double) * nn * nsolve : 0,
-                             heap ? sizeof(double2) * nn * ngrids : 0, heap ? sizeof(double) * nn * hchunk : 0,
-                             heap ? nn * hchunk : 0, heap ? sizeof(unsigned) * (size_t)hcap * hchunk : 0,
-                             sizeof(int)});
+                             heap ? sizeof(double2) * nn * ngrids : 0,
+                             eik3_heap_scratch_bytes(nx, ny, nz, hchunk), sizeof(int)});
   rc = g_ws.reserve(bytes); if (rc) return rc;
   Carve cv(g_ws.p);
   double *d_vel = cv.take<double>(nn * ngrids);
@@ -549,10 +547,8 @@ int mct_eikonal3d_batch(int nsolve, int nx, int ny, int nz, double dx, double dy
   double *d_tf = tfield ? cv.take<double>(nn * nsolve) : nullptr;
   if (heap) {
     job.hvn = cv.take<double2>(nn * ngrids);
-    job.ht = cv.take<double>(nn * hchunk);
-    job.hst = cv.take<unsigned char>(nn * hchunk);
-    job.hheap = cv.take<unsigned>((size_t)hcap * hchunk);
-    job.hchunk = hchunk; job.hcap = hcap;
+    Carve hc(cv.take<char>(eik3_heap_scratch_bytes(nx, ny, nz, hchunk)));
+    eik3_heap_take(job, hc, hchunk);
   }
   job.herr = cv.take<int>(1);
   std::vector<double> hsrc(3 * (size_t)nsolve), hrev(3 * (size_t)nrev);

@@ -220,38 +220,321 @@ __device__ double solve_high(const Stencil &S, double vel, double nis, const Axe
   return updated;
 }
 
-template <int G>
+// ---------------------------------------------------------------------------
+// The same updates with fewer and shorter FP64 steps. On this GPU a
+// dependent FP64 add or multiply costs ~64 cycles and a division or square
+// root ~550, and the FP64 pipe is shared by the whole SM, so the update's
+// dependent chain bounds each pop and its instruction count bounds many
+// solves at once. Divisions by divisors known in advance (3, and 2A, which
+// takes one of 108 values per launch: the axes of the slots in sorted order
+// and which of them are second order) use Markstein's correction step
+// (P. Markstein, "Computation of elementary functions on the IBM RISC
+// System/6000 processor", IBM J. Res. Dev. 34(1), 1990): with yinv = RN(1/y),
+// q = RN(x*yinv), r = x - q*y (exact with a fused multiply-add) and
+// RN(q + r*yinv) is the correctly rounded x/y, so the results are the same
+// bits as the reference's divisions. Comparisons use the integer order of
+// the bit patterns. Every other operation is the reference's, in its order.
+// ---------------------------------------------------------------------------
+struct Combo {
+  double four_a, two_a, rtwo_a, pad;
+};
+constexpr int kCombos = 36 + 72;   // i = 2: 9 slot-axis pairs x 4 flag sets; i = 3: 9 x 8
+constexpr double kThird = 1.0 / 3.0;
+
+// Correctly rounded x / y given yinv = RN(1/y) (Markstein's correction).
+__device__ __forceinline__ double div_known(double x, double y, double yinv) {
+  const double q = __dmul_rn(x, yinv);
+  const double r = __fma_rn(-q, y, x);
+  return __fma_rn(r, yinv, q);
+}
+
+// A of the reference's quadratic for every candidate shape, summed in the
+// reference's order (0.0 + alpha of slot 0 + alpha of slot 1 [+ slot 2]),
+// with 4A, 2A and RN(1/(2A)).
+__device__ void build_combos(Combo *tab, const Axes &ax, int tid, int nthreads) {
+  for (int c = tid; c < kCombos; c += nthreads) {
+    const int i = c < 36 ? 2 : 3;
+    const int pair = c < 36 ? c / 4 : (c - 36) / 8, flags = c < 36 ? c % 4 : (c - 36) % 8;
+    const int d0 = pair / 3, d1 = pair % 3, d2 = 3 - d0 - d1;
+    Combo cb{0.0, 0.0, 0.0, 0.0};
+    if (d0 != d1) {
+      const int dd[3] = {d0, d1, d2};
+      double A = 0.0;
+      for (int q = 0; q < i; ++q) A += ((flags >> q) & 1) ? ax.a2[dd[q]] : ax.a1[dd[q]];
+      cb.four_a = 4 * A; cb.two_a = 2 * A; cb.rtwo_a = 1.0 / (2 * A);
+    }
+    tab[c] = cb;
+  }
+}
+
+__device__ __forceinline__ int combo_index(int i, int pair, int flags) {
+  return i == 2 ? pair * 4 + (flags & 3) : 36 + pair * 8 + flags;
+}
+
+// quad < 0 on the bit pattern (quad is never NaN here; -0 is not < 0)
+__device__ __forceinline__ bool negative(double x) {
+  const long long b = bits(x);
+  return b < 0 && b != (long long)0x8000000000000000ULL;
+}
+
+__device__ double solve_first_fast(const Stencil &S, double vel, double nis, const Axes &ax, const Combo *tab) {
+  const double INF = __longlong_as_double(kInfBits);
+  double tv[3]; double dummy[3]; int dm[3];
+  int cnt = 0;
+#pragma unroll
+  for (int e = 0; e < 3; ++e) {
+    const bool p0 = (S.pres >> (4 * e)) & 1, p1 = (S.pres >> (4 * e + 2)) & 1;
+    double m;
+    if (p0 && p1) m = lt(S.v[e][0], S.v[e][2]) ? S.v[e][0] : S.v[e][2];
+    else m = p0 ? S.v[e][0] : S.v[e][2];
+    const bool use = !is_inf(m) && lt(m, S.cur);
+    tv[e] = use ? m : INF;
+    dummy[e] = 0.0;
+    dm[e] = e;
+    cnt += use ? 1 : 0;
+  }
+  if (cnt == 0) return INF;
+  sort3(tv, dummy, dm);
+  const int pair = dm[0] * 3 + dm[1];
+  double B = 0.0, C = nis;
+  double updated = 0.0;
+  bool done = false;
+#pragma unroll
+  for (int i = 1; i <= 3; ++i) {
+    if (done || i > cnt) continue;
+    const double alpha = sel3(ax.a1, dm[i - 1]);
+    C += tv[i - 1] * tv[i - 1] * alpha;
+    B += -2.0 * tv[i - 1] * alpha;
+    if (i == 1) {
+      updated = tv[0] + sel3(ax.h, dm[0]) / vel;
+    } else {
+      const Combo &cb = tab[combo_index(i, pair, 0)];
+      const double quad = B * B - cb.four_a * C;
+      updated = negative(quad) ? INF : div_known(-B + sqrt(quad), cb.two_a, cb.rtwo_a);
+    }
+    if (i == cnt) done = true;
+    else if (lt(updated - tv[i < 3 ? i : 2], kMargin)) done = true;
+  }
+  return updated;
+}
+
+__device__ double solve_high_fast(const Stencil &S, double vel, double nis, const Axes &ax, const Combo *tab) {
+  const double INF = __longlong_as_double(kInfBits);
+  double t1[3], t2[3]; int dm[3];
+  int cnt = 0;
+#pragma unroll
+  for (int e = 0; e < 3; ++e) {
+    double minT = DBL_MAX, minT2 = DBL_MAX;
+#pragma unroll
+    for (int sd = 0; sd < 2; ++sd) {
+      const bool pf = (S.pres >> (4 * e + 2 * sd)) & 1, ps = (S.pres >> (4 * e + 2 * sd + 1)) & 1;
+      if (pf) {
+        const double tval = S.v[e][2 * sd];
+        if (!is_inf(tval) && lt(tval, minT)) {
+          minT = tval;
+          minT2 = DBL_MAX;
+          if (ps) {
+            const double tval2 = S.v[e][2 * sd + 1];
+            if (!is_inf(tval2) && le(tval2, tval)) minT2 = tval2;
+          }
+        }
+      }
+    }
+    bool use = false;
+    double u1 = INF, u2 = INF;
+    if (lt(minT2, DBL_MAX) && lt(minT, S.cur)) { use = true; u1 = minT; u2 = minT2; }
+    else if (lt(minT, DBL_MAX) && lt(minT, S.cur)) { use = true; u1 = minT; u2 = INF; }
+    t1[e] = u1; t2[e] = u2; dm[e] = e;
+    cnt += use ? 1 : 0;
+  }
+  if (cnt == 0) return S.cur;
+  sort3(t1, t2, dm);
+  double cC[3], cB[3];
+  int fl = 0;
+#pragma unroll
+  for (int q = 0; q < 3; ++q) {
+    cC[q] = 0.0; cB[q] = 0.0;
+    if (q >= cnt) continue;
+    if (!is_inf(t2[q])) {
+      const double alpha = sel3(ax.a2, dm[q]);
+      const double tt = div_known(4.0 * t1[q] - t2[q], 3.0, kThird);
+      cC[q] = tt * tt * alpha; cB[q] = -2.0 * tt * alpha;
+      fl |= 1 << q;
+    } else {
+      const double alpha = sel3(ax.a1, dm[q]);
+      cC[q] = t1[q] * t1[q] * alpha; cB[q] = -2.0 * t1[q] * alpha;
+    }
+  }
+  double Cs[3], Bs[3];
+  {
+    double B = 0.0, C = nis;
+#pragma unroll
+    for (int q = 0; q < 3; ++q) {
+      C += cC[q]; B += cB[q];
+      Cs[q] = C; Bs[q] = B;
+    }
+  }
+  const int pair = dm[0] * 3 + dm[1];
+  double updated = INF;
+  bool done = false;
+#pragma unroll
+  for (int i = 3; i >= 1; --i) {
+    if (done || i > cnt) continue;
+    double cand;
+    if (i == 1) {
+      cand = t1[0] + sel3(ax.h, dm[0]) / vel;
+    } else {
+      const Combo &cb = tab[combo_index(i, pair, fl)];
+      const double B = Bs[i - 1], C = Cs[i - 1];
+      const double quad = B * B - cb.four_a * C;
+      cand = negative(quad) ? INF : div_known(-B + sqrt(quad), cb.two_a, cb.rtwo_a);
+    }
+    if (!is_inf(cand) && gt(cand - t1[i - 1], kMargin)) { updated = cand; done = true; }
+  }
+  return updated;
+}
+
+// ---------------------------------------------------------------------------
+// The heap. Entries are (key, node) pairs in two arrays, hkey[] and hid[],
+// so that the entries of one heap level are contiguous. The reference's key
+// is the node's live time; it is kept in hkey[] by updating, in place and
+// without a sift, every entry of a node whose time changes (exactly what the
+// reference's comparisons see: the old entry's key drops with the node's
+// time). For that, each node records the heap positions of its first two
+// entries (hpos[2*node + slot], rewritten on every move; hid[] carries the
+// slot in its top two bits). A node that gets a third entry (measured: ~0.3%
+// of nodes) switches to "live" keys: its entries' hkey hold a marker and
+// comparisons read the node's time instead.
+// ---------------------------------------------------------------------------
+constexpr unsigned kNone = 0xFFFFFFFFu;       // hpos: no entry in this slot
+constexpr unsigned kLiveFlag = 0xFFFFFFFEu;   // hpos: node uses live keys
+constexpr unsigned kIdMask = 0x3FFFFFFFu;
+constexpr unsigned kUntracked = 3u;           // slot bits of a live-key entry
+constexpr long long kLiveBits = (long long)0xFFF8000000000001ULL;   // sign set: not a time
+
+__device__ __forceinline__ bool is_live(double k) { return bits(k) < 0; }
+
+struct Heap {
+  double *t;
+  unsigned char *st;
+  double *hkey;
+  unsigned *hid;
+  unsigned *hpos;
+  unsigned n, cap;
+};
+
+// Write entry (key, idw) at position p and record the move.
+__device__ __forceinline__ void put(const Heap &H, unsigned p, double key, unsigned idw) {
+  H.hkey[p] = key;
+  H.hid[p] = idw;
+  const unsigned slot = idw >> 30;
+  if (slot < 2) H.hpos[2 * (idw & kIdMask) + slot] = p;
+}
+
+__device__ __forceinline__ double resolve(const Heap &H, double key, unsigned idw) {
+  return is_live(key) ? H.t[idw & kIdMask] : key;
+}
+
+// push_heap of an entry whose live key is tv.
+__device__ __forceinline__ void heap_push(const Heap &H, unsigned &size, double key, unsigned idw, double tv,
+                                          int &err) {
+  if (size >= H.cap) { err |= HERR_OVERFLOW; return; }
+  unsigned hole = size++;
+  while (hole > 0) {
+    const unsigned parent = (hole - 1) / 2;
+    const double pk = H.hkey[parent];
+    const unsigned pid = H.hid[parent];
+    if ((pid & kIdMask) >= H.n) { err |= HERR_INDEX; break; }
+    if (!gt(resolve(H, pk, pid), tv)) break;
+    put(H, hole, pk, pid);
+    hole = parent;
+  }
+  put(H, hole, key, idw);
+}
+
+// t[j] = tv, then push j (fmm.hpp:103-115 for the source, :138-148 for the
+// updates). fresh: j has no entry yet (it was OPEN).
+__device__ void assign_push(const Heap &H, unsigned &size, unsigned j, double tv, bool fresh, int &err) {
+  H.t[j] = tv;
+  double key = tv;
+  unsigned slot = 0;
+  if (!fresh) {
+    const uint2 hp = reinterpret_cast<const uint2 *>(H.hpos)[j];
+    if (hp.x == kLiveFlag) {
+      key = __longlong_as_double(kLiveBits); slot = kUntracked;
+    } else if (hp.x == kNone) {
+      slot = 0;
+    } else if (hp.y == kNone) {
+      H.hkey[hp.x] = tv;
+      slot = 1;
+    } else {
+      const double live = __longlong_as_double(kLiveBits);
+      H.hkey[hp.x] = live; H.hid[hp.x] = j | (kUntracked << 30);
+      H.hkey[hp.y] = live; H.hid[hp.y] = j | (kUntracked << 30);
+      reinterpret_cast<uint2 *>(H.hpos)[j] = make_uint2(kLiveFlag, kLiveFlag);
+      key = live; slot = kUntracked;
+    }
+  }
+  heap_push(H, size, key, j | (slot << 30), tv, err);
+}
+
+template <int E>
 struct alignas(16) GroupSmem {
-  // subtree below the hole: entries 0..2G-3 by level
-  unsigned sub_id[2 * G];
-  double sub_t[2 * G];
-  // sift-down path: position, node and time of each element moved up
+  // subtree below the hole, entries by level: stored key, live key, node
+  double sub_raw[E];
+  double sub_res[E];
+  unsigned sub_id[E];
+  // sift-down path: position, stored key, live key and node of the element
+  // moved up into each level
   unsigned path_pos[kMaxDepth];
   unsigned path_id[kMaxDepth];
-  double path_t[kMaxDepth];
+  double path_raw[kMaxDepth];
+  double path_res[kMaxDepth];
   // neighbour results
   double nb_t[6];
   unsigned nb_j[6];
   int nb_act[6];          // 0 none, 1 OPEN -> NARROW, 2 improved
-  // walk state
-  unsigned size, len, hole, second, sub_root, top, val;
-  double ttop, tval;
-  int lv, depth, need, active;
+  unsigned size, top, val;
+  double ttop, val_raw, val_res;
+  int active;
 };
 
-template <int G>
-struct Lg { static constexpr int value = G == 8 ? 3 : (G == 16 ? 4 : 5); };
+// Position of subtree entry e (levels 1.. below the subtree root R, level
+// order) in the heap.
+__device__ __forceinline__ unsigned long long sub_pos(unsigned R, int e) {
+  const int L = 31 - __clz(e + 2);
+  return (((unsigned long long)R + 1) << L) - 1 + (unsigned long long)(e + 2 - (1 << L));
+}
 
-// One group of G lanes per solve; kBlock / G solves per block.
-template <int G>
+// One group of G lanes per solve, kBlock / G solves per block; the pop
+// walks subtrees of D levels (2^(D+1) - 2 entries) per round trip.
+//
+// The pop (libstdc++'s pop_heap: adjust, then push_up of the last element)
+// runs on all lanes of the group at once: after one round trip fetches a
+// subtree's keys, each lane decides for its internal nodes of the subtree
+// which child the walk would take (the larger key loses; ties go right;
+// the reference's end-of-heap cases), a ballot gathers the decisions, every
+// lane follows them from the root to get the same path, and the lanes that
+// hold the path's entries move them up. The final push_up of the last
+// element along the path is one more ballot (which path entries are larger)
+// and parallel moves.
+template <int G, int D>
 __global__ void __launch_bounds__(kBlock) heap_march_kernel(Eik3Job job, int s0, int nsol) {
   // at least six lanes: one per neighbour in the update step
   static_assert(G == 8 || G == 16 || G == 32, "group size");
-  constexpr int D = Lg<G>::value;          // subtree levels fetched per round trip
-  constexpr int E = 2 * G - 2;             // subtree entries
-  __shared__ GroupSmem<G> sm_all[kBlock / G];
+  static_assert(D >= 2 && D <= 5, "subtree depth");
+  constexpr int E = (2 << D) - 2;             // subtree entries
+  constexpr int NI = (1 << D) - 1;            // internal nodes of a subtree (<= 31)
+  constexpr int PER = (E + G - 1) / G;        // entries per lane
+  constexpr int PERI = (NI + G - 1) / G;      // internal nodes per lane
+  constexpr int PERD = (kMaxDepth + G - 1) / G;       // path levels per lane
+  static_assert((PERI - 1) * G < 32 && (PERD - 1) * G < 64, "decision masks fit their words");
+  __shared__ GroupSmem<E> sm_all[kBlock / G];
+  __shared__ Combo tab[kCombos];
   const int gi = threadIdx.x / G, gl = threadIdx.x % G;
-  GroupSmem<G> &sm = sm_all[gi];
+  const int gshift = (threadIdx.x % 32) / G * G;      // the group's first lane in the warp
+  const unsigned gmask_bits = G == 32 ? 0xffffffffu : ((1u << G) - 1);
+  GroupSmem<E> &sm = sm_all[gi];
   const int sl = blockIdx.x * (kBlock / G) + gi;          // solve within the chunk
   const bool live = sl < nsol;
   const int s = s0 + (live ? sl : 0);
@@ -259,9 +542,16 @@ __global__ void __launch_bounds__(kBlock) heap_march_kernel(Eik3Job job, int s0,
   const unsigned n = (unsigned)job.nx * job.ny * job.nz;
   const int strideA[3] = {job.ny * job.nz, job.nz, 1};
   const int dimA[3] = {job.nx, job.ny, job.nz};
-  double *t = job.ht + (size_t)(live ? sl : 0) * n;
-  unsigned char *st = job.hst + (size_t)(live ? sl : 0) * n;
-  unsigned *heap = job.hheap + (size_t)(live ? sl : 0) * job.hcap;
+  const size_t so = (size_t)(live ? sl : 0);
+  Heap H;
+  H.t = job.ht + so * n;
+  H.st = job.hst + so * n;
+  H.hkey = job.hkey + so * job.hcap;
+  H.hid = job.hid + so * job.hcap;
+  H.hpos = job.hpos + so * 2 * (size_t)n;
+  H.n = n; H.cap = job.hcap;
+  double *t = H.t;
+  unsigned char *st = H.st;
   const double2 *vn = job.hvn + (size_t)job.solve_grid[s] * n;
   Axes ax;
   {
@@ -273,11 +563,14 @@ __global__ void __launch_bounds__(kBlock) heap_march_kernel(Eik3Job job, int s0,
       ax.a2[q] = 9.0 / 4.0 / (h[q] * h[q]);
     }
   }
+  build_combos(tab, ax, threadIdx.x, blockDim.x);
+  __syncthreads();
   const bool high = job.order == 1;
   int err = 0;
 
-  // ---- source: 8 corners with times dist*2/(v_src + v_corner), pushed in
-  // corner order (solver.hpp:72-92 setInitialPoints, fmm.hpp:103-115)
+  // ---- source: 8 corners with times dist*2/(v_src + v_corner), assigned
+  // and pushed in corner order (solver.hpp:72-92 setInitialPoints,
+  // fmm.hpp:103-115); a corner clamped onto another is assigned again
   if (gl == 0) {
     sm.size = 0; sm.active = live ? 1 : 0;
     if (live) {
@@ -300,18 +593,9 @@ __global__ void __launch_bounds__(kBlock) heap_march_kernel(Eik3Job job, int s0,
         dist = sqrt(dist);
         const unsigned id = (unsigned)e3_nidx(d, vc[0], vc[1], vc[2]);
         const double tv = dist * 2 / (v + vn[id].x);
-        t[id] = tv;
+        const bool fresh = st[id] == kOpen;
         st[id] = kNarrow;
-        // push_heap
-        unsigned hole = size++;
-        while (hole > 0) {
-          const unsigned parent = (hole - 1) / 2;
-          const unsigned pid = heap[parent];
-          if (!gt(t[pid], tv)) break;
-          heap[hole] = pid;
-          hole = parent;
-        }
-        heap[hole] = id;
+        assign_push(H, size, id, tv, fresh, err);
       }
       sm.size = size;
     }
@@ -320,103 +604,195 @@ __global__ void __launch_bounds__(kBlock) heap_march_kernel(Eik3Job job, int s0,
 
   const long long max_pops = 8LL * n + 64;
   for (long long it = 0;; ++it) {
-    // ---------------- pop: start the walk at the root
-    if (gl == 0 && sm.active) {
-      if (sm.size == 0 || it >= max_pops) {
-        if (sm.size != 0) err |= HERR_STEPS;
-        sm.active = 0;
-      } else {
-        sm.len = sm.size - 1;
-        sm.hole = 0; sm.second = 0; sm.sub_root = 0; sm.lv = 0; sm.depth = 0;
-        sm.need = 1;
-      }
+    // ---------------- pop
+    if (gl == 0 && sm.active && (sm.size == 0 || it >= max_pops || err)) {
+      if (sm.size != 0 && !err) err |= HERR_STEPS;
+      sm.active = 0;
     }
     __syncwarp();
     const bool act = sm.active != 0;
     if (!__any_sync(kFull, act)) break;
-    bool first = true;
-    for (;;) {
-      const bool need = act && sm.need;
+    const unsigned size = sm.size;
+    const unsigned len = act ? size - 1 : 0;
+    const unsigned limit = len > 0 ? (len - 1) / 2 : 0;
+    const bool even = (len & 1) == 0;
+    const unsigned last_parent = len >= 2 ? (len - 2) / 2 : kNone;   // the odd case's node
+    unsigned R = 0, hole = 0;
+    int depth = 0;
+    bool need = act;
+
+    // stencil of this lane's neighbour of the popped node, loaded while the
+    // walk runs (times do not change during a pop)
+    Stencil S;
+    S.pres = 0; S.cur = 0.0;
+    unsigned char sj = kFrozen;
+    double2 v2 = make_double2(0.0, 0.0);
+    unsigned j = 0;
+    bool has = false;
+    const int q = gl, ax_q = q >> 1, side = q & 1;
+
+    for (int iter = 0;; ++iter) {
       if (!__any_sync(kFull, need)) break;
+      double kraw[PER], kres[PER]; unsigned kid[PER];
       if (need) {
-        const unsigned R = sm.sub_root, len = sm.len;
-        // round 1: node indices of the subtree (and root / last on the first)
-        unsigned ida = UINT_MAX, idb = UINT_MAX, idx_extra = UINT_MAX;
-        int ea = gl, eb = gl + G;
-        auto pos_of = [&](int e) -> unsigned long long {
-          const int L = 31 - __clz(e + 2);
-          const unsigned long long o = (unsigned long long)(e + 2 - (1 << L));
-          return (((unsigned long long)R + 1) << L) - 1 + o;
-        };
-        if (ea < E) { const unsigned long long p = pos_of(ea); if (p < len) ida = heap[p]; }
-        if (eb < E) { const unsigned long long p = pos_of(eb); if (p < len) idb = heap[p]; }
-        if (first && gl == G - 2) idx_extra = heap[0];
-        if (first && gl == G - 1 && len > 0) idx_extra = heap[len];
-        // round 2: their times
-        auto tload = [&](unsigned id) -> double {
-          if (id == UINT_MAX) return 0.0;
-          if (id >= n) { err |= HERR_INDEX; return 0.0; }
-          return t[id];
-        };
-        const double ta = tload(ida), tb = tload(idb), tx = tload(idx_extra);
-        if (ea < E) { sm.sub_id[ea] = ida; sm.sub_t[ea] = ta; }
-        if (eb < E) { sm.sub_id[eb] = idb; sm.sub_t[eb] = tb; }
-        if (first && gl == G - 2) { sm.top = idx_extra < n ? idx_extra : 0; sm.ttop = tx; }
-        if (first && gl == G - 1) { sm.val = idx_extra < n ? idx_extra : 0; sm.tval = tx; }
+        // one round trip: keys and nodes of the whole subtree (and the root
+        // and last entry on the first)
+#pragma unroll
+        for (int u = 0; u < PER; ++u) {
+          const int e = gl + u * G;
+          kraw[u] = 0.0; kid[u] = kNone;
+          if (e < E) {
+            const unsigned long long p = sub_pos(R, e);
+            if (p < len) { kraw[u] = H.hkey[p]; kid[u] = H.hid[p]; }
+          }
+        }
+        double xr = 0.0; unsigned xi = kNone;
+        if (iter == 0 && gl == G - 2) { xr = H.hkey[0]; xi = H.hid[0]; }
+        if (iter == 0 && gl == G - 1 && len > 0) { xr = H.hkey[len]; xi = H.hid[len]; }
+#pragma unroll
+        for (int u = 0; u < PER; ++u) {
+          const int e = gl + u * G;
+          kres[u] = kraw[u];
+          if (kid[u] != kNone) {
+            if ((kid[u] & kIdMask) >= n) { err |= HERR_INDEX; kid[u] = kNone; }
+            else if (is_live(kraw[u])) kres[u] = t[kid[u] & kIdMask];   // live key (rare)
+          }
+          if (e < E) { sm.sub_raw[e] = kraw[u]; sm.sub_res[e] = kres[u]; sm.sub_id[e] = kid[u]; }
+        }
+        if (xi != kNone) {
+          double xres = xr;
+          if ((xi & kIdMask) >= n) { err |= HERR_INDEX; xi = 0; xres = 0.0; }
+          else if (is_live(xr)) xres = t[xi & kIdMask];
+          if (gl == G - 2) { sm.top = xi & kIdMask; sm.ttop = xres; }
+          else { sm.val = xi; sm.val_raw = xr; sm.val_res = xres; }
+        }
       }
       __syncwarp();
-      if (need && gl == 0) {
-        // walk the subtree: adjust() of libstdc++'s pop_heap
-        const unsigned len = sm.len, limit = (len - 1) / 2;   // len >= 1 here (else no loop)
-        unsigned hole = sm.hole, second = sm.second, R = sm.sub_root;
-        int lv = sm.lv, depth = sm.depth;
-        bool finished = false, reload = false;
-        if (len == 0) finished = true;
-        while (!finished && !reload) {
-          const bool two = second < limit;
-          const bool odd = !two && (len & 1) == 0 && second == (len - 2) / 2;
-          if (!two && !odd) { finished = true; break; }
-          if (lv + 1 > D) { reload = true; break; }
-          const unsigned right = 2 * (second + 1), left = right - 1;
-          const unsigned long long base = (((unsigned long long)R + 1) << (lv + 1)) - 1;
-          const int eL = (1 << (lv + 1)) - 2 + (int)(left - base);
-          unsigned pick; int ep;
-          if (two) {
-            const int eR = eL + 1;
-            if (gt(sm.sub_t[eR], sm.sub_t[eL])) { pick = left; ep = eL; } else { pick = right; ep = eR; }
-          } else {
-            pick = left; ep = eL;
-          }
-          const unsigned id = sm.sub_id[ep];
-          heap[hole] = id;
-          if (depth < kMaxDepth) { sm.path_pos[depth] = hole; sm.path_id[depth] = id; sm.path_t[depth] = sm.sub_t[ep]; }
-          ++depth;
-          second = pick; hole = pick; ++lv;
-          if (odd) { finished = true; break; }
+      if (iter == 0 && act && q < 6) {
+        // issue the stencil loads now; they are consumed after the walk
+        const unsigned top = sm.top;
+        int ci[3];
+        {
+          const unsigned k = top % (unsigned)job.nz, r = top / (unsigned)job.nz;
+          ci[2] = (int)k; ci[1] = (int)(r % (unsigned)job.ny); ci[0] = (int)(r / (unsigned)job.ny);
         }
-        if (reload) {
-          sm.sub_root = hole; sm.lv = 0;
-        }
-        sm.hole = hole; sm.second = second; sm.depth = depth;
-        if (finished) {
-          sm.need = 0;
-          // push_up of the last element from the hole along the path
-          if (sm.size > 1) {
-            const unsigned val = sm.val; const double tval = sm.tval;
-            int k = depth - 1;
-            while (hole > 0 && k >= 0 && k < kMaxDepth && gt(sm.path_t[k], tval)) {
-              heap[hole] = sm.path_id[k];
-              hole = sm.path_pos[k];
-              --k;
+        const int cq = seli(ci, ax_q) + (side ? 1 : -1);
+        if (cq >= 0 && cq < seli(dimA, ax_q)) {
+          has = true;
+          const unsigned sq = (unsigned)seli(strideA, ax_q);
+          j = side ? top + sq : top - sq;
+          int cj[3];
+#pragma unroll
+          for (int e = 0; e < 3; ++e) cj[e] = e == ax_q ? cq : ci[e];
+          sj = st[j];
+          v2 = vn[j];
+          S.cur = t[j];
+#pragma unroll
+          for (int e = 0; e < 3; ++e) {
+            const int off[4] = {-1, -2, 1, 2};
+#pragma unroll
+            for (int m = 0; m < 4; ++m) {
+              S.v[e][m] = 0.0;
+              if (!high && (m == 1 || m == 3)) continue;
+              const int c = cj[e] + off[m];
+              if (c >= 0 && c < dimA[e]) {
+                S.pres |= 1u << (4 * e + m);
+                S.v[e][m] = t[(long long)j + (long long)off[m] * strideA[e]];
+              }
             }
-            heap[hole] = val;
           }
-          sm.size = sm.size - 1;
         }
       }
-      first = false;
+      // the walk's decision at each internal node of the subtree
+      unsigned m_two = 0, m_odd = 0, m_right = 0;
+#pragma unroll
+      for (int u = 0; u < PERI; ++u) {
+        const int k = gl + u * G;
+        bool two = false, odd = false, right = false;
+        if (need && k < NI) {
+          const unsigned long long pk = k == 0 ? R : sub_pos(R, k - 1);
+          if (k == 0 || pk < len) {
+            two = pk < limit;
+            odd = !two && even && pk == last_parent;
+            if (two) right = !gt(sm.sub_res[2 * k + 1], sm.sub_res[2 * k]);
+          }
+        }
+        const unsigned b2 = (__ballot_sync(kFull, two) >> gshift) & gmask_bits;
+        const unsigned bo = (__ballot_sync(kFull, odd) >> gshift) & gmask_bits;
+        const unsigned br = (__ballot_sync(kFull, right) >> gshift) & gmask_bits;
+        m_two |= b2 << (u * G); m_odd |= bo << (u * G); m_right |= br << (u * G);
+      }
+      if (need) {
+        // follow the decisions from the subtree root (same on every lane)
+        int k = 0, steps = 0, lastc = -1;
+        bool ended = false;
+        unsigned long long chosen = 0;
+#pragma unroll
+        for (int lvl = 0; lvl < D; ++lvl) {
+          if (ended) continue;
+          int c;
+          if ((m_two >> k) & 1) c = 2 * k + (int)((m_right >> k) & 1);
+          else if ((m_odd >> k) & 1) { c = 2 * k; ended = true; }
+          else { ended = true; continue; }
+          chosen |= 1ull << c; lastc = c; ++steps;
+          k = c + 1;
+        }
+        // the lanes holding the path's entries move them up one level
+#pragma unroll
+        for (int u = 0; u < PER; ++u) {
+          const int e = gl + u * G;
+          if (e < E && ((chosen >> e) & 1)) {
+            const unsigned p = (unsigned)sub_pos(R, e);
+            const unsigned parent = (p - 1) / 2;
+            put(H, parent, kraw[u], kid[u]);
+            const int dl = depth + (31 - __clz(e + 2)) - 1;
+            if (dl < kMaxDepth) {
+              sm.path_pos[dl] = parent; sm.path_id[dl] = kid[u]; sm.path_raw[dl] = kraw[u]; sm.path_res[dl] = kres[u];
+            }
+          }
+        }
+        depth += steps;
+        if (steps > 0) hole = (unsigned)sub_pos(R, lastc);
+        if (ended) {
+          need = false;
+        } else {
+          // D levels walked: continue below the new hole if it has children
+          const bool more = hole < limit || (even && hole == last_parent);
+          if (more) R = hole; else need = false;
+        }
+      }
       __syncwarp();
     }
+
+    // push_up of the last element from the hole along the path
+    const bool up = act && size > 1;
+    unsigned long long bmask = 0;     // bit k: path entry k is larger than the last element
+    {
+      const double vres = up ? sm.val_res : 0.0;
+#pragma unroll
+      for (int u = 0; u < PERD; ++u) {
+        const int k = gl + u * G;
+        const bool b = up && k < depth && k < kMaxDepth && gt(sm.path_res[k], vres);
+        bmask |= (unsigned long long)((__ballot_sync(kFull, b) >> gshift) & gmask_bits) << (u * G);
+      }
+    }
+    if (up) {
+      const int dd = depth < kMaxDepth ? depth : kMaxDepth;
+      const unsigned long long valid = (1ull << dd) - 1;   // dd <= 33
+      const unsigned long long F = ~bmask & valid;
+      const int m = F == 0 ? 0 : 64 - __clzll(F);        // entries m..depth-1 move down one level
+#pragma unroll
+      for (int u = 0; u < PERD; ++u) {
+        const int k = gl + u * G;
+        if (k >= m && k < dd) {
+          const unsigned to = k + 1 < dd ? sm.path_pos[k + 1] : hole;
+          put(H, to, sm.path_raw[k], sm.path_id[k]);
+        }
+      }
+      if (gl == 0) put(H, m < dd ? sm.path_pos[m] : hole, sm.val_raw, sm.val);
+    }
+    if (act && gl == 0) sm.size = size - 1;
+    __syncwarp();
 
     // ---------------- update the six neighbours of the popped node
     const unsigned top = sm.top;
@@ -425,50 +801,16 @@ __global__ void __launch_bounds__(kBlock) heap_march_kernel(Eik3Job job, int s0,
       st[top] = kFrozen;
       if (is_inf(ttop)) err |= HERR_INF;
     }
-    int ci[3];
-    {
-      const unsigned k = top % (unsigned)job.nz, r = top / (unsigned)job.nz;
-      ci[2] = (int)k; ci[1] = (int)(r % (unsigned)job.ny); ci[0] = (int)(r / (unsigned)job.ny);
-    }
-    Stencil S;
-    double nt = 0.0, vel = 0.0, nis = 0.0;
+    double nt = 0.0;
     bool valid = false;
     int act_code = 0;
-    unsigned char sj = kFrozen;
-    unsigned j = 0;
-    const int q = gl, ax_q = q >> 1, side = q & 1;
     if (act && q < 6) {
-      const int cq = seli(ci, ax_q) + (side ? 1 : -1);
-      if (cq >= 0 && cq < seli(dimA, ax_q)) {
-        const unsigned sq = (unsigned)seli(strideA, ax_q);
-        j = side ? top + sq : top - sq;
-        int cj[3];
-#pragma unroll
-        for (int e = 0; e < 3; ++e) cj[e] = e == ax_q ? cq : ci[e];
-        // all loads of the stencil at once
-        sj = st[j];
-        const double2 v2 = vn[j];
-        S.cur = t[j];
-        S.pres = 0;
-#pragma unroll
-        for (int e = 0; e < 3; ++e) {
-          const int off[4] = {-1, -2, 1, 2};
-#pragma unroll
-          for (int m = 0; m < 4; ++m) {
-            S.v[e][m] = 0.0;
-            if (!high && (m == 1 || m == 3)) continue;
-            const int c = cj[e] + off[m];
-            if (c >= 0 && c < dimA[e]) {
-              S.pres |= 1u << (4 * e + m);
-              S.v[e][m] = t[(long long)j + (long long)off[m] * strideA[e]];
-            }
-          }
-        }
-        vel = v2.x; nis = v2.y;
+      if (has) {
+        const double vel = v2.x, nis = v2.y;
         valid = sj != kFrozen && !(vel < kMargin);
         if (valid) {
-          nt = high ? solve_high(S, vel, nis, ax) : solve_first(S, vel, nis, ax);
-          if (sj == kNarrow) act_code = (nt + kMargin < S.cur) ? 2 : 0;   // isTimeBetterThan
+          nt = high ? solve_high_fast(S, vel, nis, ax, tab) : solve_first_fast(S, vel, nis, ax, tab);
+          if (sj == kNarrow) act_code = lt(nt + kMargin, S.cur) ? 2 : 0;   // isTimeBetterThan
           else act_code = 1;
         }
       }
@@ -491,8 +833,8 @@ __global__ void __launch_bounds__(kBlock) heap_march_kernel(Eik3Job job, int s0,
       }
       if (__any_sync(kFull, redo)) {
         if (redo) {
-          nt = solve_high(S, vel, nis, ax);
-          const int code = (sj == kNarrow) ? ((nt + kMargin < S.cur) ? 2 : 0) : 1;
+          nt = solve_high_fast(S, v2.x, v2.y, ax, tab);
+          const int code = (sj == kNarrow) ? (lt(nt + kMargin, S.cur) ? 2 : 0) : 1;
           sm.nb_act[q] = code; sm.nb_t[q] = nt;
         }
         __syncwarp();
@@ -500,30 +842,15 @@ __global__ void __launch_bounds__(kBlock) heap_march_kernel(Eik3Job job, int s0,
     }
     // ---------------- apply in the reference's order: time, state, push
     if (act && gl == 0) {
-      unsigned size = sm.size;
-      bool stop = false;
-      for (int r = 0; r < 6 && !stop; ++r) {
+      unsigned sz = sm.size;
+      for (int r = 0; r < 6 && !err; ++r) {
         const int code = sm.nb_act[r];
         if (code == 0) continue;
         const unsigned jj = sm.nb_j[r];
-        const double tv = sm.nb_t[r];
-        t[jj] = tv;
         if (code == 1) st[jj] = kNarrow;
-        if (size >= job.hcap) { err |= HERR_OVERFLOW; stop = true; break; }
-        unsigned hole = size++;
-        while (hole > 0) {
-          const unsigned parent = (hole - 1) / 2;
-          const unsigned pid = heap[parent];
-          if (pid >= n) { err |= HERR_INDEX; break; }
-          if (!gt(t[pid], tv)) break;
-          heap[hole] = pid;
-          hole = parent;
-        }
-        heap[hole] = jj;
+        assign_push(H, sz, jj, sm.nb_t[r], code == 1, err);
       }
-      sm.size = size;
-      if (stop) sm.active = 0;
-      // clear for the next step (lanes 0..5 rewrite them when active)
+      sm.size = sz;
       for (int r = 0; r < 6; ++r) sm.nb_act[r] = 0;
     }
     __syncwarp();
@@ -538,11 +865,12 @@ __global__ void vn_kernel(const double *vel, double2 *vn, size_t n) {
   }
 }
 
-__global__ void heap_fill_kernel(double *t, unsigned char *st, size_t n) {
+__global__ void heap_fill_kernel(double *t, unsigned char *st, uint2 *hpos, size_t n) {
   const double INF = __longlong_as_double(kInfBits);
   for (size_t q = blockIdx.x * (size_t)blockDim.x + threadIdx.x; q < n; q += (size_t)gridDim.x * blockDim.x) {
     t[q] = INF;
     st[q] = kOpen;
+    hpos[q] = make_uint2(kNone, kNone);
   }
 }
 
@@ -564,15 +892,69 @@ __global__ void heap_readout_kernel(Eik3Job job, int s0, int nsol) {
   }
 }
 
-int g_group = 8;
+int g_variant = 0;       // diagnostics: lane-group / subtree-depth variant
 int g_chunk_cap = 0;     // diagnostics: solves per launch at most (0: no cap)
 
-template <int G>
-int launch_group(const Eik3Job &job, int s0, int nsol, cudaStream_t s) {
+template <int G, int D>
+int launch_variant(const Eik3Job &job, int s0, int nsol, cudaStream_t s) {
   constexpr int per_block = kBlock / G;
-  heap_march_kernel<G><<<(nsol + per_block - 1) / per_block, kBlock, 0, s>>>(job, s0, nsol);
+  heap_march_kernel<G, D><<<(nsol + per_block - 1) / per_block, kBlock, 0, s>>>(job, s0, nsol);
   MCT_CUDA_TRY(cudaGetLastError());
   return MCT_OK;
+}
+
+int launch_march(const Eik3Job &job, int s0, int nsol, cudaStream_t s) {
+  switch (g_variant) {
+    case 1: return launch_variant<8, 4>(job, s0, nsol, s);
+    case 2: return launch_variant<16, 5>(job, s0, nsol, s);
+    case 3: return launch_variant<32, 5>(job, s0, nsol, s);
+    case 4: return launch_variant<16, 4>(job, s0, nsol, s);
+    case 5: return launch_variant<8, 3>(job, s0, nsol, s);
+    default: return launch_variant<8, 5>(job, s0, nsol, s);
+  }
+}
+
+// Random stencils shaped like a marching front (times near a base time,
+// some neighbours unreached or outside the grid) for the update check.
+__device__ unsigned long long mix64(unsigned long long x) {
+  x ^= x >> 33; x *= 0xff51afd7ed558ccdULL; x ^= x >> 33; x *= 0xc4ceb9fe1a85ec53ULL; x ^= x >> 33;
+  return x;
+}
+__device__ double unit(unsigned long long &rs) {
+  rs = mix64(rs + 0x9E3779B97F4A7C15ULL);
+  return (double)(rs >> 11) * (1.0 / 9007199254740992.0);
+}
+
+__global__ void update_check_kernel(int order, Axes ax, unsigned long long count, unsigned long long seed,
+                                    unsigned long long *out) {
+  __shared__ Combo tab[kCombos];
+  build_combos(tab, ax, threadIdx.x, blockDim.x);
+  __syncthreads();
+  const double INF = __longlong_as_double(kInfBits);
+  for (unsigned long long k = blockIdx.x * (unsigned long long)blockDim.x + threadIdx.x; k < count;
+       k += (unsigned long long)gridDim.x * blockDim.x) {
+    unsigned long long rs = mix64(k * 7 + seed);
+    Stencil S;
+    const double T = 0.2 + 30.0 * unit(rs);
+    S.pres = 0;
+    for (int e = 0; e < 3; ++e)
+      for (int m = 0; m < 4; ++m) {
+        S.v[e][m] = 0.0;
+        if (order == 0 && (m == 1 || m == 3)) continue;
+        if (unit(rs) < 0.1) continue;
+        S.pres |= 1u << (4 * e + m);
+        const double spread = (m == 1 || m == 3) ? 0.5 : 0.25;
+        const double v = unit(rs) < 0.25 ? INF : T + spread * (2 * unit(rs) - 1);
+        S.v[e][m] = v < 0 ? 0.0 : v;
+      }
+    S.cur = unit(rs) < 0.4 ? INF : T + 0.3 * unit(rs);
+    const double vel = 1.0 + 7.0 * unit(rs);
+    const double nis = -1.0 / (vel * vel);
+    const double a = order ? solve_high(S, vel, nis, ax) : solve_first(S, vel, nis, ax);
+    const double b = order ? solve_high_fast(S, vel, nis, ax, tab) : solve_first_fast(S, vel, nis, ax, tab);
+    if (bits(a) != bits(b)) atomicAdd(out, 1ULL);
+    if (!is_inf(a)) atomicAdd(out + 1, 1ULL);
+  }
 }
 
 }  // namespace
@@ -583,19 +965,42 @@ int eik3_resolve_method(int order, int method) {
 }
 
 unsigned eik3_heap_cap(int nx, int ny, int nz) {
-  // the reference reserves one entry per node; the live narrow band with
-  // its stale entries stays far below that
-  return (unsigned)((size_t)nx * ny * nz);
+  // the live narrow band with its stale entries stays far below half the
+  // nodes (measured: under 3% on 101x101x51 grids); overflow is an error
+  const size_t nn = (size_t)nx * ny * nz;
+  return (unsigned)std::max<size_t>(64, nn / 2);
 }
 
 size_t eik3_heap_bytes_per_solve(int nx, int ny, int nz) {
   const size_t nn = (size_t)nx * ny * nz;
-  return carve_size({sizeof(double) * nn, nn, sizeof(unsigned) * (size_t)eik3_heap_cap(nx, ny, nz)});
+  const size_t cap = eik3_heap_cap(nx, ny, nz);
+  return carve_size({sizeof(double) * nn, nn, sizeof(double) * cap, sizeof(unsigned) * cap,
+                     2 * sizeof(unsigned) * nn});
+}
+
+void eik3_heap_take(Eik3Job &job, Carve &cv, int chunk) {
+  const size_t nn = (size_t)job.nx * job.ny * job.nz;
+  const size_t cap = eik3_heap_cap(job.nx, job.ny, job.nz);
+  const size_t c = chunk > 0 ? (size_t)chunk : 0;
+  job.ht = cv.take<double>(nn * c);
+  job.hst = cv.take<unsigned char>(nn * c);
+  job.hkey = cv.take<double>(cap * c);
+  job.hid = cv.take<unsigned>(cap * c);
+  job.hpos = cv.take<unsigned>(2 * nn * c);
+  job.hchunk = chunk; job.hcap = (unsigned)cap;
+}
+
+size_t eik3_heap_scratch_bytes(int nx, int ny, int nz, int chunk) {
+  const size_t nn = (size_t)nx * ny * nz;
+  const size_t cap = eik3_heap_cap(nx, ny, nz);
+  const size_t c = chunk > 0 ? (size_t)chunk : 0;
+  return carve_size({sizeof(double) * nn * c, nn * c, sizeof(double) * cap * c, sizeof(unsigned) * cap * c,
+                     2 * sizeof(unsigned) * nn * c});
 }
 
 int launch_eik3_heap(Eik3Job &job, cudaStream_t s, double *tfield) {
   const size_t nn = (size_t)job.nx * job.ny * job.nz;
-  if (nn >= (size_t)UINT_MAX / 2 || job.hchunk < 1 || job.hcap < 8) {
+  if (nn > (size_t)kIdMask || job.hchunk < 1 || job.hcap < 8) {
     mct_set_error("launch_eik3_heap", "grid too large or no heap scratch", __FILE__, __LINE__);
     return MCT_ERR_ARG;
   }
@@ -609,11 +1014,9 @@ int launch_eik3_heap(Eik3Job &job, cudaStream_t s, double *tfield) {
   const int per = (job.nsolve + nchunks - 1) / nchunks;
   for (int s0 = 0; s0 < job.nsolve; s0 += per) {
     const int nsol = std::min(per, job.nsolve - s0);
-    heap_fill_kernel<<<1024, 256, 0, s>>>(job.ht, job.hst, nn * nsol);
+    heap_fill_kernel<<<1024, 256, 0, s>>>(job.ht, job.hst, reinterpret_cast<uint2 *>(job.hpos), nn * nsol);
     MCT_CUDA_TRY(cudaGetLastError());
-    int rc = g_group == 32 ? launch_group<32>(job, s0, nsol, s)
-           : g_group == 16 ? launch_group<16>(job, s0, nsol, s)
-           : launch_group<8>(job, s0, nsol, s);
+    int rc = launch_march(job, s0, nsol, s);
     if (rc) return rc;
     if (job.nrev > 0) {
       heap_readout_kernel<<<dim3((job.nrev + 127) / 128, nsol), 128, 0, s>>>(job, s0, nsol);
@@ -637,11 +1040,12 @@ int launch_eik3_heap(Eik3Job &job, cudaStream_t s, double *tfield) {
   return MCT_OK;
 }
 
-// Diagnostics (not part of the public header): lanes per solve of the heap
-// march (8, 16 or 32); returns the previous value.
-extern "C" int mct_debug_eik3_heap_group(int g) {
-  const int old = g_group;
-  if (g == 8 || g == 16 || g == 32) g_group = g;
+// Diagnostics (not part of the public header): lane-group / subtree-depth
+// variant of the heap march (0: 8 lanes, 5 levels; 1: 8/4; 2: 16/5; 3: 32/5;
+// 4: 16/4; 5: 8/3); returns the previous value.
+extern "C" int mct_debug_eik3_heap_variant(int v) {
+  const int old = g_variant;
+  if (v >= 0 && v <= 5) g_variant = v;
   return old;
 }
 
@@ -651,4 +1055,28 @@ extern "C" int mct_debug_eik3_heap_chunk(int n) {
   const int old = g_chunk_cap;
   g_chunk_cap = n > 0 ? n : 0;
   return old;
+}
+
+// Diagnostics (not part of the public header): evaluates count random
+// front-like stencils with both the reference-order FP64 update and the
+// update the march uses (Markstein divisions, integer comparisons) and
+// counts results whose bits differ (out[0]) and finite results (out[1]).
+extern "C" int mct_debug_eik3_update_check(int order, double dx, double dy, double dz, unsigned long long count,
+                                           unsigned long long seed, unsigned long long *out) {
+  Axes ax;
+  const double h[3] = {dx, dy, dz};
+  for (int q = 0; q < 3; ++q) {
+    ax.h[q] = h[q];
+    ax.a1[q] = 1.0 / (h[q] * h[q]);
+    ax.a2[q] = 9.0 / 4.0 / (h[q] * h[q]);
+  }
+  unsigned long long *d = nullptr;
+  MCT_CUDA_TRY(cudaMalloc(&d, 2 * sizeof(unsigned long long)));
+  MCT_CUDA_TRY(cudaMemset(d, 0, 2 * sizeof(unsigned long long)));
+  update_check_kernel<<<152 * 8, 256>>>(order, ax, count, seed, d);
+  cudaError_t e = cudaGetLastError();
+  if (e == cudaSuccess) e = cudaMemcpy(out, d, 2 * sizeof(unsigned long long), cudaMemcpyDeviceToHost);
+  cudaFree(d);
+  MCT_CUDA_TRY(e);
+  return MCT_OK;
 }

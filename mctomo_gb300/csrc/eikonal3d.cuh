@@ -27,7 +27,9 @@ struct Eik3Job {
   // heap march scratch (solves run in chunks of hchunk)
   double *ht;                     // [hchunk][nn] arrival times
   unsigned char *hst;             // [hchunk][nn] OPEN / NARROW / FROZEN
-  unsigned *hheap;                // [hchunk][hcap] heap of node indices
+  double *hkey;                   // [hchunk][hcap] heap entry keys
+  unsigned *hid;                  // [hchunk][hcap] heap entry nodes (+ position slot)
+  unsigned *hpos;                 // [hchunk][nn][2] heap positions of a node's entries
   double2 *hvn;                   // [ngrids][nn] (velocity, -1/velocity^2)
   int hchunk;
   unsigned hcap;
@@ -45,8 +47,12 @@ int eik3_shift_for(double tmax_bound);
 // Resolves EIK3_DEFAULT: the heap march for the mixed second-order scheme
 // (whose result depends on the acceptance order), tiles for first order.
 int eik3_resolve_method(int order, int method);
-// Heap-march scratch per solve (times, states, heap) and per velocity grid.
+// Heap-march scratch per solve (times, states, heap, entry positions), the
+// bytes for a chunk of solves, and carving it (sets ht..hpos, hchunk, hcap).
+struct Carve;
 size_t eik3_heap_bytes_per_solve(int nx, int ny, int nz);
+size_t eik3_heap_scratch_bytes(int nx, int ny, int nz, int chunk);
+void eik3_heap_take(Eik3Job &job, Carve &cv, int chunk);
 unsigned eik3_heap_cap(int nx, int ny, int nz);
 int launch_eik3(Eik3Job &job, cudaStream_t s, int max_passes, int *passes_out, double *tfield);
 int launch_eik3_heap(Eik3Job &job, cudaStream_t s, double *tfield);

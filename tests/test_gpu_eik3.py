@@ -99,14 +99,15 @@ def test_eikonal3d_batch_tiles_many_sources_and_grids(orc, gpulib):
 # ---------------------------------------------------------------- heap march
 
 @pytest.mark.parametrize("order", [0, 1])
-@pytest.mark.parametrize("group", [8, 32, 16])
-def test_heap_march_bit_exact(orc, gpulib, order, group):
-    rng = np.random.default_rng(20 + order + group)
+@pytest.mark.parametrize("variant", [0, 1, 2, 3, 4, 5])
+def test_heap_march_bit_exact(orc, gpulib, order, variant):
+    # variants: lanes per solve x subtree levels per round trip
+    rng = np.random.default_rng(20 + order + 7 * variant)
     shape = (29, 23, 17)
     h = np.array([0.5, 0.45, 0.4]); lo = np.array([-3.0, 1.0, 0.0])
     vel = layered_voronoi(rng, shape, h, 50, (3.0, 7.5))
     ext = (np.array(shape) - 1) * h
-    old = gpulib.mct_debug_eik3_heap_group(group)
+    old = gpulib.mct_debug_eik3_heap_variant(variant)
     try:
         for trial in range(2):
             src = lo + ext * rng.uniform(0.0, 1.0, 3)
@@ -118,7 +119,7 @@ def test_heap_march_bit_exact(orc, gpulib, order, group):
             np.testing.assert_array_equal(gf, ef)
             np.testing.assert_array_equal(got, exp)
     finally:
-        gpulib.mct_debug_eik3_heap_group(old)
+        gpulib.mct_debug_eik3_heap_variant(old)
 
 
 def test_heap_march_is_the_order1_default(orc, gpulib):
@@ -195,3 +196,19 @@ def test_heap_march_batch_chunks(orc, gpulib):
         exp, ef = oracle_fmm(orc, vels[grid_of[i]], h, lo, srcs[i], rev, 1)
         np.testing.assert_array_equal(gf[i], ef)
         np.testing.assert_array_equal(got[i], exp)
+
+
+@pytest.mark.parametrize("order", [0, 1])
+@pytest.mark.parametrize("h", [(0.5, 0.5, 0.5), (0.5, 0.45, 0.4)])
+def test_heap_march_update_bits(gpulib, order, h):
+    # the march's update (Markstein divisions for the divisors known in
+    # advance, integer comparisons) against the reference-order FP64 update
+    # on 2^26 random front-like stencils: no result may differ in any bit
+    fn = gpulib.mct_debug_eik3_update_check
+    fn.restype = ctypes.c_int
+    fn.argtypes = [ctypes.c_int, ctypes.c_double, ctypes.c_double, ctypes.c_double, ctypes.c_ulonglong,
+                   ctypes.c_ulonglong, ctypes.c_void_p]
+    out = np.zeros(2, np.uint64)
+    assert fn(order, *h, 1 << 26, 12345 + order, out.ctypes.data) == 0
+    assert out[1] > (1 << 25)          # most stencils give a finite time
+    assert out[0] == 0, "%d of %d updates differ" % (out[0], 1 << 26)
