@@ -15,31 +15,35 @@
 // not, so the result depends on the order in which nodes are accepted; only
 // the same sequence of pops, with the same floating-point operations, gives
 // the same times. That sequence is inherently serial, so here the
-// parallelism is across solves: one group of G lanes marches one solve, and
-// the lanes of a group share the work of each step:
+// parallelism is across solves: one group of G lanes (8 or 32) marches one
+// solve, and the lanes of a group share the work of each step:
 //
-//  * pop: the hole-moving sift-down needs, per level, the two children's
-//    node indices and then their times (two dependent loads). The G lanes
-//    fetch a whole subtree of depth log2(G) below the hole at once (indices,
-//    then times: two memory round trips for log2(G) levels), and the group
-//    leader walks it in shared memory. The final sift-up of the moved last
-//    element runs along the path just walked, whose entries are known.
+//  * pop: the heap keeps each entry's key beside its node index (kept equal
+//    to the node's live time, see the heap section below), so one round
+//    trip fetches the keys of a whole subtree of D levels below the hole.
+//    Every lane decides the walk's step at its internal nodes of the
+//    subtree, a ballot gathers the decisions, all lanes follow them to the
+//    same path, and the lanes holding the path's entries move them up; the
+//    final sift-up of the last element along the path is one more ballot.
 //  * update: lanes 0..5 take the six neighbours of the popped node (x-, x+,
-//    y-, y+, z-, z+), load their whole stencils (up to 12 times, state,
-//    velocity) in one round trip and evaluate the reference's update in
-//    FP64 with its exact operation order. Neighbours on different axes do
-//    not read each other; the + neighbour of an axis can read the -
-//    neighbour (two steps away in the second-order stencil), so it is
-//    evaluated again with the new value in the rare case that value enters
-//    its stencil (it is at most the popped time).
+//    y-, y+, z-, z+), issue the loads of their whole stencils (up to 12
+//    times, state, velocity) while the pop runs, and evaluate the
+//    reference's update in FP64 with its exact operation order. Neighbours
+//    on different axes do not read each other; the + neighbour of an axis
+//    can read the - neighbour (two steps away in the second-order stencil),
+//    so it is evaluated again with the new value in the rare case that
+//    value enters its stencil (it is at most the popped time).
 //  * accept: the leader applies the results in the reference's order (write
-//    the time, then push, for each neighbour in turn), so every comparison
-//    in every push sees exactly the live times the reference's push sees.
+//    the time, update the keys of the node's older entries, push), so every
+//    comparison in every push sees exactly the keys the reference's push
+//    sees.
 //
 // Comparisons between times are integer comparisons of the IEEE bit
 // patterns (all times are >= 0 or +inf), which are exact and keep them off
 // the FP64 pipe; the arithmetic of the update is the reference's, FP64,
-// without contraction (the library is built with -fmad=false).
+// without contraction (the library is built with -fmad=false), except that
+// divisions by divisors known in advance take Markstein's FMA correction,
+// which returns the same correctly rounded quotient in fewer steps.
 //
 // Loops are bounded: the march stops with an error bit after 8 * nodes
 // pops (every pop matches one push; a node is pushed once when reached and
@@ -892,7 +896,7 @@ __global__ void heap_readout_kernel(Eik3Job job, int s0, int nsol) {
   }
 }
 
-int g_variant = 0;       // diagnostics: lane-group / subtree-depth variant
+int g_variant = -1;      // diagnostics: lane-group / subtree-depth variant (-1: by batch size)
 int g_chunk_cap = 0;     // diagnostics: solves per launch at most (0: no cap)
 
 template <int G, int D>
@@ -904,7 +908,12 @@ int launch_variant(const Eik3Job &job, int s0, int nsol, cudaStream_t s) {
 }
 
 int launch_march(const Eik3Job &job, int s0, int nsol, cudaStream_t s) {
-  switch (g_variant) {
+  // Few solves: the march's latency decides, and 32 lanes per solve give
+  // the shortest steps. Many solves: the SM's shared FP64 pipe decides, and
+  // 8-lane groups let four solves share each FP64 instruction (measured on
+  // 101x101x51: 3.7 s vs 4.4 s for one solve, 7.6 s vs 11.2 s for 3840).
+  const int v = g_variant >= 0 ? g_variant : (nsol >= 4 * 152 ? 1 : 3);
+  switch (v) {
     case 1: return launch_variant<8, 4>(job, s0, nsol, s);
     case 2: return launch_variant<16, 5>(job, s0, nsol, s);
     case 3: return launch_variant<32, 5>(job, s0, nsol, s);
@@ -1042,10 +1051,11 @@ int launch_eik3_heap(Eik3Job &job, cudaStream_t s, double *tfield) {
 
 // Diagnostics (not part of the public header): lane-group / subtree-depth
 // variant of the heap march (0: 8 lanes, 5 levels; 1: 8/4; 2: 16/5; 3: 32/5;
-// 4: 16/4; 5: 8/3); returns the previous value.
+// 4: 16/4; 5: 8/3; -1: chosen by the number of solves); returns the previous
+// value.
 extern "C" int mct_debug_eik3_heap_variant(int v) {
   const int old = g_variant;
-  if (v >= 0 && v <= 5) g_variant = v;
+  if (v >= -1 && v <= 5) g_variant = v;
   return old;
 }
 

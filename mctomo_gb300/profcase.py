@@ -2,6 +2,7 @@
 
     python -m mctomo_gb300.profcase fm2d [--precision P] [--maps M] [--repeat R]
     python -m mctomo_gb300.profcase eik3 [--order O]
+    python -m mctomo_gb300.profcase eik3heap [--order O] [--solves N]
     python -m mctomo_gb300.profcase disp [--precision P] [--columns N]
     python -m mctomo_gb300.profcase grid
 
@@ -9,7 +10,8 @@ fm2d: M Voronoi phase maps of 41 x 41 vertices (1 km spacing), 50 stations
 between 2 and 38 km, every station pair once, source refinement 4 x over
 8 cells (the surface-wave likelihood's fm2d settings); R calls of
 mct_modrays_batch. eik3: 8 velocity grids of 101 x 101 x 51 nodes (0.5 km),
-120 solves. disp: N layered columns (12-40 layers, no low-velocity layers),
+120 solves. eik3heap: the exact heap march, N solves (default 8) on 4
+Voronoi grids of 51 x 51 x 26 nodes (0.5 km, velocities 3-7.5 km/s). disp: N layered columns (12-40 layers, no low-velocity layers),
 20 Rayleigh fundamental-mode phase periods log-spaced 0.5-5 s, the surface
 likelihood's search increment 1e-3 km/s. grid: nearest-nucleus gridding of a
 101 x 101 x 51 grid over 50 x 50 x 25 km from 800 nuclei. Each case prints
@@ -55,6 +57,28 @@ def eik3(order=0):
     print(f"eik3 order={order} solves={nsolve} passes={passes} call_s={dt:.4f} t00={tt[0, 0]:.6f}")
 
 
+def eik3heap(order=1, solves=8):
+    rng = np.random.default_rng(4)
+    shape = (51, 51, 26)
+    h = (0.5, 0.5, 0.5)
+    lo = np.zeros(3); hi = (np.array(shape) - 1) * 0.5
+    X, Y, Z = np.meshgrid(*[np.arange(k) * 0.5 for k in shape], indexing="ij")
+    nodes = np.stack([X.ravel(), Y.ravel(), Z.ravel()], 1)
+    vels = []
+    for g in range(4):
+        pts, par = synthetic.voronoi_model_3d(rng, 120, lo, hi, (3.0 / 1.73, 7.5 / 1.73))
+        d = ((nodes[:, None, :] - pts[None]) ** 2).sum(-1)
+        vels.append((par[:, 1] * 1.73)[d.argmin(1)].reshape(shape))
+    vels = np.stack(vels)
+    grid = (np.arange(solves) % 4).astype(np.int32)
+    srcs = rng.uniform([1, 1, 0], [24, 24, 0.2], (solves, 3))
+    rev = rng.uniform([1, 1, 1], [24, 24, 12], (40, 3))
+    t0 = time.perf_counter()
+    tt, _, _ = forward.eikonal3d_batch(vels, h, lo, grid, srcs, rev, order=order, solver="heap")
+    dt = time.perf_counter() - t0
+    print(f"eik3heap order={order} solves={solves} call_s={dt:.4f} t00={tt[0, 0]:.6f}")
+
+
 def disp(precision=1, columns=4096):
     rng = np.random.default_rng(2)
     nl, thk, vp, vs, rho = synthetic.layered_columns(rng, columns, lvl_prob=0.0)
@@ -80,17 +104,20 @@ def grid():
 
 def main(argv=None):
     ap = argparse.ArgumentParser(description=__doc__, formatter_class=argparse.RawDescriptionHelpFormatter)
-    ap.add_argument("case", choices=["fm2d", "eik3", "disp", "grid"])
+    ap.add_argument("case", choices=["fm2d", "eik3", "eik3heap", "disp", "grid"])
+    ap.add_argument("--solves", type=int, default=8)
     ap.add_argument("--columns", type=int, default=4096)
     ap.add_argument("--precision", type=int, default=1)
     ap.add_argument("--maps", type=int, default=16)
     ap.add_argument("--repeat", type=int, default=2)
-    ap.add_argument("--order", type=int, default=0)
+    ap.add_argument("--order", type=int, default=None)
     a = ap.parse_args(argv)
     if a.case == "fm2d":
         fm2d(a.precision, a.maps, a.repeat)
     elif a.case == "eik3":
-        eik3(a.order)
+        eik3(a.order or 0)
+    elif a.case == "eik3heap":
+        eik3heap(1 if a.order is None else a.order, a.solves)
     elif a.case == "disp":
         disp(a.precision, a.columns)
     else:
