@@ -403,6 +403,73 @@ int mct_body_noise_likelihood(mct_body_ctx *ctx, int nchains,
 int mct_body_phase_time(mct_body_ctx *ctx, int index, double *phase_time,
                         int *passes);
 
+
+/* ------------------------------------------------------------------------
+ * 2D travel-time likelihood for many chains, replaces the 2D code's
+ * likelihood call (mcmc2d/likelihood_joint.f90:56) -> body_likelihood
+ * (mcmc2d/likelihood_dd.F90:349-529) and the kdtree_to_grid call before it
+ * (mcmc2d/mcmc.f90:1469-1525): nearest-nucleus velocity grid (ny, nx),
+ * padded vertex grid, modrays from every source (or straight rays), then
+ * sigma and the misfit; datatype 1 adds the differential times of every
+ * source pair. The grid's y axis is divided by its scaling for the
+ * travel times, as the reference's call does; nz is ignored.
+ * ---------------------------------------------------------------------- */
+typedef struct {
+  int gridx, gridy;   /* fm2d B-spline refinement of the vertex grid */
+  int sgref;          /* 1: refined source grid */
+  int sgdic, sgext;   /* source grid refinement factor and extent */
+  int order;          /* fm2d: 0 first order, 1 mixed order (fom) */
+  int sigdep;         /* 0 data sigma, else sigma = n0 * time + n1 */
+  int datatype;       /* 0 travel times; 1 travel times + differential times */
+  int straight;       /* 1: straight rays (isStraight) instead of fm2d */
+  int precision;      /* fm2d: 0 FP64 in the reference's order, 1 double-float */
+} mct_tt2d_settings;
+
+typedef struct {
+  int nsrc, nrev;
+  const double *src;      /* (2, nsrc) source x, y (dat%src) */
+  const double *rev;      /* (2, nrev) receiver x, y (dat%rev) */
+  const int *raystat;     /* (nsrc*nrev): 1 where a time exists (dat%raystat(:,1,1)) */
+  const double *ttime;    /* (nsrc*nrev) observed times (dat%ttime(:,1,1)) */
+  const double *sigma;    /* (nsrc*nrev) data sigma (dat%ttime(:,2,1)), or NULL */
+  int nrays;
+  /* datatype 1: (nrev, nsrc*(nsrc-1)/2) column-major as dat%dtime(:,:,1)
+   * and dat%dcc(:,:,1) (pairs i<j in order), and dat%ndtime */
+  const double *dtime;
+  const double *dcc;
+  int ndtime;
+} mct_tt2d_data;
+
+typedef struct mct_tt2d_ctx mct_tt2d_ctx;
+
+/* MCT_ERR_ARG also where the reference's differential-time test
+ * (abs(dat%dtime(ddindex,k,1)), indices swapped) would read outside
+ * dat%dtime. */
+int mct_tt2d_create(const mct_grid *grid, const mct_tt2d_settings *settings,
+                    const mct_tt2d_data *data, int nslots, int ncell_max,
+                    mct_tt2d_ctx **ctx);
+int mct_tt2d_destroy(mct_tt2d_ctx *ctx);
+/* points [nchains][ncell_max][2] (x, y) = RTI%points, params
+ * [nchains][ncell_max][3] (velocity first) = RTI%parameters, n0/n1
+ * [nchains][2] = RTI%snoise0/1 (travel times, differential times);
+ * out [nchains][4] = like, misfit, unweighted misfit, status (8: zero
+ * sigma, the reference's fatal error; like = DBL_MAX when nonzero). Host
+ * pointers, synchronous. */
+int mct_tt2d_forward(mct_tt2d_ctx *ctx, int nchains, const int *ncells,
+                     const double *points, const double *params,
+                     const double *n0, const double *n1, double *out);
+/* Noise-only likelihood, replaces the 2D body_noise_likelihood
+ * (mcmc2d/likelihood_dd.F90:32-106): the last forward's times of batch
+ * positions 0..nchains-1 with new n0/n1; sigma = n0 * srdist + n1 (srdist:
+ * the times when sigdep != 0, else the source-receiver distances), the
+ * differential sigma log-sum kept in an integer as the reference does; out
+ * as mct_tt2d_forward (unweighted misfit: the forward's). */
+int mct_tt2d_noise_likelihood(mct_tt2d_ctx *ctx, int nchains,
+                              const double *n0, const double *n1, double *out);
+/* Last forward's times (nsrc, nrev) = phaseTime(k,j,1) of batch position
+ * index. */
+int mct_tt2d_phase_time(mct_tt2d_ctx *ctx, int index, double *phase_time);
+
 #ifdef __cplusplus
 }
 #endif

@@ -160,3 +160,59 @@ def voronoi_phase_maps(rng, nmaps, nvx, nvz, dx, dz, ncell=50, vrange=(0.4, 2.2)
         out[m, 0] = out[m, 1]; out[m, -1] = out[m, -2]
         out[m, :, 0] = out[m, :, 1]; out[m, :, -1] = out[m, :, -2]
     return out
+
+
+def tt2d_workload(rng, nx=51, ny=51, extent=10.0, nstations=16, inset=0.5, noise=0.05, datatype=0):
+    """The plain 2D travel-time configuration: a square grid over extent km,
+    nstations equally spaced on a square perimeter inset from the edges (the
+    reference's refined-source pass reads undefined memory for sources on
+    the maximum edges), every station a source to every other one, observed
+    times = straight-ray times at 3 km/s plus Gaussian noise. datatype 1
+    adds differential times of every source pair at every receiver (zero,
+    i.e. absent, where the receiver is one of the two sources) with
+    cross-correlation coefficients in [0.5, 1]. Returns grid, settings,
+    data for TravelTime2DLikelihood."""
+    grid = dict(nx=nx, ny=ny, nz=1, xmin=0.0, ymin=0.0, zmin=0.0, dx=extent / (nx - 1), dy=extent / (ny - 1),
+                dz=1.0, scaling=1.0, water_depth=0.0)
+    side = extent - 2 * inset
+    s = np.arange(nstations) * (4 * side / nstations)
+    st = np.zeros((nstations, 2))
+    for n, a in enumerate(s):
+        e, f = int(a // side), a % side
+        st[n] = [(inset + f, inset), (extent - inset, inset + f), (extent - inset - f, extent - inset),
+                 (inset, extent - inset - f)][e]
+    raystat = (1 - np.eye(nstations, dtype=np.int32)).reshape(-1)
+    dist = np.hypot(st[:, None, 0] - st[None, :, 0], st[:, None, 1] - st[None, :, 1])
+    tt = (dist / 3.0 + noise * rng.standard_normal(dist.shape)) * (1 - np.eye(nstations))
+    settings = dict(gridx=1, gridy=1, sgref=1, sgdic=5, sgext=10, order=1, sigdep=0, datatype=datatype, straight=0,
+                    precision=0)
+    data = dict(src=st, rev=st, raystat=raystat, ttime=tt.reshape(-1), sigma=np.full(raystat.size, noise),
+                nrays=int(raystat.sum()))
+    if datatype == 1:
+        pairs = [(i, j) for i in range(nstations) for j in range(i + 1, nstations)]
+        dt = np.zeros((len(pairs), nstations))
+        dcc = rng.uniform(0.5, 1.0, dt.shape)
+        for d, (i, j) in enumerate(pairs):
+            for k in range(nstations):
+                if k not in (i, j):
+                    dt[d, k] = tt[j, k] - tt[i, k] + 0.01 * rng.standard_normal()
+        data.update(dtime=dt, dcc=dcc, ndtime=int((dt != 0).sum()))
+    return grid, settings, data
+
+
+def tt2d_chain_models(rng, nchains, ncell_max, grid, ncell_range=(4, 100), vrange=(2.0, 4.0)):
+    """2D Voronoi models (nuclei uniform in the domain, velocity uniform on
+    vrange): ncells, points (nchains, ncell_max, 2), params (nchains,
+    ncell_max, 3) with the velocity first."""
+    lo = np.array([grid["xmin"], grid["ymin"]])
+    hi = lo + np.array([grid["dx"] * (grid["nx"] - 1), grid["dy"] * (grid["ny"] - 1)])
+    ncells = rng.integers(ncell_range[0], ncell_range[1] + 1, nchains).astype(np.int32)
+    points = np.zeros((nchains, ncell_max, 2))
+    params = np.zeros((nchains, ncell_max, 3))
+    for c in range(nchains):
+        n = int(ncells[c])
+        points[c, :n] = lo + (hi - lo) * rng.random((n, 2))
+        params[c, :n, 0] = rng.uniform(vrange[0], vrange[1], n)
+        params[c, :n, 1] = params[c, :n, 0] / 1.73
+        params[c, :n, 2] = 2.0
+    return ncells, points, params

@@ -11,13 +11,22 @@
 //   surf_noise_likelihood src/likelihood_surf.F90:56-99
 //   body_likelihood   src/likelihood_body.F90:176-195,284-333
 //   body_noise_likelihood src/likelihood_body.F90:38-80
-//   2D body_likelihood mcmc2d/likelihood_dd.F90:468-499 (datatype 0)
+//   2D body_likelihood mcmc2d/likelihood_dd.F90:455-529 (datatypes 0, 1)
+//   2D body_noise_likelihood mcmc2d/likelihood_dd.F90:32-106
 //   vs2vp / vp2rho    src/utils.f90:90-135
 #include <cmath>
+#include <vector>
 #include "oracle.h"
 
 namespace {
 const double PI2 = (double)6.283185f;  // REAL*8 parameter set from a REAL*4 literal
+const double EPS2D = (double)0.000000001f;  // utils/utils.f90:58, a REAL*4 literal
+
+// INTEGER = REAL*8 as the x86 build does it: truncation, -2^31 out of range
+int fortran_int(double x) {
+  if (!(x > -2147483649.0 && x < 2147483648.0)) return -2147483647 - 1;
+  return (int)x;
+}
 }
 
 extern "C" {
@@ -172,6 +181,119 @@ int orc_body_misfit(int nsrc, int nrev, int np, const double *phase_time,
 
 // src/utils.f90:98-135 vs2vp_3d / vp2rho_3d: vp = vs*1.730, rho = 1.74*vp**0.25
 // (both constants are REAL*4 literals widened to double).
+// 2D body_likelihood after modrays (mcmc2d/likelihood_dd.F90:455-529).
+// phase_time [nsrc][nrev] = phaseTime(k,j,1); dat_ttime, dat_sigma,
+// raystat per pair nrr = k + (j-1)*nrev; dtime, dcc (nrev, ndd)
+// column-major = dat%dtime(:,:,1), dat%dcc(:,:,1); n0, n1 [2] = snoise0/1
+// (travel times, differential times). out = like, misfit, unweighted.
+// Returns 8 where the reference raises 'The noise level is 0!'.
+int orc_tt2d_misfit(int nsrc, int nrev, const double *phase_time, const double *dat_ttime, const double *dat_sigma,
+                    const int *raystat, int sigdep, int datatype, const double *dtime, const double *dcc, int ndtime,
+                    const double *n0, const double *n1, int nrays, double *out) {
+  const int npairs = nsrc * nrev;
+  std::vector<double> sigma(npairs);
+  for (int q = 0; q < npairs; ++q) sigma[q] = sigdep != 0 ? n0[0] * phase_time[q] + n1[0] : dat_sigma[q];
+  const int ndd = nsrc * (nsrc - 1) / 2;
+  std::vector<double> dtm, dsig;
+  if (datatype == 1) {
+    dtm.resize((size_t)ndd * nrev); dsig.resize((size_t)ndd * nrev);
+    int dd = 0;
+    for (int i = 0; i < nsrc; ++i)
+      for (int j = i + 1; j < nsrc; ++j, ++dd)
+        for (int k = 0; k < nrev; ++k) {
+          dtm[(size_t)dd * nrev + k] = phase_time[(size_t)j * nrev + k] - phase_time[(size_t)i * nrev + k];
+          dsig[(size_t)dd * nrev + k] = n0[1] * (1 - dcc[(size_t)dd * nrev + k]) + n1[1];
+        }
+  }
+  int status = 0;
+  double like = 0, misfit = 0, umis = 0;
+  int nrr = 0;
+  for (int j = 0; j < nsrc; ++j)
+    for (int k = 0; k < nrev; ++k, ++nrr) {
+      if (raystat[nrr] == 1) {
+        if (sigma[nrr] == 0) status = 8;
+        const double r = phase_time[(size_t)j * nrev + k] - dat_ttime[nrr];
+        like = like + (r * r) / (2 * (sigma[nrr] * sigma[nrr]));
+        misfit = misfit + (r * r) / (sigma[nrr] * sigma[nrr]);
+        umis = umis + r * r;
+      } else {
+        sigma[nrr] = 1.0;
+      }
+    }
+  double slog = 0;
+  for (int q = 0; q < npairs; ++q) slog = slog + std::log(sigma[q]);
+  like = like + slog + (double)((float)nrays / 2.0f) * std::log(PI2);
+  if (datatype == 1) {
+    double sumdsigma = 0;
+    int dd = 0;
+    for (int i = 0; i < nsrc; ++i)
+      for (int j = i + 1; j < nsrc; ++j, ++dd)
+        for (int k = 0; k < nrev; ++k) {
+          // dat%dtime(ddindex,k,1): indices swapped, column-major element
+          if (std::fabs(dtime[(size_t)dd + (size_t)k * nrev]) > EPS2D) {
+            const double r = dtm[(size_t)dd * nrev + k] - dtime[(size_t)dd * nrev + k];
+            const double s2 = dsig[(size_t)dd * nrev + k];
+            like = like + (r * r) / (2 * (s2 * s2));
+            misfit = misfit + (r * r) / (s2 * s2);
+            umis = umis + r * r;
+            sumdsigma = sumdsigma + std::log(s2);
+          }
+        }
+    like = like + sumdsigma + (double)((float)ndtime / 2.0f) * std::log(PI2);
+  }
+  out[0] = like; out[1] = misfit; out[2] = umis;
+  return status;
+}
+
+// 2D body_noise_likelihood (mcmc2d/likelihood_dd.F90:32-106) on given
+// times: sigma = n0 * srdist + n1; the differential sigma log-sum is an
+// INTEGER there. out = like, misfit (the unweighted misfit is untouched).
+int orc_tt2d_noise(int nsrc, int nrev, const double *phase_time, const double *dat_ttime, const int *raystat,
+                   const double *srdist, int datatype, const double *dtime, const double *dcc, int ndtime,
+                   const double *n0, const double *n1, int nrays, double *out) {
+  const int npairs = nsrc * nrev;
+  std::vector<double> sigma(npairs);
+  for (int q = 0; q < npairs; ++q) sigma[q] = n0[0] * srdist[q] + n1[0];
+  int status = 0;
+  double like = 0, misfit = 0;
+  int nrr = 0;
+  for (int j = 0; j < nsrc; ++j)
+    for (int k = 0; k < nrev; ++k, ++nrr) {
+      if (raystat[nrr] == 1) {
+        if (sigma[nrr] == 0) status = 8;
+        const double r = phase_time[(size_t)j * nrev + k] - dat_ttime[nrr];
+        like = like + (r * r) / (2 * (sigma[nrr] * sigma[nrr]));
+        misfit = misfit + (r * r) / (sigma[nrr] * sigma[nrr]);
+      } else {
+        sigma[nrr] = 1.0;
+      }
+    }
+  for (int q = 0; q < npairs; ++q)
+    if (sigma[q] < EPS2D) status = 8;
+  double slog = 0;
+  for (int q = 0; q < npairs; ++q) slog = slog + std::log(sigma[q]);
+  like = like + slog + (double)((float)nrays / 2.0f) * std::log(PI2);
+  if (datatype == 1) {
+    int sumdsigma = 0;
+    int dd = 0;
+    for (int i = 0; i < nsrc; ++i)
+      for (int j = i + 1; j < nsrc; ++j, ++dd)
+        for (int k = 0; k < nrev; ++k) {
+          if (std::fabs(dtime[(size_t)dd + (size_t)k * nrev]) > EPS2D) {
+            const double dtm = phase_time[(size_t)j * nrev + k] - phase_time[(size_t)i * nrev + k];
+            const double s2 = n0[1] * (1 - dcc[(size_t)dd * nrev + k]) + n1[1];
+            const double r = dtm - dtime[(size_t)dd * nrev + k];
+            like = like + (r * r) / (2 * (s2 * s2));
+            misfit = misfit + (r * r) / (s2 * s2);
+            sumdsigma = fortran_int((double)sumdsigma + std::log(s2));
+          }
+        }
+    like = like + (double)sumdsigma + (double)((float)ndtime / 2.0f) * std::log(PI2);
+  }
+  out[0] = like; out[1] = misfit;
+  return status;
+}
+
 double orc_vs2vp(double vs) { return vs * (double)1.730f; }
 double orc_vp2rho(double vp) { return (double)1.74f * std::pow(vp, 0.25); }
 

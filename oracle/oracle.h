@@ -64,6 +64,14 @@ int orc_surf_misfit(int nsrc, int nrev, int np, const double *phase_time,
                     const double *srdist, int sigdep, const double *n0,
                     const double *n1, int nrays, double *sigma_out,
                     double *out);
+int orc_tt2d_misfit(int nsrc, int nrev, const double *phase_time, const double *dat_ttime,
+                    const double *dat_sigma, const int *raystat, int sigdep, int datatype,
+                    const double *dtime, const double *dcc, int ndtime, const double *n0,
+                    const double *n1, int nrays, double *out);
+int orc_tt2d_noise(int nsrc, int nrev, const double *phase_time, const double *dat_ttime,
+                   const int *raystat, const double *srdist, int datatype, const double *dtime,
+                   const double *dcc, int ndtime, const double *n0, const double *n1, int nrays,
+                   double *out);
 int orc_body_misfit(int nsrc, int nrev, int np, const double *phase_time,
                     const double *t0, const double *dat_ttime,
                     const int *raystat, const double *srdist, int sigdep,
