@@ -458,12 +458,18 @@ int mct_tt2d_destroy(mct_tt2d_ctx *ctx);
 int mct_tt2d_forward(mct_tt2d_ctx *ctx, int nchains, const int *ncells,
                      const double *points, const double *params,
                      const double *n0, const double *n1, double *out);
+/* After the Metropolis test: chains with accept[c] != 0 (and a valid
+ * forward) keep the last forward's times as their state, as the
+ * reference keeps the accepted like and restores the backed-up one on
+ * reject (mcmc2d/mcmc.f90:456-465). */
+int mct_tt2d_commit(mct_tt2d_ctx *ctx, int nchains, const int *accept);
 /* Noise-only likelihood, replaces the 2D body_noise_likelihood
- * (mcmc2d/likelihood_dd.F90:32-106): the last forward's times of batch
- * positions 0..nchains-1 with new n0/n1; sigma = n0 * srdist + n1 (srdist:
- * the times when sigdep != 0, else the source-receiver distances), the
- * differential sigma log-sum kept in an integer as the reference does; out
- * as mct_tt2d_forward (unweighted misfit: the forward's). */
+ * (mcmc2d/likelihood_dd.F90:32-106): chains 0..nchains-1's committed times
+ * with new n0/n1; sigma = n0 * srdist + n1 (srdist: the times when sigdep
+ * != 0, else the source-receiver distances), the differential sigma
+ * log-sum kept in an integer as the reference does; out as
+ * mct_tt2d_forward (unweighted misfit: the committed forward's; status 16:
+ * nothing committed yet). */
 int mct_tt2d_noise_likelihood(mct_tt2d_ctx *ctx, int nchains,
                               const double *n0, const double *n1, double *out);
 /* Last forward's times (nsrc, nrev) = phaseTime(k,j,1) of batch position

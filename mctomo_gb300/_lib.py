@@ -48,6 +48,7 @@ SIGNATURES = {
     "mct_tt2d_create": (I, [P, P, P, I, I, P]),
     "mct_tt2d_destroy": (I, [P]),
     "mct_tt2d_forward": (I, [P, I, P, P, P, P, P, P]),
+    "mct_tt2d_commit": (I, [P, I, P]),
     "mct_tt2d_noise_likelihood": (I, [P, I, P, P, P]),
     "mct_tt2d_phase_time": (I, [P, I, P]),
     "mct_surf_create": (I, [P, P, P, I, I, P]),

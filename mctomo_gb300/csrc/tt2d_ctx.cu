@@ -227,7 +227,7 @@ __global__ void tt2d_misfit_kernel(Tt2dDev d, const double *tt, const double *n0
 // times; the differential sigma log-sum is an INTEGER there, truncated
 // after every term, so one thread adds it in the reference's order.
 __global__ void tt2d_noise_kernel(Tt2dDev d, const double *tt, const double *n0, const double *n1,
-                                  const double *umis_keep, double *out) {
+                                  const double *umis_keep, const int *committed, double *out) {
   const int c = blockIdx.x;
   const int npairs = d.nsrc * d.nrev;
   const double *T = tt + (size_t)c * npairs;
@@ -273,10 +273,11 @@ __global__ void tt2d_noise_kernel(Tt2dDev d, const double *tt, const double *n0,
       L = L + red[3][0] + (double)sumdsigma + (double)((float)d.ndtime / 2.0f) * log(kPI2);
       mis += red[4][0];
     }
-    out[(size_t)c * 4 + 0] = sbad ? DBL_MAX : L;
+    const int stt = (sbad ? 8 : 0) | (committed[c] ? 0 : 16);
+    out[(size_t)c * 4 + 0] = stt ? DBL_MAX : L;
     out[(size_t)c * 4 + 1] = mis;
     out[(size_t)c * 4 + 2] = umis_keep[c];
-    out[(size_t)c * 4 + 3] = sbad ? 8.0 : 0.0;
+    out[(size_t)c * 4 + 3] = (double)stt;
   }
 }
 
@@ -301,6 +302,17 @@ double norm2_fortran(double a, double b) {
   return scale * std::sqrt(ssq);
 }
 
+// An accepted proposal becomes its chain's state: times and unweighted
+// misfit (what the reference keeps in `like` after the Metropolis step).
+__global__ void tt2d_commit_kernel(int npairs, const int *accept, const double *out, const double *tt,
+                                   const double *umis, double *ctt, double *cumis, int *committed) {
+  const int c = blockIdx.y;
+  if (!accept[c] || out[(size_t)c * 4 + 3] != 0.0) return;
+  for (int q = blockIdx.x * blockDim.x + threadIdx.x; q < npairs; q += gridDim.x * blockDim.x)
+    ctt[(size_t)c * npairs + q] = tt[(size_t)c * npairs + q];
+  if (blockIdx.x == 0 && threadIdx.x == 0) { cumis[c] = umis[c]; committed[c] = 1; }
+}
+
 }  // namespace
 
 struct mct_tt2d_ctx {
@@ -317,6 +329,8 @@ struct mct_tt2d_ctx {
   int *sites = nullptr, *tie_count = nullptr, *tie_nodes = nullptr, *gstatus = nullptr;
   void *kd = nullptr;
   double *vel = nullptr, *velv = nullptr, *tt = nullptr;
+  double *ctt = nullptr, *cumis = nullptr;     // committed state per slot
+  int *committed = nullptr, *accept = nullptr;
 };
 
 extern "C" {
@@ -379,9 +393,10 @@ int mct_tt2d_create(const mct_grid *g, const mct_tt2d_settings *st, const mct_tt
   const bool fm = !st->straight;
   std::vector<size_t> sz = {
       sizeof(int) * nslots, sizeof(double) * (size_t)nslots * ncell_max * 5, sizeof(double) * 4 * nslots,
-      sizeof(double) * 4 * nslots, sizeof(double) * nslots,
+      sizeof(double) * 8 * nslots, sizeof(double) * nslots,
       sizeof(int) * nslots * nodes, sizeof(int) * nslots, sizeof(int) * nslots * nodes, kd * nslots, sizeof(int) * 2,
       sizeof(double) * 3 * nslots * nodes, sizeof(double) * nslots * nvv, sizeof(double) * (size_t)nslots * npairs,
+      sizeof(double) * (size_t)nslots * (npairs + 1), sizeof(int) * 2 * nslots,
       // data
       sizeof(int) * npairs, sizeof(double) * 5 * (size_t)npairs, sizeof(double) * 2 * (size_t)ndd * nrev,
       sizeof(int2) * (size_t)std::max(ndd, 1), sizeof(double) * 2 * (nsrc + nrev), sizeof(double) * 2 * (nsrc + nrev),
@@ -406,7 +421,7 @@ int mct_tt2d_create(const mct_grid *g, const mct_tt2d_settings *st, const mct_tt
   c->points = cv.take<double>((size_t)nslots * ncell_max * 5);
   c->params = c->points + (size_t)nslots * ncell_max * 2;
   c->n0 = cv.take<double>((size_t)4 * nslots); c->n1 = c->n0 + 2 * (size_t)nslots;
-  c->out = cv.take<double>((size_t)4 * nslots);
+  c->out = cv.take<double>((size_t)8 * nslots);     // forward results, then noise-only results
   c->umis = cv.take<double>(nslots);
   c->sites = cv.take<int>(nslots * nodes);
   c->tie_count = cv.take<int>(nslots);
@@ -416,6 +431,10 @@ int mct_tt2d_create(const mct_grid *g, const mct_tt2d_settings *st, const mct_tt
   c->vel = cv.take<double>(3 * nslots * nodes);
   c->velv = cv.take<double>(nslots * nvv);
   c->tt = cv.take<double>((size_t)nslots * npairs);
+  c->ctt = cv.take<double>((size_t)nslots * (npairs + 1));
+  c->cumis = c->ctt + (size_t)nslots * npairs;
+  c->committed = cv.take<int>(2 * nslots);
+  c->accept = c->committed + nslots;
   int *d_rays = cv.take<int>(npairs);
   double *d_pd = cv.take<double>(5 * (size_t)npairs);
   double *d_dd = cv.take<double>(2 * (size_t)ndd * nrev);
@@ -463,7 +482,9 @@ int mct_tt2d_create(const mct_grid *g, const mct_tt2d_settings *st, const mct_tt
             cudaMemcpy(d_xy, xy.data(), sizeof(double) * xy.size(), cudaMemcpyHostToDevice) == cudaSuccess &&
             cudaMemcpy(d_sep, sep.data(), sizeof(double) * sep.size(), cudaMemcpyHostToDevice) == cudaSuccess &&
             cudaMemset(c->tt, 0, sizeof(double) * (size_t)nslots * npairs) == cudaSuccess &&
-            cudaMemset(c->umis, 0, sizeof(double) * nslots) == cudaSuccess;
+            cudaMemset(c->umis, 0, sizeof(double) * nslots) == cudaSuccess &&
+            cudaMemset(c->ctt, 0, sizeof(double) * (size_t)nslots * (npairs + 1)) == cudaSuccess &&
+            cudaMemset(c->committed, 0, sizeof(int) * 2 * nslots) == cudaSuccess;
   if (ok && ndd > 0)
     ok = cudaMemcpy(d_dd, dat->dtime, sizeof(double) * (size_t)ndd * nrev, cudaMemcpyHostToDevice) == cudaSuccess &&
          cudaMemcpy(d_dd + (size_t)ndd * nrev, dat->dcc, sizeof(double) * (size_t)ndd * nrev,
@@ -557,18 +578,34 @@ int mct_tt2d_forward(mct_tt2d_ctx *c, int nchains, const int *ncells, const doub
   return MCT_OK;
 }
 
+int mct_tt2d_commit(mct_tt2d_ctx *c, int nchains, const int *accept) {
+  if (!c || nchains < 1 || nchains > c->last_nchains || !accept) {
+    mct_set_error("mct_tt2d_commit", "bad arguments (commit follows a forward of at least nchains)", __FILE__,
+                  __LINE__);
+    return MCT_ERR_ARG;
+  }
+  cudaStream_t s = c->stream;
+  const int npairs = c->dev.nsrc * c->dev.nrev;
+  MCT_CUDA_TRY(cudaMemcpyAsync(c->accept, accept, sizeof(int) * nchains, cudaMemcpyHostToDevice, s));
+  tt2d_commit_kernel<<<dim3((npairs + 255) / 256, nchains), 256, 0, s>>>(npairs, c->accept, c->out, c->tt, c->umis,
+                                                                         c->ctt, c->cumis, c->committed);
+  MCT_CUDA_TRY(cudaGetLastError());
+  MCT_CUDA_TRY(cudaStreamSynchronize(s));
+  return MCT_OK;
+}
+
 int mct_tt2d_noise_likelihood(mct_tt2d_ctx *c, int nchains, const double *n0, const double *n1, double *out) {
-  if (!c || nchains < 1 || nchains > c->last_nchains || !n0 || !n1 || !out) {
-    mct_set_error("mct_tt2d_noise_likelihood", "bad arguments (call after a forward of at least nchains)",
-                  __FILE__, __LINE__);
+  if (!c || nchains < 1 || nchains > c->nslots || !n0 || !n1 || !out) {
+    mct_set_error("mct_tt2d_noise_likelihood", "bad arguments", __FILE__, __LINE__);
     return MCT_ERR_ARG;
   }
   cudaStream_t s = c->stream;
   MCT_CUDA_TRY(cudaMemcpyAsync(c->n0, n0, sizeof(double) * 2 * nchains, cudaMemcpyHostToDevice, s));
   MCT_CUDA_TRY(cudaMemcpyAsync(c->n1, n1, sizeof(double) * 2 * nchains, cudaMemcpyHostToDevice, s));
-  tt2d_noise_kernel<<<nchains, 256, 0, s>>>(c->dev, c->tt, c->n0, c->n1, c->umis, c->out);
+  double *nout = c->out + 4 * (size_t)c->nslots;   // the forward's results stay for commit
+  tt2d_noise_kernel<<<nchains, 256, 0, s>>>(c->dev, c->ctt, c->n0, c->n1, c->cumis, c->committed, nout);
   MCT_CUDA_TRY(cudaGetLastError());
-  MCT_CUDA_TRY(cudaMemcpyAsync(out, c->out, sizeof(double) * 4 * nchains, cudaMemcpyDeviceToHost, s));
+  MCT_CUDA_TRY(cudaMemcpyAsync(out, nout, sizeof(double) * 4 * nchains, cudaMemcpyDeviceToHost, s));
   MCT_CUDA_TRY(cudaStreamSynchronize(s));
   return MCT_OK;
 }

@@ -91,9 +91,14 @@ class TravelTime2DLikelihood:
                                                          ptr(n0), ptr(n1), ptr(out)))
         return out
 
+    def commit(self, accept):
+        """Chains with accept[c] keep the last forward as their state."""
+        accept = np.ascontiguousarray(accept, np.int32)
+        check("mct_tt2d_commit", lib().mct_tt2d_commit(self.h, accept.size, ptr(accept)))
+
     def noise_likelihood(self, n0, n1):
-        """body_noise_likelihood of the 2D code on the last forward's times
-        of batch positions 0..nch-1 with new n0/n1 (nch, 2)."""
+        """body_noise_likelihood of the 2D code on chains 0..nch-1's
+        committed times with new n0/n1 (nch, 2)."""
         n0 = np.ascontiguousarray(n0, np.float64)
         nch = n0.shape[0]
         n0 = n0.reshape(nch, 2)

@@ -114,6 +114,13 @@ def test_tt2d_noise_likelihood_matches_oracle(orc, gpulib, datatype, sigdep, str
     lk = TravelTime2DLikelihood(grid, settings, data, nslots=nch, ncell_max=ncell_max)
     fwd = lk.forward(ncells, pts, par, np.tile([0.01, 0.02], (nch, 1)), np.tile([0.04, 0.01], (nch, 1)))
     m0 = rng.uniform(0.0, 0.03, (nch, 2)); m1 = rng.uniform(0.01, 0.05, (nch, 2))
+    assert np.all(lk.noise_likelihood(m0, m1)[:, 3] == 16)      # nothing committed yet
+    lk.commit(np.ones(nch, np.int32))
+    # a later proposal that is rejected does not change the committed state
+    nc2, pts2, par2 = synthetic.tt2d_chain_models(rng, nch, ncell_max, grid)
+    lk.forward(nc2, pts2, par2, np.tile([0.01, 0.02], (nch, 1)), np.tile([0.04, 0.01], (nch, 1)))
+    lk.commit(np.zeros(nch, np.int32))
+    lk.forward(ncells, pts, par, np.tile([0.01, 0.02], (nch, 1)), np.tile([0.04, 0.01], (nch, 1)))
     got = lk.noise_likelihood(m0, m1)
     src, rev = np.asarray(data["src"]), np.asarray(data["rev"])
     nsrc, nrev = len(src), len(rev)
