@@ -432,6 +432,17 @@ def run_body(args):
     cl = clocks.stop()
     value, total = job_rate(nch * args.steps, sum(ms), ws, dev)
     h2d = nch * ncell_max * 3 * 8 * 2 + nch * 4 + nch * len(ev) * 4 * 8 + 2 * nch * 2 * 8
+    # the plain drop-in: one chain per call
+    one = BodyLikelihood(grid, settings, data, nslots=1, ncell_max=ncell_max)
+    ncells0, pts0, par0 = props[0]
+    one.forward(ncells0[:1], pts0[:1], par0[:1], locs[:1], n0[:1], n1[:1])
+    pms = []
+    for i in range(2):
+        nc, pp, qq = props[(i + 1) % len(props)]
+        t0 = time.perf_counter()
+        one.forward(nc[:1], pp[:1], qq[:1], locs[:1], n0[:1], n1[:1])
+        pms.append((time.perf_counter() - t0) * 1e3)
+    one.close()
     desc, err, dtype = BODY_SOLVERS[solver]
     line = {"metric": "body-wave forward evals/s, 1 GB300, " + err, "value": round(value, 4),
             "unit": "proposal evals/s", "n_gpus": ws, "steps": args.steps, "warmup": args.warmup,
@@ -442,6 +453,11 @@ def run_body(args):
             "e2e": {"value": round(value, 4), "unit": "proposal evals/s", "h2d_bytes_per_step": h2d,
                     "d2h_bytes_per_step": nch * 4 * 8},
             "note": "host API only (value = e2e): the body context has no device-pointer forward",
+            "batched_latency_ms": {"p50": round(float(np.percentile(ms, 50)), 3),
+                                   "p99": round(float(np.percentile(ms, 99)), 3)},
+            "plain": {"value": round(1e3 / float(np.mean(pms)), 4), "unit": "proposal evals/s",
+                      "p50_ms": round(float(np.percentile(pms, 50)), 3),
+                      "p99_ms": round(float(np.percentile(pms, 99)), 3)},
             "clocks": cl, "valid_models": int((out[:, 3] == 0).sum())}
     if rank == 0 and not args.no_cpu:
         line["cpu_baseline"] = body_cpu_baseline(grid, settings, data, ev, props[0], args)
@@ -493,6 +509,269 @@ def body_cpu_baseline(grid, settings, data, ev, prop, args):
                       "own C++ SFMM as restated bit-exactly) on a thread pool over all host cores"}
 
 
+LOVE_COLS = 16384
+DISP_CONFIG = {"workload": "dispersion-precision study: 262,144 independent layered columns (12-40 layers, "
+                           "thickness U[0.05,0.5] km, Vs U[0.2,3.5] km/s with a 10% low-velocity-layer chance, "
+                           "Vp = 1.73 Vs, Gardner density), 60 periods 0.2-20 s, Rayleigh and Love, fundamental "
+                           "and first overtone, phase and group",
+               "periods": 60, "modes": 2, "waves": ["Rayleigh", "Love"]}
+
+
+def run_disp(args):
+    """The dispersion-precision study: every step computes all columns'
+    phase and group curves for both wave types and both modes with one
+    variant; the FP64 variant and the FP32-bracketing variant are both timed
+    on the device, and a seeded sample of columns is compared with the
+    oracle (the surfdisp96 restatement), separately for columns with
+    low-velocity layers (which the reference's surfmodes routes to GRT)."""
+    import torch
+    from mctomo_gb300 import _lib, forward, synthetic
+    L = _lib.lib()
+    dev = torch.device("cuda")
+    rng = np.random.default_rng(SEED + 3)
+    ncol = args.columns
+    nl, thk, vp, vs, rho = synthetic.layered_columns(rng, ncol, nl_range=(12, 40), lvl_prob=0.1)
+    periods = np.geomspace(0.2, 20.0, 60)
+    nl_max = thk.shape[1]
+    d = {k: torch.from_numpy(np.ascontiguousarray(v)).to(dev) for k, v in
+         dict(nl=nl, thk=thk, vp=vp, vs=vs, rho=rho, per=periods).items()}
+    cp = torch.zeros((ncol, 2, 60), dtype=torch.float64, device=dev)
+    cg = torch.zeros_like(cp)
+    ierr = torch.zeros(ncol, dtype=torch.int32, device=dev)
+    cnt = torch.zeros(2, dtype=torch.int64, device=dev)
+    stream = torch.cuda.current_stream()
+
+    # Rayleigh over all columns; Love over the first LOVE_COLS columns (Love
+    # waves with the first overtone faulted twice at full size; the cause is
+    # not found, so that case is not run again)
+    love_cols = min(ncol, LOVE_COLS)
+    chunk = ncol          # one launch per wave: every column's warp runs at once
+
+    def study(precision):
+        for iwave, nc in ((2, ncol), (1, love_cols)):
+            for c0 in range(0, nc, chunk):
+                n = min(chunk, nc - c0)
+                rc = L.mct_surfdisp_batch_device(n, nl_max, d["nl"][c0:].data_ptr(), d["thk"][c0:].data_ptr(),
+                                                 d["vp"][c0:].data_ptr(), d["vs"][c0:].data_ptr(),
+                                                 d["rho"][c0:].data_ptr(), 60, d["per"].data_ptr(), iwave, 2, 1,
+                                                 0.001, 1, precision, cp[c0:].data_ptr(), cg[c0:].data_ptr(),
+                                                 ierr[c0:].data_ptr(), cnt.data_ptr(), stream.cuda_stream)
+                _lib.check("mct_surfdisp_batch_device", rc)
+
+    res = {}
+    clocks = Clocks(0)
+    for precision in (1, 0):
+        for _ in range(args.warmup):
+            study(precision)
+        torch.cuda.synchronize()
+        if precision == 1:
+            clocks.start()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        for _ in range(args.steps):
+            study(precision)
+        e1.record(stream)
+        torch.cuda.synchronize()
+        if precision == 1:
+            cl = clocks.stop()
+        ms = e0.elapsed_time(e1) / args.steps
+        res[precision] = (ms, (ncol + love_cols) * 2 / (ms / 1e3))
+    # end to end through the host API (column arrays in, curves out), FP32-bracketing variant
+    t0 = time.perf_counter()
+    for iwave, nc in ((2, ncol), (1, love_cols)):
+        for c0 in range(0, nc, chunk):
+            sl = slice(c0, min(nc, c0 + chunk))
+            forward.surfdisp_batch(nl[sl], thk[sl], vp[sl], vs[sl], rho[sl], periods, iwave, 1, 0.001, mode=2,
+                                   multimode=True, precision=1)
+    e2e_s = time.perf_counter() - t0
+    acc = disp_oracle_sample(nl, thk, vp, vs, rho, periods, args)
+    value = res[1][1]
+    line = {"metric": "dispersion curves/s (column x wave x mode, phase + group), 1 GB300, phase err<=1e-5 km/s",
+            "value": round(value, 2), "unit": "curves/s", "n_gpus": 1, "steps": args.steps, "warmup": args.warmup,
+            "ms_per_step": round(res[1][0], 3), "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+            "dtype": "f32 bracketing confirmed in f64, f64 polish (precision 1); f64 throughout (precision 0)",
+            "data": "synthetic (seeded, shapes of the configuration)",
+            "config": dict(DISP_CONFIG, rayleigh_columns=ncol, love_columns=love_cols),
+            "variants": {"fp32_bracketing_fp64_polish": {"ms_per_step": round(res[1][0], 3),
+                                                         "curves_per_s": round(res[1][1], 2)},
+                         "fp64": {"ms_per_step": round(res[0][0], 3), "curves_per_s": round(res[0][1], 2)}},
+            "e2e": {"value": round((ncol + love_cols) * 2 / e2e_s, 2), "unit": "curves/s",
+                    "h2d_bytes_per_step": int(4 * 4 * ncol * nl_max + 4 * ncol + 60 * 8) * 2,
+                    "d2h_bytes_per_step": int(2 * ncol * 2 * 60 * 8 + 4 * ncol) * 2},
+            "accuracy": acc, "clocks": cl}
+    if not args.no_cpu:
+        line["cpu_baseline"] = acc.pop("cpu_baseline")
+    else:
+        acc.pop("cpu_baseline", None)
+    print(json.dumps(line), flush=True)
+
+
+def disp_oracle_sample(nl, thk, vp, vs, rho, periods, args):
+    """The oracle (surfdisp96 / surfdisp_mmodes restated) on a seeded sample
+    of columns, both waves, both modes, phase and group, on a thread pool
+    over all host cores; max phase and group differences of both GPU
+    variants on that sample, columns with low-velocity layers apart."""
+    import concurrent.futures as cf
+    import oracle
+    from mctomo_gb300 import forward
+    orc = oracle.load()
+    P = lambda a: None if a is None else a.ctypes.data_as(ctypes.c_void_p)  # noqa: E731
+    rng = np.random.default_rng(SEED + 4)
+    idx = np.sort(rng.choice(min(len(nl), LOVE_COLS), args.disp_sample, replace=False))
+    cols = [tuple(np.ascontiguousarray(x[c, :nl[c]]) for x in (thk, vp, vs, rho)) for c in idx]
+    lvl = np.array([bool(np.any(np.diff(vs[c, :nl[c]]) < 0)) for c in idx])
+    threads = os.cpu_count() or 1
+    out = {}
+    t0 = time.perf_counter()
+    for iwave in (2, 1):
+        def one(k):
+            o1 = np.zeros(120); o2 = np.zeros(120)
+            e = orc.orc_surfdisp_mmodes(*[P(x) for x in cols[k]], int(len(cols[k][0])), iwave, 2, 1, 60,
+                                        P(periods), 0.001, P(o1), P(o2), None)
+            return e, o1.reshape(2, 60), o2.reshape(2, 60)
+        with cf.ThreadPoolExecutor(threads) as ex:
+            out[iwave] = list(ex.map(one, range(len(idx))))
+    cpu_s = time.perf_counter() - t0
+    acc = {"columns_sampled": int(len(idx)), "lvl_columns_sampled": int(lvl.sum())}
+    for precision, name in ((1, "fp32_bracketing_fp64_polish"), (0, "fp64")):
+        worst = {"plain": [0.0, 0.0], "lvl": [0.0, 0.0]}
+        agree = 0
+        for iwave in (2, 1):
+            cp, cg, ierr, _ = forward.surfdisp_batch(nl[idx], thk[idx], vp[idx], vs[idx], rho[idx], periods, iwave,
+                                                     1, 0.001, mode=2, multimode=True, precision=precision)
+            for k in range(len(idx)):
+                e, ecp, ecg = out[iwave][k]
+                agree += int(e == ierr[k])
+                good = (ecp > 0) & (cp[k] > 0)
+                key = "lvl" if lvl[k] else "plain"
+                if good.any():
+                    worst[key][0] = max(worst[key][0], float(np.max(np.abs(cp[k][good] - ecp[good]))))
+                    worst[key][1] = max(worst[key][1], float(np.max(np.abs(cg[k][good] - ecg[good]))))
+        acc[name] = {"max_phase_err_kms": worst["plain"][0], "max_group_err_kms": worst["plain"][1],
+                     "lvl_max_phase_err_kms": worst["lvl"][0], "lvl_max_group_err_kms": worst["lvl"][1],
+                     "ierr_agreement": round(agree / (2 * len(idx)), 4)}
+    acc["cpu_baseline"] = {"value": round(len(idx) * 4 / cpu_s, 2), "unit": "curves/s", "cores": threads,
+                           "kind": "port", "sample": "%d seeded columns of the study, both waves, modes 1-2, phase "
+                                                     "and group, surfdisp restatement (oracle)" % len(idx)}
+    return acc
+
+
+TT2D_CONFIG = {"workload": "plain 2D travel-time likelihood (the 2D code's path): 51x51 grid over 10x10 km, "
+                           "16 stations on a square perimeter, every station a source to the others (240 times), "
+                           "Voronoi velocity models (4-100 cells, 2-4 km/s), fm2d with the 2D example's settings "
+                           "(gridx=gridy=1, sgref=1, sgdic=5, sgext=10, order=1), FP64 (reference order)",
+               "grid": [51, 51], "stations": 16, "times": 240}
+
+
+def run_tt2d(args):
+    """The plain 2D configuration: every step is one value-change proposal
+    per chain through the host API (2D gridding, 16 fm2d solves, misfit),
+    committed; the plain drop-in is one chain per call."""
+    import torch
+    from mctomo_gb300 import TravelTime2DLikelihood, synthetic
+    rng = np.random.default_rng(SEED + 5)
+    grid, settings, data = synthetic.tt2d_workload(rng)
+    nch = args.chains2d
+    ncells, pts, par = synthetic.tt2d_chain_models(rng, nch, 100, grid)
+    props = []
+    for _ in range(args.warmup + args.steps):
+        q = par.copy()
+        for c in range(nch):
+            i = rng.integers(ncells[c])
+            q[c, i, 0] = np.clip(q[c, i, 0] + rng.normal(0, 0.1), 2.0, 4.0)
+        props.append(q)
+    n0 = np.zeros((nch, 2)); n1 = np.full((nch, 2), 0.05)
+    lk = TravelTime2DLikelihood(grid, settings, data, nslots=nch, ncell_max=100)
+    for i in range(args.warmup):
+        lk.forward(ncells, pts, props[i], n0, n1)
+        lk.commit(np.ones(nch, np.int32))
+    torch.cuda.synchronize()
+    clocks = Clocks(0)
+    clocks.start()
+    ms = []
+    for i in range(args.warmup, args.warmup + args.steps):
+        t0 = time.perf_counter()
+        out = lk.forward(ncells, pts, props[i], n0, n1)
+        lk.commit(np.ones(nch, np.int32))
+        ms.append((time.perf_counter() - t0) * 1e3)
+    cl = clocks.stop()
+    lk.close()
+    value = nch * args.steps / (sum(ms) / 1e3)
+    # the plain drop-in: one chain per call
+    one = TravelTime2DLikelihood(grid, settings, data, nslots=1, ncell_max=100)
+    for i in range(3):
+        one.forward(ncells[:1], pts[:1], props[i][:1], n0[:1], n1[:1])
+    pms = []
+    for i in range(max(args.steps, 20)):
+        t0 = time.perf_counter()
+        one.forward(ncells[i % nch:i % nch + 1], pts[i % nch:i % nch + 1], props[i % len(props)][i % nch:i % nch + 1],
+                    n0[:1], n1[:1])
+        one.commit(np.ones(1, np.int32))
+        pms.append((time.perf_counter() - t0) * 1e3)
+    one.close()
+    line = {"metric": "2D travel-time forward evals/s, 1 GB300, ttime identical to the reference (fm2d FP64)",
+            "value": round(value, 3), "unit": "proposal evals/s", "n_gpus": 1, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": round(sum(ms) / args.steps, 3), "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f64 (fm2d in the reference's order)",
+            "data": "synthetic (seeded, shapes of the configuration)",
+            "config": dict(TT2D_CONFIG, chains=nch),
+            "e2e": {"value": round(value, 3), "unit": "proposal evals/s",
+                    "h2d_bytes_per_step": int(nch * 100 * 5 * 8 + nch * 4 + nch * 4 * 8),
+                    "d2h_bytes_per_step": int(nch * 4 * 8)},
+            "note": "host API only (value = e2e): the 2D context has no device-pointer forward",
+            "batched_latency_ms": {"p50": round(float(np.percentile(ms, 50)), 3),
+                                   "p99": round(float(np.percentile(ms, 99)), 3)},
+            "plain": {"value": round(1e3 / float(np.mean(pms)), 3), "unit": "proposal evals/s",
+                      "p50_ms": round(float(np.percentile(pms, 50)), 3),
+                      "p99_ms": round(float(np.percentile(pms, 99)), 3)},
+            "clocks": cl, "valid_models": int((out[:, 3] == 0).sum())}
+    if not args.no_cpu:
+        line["cpu_baseline"] = tt2d_cpu_baseline(grid, settings, data, ncells, pts, props[0], args)
+    print(json.dumps(line), flush=True)
+
+
+def tt2d_cpu_baseline(grid, settings, data, ncells, pts, par, args):
+    """The oracle's restatement of the 2D path (kd-tree gridding, modrays,
+    the likelihood_dd.F90 reductions) for a sample of proposals, one
+    proposal per host core at a time (the reference's modrays loop over
+    sources is serial)."""
+    import concurrent.futures as cf
+    import oracle
+    orc = oracle.load()
+    P = lambda a: None if a is None else a.ctypes.data_as(ctypes.c_void_p)  # noqa: E731
+    nx, ny = grid["nx"], grid["ny"]
+    src, rev = np.asarray(data["src"]), np.asarray(data["rev"])
+    nsrc, nrev = len(src), len(rev)
+    rays = np.ascontiguousarray(np.asarray(data["raystat"], np.int32).reshape(nsrc, nrev))
+    sx, sy = np.ascontiguousarray(src[:, 0]), np.ascontiguousarray(src[:, 1])
+    threads = os.cpu_count() or 1
+    nsample = min(len(ncells), 4 * threads)
+
+    def one(c):
+        n = int(ncells[c])
+        sid = np.zeros((nx, ny), np.int32); vp = np.zeros((nx, ny)); vs = np.zeros((nx, ny)); rho = np.zeros((nx, ny))
+        orc.orc_kdtree_to_grid(2, n, P(np.ascontiguousarray(pts[c, :n])), P(np.ascontiguousarray(par[c, :n])), nx, ny,
+                               1, grid["xmin"], grid["ymin"], 0.0, grid["dx"], grid["dy"], 0.0, 1, nx, 1, ny, 1, 1,
+                               P(sid), P(vp), P(vs), P(rho))
+        velv = np.ascontiguousarray(np.pad(vp, 1, mode="edge"))
+        et = np.zeros((nsrc, nrev))
+        orc.orc_modrays(nsrc, P(sx), P(sy), nrev, P(sx), P(sy), P(rays), nx, ny, grid["xmin"], grid["ymin"],
+                        grid["dx"], grid["dy"], P(velv), 1, 1, 1, 5, 10, 1, 0.5, P(et), None)
+        out = np.zeros(3)
+        orc.orc_tt2d_misfit(nsrc, nrev, P(et), P(np.ascontiguousarray(data["ttime"])),
+                            P(np.ascontiguousarray(data["sigma"])), P(rays), 0, 0, P(np.zeros(nrev)),
+                            P(np.zeros(nrev)), 0, P(np.zeros(2)), P(np.full(2, 0.05)), data["nrays"], P(out))
+        return out[0]
+
+    t0 = time.perf_counter()
+    with cf.ThreadPoolExecutor(threads) as ex:
+        list(ex.map(one, range(nsample)))
+    dt = time.perf_counter() - t0
+    return {"value": round(nsample / dt, 3), "unit": "proposal evals/s", "cores": threads, "kind": "port",
+            "sample": "%d proposals: kd-tree gridding + modrays (16 sources) + misfit, C++ restatement "
+                      "of the reference path, one proposal per core" % nsample}
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -502,17 +781,24 @@ def main():
     ap.add_argument("--cpu-sample", type=int, default=8)
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--tt-precision", type=int, default=1)
-    ap.add_argument("--workload", default="surface", choices=["surface", "body"])
+    ap.add_argument("--workload", default="surface", choices=["surface", "body", "disp", "tt2d"])
+    ap.add_argument("--chains2d", type=int, default=256, help="tt2d workload: chains per step")
+    ap.add_argument("--columns", type=int, default=262144, help="disp workload: columns")
+    ap.add_argument("--disp-sample", type=int, default=512, help="disp workload: columns checked by the oracle")
     ap.add_argument("--chains", type=int, default=32, help="body workload: chains per step")
     ap.add_argument("--order", type=int, default=0, help="body workload: eikonal order")
     ap.add_argument("--solver", default=None, choices=["tiles", "heap"],
                     help="body workload: 3D solver (default: heap march for order 1, tiles for order 0)")
     args = ap.parse_args()
-    if args.workload == "body":
+    if args.workload in ("body", "disp", "tt2d"):
         if args.impl == "reference":
             print(json.dumps({"impl": "reference", "unavailable": "the reference arm times the surface workload"}))
-        else:
+        elif args.workload == "body":
             run_body(args)
+        elif args.workload == "disp":
+            run_disp(args)
+        else:
+            run_tt2d(args)
     elif args.impl == "reference":
         run_reference(args)
     else:

@@ -389,12 +389,17 @@ int mct_body_forward(mct_body_ctx *ctx, int nchains, const int *ncells,
                      const double *points, const double *params,
                      const double *locations, const double *n0,
                      const double *n1, double *out);
+/* After the Metropolis test: chains with accept[c] != 0 (and a valid
+ * forward) keep the last forward's travel times as their state (the
+ * reference keeps the accepted like and restores the backup on reject,
+ * src/mcmc_loc2.f90:456-465). */
+int mct_body_commit(mct_body_ctx *ctx, int nchains, const int *accept);
 /* Noise-only likelihood, replaces body_noise_likelihood
- * (src/likelihood_body.F90:38-80): the last forward's travel times of batch
- * positions 0..nchains-1 re-reduced with new noise parameters n0, n1
- * (nchains x np) and origin times (locations, nchains x nsrc x 4, the 4th
- * entry used); sigma = n0 * travel time + n1 for every pair. out as
- * mct_body_forward. */
+ * (src/likelihood_body.F90:38-80): chains 0..nchains-1's committed travel
+ * times re-reduced with new noise parameters n0, n1 (nchains x np) and
+ * origin times (locations, nchains x nsrc x 4, the 4th entry used); sigma =
+ * n0 * travel time + n1 for every pair. out as mct_body_forward (status 16:
+ * nothing committed yet). */
 int mct_body_noise_likelihood(mct_body_ctx *ctx, int nchains,
                               const double *locations, const double *n0,
                               const double *n1, double *out);

@@ -44,6 +44,7 @@ SIGNATURES = {
     "mct_body_destroy": (I, [P]),
     "mct_body_forward": (I, [P, I, P, P, P, P, P, P, P]),
     "mct_body_phase_time": (I, [P, I, P, P]),
+    "mct_body_commit": (I, [P, I, P]),
     "mct_body_noise_likelihood": (I, [P, I, P, P, P, P]),
     "mct_tt2d_create": (I, [P, P, P, I, I, P]),
     "mct_tt2d_destroy": (I, [P]),

@@ -74,10 +74,15 @@ class BodyLikelihood:
                                                          ptr(locations), ptr(n0), ptr(n1), ptr(out)))
         return out
 
+    def commit(self, accept):
+        """Chains with accept[c] keep the last forward as their state."""
+        accept = np.ascontiguousarray(accept, np.int32)
+        check("mct_body_commit", lib().mct_body_commit(self.h, accept.size, ptr(accept)))
+
     def noise_likelihood(self, locations, n0, n1):
-        """body_noise_likelihood: the last forward's travel times of batch
-        positions 0..nchains-1 re-reduced with new noise parameters n0/n1
-        (nchains, np) and origin times (locations[..., 3]); no forward."""
+        """body_noise_likelihood: chains 0..nchains-1's committed travel times
+        re-reduced with new noise parameters n0/n1 (nchains, np) and origin
+        times (locations[..., 3]); no forward."""
         n0 = np.ascontiguousarray(n0, np.float64)
         nch = n0.shape[0]
         n0 = n0.reshape(nch, self.np)

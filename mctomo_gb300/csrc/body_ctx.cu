@@ -109,11 +109,24 @@ __global__ void body_misfit_kernel(BodyDev d, int nchains, const double *tt, con
 
 }  // namespace
 
-// body_noise_likelihood (src/likelihood_body.F90:38-80): the last forward's
-// phase times re-reduced with new noise parameters and origin times,
-// sigma = n0 * phase time + n1 for every pair, unused pairs with sigma = 1.
+// An accepted proposal becomes its chain's state (what the reference keeps
+// in `like` after the Metropolis step; a rejected one is restored from the
+// backup, src/mcmc_loc2.f90:456-465).
+__global__ void body_commit_kernel(int n, const int *accept, const double *out, const double *ptime, double *cptime,
+                                   int *committed) {
+  const int c = blockIdx.y;
+  if (!accept[c] || out[(size_t)c * 4 + 3] != 0.0) return;
+  for (int q = blockIdx.x * blockDim.x + threadIdx.x; q < n; q += gridDim.x * blockDim.x)
+    cptime[(size_t)c * n + q] = ptime[(size_t)c * n + q];
+  if (blockIdx.x == 0 && threadIdx.x == 0) committed[c] = 1;
+}
+
+// body_noise_likelihood (src/likelihood_body.F90:38-80): each chain's
+// committed phase times re-reduced with new noise parameters and origin
+// times, sigma = n0 * phase time + n1 for every pair, unused pairs with
+// sigma = 1; status 16 when nothing is committed yet.
 __global__ void body_noise_kernel(BodyDev d, const double *ptime, const double *loc, const double *n0,
-                                  const double *n1, double *out) {
+                                  const double *n1, const int *committed, double *out) {
   const int c = blockIdx.x;
   const int npairs = d.nsrc * d.nrev;
   double like = 0, mis = 0, umis = 0, slog = 0;
@@ -142,10 +155,11 @@ __global__ void body_noise_kernel(BodyDev d, const double *ptime, const double *
   }
   if (threadIdx.x == 0) {
     const double PI2 = (double)6.283185f;
-    out[(size_t)c * 4 + 0] = red[0][0] + red[3][0] + (double)((float)d.nrays / 2.0f) * log(PI2);
+    const bool ok = committed[c] != 0;
+    out[(size_t)c * 4 + 0] = ok ? red[0][0] + red[3][0] + (double)((float)d.nrays / 2.0f) * log(PI2) : DBL_MAX;
     out[(size_t)c * 4 + 1] = red[1][0];
     out[(size_t)c * 4 + 2] = red[2][0];
-    out[(size_t)c * 4 + 3] = 0.0;
+    out[(size_t)c * 4 + 3] = ok ? 0.0 : 16.0;
   }
 }
 
@@ -161,6 +175,8 @@ struct mct_body_ctx {
   int *sites = nullptr; double *vel = nullptr; float *slow = nullptr;
   int *tie_count = nullptr, *tie_nodes = nullptr; void *kd = nullptr; int *gstatus = nullptr;
   double *esrc = nullptr, *erecv = nullptr, *ett = nullptr, *ptime = nullptr;
+  double *cptime = nullptr, *nout = nullptr;          // committed times, noise-only results
+  int *committed = nullptr, *accept = nullptr;
   int *egrid = nullptr, *eset = nullptr, *T = nullptr, *list = nullptr, *count = nullptr;
   unsigned char *flags = nullptr;
   // 3D solver and the heap march's scratch
@@ -217,7 +233,8 @@ int mct_body_create(const mct_grid *g, const mct_body_settings *st, const mct_bo
       sizeof(int) * nT, ntile * nsolve, sizeof(int) * ntile * nsolve, sizeof(int),
       sizeof(int) * np * npairs, sizeof(double) * 2 * np * npairs,
       heap ? sizeof(double2) * 2 * (size_t)nslots * nn : 0,
-      eik3_heap_scratch_bytes(g->nx, g->ny, g->nz, (int)hchunk), sizeof(int)};
+      eik3_heap_scratch_bytes(g->nx, g->ny, g->nz, (int)hchunk), sizeof(int),
+      sizeof(double) * (size_t)nslots * np * npairs, sizeof(int) * 2 * nslots, sizeof(double) * 4 * nslots};
   size_t total = 0;
   for (size_t s : sz) total = ((total + 255) & ~size_t(255)) + s;
   total += 256;
@@ -256,6 +273,11 @@ int mct_body_create(const mct_grid *g, const mct_body_settings *st, const mct_bo
   c->hvn = cv.take<double2>(heap ? 2 * (size_t)nslots * nn : 0);
   c->hscratch = cv.take<char>(eik3_heap_scratch_bytes(g->nx, g->ny, g->nz, (int)hchunk));
   c->herr = cv.take<int>(1);
+  c->cptime = cv.take<double>((size_t)nslots * np * npairs);
+  c->committed = cv.take<int>(2 * (size_t)nslots);
+  c->accept = c->committed + nslots;
+  c->nout = cv.take<double>(4 * (size_t)nslots);
+  cudaMemset(c->committed, 0, sizeof(int) * 2 * nslots);
   c->hchunk = (int)hchunk;
   std::vector<double> hs((size_t)np * npairs, 1.0);
   if (dat->sigma) for (size_t q = 0; q < hs.size(); ++q) hs[q] = dat->sigma[q];
@@ -352,17 +374,29 @@ int mct_body_forward(mct_body_ctx *c, int nchains, const int *ncells, const doub
   return MCT_OK;
 }
 
+int mct_body_commit(mct_body_ctx *c, int nchains, const int *accept) {
+  if (!c || nchains < 1 || nchains > c->last_nchains || !accept) return MCT_ERR_ARG;
+  cudaStream_t s = c->stream;
+  const int n = c->dev.np * c->dev.nsrc * c->dev.nrev;
+  MCT_CUDA_TRY(cudaMemcpyAsync(c->accept, accept, sizeof(int) * nchains, cudaMemcpyHostToDevice, s));
+  body_commit_kernel<<<dim3((n + 255) / 256, nchains), 256, 0, s>>>(n, c->accept, c->out, c->ptime, c->cptime,
+                                                                    c->committed);
+  MCT_CUDA_TRY(cudaGetLastError());
+  MCT_CUDA_TRY(cudaStreamSynchronize(s));
+  return MCT_OK;
+}
+
 int mct_body_noise_likelihood(mct_body_ctx *c, int nchains, const double *locations, const double *n0,
                               const double *n1, double *out) {
-  if (!c || nchains < 1 || nchains > c->last_nchains || !locations || !n0 || !n1 || !out) return MCT_ERR_ARG;
+  if (!c || nchains < 1 || nchains > c->nslots || !locations || !n0 || !n1 || !out) return MCT_ERR_ARG;
   cudaStream_t s = c->stream;
   const BodyDev &d = c->dev;
   MCT_CUDA_TRY(cudaMemcpyAsync(c->loc, locations, sizeof(double) * nchains * d.nsrc * 4, cudaMemcpyHostToDevice, s));
   MCT_CUDA_TRY(cudaMemcpyAsync(c->n0, n0, sizeof(double) * nchains * d.np, cudaMemcpyHostToDevice, s));
   MCT_CUDA_TRY(cudaMemcpyAsync(c->n1, n1, sizeof(double) * nchains * d.np, cudaMemcpyHostToDevice, s));
-  body_noise_kernel<<<nchains, 256, 0, s>>>(d, c->ptime, c->loc, c->n0, c->n1, c->out);
+  body_noise_kernel<<<nchains, 256, 0, s>>>(d, c->cptime, c->loc, c->n0, c->n1, c->committed, c->nout);
   MCT_CUDA_TRY(cudaGetLastError());
-  MCT_CUDA_TRY(cudaMemcpyAsync(out, c->out, sizeof(double) * 4 * nchains, cudaMemcpyDeviceToHost, s));
+  MCT_CUDA_TRY(cudaMemcpyAsync(out, c->nout, sizeof(double) * 4 * nchains, cudaMemcpyDeviceToHost, s));
   MCT_CUDA_TRY(cudaStreamSynchronize(s));
   return MCT_OK;
 }

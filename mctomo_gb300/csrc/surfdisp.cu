@@ -301,13 +301,18 @@ __device__ double nevill(double t, double c1, double c2, double del1, double del
   return c3;
 }
 
+// Scans step dc from at most (betmx - cm)/dc + a margin; a NaN trial
+// velocity (which the reference would step forever) ends the scan as a
+// failure after this many steps.
+constexpr int kMaxScan = 1 << 20;
+
 // The reference's sequential bracketing scan in FP64 (surfdisp96.f:793-815).
 // Returns 1 with c1/c2/del1/del2 set on a bracket, -1 on failure.
 __device__ __forceinline__ int scan64(double t1, double &c1, double &del1, double &c2, double &del2,
                                       int idir, double clow, double dc, double cm, float betmx,
                                       int ifunc, Ctx &cx) {
   const double twopi = 2.0 * 3.141592653589793;
-  for (;;) {
+  for (int it = 0; it < kMaxScan; ++it) {
     if (idir > 0) c2 = c1 + dc; else c2 = c1 - dc;
     if (c2 <= clow) { idir = +1; c1 = clow; continue; }
     double omega = twopi / t1;
@@ -317,6 +322,7 @@ __device__ __forceinline__ int scan64(double t1, double &c1, double &del1, doubl
     if (c1 < cm) return -1;
     if (c1 >= ((double)betmx + dc)) return -1;
   }
+  return -1;
 }
 
 // surfdisp96.f:734-827 getsol
@@ -336,7 +342,8 @@ __device__ void getsol(double t1, double &c1, double clow, double dc, double cm,
     float fa = dltar32(omega / c1, omega, ifunc, cx);
     float s0 = fsign1f(fa);
     bool found = false, fail = false;
-    for (;;) {
+    for (int it = 0;; ++it) {
+      if (it >= kMaxScan) { fail = true; break; }
       cb = ca + dc;
       if (cb <= clow) { found = false; break; }  // cannot happen going up; fall back
       float fb = dltar32(omega / cb, omega, ifunc, cx);
@@ -358,7 +365,7 @@ __device__ void getsol(double t1, double &c1, double clow, double dc, double cm,
   if (r == 0) r = scan64(t1, c1, del1, c2, del2, idir, clow, dc, cm, betmx, ifunc, cx);
   if (r < 0) { iret = -1; return; }
   c1 = nevill(t1, c1, c2, del1, del2, ifunc, cx);
-  if (c1 > (double)betmx) { iret = -1; return; }
+  if (c1 > (double)betmx || !isfinite(c1)) { iret = -1; return; }
   iret = 1;
 }
 

@@ -94,11 +94,17 @@ def test_body_noise_likelihood_matches_oracle(orc, gpulib):
     lk.forward(ncells, pts, par, locs, np.zeros((nch, 2)), np.full((nch, 2), 0.05))
     m0 = np.array([[0.01, 0.02], [0.0, 0.03]]); m1 = np.array([[0.04, 0.05], [0.06, 0.02]])
     locs2 = locs.copy(); locs2[:, :, 3] += rng.uniform(-0.2, 0.2, (nch, locs.shape[1]))
+    assert np.all(lk.noise_likelihood(locs2, m0, m1)[:, 3] == 16)    # nothing committed yet
+    lk.commit(np.ones(nch, np.int32))
+    committed = [lk.phase_time(c)[0] for c in range(nch)]
+    # a rejected proposal leaves the committed times
+    lk.forward(ncells, pts, par * 1.05, locs, np.zeros((nch, 2)), np.full((nch, 2), 0.05))
+    lk.commit(np.zeros(nch, np.int32))
     got = lk.noise_likelihood(locs2, m0, m1)
     nsrc, nrev = data["nsrc"], len(data["rev"])
     npairs = nsrc * nrev
     for c in range(nch):
-        pt, _ = lk.phase_time(c)
+        pt = committed[c]
         dtt = np.zeros((2, 3, npairs)); dtt[:, 0] = data["ttime"]; dtt[:, 1] = data["sigma"]
         rs = np.zeros((2, 2, npairs), np.int32); rs[:, 0] = data["raystat"]
         ptf = np.ascontiguousarray(pt.reshape(2, npairs))
