@@ -184,7 +184,13 @@ int mct_surfdisp_batch_device(int ncol, int nl_max, const int *nl, const float *
   job.np = np; job.periods = periods; job.iwave = iwave; job.mode = mode; job.igr = igr;
   job.dphase = dphase; job.multimode = multimode; job.precision = precision ? 1 : 0;
   job.cp = cp; job.cg = cg; job.ierr = ierr; job.ndltar = ndltar;
-  return launch_surfdisp(job, static_cast<cudaStream_t>(stream));
+  if (ncol == 0) return MCT_OK;
+  // the column order scratch, on the caller's stream ordering
+  cudaStream_t s = static_cast<cudaStream_t>(stream);
+  MCT_CUDA_TRY(cudaMallocAsync(&job.order, sizeof(int) * (size_t)ncol, s));
+  const int rc = launch_surfdisp(job, s);
+  cudaFreeAsync(job.order, s);
+  return rc;
 }
 
 int mct_surfdisp_batch(int ncol, int nl_max, const int *nl, const float *thk, const float *vp,
@@ -200,7 +206,8 @@ int mct_surfdisp_batch(int ncol, int nl_max, const int *nl, const float *thk, co
   size_t lay = (size_t)ncol * nl_max;
   size_t outn = (size_t)ncol * mode * np;
   size_t bytes = carve_size({sizeof(int) * ncol, 4 * sizeof(float) * lay, sizeof(double) * np,
-                             2 * sizeof(double) * outn, sizeof(int) * ncol, 2 * sizeof(unsigned long long)});
+                             2 * sizeof(double) * outn, sizeof(int) * ncol, 2 * sizeof(unsigned long long),
+                             sizeof(int) * ncol});
   rc = g_ws.reserve(bytes); if (rc) return rc;
   Carve cv(g_ws.p);
   int *d_nl = cv.take<int>(ncol);
@@ -209,6 +216,7 @@ int mct_surfdisp_batch(int ncol, int nl_max, const int *nl, const float *thk, co
   double *d_out = cv.take<double>(2 * outn);
   int *d_ierr = cv.take<int>(ncol);
   unsigned long long *d_cnt = cv.take<unsigned long long>(2);
+  int *d_order = cv.take<int>(ncol);
   cudaStream_t s = g_stream;
   MCT_CUDA_TRY(cudaMemcpyAsync(d_nl, nl, sizeof(int) * ncol, cudaMemcpyHostToDevice, s));
   MCT_CUDA_TRY(cudaMemcpyAsync(d_lay, thk, sizeof(float) * lay, cudaMemcpyHostToDevice, s));
@@ -222,7 +230,7 @@ int mct_surfdisp_batch(int ncol, int nl_max, const int *nl, const float *thk, co
   job.thk = d_lay; job.vp = d_lay + lay; job.vs = d_lay + 2 * lay; job.rho = d_lay + 3 * lay;
   job.np = np; job.periods = d_per; job.iwave = iwave; job.mode = mode; job.igr = igr;
   job.dphase = dphase; job.multimode = multimode; job.precision = precision ? 1 : 0;
-  job.cp = d_out; job.cg = d_out + outn; job.ierr = d_ierr; job.ndltar = d_cnt;
+  job.cp = d_out; job.cg = d_out + outn; job.ierr = d_ierr; job.ndltar = d_cnt; job.order = d_order;
   rc = launch_surfdisp(job, s); if (rc) return rc;
   MCT_CUDA_TRY(cudaMemcpyAsync(cp, d_out, sizeof(double) * outn, cudaMemcpyDeviceToHost, s));
   MCT_CUDA_TRY(cudaMemcpyAsync(cg, d_out + outn, sizeof(double) * outn, cudaMemcpyDeviceToHost, s));

@@ -94,5 +94,6 @@ struct DispJob {
   double *cp, *cg;       // [ncol][mode][np]
   int *ierr;             // [ncol]
   unsigned long long *ndltar; // optional [2]: FP64 and FP32 period-equation evaluations
+  int *order;            // optional [ncol] scratch: columns are run in order of layer count
 };
 int launch_surfdisp(const DispJob &job, cudaStream_t s);

@@ -128,7 +128,8 @@ int surf_create(const mct_grid *g, const mct_surf_settings *st, const mct_surf_d
       sizeof(int) * (size_t)nslots * np, sizeof(double) * (size_t)npairs, sizeof(double) * 2 * (nsrc + nrev),
       sizeof(double) * (size_t)nslots * np * npairs,
       (b.igr && !b.straight) ? sizeof(double) * (size_t)fp.nref_max * nsolve : 0,
-      (b.igr && !b.straight) ? sizeof(short) * (size_t)fp.nref_max * nsolve : 0};
+      (b.igr && !b.straight) ? sizeof(short) * (size_t)fp.nref_max * nsolve : 0,
+      sizeof(int) * (size_t)nslots * ncol};
   size_t total = 0;
   for (size_t s : sz) total = ((total + 255) & ~size_t(255)) + s;
   total += 256;
@@ -210,6 +211,7 @@ int surf_create(const mct_grid *g, const mct_surf_settings *st, const mct_surf_d
   b.csrd = cv.take<double>((size_t)nslots * np * npairs);
   fj.ref_t = cv.take<double>((b.igr && !b.straight) ? (size_t)fp.nref_max * nsolve : 0);
   fj.ref_s = cv.take<short>((b.igr && !b.straight) ? (size_t)fp.nref_max * nsolve : 0);
+  b.lorder = cv.take<int>((size_t)nslots * ncol);
   b.sdist = sdist;
   c->plan.src_xy = sxy; c->plan.rev_xy = sxy + 2 * nsrc;
   {

@@ -377,7 +377,7 @@ int surf_forward(SurfBatch &b, const SurfPlan &plan, cudaStream_t s, SurfProfile
   dj.thk = b.lthk; dj.vp = b.lvp; dj.vs = b.lvs; dj.rho = b.lrho;
   dj.np = b.np; dj.periods = b.periods; dj.iwave = b.iwave; dj.mode = 1; dj.igr = b.igr;
   dj.dphase = b.dphase; dj.multimode = 0; dj.precision = b.precision;
-  dj.cp = b.lcp; dj.cg = b.lcg; dj.ierr = b.lierr; dj.ndltar = b.ndltar;
+  dj.cp = b.lcp; dj.cg = b.lcg; dj.ierr = b.lierr; dj.ndltar = b.ndltar; dj.order = b.lorder;
   rc = launch_surfdisp(dj, s); if (rc) return rc;
   gather_committed_maps<<<dim3(64, nch), 256, 0, s>>>(b);
   MCT_CUDA_TRY(cudaGetLastError());

@@ -37,6 +37,7 @@ struct SurfBatch {
   int nl_max;
   int *lnl; float *lthk, *lvp, *lvs, *lrho;   // [nchains*ncol][nl_max]
   double *lcp, *lcg; int *lierr;               // [nchains*ncol][np]
+  int *lorder;                                 // [nchains*ncol] dispersion column order
   unsigned long long *ndltar;
   double *pvel;              // [nchains][np][nx][ny]
   double *velv;              // [nchains*np][(nx+2)*(ny+2)]

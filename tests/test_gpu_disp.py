@@ -116,3 +116,26 @@ def test_lvl_columns_of_the_precision_study_run_on_surfdisp96(orc, gpulib):
     assert same.mean() > 0.95
     ok = (ierr == 0) & (eierr == 0)
     assert np.max(np.abs(cp[ok] - ecp[ok])) <= PHASE_TOL
+
+
+@pytest.mark.parametrize("iwave,precision", [(2, 1), (1, 1), (2, 0)])
+def test_lanes_evaluating_ahead_give_the_same_roots(gpulib, iwave, precision):
+    # idle lanes evaluate the next trial velocities of long bracketing scans,
+    # and the columns run in order of layer count; every root, group
+    # velocity, error flag must be the same bits as with each column
+    # scanning alone in batch order (multimode, group, columns of the
+    # precision study with low-velocity layers, which give the long scans)
+    rng = np.random.default_rng(44 + iwave + precision)
+    nl, thk, vp, vs, rho = synthetic.layered_columns(rng, 256, nl_range=(12, 40), lvl_prob=0.1)
+    per = np.geomspace(0.2, 20.0, 60)
+    old = gpulib.mct_debug_disp_share(0)       # no lookahead, columns in batch order
+    try:
+        a = surfdisp_batch(nl, thk, vp, vs, rho, per, iwave, 1, 0.001, mode=2, multimode=True, precision=precision)
+        gpulib.mct_debug_disp_share(3)           # lookahead, columns by layer count
+        b = surfdisp_batch(nl, thk, vp, vs, rho, per, iwave, 1, 0.001, mode=2, multimode=True, precision=precision)
+    finally:
+        gpulib.mct_debug_disp_share(old)
+    np.testing.assert_array_equal(a[2], b[2])
+    np.testing.assert_array_equal(a[0], b[0])
+    np.testing.assert_array_equal(a[1], b[1])
+    assert sum(b[3]) > sum(a[3])      # some values were evaluated ahead (and some not used)
