@@ -3,7 +3,7 @@
     python -m mctomo_gb300.profcase fm2d [--precision P] [--maps M] [--repeat R]
     python -m mctomo_gb300.profcase eik3 [--order O]
     python -m mctomo_gb300.profcase eik3heap [--order O] [--solves N]
-    python -m mctomo_gb300.profcase disp [--precision P] [--columns N]
+    python -m mctomo_gb300.profcase disp [--precision P] [--columns N] [--study]
     python -m mctomo_gb300.profcase grid
 
 fm2d: M Voronoi phase maps of 41 x 41 vertices (1 km spacing), 50 stations
@@ -13,7 +13,10 @@ mct_modrays_batch. eik3: 8 velocity grids of 101 x 101 x 51 nodes (0.5 km),
 120 solves. eik3heap: the exact heap march, N solves (default 8) on 4
 Voronoi grids of 51 x 51 x 26 nodes (0.5 km, velocities 3-7.5 km/s). disp: N layered columns (12-40 layers, no low-velocity layers),
 20 Rayleigh fundamental-mode phase periods log-spaced 0.5-5 s, the surface
-likelihood's search increment 1e-3 km/s. grid: nearest-nucleus gridding of a
+likelihood's search increment 1e-3 km/s; with --study, N columns of the
+dispersion-precision study instead (12-40 layers with a 10 % low-velocity
+layer chance, 60 periods 0.2-20 s, fundamental and first overtone, phase and
+group, multimode). grid: nearest-nucleus gridding of a
 101 x 101 x 51 grid over 50 x 50 x 25 km from 800 nuclei. Each case prints
 one line and exits 0.
 """
@@ -79,14 +82,21 @@ def eik3heap(order=1, solves=8):
     print(f"eik3heap order={order} solves={solves} call_s={dt:.4f} t00={tt[0, 0]:.6f}")
 
 
-def disp(precision=1, columns=4096):
+def disp(precision=1, columns=4096, study=False):
     rng = np.random.default_rng(2)
-    nl, thk, vp, vs, rho = synthetic.layered_columns(rng, columns, lvl_prob=0.0)
-    periods = np.geomspace(0.5, 5.0, 20)
+    if study:
+        nl, thk, vp, vs, rho = synthetic.layered_columns(rng, columns, nl_range=(12, 40), lvl_prob=0.1)
+        periods = np.geomspace(0.2, 20.0, 60)
+        kw = dict(mode=2, multimode=True)
+    else:
+        nl, thk, vp, vs, rho = synthetic.layered_columns(rng, columns, lvl_prob=0.0)
+        periods = np.geomspace(0.5, 5.0, 20)
+        kw = {}
     t0 = time.perf_counter()
-    cp, _, ierr, cnt = forward.surfdisp_batch(nl, thk, vp, vs, rho, periods, 2, 0, 1e-3, precision=precision)
+    cp, _, ierr, cnt = forward.surfdisp_batch(nl, thk, vp, vs, rho, periods, 2, int(study), 1e-3,
+                                              precision=precision, **kw)
     dt = time.perf_counter() - t0
-    print(f"disp precision={precision} columns={columns} call_s={dt:.4f} ierr={int((ierr != 0).sum())} "
+    print(f"disp precision={precision} columns={columns} study={int(study)} call_s={dt:.4f} ierr={int((ierr != 0).sum())} "
           f"evals_fp64={cnt[0]} evals_fp32={cnt[1]} cp00={cp[0, 0, 0]:.6f}")
 
 
@@ -111,6 +121,7 @@ def main(argv=None):
     ap.add_argument("--maps", type=int, default=16)
     ap.add_argument("--repeat", type=int, default=2)
     ap.add_argument("--order", type=int, default=None)
+    ap.add_argument("--study", action="store_true")
     a = ap.parse_args(argv)
     if a.case == "fm2d":
         fm2d(a.precision, a.maps, a.repeat)
@@ -119,7 +130,7 @@ def main(argv=None):
     elif a.case == "eik3heap":
         eik3heap(1 if a.order is None else a.order, a.solves)
     elif a.case == "disp":
-        disp(a.precision, a.columns)
+        disp(a.precision, a.columns, a.study)
     else:
         grid()
 
