@@ -510,6 +510,16 @@ def body_cpu_baseline(grid, settings, data, ev, prop, args):
 
 
 LOVE_COLS = 16384
+# FP64 operations (add, sub, mul, div, sqrt) of one layer iteration of the
+# period equation, counted from the source (surfdisp96.f:1119-1217 with var
+# 1220-1337, dnka 1370-1414, normc 1341-1366 for Rayleigh; dltar1
+# 1056-1115 for Love), propagating case; sin / cos / exp are counted
+# separately (5 per Rayleigh layer, 2 per Love layer). Rayleigh: layer
+# set-up 16 (3 div, 2 sqrt) + var 14 (2 div) + dnka 78 (4 div) + 5x5
+# matrix-vector product 50 + normalisation 5 (div) = 163. Love: 20 (4 div,
+# 1 sqrt).
+DISP_OPS_PER_LAYER = {2: 163, 1: 20}
+FP64_NOMINAL_TFLOPS = 1.25
 DISP_CONFIG = {"workload": "dispersion-precision study: 262,144 independent layered columns (12-40 layers, "
                            "thickness U[0.05,0.5] km, Vs U[0.2,3.5] km/s with a 10% low-velocity-layer chance, "
                            "Vp = 1.73 Vs, Gardner density), 60 periods 0.2-20 s, Rayleigh and Love, fundamental "
@@ -586,6 +596,17 @@ def run_disp(args):
     e2e_s = time.perf_counter() - t0
     acc = disp_oracle_sample(nl, thk, vp, vs, rho, periods, args)
     value = res[1][1]
+    # Roofline of the FP64 variant, whose evaluations are the reference's own:
+    # algorithmic FP64 operations = the oracle's layer-evaluations x the
+    # operations of one layer of the period equation (see DISP_OPS_PER_LAYER)
+    lev = acc.pop("oracle_layer_evals_per_column")
+    ops = DISP_OPS_PER_LAYER[2] * lev[2] * ncol + DISP_OPS_PER_LAYER[1] * lev[1] * love_cols
+    achieved = ops / (res[0][0] / 1e3) / 1e12
+    roofline = {"kernel": "surfdisp_kernel, FP64 variant", "bound": "fp64", "achieved": round(achieved, 4),
+                "peak": FP64_NOMINAL_TFLOPS, "peak_kind": "nominal (no measured FP64 peak)", "unit": "TFLOP/s",
+                "frac": round(achieved / FP64_NOMINAL_TFLOPS, 4), "traffic": None,
+                "algorithmic_fp64_ops_per_step": round(ops), "ops_per_layer": DISP_OPS_PER_LAYER,
+                "transcendentals_per_layer": {"rayleigh": 5, "love": 2}}
     line = {"metric": "dispersion curves/s (column x wave x mode, phase + group), 1 GB300, phase err<=1e-5 km/s",
             "value": round(value, 2), "unit": "curves/s", "n_gpus": 1, "steps": args.steps, "warmup": args.warmup,
             "ms_per_step": round(res[1][0], 3), "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
@@ -598,7 +619,7 @@ def run_disp(args):
             "e2e": {"value": round((ncol + love_cols) * 2 / e2e_s, 2), "unit": "curves/s",
                     "h2d_bytes_per_step": int(4 * 4 * ncol * nl_max + 4 * ncol + 60 * 8) * 2,
                     "d2h_bytes_per_step": int(2 * ncol * 2 * 60 * 8 + 4 * ncol) * 2},
-            "accuracy": acc, "clocks": cl}
+            "accuracy": acc, "clocks": cl, "roofline": roofline, "gpu_launches": 4 * args.steps}
     if not args.no_cpu:
         line["cpu_baseline"] = acc.pop("cpu_baseline")
     else:
@@ -625,14 +646,20 @@ def disp_oracle_sample(nl, thk, vp, vs, rho, periods, args):
     t0 = time.perf_counter()
     for iwave in (2, 1):
         def one(k):
-            o1 = np.zeros(120); o2 = np.zeros(120)
+            o1 = np.zeros(120); o2 = np.zeros(120); n = np.zeros(1, np.int64)
             e = orc.orc_surfdisp_mmodes(*[P(x) for x in cols[k]], int(len(cols[k][0])), iwave, 2, 1, 60,
-                                        P(periods), 0.001, P(o1), P(o2), None)
-            return e, o1.reshape(2, 60), o2.reshape(2, 60)
+                                        P(periods), 0.001, P(o1), P(o2), P(n))
+            return e, o1.reshape(2, 60), o2.reshape(2, 60), int(n[0])
         with cf.ThreadPoolExecutor(threads) as ex:
             out[iwave] = list(ex.map(one, range(len(idx))))
     cpu_s = time.perf_counter() - t0
     acc = {"columns_sampled": int(len(idx)), "lvl_columns_sampled": int(lvl.sum())}
+    # the reference's own FP64 work, counted by the oracle: evaluations x layer
+    # iterations per evaluation (nl - llw; llw = 2 under a water layer), mean
+    # per column of the sample, per wave type
+    layers = np.array([len(c[0]) - (2 if c[2][0] <= 0 else 1) for c in cols])
+    acc["oracle_layer_evals_per_column"] = {
+        w: float(np.mean([out[w][k][3] * layers[k] for k in range(len(idx))])) for w in (2, 1)}
     for precision, name in ((1, "fp32_bracketing_fp64_polish"), (0, "fp64")):
         worst = {"plain": [0.0, 0.0], "lvl": [0.0, 0.0]}
         agree = 0
@@ -640,7 +667,7 @@ def disp_oracle_sample(nl, thk, vp, vs, rho, periods, args):
             cp, cg, ierr, _ = forward.surfdisp_batch(nl[idx], thk[idx], vp[idx], vs[idx], rho[idx], periods, iwave,
                                                      1, 0.001, mode=2, multimode=True, precision=precision)
             for k in range(len(idx)):
-                e, ecp, ecg = out[iwave][k]
+                e, ecp, ecg, _ = out[iwave][k]
                 agree += int(e == ierr[k])
                 good = (ecp > 0) & (cp[k] > 0)
                 key = "lvl" if lvl[k] else "plain"

@@ -111,8 +111,10 @@ int mct_surfmodes(const double *thick, const double *vp, const double *vs,
 /* Many columns at once (host buffers): layer arrays [ncol][nl_max] REAL*4,
  * nl[ncol]; cp/cg [ncol][mode][np]; ierr[ncol]. precision 0 = FP64 root
  * search as the reference; 1 = FP32 bracketing confirmed in FP64, then FP64
- * polish (same roots). ndltar (optional, 2 entries) counts FP64 and FP32
- * period-equation evaluations. */
+ * polish (same roots). ndltar (optional, 2 entries) counts the FP64 and
+ * FP32 period-equation evaluations the root searches used; with precision 0
+ * the FP64 count is the reference's own (values the kernel evaluates ahead
+ * of a scan and the scan never reaches are not counted). */
 int mct_surfdisp_batch(int ncol, int nl_max, const int *nl, const float *thk,
                        const float *vp, const float *vs, const float *rho,
                        int np, const double *periods, int iwave, int mode,

@@ -746,6 +746,31 @@ __device__ double refined_velocity(const Fm2dJob &job, const RefineBox &rb, int 
   return sum[0] + sum[1] + sum[2] + sum[3];
 }
 
+// The same with the B-spline weights bsw(q, u) read from tables: wu[(l-1)*4
+// + q] = bsw(q, (l-1)/nrxr) for l = 1 .. nrxr+1, wv likewise along z. The
+// weights are the same values computed once, so the velocity is the same.
+__device__ double refined_velocity_tab(const Fm2dJob &job, const RefineBox &rb, int idm1, int idm2,
+                                       const double *wu, const double *wv) {
+  const int sgdl = job.sgdl;
+  int st1 = idm1 + rb.origz - 1, st2 = idm2 + rb.origx - 1;
+  int i = (st1 - 1) / rb.nrzr + 1; if (i > job.nvz - 1) i = job.nvz - 1;
+  int k = st1 - rb.nrzr * (i - 1);
+  int j = (st2 - 1) / rb.nrxr + 1; if (j > job.nvx - 1) j = job.nvx - 1;
+  int l = st2 - rb.nrxr * (j - 1);
+  int c1 = job.gdz * (i - 1) + (k - 1) / sgdl + 1;
+  int c2 = job.gdx * (j - 1) + (l - 1) / sgdl + 1;
+  if (c1 < rb.vnt || c1 > rb.vnb || c2 < rb.vnl || c2 > rb.vnr) return 0.0;
+  const double *bu = wu + 4 * (l - 1), *bv = wv + 4 * (k - 1);
+  double sum[4];
+  for (int i1 = 1; i1 <= 4; ++i1) {
+    sum[i1 - 1] = 0.0;
+    for (int j1 = 1; j1 <= 4; ++j1)
+      sum[i1 - 1] = sum[i1 - 1] + bu[j1 - 1] * rb.velv[(size_t)(j - 2 + j1) * rb.ldv + (i - 2 + i1)];
+    sum[i1 - 1] = bv[i1 - 1] * sum[i1 - 1];
+  }
+  return sum[0] + sum[1] + sum[2] + sum[3];
+}
+
 // GetVelocity (src/likelihood_surf.F90:496-521): bilinear velocity of one
 // map of the model grid (Fortran (nvz, nvx)) at (px, pz).
 __device__ double get_velocity(const double *vel, int nx, int nz, double gox, double goz, double dx, double dz,
@@ -860,8 +885,25 @@ fm2d_refined_kernel(Fm2dJob job, int warp_bytes, int heap_cap, int redo) {
   const int ldv = job.nvz + 2;
   const RefineBox rb{job.velv + (size_t)sg.map * (job.nvx + 2) * ldv, ldv, (vnl - 1) * sgdl + 1,
                      (vnt - 1) * sgdl + 1, job.gdx * sgdl, job.gdz * sgdl, vnl, vnr, vnt, vnb};
-  for (int node = lane; node < nrnx * nrnz; node += 32)
-    store_slowness(Sr, node, 1.0 / refined_velocity(job, rb, node % nrnz + 1, node / nrnz + 1), job.precision);
+  // the B-spline weight tables sit in the (not yet used) time array
+  const int ntab = 4 * (rb.nrxr + 1) + 4 * (rb.nrzr + 1);
+  if ((size_t)ntab * sizeof(double) <= (size_t)job.nref_max * sizeof(TT)) {
+    double *wu = reinterpret_cast<double *>(w.T), *wv = wu + 4 * (rb.nrxr + 1);
+    for (int q = lane; q < ntab; q += 32) {
+      const bool alx = q < 4 * (rb.nrxr + 1);
+      const int e = alx ? q : q - 4 * (rb.nrxr + 1);
+      const double u = (double)(e / 4) / (double)(alx ? rb.nrxr : rb.nrzr);
+      wu[q] = bsw(e & 3, u);
+    }
+    __syncwarp();
+    for (int node = lane; node < nrnx * nrnz; node += 32)
+      store_slowness(Sr, node, 1.0 / refined_velocity_tab(job, rb, node % nrnz + 1, node / nrnz + 1, wu, wv),
+                     job.precision);
+    __syncwarp();
+  } else {
+    for (int node = lane; node < nrnx * nrnz; node += 32)
+      store_slowness(Sr, node, 1.0 / refined_velocity(job, rb, node % nrnz + 1, node / nrnz + 1), job.precision);
+  }
   for (int q = lane; q < nrnx * nrnz; q += 32) w.S[q] = -1;
   w.ld = gr.ld;
   __syncwarp();

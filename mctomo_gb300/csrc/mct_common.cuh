@@ -93,7 +93,7 @@ struct DispJob {
   int precision;         // 0: FP64 bracketing, 1: FP32 bracketing + FP64 polish
   double *cp, *cg;       // [ncol][mode][np]
   int *ierr;             // [ncol]
-  unsigned long long *ndltar; // optional [2]: FP64 and FP32 period-equation evaluations
+  unsigned long long *ndltar; // optional [2]: FP64 and FP32 period-equation evaluations used
   int *order;            // optional [ncol] scratch: columns are run in order of layer count
 };
 int launch_surfdisp(const DispJob &job, cudaStream_t s);

@@ -317,12 +317,17 @@ struct Search {
   // the one the step computes; any real request empties the buffer.
   double pfc[32], pfv[32];
   int pf_n, pf_i, pf32;
+  unsigned long long used64, used32;   // values ahead that the search used
 
   __device__ void request(double cval, int fp32, int resume) {
     req = cval; req32 = fp32; st = resume; pf_n = 0; pf_i = 0;
   }
   __device__ bool prefetched(double cval, int fp32, double &v) {
-    if (pf_i < pf_n && pf32 == fp32 && pfc[pf_i] == cval) { v = pfv[pf_i++]; return true; }
+    if (pf_i < pf_n && pf32 == fp32 && pfc[pf_i] == cval) {
+      v = pfv[pf_i++];
+      if (fp32) ++used32; else ++used64;
+      return true;
+    }
     return false;
   }
   // The trial velocity `ahead` steps after the pending request `c` of a
@@ -676,7 +681,7 @@ __global__ void __launch_bounds__(32) surfdisp_kernel(DispJob job, int share) {
   unsigned long long n64 = 0, n32 = 0;
   Search S;
   S.st = S_DONE; S.req = 0.0; S.req32 = 0; S.omega = 0.0; S.dc = 0.0; S.clow = 0.0; S.idir = 1; S.it = 0;
-  S.pf_n = S.pf_i = 0; S.pf32 = 0;
+  S.pf_n = S.pf_i = 0; S.pf32 = 0; S.used64 = S.used32 = 0;
   if (valid) {
     const int nl = job.nl[col];
     double *cp = job.cp + (size_t)col * mode * kmax;
@@ -763,11 +768,11 @@ __global__ void __launch_bounds__(32) surfdisp_kernel(DispJob job, int share) {
     }
     double ev = 0.0;
     if (eval) {
-      if (pass32) { ev = (double)dltar32(eom / ec, eom, ifunc, em); ++n32; }
-      else { ev = dltar64(eom / ec, eom, ifunc, em); ++n64; }
+      if (pass32) ev = (double)dltar32(eom / ec, eom, ifunc, em);
+      else ev = dltar64(eom / ec, eom, ifunc, em);
     }
     if (serve) {
-      if (pass32) v32 = (float)ev; else v64 = ev;
+      if (pass32) { v32 = (float)ev; ++n32; } else { v64 = ev; ++n64; }
       pending = false;
     }
     if (sharing) {
@@ -785,6 +790,9 @@ __global__ void __launch_bounds__(32) surfdisp_kernel(DispJob job, int share) {
     }
   }
   if (valid) job.ierr[col] = S.ierr;
+  // evaluations the searches used (values evaluated ahead and not reached
+  // are not counted), so the FP64 count of precision 0 is the reference's
+  n64 += S.used64; n32 += S.used32;
   if (job.ndltar && (n64 | n32)) {
     atomicAdd(&job.ndltar[0], n64);
     atomicAdd(&job.ndltar[1], n32);
