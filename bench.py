@@ -799,6 +799,104 @@ def tt2d_cpu_baseline(grid, settings, data, ncells, pts, par, args):
                       "of the reference path, one proposal per core" % nsample}
 
 
+SERVED_CONFIG = {
+    "workload": "served joint inversion loop: Poisson stream of chains (mean 40 chains/s), kinds drawn uniformly "
+                "from 2D travel time (51x51 over 10x10 km, 16 stations, fm2d), surface waves (41x41x31 over "
+                "40x40x6 km, 50 stations, 20 periods), body waves (101x101x51 over 50x50x25 km, 200 events, "
+                "60 stations, P and S, first-order tiles) and joint surface + body (one 3D model on both), "
+                "1,000 proposals per chain, device-resident state, slots sized within a 150 GB budget, "
+                "chains evicted on completion",
+    "rate_chains_per_s": 40.0, "proposals_per_chain": 1000, "hbm_budget_gb": 150}
+SERVED_SLOTS = {"tt2d": 256, "surface": 64, "body": 32, "joint": 16}
+
+
+def served_backends(single, slots):
+    """The four kinds' backends at the configurations' shapes (single: one
+    chain per call on one-slot contexts). Returns (backends, bytes per kind)."""
+    import torch
+    from mctomo_gb300 import BodyLikelihood, SurfaceLikelihood, TravelTime2DLikelihood, serving, synthetic
+    rng = np.random.default_rng(SEED + 6)
+    used = {}
+
+    def sized(kind, make):
+        torch.cuda.synchronize()
+        f0 = torch.cuda.mem_get_info()[0]
+        obj = make()
+        torch.cuda.synchronize()
+        used[kind] = used.get(kind, 0) + max(0, f0 - torch.cuda.mem_get_info()[0])
+        return obj
+    n = {k: (1 if single else v) for k, v in slots.items()}
+    g2, s2, d2 = synthetic.tt2d_workload(rng)
+    nm, pr = synthetic.serving_models("tt2d", g2, 100, (4, 100))
+    tt2d = serving.TT2DBackend(sized("tt2d", lambda: TravelTime2DLikelihood(g2, s2, d2, n["tt2d"], 100)), n["tt2d"],
+                               nm, pr, single=single)
+    gs, ss, ds = synthetic.surface_workload(rng)
+    ss["tt_precision"] = 1
+    nm, pr = synthetic.serving_models("surface", gs, 400, (10, 400))
+    surf = serving.SurfaceBackend(sized("surface", lambda: SurfaceLikelihood(gs, ss, ds, n["surface"], 400)),
+                                  n["surface"], nm, pr, len(ds["freqs"]), single=single)
+    gb, sb, db, ev = synthetic.body_workload(rng)
+    sb["order"] = 0
+    sb["solver"] = 0x10
+    nm, pr = synthetic.serving_models("body", gb, 800, (20, 800))
+    body = serving.BodyBackend(sized("body", lambda: BodyLikelihood(gb, sb, db, n["body"], 800)), n["body"], nm, pr,
+                               ev, single=single)
+    nmj, prj = synthetic.serving_models("joint", gb, 800, (20, 800))
+    js = serving.SurfaceBackend(sized("joint", lambda: SurfaceLikelihood(gs, ss, ds, n["joint"], 800)), n["joint"],
+                                nmj, prj, len(ds["freqs"]), single=single)
+    jb = serving.BodyBackend(sized("joint", lambda: BodyLikelihood(gb, sb, db, n["joint"], 800)), n["joint"], nmj,
+                             prj, ev, single=single)
+    return {"tt2d": tt2d, "surface": surf, "body": body, "joint": serving.JointBackend(js, jb)}, used
+
+
+def run_served(args):
+    """Configuration 5: the served loop (continuous batching over the four
+    kinds' contexts, one worker thread and stream per kind) on a Poisson
+    stream, then the same stream through the plain drop-in (one-slot
+    contexts, one call per proposal). Per-proposal latency is the time from
+    a proposal's submission to its result."""
+    import torch
+    from mctomo_gb300 import serving
+    names = ["tt2d", "surface", "body", "joint"]
+    rng = np.random.default_rng(SEED + 7)
+    dur, warm = args.served_seconds, args.served_seconds / 3.0
+    arrivals = serving.poisson_arrivals(rng, SERVED_CONFIG["rate_chains_per_s"], dur, names)
+    res = {}
+    for plain in (False, True):
+        backends, used = served_backends(plain, SERVED_SLOTS)
+        if sum(used.values()) > SERVED_CONFIG["hbm_budget_gb"] * 1e9:
+            raise SystemExit("served contexts exceed the HBM budget: %s" % used)
+        # one warm-up step per kind outside the stream
+        for k in names:
+            b = backends[k]
+            mdl = [b.new_model(np.random.default_rng(1))]
+            b.forward([0], mdl)
+            b.commit([0], [0])
+        torch.cuda.synchronize()
+        workers = [serving.Worker(k, backends[k], SERVED_CONFIG["proposals_per_chain"], plain=plain) for k in names]
+        clocks = Clocks(0)
+        clocks.start()
+        stats, chains = serving.run_stream(workers, arrivals, dur, (warm, dur), seed=SEED)
+        stats["clocks"] = clocks.stop()
+        stats["device_bytes"] = {k: int(v) for k, v in used.items()}
+        res["plain" if plain else "served"] = stats
+        del backends, workers
+        torch.cuda.synchronize()
+    sv, pl = res["served"], res["plain"]
+    line = {"metric": "served proposal evals/s & p99 proposal latency, mixed stream, 1 GB300",
+            "value": round(sv["evals_per_s"], 3), "unit": "proposal evals/s", "n_gpus": 1, "steps": None,
+            "warmup": None, "ms_per_step": None, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None,
+            "dtype": "f64 dispersion polish, f32 bracketing; double-float fm2d; int32 fixed-point 3D tiles",
+            "data": "synthetic (seeded, shapes of configurations 1-3)",
+            "config": dict(SERVED_CONFIG, slots=SERVED_SLOTS, seconds=dur, measured_window_s=[round(warm, 1), dur],
+                           arrivals=len(arrivals)),
+            "served": sv, "plain": pl,
+            "served_over_plain": round(sv["evals_per_s"] / pl["evals_per_s"], 3) if pl["evals_per_s"] else None,
+            "clocks": sv["clocks"]}
+    print(json.dumps(line), flush=True)
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -808,7 +906,8 @@ def main():
     ap.add_argument("--cpu-sample", type=int, default=8)
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--tt-precision", type=int, default=1)
-    ap.add_argument("--workload", default="surface", choices=["surface", "body", "disp", "tt2d"])
+    ap.add_argument("--workload", default="surface", choices=["surface", "body", "disp", "tt2d", "served"])
+    ap.add_argument("--served-seconds", type=float, default=60.0, help="served workload: stream length (s)")
     ap.add_argument("--chains2d", type=int, default=256, help="tt2d workload: chains per step")
     ap.add_argument("--columns", type=int, default=262144, help="disp workload: columns")
     ap.add_argument("--disp-sample", type=int, default=512, help="disp workload: columns checked by the oracle")
@@ -817,9 +916,11 @@ def main():
     ap.add_argument("--solver", default=None, choices=["tiles", "heap"],
                     help="body workload: 3D solver (default: heap march for order 1, tiles for order 0)")
     args = ap.parse_args()
-    if args.workload in ("body", "disp", "tt2d"):
+    if args.workload in ("body", "disp", "tt2d", "served"):
         if args.impl == "reference":
             print(json.dumps({"impl": "reference", "unavailable": "the reference arm times the surface workload"}))
+        elif args.workload == "served":
+            run_served(args)
         elif args.workload == "body":
             run_body(args)
         elif args.workload == "disp":

@@ -177,6 +177,7 @@ struct mct_body_ctx {
   double *esrc = nullptr, *erecv = nullptr, *ett = nullptr, *ptime = nullptr;
   double *cptime = nullptr, *nout = nullptr;          // committed times, noise-only results
   int *committed = nullptr, *accept = nullptr;
+  int *gshift = nullptr;                              // [2 * nslots] fixed-point shift per grid
   int *egrid = nullptr, *eset = nullptr, *T = nullptr, *list = nullptr, *count = nullptr;
   unsigned char *flags = nullptr;
   // 3D solver and the heap march's scratch
@@ -234,7 +235,8 @@ int mct_body_create(const mct_grid *g, const mct_body_settings *st, const mct_bo
       sizeof(int) * np * npairs, sizeof(double) * 2 * np * npairs,
       heap ? sizeof(double2) * 2 * (size_t)nslots * nn : 0,
       eik3_heap_scratch_bytes(g->nx, g->ny, g->nz, (int)hchunk), sizeof(int),
-      sizeof(double) * (size_t)nslots * np * npairs, sizeof(int) * 2 * nslots, sizeof(double) * 4 * nslots};
+      sizeof(double) * (size_t)nslots * np * npairs, sizeof(int) * 2 * nslots, sizeof(double) * 4 * nslots,
+      sizeof(int) * 2 * nslots};
   size_t total = 0;
   for (size_t s : sz) total = ((total + 255) & ~size_t(255)) + s;
   total += 256;
@@ -277,6 +279,7 @@ int mct_body_create(const mct_grid *g, const mct_body_settings *st, const mct_bo
   c->committed = cv.take<int>(2 * (size_t)nslots);
   c->accept = c->committed + nslots;
   c->nout = cv.take<double>(4 * (size_t)nslots);
+  c->gshift = cv.take<int>(2 * (size_t)nslots);
   cudaMemset(c->committed, 0, sizeof(int) * 2 * nslots);
   c->hchunk = (int)hchunk;
   std::vector<double> hs((size_t)np * npairs, 1.0);
@@ -339,20 +342,29 @@ int mct_body_forward(mct_body_ctx *c, int nchains, const int *ncells, const doub
   std::vector<double> hp(pc);
   MCT_CUDA_TRY(cudaMemcpyAsync(hp.data(), c->params, sizeof(double) * pc, cudaMemcpyDeviceToHost, s));
   MCT_CUDA_TRY(cudaStreamSynchronize(s));
-  double vmin = 1e300;
-  for (int ch = 0; ch < nchains; ++ch)
-    for (int i = 0; i < ncells[ch]; ++i) {
-      const double *q = &hp[((size_t)ch * c->ncell_max + i) * 3];
-      if (q[0] > 0 && q[0] < vmin) vmin = q[0];
-      if (d.np > 1 && q[1] > 0 && q[1] < vmin) vmin = q[1];
-    }
+  // per chain, so that a chain's times do not depend on the other chains of
+  // the call (its P and S grids share the chain's scale)
   const double dzs = g.dz / g.scaling;
   const double diag = sqrt(((g.nx - 1) * g.dx) * ((g.nx - 1) * g.dx) + ((g.ny - 1) * g.dy) * ((g.ny - 1) * g.dy) +
                            ((g.nz - 1) * dzs) * ((g.nz - 1) * dzs));
+  double vmin = 1e300;
+  std::vector<int> hshift((size_t)2 * c->nslots, 30);
+  for (int ch = 0; ch < nchains; ++ch) {
+    double vc = 1e300;
+    for (int i = 0; i < ncells[ch]; ++i) {
+      const double *q = &hp[((size_t)ch * c->ncell_max + i) * 3];
+      if (q[0] > 0 && q[0] < vc) vc = q[0];
+      if (d.np > 1 && q[1] > 0 && q[1] < vc) vc = q[1];
+    }
+    hshift[ch] = hshift[c->nslots + ch] = eik3_shift_for(4.0 * diag / vc);
+    vmin = std::min(vmin, vc);
+  }
+  MCT_CUDA_TRY(cudaMemcpyAsync(c->gshift, hshift.data(), sizeof(int) * hshift.size(), cudaMemcpyHostToDevice, s));
   Eik3Job job{};
   job.nsolve = nsolve; job.nx = g.nx; job.ny = g.ny; job.nz = g.nz; job.dx = g.dx; job.dy = g.dy; job.dz = dzs;
   job.vel = c->vel; job.slow = c->slow; job.ngrids = 2 * c->nslots; job.solve_grid = c->egrid; job.src = c->esrc;
   job.order = c->order; job.method = c->method; job.shift = eik3_shift_for(4.0 * diag / vmin);
+  job.grid_shift = c->gshift;
   job.T = c->T; job.flags = c->flags; job.list = c->list; job.count = c->count;
   job.hvn = c->hvn; job.herr = c->herr;
   if (c->method == EIK3_HEAP) {

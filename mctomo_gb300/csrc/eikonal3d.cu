@@ -68,6 +68,12 @@ __device__ double trilinear(const Dims &d, const double h[3], const double p[3],
   return e3_trilinear(E3Dims{d.nx, d.ny, d.nz}, h, p, value);
 }
 
+// Fixed-point shift of solve s: its grid's own when the caller gives one per
+// grid (then a solve's times do not depend on the other solves of the call).
+__device__ __forceinline__ int solve_shift(const Eik3Job &job, int s) {
+  return job.grid_shift ? job.grid_shift[job.solve_grid[s]] : job.shift;
+}
+
 // Source initialisation (solver.hpp:72-92) and seeding of the first tiles.
 __global__ void init_kernel(Eik3Job job) {
   const int s = blockIdx.x * blockDim.x + threadIdx.x;
@@ -86,7 +92,7 @@ __global__ void init_kernel(Eik3Job job) {
     if (c < 0) c = 0; else if (c >= dimsz[q]) c = dimsz[q] - 1;
     pc[q] = c;
   }
-  const double scale = ldexp(1.0, job.shift);
+  const double scale = ldexp(1.0, solve_shift(job, s));
   for (int vtx = 0; vtx < 8; ++vtx) {
     int vc[3];
     for (int q = 0; q < 3; ++q) {
@@ -267,7 +273,8 @@ __global__ void __launch_bounds__(512) tile_kernel(Eik3Job job, const int *list)
   const int me = (lz + HALO) + SZ * ((ly + HALO) + SY * (lx + HALO));
   const int orig = sT[me];
   const float hh[3] = {(float)job.dx, (float)job.dy, (float)job.dz};
-  const float scale = ldexpf(1.f, job.shift), inv_scale = ldexpf(1.f, -job.shift);
+  const int shift = solve_shift(job, s);
+  const float scale = ldexpf(1.f, shift), inv_scale = ldexpf(1.f, -shift);
   int last_change = 0;
   for (int it = 0; it < NLOCAL; ++it) {
     int mine = 0;
@@ -308,7 +315,7 @@ __global__ void readout_kernel(Eik3Job job) {
   const size_t nn = (size_t)d.nx * d.ny * d.nz;
   const int *T = job.T + (size_t)s * nn;
   const double h[3] = {job.dx, job.dy, job.dz};
-  const double inv = ldexp(1.0, -job.shift);
+  const double inv = ldexp(1.0, -solve_shift(job, s));
   const int rs = job.solve_rev ? job.solve_rev[s] : (job.rev_per_solve ? s : 0);
   for (int r = blockIdx.x * blockDim.x + threadIdx.x; r < job.nrev; r += gridDim.x * blockDim.x) {
     const double *p = job.rev + ((size_t)rs * job.nrev + r) * 3;
@@ -324,7 +331,7 @@ __global__ void readout_kernel(Eik3Job job) {
 __global__ void field_kernel(Eik3Job job, double *tfield) {
   const int s = blockIdx.y;
   const size_t nn = (size_t)job.nx * job.ny * job.nz;
-  const double inv = ldexp(1.0, -job.shift);
+  const double inv = ldexp(1.0, -solve_shift(job, s));
   for (size_t q = blockIdx.x * (size_t)blockDim.x + threadIdx.x; q < nn; q += (size_t)gridDim.x * blockDim.x) {
     int t = job.T[(size_t)s * nn + q];
     tfield[(size_t)s * nn + q] = t == TINF ? (double)INFINITY : (double)t * inv;

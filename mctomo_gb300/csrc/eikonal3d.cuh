@@ -21,6 +21,7 @@ struct Eik3Job {
   int method;                     // EIK3_TILES or EIK3_HEAP (resolved, never EIK3_DEFAULT)
   // tile iteration scratch
   int shift;                      // times stored in units of 2^-shift s
+  const int *grid_shift;          // optional [ngrids]: the shift of each grid's solves (overrides shift)
   int *T;                         // [nsolve][nx][ny][nz] scratch: fixed-point times
   unsigned char *flags;           // [nsolve][tiles] scratch
   int *list, *count;              // scratch: active (solve, tile) list

@@ -216,3 +216,42 @@ def tt2d_chain_models(rng, nchains, ncell_max, grid, ncell_range=(4, 100), vrang
         params[c, :n, 1] = params[c, :n, 0] / 1.73
         params[c, :n, 2] = 2.0
     return ncells, points, params
+
+
+def serving_models(kind, grid, ncell_max, ncell_range):
+    """(new_model, propose) for one chain of a serving stream: new_model(rng)
+    draws a Voronoi model (ncells, points, params) padded to ncell_max;
+    propose(rng, model) returns the proposal. kind "tt2d": 2D cells with
+    velocity on [2, 4] km/s and value-change proposals; "surface": 3D cells
+    with Vs on [0.3, 2.5] km/s; "body" / "joint": 3D cells with Vp on
+    [3, 7.5] km/s, Vs = Vp / 1.73; 3D proposals move one nucleus and keep Vs
+    sorted by depth (perturb_chain_models)."""
+    if kind == "tt2d":
+        def new_model(rng):
+            nc, p, q = tt2d_chain_models(rng, 1, ncell_max, grid, ncell_range=ncell_range)
+            return int(nc[0]), p[0], q[0]
+
+        def propose(rng, model):
+            nc, p, q = model
+            q = q.copy()
+            i = int(rng.integers(nc))
+            q[i, 0] = float(np.clip(q[i, 0] + rng.normal(0.0, 0.1), 2.0, 4.0))
+            q[i, 1] = q[i, 0] / 1.73
+            return nc, p, q
+        return new_model, propose
+    vs_range = (0.3, 2.5) if kind == "surface" else (3.0 / 1.73, 7.5 / 1.73)
+    lo = np.array([grid["xmin"], grid["ymin"], grid["zmin"]])
+    hi = lo + np.array([grid["dx"] * (grid["nx"] - 1), grid["dy"] * (grid["ny"] - 1), grid["dz"] * (grid["nz"] - 1)])
+
+    def new_model(rng):
+        n = int(rng.integers(ncell_range[0], ncell_range[1] + 1))
+        p, q = voronoi_model_3d(rng, n, lo, hi, vs_range, rho_value=2.0)
+        pts = np.zeros((ncell_max, 3)); par = np.zeros((ncell_max, 3))
+        pts[:n] = p; par[:n] = q
+        return n, pts, par
+
+    def propose(rng, model):
+        nc, p, q = model
+        p2, q2 = perturb_chain_models(rng, np.array([nc]), p[None], q[None], grid, vs_range)
+        return nc, p2[0], q2[0]
+    return new_model, propose

@@ -90,3 +90,41 @@ def test_body_batch_matches_oracle(orc, gpulib, order, solver):
             # end to end: times within 1e-4 s keep the likelihood close
             np.testing.assert_allclose(out[c, :3], eo, rtol=2e-3)
     lk.close()
+
+
+@pytest.mark.parametrize("order,solver", [(0, EIK3_TILES), (1, EIK3_HEAP)])
+def test_body_result_is_the_same_alone_and_in_the_mix(gpulib, order, solver):
+    # the heap march is exact: a chain's times are the same bits alone and in
+    # a call with other chains. The tile solver's fixed-point scale is chosen
+    # per chain, and its relaxation order within a call varies with the
+    # other chains' tiles, which moves the odd time by a few fixed-point
+    # units (about 1e-8 s)
+    rng = np.random.default_rng(48 + order)
+    grid, settings, data, ev = synthetic.body_workload(rng, nx=31, ny=29, nz=17, extent=(15.0, 14.0, 8.0),
+                                                      nevents=24, nstations=9)
+    settings["order"] = order
+    settings["solver"] = solver
+    lo = np.zeros(3); hi = np.array([15.0, 14.0, 8.0])
+    nch, ncell_max = 4, 40
+    ncells = np.array([12, 25, 40, 7], np.int32)
+    pts = np.zeros((nch, ncell_max, 3)); par = np.zeros((nch, ncell_max, 3))
+    for c in range(nch):
+        vr = (3.0 / 1.73, 7.5 / 1.73) if c != 2 else (1.0, 1.5)     # one slow chain
+        p, q = synthetic.voronoi_model_3d(rng, int(ncells[c]), lo, hi, vr)
+        q[:, 0] = q[:, 1] * 1.73
+        pts[c, :ncells[c]] = p; par[c, :ncells[c]] = q
+    locs = np.repeat(ev[None], nch, 0)
+    n0 = np.zeros((nch, 2)); n1 = np.full((nch, 2), 0.05)
+    mix = BodyLikelihood(grid, settings, data, nslots=nch, ncell_max=ncell_max)
+    out = mix.forward(ncells, pts, par, locs, n0, n1)
+    one = BodyLikelihood(grid, settings, data, nslots=1, ncell_max=ncell_max)
+    for c in range(nch):
+        o = one.forward(ncells[c:c + 1], pts[c:c + 1], par[c:c + 1], locs[:1], n0[:1], n1[:1])
+        if solver == EIK3_HEAP:
+            np.testing.assert_array_equal(o[0], out[c])
+            np.testing.assert_array_equal(one.phase_time(0)[0], mix.phase_time(c)[0])
+        else:
+            assert o[0, 3] == out[c, 3]
+            np.testing.assert_allclose(o[0, :3], out[c, :3], rtol=1e-8)
+            np.testing.assert_allclose(one.phase_time(0)[0], mix.phase_time(c)[0], rtol=0, atol=1e-6)
+    mix.close(); one.close()
