@@ -424,8 +424,10 @@ __device__ float2 combo_time(const WarpStateT<float2> &w, const Grid2 &, const S
   const DF IA = !two ? df(1.f) : ci == 0 ? K.ia[0] : ci == 1 ? K.ia[1] : ci == 2 ? K.ia[2] : K.ia[3];
   const DF e = two ? dsub(dmulf(Rp, k), Rq) : df(0.f);
   const DF B = dmulf(dmul(e, uu), k);
-  const DF c = dmul(uu, dsub(dmul(e, e), dmul(dmul(slown, slown), vv)));
-  DF disc = dsub(dmul(B, B), dmul(A, c));
+  // B^2 - A c with A = vv + k^2 uu (every case's a) and c = uu (e^2 - s^2 vv)
+  // is uu vv (A s^2 - e^2): the same discriminant without the cancellation
+  // of B^2 against A c, and a shorter dependent chain
+  DF disc = dmul(dmul(uu, vv), dsub(dmul(A, dmul(slown, slown)), dmul(e, e)));
   if (disc.hi < 0.f) disc = df(0.f);
   DF trav = dadd(Rp, dmul(dsub(dsqrt(disc), B), IA));
   trav = dmul(trav, op == 2 ? df_from(1.0 / 3.0) : df(1.f));
