@@ -26,21 +26,27 @@
 #include "eikonal3d.cuh"
 #include "eik3_common.cuh"
 #include <climits>
+#include <map>
+#include <mutex>
+#include <tuple>
 
 namespace {
 
-constexpr int TX = 8, TY = 8, TZ = 8, HALO = 2;
-constexpr int SX = TX + 2 * HALO, SY = TY + 2 * HALO, SZ = TZ + 2 * HALO;
-constexpr int NLOCAL = 12;           // local relaxation sweeps per visit
+// Tiles of 512 nodes with a two-node halo; the tile shape (TX, TY, TZ) and
+// the number of local sweeps per visit are chosen per grid shape by the
+// tuner below (launch_eik3).
+constexpr int HALO = 2;
 constexpr int TINF = INT_MAX;
 
 struct Dims {
   int nx, ny, nz, tnx, tny, tnz;
 };
 
-__device__ __forceinline__ Dims dims(const Eik3Job &j) {
+template <int TX, int TY, int TZ>
+__host__ __device__ __forceinline__ Dims dims(const Eik3Job &j) {
   return Dims{j.nx, j.ny, j.nz, (j.nx + TX - 1) / TX, (j.ny + TY - 1) / TY, (j.nz + TZ - 1) / TZ};
 }
+__device__ __forceinline__ Dims grid_dims(const Eik3Job &j) { return Dims{j.nx, j.ny, j.nz, 0, 0, 0}; }
 
 // node index with z fastest (the reference's vel[nx][ny][nz] layout)
 __device__ __forceinline__ size_t nidx(const Dims &d, int i, int j, int k) {
@@ -75,10 +81,11 @@ __device__ __forceinline__ int solve_shift(const Eik3Job &job, int s) {
 }
 
 // Source initialisation (solver.hpp:72-92) and seeding of the first tiles.
+template <int TX, int TY, int TZ>
 __global__ void init_kernel(Eik3Job job) {
   const int s = blockIdx.x * blockDim.x + threadIdx.x;
   if (s >= job.nsolve) return;
-  const Dims d = dims(job);
+  const Dims d = dims<TX, TY, TZ>(job);
   const double h[3] = {job.dx, job.dy, job.dz};
   const double *vel = job.vel + (size_t)job.solve_grid[s] * d.nx * d.ny * d.nz;
   int *T = job.T + (size_t)s * d.nx * d.ny * d.nz;
@@ -115,9 +122,7 @@ __global__ void init_kernel(Eik3Job job) {
 }
 
 // Builds the list of (solve, tile) pairs flagged for the next pass.
-__global__ void compact_kernel(Eik3Job job, int *list, int *count) {
-  const Dims d = dims(job);
-  const size_t ntile = (size_t)d.tnx * d.tny * d.tnz;
+__global__ void compact_kernel(Eik3Job job, size_t ntile, int *list, int *count) {
   const size_t total = ntile * job.nsolve;
   for (size_t q = blockIdx.x * (size_t)blockDim.x + threadIdx.x; q < total; q += (size_t)gridDim.x * blockDim.x) {
     if (job.flags[q]) {
@@ -131,6 +136,7 @@ __global__ void compact_kernel(Eik3Job job, int *list, int *count) {
 // One relaxation of node (x,y,z) of the shared tile; returns the candidate
 // (fixed point) or TINF when no update applies. Mirrors solveEikonal /
 // highAccuracySolveEikonal, including their acceptance rules.
+template <int SY, int SZ>
 __device__ __forceinline__ int relax(const int *sT, int x, int y, int z, float slow, const float hh[3],
                                      int order, float inv_scale, float scale) {
   const int sidx = z + SZ * (y + SY * x);
@@ -241,10 +247,13 @@ __device__ __forceinline__ int relax(const int *sT, int x, int y, int z, float s
   return (int)res;
 }
 
-__global__ void __launch_bounds__(512) tile_kernel(Eik3Job job, const int *list) {
+template <int TX, int TY, int TZ>
+__global__ void __launch_bounds__(512) tile_kernel(Eik3Job job, const int *list, int nlocal) {
+  static_assert(TX * TY * TZ == 512, "one thread per tile node");
+  constexpr int SX = TX + 2 * HALO, SY = TY + 2 * HALO, SZ = TZ + 2 * HALO;
   __shared__ int sT[SX * SY * SZ];
   __shared__ int s_face[6];
-  const Dims d = dims(job);
+  const Dims d = dims<TX, TY, TZ>(job);
   const int ntile = d.tnx * d.tny * d.tnz;
   const int e = list[blockIdx.x];
   const int s = e / ntile, tile = e % ntile;
@@ -276,10 +285,10 @@ __global__ void __launch_bounds__(512) tile_kernel(Eik3Job job, const int *list)
   const int shift = solve_shift(job, s);
   const float scale = ldexpf(1.f, shift), inv_scale = ldexpf(1.f, -shift);
   int last_change = 0;
-  for (int it = 0; it < NLOCAL; ++it) {
+  for (int it = 0; it < nlocal; ++it) {
     int mine = 0;
     if (inside && !obstacle) {
-      int c = relax(sT, lx + HALO, ly + HALO, lz + HALO, slow, hh, job.order, inv_scale, scale);
+      int c = relax<SY, SZ>(sT, lx + HALO, ly + HALO, lz + HALO, slow, hh, job.order, inv_scale, scale);
       if (c < sT[me]) { sT[me] = c; mine = 1; }
     }
     last_change = __syncthreads_or(mine);
@@ -311,7 +320,7 @@ __global__ void __launch_bounds__(512) tile_kernel(Eik3Job job, const int *list)
 // Receiver read-out (ndgridmap.hpp:462-490) per (solve, receiver).
 __global__ void readout_kernel(Eik3Job job) {
   const int s = blockIdx.y;
-  const Dims d = dims(job);
+  const Dims d = grid_dims(job);
   const size_t nn = (size_t)d.nx * d.ny * d.nz;
   const int *T = job.T + (size_t)s * nn;
   const double h[3] = {job.dx, job.dy, job.dz};
@@ -338,10 +347,122 @@ __global__ void field_kernel(Eik3Job job, double *tfield) {
   }
 }
 
+// The pass loop of one tile shape: relax every flagged (solve, tile) until
+// no tile is flagged. Returns the number of passes, or -1 past max_passes.
+template <int TX, int TY, int TZ>
+int run_tiles(const Eik3Job &job, cudaStream_t s, int max_passes, int nlocal, int *err) {
+  const Dims d = dims<TX, TY, TZ>(job);
+  const size_t ntile = (size_t)d.tnx * d.tny * d.tnz;
+  *err = 0;
+  if (cudaMemsetAsync(job.flags, 0, ntile * job.nsolve, s) != cudaSuccess) { *err = 1; return 0; }
+  init_kernel<TX, TY, TZ><<<(job.nsolve + 127) / 128, 128, 0, s>>>(job);
+  int passes = 0;
+  for (;;) {
+    if (cudaMemsetAsync(job.count, 0, sizeof(int), s) != cudaSuccess) { *err = 1; return passes; }
+    compact_kernel<<<1024, 256, 0, s>>>(job, ntile, job.list, job.count);
+    int n = 0;
+    if (cudaMemcpyAsync(&n, job.count, sizeof(int), cudaMemcpyDeviceToHost, s) != cudaSuccess ||
+        cudaStreamSynchronize(s) != cudaSuccess) { *err = 1; return passes; }
+    if (n == 0) return passes;
+    if (++passes > max_passes) return -1;
+    tile_kernel<TX, TY, TZ><<<n, 512, 0, s>>>(job, job.list, nlocal);
+  }
+}
+
+// Tile shapes (512 nodes each) and local sweeps per visit the tuner tries.
+struct TileShape { int tx, ty, tz; };
+constexpr TileShape kShapes[] = {{8, 8, 8}, {4, 8, 16}, {8, 4, 16}, {16, 8, 4}, {8, 16, 4}};
+constexpr int kNShapes = sizeof(kShapes) / sizeof(kShapes[0]);
+constexpr int kSweeps[] = {12, 24, 48, 96};
+constexpr int kNSweeps = sizeof(kSweeps) / sizeof(kSweeps[0]);
+constexpr int kNConfigs = kNShapes * kNSweeps;
+
+int run_config(int cfg, const Eik3Job &job, cudaStream_t s, int max_passes, int *err) {
+  const int nl = kSweeps[cfg % kNSweeps];
+  switch (cfg / kNSweeps) {
+    case 0: return run_tiles<8, 8, 8>(job, s, max_passes, nl, err);
+    case 1: return run_tiles<4, 8, 16>(job, s, max_passes, nl, err);
+    case 2: return run_tiles<8, 4, 16>(job, s, max_passes, nl, err);
+    case 3: return run_tiles<16, 8, 4>(job, s, max_passes, nl, err);
+    default: return run_tiles<8, 16, 4>(job, s, max_passes, nl, err);
+  }
+}
+
+// Tuned configuration per (grid shape, order, SM count): the first call on a
+// key times every configuration on the first solves of its job (up to
+// kTuneSolves, enough to fill the GPU) and keeps the fastest; later calls
+// reuse it. The configurations reach the same fixed point of the update up
+// to the rounding of the fixed-point times (a few units of 2^-shift s).
+constexpr int kTuneSolves = 256;
+std::mutex g_tune_mu;
+std::map<std::tuple<int, int, int, int, int>, int> g_tuned;
+int g_force_cfg = -1;     // diagnostics: a fixed configuration (-1: tuned)
+
+int tuned_config(const Eik3Job &job, cudaStream_t s, int max_passes) {
+  if (g_force_cfg >= 0) return g_force_cfg;
+  int dev = 0, sms = 0;
+  cudaGetDevice(&dev);
+  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+  const auto key = std::make_tuple(job.nx, job.ny, job.nz, job.order, sms);
+  {
+    std::lock_guard<std::mutex> lk(g_tune_mu);
+    auto it = g_tuned.find(key);
+    if (it != g_tuned.end()) return it->second;
+  }
+  Eik3Job sub = job;
+  sub.nsolve = job.nsolve < kTuneSolves ? job.nsolve : kTuneSolves;
+  sub.nrev = 0;
+  cudaEvent_t e0, e1;
+  if (cudaEventCreate(&e0) != cudaSuccess || cudaEventCreate(&e1) != cudaSuccess) return 0;
+  int best = 0;
+  float best_ms = 3.4e38f;
+  const size_t nn = (size_t)job.nx * job.ny * job.nz;
+  for (int cfg = 0; cfg < kNConfigs; ++cfg) {
+    int err = 0;
+    cudaEventRecord(e0, s);
+    fill_kernel<<<1024, 256, 0, s>>>(sub.T, nn * sub.nsolve);
+    const int passes = run_config(cfg, sub, s, max_passes, &err);
+    cudaEventRecord(e1, s);
+    if (cudaEventSynchronize(e1) != cudaSuccess || err || passes < 0) continue;
+    float ms = 0.f;
+    cudaEventElapsedTime(&ms, e0, e1);
+    if (ms < best_ms) { best_ms = ms; best = cfg; }
+  }
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  std::lock_guard<std::mutex> lk(g_tune_mu);
+  g_tuned[key] = best;
+  return best;
+}
+
 }  // namespace
 
 size_t eik3_tiles(const Eik3Job &j) {
-  return (size_t)((j.nx + TX - 1) / TX) * ((j.ny + TY - 1) / TY) * ((j.nz + TZ - 1) / TZ);
+  // the most tiles over the shapes the tuner may choose (flags and list scratch)
+  size_t m = 0;
+  for (const TileShape &t : kShapes) {
+    const size_t n = (size_t)((j.nx + t.tx - 1) / t.tx) * ((j.ny + t.ty - 1) / t.ty) * ((j.nz + t.tz - 1) / t.tz);
+    if (n > m) m = n;
+  }
+  return m;
+}
+
+// Diagnostics (not part of the public header): fixes the tile solver's
+// configuration (tile shape index * 4 + sweep index; -1: tuned per grid
+// shape) and returns the previous setting; with cfg < -1 only reports the
+// configuration tuned for the key (nx, ny, nz, order) (-1 if none yet).
+extern "C" int mct_debug_eik3_tile_config(int cfg, int nx, int ny, int nz, int order) {
+  if (cfg < -1) {
+    int dev = 0, sms = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    std::lock_guard<std::mutex> lk(g_tune_mu);
+    auto it = g_tuned.find(std::make_tuple(nx, ny, nz, order, sms));
+    return it == g_tuned.end() ? -1 : it->second;
+  }
+  const int old = g_force_cfg;
+  if (cfg < kNConfigs) g_force_cfg = cfg;
+  return old;
 }
 
 int eik3_shift_for(double tmax_bound) {
@@ -356,27 +477,16 @@ int launch_eik3(Eik3Job &job, cudaStream_t s, int max_passes, int *passes_out, d
     return launch_eik3_heap(job, s, tfield);
   }
   const size_t nn = (size_t)job.nx * job.ny * job.nz;
-  const size_t ntile = eik3_tiles(job);
   slowness_kernel<<<1024, 256, 0, s>>>(job.vel, job.slow, nn * job.ngrids);
   MCT_CUDA_TRY(cudaGetLastError());
+  const int cfg = tuned_config(job, s, max_passes);   // after the slowness, which the trials read
   fill_kernel<<<1024, 256, 0, s>>>(job.T, nn * job.nsolve);
   MCT_CUDA_TRY(cudaGetLastError());
-  MCT_CUDA_TRY(cudaMemsetAsync(job.flags, 0, ntile * job.nsolve, s));
-  init_kernel<<<(job.nsolve + 127) / 128, 128, 0, s>>>(job);
+  int err = 0;
+  const int passes = run_config(cfg, job, s, max_passes, &err);
   MCT_CUDA_TRY(cudaGetLastError());
-  int passes = 0;
-  for (;;) {
-    MCT_CUDA_TRY(cudaMemsetAsync(job.count, 0, sizeof(int), s));
-    compact_kernel<<<1024, 256, 0, s>>>(job, job.list, job.count);
-    MCT_CUDA_TRY(cudaGetLastError());
-    int n = 0;
-    MCT_CUDA_TRY(cudaMemcpyAsync(&n, job.count, sizeof(int), cudaMemcpyDeviceToHost, s));
-    MCT_CUDA_TRY(cudaStreamSynchronize(s));
-    if (n == 0) break;
-    if (++passes > max_passes) return MCT_ERR_TIMEOUT;
-    tile_kernel<<<n, 512, 0, s>>>(job, job.list);
-    MCT_CUDA_TRY(cudaGetLastError());
-  }
+  if (err) return MCT_ERR_CUDA;
+  if (passes < 0) return MCT_ERR_TIMEOUT;
   if (passes_out) *passes_out = passes;
   if (job.nrev > 0) {
     readout_kernel<<<dim3((job.nrev + 127) / 128, job.nsolve), 128, 0, s>>>(job);

@@ -212,3 +212,34 @@ def test_heap_march_update_bits(gpulib, order, h):
     assert fn(order, *h, 1 << 26, 12345 + order, out.ctypes.data) == 0
     assert out[1] > (1 << 25)          # most stencils give a finite time
     assert out[0] == 0, "%d of %d updates differ" % (out[0], 1 << 26)
+
+
+def test_tile_solver_configurations_all_match_reference(orc, gpulib):
+    # every tile shape / sweep count the tuner may choose reaches the first-
+    # order solution within the bound; the tuner records one for the grid
+    rng = np.random.default_rng(33)
+    shape = (37, 33, 19)
+    h = np.array([0.5, 0.5, 0.5]); lo = np.zeros(3)
+    vel = layered_voronoi(rng, shape, h, 50, (3.0, 7.5))[None]
+    ext = (np.array(shape) - 1) * h
+    srcs = lo + ext * rng.uniform(0.05, 0.95, (3, 3))
+    rev = lo + ext * rng.uniform(0.02, 0.98, (30, 3))
+    exp = [oracle_fmm(orc, vel[0], h, lo, s, rev, 0)[0] for s in srcs]
+    grid_of = np.zeros(3, np.int32)
+    old = gpulib.mct_debug_eik3_tile_config(-1, 0, 0, 0, 0)
+    try:
+        results = []
+        for cfg in range(20):
+            gpulib.mct_debug_eik3_tile_config(cfg, 0, 0, 0, 0)
+            got, _, _ = eikonal3d_batch(vel, h, lo, grid_of, srcs, rev, order=0, solver="tiles")
+            for i in range(3):
+                assert np.max(np.abs(got[i] - exp[i])) <= TOL, (cfg, i)
+            results.append(got)
+        # the configurations differ only by fixed-point rounding
+        for got in results[1:]:
+            assert np.max(np.abs(got - results[0])) <= 1e-6
+        gpulib.mct_debug_eik3_tile_config(-1, 0, 0, 0, 0)
+        eikonal3d_batch(vel, h, lo, grid_of, srcs, rev, order=0, solver="tiles")
+        assert 0 <= gpulib.mct_debug_eik3_tile_config(-2, *shape, 0) < 20
+    finally:
+        gpulib.mct_debug_eik3_tile_config(old, 0, 0, 0, 0)
