@@ -5,6 +5,7 @@
     python -m mctomo_gb300.profcase eik3heap [--order O] [--solves N]
     python -m mctomo_gb300.profcase disp [--precision P] [--columns N] [--study]
     python -m mctomo_gb300.profcase grid
+    python -m mctomo_gb300.profcase tiles [--chains N]
 
 fm2d: M Voronoi phase maps of 41 x 41 vertices (1 km spacing), 50 stations
 between 2 and 38 km, every station pair once, source refinement 4 x over
@@ -18,7 +19,10 @@ dispersion-precision study instead (12-40 layers with a 10 % low-velocity
 layer chance, 60 periods 0.2-20 s, fundamental and first overtone, phase and
 group, multimode). grid: nearest-nucleus gridding of a
 101 x 101 x 51 grid over 50 x 50 x 25 km from 800 nuclei. Each case prints
-one line and exits 0.
+one line and exits 0. tiles: the body-wave forward (101 x 101 x 51 grid, 200
+events, 60 stations, P and S, first order) of N chains with each
+configuration of the 3D tile solver forced in turn, then the tuned one; one
+line per configuration.
 """
 import argparse
 import time
@@ -112,9 +116,43 @@ def grid():
     print(f"grid nodes={sid.size} nuclei=800 call_s={dt:.4f} sid0={int(sid.ravel()[0])}")
 
 
+def tiles(chains=32):
+    from . import BodyLikelihood, lib
+    L = lib()
+    rng = np.random.default_rng(5)
+    grid, settings, data, ev = synthetic.body_workload(rng)
+    settings["order"] = 0
+    settings["solver"] = 0x10
+    lo = np.zeros(3); hi = np.array([50.0, 50.0, 25.0]); ncell_max = 800
+    ncells = rng.integers(20, ncell_max + 1, chains).astype(np.int32)
+    pts = np.zeros((chains, ncell_max, 3)); par = np.zeros((chains, ncell_max, 3))
+    for c in range(chains):
+        p, q = synthetic.voronoi_model_3d(rng, int(ncells[c]), lo, hi, (3.0 / 1.73, 7.5 / 1.73))
+        q[:, 0] = q[:, 1] * 1.73
+        pts[c, :ncells[c]] = p; par[c, :ncells[c]] = q
+    locs = np.repeat(ev[None], chains, 0)
+    n0 = np.zeros((chains, 2)); n1 = np.full((chains, 2), 0.05)
+    lk = BodyLikelihood(grid, settings, data, nslots=chains, ncell_max=ncell_max)
+    old = L.mct_debug_eik3_tile_config(-1, 0, 0, 0, 0)
+    ref = None
+    for cfg in list(range(20)) + [-1]:
+        L.mct_debug_eik3_tile_config(cfg, 0, 0, 0, 0)
+        lk.forward(ncells, pts, par, locs, n0, n1)
+        t0 = time.perf_counter()
+        out = lk.forward(ncells, pts, par, locs, n0, n1)
+        dt = time.perf_counter() - t0
+        ref = out if ref is None else ref
+        print(f"tiles cfg={cfg} chains={chains} forward_s={dt:.3f} passes={lk.phase_time(0)[1]} "
+              f"max_like_diff={float(np.max(np.abs(out[:, 0] - ref[:, 0]))):.3g}", flush=True)
+    print(f"tiles tuned_cfg={L.mct_debug_eik3_tile_config(-2, 101, 101, 51, 0)}")
+    L.mct_debug_eik3_tile_config(old, 0, 0, 0, 0)
+    lk.close()
+
+
 def main(argv=None):
     ap = argparse.ArgumentParser(description=__doc__, formatter_class=argparse.RawDescriptionHelpFormatter)
-    ap.add_argument("case", choices=["fm2d", "eik3", "eik3heap", "disp", "grid"])
+    ap.add_argument("case", choices=["fm2d", "eik3", "eik3heap", "disp", "grid", "tiles"])
+    ap.add_argument("--chains", type=int, default=32)
     ap.add_argument("--solves", type=int, default=8)
     ap.add_argument("--columns", type=int, default=4096)
     ap.add_argument("--precision", type=int, default=1)
@@ -131,6 +169,8 @@ def main(argv=None):
         eik3heap(1 if a.order is None else a.order, a.solves)
     elif a.case == "disp":
         disp(a.precision, a.columns, a.study)
+    elif a.case == "tiles":
+        tiles(a.chains)
     else:
         grid()
 
