@@ -281,7 +281,12 @@ def run_gpu(args):
         "valid_models": int((out[:, 3] == 0).sum()),
     }
     if rank == 0 and not args.no_cpu:
-        line["cpu_baseline"] = cpu_baseline(grid, settings, data, ncells, init, props, n0, n1, args)
+        collected = []
+        line["cpu_baseline"] = cpu_baseline(grid, settings, data, ncells, init, props, n0, n1, args, collected)
+        try:
+            line["accuracy"] = surface_accuracy(grid, settings, data, ncells, init, props, n0, n1, collected)
+        except Exception as e:   # the throughput line stands without it
+            line["accuracy"] = {"error": "%s: %s" % (type(e).__name__, e)}
     if rank == 0:
         print(json.dumps(line), flush=True)
     lk.close()
@@ -289,11 +294,13 @@ def run_gpu(args):
         torch.distributed.destroy_process_group()
 
 
-def cpu_sample(grid, settings, data, ncells, init, props, n0, n1, nprop, threads):
+def cpu_sample(grid, settings, data, ncells, init, props, n0, n1, nprop, threads, collect=None):
     """Times the oracle's restatement of the reference path on nprop proposals
     (one chain each), each against its chain's committed state: only the
     columns whose model changed get new dispersion curves, as the reference's
-    CGAL box arranges. The timed call includes the chain's kd-tree gridding."""
+    CGAL box arranges. The timed call includes the chain's kd-tree gridding.
+    With collect (a list), each proposal's (chain, travel times, phase maps,
+    out) are appended for the accuracy check."""
     os.environ["OMP_NUM_THREADS"] = str(threads)
     import oracle
     orc = oracle.load()
@@ -316,11 +323,12 @@ def cpu_sample(grid, settings, data, ncells, init, props, n0, n1, nprop, threads
                                P(sid), P(a), P(b), P(c))
         return b
 
-    def like(p, q, n, c, mask, pv):
+    def like(p, q, n, c, mask, pv, pt=None):
         out = np.zeros(4)
         orc.orc_surf_likelihood(P(gi), P(gd), P(iset), settings["dphase"], settings["rho_value"], n,
                                 P(f(p[:n])), P(f(q[:n])), npd, P(freqs), nsta, P(src), nsta, P(src), P(raystat),
-                                P(ttime), None, data["nrays"], P(f(n0[c])), P(f(n1[c])), P(mask), P(pv), None, P(out))
+                                P(ttime), None, data["nrays"], P(f(n0[c])), P(f(n1[c])), P(mask), P(pv), P(pt),
+                                P(out))
         return out
 
     t_total = 0.0
@@ -331,20 +339,47 @@ def cpu_sample(grid, settings, data, ncells, init, props, n0, n1, nprop, threads
         like(init[0][c], init[1][c], n, c, None, pv)          # committed state (untimed)
         p1, q1 = props[0][0][c], props[0][1][c]
         mask = f((vs_grid(init[0][c], init[1][c], n) != vs_grid(p1, q1, n)).any(axis=2).reshape(-1), np.int32)
+        pt = np.zeros((npd, nsta, nsta)) if collect is not None else None
         t0 = time.perf_counter()
-        like(p1, q1, n, c, mask, pv)
+        out = like(p1, q1, n, c, mask, pv, pt)
         t_total += time.perf_counter() - t0
+        if collect is not None:
+            collect.append((c, pt, pv.copy(), out))
     return nprop / t_total
 
 
-def cpu_baseline(grid, settings, data, ncells, init, props, n0, n1, args):
+def cpu_baseline(grid, settings, data, ncells, init, props, n0, n1, args, collect=None):
     threads = os.cpu_count() or 1
     nprop = args.cpu_sample
-    v = cpu_sample(grid, settings, data, ncells, init, props, n0, n1, nprop, threads)
+    v = cpu_sample(grid, settings, data, ncells, init, props, n0, n1, nprop, threads, collect)
     return {"value": round(v, 4), "unit": "proposal evals/s", "cores": threads, "kind": "port",
             "sample": "%d move proposals of the same workload (one chain each, changed columns only), "
                       "C++ restatement of the reference's Fortran path with OpenMP over columns and periods"
                       % nprop}
+
+
+def surface_accuracy(grid, settings, data, ncells, init, props, n0, n1, collected):
+    """The GPU path on the oracle's sampled proposals (a one-slot context,
+    the chain's committed state first): max differences of the travel times
+    (paths with data), the phase-velocity maps and -log L."""
+    from mctomo_gb300 import SurfaceLikelihood
+    lk = SurfaceLikelihood(grid, settings, data, nslots=1, ncell_max=NCELL_MAX)
+    rays = np.asarray(data["raystat"]).reshape(len(data["freqs"]), len(data["src"]), len(data["src"])) == 1
+    err_t = err_v = err_l = 0.0
+    one = np.zeros(1, np.int32)
+    for c, ept, epv, eout in collected:
+        sl = np.zeros(1, np.int32)
+        lk.forward(sl, ncells[c:c + 1], init[0][c:c + 1], init[1][c:c + 1], n0[c:c + 1], n1[c:c + 1])
+        lk.commit(one + 1)
+        o = lk.forward(sl, ncells[c:c + 1], props[0][0][c:c + 1], props[0][1][c:c + 1], n0[c:c + 1], n1[c:c + 1])
+        lk.commit(one)
+        pt, pv = lk.phase_time(0)
+        err_t = max(err_t, float(np.max(np.abs(pt - ept)[rays])))
+        err_v = max(err_v, float(np.max(np.abs(pv - epv))))
+        err_l = max(err_l, float(abs(o[0, 0] - eout[0]) / abs(eout[0])))
+    lk.close()
+    return {"proposals_checked": len(collected), "max_ttime_err_s": err_t, "max_phase_vel_err_kms": err_v,
+            "max_like_rel_err": err_l, "reference": "oracle restatement of the reference path, FP64"}
 
 
 def run_reference(args):
