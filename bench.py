@@ -43,7 +43,7 @@ CONFIG = {"workload": "batched 3D surface-wave rjMCMC: 64 chains, 41x41x31 grid 
                       "1225 paths/period, move proposals committed each step",
           "chains": NCHAINS, "grid": [41, 41, 31], "periods": 20, "stations": 50,
           "paths_per_period": 1225, "dispersion_root_search": "FP32 bracketing + FP64 polish",
-          "fm2d": "reference marching order, double-float (FP32 pair) updates",
+          "fm2d": "reference marching order, FP64 updates in the reference's operation order",
           "l2": "flushed (512 MB write) between steps"}
 
 
@@ -264,8 +264,13 @@ def run_gpu(args):
     line = {
         "metric": METRIC, "value": round(value, 3), "unit": "proposal evals/s", "n_gpus": ws,
         "steps": K, "warmup": W, "ms_per_step": round(total_ms / K, 4), "higher_is_better": True,
-        "scaling": "weak", "vs_baseline": None, "dtype": "f64 dispersion polish; f32 dispersion bracketing; double-float (f32 pairs) fm2d",
-        "data": "synthetic (seeded, shapes of the configuration)", "config": CONFIG,
+        "scaling": "weak", "vs_baseline": None,
+        "dtype": "f64 dispersion polish; f32 dispersion bracketing; " + (
+            "f64 fm2d in the reference's operation order (times identical to the reference)" if args.tt_precision == 0
+            else "double-float (f32 pairs) fm2d"),
+        "data": "synthetic (seeded, shapes of the configuration)",
+        "config": CONFIG if args.tt_precision == 0 else dict(CONFIG, fm2d="reference marching order, " + (
+            "double-float (FP32 pair) updates" if args.tt_precision == 1 else "int32 fixed-point times")),
         "e2e": {"value": round(e2e_value, 3), "unit": "proposal evals/s", "h2d_bytes_per_step": h2d,
                 "d2h_bytes_per_step": d2h},
         "plain": {"value": round(plain_value, 3), "unit": "proposal evals/s", "p50_ms": round(float(np.percentile(plain_ms, 50)), 3),
@@ -280,13 +285,51 @@ def run_gpu(args):
         "clocks": cl,
         "valid_models": int((out[:, 3] == 0).sum()),
     }
+    collected = []
     if rank == 0 and not args.no_cpu:
-        collected = []
         line["cpu_baseline"] = cpu_baseline(grid, settings, data, ncells, init, props, n0, n1, args, collected)
         try:
             line["accuracy"] = surface_accuracy(grid, settings, data, ncells, init, props, n0, n1, collected)
         except Exception as e:   # the throughput line stands without it
             line["accuracy"] = {"error": "%s: %s" % (type(e).__name__, e)}
+    if rank == 0 and args.tt_precision == 0 and not args.no_variant:
+        # the double-float fm2d variant on the same proposals, device path
+        vs = dict(settings, tt_precision=1)
+        lk2 = SurfaceLikelihood(grid, vs, data, nslots=NCHAINS, ncell_max=NCELL_MAX)
+        lk2.forward(slots, ncells, init[0], init[1], n0, n1)
+        lk2.commit(np.ones(NCHAINS, np.int32))
+        sp2 = ctypes.c_void_p()
+        check("mct_surf_stream", L.mct_surf_stream(lk2.h, ctypes.byref(sp2)))
+        ext2 = torch.cuda.ExternalStream(sp2.value)
+
+        def vstep(i):
+            check("mct_surf_forward_device", L.mct_surf_forward_device(
+                lk2.h, NCHAINS, d_slots.data_ptr(), d_ncells.data_ptr(), d_pts[i].data_ptr(), d_par[i].data_ptr(),
+                d_n0.data_ptr(), d_n1.data_ptr(), d_out.data_ptr(), None))
+            check("mct_surf_commit_device", L.mct_surf_commit_device(lk2.h, d_acc.data_ptr(), None))
+        for i in range(W):
+            vstep(i)
+        torch.cuda.synchronize()
+        ev = []
+        with torch.cuda.stream(ext2):
+            for i in range(W, W + K):
+                flush.fill_(i & 0xff)
+                e0 = torch.cuda.Event(enable_timing=True); e1 = torch.cuda.Event(enable_timing=True)
+                e0.record(ext2)
+                vstep(i)
+                e1.record(ext2)
+                ev.append((e0, e1))
+        torch.cuda.synchronize()
+        vms = sum(a.elapsed_time(b) for a, b in ev)
+        lk2.close()
+        var = {"value": round(NCHAINS * K / (vms / 1e3), 3), "unit": "proposal evals/s",
+               "ms_per_step": round(vms / K, 4), "fm2d": "double-float (f32 pairs) updates"}
+        if collected:
+            try:
+                var["accuracy"] = surface_accuracy(grid, vs, data, ncells, init, props, n0, n1, collected)
+            except Exception as e:
+                var["accuracy"] = {"error": "%s: %s" % (type(e).__name__, e)}
+        line["variants"] = {"double_float_fm2d": var}
     if rank == 0:
         print(json.dumps(line), flush=True)
     lk.close()
@@ -366,6 +409,7 @@ def surface_accuracy(grid, settings, data, ncells, init, props, n0, n1, collecte
     lk = SurfaceLikelihood(grid, settings, data, nslots=1, ncell_max=NCELL_MAX)
     rays = np.asarray(data["raystat"]).reshape(len(data["freqs"]), len(data["src"]), len(data["src"])) == 1
     err_t = err_v = err_l = 0.0
+    errs = []
     one = np.zeros(1, np.int32)
     for c, ept, epv, eout in collected:
         sl = np.zeros(1, np.int32)
@@ -374,12 +418,17 @@ def surface_accuracy(grid, settings, data, ncells, init, props, n0, n1, collecte
         o = lk.forward(sl, ncells[c:c + 1], props[0][0][c:c + 1], props[0][1][c:c + 1], n0[c:c + 1], n1[c:c + 1])
         lk.commit(one)
         pt, pv = lk.phase_time(0)
-        err_t = max(err_t, float(np.max(np.abs(pt - ept)[rays])))
+        e = np.abs(pt - ept)[rays]
+        errs.append(e)
+        err_t = max(err_t, float(np.max(e)))
         err_v = max(err_v, float(np.max(np.abs(pv - epv))))
         err_l = max(err_l, float(abs(o[0, 0] - eout[0]) / abs(eout[0])))
     lk.close()
-    return {"proposals_checked": len(collected), "max_ttime_err_s": err_t, "max_phase_vel_err_kms": err_v,
-            "max_like_rel_err": err_l, "reference": "oracle restatement of the reference path, FP64"}
+    e = np.concatenate(errs) if errs else np.zeros(1)
+    return {"proposals_checked": len(collected), "paths_checked": int(e.size), "max_ttime_err_s": err_t,
+            "p99_ttime_err_s": float(np.quantile(e, 0.99)), "frac_paths_within_1e-4_s": float(np.mean(e <= 1e-4)),
+            "max_phase_vel_err_kms": err_v, "max_like_rel_err": err_l,
+            "reference": "oracle restatement of the reference path, FP64"}
 
 
 def run_reference(args):
@@ -940,7 +989,9 @@ def main():
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--cpu-sample", type=int, default=8)
     ap.add_argument("--no-cpu", action="store_true")
-    ap.add_argument("--tt-precision", type=int, default=1)
+    ap.add_argument("--tt-precision", type=int, default=0,
+                    help="surface workload: fm2d arithmetic (0 FP64 exact, 1 double-float, 2 fixed point)")
+    ap.add_argument("--no-variant", action="store_true", help="surface workload: skip the double-float variant")
     ap.add_argument("--workload", default="surface", choices=["surface", "body", "disp", "tt2d", "served"])
     ap.add_argument("--served-seconds", type=float, default=60.0, help="served workload: stream length (s)")
     ap.add_argument("--chains2d", type=int, default=256, help="tt2d workload: chains per step")

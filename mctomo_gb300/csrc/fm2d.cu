@@ -157,11 +157,6 @@ __host__ __device__ __forceinline__ SolveLayout solve_layout(int tbytes, int n, 
 constexpr int REFINED_HEAP_CAP = 1024;
 
 // ---- upwind arithmetic ------------------------------------------------------
-__device__ __forceinline__ double quad_root(double a, double b, double c) {
-  double rd1 = b * b - 4.0 * a * c;
-  if (rd1 < 0.0) rd1 = 0.0;
-  return (-b + sqrt(rd1)) / (2.0 * a);
-}
 
 // Double-float variant (precision == 1): times are unevaluated sums of two
 // FP32 numbers (hi + lo, |lo| <= ulp(hi)/2) and every operation of the
@@ -329,6 +324,30 @@ __device__ __forceinline__ void store_slowness(double *base, size_t i, double s,
 template <class TT> struct UpdConst {
   __device__ void init(const Grid2 &) {}
 };
+// FP64 (precision 0): RN(1/(2a)) for the quadratic of each case, a computed
+// with the reference's expression vv + m uu (4: one term, a = 1). The
+// divisions by 2a and by 3 then take Markstein's correction step (P.
+// Markstein, "Computation of elementary functions on the IBM RISC
+// System/6000 processor", IBM J. Res. Dev. 34(1), 1990): with yinv =
+// RN(1/y), q = RN(x yinv), r = x - q y (exact with a fused multiply-add) and
+// RN(q + r yinv) is the correctly rounded x / y, the bits of the reference's
+// division, in three dependent FP64 operations instead of a division
+// (~550 cycles of latency each on this GPU).
+template <> struct UpdConst<double> {
+  double rtwo_a[5];
+  __device__ void init(const Grid2 &g) {
+    const double u2x = 2.0 * g.dnx, u2z = 2.0 * g.dnz;
+    const double hx1 = g.dnx * g.dnx, hz1 = g.dnz * g.dnz, hx2 = u2x * u2x, hz2 = u2z * u2z;
+    const double a[5] = {hz2 + 1.0 * hx2, hx2 + 9.0 * hz1, hz2 + 9.0 * hx1, hz1 + 1.0 * hx1, 1.0};
+#pragma unroll
+    for (int i = 0; i < 5; ++i) rtwo_a[i] = 1.0 / (2.0 * a[i]);
+  }
+};
+__device__ __forceinline__ double div_known(double x, double y, double yinv) {
+  const double q = __dmul_rn(x, yinv);
+  const double r = __fma_rn(-q, y, x);
+  return __fma_rn(r, yinv, q);
+}
 template <> struct UpdConst<float2> {
   DF dnx, dnz, hx1, hz1, a[4], ia[4];
   __device__ void init(const Grid2 &g) {
@@ -360,27 +379,28 @@ template <> struct UpdConst<int> {
 // FP64, the reference's arithmetic (precision 0). slown is the node's
 // slowness 1/V, precomputed per node with the reference's division.
 __device__ double combo_time(const WarpStateT<double> &w, const Grid2 &g, const Stencil &s, double slown, int fom,
-                             const Fx &, const UpdConst<double> &) {
+                             const Fx &, const UpdConst<double> &K) {
   const double ss = slown * slown;
   const double u2x = 2.0 * g.dnx, u2z = 2.0 * g.dnz;
   const double hx1 = g.dnx * g.dnx, hz1 = g.dnz * g.dnz, hx2 = u2x * u2x, hz2 = u2z * u2z;
   const double Tj = w.T[s.lj], Tk = w.T[s.lk];
   double a = 1.0, b = 0.0, c, tref, tdiv = 1.0;
+  int ci = 4;
   if (s.X && s.Z) {
     double uu, vv, m = 1.0, kb = 2.0, em;
     if (s.X == 2 && s.Z == 2) {
       tref = 4.0 * Tj - w.T[s.lj2];
       em = (tref - 4.0 * Tk) + w.T[s.lk2];
-      uu = hx2; vv = hz2; tdiv = 3.0;
+      uu = hx2; vv = hz2; tdiv = 3.0; ci = 0;
     } else if (s.X == 2) {
       em = (3.0 * Tk - 4.0 * Tj) + w.T[s.lj2];
-      uu = hz1; vv = hx2; m = 9.0; kb = 6.0; tref = Tk;
+      uu = hz1; vv = hx2; m = 9.0; kb = 6.0; tref = Tk; ci = 1;
     } else if (s.Z == 2) {
       em = (3.0 * Tj - 4.0 * Tk) + w.T[s.lk2];
-      uu = hx1; vv = hz2; m = 9.0; kb = 6.0; tref = Tj;
+      uu = hx1; vv = hz2; m = 9.0; kb = 6.0; tref = Tj; ci = 2;
     } else {
       em = Tj - Tk;
-      uu = hx1; vv = hz1; tref = Tj;
+      uu = hx1; vv = hz1; tref = Tj; ci = 3;
     }
     a = vv + m * uu;
     b = (kb * em) * uu;
@@ -393,7 +413,11 @@ __device__ double combo_time(const WarpStateT<double> &w, const Grid2 &g, const 
     else if (fom == 1) { tref = Tk; c = -(ss * hz1); }
     else { const double sd = slown * g.dnz; tref = Tk; c = -(sd * sd); }
   }
-  return (tref + quad_root(a, b, c)) / tdiv;
+  // quad_root with the known divisors 2a and 3 (see UpdConst<double>)
+  double rd1 = b * b - 4.0 * a * c;
+  if (rd1 < 0.0) rd1 = 0.0;
+  const double t = tref + div_known(-b + sqrt(rd1), 2.0 * a, K.rtwo_a[ci]);
+  return tdiv == 3.0 ? div_known(t, 3.0, 1.0 / 3.0) : t;
 }
 
 // Double-float (precision 1): the same cases and stencils in FP32-pair
