@@ -259,8 +259,8 @@ def run_gpu(args):
     achieved = alg_bytes / (stage_ms[dom] / 1e3) / 1e9 if alg_bytes else 0.0
     # DRAM bytes (read + write) of the fm2d launches of one forward of this
     # workload, measured with ncu (dram__bytes_read.sum, dram__bytes_write.sum,
-    # one pass) on the double-float path
-    traffic = FM2D_DRAM_BYTES_PER_FORWARD if dom == 2 and args.tt_precision == 1 else None
+    # one pass): 2.19 GB on both the FP64 and the double-float path
+    traffic = FM2D_DRAM_BYTES_PER_FORWARD if dom == 2 and args.tt_precision in (0, 1) else None
     line = {
         "metric": METRIC, "value": round(value, 3), "unit": "proposal evals/s", "n_gpus": ws,
         "steps": K, "warmup": W, "ms_per_step": round(total_ms / K, 4), "higher_is_better": True,
