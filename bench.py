@@ -915,7 +915,7 @@ def served_backends(single, slots):
     tt2d = serving.TT2DBackend(sized("tt2d", lambda: TravelTime2DLikelihood(g2, s2, d2, n["tt2d"], 100)), n["tt2d"],
                                nm, pr, single=single)
     gs, ss, ds = synthetic.surface_workload(rng)
-    ss["tt_precision"] = 1
+    ss["tt_precision"] = 0            # FP64 fm2d: times identical to the reference
     nm, pr = synthetic.serving_models("surface", gs, 400, (10, 400))
     surf = serving.SurfaceBackend(sized("surface", lambda: SurfaceLikelihood(gs, ss, ds, n["surface"], 400)),
                                   n["surface"], nm, pr, len(ds["freqs"]), single=single)
@@ -971,7 +971,7 @@ def run_served(args):
             "value": round(sv["evals_per_s"], 3), "unit": "proposal evals/s", "n_gpus": 1, "steps": None,
             "warmup": None, "ms_per_step": None, "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None,
-            "dtype": "f64 dispersion polish, f32 bracketing; double-float fm2d; int32 fixed-point 3D tiles",
+            "dtype": "f64 dispersion polish, f32 bracketing; f64 fm2d (reference order); int32 fixed-point 3D tiles",
             "data": "synthetic (seeded, shapes of configurations 1-3)",
             "config": dict(SERVED_CONFIG, slots=SERVED_SLOTS, seconds=dur, measured_window_s=[round(warm, 1), dur],
                            arrivals=len(arrivals)),
