@@ -1,6 +1,6 @@
 """GPU parity: surfdisp96 dispersion kernel vs the CPU restatement.
 
-Tolerance: phase velocity within 1e-5 km/s (the benchmark spec's bound); the
+Tolerance: phase velocity within 1e-5 km/s (the stated accuracy bound); the
 outputs are REAL*4-rounded roots, so in practice they agree to the last
 REAL*4 bit except where CUDA's and the host's sin/cos/exp differ by an ulp
 right at a sign decision. Group velocity (REAL*4 finite difference in the

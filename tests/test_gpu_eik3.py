@@ -6,7 +6,7 @@ reference's SFMM run step for step; times and fields must be identical, bit
 for bit, for every lane-group size and chunking.
 
 Tile solver (fast iterative method on the reference's update operator):
-first order (order 0) within 1e-4 s on receiver times, the north-star
+first order (order 0) within 1e-4 s on receiver times, the stated
 bound: the iteration's fixed point is the heap march's discrete solution and
 the FP32 local solves on fixed-point times add ~1e-6 s. Mixed second order
 (order 1) 5e-2 s: the reference's heap march feeds second-order stencils with

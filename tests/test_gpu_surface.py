@@ -11,7 +11,7 @@ from mctomo_gb300 import SurfaceLikelihood, synthetic
 
 pytestmark = pytest.mark.gpu
 P = lambda a: None if a is None else a.ctypes.data_as(ctypes.c_void_p)  # noqa: E731
-TT_TOL = 1e-4      # s, travel times (spec bound)
+TT_TOL = 1e-4      # s, travel times (the stated accuracy bound)
 LIKE_RTOL = 1e-6
 
 
