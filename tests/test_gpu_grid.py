@@ -94,3 +94,22 @@ def test_grid_deterministic_repeat(gpulib):
     b = kdtree_to_grid(pts, par, 41, 41, 41, lo, st)
     for x, y in zip(a, b):
         np.testing.assert_array_equal(x, y)
+
+
+@pytest.mark.parametrize("k,shape,lo,st", [
+    (1, (41, 51, 31), (-2.0, -2.0, 0.0), (0.1, 0.1, 0.1)),
+    (2, (51, 141, 21), (0.0, 0.0, 0.0), (0.1, 0.1, 0.1)),
+])
+def test_grid_reference_vertices_match_oracle(orc, gpulib, k, shape, lo, st):
+    # the Voronoi nuclei the reference ships (plot/run_time_vertices_k.txt,
+    # fixture made by tests/golden/make_vertices.py), gridded at 0.1 km
+    import os
+    d = np.load(os.path.join(os.path.dirname(__file__), "golden", "reference_vertices.npz"))
+    pts, val = d["pts%d" % k], d["val%d" % k]
+    par = np.ascontiguousarray(np.column_stack([val[:, 0], val[:, 1], np.full(len(pts), 2.0)]))
+    lo = np.array(lo); st = np.array(st)
+    nx, ny, nz = shape
+    got = kdtree_to_grid(np.ascontiguousarray(pts), par, nx, ny, nz, lo, st)
+    exp = oracle_grid(orc, np.ascontiguousarray(pts), par, nx, ny, nz, lo, st)
+    for g, e in zip(got, exp):
+        np.testing.assert_array_equal(g, e)

@@ -218,3 +218,20 @@ def test_straight_rays_uniform_velocity(orc):
     np.testing.assert_allclose(d, ds, rtol=1e-15)
     np.testing.assert_allclose(t[raystat == 1], ds[raystat == 1] / 2.5, rtol=1e-12)
     assert np.all(t[raystat == 0] == 0)
+
+
+def test_kdtree_oracle_on_the_reference_vertices(orc):
+    # the nuclei the reference ships with its plots (fixture from
+    # tests/golden/make_vertices.py): the kd-tree search returns a nearest
+    # nucleus for grid-like queries, the smallest index among exact ties
+    # excepted (those follow the kd-tree visiting order)
+    d = np.load(os.path.join(os.path.dirname(__file__), "golden", "reference_vertices.npz"))
+    rng = np.random.default_rng(4)
+    for k in (1, 2):
+        pts = np.ascontiguousarray(d["pts%d" % k])
+        lo, hi = pts.min(0), pts.max(0)
+        for _ in range(300):
+            q = np.round(rng.uniform(lo, hi) / 0.1) * 0.1
+            i = orc.orc_kdtree_nearest(3, pts.shape[0], P(pts), P(np.ascontiguousarray(q)))
+            dd = ((pts - q) ** 2).sum(1)
+            assert dd[i - 1] == dd.min()
