@@ -172,7 +172,7 @@ struct SearchFrame { int node, stage, farther; double dis; };
 // kdtree2.f90:1369-1443 search + 1496-1599 process_terminal_node (nn = 1).
 __device__ int kd_nearest(const KdTree &t, const double *qv, int *err) {
   double ballsize = (double)FLT_MAX;   // huge(1.0)
-  int nfound = 0, best = 0;
+  int best = 0;
   SearchFrame st[64];
   int sp = 0;
   st[sp++] = {t.root, 0, -1, 0.0};
@@ -192,7 +192,6 @@ __device__ int kd_nearest(const KdTree &t, const double *qv, int *err) {
           if (skip) continue;
           best = t.ind[i - 1];
           ballsize = sd;
-          nfound = 1;
         }
         --sp;
         continue;
@@ -235,7 +234,6 @@ __device__ int kd_nearest(const KdTree &t, const double *qv, int *err) {
       --sp;
     }
   }
-  (void)nfound;
   return best;
 }
 
