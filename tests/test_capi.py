@@ -83,3 +83,51 @@ def test_fortran_module_covers_the_header():
             fields += [(kinds[t.strip()], n.strip()) for n in names.split(",")]
         assert fields == structs[m.group(1)], m.group(1)
     assert set(structs) == set(re.findall(r"type, bind\(C\) :: (\w+)", f))
+
+
+def test_null_contexts_and_bad_sizes_are_refused_without_a_gpu(gpulib):
+    # every context call checks its handle and sizes before touching the
+    # device, so these return MCT_ERR_ARG (-1) on a machine without a GPU
+    import numpy as np
+    L = gpulib
+    N = None
+    d = np.zeros(16)
+    i = np.zeros(16, np.int32)
+    P = lambda a: a.ctypes.data_as(ctypes.c_void_p)  # noqa: E731
+    calls = {
+        "mct_surf_forward": lambda: L.mct_surf_forward(N, 1, P(i), P(i), P(d), P(d), P(d), P(d), P(d)),
+        "mct_surf_commit": lambda: L.mct_surf_commit(N, P(i)),
+        "mct_surf_forward_device": lambda: L.mct_surf_forward_device(N, 1, N, N, N, N, N, N, N, N),
+        "mct_surf_commit_device": lambda: L.mct_surf_commit_device(N, N, N),
+        "mct_surf_noise_likelihood": lambda: L.mct_surf_noise_likelihood(N, 1, P(i), P(d), P(d), P(d)),
+        "mct_surf_phase_time": lambda: L.mct_surf_phase_time(N, 0, P(d), P(d)),
+        "mct_surf_profile_start": lambda: L.mct_surf_profile_start(N, 1),
+        "mct_surf_profile_read": lambda: L.mct_surf_profile_read(N, P(d), P(i), P(d)),
+        "mct_surf_stream": lambda: L.mct_surf_stream(N, P(d)),
+        "mct_surf_admit": lambda: L.mct_surf_admit(N, P(i)),
+        "mct_surf_evict": lambda: L.mct_surf_evict(N, 0),
+        "mct_surf_submit": lambda: L.mct_surf_submit(N, 1, P(i), P(i), P(d), P(d), P(d), P(d)),
+        "mct_surf_poll": lambda: L.mct_surf_poll(N, P(d), P(i)),
+        "mct_surf_create": lambda: L.mct_surf_create(N, N, N, 1, 1, N),
+        "mct_surf_device_bytes": lambda: L.mct_surf_device_bytes(N, N, N, 1, 1, N),
+        "mct_body_create": lambda: L.mct_body_create(N, N, N, 1, 1, N),
+        "mct_body_forward": lambda: L.mct_body_forward(N, 1, P(i), P(d), P(d), P(d), P(d), P(d), P(d)),
+        "mct_body_commit": lambda: L.mct_body_commit(N, 1, P(i)),
+        "mct_body_noise_likelihood": lambda: L.mct_body_noise_likelihood(N, 1, P(d), P(d), P(d), P(d)),
+        "mct_body_phase_time": lambda: L.mct_body_phase_time(N, 0, P(d), P(i)),
+        "mct_tt2d_forward": lambda: L.mct_tt2d_forward(N, 1, P(i), P(d), P(d), P(d), P(d), P(d)),
+        "mct_tt2d_commit": lambda: L.mct_tt2d_commit(N, 1, P(i)),
+        "mct_tt2d_noise_likelihood": lambda: L.mct_tt2d_noise_likelihood(N, 1, P(d), P(d), P(d)),
+        "mct_tt2d_phase_time": lambda: L.mct_tt2d_phase_time(N, 0, P(d)),
+        "mct_kdtree_to_grid": lambda: L.mct_kdtree_to_grid(4, 1, P(d), P(d), 2, 2, 2, P(d), P(d), N, P(i), P(d), P(d),
+                                                           P(d)),
+        "mct_surfdisp_batch": lambda: L.mct_surfdisp_batch(1, 1, P(i), P(d), P(d), P(d), P(d), 61, P(d), 2, 1, 0,
+                                                           0.001, 0, 0, P(d), P(d), P(i), N),
+        "mct_surfmodes": lambda: L.mct_surfmodes(P(d), P(d), P(d), P(d), 0, P(d), 1, 0, 0, 0.001, P(d), P(d), P(i)),
+        "mct_eikonal3d_batch": lambda: L.mct_eikonal3d_batch(0, 2, 2, 2, 1., 1., 1., 0., 0., 0., 1, P(d), P(i),
+                                                             P(d), 0, P(d), 0, P(d), N, P(i)),
+    }
+    for name, call in calls.items():
+        assert call() == -1, name
+    # destroying a null context is a no-op
+    assert L.mct_surf_destroy(N) == 0 and L.mct_body_destroy(N) == 0 and L.mct_tt2d_destroy(N) == 0
