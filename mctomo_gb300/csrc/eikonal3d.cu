@@ -8,18 +8,21 @@
 //
 // The reference's heap march is one sequential chain of ~10^6 dependent
 // steps. Here the same local update is iterated to convergence on tiles: a
-// tile-based fast iterative method. Every (solve, 8x8x8 tile) with pending
-// change is one CTA; the tile and a two-node halo are relaxed in shared
-// memory until they settle, changed values are written back, and the tiles
-// across any face whose outer two layers changed are queued for the next
-// pass. A node's time only ever decreases, so the iteration ends at a fixed
-// point of the reference's update operator; for the first-order scheme that
-// is the discrete solution the heap march computes.
+// tile-based fast iterative method. Every (solve, 512-node tile) with
+// pending change is one CTA; the tile and a two-node halo are relaxed in
+// shared memory until they settle or a number of local sweeps is done,
+// changed values are written back, and the tiles across any face whose
+// outer two layers changed are queued for the next pass. The tile shape and
+// the sweeps per visit are tuned per grid shape (launch_eik3). A node's time
+// only ever decreases, so the iteration ends at a fixed point of the
+// reference's update operator; for the first-order scheme that is the
+// discrete solution the heap march computes.
 //
 // Times are stored as int32 fixed point in units of 2^-shift s (shift chosen
-// per call so the largest possible time fits), so comparisons and the final
-// additions are integer operations; each local quadratic is solved in FP32
-// on times taken relative to its smallest neighbour. No FP64 arithmetic runs
+// per velocity grid, or per call, so the largest possible time fits), so
+// comparisons and the final additions are integer operations; each local
+// quadratic is solved in FP32 on times taken relative to its smallest
+// neighbour. No FP64 arithmetic runs
 // in the iteration (FP64 throughput is scarce on this GPU); the accumulated
 // rounding stays far below the 1e-4 s travel-time bound.
 #include "mct_common.cuh"
