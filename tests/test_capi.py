@@ -131,3 +131,25 @@ def test_null_contexts_and_bad_sizes_are_refused_without_a_gpu(gpulib):
         assert call() == -1, name
     # destroying a null context is a no-op
     assert L.mct_surf_destroy(N) == 0 and L.mct_body_destroy(N) == 0 and L.mct_tt2d_destroy(N) == 0
+
+
+def test_header_is_strict_c99_and_cxx(tmp_path):
+    # the C ABI header compiles as ISO C99 and C++11 with warnings as errors,
+    # and a C program can take every declared entry point's address
+    import shutil
+    import subprocess
+    if not shutil.which("gcc") or not shutil.which("g++"):
+        import pytest
+        pytest.skip("no host C compiler")
+    syms = declared_symbols()
+    src = tmp_path / "abi.c"
+    body = "\n".join("  p[%d] = (void (*)(void))%s;" % (i, s) for i, s in enumerate(syms))
+    src.write_text('#include "mctomo.h"\nint main(void) {\n  void (*p[%d])(void);\n%s\n  return p[0] == 0;\n}\n'
+                   % (len(syms), body))
+    inc = "-I" + os.path.join(ROOT, "include")
+    for cmd in (["gcc", "-std=c99", "-Wall", "-Wextra", "-pedantic", "-Werror", inc, "-c", str(src), "-o",
+                 str(tmp_path / "a.o")],
+                ["g++", "-std=c++11", "-Wall", "-Wextra", "-pedantic", "-Werror", inc, "-x", "c++", "-c", str(src),
+                 "-o", str(tmp_path / "b.o")]):
+        r = subprocess.run(cmd, capture_output=True, text=True)
+        assert r.returncode == 0, r.stderr
