@@ -104,6 +104,11 @@ module mctomo_gb300
       real(c_double), intent(in) :: grid_lo(*), grid_step(*)
       type(c_ptr), value :: box, sites_id, vp, vs, rho, stream
     end function
+    integer(c_int) function mct_grid_status(stream, status) bind(C, name="mct_grid_status")
+      import :: c_int, c_ptr
+      type(c_ptr), value :: stream
+      integer(c_int), intent(out) :: status
+    end function
     integer(c_int) function mct_grid_nearest_batch_device_noalloc(d, nchains, ncell_max, ncells, points, params, &
         nx, ny, nz, grid_lo, grid_step, box, sites_id, vp, vs, rho, stream) &
         bind(C, name="mct_grid_nearest_batch_device_noalloc")

@@ -53,13 +53,26 @@ int mct_kdtree_to_grid(int d, int n, const double *points, const double *params,
 
 /* Batched form on device memory: nchains chains, nucleus arrays strided by
  * ncell_max (points [nchains][ncell_max][d], params [nchains][ncell_max][3]),
- * boxes [nchains][6] or NULL, outputs [nchains][grid]. */
+ * boxes [nchains][6] or NULL, outputs [nchains][grid]. The launch is
+ * asynchronous on stream; the device-side inputs are checked on the device:
+ * a box reaching outside the grid is clipped to it, and a chain whose
+ * clipped box is empty or whose ncells lies outside [1, ncell_max] is
+ * skipped (its outputs untouched) with MCT_ERR_ARG recorded. A node whose
+ * tie resolution fails (a kd-tree deeper than the fixed search stacks, only
+ * on degenerate nucleus sets) gets sites_id 0 and vp = vs = rho = 0, with
+ * MCT_ERR_INTERNAL recorded. mct_grid_status reads what was recorded. */
 int mct_grid_nearest_batch_device(int d, int nchains, int ncell_max,
                                   const int *ncells, const double *points,
                                   const double *params, int nx, int ny, int nz,
                                   const double *grid_lo, const double *grid_step,
                                   const int *box, int *sites_id, double *vp,
                                   double *vs, double *rho, void *stream);
+
+/* Waits for stream, then returns in *status the first error recorded on the
+ * device by any gridding call since the previous mct_grid_status (MCT_OK if
+ * none) and clears it. No counterpart in the reference, whose kdtree2 runs
+ * on the host and stops the program on errors. */
+int mct_grid_status(void *stream, int *status);
 
 /* Same as mct_grid_nearest_batch_device, same arguments and results, but it
  * allocates no device memory: its scratch is a fixed array of
@@ -69,8 +82,11 @@ int mct_grid_nearest_batch_device(int d, int nchains, int ncell_max,
  * ahead on one stream). A call needing more scratch than the array holds
  * (about 4 B per node per chain plus the kd-tree storage) returns
  * MCT_ERR_ARG. The first call on a device does a one-time address lookup;
- * make it before any stream capture. All calls on a device share the array:
- * calls that overlap in time race and must be ordered by the caller. */
+ * make it before any stream capture; the address is not looked up again, so
+ * calls after a cudaDeviceReset in the same process are not supported. All
+ * calls on a device share the array: calls that overlap in time race and
+ * must be ordered by the caller. Device-side errors: as the allocating form,
+ * read with mct_grid_status. */
 #define MCT_GRID_NOALLOC_SCRATCH_BYTES (32u * 1024u * 1024u)
 int mct_grid_nearest_batch_device_noalloc(int d, int nchains, int ncell_max,
                                           const int *ncells, const double *points,

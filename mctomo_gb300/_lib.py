@@ -29,6 +29,7 @@ SIGNATURES = {
     "mct_kdtree_to_grid": (I, [I, I, P, P, I, I, I, P, P, P, P, P, P, P]),
     "mct_grid_nearest_batch_device": (I, [I, I, I, P, P, P, I, I, I, P, P, P, P, P, P, P, P]),
     "mct_grid_nearest_batch_device_noalloc": (I, [I, I, I, P, P, P, I, I, I, P, P, P, P, P, P, P, P]),
+    "mct_grid_status": (I, [P, P]),
     "mct_surfdisp96": (I, [P, P, P, P, I, I, I, I, I, I, P, D, P, P, P]),
     "mct_surfdisp_mmodes": (I, [P, P, P, P, I, I, I, I, I, I, P, D, P, P, P]),
     "mct_surfmodes": (I, [P, P, P, P, I, P, I, I, I, D, P, P, P]),

@@ -19,6 +19,20 @@ void mct_set_error(const char *what, const char *why, const char *file, int line
   g_last_error = buf;
 }
 
+int mct_smem_attr_raw(const void *func, int bytes) {
+  int dev = 0;
+  MCT_CUDA_TRY(cudaGetDevice(&dev));
+  struct Rec { int dev; const void *func; int bytes; };
+  static std::mutex mu;
+  static std::vector<Rec> done;
+  std::lock_guard<std::mutex> lk(mu);
+  for (const Rec &r : done)
+    if (r.dev == dev && r.func == func && r.bytes >= bytes) return MCT_OK;
+  MCT_CUDA_TRY(cudaFuncSetAttribute(func, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes));
+  done.push_back({dev, func, bytes});
+  return MCT_OK;
+}
+
 namespace {
 
 std::mutex g_mu;
@@ -91,6 +105,11 @@ int mct_grid_nearest_batch_device(int d, int nchains, int ncell_max, const int *
   int rc = launch_grid_nearest(job, s);
   cudaFreeAsync(scratch, s);
   return rc;
+}
+
+int mct_grid_status(void *stream, int *status) {
+  if (!status) return arg_error("mct_grid_status: status is NULL");
+  return grid_status_read(stream, status);
 }
 
 int mct_kdtree_to_grid(int d, int n, const double *points, const double *params, int nx, int ny,

@@ -1304,12 +1304,9 @@ int fm2d_plan(const Fm2dJob &job, Fm2dPlan *plan) {
 namespace {
 template <class TT>
 int launch_solves(const Fm2dJob &job, const Fm2dPlan &plan, cudaStream_t s) {
-  static bool attr = false;
-  if (!attr) {
-    cudaFuncSetAttribute(fm2d_refined_kernel<TT>, cudaFuncAttributeMaxDynamicSharedMemorySize, 227 * 1024);
-    cudaFuncSetAttribute(fm2d_coarse_kernel<TT>, cudaFuncAttributeMaxDynamicSharedMemorySize, 227 * 1024);
-    attr = true;
-  }
+  int rc = mct_smem_attr(fm2d_refined_kernel<TT>, 227 * 1024);
+  if (!rc) rc = mct_smem_attr(fm2d_coarse_kernel<TT>, 227 * 1024);
+  if (rc) return rc;
   if (job.asgr == 1) {
     if (!job.ovf_list || !job.ovf_count) return MCT_ERR_ARG;
     MCT_CUDA_TRY(cudaMemsetAsync(job.ovf_count, 0, sizeof(int), s));

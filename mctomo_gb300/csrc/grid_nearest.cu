@@ -243,16 +243,33 @@ __device__ __forceinline__ double node_coord(double origin, int i1, double step)
 
 struct BoxIdx { int ix0, ix1, iy0, iy1, iz0, iz1; };
 
-__device__ __forceinline__ BoxIdx chain_box(const GridJob &job, int c) {
-  BoxIdx b;
+// The chain's box clipped to the grid. Returns false for an empty or
+// inverted box (the chain is then skipped and the call's status set).
+__device__ __forceinline__ bool chain_box(const GridJob &job, int c, BoxIdx &b) {
   if (job.box) {
     const int *p = job.box + 6 * c;
-    b = {p[0], p[1], p[2], p[3], p[4], p[5]};
+    b = {max(p[0], 1), min(p[1], job.nx), max(p[2], 1), min(p[3], job.ny), max(p[4], 1), min(p[5], job.nz)};
   } else {
     b = {1, job.nx, 1, job.ny, 1, job.nz};
   }
   if (job.d == 2) { b.iz0 = 1; b.iz1 = 1; }
-  return b;
+  return b.ix0 <= b.ix1 && b.iy0 <= b.iy1 && b.iz0 <= b.iz1;
+}
+
+// The chain's nucleus count, or -1 when it lies outside [1, ncell_max]
+// (the chain is then skipped and the call's status set).
+__device__ __forceinline__ int chain_cells(const GridJob &job, int c) {
+  const int n = job.ncells[c];
+  return (n >= 1 && n <= job.ncell_max) ? n : -1;
+}
+
+// Error word that outlives the calls: every launch folds its own status into
+// it (the first nonzero code stays until read by mct_grid_status).
+__device__ int g_grid_status;
+
+__global__ void fold_status_kernel(const int *status) {
+  const int st = *status;
+  if (st != 0) atomicCAS(&g_grid_status, 0, st);
 }
 
 __global__ void __launch_bounds__(GRID_THREADS)
@@ -260,7 +277,13 @@ grid_nearest_kernel(GridJob job) {
   extern __shared__ float4 nuc[];
   __shared__ float s_scale;
   const int c = blockIdx.y;
-  const int n = job.ncells[c];
+  const int n = chain_cells(job, c);
+  BoxIdx b;
+  const bool box_ok = chain_box(job, c, b);
+  if (n < 0 || !box_ok) {
+    if (blockIdx.x == 0 && threadIdx.x == 0) atomicExch(job.status, MCT_ERR_ARG);
+    return;
+  }
   const int d = job.d;
   const double *pts = job.points + (size_t)c * job.ncell_max * d;
   const double *par = job.params + (size_t)c * job.ncell_max * 3;
@@ -277,7 +300,6 @@ grid_nearest_kernel(GridJob job) {
   // shifted coordinates are non-negative finite floats: compare as ints
   atomicMax(reinterpret_cast<int *>(&s_scale), __float_as_int(lmax));
   __syncthreads();
-  BoxIdx b = chain_box(job, c);
   const int bnx = b.ix1 - b.ix0 + 1, bny = b.iy1 - b.iy0 + 1, bnz = b.iz1 - b.iz0 + 1;
   const long nbox = (long)bnx * bny * bnz;
   const float ext = fmaxf(s_scale, fmaxf((float)((job.nx - 1) * job.dx),
@@ -343,9 +365,11 @@ grid_nearest_kernel(GridJob job) {
 // (thread 0) and resolve those nodes with the kdtree2 search.
 __global__ void kd_resolve_kernel(GridJob job, size_t scratch_stride) {
   const int c = blockIdx.x;
+  const int n = chain_cells(job, c);
+  BoxIdx bx;
+  if (n < 0 || !chain_box(job, c, bx)) return;   // skipped by grid_nearest_kernel
   const int cnt = job.tie_count[c];
   if (cnt == 0) return;
-  const int n = job.ncells[c];
   const int d = job.d;
   char *base = static_cast<char *>(job.kd_scratch) + (size_t)c * scratch_stride;
   KdTree t;
@@ -363,7 +387,6 @@ __global__ void kd_resolve_kernel(GridJob job, size_t scratch_stride) {
     s_root = t.root; s_nn = t.nnodes;
   }
   __syncthreads();
-  if (!s_ok) { if (threadIdx.x == 0) atomicExch(job.status, MCT_ERR_INTERNAL); return; }
   t.root = s_root; t.nnodes = s_nn;
   const double *par = job.params + (size_t)c * job.ncell_max * 3;
   const int nzz = d == 3 ? job.nz : 1;
@@ -377,9 +400,16 @@ __global__ void kd_resolve_kernel(GridJob job, size_t scratch_stride) {
     double qv[3] = {node_coord(job.xmin, i, job.dx), node_coord(job.ymin, j, job.dy),
                     d == 3 ? node_coord(job.zmin, k, job.dz) : 0.0};
     int err = 0;
-    int idx = kd_nearest(t, qv, &err);
-    if (err || idx < 1) { atomicExch(job.status, MCT_ERR_INTERNAL); continue; }
+    int idx = s_ok ? kd_nearest(t, qv, &err) : 0;
     size_t oo = (size_t)c * nodes_total + o;
+    if (!s_ok || err || idx < 1) {
+      // the kd-tree could not be built or searched (its depth exceeds the
+      // fixed stacks): the node gets the documented failure value
+      atomicExch(job.status, MCT_ERR_INTERNAL);
+      job.sites_id[oo] = 0;
+      if (job.vp) { job.vp[oo] = 0.0; job.vs[oo] = 0.0; job.rho[oo] = 0.0; }
+      continue;
+    }
     job.sites_id[oo] = idx;
     if (job.vp) {
       job.vp[oo] = par[(size_t)(idx - 1) * 3 + 0];
@@ -402,10 +432,9 @@ int launch_grid_nearest(const GridJob &job, cudaStream_t s) {
   if (job.nchains < 1 || job.ncell_max < 1 || (job.d != 2 && job.d != 3)) return MCT_ERR_ARG;
   size_t smem = (size_t)job.ncell_max * sizeof(float4);
   if (smem > 200 * 1024) return MCT_ERR_ARG;
-  static bool attr = false;
-  if (!attr) {
-    cudaFuncSetAttribute(grid_nearest_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
-    attr = true;
+  if (smem > 48 * 1024) {
+    const int rc = mct_smem_attr(grid_nearest_kernel, 200 * 1024);
+    if (rc) return rc;
   }
   long nodes = (long)job.nx * job.ny * (job.d == 3 ? job.nz : 1);
   MCT_CUDA_TRY(cudaMemsetAsync(job.tie_count, 0, sizeof(int) * job.nchains, s));
@@ -415,5 +444,17 @@ int launch_grid_nearest(const GridJob &job, cudaStream_t s) {
   MCT_CUDA_TRY(cudaGetLastError());
   kd_resolve_kernel<<<job.nchains, 128, 0, s>>>(job, kd_scratch_bytes(job.ncell_max));
   MCT_CUDA_TRY(cudaGetLastError());
+  fold_status_kernel<<<1, 1, 0, s>>>(job.status);
+  MCT_CUDA_TRY(cudaGetLastError());
+  return MCT_OK;
+}
+
+int grid_status_read(void *stream, int *status) {
+  MCT_CUDA_TRY(cudaStreamSynchronize(static_cast<cudaStream_t>(stream)));
+  int st = 0;
+  MCT_CUDA_TRY(cudaMemcpyFromSymbol(&st, g_grid_status, sizeof(int)));
+  const int zero = 0;
+  MCT_CUDA_TRY(cudaMemcpyToSymbol(g_grid_status, &zero, sizeof(int)));
+  *status = st;
   return MCT_OK;
 }

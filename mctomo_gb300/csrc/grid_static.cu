@@ -16,7 +16,13 @@
 //    whose chains, grid and nucleus count need more is rejected with
 //    MCT_ERR_ARG before anything is launched;
 //  * the first call on a device looks up the array's device address with
-//    that device current; make that first call before any stream capture;
+//    that device current; make that first call before any stream capture.
+//    The address is kept for the life of the process: after cudaDeviceReset
+//    (which destroys the device's copy of the array) further calls are not
+//    supported;
+//  * errors found on the device (bad per-chain inputs, a failed tie
+//    resolution) are recorded as for the allocating entry point and read
+//    with mct_grid_status;
 //  * the array is shared by every call on the device: two calls whose work
 //    overlaps in time (different streams, or different host threads without
 //    ordering between them) race on it and produce wrong grids. Order such

@@ -17,6 +17,15 @@
 
 void mct_set_error(const char *what, const char *why, const char *file, int line);
 
+// Raises a kernel's dynamic shared-memory limit to bytes on the current
+// device, once per (device, kernel) and safely from several host threads; the
+// CUDA return code is checked. The record does not survive cudaDeviceReset
+// (calls after a reset in the same process are not supported).
+int mct_smem_attr_raw(const void *func, int bytes);
+template <class K> inline int mct_smem_attr(K *kernel, int bytes) {
+  return mct_smem_attr_raw(reinterpret_cast<const void *>(kernel), bytes);
+}
+
 // Grow-only device buffer (reused across synchronous drop-in calls).
 struct DevBuf {
   void *p = nullptr;
@@ -75,6 +84,10 @@ struct GridJob {
 };
 size_t kd_scratch_bytes(int ncell_max);
 int launch_grid_nearest(const GridJob &job, cudaStream_t s);
+// Waits for the stream, then returns and clears the device's sticky gridding
+// error word (the first nonzero status of any gridding launch since the last
+// read).
+int grid_status_read(void *stream, int *status);
 
 // Dispersion: surfdisp96 per column.
 struct DispJob {

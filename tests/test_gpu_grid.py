@@ -113,3 +113,106 @@ def test_grid_reference_vertices_match_oracle(orc, gpulib, k, shape, lo, st):
     exp = oracle_grid(orc, np.ascontiguousarray(pts), par, nx, ny, nz, lo, st)
     for g, e in zip(got, exp):
         np.testing.assert_array_equal(g, e)
+
+
+def _batch_call(torch, lib, d, ncells, pts, par, shape, lo, st, box=None, guard=64):
+    """mct_grid_nearest_batch_device on device copies; outputs start from a
+    sentinel and carry guard regions before and after them. Returns (rc,
+    status word, sites, (vp, vs, rho), guards intact)."""
+    nch, ncell_max = pts.shape[0], pts.shape[1]
+    nx, ny, nz = shape
+    nodes = nx * ny * (nz if d == 3 else 1)
+    sid = torch.full((nch * nodes + 2 * guard,), -7, dtype=torch.int32, device="cuda")
+    vel = torch.full((3, nch * nodes + 2 * guard), -1.5, dtype=torch.float64, device="cuda")
+    dn = torch.tensor(np.asarray(ncells, np.int32), device="cuda")
+    dp = torch.tensor(np.ascontiguousarray(pts), device="cuda")
+    dq = torch.tensor(np.ascontiguousarray(par), device="cuda")
+    db = torch.tensor(np.asarray(box, np.int32), device="cuda") if box is not None else None
+    lo_h = np.ascontiguousarray(np.asarray(lo, float)[:3]); st_h = np.ascontiguousarray(np.asarray(st, float)[:3])
+    s = torch.cuda.current_stream().cuda_stream
+    off = lambda t: t.data_ptr() + guard * t.element_size()  # noqa: E731
+    rc = lib.mct_grid_nearest_batch_device(d, nch, ncell_max, dn.data_ptr(), dp.data_ptr(), dq.data_ptr(),
+                                           nx, ny, nz if d == 3 else 1, P(lo_h), P(st_h),
+                                           db.data_ptr() if db is not None else None, off(sid), off(vel[0]),
+                                           off(vel[1]), off(vel[2]), s)
+    status = ctypes.c_int(99)
+    assert lib.mct_grid_status(s, ctypes.byref(status)) == 0
+    sid = sid.cpu().numpy(); vel = vel.cpu().numpy()
+    guards_ok = bool((sid[:guard] == -7).all() and (sid[-guard:] == -7).all() and
+                     (vel[:, :guard] == -1.5).all() and (vel[:, -guard:] == -1.5).all())
+    gshape = (nch, nx, ny, nz) if d == 3 else (nch, nx, ny)
+    return rc, status.value, sid[guard:-guard].reshape(gshape), vel[:, guard:-guard].reshape((3,) + gshape), guards_ok
+
+
+def test_batch_box_outside_grid_is_clipped(orc, gpulib):
+    torch = pytest.importorskip("torch")
+    rng = np.random.default_rng(21)
+    nx, ny, nz = 24, 19, 11
+    lo = np.zeros(3); st = np.array([0.5, 0.5, 0.3])
+    hi = lo + st * (np.array([nx, ny, nz]) - 1)
+    pts = np.zeros((2, 90, 3)); par = np.zeros((2, 90, 3))
+    for c in range(2):
+        p, q = synthetic.voronoi_model_3d(rng, 90, lo, hi, (0.3, 2.5))
+        pts[c], par[c] = p, q
+    # chain 0: a box reaching past every face; chain 1: inside the grid
+    box = [[-3, nx + 5, 2, ny + 10, 0, nz + 1], [3, 9, 1, 7, 2, 5]]
+    rc, status, sid, vel, guards_ok = _batch_call(torch, gpulib, 3, [90, 90], pts, par, (nx, ny, nz), lo, st, box)
+    assert rc == 0 and status == 0
+    assert guards_ok, "a gridding write landed outside the output arrays"
+    for c, b in enumerate([[1, nx, 2, ny, 1, nz], box[1]]):
+        e = oracle_grid(orc, pts[c], par[c], nx, ny, nz, lo, st, box=b)
+        inside = np.zeros((nx, ny, nz), bool)
+        inside[b[0] - 1:b[1], b[2] - 1:b[3], b[4] - 1:b[5]] = True
+        np.testing.assert_array_equal(sid[c][inside], e[0][inside])
+        np.testing.assert_array_equal(vel[1, c][inside], e[2][inside])
+        assert (sid[c][~inside] == -7).all() and (vel[:, c][:, ~inside] == -1.5).all()
+
+
+def test_batch_bad_chain_inputs_are_skipped_and_reported(orc, gpulib):
+    torch = pytest.importorskip("torch")
+    rng = np.random.default_rng(22)
+    nx, ny, nz = 16, 14, 9
+    lo = np.zeros(3); st = np.array([0.5, 0.5, 0.5])
+    hi = lo + st * (np.array([nx, ny, nz]) - 1)
+    pts = np.zeros((4, 50, 3)); par = np.zeros((4, 50, 3))
+    for c in range(4):
+        p, q = synthetic.voronoi_model_3d(rng, 50, lo, hi, (0.3, 2.5))
+        pts[c], par[c] = p, q
+    # chain 1: ncells above ncell_max; chain 2: no nuclei; chain 3: inverted box
+    ncells = [50, 51, 0, 50]
+    box = [[1, nx, 1, ny, 1, nz]] * 3 + [[9, 4, 1, ny, 1, nz]]
+    rc, status, sid, vel, guards_ok = _batch_call(torch, gpulib, 3, ncells, pts, par, (nx, ny, nz), lo, st, box)
+    assert rc == 0 and guards_ok
+    assert status == -1            # MCT_ERR_ARG recorded on the device
+    e = oracle_grid(orc, pts[0], par[0], nx, ny, nz, lo, st)
+    np.testing.assert_array_equal(sid[0], e[0])
+    for c in (1, 2, 3):
+        assert (sid[c] == -7).all() and (vel[:, c] == -1.5).all()
+
+
+def test_batch_kd_failure_gives_sentinel_and_status(orc, gpulib):
+    # Nuclei at x = 16^i (i < 250) make kdtree2's average split peel off a few
+    # points per level: a tree ~120 levels deep, beyond the device search
+    # stacks. Two more nuclei make the nodes with y = 2 exact ties, which only
+    # the kd-tree resolves; those nodes get the documented failure value.
+    torch = pytest.importorskip("torch")
+    n = 252
+    pts = np.zeros((1, n, 3))
+    pts[0, :250, 0] = 16.0 ** np.arange(250)
+    pts[0, 250] = [2.0, 1.0, 0.0]
+    pts[0, 251] = [2.0, 3.0, 0.0]
+    par = np.stack([np.arange(n) + 1.0, np.arange(n) + 0.5, np.full(n, 2.0)], 1)[None]
+    shape = (4, 4, 2)
+    lo = np.zeros(3); st = np.ones(3)
+    rc, status, sid, vel, guards_ok = _batch_call(torch, gpulib, 3, [n], pts, par, shape, lo, st)
+    assert rc == 0 and guards_ok
+    assert status == -7            # MCT_ERR_INTERNAL recorded on the device
+    e = oracle_grid(orc, pts[0], par[0], *shape, lo, st)
+    failed = sid[0] == 0
+    assert failed[:, 2, :].all()   # the tie nodes
+    np.testing.assert_array_equal(sid[0][~failed], e[0][~failed])
+    assert (vel[:, 0][:, failed] == 0.0).all()
+    # the status word is cleared by the read
+    s = torch.cuda.current_stream().cuda_stream
+    st2 = ctypes.c_int(99)
+    assert gpulib.mct_grid_status(s, ctypes.byref(st2)) == 0 and st2.value == 0

@@ -79,6 +79,44 @@ def test_noalloc_matches_allocating_entry(gpulib, d, nchains, ncell_max, shape, 
         np.testing.assert_array_equal(got[1], ref[1])
 
 
+def test_noalloc_resolves_ties_like_allocating_entry(gpulib):
+    # Nuclei mirrored across grid planes put many nodes at exactly equal
+    # distances from two nuclei. Those nodes are resolved by the kd-tree
+    # search, whose per-chain tree storage sits in the fixed scratch array.
+    torch = pytest.importorskip("torch")
+    if not torch.cuda.is_available():
+        pytest.skip("needs a GPU")
+    rng = np.random.default_rng(9)
+    nchains, shape = 3, (21, 21, 11)
+    lo = np.zeros(3); st = np.ones(3)
+    models, bases = [], []
+    for c in range(nchains):
+        base = rng.integers(1, 19, (40 + 10 * c, 3)).astype(float)
+        base[:, 2] = rng.integers(1, 10, len(base))
+        p = np.unique(np.concatenate([base + [0.5, 0, 0], base - [0.5, 0, 0], base + [0, 0.5, 0.5]]), axis=0)
+        models.append(p)
+        bases.append(base)
+    ncell_max = max(len(p) for p in models)
+    pts = np.zeros((nchains, ncell_max, 3)); par = np.zeros((nchains, ncell_max, 3))
+    for c, p in enumerate(models):
+        pts[c, :len(p)] = p
+        par[c, :len(p)] = np.stack([np.arange(len(p)) + 1.0, np.arange(len(p)) * 0.5 + 1, np.ones(len(p))], 1)
+    # the inputs really hold exact ties: grid node `base` lies halfway
+    # between its nucleus pair at x +- 0.5, with nothing closer
+    d2 = ((models[0][None] - bases[0][:, None]) ** 2).sum(-1)
+    d2.sort(axis=1)
+    assert (d2[:, 0] == d2[:, 1]).all()
+    ncells = np.array([len(p) for p in models], np.int32)
+    dev = dict(ncells=torch.tensor(ncells, device="cuda"), pts=torch.tensor(pts, device="cuda"),
+               par=torch.tensor(par, device="cuda"), box=None)
+    ref = _run(torch, gpulib, "mct_grid_nearest_batch_device", 3, nchains, ncell_max, shape, dev, lo, st)
+    for _ in range(2):
+        got = _run(torch, gpulib, "mct_grid_nearest_batch_device_noalloc", 3, nchains, ncell_max, shape,
+                   dev, lo, st)
+        np.testing.assert_array_equal(got[0], ref[0])
+        np.testing.assert_array_equal(got[1], ref[1])
+
+
 def test_noalloc_rejects_oversized_call(gpulib):
     torch = pytest.importorskip("torch")
     if not torch.cuda.is_available():
