@@ -153,8 +153,8 @@ def run_gpu(args):
     ws, rank = dist_env()
     if ws > 1:
         import torch.distributed as dist
-        dist.init_process_group("nccl")
         torch.cuda.set_device(int(os.environ.get("LOCAL_RANK", "0")))
+        dist.init_process_group("nccl")
     dev = torch.device("cuda")
     K, W = args.steps, args.warmup
     grid, settings, data, ncells, init, props, n0, n1 = make_workload(K + W + 1)
@@ -375,20 +375,38 @@ def cpu_sample(grid, settings, data, ncells, init, props, n0, n1, nprop, threads
         return out
 
     t_total = 0.0
-    for k in range(nprop):
-        c = k % len(ncells)
+    for k, (c, st) in enumerate(sample_proposals(len(ncells), len(props), nprop)):
         n = int(ncells[c])
         pv = np.zeros((npd, grid["nx"], grid["ny"]))
-        like(init[0][c], init[1][c], n, c, None, pv)          # committed state (untimed)
-        p1, q1 = props[0][0][c], props[0][1][c]
-        mask = f((vs_grid(init[0][c], init[1][c], n) != vs_grid(p1, q1, n)).any(axis=2).reshape(-1), np.int32)
+        p0, q0 = committed_state(init, props, c, st)
+        like(p0, q0, n, c, None, pv)          # committed state (untimed)
+        p1, q1 = props[st][0][c], props[st][1][c]
+        mask = f((vs_grid(p0, q0, n) != vs_grid(p1, q1, n)).any(axis=2).reshape(-1), np.int32)
         pt = np.zeros((npd, nsta, nsta)) if collect is not None else None
         t0 = time.perf_counter()
         out = like(p1, q1, n, c, mask, pv, pt)
         t_total += time.perf_counter() - t0
         if collect is not None:
-            collect.append((c, pt, pv.copy(), out))
+            collect.append((c, st, pt, pv.copy(), out))
     return nprop / t_total
+
+
+def sample_proposals(nchains, nsteps, nprop):
+    """(chain, step) of the sampled proposals: chains spread over the whole
+    batch, steps spread over the whole run."""
+    out = []
+    for k in range(nprop):
+        c = (k * 37 + 5) % nchains
+        st = (k * max(1, nsteps // max(nprop, 1))) % nsteps
+        out.append((c, st))
+    return out
+
+
+def committed_state(init, props, c, st):
+    """Chain c's committed nucleus set before step st (every step commits)."""
+    if st == 0:
+        return init[0][c], init[1][c]
+    return props[st - 1][0][c], props[st - 1][1][c]
 
 
 def cpu_baseline(grid, settings, data, ncells, init, props, n0, n1, args, collect=None):
@@ -411,11 +429,13 @@ def surface_accuracy(grid, settings, data, ncells, init, props, n0, n1, collecte
     err_t = err_v = err_l = 0.0
     errs = []
     one = np.zeros(1, np.int32)
-    for c, ept, epv, eout in collected:
+    for c, st, ept, epv, eout in collected:
         sl = np.zeros(1, np.int32)
-        lk.forward(sl, ncells[c:c + 1], init[0][c:c + 1], init[1][c:c + 1], n0[c:c + 1], n1[c:c + 1])
+        p0, q0 = committed_state(init, props, c, st)
+        lk.forward(sl, ncells[c:c + 1], p0[None], q0[None], n0[c:c + 1], n1[c:c + 1])
         lk.commit(one + 1)
-        o = lk.forward(sl, ncells[c:c + 1], props[0][0][c:c + 1], props[0][1][c:c + 1], n0[c:c + 1], n1[c:c + 1])
+        o = lk.forward(sl, ncells[c:c + 1], props[st][0][c:c + 1], props[st][1][c:c + 1], n0[c:c + 1],
+                       n1[c:c + 1])
         lk.commit(one)
         pt, pv = lk.phase_time(0)
         e = np.abs(pt - ept)[rays]
@@ -425,7 +445,9 @@ def surface_accuracy(grid, settings, data, ncells, init, props, n0, n1, collecte
         err_l = max(err_l, float(abs(o[0, 0] - eout[0]) / abs(eout[0])))
     lk.close()
     e = np.concatenate(errs) if errs else np.zeros(1)
-    return {"proposals_checked": len(collected), "paths_checked": int(e.size), "max_ttime_err_s": err_t,
+    return {"proposals_checked": len(collected),
+            "sampled_chain_step": [[int(c), int(st)] for c, st, _, _, _ in collected],
+            "paths_checked": int(e.size), "max_ttime_err_s": err_t,
             "p99_ttime_err_s": float(np.quantile(e, 0.99)), "frac_paths_within_1e-4_s": float(np.mean(e <= 1e-4)),
             "max_phase_vel_err_kms": err_v, "max_like_rel_err": err_l,
             "reference": "oracle restatement of the reference path, FP64"}
@@ -478,8 +500,8 @@ def run_body(args):
     ws, rank = dist_env()
     if ws > 1:
         import torch.distributed as dist
-        dist.init_process_group("nccl")
         torch.cuda.set_device(int(os.environ.get("LOCAL_RANK", "0")))
+        dist.init_process_group("nccl")
     dev = torch.device("cuda")
     nch = args.chains
     rng = np.random.default_rng(SEED + 1)
@@ -528,12 +550,16 @@ def run_body(args):
         pms.append((time.perf_counter() - t0) * 1e3)
     one.close()
     desc, err, dtype = BODY_SOLVERS[solver]
+    from mctomo_gb300 import lib as _mlib
+    # the tile solver's tuned configuration (shape index * 4 + sweeps index)
+    tile_cfg = int(_mlib().mct_eik3_tile_config(-2, grid["nx"], grid["ny"], grid["nz"], args.order))
     line = {"metric": "body-wave forward evals/s, 1 GB300, " + err, "value": round(value, 4),
             "unit": "proposal evals/s", "n_gpus": ws, "steps": args.steps, "warmup": args.warmup,
             "ms_per_step": round(total / args.steps, 3), "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": dtype,
             "data": "synthetic (seeded, shapes of the configuration)",
-            "config": dict(BODY_CONFIG, chains=nch, order=args.order, eikonal=desc),
+            "config": dict(BODY_CONFIG, chains=nch, order=args.order, eikonal=desc,
+                           tile_config=(tile_cfg if solver == "tiles" else None)),
             "e2e": {"value": round(value, 4), "unit": "proposal evals/s", "h2d_bytes_per_step": h2d,
                     "d2h_bytes_per_step": nch * 4 * 8},
             "note": "host API only (value = e2e): the body context has no device-pointer forward",
@@ -543,54 +569,100 @@ def run_body(args):
                       "p50_ms": round(float(np.percentile(pms, 50)), 3),
                       "p99_ms": round(float(np.percentile(pms, 99)), 3)},
             "clocks": cl, "valid_models": int((out[:, 3] == 0).sum())}
-    if rank == 0 and not args.no_cpu:
-        line["cpu_baseline"] = body_cpu_baseline(grid, settings, data, ev, props[0], args)
     if rank == 0:
+        chains = sorted({0, nch // 3, (2 * nch) // 3})[:args.body_sample]
+        try:
+            cpu, acc = body_cpu_and_accuracy(lk, grid, settings, data, ev, props[0], locs, n0, n1, chains,
+                                             not args.no_cpu)
+            if cpu is not None:
+                line["cpu_baseline"] = cpu
+            line["accuracy"] = acc
+        except Exception as e:   # the throughput line stands without it
+            line["accuracy"] = {"error": "%s: %s" % (type(e).__name__, e)}
         print(json.dumps(line), flush=True)
     lk.close()
     if ws > 1:
         torch.distributed.destroy_process_group()
 
 
-def body_cpu_baseline(grid, settings, data, ev, prop, args):
+def body_oracle_proposal(grid, settings, data, ev, n, pts, par, n0, n1, threads):
     """The oracle's restatement of the reference's body path for one chain's
     proposal: kd-tree gridding, then fastMarching3D from each station for P
-    and S (the reference's OpenMP loop over stations, here a thread pool over
-    all host cores), then the misfit."""
+    and S (the reference's OpenMP loop over stations, here a thread pool),
+    then the misfit reduction. Returns (phase times (np, nsrc, nrev), misfit
+    out, seconds)."""
     import concurrent.futures as cf
     import oracle
     orc = oracle.load()
     P = lambda a: None if a is None else a.ctypes.data_as(ctypes.c_void_p)  # noqa: E731
-    ncells, pts, par = prop
-    n = int(ncells[0])
     nx, ny, nz = grid["nx"], grid["ny"], grid["nz"]
     shp = (nx, ny, nz)
-    threads = os.cpu_count() or 1
     rev = np.asarray(data["rev"])
     locs = np.ascontiguousarray(ev[:, :3])
+    dzs, zms = grid["dz"] / grid["scaling"], grid["zmin"] / grid["scaling"]
+    npp = settings["np"]
     t0 = time.perf_counter()
     sid = np.zeros(shp, np.int32); vp = np.zeros(shp); vs = np.zeros(shp); rho = np.zeros(shp)
-    orc.orc_kdtree_to_grid(3, n, P(np.ascontiguousarray(pts[0, :n])), P(np.ascontiguousarray(par[0, :n])), nx, ny,
+    orc.orc_kdtree_to_grid(3, n, P(np.ascontiguousarray(pts[:n])), P(np.ascontiguousarray(par[:n])), nx, ny,
                            nz, grid["xmin"], grid["ymin"], grid["zmin"], grid["dx"], grid["dy"], grid["dz"], 1, nx, 1,
                            ny, 1, nz, P(sid), P(vp), P(vs), P(rho))
-    jobs = [(p, k) for p in range(2) for k in range(len(rev))]
+    jobs = [(p, k) for p in range(npp) for k in range(len(rev))]
     vels = [vp, vs]
-    pt = np.zeros((2, data["nsrc"], len(rev)))
+    pt = np.zeros((npp, data["nsrc"], len(rev)))
 
     def solve(job):
         p, k = job
         tt = np.zeros(data["nsrc"])
-        orc.orc_fast_marching3d(nx, ny, nz, grid["dx"], grid["dy"], grid["dz"], grid["xmin"], grid["ymin"],
-                                grid["zmin"], P(vels[p]), P(np.ascontiguousarray(rev[k])), P(locs), data["nsrc"],
+        orc.orc_fast_marching3d(nx, ny, nz, grid["dx"], grid["dy"], dzs, grid["xmin"], grid["ymin"], zms,
+                                P(vels[p]), P(np.ascontiguousarray(rev[k])), P(locs), data["nsrc"],
                                 settings["order"], P(tt), None)
         pt[p, :, k] = tt
 
     with cf.ThreadPoolExecutor(threads) as ex:
         list(ex.map(solve, jobs))
-    dt = time.perf_counter() - t0
-    return {"value": round(1.0 / dt, 4), "unit": "proposal evals/s", "cores": threads, "kind": "reference",
-            "sample": "1 proposal (one chain): kd-tree gridding + 120 fastMarching3D solves (the reference's "
-                      "own C++ SFMM as restated bit-exactly) on a thread pool over all host cores"}
+    # the misfit with origin times (src/likelihood_body.F90:284-333)
+    nsrc, nrev = data["nsrc"], len(rev)
+    npairs = nsrc * nrev
+    dtt = np.zeros((npp, 3, npairs))
+    dtt[:, 0] = np.asarray(data["ttime"]).reshape(npp, npairs)
+    dtt[:, 1] = np.asarray(data["sigma"]).reshape(npp, npairs)
+    rs = np.zeros((npp, 2, npairs), np.int32); rs[:, 0] = np.asarray(data["raystat"]).reshape(npp, npairs)
+    sig = np.zeros((npp, npairs)); out = np.zeros(3)
+    ptf = np.ascontiguousarray(pt.reshape(npp, npairs))
+    orc.orc_body_misfit(nsrc, nrev, npp, P(ptf), P(np.ascontiguousarray(ev[:, 3])), P(np.ascontiguousarray(dtt)),
+                        P(np.ascontiguousarray(rs)), P(ptf), settings["sigdep"], P(np.ascontiguousarray(n0)),
+                        P(np.ascontiguousarray(n1)), data["nrays"], P(sig), P(out))
+    return pt, out, time.perf_counter() - t0
+
+
+def body_cpu_and_accuracy(lk, grid, settings, data, ev, prop, locs, n0, n1, chains, with_cpu):
+    """The oracle on whole proposals (every one of the 120 solves) of the
+    given chains of one step: the first one timed as the CPU baseline; the
+    GPU context's travel times and -log L for the same proposals (one more
+    forward of that step) compared with it."""
+    threads = os.cpu_count() or 1
+    ncells, pts, par = prop
+    out_gpu = lk.forward(ncells, pts, par, locs, n0, n1)
+    errs, err_l, cpu = [], 0.0, None
+    for c in chains:
+        ept, eout, dt = body_oracle_proposal(grid, settings, data, ev, int(ncells[c]), pts[c], par[c], n0[c], n1[c],
+                                             threads)
+        if cpu is None:
+            cpu = {"value": round(1.0 / dt, 4), "unit": "proposal evals/s", "cores": threads, "kind": "reference",
+                   "sample": "1 proposal (one chain): kd-tree gridding + 120 fastMarching3D solves (the reference's "
+                             "own C++ SFMM as restated bit-exactly) on a thread pool over all host cores, misfit"}
+        pt, _ = lk.phase_time(c)
+        rays = np.asarray(data["raystat"]).reshape(pt.shape) == 1
+        errs.append(np.abs(pt - ept)[rays])
+        err_l = max(err_l, float(abs(out_gpu[c, 0] - eout[0]) / abs(eout[0])))
+    e = np.concatenate(errs)
+    acc = {"proposals_checked": len(chains), "sampled_chains": [int(c) for c in chains],
+           "times_checked": int(e.size), "max_ttime_err_s": float(e.max()),
+           "p99_ttime_err_s": float(np.quantile(e, 0.99)), "frac_times_within_1e-4_s": float(np.mean(e <= 1e-4)),
+           "max_like_rel_err": err_l,
+           "reference": "oracle restatement of the reference's fastMarching3D (FP64, pinned bit-for-bit to the "
+                        "compiled reference) + misfit"}
+    return (cpu if with_cpu else None), acc
 
 
 LOVE_COLS = 16384
@@ -603,7 +675,11 @@ LOVE_COLS = 16384
 # matrix-vector product 50 + normalisation 5 (div) = 163. Love: 20 (4 div,
 # 1 sqrt).
 DISP_OPS_PER_LAYER = {2: 163, 1: 20}
-FP64_NOMINAL_TFLOPS = 1.25
+# FP64 peak: ncu reports sm__sass_thread_inst_executed_op_dfma_pred_on
+# .sum.peak_sustained = 304 DFMA per cycle on this GPU (2 per SM), i.e.
+# 304 x 2 flop x 2.07 GHz (maximum SM clock) = 1.259 TFLOP/s. It is the
+# device's rated issue rate, not a timed measurement.
+FP64_PEAK_TFLOPS = 304 * 2 * 2.07e9 / 1e12
 DISP_CONFIG = {"workload": "dispersion-precision study: 262,144 independent layered columns (12-40 layers, "
                            "thickness U[0.05,0.5] km, Vs U[0.2,3.5] km/s with a 10% low-velocity-layer chance, "
                            "Vp = 1.73 Vs, Gardner density), 60 periods 0.2-20 s, Rayleigh and Love, fundamental "
@@ -687,8 +763,9 @@ def run_disp(args):
     ops = DISP_OPS_PER_LAYER[2] * lev[2] * ncol + DISP_OPS_PER_LAYER[1] * lev[1] * love_cols
     achieved = ops / (res[0][0] / 1e3) / 1e12
     roofline = {"kernel": "surfdisp_kernel, FP64 variant", "bound": "fp64", "achieved": round(achieved, 4),
-                "peak": FP64_NOMINAL_TFLOPS, "peak_kind": "nominal (no measured FP64 peak)", "unit": "TFLOP/s",
-                "frac": round(achieved / FP64_NOMINAL_TFLOPS, 4), "traffic": None,
+                "peak": round(FP64_PEAK_TFLOPS, 4),
+                "peak_kind": "rated (ncu: 2 DFMA/cycle/SM x 152 SMs x 2.07 GHz); MEASURED_PEAKS.json has no FP64 figure",
+                "unit": "TFLOP/s", "frac": round(achieved / FP64_PEAK_TFLOPS, 4), "traffic": None,
                 "algorithmic_fp64_ops_per_step": round(ops), "ops_per_layer": DISP_OPS_PER_LAYER,
                 "transcendentals_per_layer": {"rayleigh": 5, "love": 2}}
     line = {"metric": "dispersion curves/s (column x wave x mode, phase + group), 1 GB300, phase err<=1e-5 km/s",
@@ -806,6 +883,13 @@ def run_tt2d(args):
         lk.commit(np.ones(nch, np.int32))
         ms.append((time.perf_counter() - t0) * 1e3)
     cl = clocks.stop()
+    cpu = acc = None
+    if not args.no_cpu:
+        try:
+            cpu, kept = tt2d_cpu_baseline(grid, settings, data, ncells, pts, props[0], args)
+            acc = tt2d_accuracy(lk, data, ncells, pts, props[0], n0, n1, kept)
+        except Exception as e:   # the throughput line stands without it
+            acc = {"error": "%s: %s" % (type(e).__name__, e)}
     lk.close()
     value = nch * args.steps / (sum(ms) / 1e3)
     # the plain drop-in: one chain per call
@@ -836,8 +920,10 @@ def run_tt2d(args):
                       "p50_ms": round(float(np.percentile(pms, 50)), 3),
                       "p99_ms": round(float(np.percentile(pms, 99)), 3)},
             "clocks": cl, "valid_models": int((out[:, 3] == 0).sum())}
-    if not args.no_cpu:
-        line["cpu_baseline"] = tt2d_cpu_baseline(grid, settings, data, ncells, pts, props[0], args)
+    if cpu is not None:
+        line["cpu_baseline"] = cpu
+    if acc is not None:
+        line["accuracy"] = acc
     print(json.dumps(line), flush=True)
 
 
@@ -858,7 +944,7 @@ def tt2d_cpu_baseline(grid, settings, data, ncells, pts, par, args):
     threads = os.cpu_count() or 1
     nsample = min(len(ncells), 4 * threads)
 
-    def one(c):
+    def one(c, keep=None):
         n = int(ncells[c])
         sid = np.zeros((nx, ny), np.int32); vp = np.zeros((nx, ny)); vs = np.zeros((nx, ny)); rho = np.zeros((nx, ny))
         orc.orc_kdtree_to_grid(2, n, P(np.ascontiguousarray(pts[c, :n])), P(np.ascontiguousarray(par[c, :n])), nx, ny,
@@ -872,15 +958,34 @@ def tt2d_cpu_baseline(grid, settings, data, ncells, pts, par, args):
         orc.orc_tt2d_misfit(nsrc, nrev, P(et), P(np.ascontiguousarray(data["ttime"])),
                             P(np.ascontiguousarray(data["sigma"])), P(rays), 0, 0, P(np.zeros(nrev)),
                             P(np.zeros(nrev)), 0, P(np.zeros(2)), P(np.full(2, 0.05)), data["nrays"], P(out))
+        if keep is not None:
+            keep[c] = (et, out.copy())
         return out[0]
 
+    kept = {}
     t0 = time.perf_counter()
     with cf.ThreadPoolExecutor(threads) as ex:
-        list(ex.map(one, range(nsample)))
+        list(ex.map(lambda c: one(c, kept), range(nsample)))
     dt = time.perf_counter() - t0
     return {"value": round(nsample / dt, 3), "unit": "proposal evals/s", "cores": threads, "kind": "port",
             "sample": "%d proposals: kd-tree gridding + modrays (16 sources) + misfit, C++ restatement "
-                      "of the reference path, one proposal per core" % nsample}
+                      "of the reference path, one proposal per core" % nsample}, kept
+
+
+def tt2d_accuracy(lk, data, ncells, pts, par, n0, n1, kept):
+    """The GPU context's times and -log L on the oracle's proposals (one
+    more forward of that step): every path with data, all sampled chains."""
+    rays = np.asarray(data["raystat"], np.int32).reshape(len(data["src"]), len(data["rev"])) == 1
+    out = lk.forward(ncells, pts, par, n0, n1)
+    errs, err_l = [], 0.0
+    for c, (et, eout) in sorted(kept.items()):
+        e = np.abs(lk.phase_time(c) - et)[rays]
+        errs.append(e)
+        err_l = max(err_l, float(abs(out[c, 0] - eout[0]) / abs(eout[0])))
+    e = np.concatenate(errs)
+    return {"proposals_checked": len(kept), "paths_checked": int(e.size), "max_ttime_err_s": float(e.max()),
+            "p99_ttime_err_s": float(np.quantile(e, 0.99)), "frac_paths_within_1e-4_s": float(np.mean(e <= 1e-4)),
+            "max_like_rel_err": err_l, "reference": "oracle restatement of the reference path (modrays), FP64"}
 
 
 SERVED_CONFIG = {
@@ -981,6 +1086,170 @@ def run_served(args):
     print(json.dumps(line), flush=True)
 
 
+# ---------------------------------------------------------------------------
+# Small fixed cases of the hot kernels, for profilers (--case). Each prints one
+# line and exits 0.
+#   fm2d: M Voronoi phase maps of 41 x 41 vertices (1 km spacing), 50 stations
+#     between 2 and 38 km, every station pair once, source refinement 4 x over
+#     8 cells (the surface likelihood's fm2d settings); R calls of
+#     mct_modrays_batch.
+#   eik3: 8 velocity grids of 101 x 101 x 51 nodes (0.5 km), 120 solves.
+#   eik3heap: the exact heap march, N solves (default 8) on 4 Voronoi grids of
+#     51 x 51 x 26 nodes (0.5 km, velocities 3-7.5 km/s).
+#   disp: N layered columns (12-40 layers, no low-velocity layers), 20 Rayleigh
+#     fundamental-mode phase periods log-spaced 0.5-5 s, search increment 1e-3
+#     km/s; with --case-study, N columns of the dispersion-precision study
+#     (10 % low-velocity-layer chance, 60 periods 0.2-20 s, fundamental and
+#     first overtone, phase and group).
+#   grid: nearest-nucleus gridding of a 101 x 101 x 51 grid over 50 x 50 x 25
+#     km from 800 nuclei.
+#   tiles: the body-wave forward (101 x 101 x 51 grid, 200 events, 60
+#     stations, P and S, first order) of N chains with each configuration of
+#     the 3D tile solver forced in turn, then the tuned one.
+# ---------------------------------------------------------------------------
+def _case_modules():
+    from mctomo_gb300 import forward, synthetic
+    return forward, synthetic
+
+
+def case_fm2d(precision=1, maps=16, repeat=2):
+    forward, synthetic = _case_modules()
+    rng = np.random.default_rng(0)
+    nvx = nvz = 41
+    st = rng.uniform(2.0, 38.0, (50, 2))
+    srs = np.triu(np.ones((50, 50), np.int32), 1)
+    velv = synthetic.voronoi_phase_maps(rng, maps, nvx, nvz, 1.0, 1.0)
+    for _ in range(repeat):
+        t0 = time.perf_counter()
+        tt = forward.modrays_batch(st, st, srs, nvx, nvz, 0.0, 0.0, 1.0, 1.0, velv, sgdl=4, sgs=8,
+                                   precision=precision)
+        dt = time.perf_counter() - t0
+    print(f"fm2d precision={precision} maps={maps} solves={maps * 49} last_call_s={dt:.4f} t01={tt[0, 0, 1]:.6f}")
+
+
+def case_eik3(order=0):
+    forward, synthetic = _case_modules()
+    rng = np.random.default_rng(1)
+    nx, ny, nz = 101, 101, 51
+    h = (0.5, 0.5, 0.5)
+    lo = (0.0, 0.0, 0.0)
+    z = np.arange(nz) * h[2]
+    vels = np.stack([np.broadcast_to(3.0 + 0.08 * z * (1 + 0.1 * g), (nx, ny, nz)).copy() *
+                     (1 + 0.05 * rng.standard_normal((nx, ny, nz))) for g in range(8)])
+    nsolve = 120
+    grid = (np.arange(nsolve) % 8).astype(np.int32)
+    srcs = rng.uniform([2, 2, 1], [48, 48, 20], (nsolve, 3))
+    rev = rng.uniform([2, 2, 0], [48, 48, 0.5], (60, 3))
+    t0 = time.perf_counter()
+    tt, _, passes = forward.eikonal3d_batch(vels, h, lo, grid, srcs, rev, order=order)
+    dt = time.perf_counter() - t0
+    print(f"eik3 order={order} solves={nsolve} passes={passes} call_s={dt:.4f} t00={tt[0, 0]:.6f}")
+
+
+def case_eik3heap(order=1, solves=8):
+    forward, synthetic = _case_modules()
+    rng = np.random.default_rng(4)
+    shape = (51, 51, 26)
+    h = (0.5, 0.5, 0.5)
+    lo = np.zeros(3); hi = (np.array(shape) - 1) * 0.5
+    X, Y, Z = np.meshgrid(*[np.arange(k) * 0.5 for k in shape], indexing="ij")
+    nodes = np.stack([X.ravel(), Y.ravel(), Z.ravel()], 1)
+    vels = []
+    for g in range(4):
+        pts, par = synthetic.voronoi_model_3d(rng, 120, lo, hi, (3.0 / 1.73, 7.5 / 1.73))
+        d = ((nodes[:, None, :] - pts[None]) ** 2).sum(-1)
+        vels.append((par[:, 1] * 1.73)[d.argmin(1)].reshape(shape))
+    vels = np.stack(vels)
+    grid = (np.arange(solves) % 4).astype(np.int32)
+    srcs = rng.uniform([1, 1, 0], [24, 24, 0.2], (solves, 3))
+    rev = rng.uniform([1, 1, 1], [24, 24, 12], (40, 3))
+    t0 = time.perf_counter()
+    tt, _, _ = forward.eikonal3d_batch(vels, h, lo, grid, srcs, rev, order=order, solver="heap")
+    dt = time.perf_counter() - t0
+    print(f"eik3heap order={order} solves={solves} call_s={dt:.4f} t00={tt[0, 0]:.6f}")
+
+
+def case_disp(precision=1, columns=4096, study=False):
+    forward, synthetic = _case_modules()
+    rng = np.random.default_rng(2)
+    if study:
+        nl, thk, vp, vs, rho = synthetic.layered_columns(rng, columns, nl_range=(12, 40), lvl_prob=0.1)
+        periods = np.geomspace(0.2, 20.0, 60)
+        kw = dict(mode=2, multimode=True)
+    else:
+        nl, thk, vp, vs, rho = synthetic.layered_columns(rng, columns, lvl_prob=0.0)
+        periods = np.geomspace(0.5, 5.0, 20)
+        kw = {}
+    t0 = time.perf_counter()
+    cp, _, ierr, cnt = forward.surfdisp_batch(nl, thk, vp, vs, rho, periods, 2, int(study), 1e-3,
+                                              precision=precision, **kw)
+    dt = time.perf_counter() - t0
+    print(f"disp precision={precision} columns={columns} study={int(study)} call_s={dt:.4f} ierr={int((ierr != 0).sum())} "
+          f"evals_fp64={cnt[0]} evals_fp32={cnt[1]} cp00={cp[0, 0, 0]:.6f}")
+
+
+def case_grid():
+    forward, synthetic = _case_modules()
+    rng = np.random.default_rng(3)
+    lo = np.zeros(3); hi = np.array([50.0, 50.0, 25.0])
+    shape = (101, 101, 51)
+    st = (hi - lo) / (np.array(shape) - 1)
+    pts, par = synthetic.voronoi_model_3d(rng, 800, lo, hi, (1.7, 4.3))
+    t0 = time.perf_counter()
+    sid, _, _, _ = forward.kdtree_to_grid(pts, par, *shape, lo, st)
+    dt = time.perf_counter() - t0
+    print(f"grid nodes={sid.size} nuclei=800 call_s={dt:.4f} sid0={int(sid.ravel()[0])}")
+
+
+def case_tiles(chains=32):
+    forward, synthetic = _case_modules()
+    from mctomo_gb300 import BodyLikelihood, lib
+    L = lib()
+    rng = np.random.default_rng(5)
+    grid, settings, data, ev = synthetic.body_workload(rng)
+    settings["order"] = 0
+    settings["solver"] = 0x10
+    lo = np.zeros(3); hi = np.array([50.0, 50.0, 25.0]); ncell_max = 800
+    ncells = rng.integers(20, ncell_max + 1, chains).astype(np.int32)
+    pts = np.zeros((chains, ncell_max, 3)); par = np.zeros((chains, ncell_max, 3))
+    for c in range(chains):
+        p, q = synthetic.voronoi_model_3d(rng, int(ncells[c]), lo, hi, (3.0 / 1.73, 7.5 / 1.73))
+        q[:, 0] = q[:, 1] * 1.73
+        pts[c, :ncells[c]] = p; par[c, :ncells[c]] = q
+    locs = np.repeat(ev[None], chains, 0)
+    n0 = np.zeros((chains, 2)); n1 = np.full((chains, 2), 0.05)
+    lk = BodyLikelihood(grid, settings, data, nslots=chains, ncell_max=ncell_max)
+    old = L.mct_eik3_tile_config(-1, 0, 0, 0, 0)
+    ref = None
+    for cfg in list(range(20)) + [-1]:
+        L.mct_eik3_tile_config(cfg, 0, 0, 0, 0)
+        lk.forward(ncells, pts, par, locs, n0, n1)
+        t0 = time.perf_counter()
+        out = lk.forward(ncells, pts, par, locs, n0, n1)
+        dt = time.perf_counter() - t0
+        ref = out if ref is None else ref
+        print(f"tiles cfg={cfg} chains={chains} forward_s={dt:.3f} passes={lk.phase_time(0)[1]} "
+              f"max_like_diff={float(np.max(np.abs(out[:, 0] - ref[:, 0]))):.3g}", flush=True)
+    print(f"tiles tuned_cfg={L.mct_eik3_tile_config(-2, 101, 101, 51, 0)}")
+    L.mct_eik3_tile_config(old, 0, 0, 0, 0)
+    lk.close()
+
+
+def run_case(a):
+    if a.case == "fm2d":
+        case_fm2d(a.case_precision, a.case_maps, a.case_repeat)
+    elif a.case == "eik3":
+        case_eik3(a.case_order or 0)
+    elif a.case == "eik3heap":
+        case_eik3heap(1 if a.case_order is None else a.case_order, a.case_solves)
+    elif a.case == "disp":
+        case_disp(a.case_precision, a.case_columns, a.case_study)
+    elif a.case == "tiles":
+        case_tiles(a.chains)
+    else:
+        case_grid()
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -999,9 +1268,22 @@ def main():
     ap.add_argument("--disp-sample", type=int, default=512, help="disp workload: columns checked by the oracle")
     ap.add_argument("--chains", type=int, default=32, help="body workload: chains per step")
     ap.add_argument("--order", type=int, default=0, help="body workload: eikonal order")
+    ap.add_argument("--body-sample", type=int, default=2, help="body workload: proposals checked by the oracle")
     ap.add_argument("--solver", default=None, choices=["tiles", "heap"],
                     help="body workload: 3D solver (default: heap march for order 1, tiles for order 0)")
+    ap.add_argument("--case", default=None, choices=["fm2d", "eik3", "eik3heap", "disp", "grid", "tiles"],
+                    help="run one small fixed case of a hot kernel (for profilers) instead of a workload")
+    ap.add_argument("--case-precision", type=int, default=1)
+    ap.add_argument("--case-maps", type=int, default=16)
+    ap.add_argument("--case-repeat", type=int, default=2)
+    ap.add_argument("--case-solves", type=int, default=8)
+    ap.add_argument("--case-columns", type=int, default=4096)
+    ap.add_argument("--case-order", type=int, default=None)
+    ap.add_argument("--case-study", action="store_true")
     args = ap.parse_args()
+    if args.case:
+        run_case(args)
+        return
     if args.workload in ("body", "disp", "tt2d", "served"):
         if args.impl == "reference":
             print(json.dumps({"impl": "reference", "unavailable": "the reference arm times the surface workload"}))

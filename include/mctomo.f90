@@ -335,6 +335,10 @@ module mctomo_gb300
       type(c_ptr), value :: tfield
       integer(c_int), intent(out) :: passes
     end function
+    integer(c_int) function mct_eik3_tile_config(cfg, nx, ny, nz, order) bind(C, name="mct_eik3_tile_config")
+      import :: c_int
+      integer(c_int), value :: cfg, nx, ny, nz, order
+    end function
 
     ! ---- body-wave likelihood (src/likelihood_body.F90 body_likelihood)
     integer(c_int) function mct_body_create(grid, settings, data, nslots, ncell_max, ctx) &

@@ -41,6 +41,7 @@ SIGNATURES = {
                                     I]),
     "mct_fast_marching3d": (I, [I, I, I, D, D, D, D, D, D, P, P, P, I, I, P, P]),
     "mct_eikonal3d_batch": (I, [I, I, I, I, D, D, D, D, D, D, I, P, P, P, I, P, I, P, P, P]),
+    "mct_eik3_tile_config": (I, [I, I, I, I, I]),
     "mct_body_create": (I, [P, P, P, I, I, P]),
     "mct_body_destroy": (I, [P]),
     "mct_body_forward": (I, [P, I, P, P, P, P, P, P, P]),

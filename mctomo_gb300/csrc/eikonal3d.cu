@@ -391,14 +391,17 @@ int run_config(int cfg, const Eik3Job &job, cudaStream_t s, int max_passes, int 
   }
 }
 
-// Tuned configuration per (grid shape, order, SM count): the first call on a
-// key times every configuration on the first solves of its job (up to
-// kTuneSolves, enough to fill the GPU) and keeps the fastest; later calls
+// Tuned configuration per (device, grid shape, order, SM count): the first
+// call on a key times every configuration on the first solves of its job (up
+// to kTuneSolves, enough to fill the GPU) and keeps the fastest; later calls
 // reuse it. The configurations reach the same fixed point of the update up
-// to the rounding of the fixed-point times (a few units of 2^-shift s).
+// to the rounding of the fixed-point times (a few units of 2^-shift s), so
+// two processes whose tuners chose differently can differ by that much;
+// mct_eik3_tile_config pins one configuration for reproducible times. A
+// tuning round in which no configuration ran is not remembered.
 constexpr int kTuneSolves = 256;
 std::mutex g_tune_mu;
-std::map<std::tuple<int, int, int, int, int>, int> g_tuned;
+std::map<std::tuple<int, int, int, int, int, int>, int> g_tuned;
 int g_force_cfg = -1;     // diagnostics: a fixed configuration (-1: tuned)
 
 int tuned_config(const Eik3Job &job, cudaStream_t s, int max_passes) {
@@ -406,7 +409,7 @@ int tuned_config(const Eik3Job &job, cudaStream_t s, int max_passes) {
   int dev = 0, sms = 0;
   cudaGetDevice(&dev);
   cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-  const auto key = std::make_tuple(job.nx, job.ny, job.nz, job.order, sms);
+  const auto key = std::make_tuple(dev, job.nx, job.ny, job.nz, job.order, sms);
   {
     std::lock_guard<std::mutex> lk(g_tune_mu);
     auto it = g_tuned.find(key);
@@ -416,8 +419,9 @@ int tuned_config(const Eik3Job &job, cudaStream_t s, int max_passes) {
   sub.nsolve = job.nsolve < kTuneSolves ? job.nsolve : kTuneSolves;
   sub.nrev = 0;
   cudaEvent_t e0, e1;
-  if (cudaEventCreate(&e0) != cudaSuccess || cudaEventCreate(&e1) != cudaSuccess) return 0;
-  int best = 0;
+  if (cudaEventCreate(&e0) != cudaSuccess) return -1;
+  if (cudaEventCreate(&e1) != cudaSuccess) { cudaEventDestroy(e0); return -1; }
+  int best = -1;
   float best_ms = 3.4e38f;
   const size_t nn = (size_t)job.nx * job.ny * job.nz;
   for (int cfg = 0; cfg < kNConfigs; ++cfg) {
@@ -433,6 +437,7 @@ int tuned_config(const Eik3Job &job, cudaStream_t s, int max_passes) {
   }
   cudaEventDestroy(e0);
   cudaEventDestroy(e1);
+  if (best < 0) return -1;
   std::lock_guard<std::mutex> lk(g_tune_mu);
   g_tuned[key] = best;
   return best;
@@ -450,17 +455,13 @@ size_t eik3_tiles(const Eik3Job &j) {
   return m;
 }
 
-// Diagnostics (not part of the public header): fixes the tile solver's
-// configuration (tile shape index * 4 + sweep index; -1: tuned per grid
-// shape) and returns the previous setting; with cfg < -1 only reports the
-// configuration tuned for the key (nx, ny, nz, order) (-1 if none yet).
-extern "C" int mct_debug_eik3_tile_config(int cfg, int nx, int ny, int nz, int order) {
+extern "C" int mct_eik3_tile_config(int cfg, int nx, int ny, int nz, int order) {
   if (cfg < -1) {
     int dev = 0, sms = 0;
     cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
     std::lock_guard<std::mutex> lk(g_tune_mu);
-    auto it = g_tuned.find(std::make_tuple(nx, ny, nz, order, sms));
+    auto it = g_tuned.find(std::make_tuple(dev, nx, ny, nz, order, sms));
     return it == g_tuned.end() ? -1 : it->second;
   }
   const int old = g_force_cfg;
@@ -483,6 +484,10 @@ int launch_eik3(Eik3Job &job, cudaStream_t s, int max_passes, int *passes_out, d
   slowness_kernel<<<1024, 256, 0, s>>>(job.vel, job.slow, nn * job.ngrids);
   MCT_CUDA_TRY(cudaGetLastError());
   const int cfg = tuned_config(job, s, max_passes);   // after the slowness, which the trials read
+  if (cfg < 0) {
+    mct_set_error("launch_eik3", "no tile-solver configuration ran while tuning", __FILE__, __LINE__);
+    return MCT_ERR_CUDA;
+  }
   fill_kernel<<<1024, 256, 0, s>>>(job.T, nn * job.nsolve);
   MCT_CUDA_TRY(cudaGetLastError());
   int err = 0;

@@ -10,8 +10,8 @@ REF=${MCT_REFERENCE:-/root/reference}
 HERE="$(cd "$(dirname "$0")" && pwd)"
 FM="$REF/fastmarching"
 if [ ! -f "$FM/fastMarching.cpp" ]; then
-  echo "reference sources not found at $FM" >&2
-  exit 1
+  echo "reference sources not found at $FM (set MCT_REFERENCE)" >&2
+  exit 2
 fi
 mkdir -p "$HERE/_ref"
 g++ -O3 -std=c++11 -frounding-math -ffp-contract=off -fPIC -shared -w \

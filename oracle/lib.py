@@ -32,10 +32,13 @@ def build_reference():
     """Compile the reference's fastMarching3D from its own sources (only where
     the reference tree is present). Returns the path or None."""
     script = os.path.join(HERE, "build_ref.sh")
-    ref = os.environ.get("MCT_REFERENCE", "/root/reference")
-    if not os.path.exists(os.path.join(ref, "fastmarching", "fastMarching.cpp")):
+    # the recipe locates the reference tree itself (MCT_REFERENCE overrides)
+    # and exits with status 2 where it is absent
+    rc = subprocess.call(["bash", script], cwd=HERE)
+    if rc == 2:
         return REF_LIB if os.path.exists(REF_LIB) else None
-    subprocess.check_call(["bash", script], cwd=HERE)
+    if rc != 0:
+        raise subprocess.CalledProcessError(rc, script)
     return REF_LIB
 
 

@@ -1,19 +1,18 @@
 """Generates tests/golden/reference_vertices.npz from the Voronoi nuclei the
 reference ships with its plotting scripts (plot/run_time_vertices_1.txt and
-_2.txt: a count, then one nucleus per line, x y z and two velocities). Run in
-a tree where the reference is present:
+_2.txt: a count, then one nucleus per line, x y z and two velocities), given
+the reference tree's root:
 
-    python tests/golden/make_vertices.py
+    python tests/golden/make_vertices.py <reference root>   (or MCT_REFERENCE)
 
 The fixture keeps the nuclei (n, 3) and their two values (n, 2) of each file
 as float64, so the gridding tests can run on the reference's own models on
 machines without the reference tree.
 """
 import os
+import sys
 
 import numpy as np
-
-REF = os.environ.get("MCT_REFERENCE", "/root/reference")
 
 
 def read(path):
@@ -25,9 +24,12 @@ def read(path):
 
 
 def main():
+    ref = sys.argv[1] if len(sys.argv) > 1 else os.environ.get("MCT_REFERENCE")
+    if not ref:
+        raise SystemExit("usage: make_vertices.py <reference root> (or set MCT_REFERENCE)")
     data = {}
     for k in (1, 2):
-        pts, val = read(os.path.join(REF, "plot", "run_time_vertices_%d.txt" % k))
+        pts, val = read(os.path.join(ref, "plot", "run_time_vertices_%d.txt" % k))
         data["pts%d" % k] = pts
         data["val%d" % k] = val
     np.savez_compressed(os.path.join(os.path.dirname(os.path.abspath(__file__)), "reference_vertices.npz"), **data)

@@ -226,11 +226,11 @@ def test_tile_solver_configurations_all_match_reference(orc, gpulib):
     rev = lo + ext * rng.uniform(0.02, 0.98, (30, 3))
     exp = [oracle_fmm(orc, vel[0], h, lo, s, rev, 0)[0] for s in srcs]
     grid_of = np.zeros(3, np.int32)
-    old = gpulib.mct_debug_eik3_tile_config(-1, 0, 0, 0, 0)
+    old = gpulib.mct_eik3_tile_config(-1, 0, 0, 0, 0)
     try:
         results = []
         for cfg in range(20):
-            gpulib.mct_debug_eik3_tile_config(cfg, 0, 0, 0, 0)
+            gpulib.mct_eik3_tile_config(cfg, 0, 0, 0, 0)
             got, _, _ = eikonal3d_batch(vel, h, lo, grid_of, srcs, rev, order=0, solver="tiles")
             for i in range(3):
                 assert np.max(np.abs(got[i] - exp[i])) <= TOL, (cfg, i)
@@ -238,8 +238,8 @@ def test_tile_solver_configurations_all_match_reference(orc, gpulib):
         # the configurations differ only by fixed-point rounding
         for got in results[1:]:
             assert np.max(np.abs(got - results[0])) <= 1e-6
-        gpulib.mct_debug_eik3_tile_config(-1, 0, 0, 0, 0)
+        gpulib.mct_eik3_tile_config(-1, 0, 0, 0, 0)
         eikonal3d_batch(vel, h, lo, grid_of, srcs, rev, order=0, solver="tiles")
-        assert 0 <= gpulib.mct_debug_eik3_tile_config(-2, *shape, 0) < 20
+        assert 0 <= gpulib.mct_eik3_tile_config(-2, *shape, 0) < 20
     finally:
-        gpulib.mct_debug_eik3_tile_config(old, 0, 0, 0, 0)
+        gpulib.mct_eik3_tile_config(old, 0, 0, 0, 0)
