@@ -376,7 +376,7 @@ int modrays_batch(int nmaps, int nsrc, const double *scx, const double *scz, int
   rc = ensure_stream(); if (rc) return rc;
   size_t bytes = carve_size({sizeof(double) * nv * nmaps, sizeof(double) * (size_t)nnx * nnz * nmaps,
                              sizeof(double) * (size_t)nnx * nnz * nmaps,
-                             sizeof(double) * (size_t)plan.nref_max * ns, sizeof(double) * (size_t)plan.map_tmp_max * ns,
+                             sizeof(double) * (size_t)plan.nref_map * nmaps, sizeof(double) * (size_t)plan.map_tmp_max * ns,
                              sizeof(short) * (size_t)plan.map_tmp_max * ns, sizeof(int) * (ns + 1),
                              sizeof(double) * 2 * (nsrc + nrc),
                              sizeof(int) * (size_t)srs_nmaps * nsrc * nrc, sizeof(int2) * ns,
@@ -393,7 +393,7 @@ int modrays_batch(int nmaps, int nsrc, const double *scx, const double *scz, int
   double *d_velv = cv.take<double>(nv * nmaps);
   job.veln = cv.take<double>((size_t)nnx * nnz * nmaps);
   job.slon = cv.take<double>((size_t)nnx * nnz * nmaps);
-  job.sref = cv.take<double>((size_t)plan.nref_max * ns);
+  job.sref = cv.take<double>((size_t)plan.nref_map * nmaps);
   job.map_tmp_t = cv.take<double>((size_t)plan.map_tmp_max * ns);
   job.map_tmp_s = cv.take<short>((size_t)plan.map_tmp_max * ns);
   job.ovf_list = cv.take<int>(ns + 1);
@@ -437,6 +437,7 @@ int modrays_batch(int nmaps, int nsrc, const double *scx, const double *scz, int
   job.srs = d_srs; job.nsolve = (int)ns; job.solves = d_solves;
   job.ttime = d_tt; job.tfield = d_tf; job.status = d_status;
   job.nodes_max = plan.nodes_max; job.nref_max = plan.nref_max; job.map_tmp_max = plan.map_tmp_max;
+  job.nref_map = plan.nref_map;
   job.precision = (precision >= 0 && precision <= 2) ? precision : 0;
   int *d_ti = nullptr; double *d_trt = nullptr;
   if (g_trace_solve >= 0) {

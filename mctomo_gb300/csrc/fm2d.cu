@@ -17,6 +17,8 @@
 // -fmad=false so nothing is fused.
 #include "mct_common.cuh"
 #include "fm2d.cuh"
+#include "exact_sqrt.cuh"
+#include <algorithm>
 #include <climits>
 #include <type_traits>
 #include <utility>
@@ -33,8 +35,10 @@ struct Grid2 {
 
 // Per-solve shared-memory state. TT is double (FP64 times, precision 0 and 1)
 // or int (fixed-point times in units of 2^-shift s, precision 2).
+struct CaseTab;
 template <class TT> struct WarpStateT {
   TT *T;              // [ld * cols]
+  CaseTab *tab;       // [8] per-case constants of the FP64 update (precision 0)
   short *S;           // node status: -1 far, 0 alive, >0 heap position
   unsigned short *H;  // heap, 1-based: H[p] = packed node ((ix-1) << 8) | (iz-1)
   int ntr;
@@ -141,12 +145,16 @@ __device__ void downtree(WarpStateT<TT> &w) {
 // Shared-memory layout of one solve: T [n], S [n], H [cap + 2] (1-based
 // heap of at most cap entries), each array starting on a 16-byte boundary.
 __host__ __device__ __forceinline__ int align16(int b) { return (b + 15) & ~15; }
-struct SolveLayout { int offS, offH, bytes; };
+// ... then the 8 per-case constant records of the FP64 update (CaseTab, 64 B
+// each).
+constexpr int CASE_TAB_BYTES = 8 * 64;
+struct SolveLayout { int offS, offH, offTab, bytes; };
 __host__ __device__ __forceinline__ SolveLayout solve_layout(int tbytes, int n, int cap) {
   SolveLayout L;
   L.offS = align16(tbytes * n);
   L.offH = L.offS + align16(2 * n);
-  L.bytes = L.offH + align16(2 * (cap + 2));
+  L.offTab = L.offH + align16(2 * (cap + 2));
+  L.bytes = L.offTab + CASE_TAB_BYTES;
   return L;
 }
 // Heap capacity of the refined source-box stage. The heap holds the narrow
@@ -324,24 +332,60 @@ __device__ __forceinline__ void store_slowness(double *base, size_t i, double s,
 template <class TT> struct UpdConst {
   __device__ void init(const Grid2 &) {}
 };
-// FP64 (precision 0): RN(1/(2a)) for the quadratic of each case, a computed
-// with the reference's expression vv + m uu (4: one term, a = 1). The
-// divisions by 2a and by 3 then take Markstein's correction step (P.
-// Markstein, "Computation of elementary functions on the IBM RISC
-// System/6000 processor", IBM J. Res. Dev. 34(1), 1990): with yinv =
-// RN(1/y), q = RN(x yinv), r = x - q y (exact with a fused multiply-add) and
-// RN(q + r yinv) is the correctly rounded x / y, the bits of the reference's
-// division, in three dependent FP64 operations instead of a division
-// (~550 cycles of latency each on this GPU).
-template <> struct UpdConst<double> {
-  double rtwo_a[5];
-  __device__ void init(const Grid2 &g) {
+// FP64 (precision 0). Every case of fouds1 / fouds2 is evaluated by one
+// straight-line sequence, so the 16 lanes of a warp run the FP64 operations
+// once whatever mix of cases they hold (GB300 issues two FP64 lanes per cycle
+// per SM and charges an FP64 warp instruction the same whatever its active
+// lanes). The sequence performs, for each case, exactly the reference's FP64
+// operations in its order, with per-case operands from a table (CaseTab) in
+// the solve's shared memory:
+//   P = A1 B1 - C1            (4 Tj - Tj2, 3 Tk, 3 Tj, Tj, 4 Tk - Tk2, Tk)
+//   em = (P - Q) + R          (two-term cases; 0 otherwise)
+//   b = (kb em) uu,  c = uu (em em - ss vv),  rd1 = b b - (4a) c
+//   t = tref + (-b + sqrt(max(rd1, 0))) / (2a),  t / 3 for second-order
+//   one-term cases
+// with a = vv + m uu per two-term case and a = 1 for one-term cases, whose
+// c = -(uu ss) the same sequence gives as uu (0 - ss 1). Multiplying by 1 or
+// subtracting 0 is exact, so P and em equal the reference's tref / em.
+// Divisions by 2a and by 3 take Markstein's correction (P. Markstein,
+// "Computation of elementary functions on the IBM RISC System/6000
+// processor", IBM J. Res. Dev. 34(1), 1990): with yinv = RN(1/y),
+// q = RN(x yinv), r = x - q y (exact with a fused multiply-add), RN(q + r
+// yinv) is the correctly rounded x / y. The square root is exact_sqrt_rn
+// (integer and FP32 pipes, the same bits as the library's).
+struct CaseTab {
+  double uu, vv, kb, fa, ta, ra;   // uu, vv, kb; 4a, 2a, RN(1/(2a))
+  int third;                       // the result is divided by 3
+  int pad[3];
+};
+// Case codes: two-term (X, Z) = (2, 2) 0, (2, 1) 1, (1, 2) 2, (1, 1) 3;
+// one-term X = 2: 4, X = 1: 5, Z = 2: 6, Z = 1: 7.
+__device__ __forceinline__ void build_case_tab(CaseTab *tab, const Grid2 &g, int lane) {
+  if (lane < 8) {
     const double u2x = 2.0 * g.dnx, u2z = 2.0 * g.dnz;
     const double hx1 = g.dnx * g.dnx, hz1 = g.dnz * g.dnz, hx2 = u2x * u2x, hz2 = u2z * u2z;
-    const double a[5] = {hz2 + 1.0 * hx2, hx2 + 9.0 * hz1, hz2 + 9.0 * hx1, hz1 + 1.0 * hx1, 1.0};
-#pragma unroll
-    for (int i = 0; i < 5; ++i) rtwo_a[i] = 1.0 / (2.0 * a[i]);
+    CaseTab t;
+    switch (lane) {   // uu, vv of fm2d_ttime.f90's cases
+      case 0: t.uu = hx2; t.vv = hz2; break;
+      case 1: t.uu = hz1; t.vv = hx2; break;
+      case 2: t.uu = hx1; t.vv = hz2; break;
+      case 3: t.uu = hx1; t.vv = hz1; break;
+      case 4: t.uu = hx2; t.vv = 1.0; break;
+      case 5: t.uu = hx1; t.vv = 1.0; break;
+      case 6: t.uu = hz2; t.vv = 1.0; break;
+      default: t.uu = hz1; t.vv = 1.0; break;
+    }
+    const bool m9 = lane == 1 || lane == 2;
+    t.kb = m9 ? 6.0 : 2.0;
+    const double a = lane < 4 ? t.vv + (m9 ? 9.0 : 1.0) * t.uu : 1.0;
+    t.fa = 4.0 * a; t.ta = 2.0 * a; t.ra = 1.0 / (2.0 * a);
+    t.third = (lane == 0 || lane == 4 || lane == 6) ? 1 : 0;
+    t.pad[0] = t.pad[1] = t.pad[2] = 0;
+    tab[lane] = t;
   }
+}
+template <> struct UpdConst<double> {
+  __device__ void init(const Grid2 &) {}
 };
 __device__ __forceinline__ double div_known(double x, double y, double yinv) {
   const double q = __dmul_rn(x, yinv);
@@ -379,45 +423,34 @@ template <> struct UpdConst<int> {
 // FP64, the reference's arithmetic (precision 0). slown is the node's
 // slowness 1/V, precomputed per node with the reference's division.
 __device__ double combo_time(const WarpStateT<double> &w, const Grid2 &g, const Stencil &s, double slown, int fom,
-                             const Fx &, const UpdConst<double> &K) {
+                             const Fx &, const UpdConst<double> &) {
   const double ss = slown * slown;
-  const double u2x = 2.0 * g.dnx, u2z = 2.0 * g.dnz;
-  const double hx1 = g.dnx * g.dnx, hz1 = g.dnz * g.dnz, hx2 = u2x * u2x, hz2 = u2z * u2z;
-  const double Tj = w.T[s.lj], Tk = w.T[s.lk];
-  double a = 1.0, b = 0.0, c, tref, tdiv = 1.0;
-  int ci = 4;
-  if (s.X && s.Z) {
-    double uu, vv, m = 1.0, kb = 2.0, em;
-    if (s.X == 2 && s.Z == 2) {
-      tref = 4.0 * Tj - w.T[s.lj2];
-      em = (tref - 4.0 * Tk) + w.T[s.lk2];
-      uu = hx2; vv = hz2; tdiv = 3.0; ci = 0;
-    } else if (s.X == 2) {
-      em = (3.0 * Tk - 4.0 * Tj) + w.T[s.lj2];
-      uu = hz1; vv = hx2; m = 9.0; kb = 6.0; tref = Tk; ci = 1;
-    } else if (s.Z == 2) {
-      em = (3.0 * Tj - 4.0 * Tk) + w.T[s.lk2];
-      uu = hx1; vv = hz2; m = 9.0; kb = 6.0; tref = Tj; ci = 2;
-    } else {
-      em = Tj - Tk;
-      uu = hx1; vv = hz1; tref = Tj; ci = 3;
-    }
-    a = vv + m * uu;
-    b = (kb * em) * uu;
-    c = uu * (em * em - ss * vv);
-  } else if (s.X) {
-    if (s.X == 2) { tref = 4.0 * Tj - w.T[s.lj2]; c = -(hx2 * ss); tdiv = 3.0; }
-    else { tref = Tj; c = -(ss * hx1); }
-  } else {
-    if (s.Z == 2) { tref = 4.0 * Tk - w.T[s.lk2]; c = -(hz2 * ss); tdiv = 3.0; }
-    else if (fom == 1) { tref = Tk; c = -(ss * hz1); }
-    else { const double sd = slown * g.dnz; tref = Tk; c = -(sd * sd); }
+  const double Tj = w.T[s.lj], Tk = w.T[s.lk], Tj2 = w.T[s.lj2], Tk2 = w.T[s.lk2];
+  const int X = s.X, Z = s.Z;
+  const bool two = X != 0 && Z != 0;
+  const int cc = two ? ((X == 2) ? (Z == 2 ? 0 : 1) : (Z == 2 ? 2 : 3)) : (X ? (X == 2 ? 4 : 5) : (Z == 2 ? 6 : 7));
+  const CaseTab &t = w.tab[cc];
+  // P = A1 B1 - C1: 0, 4: 4 Tj - Tj2; 1: 3 Tk; 2: 3 Tj; 3, 5: Tj; 6: 4 Tk - Tk2; 7: Tk
+  const double A1 = (cc == 0 || cc == 4 || cc == 6) ? 4.0 : ((cc == 1 || cc == 2) ? 3.0 : 1.0);
+  const double B1 = (cc == 1 || cc >= 6) ? Tk : Tj;
+  const double C1 = (cc == 0 || cc == 4) ? Tj2 : (cc == 6 ? Tk2 : 0.0);
+  const double P = A1 * B1 - C1;
+  // em = (P - Q) + R: 0: 4 Tk, Tk2; 1: 4 Tj, Tj2; 2: 4 Tk, Tk2; 3: Tk, 0
+  const double Q = two ? (cc == 3 ? 1.0 : 4.0) * (cc == 1 ? Tj : Tk) : 0.0;
+  const double R = two ? (cc == 1 ? Tj2 : (cc == 3 ? 0.0 : Tk2)) : 0.0;
+  const double em = ((two ? P : 0.0) - Q) + R;
+  const double tref = cc == 1 ? Tk : ((cc == 2 || cc == 3) ? Tj : P);
+  const double b = (t.kb * em) * t.uu;
+  double c = t.uu * (em * em - ss * t.vv);
+  if (fom == 0 && cc == 7) {   // first-order z-only stencil of fouds1
+    const double sd = slown * g.dnz;
+    c = -(sd * sd);
   }
-  // quad_root with the known divisors 2a and 3 (see UpdConst<double>)
-  double rd1 = b * b - 4.0 * a * c;
-  if (rd1 < 0.0) rd1 = 0.0;
-  const double t = tref + div_known(-b + sqrt(rd1), 2.0 * a, K.rtwo_a[ci]);
-  return tdiv == 3.0 ? div_known(t, 3.0, 1.0 / 3.0) : t;
+  double rd1 = b * b - t.fa * c;
+  if (__double_as_longlong(rd1) < 0) rd1 = 0.0;   // rd1 < 0 (rd1 is never -0 or NaN)
+  const double tt = tref + div_known(-b + exact_sqrt_rn(rd1), t.ta, t.ra);
+  const double t3 = div_known(tt, 3.0, 1.0 / 3.0);
+  return t.third ? t3 : tt;
 }
 
 // Double-float (precision 1): the same cases and stencils in FP32-pair
@@ -557,8 +590,8 @@ __device__ __forceinline__ double bilinear(const double nv[2][2], double dsx, do
 struct Trace { int *ti; double *tt; int max; int n; };
 
 template <class TT>
-__device__ void march(WarpStateT<TT> &w, const Grid2 &g, const SlowT<TT> *SL, int fom, int urg, int vnl, int vnr,
-                      int vnt, int vnb, const Fx &fx, Trace *tr = nullptr) {
+__device__ void march(WarpStateT<TT> &w, const Grid2 &g, const SlowT<TT> *SL, int sld, int fom, int urg, int vnl,
+                      int vnr, int vnt, int vnb, const Fx &fx, Trace *tr = nullptr) {
   const int lane = threadIdx.x & 31;
   // lanes 16-31 work on neighbour q = (lane - 16) / 4 of the accepted node,
   // in the reference's order (x-1, x+1, z-1, z+1), stencil combination lane % 4
@@ -570,6 +603,10 @@ __device__ void march(WarpStateT<TT> &w, const Grid2 &g, const SlowT<TT> *SL, in
   SlowT<TT> sl_pred = SlowT<TT>();
   UpdConst<TT> K;
   K.init(g);
+  if constexpr (std::is_same<TT, double>::value) {
+    build_case_tab(w.tab, g, lane);
+    __syncwarp();
+  }
   for (;;) {
     int pk = -1;   // accepted node ((ix-1) << 8) | (iz-1), or -1 to stop
     if (lane == 0 && w.ntr > 0 && !w.overflow) {
@@ -614,7 +651,7 @@ __device__ void march(WarpStateT<TT> &w, const Grid2 &g, const SlowT<TT> *SL, in
         Stencil sc;
         if (st != 0 && combo_stencil(w, g, nz_, nx_, cmb, fom, sc)) {
           have = true;
-          cand = combo_time(w, g, sc, pk == pred ? sl_pred : SL[ln], fom, fx, K);
+          cand = combo_time(w, g, sc, pk == pred ? sl_pred : SL[(nz_ - 1) + (size_t)sld * (nx_ - 1)], fom, fx, K);
         }
       }
     }
@@ -653,7 +690,7 @@ __device__ void march(WarpStateT<TT> &w, const Grid2 &g, const SlowT<TT> *SL, in
     if (lane >= 16 && nxt >= 0) {
       const int nx_ = (nxt >> 8) + 1 + dqx, nz_ = (nxt & 255) + 1 + dqz;
       pred = nxt;
-      if (nx_ >= 1 && nx_ <= g.nnx && nz_ >= 1 && nz_ <= g.nnz) sl_pred = SL[lin(g, nz_, nx_)];
+      if (nx_ >= 1 && nx_ <= g.nnx && nz_ >= 1 && nz_ <= g.nnz) sl_pred = SL[(nz_ - 1) + (size_t)sld * (nx_ - 1)];
     }
     __syncwarp();
     if (lane == 0) {
@@ -742,6 +779,48 @@ __global__ void gridder_kernel(Fm2dJob job) {
   }
 }
 
+// bsplrefine (fm2dray_cartesian.f90:608-674) over the whole map: the refined
+// grid of every source box is a window of one grid, (nvx-1) gdx sgdl + 1 by
+// (nvz-1) gdz sgdl + 1 nodes, and the velocity of a refined node depends only
+// on its position in that grid. So the slowness 1 / v of every refined node
+// is computed once per map (blockIdx.y), with the B-spline weights of the
+// nrxr + 1 (nrzr + 1) positions in a cell tabulated in shared memory, in the
+// operation order of refined_velocity below.
+__global__ void refine_slowness_kernel(Fm2dJob job) {
+  extern __shared__ __align__(16) unsigned char smem[];
+  const int map = blockIdx.y;
+  const int sgdl = job.sgdl;
+  const int nrxr = job.gdx * sgdl, nrzr = job.gdz * sgdl;
+  const int nrgx = (job.nvx - 1) * nrxr + 1, nrgz = (job.nvz - 1) * nrzr + 1;
+  double *wu = reinterpret_cast<double *>(smem), *wv = wu + 4 * (nrxr + 1);
+  for (int q = threadIdx.x; q < 4 * (nrxr + 1) + 4 * (nrzr + 1); q += blockDim.x) {
+    const bool alx = q < 4 * (nrxr + 1);
+    const int e = alx ? q : q - 4 * (nrxr + 1);
+    wu[q] = bsw(e & 3, (double)(e / 4) / (double)(alx ? nrxr : nrzr));
+  }
+  __syncthreads();
+  const int ldv = job.nvz + 2;
+  const double *velv = job.velv + (size_t)map * (job.nvx + 2) * ldv;
+  const int n = nrgx * nrgz;
+  for (int node = blockIdx.x * blockDim.x + threadIdx.x; node < n; node += gridDim.x * blockDim.x) {
+    const int st1 = node % nrgz + 1, st2 = node / nrgz + 1;
+    int i = (st1 - 1) / nrzr + 1; if (i > job.nvz - 1) i = job.nvz - 1;
+    const int k = st1 - nrzr * (i - 1);
+    int j = (st2 - 1) / nrxr + 1; if (j > job.nvx - 1) j = job.nvx - 1;
+    const int l = st2 - nrxr * (j - 1);
+    const double *bu = wu + 4 * (l - 1), *bv = wv + 4 * (k - 1);
+    double sum[4];
+    for (int i1 = 1; i1 <= 4; ++i1) {
+      sum[i1 - 1] = 0.0;
+      for (int j1 = 1; j1 <= 4; ++j1)
+        sum[i1 - 1] = sum[i1 - 1] + bu[j1 - 1] * velv[(size_t)(j - 2 + j1) * ldv + (i - 2 + i1)];
+      sum[i1 - 1] = bv[i1 - 1] * sum[i1 - 1];
+    }
+    store_slowness(job.sref, (size_t)map * job.nref_map + node, 1.0 / (sum[0] + sum[1] + sum[2] + sum[3]),
+                   job.precision);
+  }
+}
+
 // bsplrefine (fm2dray_cartesian.f90:608-674): the cubic B-spline velocity of
 // refined node (idm1, idm2) (1-based z, x) of the source box whose corner is
 // refined node (origz, origx) of the whole grid; 0 outside the coarse box
@@ -768,31 +847,6 @@ __device__ double refined_velocity(const Fm2dJob &job, const RefineBox &rb, int 
     for (int j1 = 1; j1 <= 4; ++j1)
       sum[i1 - 1] = sum[i1 - 1] + bsw(j1 - 1, u) * rb.velv[(size_t)(j - 2 + j1) * rb.ldv + (i - 2 + i1)];
     sum[i1 - 1] = bsw(i1 - 1, v) * sum[i1 - 1];
-  }
-  return sum[0] + sum[1] + sum[2] + sum[3];
-}
-
-// The same with the B-spline weights bsw(q, u) read from tables: wu[(l-1)*4
-// + q] = bsw(q, (l-1)/nrxr) for l = 1 .. nrxr+1, wv likewise along z. The
-// weights are the same values computed once, so the velocity is the same.
-__device__ double refined_velocity_tab(const Fm2dJob &job, const RefineBox &rb, int idm1, int idm2,
-                                       const double *wu, const double *wv) {
-  const int sgdl = job.sgdl;
-  int st1 = idm1 + rb.origz - 1, st2 = idm2 + rb.origx - 1;
-  int i = (st1 - 1) / rb.nrzr + 1; if (i > job.nvz - 1) i = job.nvz - 1;
-  int k = st1 - rb.nrzr * (i - 1);
-  int j = (st2 - 1) / rb.nrxr + 1; if (j > job.nvx - 1) j = job.nvx - 1;
-  int l = st2 - rb.nrxr * (j - 1);
-  int c1 = job.gdz * (i - 1) + (k - 1) / sgdl + 1;
-  int c2 = job.gdx * (j - 1) + (l - 1) / sgdl + 1;
-  if (c1 < rb.vnt || c1 > rb.vnb || c2 < rb.vnl || c2 > rb.vnr) return 0.0;
-  const double *bu = wu + 4 * (l - 1), *bv = wv + 4 * (k - 1);
-  double sum[4];
-  for (int i1 = 1; i1 <= 4; ++i1) {
-    sum[i1 - 1] = 0.0;
-    for (int j1 = 1; j1 <= 4; ++j1)
-      sum[i1 - 1] = sum[i1 - 1] + bu[j1 - 1] * rb.velv[(size_t)(j - 2 + j1) * rb.ldv + (i - 2 + i1)];
-    sum[i1 - 1] = bv[i1 - 1] * sum[i1 - 1];
   }
   return sum[0] + sum[1] + sum[2] + sum[3];
 }
@@ -868,6 +922,7 @@ __device__ __forceinline__ WarpStateT<TT> warp_state(unsigned char *base, int no
   w.T = reinterpret_cast<TT *>(base);
   w.S = reinterpret_cast<short *>(base + lay.offS);
   w.H = reinterpret_cast<unsigned short *>(base + lay.offH);
+  w.tab = reinterpret_cast<CaseTab *>(base + lay.offTab);
   w.ntr = 0;
   w.ld = 1;
   return w;
@@ -904,39 +959,24 @@ fm2d_refined_kernel(Fm2dJob job, int warp_bytes, int heap_cap, int redo) {
            job.dvxd / (double)(job.gdx * sgdl), job.dvzd / (double)(job.gdz * sgdl)};
   Trace trace{job.trace_i, job.trace_t, job.trace_max / 2, 0};
   Trace *tr = (job.trace_i && solve == job.trace_solve && lane == 0) ? &trace : nullptr;
-  // refined slowness (1 / bsplrefine velocity; +inf outside the box, as
-  // the reference's 1/0 there)
-  double *Sr = job.sref + (size_t)solve * job.nref_max;
-  const SlowT<TT> *SLr = reinterpret_cast<const SlowT<TT> *>(Sr);
+  // the box's nodes in the map's refined slowness field (refine_slowness
+  // kernel): refined node (iz, ix) of the box is node (iz + (vnt-1) sgdl,
+  // ix + (vnl-1) sgdl) of the whole refined grid, and every node of the box
+  // lies inside the box's coarse cells, where bsplrefine gives the same
+  // velocity from either numbering
   const int ldv = job.nvz + 2;
   const RefineBox rb{job.velv + (size_t)sg.map * (job.nvx + 2) * ldv, ldv, (vnl - 1) * sgdl + 1,
                      (vnt - 1) * sgdl + 1, job.gdx * sgdl, job.gdz * sgdl, vnl, vnr, vnt, vnb};
-  // the B-spline weight tables sit in the (not yet used) time array
-  const int ntab = 4 * (rb.nrxr + 1) + 4 * (rb.nrzr + 1);
-  if ((size_t)ntab * sizeof(double) <= (size_t)job.nref_max * sizeof(TT)) {
-    double *wu = reinterpret_cast<double *>(w.T), *wv = wu + 4 * (rb.nrxr + 1);
-    for (int q = lane; q < ntab; q += 32) {
-      const bool alx = q < 4 * (rb.nrxr + 1);
-      const int e = alx ? q : q - 4 * (rb.nrxr + 1);
-      const double u = (double)(e / 4) / (double)(alx ? rb.nrxr : rb.nrzr);
-      wu[q] = bsw(e & 3, u);
-    }
-    __syncwarp();
-    for (int node = lane; node < nrnx * nrnz; node += 32)
-      store_slowness(Sr, node, 1.0 / refined_velocity_tab(job, rb, node % nrnz + 1, node / nrnz + 1, wu, wv),
-                     job.precision);
-    __syncwarp();
-  } else {
-    for (int node = lane; node < nrnx * nrnz; node += 32)
-      store_slowness(Sr, node, 1.0 / refined_velocity(job, rb, node % nrnz + 1, node / nrnz + 1), job.precision);
-  }
+  const int nrgz = (job.nvz - 1) * job.gdz * sgdl + 1;
+  const SlowT<TT> *SLr = reinterpret_cast<const SlowT<TT> *>(job.sref) + (size_t)sg.map * job.nref_map +
+                         (size_t)(vnl - 1) * sgdl * nrgz + (size_t)(vnt - 1) * sgdl;
   for (int q = lane; q < nrnx * nrnz; q += 32) w.S[q] = -1;
   w.ld = gr.ld;
   __syncwarp();
   if (lane == 0)
     init_source(w, gr, [&](int zz, int xx) { return refined_velocity(job, rb, zz, xx); }, sg.x, sg.z, fx);
   __syncwarp();
-  march(w, gr, SLr, job.fom, 1, vnl, vnr, vnt, vnb, fx, tr);
+  march(w, gr, SLr, nrgz, job.fom, 1, vnl, vnr, vnt, vnb, fx, tr);
   if (__shfl_sync(0xffffffffu, (int)w.overflow, 0)) {
     if (lane == 0) job.ovf_list[atomicAdd(job.ovf_count, 1)] = solve;
     return;
@@ -1172,11 +1212,11 @@ fm2d_coarse_kernel(Fm2dJob job, int warp_bytes) {
           if (w.S[lin(gc, j, i)] > 0) addtree(w, gc, j, i);
     }
     __syncwarp();
-    march(w, gc, SLc, job.fom, 2, vnl, vnr, vnt, vnb, fx, tr);
+    march(w, gc, SLc, nnz, job.fom, 2, vnl, vnr, vnt, vnb, fx, tr);
   } else {
     if (lane == 0) init_source(w, gc, [&](int zz, int xx) { return Vc[lin(gc, zz, xx)]; }, x, z, fx);
     __syncwarp();
-    march(w, gc, SLc, job.fom, 0, vnl, vnr, vnt, vnb, fx, tr);
+    march(w, gc, SLc, nnz, job.fom, 0, vnl, vnr, vnt, vnb, fx, tr);
   }
   // optional travel-time field
   if (job.tfield) {
@@ -1277,6 +1317,82 @@ extern "C" int mct_debug_fm2d_heap_cap(int cap) {
   return MCT_OK;
 }
 
+namespace {
+__device__ __forceinline__ unsigned long long splitmix64(unsigned long long &x) {
+  unsigned long long z = (x += 0x9E3779B97F4A7C15ull);
+  z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ull;
+  z = (z ^ (z >> 27)) * 0x94D049BB133111EBull;
+  return z ^ (z >> 31);
+}
+
+// Inputs of four kinds, by index mod 4: random positive normal numbers over
+// the whole exponent range; products y * y and their neighbours within
+// 3 ulps (exact and near-exact squares); products y * next(y), next to the
+// squares of the midpoints between two doubles (the hardest rounding cases),
+// and their neighbours; zeros, subnormals, infinities, NaNs and negative
+// numbers.
+__global__ void sqrt_check_kernel(unsigned long long count, unsigned long long seed, unsigned long long *out) {
+  for (unsigned long long i = blockIdx.x * (unsigned long long)blockDim.x + threadIdx.x; i < count;
+       i += (unsigned long long)gridDim.x * blockDim.x) {
+    unsigned long long st = seed ^ (i * 0xD1B54A32D192ED03ull);
+    const unsigned long long r1 = splitmix64(st), r2 = splitmix64(st);
+    unsigned long long bits;
+    switch (i & 3) {
+      case 0:
+        bits = (r1 & 0xFFFFFFFFFFFFFull) | ((1 + r2 % 2046) << 52);
+        break;
+      case 1:
+      case 2: {
+        // y in [2^-500, 2^500)
+        const unsigned long long yb = (r1 & 0xFFFFFFFFFFFFFull) | ((523 + r2 % 1000) << 52);
+        const double y = __longlong_as_double((long long)yb);
+        const double y2 = (i & 3) == 1 ? y : __longlong_as_double((long long)(yb + 1));
+        bits = (unsigned long long)__double_as_longlong(__dmul_rn(y, y2));
+        bits += (long long)((r2 >> 40) % 7) - 3;
+        break;
+      }
+      default: {
+        const unsigned k = (unsigned)(r2 % 8);
+        if (k == 0) bits = 0;
+        else if (k == 1) bits = 1ull << 63;
+        else if (k <= 3) bits = r1 & 0xFFFFFFFFFFFFFull;                 // subnormal
+        else if (k == 4) bits = 0x7FFull << 52;                          // +inf
+        else if (k == 5) bits = (0x7FFull << 52) | (r1 & 0xFFFFFFFFFFFFFull) | 1;   // NaN
+        else bits = (1ull << 63) | (r1 & 0x7FFFFFFFFFFFFFFFull);         // negative
+        break;
+      }
+    }
+    const double x = __longlong_as_double((long long)bits);
+    const double a = exact_sqrt_rn(x), b = sqrt(x);
+    const bool same = __double_as_longlong(a) == __double_as_longlong(b) || (isnan(a) && isnan(b));
+    if (!same) {
+      atomicAdd(&out[0], 1ull);
+      atomicCAS(&out[2], 0ull, bits);
+    }
+  }
+}
+}  // namespace
+
+// Diagnostics (not part of the public header): exact_sqrt_rn against the
+// library's sqrt on count generated inputs (sqrt_check_kernel); out[0]
+// receives the number of results whose bits differ, out[1] the count, out[2]
+// the bits of one differing input (0 if none).
+extern "C" int mct_debug_exact_sqrt_check(unsigned long long count, unsigned long long seed,
+                                          unsigned long long *out) {
+  unsigned long long *d = nullptr;
+  MCT_CUDA_TRY(cudaMalloc(&d, 3 * sizeof(unsigned long long)));
+  cudaError_t e = cudaMemset(d, 0, 3 * sizeof(unsigned long long));
+  if (e == cudaSuccess) {
+    sqrt_check_kernel<<<152 * 8, 256>>>(count, seed, d);
+    e = cudaGetLastError();
+  }
+  if (e == cudaSuccess) e = cudaMemcpy(out, d, 3 * sizeof(unsigned long long), cudaMemcpyDeviceToHost);
+  cudaFree(d);
+  MCT_CUDA_TRY(e);
+  out[1] = count;
+  return MCT_OK;
+}
+
 int fm2d_plan(const Fm2dJob &job, Fm2dPlan *plan) {
   const int nnx = (job.nvx - 1) * job.gdx + 1, nnz = (job.nvz - 1) * job.gdz + 1;
   int nodes = nnx * nnz;
@@ -1292,6 +1408,14 @@ int fm2d_plan(const Fm2dJob &job, Fm2dPlan *plan) {
   const int tbytes = job.precision == 2 ? (int)sizeof(int) : (int)sizeof(double);
   plan->nodes_max = nodes_max;
   plan->nref_max = nref;
+  plan->nref_map = 0;
+  if (job.asgr == 1) {
+    // the map's whole refined grid, and the refine kernel's weight tables
+    const long nrx = (long)(job.nvx - 1) * job.gdx * job.sgdl + 1, nrz = (long)(job.nvz - 1) * job.gdz * job.sgdl + 1;
+    const long tab = 8L * 4 * ((long)job.gdx * job.sgdl + 1 + (long)job.gdz * job.sgdl + 1);
+    if (nrx * nrz > (1L << 30) || tab > 48 * 1024) return MCT_ERR_ARG;
+    plan->nref_map = (int)(nrx * nrz);
+  }
   plan->map_tmp_max = tmp;
   plan->warp_bytes = solve_layout(tbytes, nodes, nodes).bytes;
   plan->ref_heap_cap = nref < g_ref_heap_cap ? nref : g_ref_heap_cap;
@@ -1344,6 +1468,13 @@ int launch_fm2d(const Fm2dJob &job, const Fm2dPlan &plan, cudaStream_t s) {
   gridder_kernel<<<job.nmaps, 256, 0, s>>>(job);
   MCT_CUDA_TRY(cudaGetLastError());
   if (job.nsolve == 0) return MCT_OK;
+  if (job.asgr == 1) {
+    const int nrxr = job.gdx * job.sgdl, nrzr = job.gdz * job.sgdl;
+    const size_t tab = sizeof(double) * 4 * (size_t)(nrxr + 1 + nrzr + 1);
+    const int bx = (int)std::min<long>((job.nref_map + 255) / 256, 64);
+    refine_slowness_kernel<<<dim3(bx, job.nmaps), 256, tab, s>>>(job);
+    MCT_CUDA_TRY(cudaGetLastError());
+  }
   if (job.precision == 2) return launch_solves<int>(job, plan, s);
   if (job.precision == 1) return launch_solves<float2>(job, plan, s);
   return launch_solves<double>(job, plan, s);

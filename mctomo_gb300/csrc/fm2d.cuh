@@ -12,7 +12,7 @@ struct Fm2dJob {
   const double *velv;        // [nmaps][nvx+2][nvz+2] padded vertex grids (Fortran (nvz+2,nvx+2))
   double *veln;              // [nmaps][nnx][nnz] scratch: B-spline node velocities
   double *slon;              // [nmaps][nnx][nnz] scratch: their slownesses (1 / veln)
-  double *sref;              // [nsolve][nref_max] scratch: refined source-box slownesses
+  double *sref;              // [nmaps][nref_map] scratch: slowness of every node of the map's refined grid
   double *map_tmp_t;         // [nsolve][map_tmp_max] scratch
   short *map_tmp_s;          // [nsolve][map_tmp_max] scratch
   int *ovf_list;             // [nsolve] scratch: solves whose refined-box heap overflowed
@@ -36,11 +36,12 @@ struct Fm2dJob {
   // optional pop trace of one solve (debugging): [stage, node, ntr] ints and times
   int trace_solve; int *trace_i; double *trace_t; int trace_max;
   // from fm2d_plan
-  int nodes_max, nref_max, map_tmp_max;
+  int nodes_max, nref_max, map_tmp_max, nref_map;
 };
 
 struct Fm2dPlan {
   int nodes_max, nref_max, map_tmp_max;
+  int nref_map;              // nodes of a map's whole refined grid (asgr = 1)
   int warp_bytes;            // shared memory per solve, coarse-grid stage
   int ref_heap_cap;          // heap entries of the refined source-box stage (asgr = 1)
   int ref_warp_bytes;        // shared memory per solve of that stage

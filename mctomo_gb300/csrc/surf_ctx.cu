@@ -104,7 +104,7 @@ int surf_create(const mct_grid *g, const mct_surf_settings *st, const mct_surf_d
   std::vector<size_t> sz = {
       sizeof(double) * np, sizeof(int) * np * npairs, sizeof(double) * np * npairs, sizeof(double) * np * npairs,
       sizeof(double) * 2 * (nsrc + nrev), sizeof(int) * np * npairs, sizeof(int2) * nsolve,
-      sizeof(double) * (size_t)fp.nref_max * nsolve, sizeof(double) * (size_t)fp.map_tmp_max * nsolve,
+      sizeof(double) * (size_t)fp.nref_map * np * nslots, sizeof(double) * (size_t)fp.map_tmp_max * nsolve,
       sizeof(short) * (size_t)fp.map_tmp_max * nsolve, sizeof(int) * (nsolve + 1),
       sizeof(double) * (size_t)nn * nz2 * np * nslots,
       sizeof(double) * (size_t)nn * nz2 * np * nslots,
@@ -159,7 +159,7 @@ int surf_create(const mct_grid *g, const mct_surf_settings *st, const mct_surf_d
   double *xy = cv.take<double>(2 * (nsrc + nrev));
   int *srs = cv.take<int>((size_t)np * npairs);
   int2 *solves = cv.take<int2>(nsolve);
-  fj.sref = cv.take<double>((size_t)fp.nref_max * nsolve);
+  fj.sref = cv.take<double>((size_t)fp.nref_map * np * nslots);
   fj.map_tmp_t = cv.take<double>((size_t)fp.map_tmp_max * nsolve);
   fj.map_tmp_s = cv.take<short>((size_t)fp.map_tmp_max * nsolve);
   fj.ovf_list = cv.take<int>(nsolve + 1);
@@ -255,6 +255,7 @@ int surf_create(const mct_grid *g, const mct_surf_settings *st, const mct_surf_d
   fj.scx = xy; fj.scz = xy + nsrc; fj.rcx = xy + 2 * nsrc; fj.rcz = xy + 2 * nsrc + nrev;
   fj.srs = srs; fj.solves = solves;
   fj.nodes_max = fp.nodes_max; fj.nref_max = fp.nref_max; fj.map_tmp_max = fp.map_tmp_max;
+  fj.nref_map = fp.nref_map;
   *out = c;
   return MCT_OK;
 }

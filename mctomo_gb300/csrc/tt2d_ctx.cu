@@ -401,7 +401,7 @@ int mct_tt2d_create(const mct_grid *g, const mct_tt2d_settings *st, const mct_tt
       sizeof(int) * npairs, sizeof(double) * 5 * (size_t)npairs, sizeof(double) * 2 * (size_t)ndd * nrev,
       sizeof(int2) * (size_t)std::max(ndd, 1), sizeof(double) * 2 * (nsrc + nrev), sizeof(double) * 2 * (nsrc + nrev),
       // fm2d scratch
-      fm ? sizeof(int2) * nsolve : 0, fm ? sizeof(double) * (size_t)c->fp.nref_max * nsolve : 0,
+      fm ? sizeof(int2) * nsolve : 0, fm ? sizeof(double) * (size_t)c->fp.nref_map * nslots : 0,
       fm ? sizeof(double) * (size_t)c->fp.map_tmp_max * nsolve : 0,
       fm ? sizeof(short) * (size_t)c->fp.map_tmp_max * nsolve : 0, sizeof(int) * (nsolve + 1),
       fm ? sizeof(double) * 2 * (size_t)nnx * nnz * nslots : 0, sizeof(int)};
@@ -442,7 +442,7 @@ int mct_tt2d_create(const mct_grid *g, const mct_tt2d_settings *st, const mct_tt
   double *d_xy = cv.take<double>(2 * (size_t)(nsrc + nrev));
   double *d_sep = cv.take<double>(2 * (size_t)(nsrc + nrev));
   int2 *d_solves = cv.take<int2>(fm ? nsolve : 0);
-  fj.sref = cv.take<double>(fm ? (size_t)c->fp.nref_max * nsolve : 0);
+  fj.sref = cv.take<double>(fm ? (size_t)c->fp.nref_map * nslots : 0);
   fj.map_tmp_t = cv.take<double>(fm ? (size_t)c->fp.map_tmp_max * nsolve : 0);
   fj.map_tmp_s = cv.take<short>(fm ? (size_t)c->fp.map_tmp_max * nsolve : 0);
   fj.ovf_list = cv.take<int>(nsolve + 1);
@@ -506,6 +506,7 @@ int mct_tt2d_create(const mct_grid *g, const mct_tt2d_settings *st, const mct_tt
   fj.scx = d_sep; fj.scz = d_sep + nsrc; fj.rcx = d_sep + 2 * nsrc; fj.rcz = d_sep + 2 * nsrc + nrev;
   fj.srs = d_rays; fj.solves = d_solves;
   fj.nodes_max = c->fp.nodes_max; fj.nref_max = c->fp.nref_max; fj.map_tmp_max = c->fp.map_tmp_max;
+  fj.nref_map = c->fp.nref_map;
   *out = c;
   return MCT_OK;
 }

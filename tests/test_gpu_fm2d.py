@@ -164,3 +164,15 @@ def test_modrays_fixed_point_error_statistics(orc, gpulib, precision):
     err = np.abs(mixed[m] - exact[m])
     assert np.quantile(err, 0.99) <= TT_MIXED_TOL
     assert err.max() <= 5e-2
+
+
+def test_exact_sqrt_matches_library_sqrt_bit_for_bit(gpulib):
+    # the FP64 update's square root runs on the integer and FP32 pipes; it
+    # must give the library sqrt's bits on every input: 2^26 inputs over the
+    # whole exponent range, exact and near-exact squares, squares of
+    # midpoints between doubles (the hardest rounding cases), and special
+    # values (zero, subnormal, infinite, NaN, negative)
+    out = (ctypes.c_ulonglong * 3)()
+    for seed in (1, 2):
+        assert gpulib.mct_debug_exact_sqrt_check(ctypes.c_ulonglong(1 << 26), ctypes.c_ulonglong(seed), out) == 0
+        assert out[0] == 0, "first differing input bits: %#x" % out[2]
