@@ -443,7 +443,39 @@ contains
         import :: c_size_t, c_ptr
         type(c_ptr), value :: str
       end function
-    end interface
+  
+    ! ---- the sampler's random number stream (src/mt19937.f90)
+    integer(c_int) function mct_rng_create(seed, rng) bind(C, name="mct_rng_create")
+      import :: c_int, c_ptr
+      integer(c_int), value :: seed
+      type(c_ptr), intent(out) :: rng
+    end function
+    subroutine mct_rng_destroy(rng) bind(C, name="mct_rng_destroy")
+      import :: c_ptr
+      type(c_ptr), value :: rng
+    end subroutine
+    integer(c_int) function mct_rng_seed(rng, seed) bind(C, name="mct_rng_seed")
+      import :: c_int, c_ptr
+      type(c_ptr), value :: rng
+      integer(c_int), value :: seed
+    end function
+    real(c_double) function mct_rng_unirand(rng) bind(C, name="mct_rng_unirand")
+      import :: c_double, c_ptr
+      type(c_ptr), value :: rng
+    end function
+    real(c_double) function mct_rng_gasdev(rng) bind(C, name="mct_rng_gasdev")
+      import :: c_double, c_ptr
+      type(c_ptr), value :: rng
+    end function
+    integer(c_int) function mct_rng_u32(rng) bind(C, name="mct_rng_u32")
+      import :: c_int, c_ptr
+      type(c_ptr), value :: rng
+    end function
+    integer(c_long_long) function mct_rng_count(rng) bind(C, name="mct_rng_count")
+      import :: c_long_long, c_ptr
+      type(c_ptr), value :: rng
+    end function
+  end interface
     p = mct_last_error()
     if (.not. c_associated(p)) then
       msg = ""

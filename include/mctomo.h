@@ -510,6 +510,26 @@ int mct_tt2d_noise_likelihood(mct_tt2d_ctx *ctx, int nchains,
  * index. */
 int mct_tt2d_phase_time(mct_tt2d_ctx *ctx, int index, double *phase_time);
 
+/* ------------------------------------------------------------------------
+ * The sampler's random number stream, replaces the module mt19937
+ * (src/mt19937.f90): MT19937 seeded as init_genrand(seed) (:96-115; the
+ * reference seeds it from init_random_seed, src/initialise.f90:119), draws
+ * as grnd (:117-172, u / (2^32 - 1) of the 32-bit output u), unirand
+ * (:224-236) and gasdev (:200-222, polar Box-Muller on two grnd draws, host
+ * libm log and sqrt). Each generator counts its draws like RTI%randcount.
+ * Host only: no GPU is used. One generator per chain; a generator is not
+ * safe to use from two threads at once.
+ * ---------------------------------------------------------------------- */
+typedef struct mct_rng mct_rng;
+int mct_rng_create(unsigned seed, mct_rng **rng);
+void mct_rng_destroy(mct_rng *rng);
+int mct_rng_seed(mct_rng *rng, unsigned seed);
+double mct_rng_unirand(mct_rng *rng);
+double mct_rng_gasdev(mct_rng *rng);
+/* the raw 32-bit output (genrand_int32), counted as one draw */
+unsigned mct_rng_u32(mct_rng *rng);
+long long mct_rng_count(const mct_rng *rng);
+
 #ifdef __cplusplus
 }
 #endif

@@ -54,6 +54,13 @@ SIGNATURES = {
     "mct_tt2d_commit": (I, [P, I, P]),
     "mct_tt2d_noise_likelihood": (I, [P, I, P, P, P]),
     "mct_tt2d_phase_time": (I, [P, I, P]),
+    "mct_rng_create": (I, [ctypes.c_uint, P]),
+    "mct_rng_destroy": (None, [P]),
+    "mct_rng_seed": (I, [P, ctypes.c_uint]),
+    "mct_rng_unirand": (D, [P]),
+    "mct_rng_gasdev": (D, [P]),
+    "mct_rng_u32": (ctypes.c_uint, [P]),
+    "mct_rng_count": (ctypes.c_longlong, [P]),
     "mct_surf_create": (I, [P, P, P, I, I, P]),
     "mct_surf_destroy": (I, [P]),
     "mct_surf_forward": (I, [P, I, P, P, P, P, P, P, P]),

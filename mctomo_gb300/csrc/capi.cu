@@ -35,17 +35,51 @@ int mct_smem_attr_raw(const void *func, int bytes) {
 
 namespace {
 
-std::mutex g_mu;
-cudaStream_t g_stream = nullptr;
-DevBuf g_ws;
+// Per host thread and device: the stream and grow-only workspace of the
+// synchronous host-pointer calls. The reference calls its per-solve routines
+// from OpenMP loops (src/likelihood_body.F90:204-224 over stations,
+// src/likelihood_surf.F90:197-206 over columns), so calls from different
+// threads run concurrently on their own streams, sharing nothing. A thread's
+// buffers are released when the thread exits.
+constexpr int kMaxDevices = 64;
+struct ThreadDev {
+  cudaStream_t stream = nullptr;
+  DevBuf ws;
+};
+struct ThreadCtx {
+  ThreadDev dev[kMaxDevices];
+  ~ThreadCtx() {
+    int cur = -1;
+    if (cudaGetDevice(&cur) != cudaSuccess) return;
+    for (int d = 0; d < kMaxDevices; ++d) {
+      if (!dev[d].stream && !dev[d].ws.p) continue;
+      if (cudaSetDevice(d) != cudaSuccess) continue;
+      if (dev[d].stream) cudaStreamDestroy(dev[d].stream);
+      dev[d].ws.release();
+    }
+    cudaSetDevice(cur);
+  }
+};
+thread_local ThreadCtx t_ctx;
+
+int thread_dev(ThreadDev **out) {
+  int d = -1;
+  MCT_CUDA_TRY(cudaGetDevice(&d));
+  if (d < 0 || d >= kMaxDevices) {
+    mct_set_error("thread_dev", "device ordinal beyond 63", __FILE__, __LINE__);
+    return MCT_ERR_ARG;
+  }
+  ThreadDev &td = t_ctx.dev[d];
+  if (!td.stream) MCT_CUDA_TRY(cudaStreamCreateWithFlags(&td.stream, cudaStreamNonBlocking));
+  *out = &td;
+  return MCT_OK;
+}
+
+// the pop trace of one fm2d solve (diagnostics; the last traced call wins)
+std::mutex g_trace_mu;
 int g_trace_solve = -1;
 std::vector<int> g_trace_i;
 std::vector<double> g_trace_t;
-
-int ensure_stream() {
-  if (!g_stream) MCT_CUDA_TRY(cudaStreamCreateWithFlags(&g_stream, cudaStreamNonBlocking));
-  return MCT_OK;
-}
 
 int arg_error(const char *msg) {
   g_last_error = msg;
@@ -127,15 +161,15 @@ int mct_kdtree_to_grid(int d, int n, const double *points, const double *params,
         b[0] > b[1] || b[2] > b[3] || b[4] > b[5])
       return arg_error("mct_kdtree_to_grid: box outside the grid");
   }
-  std::lock_guard<std::mutex> lk(g_mu);
-  int rc = ensure_stream(); if (rc) return rc;
+  ThreadDev *td = nullptr;
+  int rc = thread_dev(&td); if (rc) return rc;
   size_t nodes = (size_t)nx * ny * nzz;
   size_t kd = kd_scratch_bytes(n);
   size_t bytes = carve_size({sizeof(double) * d * n, sizeof(double) * 3 * n, sizeof(int), sizeof(int) * 6,
                              sizeof(int) * nodes, sizeof(double) * nodes * 3, sizeof(int), sizeof(int) * nodes,
                              kd, sizeof(int)});
-  rc = g_ws.reserve(bytes); if (rc) return rc;
-  Carve cv(g_ws.p);
+  rc = td->ws.reserve(bytes); if (rc) return rc;
+  Carve cv(td->ws.p);
   double *d_pts = cv.take<double>((size_t)d * n);
   double *d_par = cv.take<double>((size_t)3 * n);
   int *d_n = cv.take<int>(1);
@@ -147,7 +181,7 @@ int mct_kdtree_to_grid(int d, int n, const double *points, const double *params,
   job.tie_nodes = cv.take<int>(nodes);
   job.kd_scratch = cv.take<char>(kd);
   job.status = cv.take<int>(1);
-  cudaStream_t s = g_stream;
+  cudaStream_t s = td->stream;
   MCT_CUDA_TRY(cudaMemcpyAsync(d_pts, points, sizeof(double) * d * n, cudaMemcpyHostToDevice, s));
   MCT_CUDA_TRY(cudaMemcpyAsync(d_par, params, sizeof(double) * 3 * n, cudaMemcpyHostToDevice, s));
   MCT_CUDA_TRY(cudaMemcpyAsync(d_n, &n, sizeof(int), cudaMemcpyHostToDevice, s));
@@ -220,15 +254,15 @@ int mct_surfdisp_batch(int ncol, int nl_max, const int *nl, const float *thk, co
     return arg_error("mct_surfdisp_batch: bad arguments");
   if (!multimode && mode != 1) return arg_error("surfdisp96 computes one mode; use multimode");
   if (ncol == 0) return MCT_OK;
-  std::lock_guard<std::mutex> lk(g_mu);
-  int rc = ensure_stream(); if (rc) return rc;
+  ThreadDev *td = nullptr;
+  int rc = thread_dev(&td); if (rc) return rc;
   size_t lay = (size_t)ncol * nl_max;
   size_t outn = (size_t)ncol * mode * np;
   size_t bytes = carve_size({sizeof(int) * ncol, 4 * sizeof(float) * lay, sizeof(double) * np,
                              2 * sizeof(double) * outn, sizeof(int) * ncol, 2 * sizeof(unsigned long long),
                              sizeof(int) * ncol});
-  rc = g_ws.reserve(bytes); if (rc) return rc;
-  Carve cv(g_ws.p);
+  rc = td->ws.reserve(bytes); if (rc) return rc;
+  Carve cv(td->ws.p);
   int *d_nl = cv.take<int>(ncol);
   float *d_lay = cv.take<float>(4 * lay);
   double *d_per = cv.take<double>(np);
@@ -236,7 +270,7 @@ int mct_surfdisp_batch(int ncol, int nl_max, const int *nl, const float *thk, co
   int *d_ierr = cv.take<int>(ncol);
   unsigned long long *d_cnt = cv.take<unsigned long long>(2);
   int *d_order = cv.take<int>(ncol);
-  cudaStream_t s = g_stream;
+  cudaStream_t s = td->stream;
   MCT_CUDA_TRY(cudaMemcpyAsync(d_nl, nl, sizeof(int) * ncol, cudaMemcpyHostToDevice, s));
   MCT_CUDA_TRY(cudaMemcpyAsync(d_lay, thk, sizeof(float) * lay, cudaMemcpyHostToDevice, s));
   MCT_CUDA_TRY(cudaMemcpyAsync(d_lay + lay, vp, sizeof(float) * lay, cudaMemcpyHostToDevice, s));
@@ -372,8 +406,8 @@ int modrays_batch(int nmaps, int nsrc, const double *scx, const double *scz, int
   const int nnx = (nvx - 1) * gdx + 1, nnz = (nvz - 1) * gdz + 1;
   const size_t nv = (size_t)(nvx + 2) * (nvz + 2);
   const size_t ns = solves.size();
-  std::lock_guard<std::mutex> lk(g_mu);
-  rc = ensure_stream(); if (rc) return rc;
+  ThreadDev *td = nullptr;
+  rc = thread_dev(&td); if (rc) return rc;
   size_t bytes = carve_size({sizeof(double) * nv * nmaps, sizeof(double) * (size_t)nnx * nnz * nmaps,
                              sizeof(double) * (size_t)nnx * nnz * nmaps,
                              sizeof(double) * (size_t)plan.nref_map * nmaps, sizeof(double) * (size_t)plan.map_tmp_max * ns,
@@ -388,8 +422,8 @@ int modrays_batch(int nmaps, int nsrc, const double *scx, const double *scz, int
                              rays ? sizeof(int) * (size_t)nmaps : 0,
                              rays ? sizeof(double) * (size_t)plan.nref_max * ns : 0,
                              rays ? sizeof(short) * (size_t)plan.nref_max * ns : 0});
-  rc = g_ws.reserve(bytes); if (rc) return rc;
-  Carve cv(g_ws.p);
+  rc = td->ws.reserve(bytes); if (rc) return rc;
+  Carve cv(td->ws.p);
   double *d_velv = cv.take<double>(nv * nmaps);
   job.veln = cv.take<double>((size_t)nnx * nnz * nmaps);
   job.slon = cv.take<double>((size_t)nnx * nnz * nmaps);
@@ -416,7 +450,7 @@ int modrays_batch(int nmaps, int nsrc, const double *scx, const double *scz, int
     job.rays = 1; job.gvel = d_gvel; job.gtime = d_gt; job.raylen = d_gt + (size_t)nmaps * nsrc * nrc;
     job.crazy = d_crazy;
   }
-  cudaStream_t s = g_stream;
+  cudaStream_t s = td->stream;
   if (rays) {
     MCT_CUDA_TRY(cudaMemcpyAsync(d_gvel, gvel, sizeof(double) * (size_t)nmaps * nvx * nvz, cudaMemcpyHostToDevice, s));
     MCT_CUDA_TRY(cudaMemsetAsync(d_gt, 0, sizeof(double) * 2 * (size_t)nmaps * nsrc * nrc, s));
@@ -440,8 +474,13 @@ int modrays_batch(int nmaps, int nsrc, const double *scx, const double *scz, int
   job.nref_map = plan.nref_map;
   job.precision = (precision >= 0 && precision <= 2) ? precision : 0;
   int *d_ti = nullptr; double *d_trt = nullptr;
-  if (g_trace_solve >= 0) {
-    job.trace_solve = g_trace_solve; job.trace_max = 20000;
+  int trace_solve;
+  {
+    std::lock_guard<std::mutex> lk(g_trace_mu);
+    trace_solve = g_trace_solve;
+  }
+  if (trace_solve >= 0) {
+    job.trace_solve = trace_solve; job.trace_max = 20000;
     MCT_CUDA_TRY(cudaMalloc(&d_ti, sizeof(int) * 3 * job.trace_max));
     MCT_CUDA_TRY(cudaMalloc(&d_trt, sizeof(double) * job.trace_max));
     MCT_CUDA_TRY(cudaMemset(d_ti, 0xff, sizeof(int) * 3 * job.trace_max));
@@ -450,6 +489,7 @@ int modrays_batch(int nmaps, int nsrc, const double *scx, const double *scz, int
   rc = launch_fm2d(job, plan, s); if (rc) return rc;
   if (d_ti) {
     MCT_CUDA_TRY(cudaStreamSynchronize(s));
+    std::lock_guard<std::mutex> lk(g_trace_mu);
     g_trace_i.resize(3 * job.trace_max); g_trace_t.resize(job.trace_max);
     MCT_CUDA_TRY(cudaMemcpy(g_trace_i.data(), d_ti, sizeof(int) * 3 * job.trace_max, cudaMemcpyDeviceToHost));
     MCT_CUDA_TRY(cudaMemcpy(g_trace_t.data(), d_trt, sizeof(double) * job.trace_max, cudaMemcpyDeviceToHost));
@@ -509,6 +549,7 @@ int mct_modrays(int nsrc, const double *scx, const double *scz, int nrc, const d
 // Diagnostics (not part of the public header): record the marching order of
 // one solve of the next mct_modrays_batch call.
 int mct_debug_fm2d_trace(int solve, int *idx_out, double *t_out, int max) {
+  std::lock_guard<std::mutex> lk(g_trace_mu);
   if (solve >= -1 && idx_out == nullptr) { g_trace_solve = solve; return MCT_OK; }
   int n = std::min<int>(max, (int)g_trace_t.size());
   for (int i = 0; i < n; ++i) { idx_out[3 * i] = g_trace_i[3 * i]; idx_out[3 * i + 1] = g_trace_i[3 * i + 1]; idx_out[3 * i + 2] = g_trace_i[3 * i + 2]; t_out[i] = g_trace_t[i]; }
@@ -541,8 +582,8 @@ int mct_eikonal3d_batch(int nsolve, int nx, int ny, int nz, double dx, double dy
     if (solve_grid[sI] < 0 || solve_grid[sI] >= ngrids) return arg_error("mct_eikonal3d_batch: bad grid index");
   const double diag = sqrt(((nx - 1) * dx) * ((nx - 1) * dx) + ((ny - 1) * dy) * ((ny - 1) * dy) +
                            ((nz - 1) * dz) * ((nz - 1) * dz));
-  std::lock_guard<std::mutex> lk(g_mu);
-  int rc = ensure_stream(); if (rc) return rc;
+  ThreadDev *td = nullptr;
+  int rc = thread_dev(&td); if (rc) return rc;
   Eik3Job job{};
   job.nsolve = nsolve; job.nx = nx; job.ny = ny; job.nz = nz; job.dx = dx; job.dy = dy; job.dz = dz;
   job.ngrids = ngrids; job.order = ord; job.method = method; job.nrev = nrev; job.rev_per_solve = 0;
@@ -560,8 +601,8 @@ int mct_eikonal3d_batch(int nsolve, int nx, int ny, int nz, double dx, double dy
                              tfield ? sizeof(double) * nn * nsolve : 0,
                              heap ? sizeof(double2) * nn * ngrids : 0,
                              eik3_heap_scratch_bytes(nx, ny, nz, hchunk), sizeof(int)});
-  rc = g_ws.reserve(bytes); if (rc) return rc;
-  Carve cv(g_ws.p);
+  rc = td->ws.reserve(bytes); if (rc) return rc;
+  Carve cv(td->ws.p);
   double *d_vel = cv.take<double>(nn * ngrids);
   job.slow = cv.take<float>(nn * ngrids);
   int *d_sg = cv.take<int>(nsolve);
@@ -586,7 +627,7 @@ int mct_eikonal3d_batch(int nsolve, int nx, int ny, int nz, double dx, double dy
   for (int q = 0; q < nrev; ++q) {
     hrev[3 * q] = rev[3 * q] - xmin; hrev[3 * q + 1] = rev[3 * q + 1] - ymin; hrev[3 * q + 2] = rev[3 * q + 2] - zmin;
   }
-  cudaStream_t s = g_stream;
+  cudaStream_t s = td->stream;
   MCT_CUDA_TRY(cudaMemcpyAsync(d_vel, vel, sizeof(double) * nn * ngrids, cudaMemcpyHostToDevice, s));
   MCT_CUDA_TRY(cudaMemcpyAsync(d_sg, solve_grid, sizeof(int) * nsolve, cudaMemcpyHostToDevice, s));
   MCT_CUDA_TRY(cudaMemcpyAsync(d_src, hsrc.data(), sizeof(double) * 3 * nsolve, cudaMemcpyHostToDevice, s));

@@ -241,10 +241,14 @@ __device__ __forceinline__ float dltar32(double wvno, double omega, int ifunc, c
 __device__ __forceinline__ double fsign1(double x) { return signbit(x) ? -1.0 : 1.0; }
 __device__ __forceinline__ float fsign1f(float x) { return signbit(x) ? -1.f : 1.f; }
 
-// Scans step dc from at most (betmx - cm)/dc + a margin; a NaN trial
-// velocity (which the reference would step forever) ends the scan as a
-// failure after this many steps.
-constexpr int kMaxScan = 1 << 20;
+// A bracketing scan moves by dc between clow >= cm and betmx + dc, at most
+// once down and once up, so it ends within scan_limit steps; a scan that
+// does not (a NaN trial velocity, which the reference would step forever)
+// ends as a failure there.
+__device__ __forceinline__ int scan_limit(double betmx, double cm, double dc) {
+  const double n = (betmx + dc - cm) / dc;
+  return (n >= 0.0 && n < 1.0e8) ? 2 * (int)n + 16 : 16;
+}
 
 // surfdisp96.f:711-732 gtsolh, REAL*4
 __device__ float gtsolh(float a, float b) {
@@ -297,6 +301,7 @@ struct Search {
   double *cp, *cg;
   // column state (surfdisp96 / surfdisp_mmodes main loops)
   int iq, k, ift, kfail, ierr, pass, st;
+  int max_scan;   // scan_limit of the column
   double c[NPMAX], cb[NPMAX];
   double del1st;
   float t1a, t1b;
@@ -409,7 +414,7 @@ struct Search {
           st = S_S32_STEP;
           break;
         case S_S32_STEP:
-          if (it >= kMaxScan) { found = 0; st = S_S32_END; break; }
+          if (it >= max_scan) { found = 0; st = S_S32_END; break; }
           cbv = ca + dc;
           if (cbv <= clow) { found = 0; st = S_S32_END; break; }   // cannot happen going up
           {
@@ -451,7 +456,7 @@ struct Search {
           st = S_S64_STEP;
           break;
         case S_S64_STEP:
-          if (it >= kMaxScan) { st = S_G_FAIL; break; }
+          if (it >= max_scan) { st = S_G_FAIL; break; }
           c2 = idir > 0 ? c1 + dc : c1 - dc;
           if (c2 <= clow) { idir = +1; c1 = clow; ++it; break; }
           if (prefetched(c2, 0, v64)) { st = S_S64_RES; break; }
@@ -600,10 +605,14 @@ struct Search {
 #endif
 constexpr int COLS_PER_WARP = DISP_COLS_PER_WARP;
 
-// Warp-loop limit: far above any column's evaluation count (each scan is
-// capped at kMaxScan steps and each polish at 100); past it the remaining
-// columns report ierr = 1.
-constexpr long long kMaxWarpSteps = 1LL << 28;
+// Warp-loop limit: a column needs at most mode x periods x 2 root searches,
+// each at most one evaluation to start, a scan of max_scan steps, two
+// confirmations and a polish of 100 evaluations; every pending evaluation is
+// served within two passes of the warp loop. Past twice the largest column
+// bound of the warp the remaining columns report ierr = 1.
+__device__ __forceinline__ long long column_eval_bound(int mode, int kmax, int max_scan) {
+  return (long long)mode * kmax * 2 * (2LL * max_scan + 110);
+}
 // Idle lanes evaluate ahead only for FP64 scans that have already taken
 // this many steps: most scans find their bracket within a few steps, and
 // evaluations past the bracket would take FP64 issue slots from other
@@ -712,6 +721,7 @@ __global__ void __launch_bounds__(32) surfdisp_kernel(DispJob job, int share) {
       S.betmx = betmx; S.h = 0.005f;
       S.periods = job.periods; S.cp = cp; S.cg = cg;
       S.iq = 1; S.k = 1; S.ift = 999; S.kfail = -1; S.ierr = 0;
+      S.max_scan = scan_limit((double)betmx, S.cm, S.dc);
       S.del1st = 0.0; S.t1b = 0.0f;
       for (int i = 0; i < kmax; ++i) { S.cb[i] = 0.0; S.c[i] = 0.0; }
       S.st = S_PERIOD;
@@ -731,8 +741,11 @@ __global__ void __launch_bounds__(32) surfdisp_kernel(DispJob job, int share) {
   double v64 = 0.0;
   float v32 = 0.0f;
   long long steps = 0;
+  long long max_steps = valid ? 2 * column_eval_bound(mode, kmax, S.max_scan) + 16 : 0;
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) max_steps = max(max_steps, __shfl_xor_sync(kFull, max_steps, o));
   while (__any_sync(kFull, !done)) {
-    if (++steps > kMaxWarpSteps) {
+    if (++steps > max_steps) {
       if (!done) S.ierr = 1;
       break;
     }

@@ -46,7 +46,8 @@ def _c_decls():
     h = open(os.path.join(ROOT, "include", "mctomo.h")).read()
     h = re.sub(r"/\*.*?\*/", "", h, flags=re.S)
     funcs = {}
-    for m in re.finditer(r"\b(?:int|const char \*)\s*\**\s*(mct_\w+)\s*\(([^)]*)\)\s*;", h):
+    for m in re.finditer(r"\b(?:int|void|double|unsigned|long long|const char \*)\s*\**\s*(mct_\w+)\s*\(([^)]*)\)\s*;",
+                         h):
         funcs[m.group(1)] = [a.strip() for a in m.group(2).split(",") if a.strip() and a.strip() != "void"]
     structs = {}
     for m in re.finditer(r"typedef struct\s*\{(.*?)\}\s*(\w+)\s*;", h, flags=re.S):
@@ -69,7 +70,8 @@ def test_fortran_module_covers_the_header():
     funcs, structs = _c_decls()
     f = open(os.path.join(ROOT, "include", "mctomo.f90")).read()
     ff = {}
-    for m in re.finditer(r'function\s+(mct_\w+)\s*\(([^)]*)\)\s*(?:&\s*)?bind\(C,\s*name="(\w+)"\)', f, flags=re.S):
+    for m in re.finditer(r'(?:function|subroutine)\s+(mct_\w+)\s*\(([^)]*)\)\s*(?:&\s*)?bind\(C,\s*name="(\w+)"\)',
+                         f, flags=re.S):
         assert m.group(1) == m.group(3)
         ff[m.group(1)] = [a for a in m.group(2).replace("&", "").split(",") if a.strip()]
     assert set(ff) == set(funcs)
