@@ -1035,7 +1035,15 @@ def served_backends(single, slots):
                                 nmj, prj, len(ds["freqs"]), single=single)
     jb = serving.BodyBackend(sized("joint", lambda: BodyLikelihood(gb, sb, db, n["joint"], 800)), n["joint"], nmj,
                              prj, ev, single=single)
-    return {"tt2d": tt2d, "surface": surf, "body": body, "joint": serving.JointBackend(js, jb)}, used
+    joint = serving.JointBackend(js, jb)
+    if not single:
+        # The body and joint kinds wait on the host between the 3D solver's
+        # passes; their streams get the device's highest priority so that
+        # their short launches are not queued behind the 2D and surface
+        # kinds' long travel-time kernels.
+        body.set_priority(True)
+        joint.set_priority(True)
+    return {"tt2d": tt2d, "surface": surf, "body": body, "joint": joint}, used
 
 
 def run_served(args):

@@ -475,6 +475,21 @@ contains
       import :: c_long_long, c_ptr
       type(c_ptr), value :: rng
     end function
+    integer(c_int) function mct_surf_set_priority(ctx, high) bind(C, name="mct_surf_set_priority")
+      import :: c_int, c_ptr
+      type(c_ptr), value :: ctx
+      integer(c_int), value :: high
+    end function
+    integer(c_int) function mct_body_set_priority(ctx, high) bind(C, name="mct_body_set_priority")
+      import :: c_int, c_ptr
+      type(c_ptr), value :: ctx
+      integer(c_int), value :: high
+    end function
+    integer(c_int) function mct_tt2d_set_priority(ctx, high) bind(C, name="mct_tt2d_set_priority")
+      import :: c_int, c_ptr
+      type(c_ptr), value :: ctx
+      integer(c_int), value :: high
+    end function
   end interface
     p = mct_last_error()
     if (.not. c_associated(p)) then

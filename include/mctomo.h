@@ -250,6 +250,11 @@ int mct_surf_create(const mct_grid *grid, const mct_surf_settings *settings,
                     const mct_surf_data *data, int nslots, int ncell_max,
                     mct_surf_ctx **ctx);
 int mct_surf_destroy(mct_surf_ctx *ctx);
+/* Runs the context's work on a stream of the device's highest priority
+ * (high != 0) or of normal priority (the default), after its pending work.
+ * No counterpart in the reference: for the served loop, where contexts of
+ * different kinds share the GPU. Refused while a submitted batch is pending. */
+int mct_surf_set_priority(mct_surf_ctx *ctx, int high);
 
 /* Evaluates one proposal per listed chain against its slot's committed
  * state. points / params: [nchains][ncell_max][3] (x, y, z) and
@@ -410,6 +415,11 @@ int mct_body_create(const mct_grid *grid, const mct_body_settings *settings,
                     const mct_body_data *data, int nslots, int ncell_max,
                     mct_body_ctx **ctx);
 int mct_body_destroy(mct_body_ctx *ctx);
+/* Runs the context's work on a stream of the device's highest priority
+ * (high != 0) or of normal priority (the default), after its pending work.
+ * No counterpart in the reference: for the served loop, where contexts of
+ * different kinds share the GPU. */
+int mct_body_set_priority(mct_body_ctx *ctx, int high);
 /* points/params [nchains][ncell_max][3] ((x,y,z) and (vp,vs,rho)),
  * locations [nchains][nsrc][4] event (x, y, z, origin time) (RTI%locations),
  * n0/n1 [nchains][np]; out [nchains][4] = like, misfit, unweighted misfit,
@@ -483,6 +493,11 @@ int mct_tt2d_create(const mct_grid *grid, const mct_tt2d_settings *settings,
                     const mct_tt2d_data *data, int nslots, int ncell_max,
                     mct_tt2d_ctx **ctx);
 int mct_tt2d_destroy(mct_tt2d_ctx *ctx);
+/* Runs the context's work on a stream of the device's highest priority
+ * (high != 0) or of normal priority (the default), after its pending work.
+ * No counterpart in the reference: for the served loop, where contexts of
+ * different kinds share the GPU. */
+int mct_tt2d_set_priority(mct_tt2d_ctx *ctx, int high);
 /* points [nchains][ncell_max][2] (x, y) = RTI%points, params
  * [nchains][ncell_max][3] (velocity first) = RTI%parameters, n0/n1
  * [nchains][2] = RTI%snoise0/1 (travel times, differential times);

@@ -54,6 +54,9 @@ SIGNATURES = {
     "mct_tt2d_commit": (I, [P, I, P]),
     "mct_tt2d_noise_likelihood": (I, [P, I, P, P, P]),
     "mct_tt2d_phase_time": (I, [P, I, P]),
+    "mct_surf_set_priority": (I, [P, I]),
+    "mct_body_set_priority": (I, [P, I]),
+    "mct_tt2d_set_priority": (I, [P, I]),
     "mct_rng_create": (I, [ctypes.c_uint, P]),
     "mct_rng_destroy": (None, [P]),
     "mct_rng_seed": (I, [P, ctypes.c_uint]),

@@ -50,6 +50,11 @@ class BodyLikelihood:
                                                        nslots, ncell_max, ctypes.byref(h)))
         self.h = h
 
+    def set_priority(self, high):
+        """Run this context's work on a high-priority (True) or a normal
+        stream of the device."""
+        check("mct_body_set_priority", lib().mct_body_set_priority(self.h, 1 if high else 0))
+
     def close(self):
         if self.h:
             lib().mct_body_destroy(self.h)

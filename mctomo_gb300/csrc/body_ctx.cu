@@ -294,6 +294,11 @@ int mct_body_create(const mct_grid *g, const mct_body_settings *st, const mct_bo
   return MCT_OK;
 }
 
+int mct_body_set_priority(mct_body_ctx *c, int high) {
+  if (!c) return MCT_ERR_ARG;
+  return mct_restream(&c->stream, high);
+}
+
 int mct_body_destroy(mct_body_ctx *c) {
   if (!c) return MCT_OK;
   cudaStreamSynchronize(c->stream);

@@ -26,7 +26,6 @@
 
 namespace {
 
-constexpr int WARPS_PER_BLOCK_MAX = 8;
 
 struct Grid2 {
   int nnx, nnz, ld;
@@ -148,13 +147,14 @@ __host__ __device__ __forceinline__ int align16(int b) { return (b + 15) & ~15; 
 // ... then the 8 per-case constant records of the FP64 update (CaseTab, 64 B
 // each).
 constexpr int CASE_TAB_BYTES = 8 * 64;
+constexpr int MAILBOX_BYTES = 128;   // ... and the solve's mailbox (last 128 B, see march)
 struct SolveLayout { int offS, offH, offTab, bytes; };
 __host__ __device__ __forceinline__ SolveLayout solve_layout(int tbytes, int n, int cap) {
   SolveLayout L;
   L.offS = align16(tbytes * n);
   L.offH = L.offS + align16(2 * n);
   L.offTab = L.offH + align16(2 * (cap + 2));
-  L.bytes = L.offTab + CASE_TAB_BYTES;
+  L.bytes = L.offTab + CASE_TAB_BYTES + MAILBOX_BYTES;
   return L;
 }
 // Heap capacity of the refined source-box stage. The heap holds the narrow
@@ -272,34 +272,46 @@ __device__ __forceinline__ double to_double(int t, const Fx &fx) { return (doubl
 // a = 1, b = 0, c = -(uu*s^2); the operand order below is the reference's
 // (scaling by 2 and negation are exact, so (2*em)*uu with em = Tj - Tk is
 // bit-identical to the reference's -(2*uu*em) with em = Tk - Tj).
-struct Stencil {
+template <class TT> struct Stencil {
   int X, Z;                 // order of the x and z terms (0, 1, 2)
-  int lj, lj2, lk, lk2;     // nodes j, j2 (along x) and k, k2 (along z)
+  TT Tj, Tj2, Tk, Tk2;      // times of nodes j, j2 (along x) and k, k2 (along z)
 };
 
 // Combination cmb (0..3) of node (iz, ix): j = ix -/+ 1, k = iz -/+ 1.
 // Returns false when the reference skips it (j or k off the grid, neither
-// accepted).
+// accepted). Node curl (the node being accepted, which the heap warp may not
+// have marked yet) counts as accepted with time tcur; it can only be j or k.
+// A second-order node's time is used only when that node is accepted; the
+// times of unused nodes are not read.
 template <class TT>
 __device__ __forceinline__ bool combo_stencil(const WarpStateT<TT> &w, const Grid2 &g, int iz, int ix, int cmb,
-                                              int fom, Stencil &s) {
+                                              int fom, int curl, TT tcur, Stencil<TT> &s) {
   const int dj = cmb < 2 ? -1 : 1, dk = (cmb & 1) ? 1 : -1;
   const int j = ix + dj, k = iz + dk;
   if (j < 1 || j > g.nnx || k < 1 || k > g.nnz) return false;
-  s.lj = lin(g, iz, j); s.lk = lin(g, k, ix);
-  s.lj2 = s.lj; s.lk2 = s.lk;
-  const bool jal = w.S[s.lj] == 0, kal = w.S[s.lk] == 0;
+  const int lj = lin(g, iz, j), lk = lin(g, k, ix);
+  const bool jcur = lj == curl, kcur = lk == curl;
+  const bool jal = jcur || w.S[lj] == 0, kal = kcur || w.S[lk] == 0;
   if (!jal && !kal) return false;
   s.X = jal ? 1 : 0; s.Z = kal ? 1 : 0;
+  s.Tj = jal ? (jcur ? tcur : w.T[lj]) : TT();
+  s.Tk = kal ? (kcur ? tcur : w.T[lk]) : TT();
+  s.Tj2 = s.Tj; s.Tk2 = s.Tk;
   if (fom == 1) {
     const int j2 = j + dj, k2 = k + dk;
     if (jal && j2 >= 1 && j2 <= g.nnx) {
       const int l2 = lin(g, iz, j2);
-      if (w.S[l2] == 0 && tlt(w.T[l2], w.T[s.lj])) { s.X = 2; s.lj2 = l2; }
+      if (w.S[l2] == 0) {
+        const TT t2 = w.T[l2];
+        if (tlt(t2, s.Tj)) { s.X = 2; s.Tj2 = t2; }
+      }
     }
     if (kal && k2 >= 1 && k2 <= g.nnz) {
       const int l2 = lin(g, k2, ix);
-      if (w.S[l2] == 0 && tlt(w.T[l2], w.T[s.lk])) { s.Z = 2; s.lk2 = l2; }
+      if (w.S[l2] == 0) {
+        const TT t2 = w.T[l2];
+        if (tlt(t2, s.Tk)) { s.Z = 2; s.Tk2 = t2; }
+      }
     }
   }
   return true;
@@ -422,10 +434,10 @@ template <> struct UpdConst<int> {
 
 // FP64, the reference's arithmetic (precision 0). slown is the node's
 // slowness 1/V, precomputed per node with the reference's division.
-__device__ double combo_time(const WarpStateT<double> &w, const Grid2 &g, const Stencil &s, double slown, int fom,
-                             const Fx &, const UpdConst<double> &) {
+__device__ double combo_time(const WarpStateT<double> &w, const Grid2 &g, const Stencil<double> &s, double slown,
+                             int fom, const Fx &, const UpdConst<double> &) {
   const double ss = slown * slown;
-  const double Tj = w.T[s.lj], Tk = w.T[s.lk], Tj2 = w.T[s.lj2], Tk2 = w.T[s.lk2];
+  const double Tj = s.Tj, Tk = s.Tk, Tj2 = s.Tj2, Tk2 = s.Tk2;
   const int X = s.X, Z = s.Z;
   const bool two = X != 0 && Z != 0;
   const int cc = two ? ((X == 2) ? (Z == 2 ? 0 : 1) : (Z == 2 ? 2 : 3)) : (X ? (X == 2 ? 4 : 5) : (Z == 2 ? 6 : 7));
@@ -461,12 +473,12 @@ __device__ double combo_time(const WarpStateT<double> &w, const Grid2 &g, const 
 //   a W^2 + 2 B W + c = 0,  B = k e uu,  c = uu (e^2 - s^2 vv),  e = k R_p - R_q,
 // k = alpha_q / alpha_p (0 for one term, whose a = vv = 1), uu and vv the
 // squared stencil spacings of p and q; T = (R_p + W) / alpha_p.
-__device__ float2 combo_time(const WarpStateT<float2> &w, const Grid2 &, const Stencil &s, float2 sl, int,
+__device__ float2 combo_time(const WarpStateT<float2> &, const Grid2 &, const Stencil<float2> &s, float2 sl, int,
                              const Fx &, const UpdConst<float2> &K) {
   const DF slown = f2df(sl);
-  const DF Tj = f2df(w.T[s.lj]), Tk = f2df(w.T[s.lk]);
-  const DF Rx2 = dsub(dmulf(Tj, 4.f), f2df(w.T[s.lj2]));
-  const DF Rz2 = dsub(dmulf(Tk, 4.f), f2df(w.T[s.lk2]));
+  const DF Tj = f2df(s.Tj), Tk = f2df(s.Tk);
+  const DF Rx2 = dsub(dmulf(Tj, 4.f), f2df(s.Tj2));
+  const DF Rz2 = dsub(dmulf(Tk, 4.f), f2df(s.Tk2));
   const DF Rx = s.X == 2 ? Rx2 : Tj, Rz = s.Z == 2 ? Rz2 : Tk;
   const bool two = s.X != 0 && s.Z != 0;
   const bool pz = s.X == 0 || (s.X == 2 && s.Z == 1);
@@ -494,26 +506,26 @@ __device__ float2 combo_time(const WarpStateT<float2> &w, const Grid2 &, const S
 // Fixed point (precision 2): the same cases in FP32 on times taken relative
 // to the combination's first accepted neighbour, rounded back to the
 // fixed-point grid.
-__device__ int combo_time(const WarpStateT<int> &w, const Grid2 &, const Stencil &s, float sl, int,
+__device__ int combo_time(const WarpStateT<int> &, const Grid2 &, const Stencil<int> &s, float sl, int,
                           const Fx &fx, const UpdConst<int> &K) {
   const float slown = sl;
-  const int base = s.X ? w.T[s.lj] : w.T[s.lk];
-  auto sh = [&](int l) { return (float)(w.T[l] - base) * fx.inv; };
-  const float Tj = sh(s.lj), Tk = sh(s.lk);
+  const int base = s.X ? s.Tj : s.Tk;
+  auto sh = [&](int t) { return (float)(t - base) * fx.inv; };
+  const float Tj = sh(s.Tj), Tk = sh(s.Tk);
   float trav;
   bool third = false;
   if (s.X && s.Z) {
     float uu, vv, em, tref, A, IA, k = 1.f;
     const float hx1 = K.dnx * K.dnx, hz1 = K.dnz * K.dnz;
     if (s.X == 2 && s.Z == 2) {
-      tref = 4.f * Tj - sh(s.lj2);
-      em = (tref - 4.f * Tk) + sh(s.lk2);
+      tref = 4.f * Tj - sh(s.Tj2);
+      em = (tref - 4.f * Tk) + sh(s.Tk2);
       uu = 4.f * hx1; vv = 4.f * hz1; A = K.a[0]; IA = K.ia[0]; third = true;
     } else if (s.X == 2) {
-      em = (3.f * Tk - 4.f * Tj) + sh(s.lj2);
+      em = (3.f * Tk - 4.f * Tj) + sh(s.Tj2);
       uu = hz1; vv = 4.f * hx1; k = 3.f; A = K.a[1]; IA = K.ia[1]; tref = Tk;
     } else if (s.Z == 2) {
-      em = (3.f * Tj - 4.f * Tk) + sh(s.lk2);
+      em = (3.f * Tj - 4.f * Tk) + sh(s.Tk2);
       uu = hx1; vv = 4.f * hz1; k = 3.f; A = K.a[2]; IA = K.ia[2]; tref = Tj;
     } else {
       em = Tj - Tk;
@@ -527,10 +539,10 @@ __device__ int combo_time(const WarpStateT<int> &w, const Grid2 &, const Stencil
   } else {
     float tref, h;
     if (s.X) {
-      if (s.X == 2) { tref = 4.f * Tj - sh(s.lj2); h = 2.f * K.dnx; third = true; }
+      if (s.X == 2) { tref = 4.f * Tj - sh(s.Tj2); h = 2.f * K.dnx; third = true; }
       else { tref = Tj; h = K.dnx; }
     } else {
-      if (s.Z == 2) { tref = 4.f * Tk - sh(s.lk2); h = 2.f * K.dnz; third = true; }
+      if (s.Z == 2) { tref = 4.f * Tk - sh(s.Tk2); h = 2.f * K.dnz; third = true; }
       else { tref = Tk; h = K.dnz; }
     }
     trav = tref + h * slown;
@@ -544,17 +556,15 @@ __device__ int combo_time(const WarpStateT<int> &w, const Grid2 &, const Stencil
 __device__ __forceinline__ double time_inf(double) { return __longlong_as_double(0x7ff0000000000000LL); }
 __device__ __forceinline__ float2 time_inf(float2) { return make_float2(__int_as_float(0x7f800000), 0.f); }
 __device__ __forceinline__ int time_inf(int) { return INT_MAX; }
-__device__ __forceinline__ double shfl_xor_time(double v, int m) { return __shfl_xor_sync(0xffffffffu, v, m); }
-__device__ __forceinline__ int shfl_xor_time(int v, int m) { return __shfl_xor_sync(0xffffffffu, v, m); }
-__device__ __forceinline__ float2 shfl_xor_time(float2 v, int m) {
-  return make_float2(__shfl_xor_sync(0xffffffffu, v.x, m), __shfl_xor_sync(0xffffffffu, v.y, m));
+__device__ __forceinline__ double shfl_xor_time(unsigned mk, double v, int m) { return __shfl_xor_sync(mk, v, m); }
+__device__ __forceinline__ int shfl_xor_time(unsigned mk, int v, int m) { return __shfl_xor_sync(mk, v, m); }
+__device__ __forceinline__ float2 shfl_xor_time(unsigned mk, float2 v, int m) {
+  return make_float2(__shfl_xor_sync(mk, v.x, m), __shfl_xor_sync(mk, v.y, m));
 }
-
-
-__device__ __forceinline__ double shfl_time(double v, int src) { return __shfl_sync(0xffffffffu, v, src); }
-__device__ __forceinline__ int shfl_time(int v, int src) { return __shfl_sync(0xffffffffu, v, src); }
-__device__ __forceinline__ float2 shfl_time(float2 v, int src) {
-  return make_float2(__shfl_sync(0xffffffffu, v.x, src), __shfl_sync(0xffffffffu, v.y, src));
+__device__ __forceinline__ double shfl_time(unsigned mk, double v, int src) { return __shfl_sync(mk, v, src); }
+__device__ __forceinline__ int shfl_time(unsigned mk, int v, int src) { return __shfl_sync(mk, v, src); }
+__device__ __forceinline__ float2 shfl_time(unsigned mk, float2 v, int src) {
+  return make_float2(__shfl_sync(mk, v.x, src), __shfl_sync(mk, v.y, src));
 }
 
 // Exact 8-byte round trip of a time through the mapping scratch.
@@ -583,128 +593,214 @@ __device__ __forceinline__ double bilinear(const double nv[2][2], double dsx, do
   return biv;
 }
 
-// The marching loop of travel (fm2d_ttime.f90:137-237), whole warp.
-// urg == 1 adds the refined-box exit test; vnr/vnb are compared with the
-// current (refined) grid size exactly as the reference's module variables
-// are at that point.
+// The marching loop of travel (fm2d_ttime.f90:137-237), run by a pair of
+// warps per solve: the heap warp and the update warp.
+//
+// Per accepted node the reference pops the heap root, restores the heap
+// (downtree), computes the new times of the root's up-to-four neighbours
+// (fouds1/fouds2, which read only accepted nodes) and sifts them into the
+// heap (addtree/updtree). Here the heap warp does all heap work (one lane per
+// solve, in the reference's order, so ties break identically) while the
+// update warp computes the neighbours' times (16 lanes per solve, one stencil
+// combination each). The two overlap: while the heap warp sifts node i's
+// neighbours and pops and restores the heap for node i+1, the update warp
+// already evaluates node i+1's neighbours, for the node that it predicts will
+// be the next root (the root left by downtree unless a sifted neighbour is
+// strictly earlier). The heap warp then reports the node it actually popped;
+// a wrong prediction (possible because fouds2 replaces, rather than lowers, a
+// close node's time, which can leave the heap out of order) is recomputed
+// before its results are used. The update warp writes nothing but the
+// mailbox; the heap warp is the only writer of the times and states, and it
+// changes no accepted node's time, so the update warp's reads (accepted
+// nodes, plus the node being accepted, whose time comes with the
+// prediction) see final values.
+//
+// Per step the warps exchange through the solve's mailbox and two named
+// barriers (64 threads): bar1 after the heap warp's pop (node, new root,
+// end flag), bar2 after the update warp's times. With two solves per pair
+// (SPW = 2) the pair marches them in lockstep: heap lanes 0 and 16, update
+// lanes 0-15 and 16-31, so the update's FP64 instructions serve both.
 struct Trace { int *ti; double *tt; int max; int n; };
 
+template <class TT> struct Mailbox {
+  TT tn[4];     // update warp -> heap warp: new times of the accepted node's neighbours
+  TT rkey;      // heap warp -> update warp: time of the heap root after the removal
+  int cd[4];    // 1: neighbour k (x-1, x+1, z-1, z+1) takes tn[k]
+  int cur;      // heap warp -> update warp: the node accepted in this step
+  int root;     // the heap root after the removal, -1 if the heap is empty
+  int stop;     // 0 marching, 1 ended, 2 ended by a heap overflow
+};
+constexpr int PAIRS_MAX = 7;   // named barriers 1..14: two per warp pair
+
+__device__ __forceinline__ void pair_sync(int id) { asm volatile("bar.sync %0, 64;" ::"r"(id) : "memory"); }
+__device__ __forceinline__ void pair_arrive(int id) { asm volatile("bar.arrive %0, 64;" ::"r"(id) : "memory"); }
+
+// New times of the up-to-four neighbours of node cur (packed; its time tcur)
+// by the 16 lanes of this half-warp: lane hl handles neighbour q = hl / 4 in
+// the reference's order (x-1, x+1, z-1, z+1) and stencil combination hl % 4;
+// the minimum over a neighbour's four lanes is fouds1/fouds2's result. On
+// return every lane of the half holds tn[4] and cd[4] (cd 1: a neighbour on
+// the grid that is not accepted).
 template <class TT>
-__device__ void march(WarpStateT<TT> &w, const Grid2 &g, const SlowT<TT> *SL, int sld, int fom, int urg, int vnl,
-                      int vnr, int vnt, int vnb, const Fx &fx, Trace *tr = nullptr) {
-  const int lane = threadIdx.x & 31;
-  // lanes 16-31 work on neighbour q = (lane - 16) / 4 of the accepted node,
-  // in the reference's order (x-1, x+1, z-1, z+1), stencil combination lane % 4
-  const int q = (lane >> 2) & 3, cmb = lane & 3;
+__device__ __forceinline__ void update_neighbours(const WarpStateT<TT> &w, const Grid2 &g, const SlowT<TT> *SL,
+                                                  int sld, int fom, const Fx &fx, const UpdConst<TT> &K, int lane,
+                                                  int cur, TT tcur, TT *tn, int *cd) {
+  const int hl = lane & 15, hbase = lane & 16;
+  const unsigned hmask = 0xFFFFu << hbase;
+  const int q = hl >> 2, cmb = hl & 3;
   const int dqx = q == 0 ? -1 : (q == 1 ? 1 : 0), dqz = q == 2 ? -1 : (q == 3 ? 1 : 0);
-  // slowness of this lane's neighbour of the node predicted to be accepted
-  // next, loaded while lane 0 sifts (a global-memory load off the critical path)
-  int pred = -1;
-  SlowT<TT> sl_pred = SlowT<TT>();
+  const int iz = (cur & 255) + 1, ix = (cur >> 8) + 1;
+  const int curl = lin(g, iz, ix);
+  const int nx_ = ix + dqx, nz_ = iz + dqz;
+  const bool valid = nx_ >= 1 && nx_ <= g.nnx && nz_ >= 1 && nz_ <= g.nnz;
+  bool open = false, have = false;
+  TT cand = time_inf(TT());
+  if (valid) {
+    open = w.S[lin(g, nz_, nx_)] != 0;
+    Stencil<TT> sc;
+    if (open && combo_stencil(w, g, nz_, nx_, cmb, fom, curl, tcur, sc)) {
+      have = true;
+      cand = combo_time(w, g, sc, SL[(nz_ - 1) + (size_t)sld * (nx_ - 1)], fom, fx, K);
+    }
+  }
+  const unsigned hb = __ballot_sync(hmask, have);
+#pragma unroll
+  for (int m = 1; m <= 2; m <<= 1) {
+    const TT o = shfl_xor_time(hmask, cand, m);
+    if (tlt(o, cand)) cand = o;
+  }
+  // a node with no usable combination gets 0, the reference's initial travm
+  if (((hb >> (lane & ~3)) & 0xFu) == 0u) cand = TT();
+  const int code = (valid && open) ? 1 : 0;
+#pragma unroll
+  for (int k = 0; k < 4; ++k) {
+    cd[k] = __shfl_sync(hmask, code, hbase + 4 * k);
+    tn[k] = shfl_time(hmask, cand, hbase + 4 * k);
+  }
+}
+
+// march (fm2d_ttime.f90:137-237) for this thread's solve (state w, mailbox
+// mb; active false without a solve), called by all threads of both warps of
+// the pair. Only the halves with marches set (both with two solves per pair,
+// the first with one) work on the solve. urg == 1 adds the refined-box exit
+// test; vnr/vnb are compared with the current (refined) grid size exactly as
+// the reference's module variables are at that point. Returns the end flag
+// (2: heap overflow) to every thread of an active solve.
+template <class TT>
+__device__ int march(WarpStateT<TT> &w, Mailbox<TT> *mb, bool active, bool marches, const Grid2 &g,
+                     const SlowT<TT> *SL, int sld, int fom, int urg, int vnl, int vnr, int vnt, int vnb, const Fx &fx,
+                     int bar1, int bar2, Trace *tr) {
+  const int t64 = threadIdx.x & 63, lane = t64 & 31, hbase = lane & 16;
+  const bool leader = (lane & 15) == 0;
   UpdConst<TT> K;
   K.init(g);
-  if constexpr (std::is_same<TT, double>::value) {
-    build_case_tab(w.tab, g, lane);
-    __syncwarp();
-  }
-  for (;;) {
-    int pk = -1;   // accepted node ((ix-1) << 8) | (iz-1), or -1 to stop
-    if (lane == 0 && w.ntr > 0 && !w.overflow) {
-      const int top = w.H[1];
-      const int iz = (top & 255) + 1, ix = (top >> 8) + 1;
-      bool go = true;
-      if (urg == 1) {
-        int swrg = 0;
-        if (ix == 1 && vnl != 1) swrg = 1;
-        if (ix == g.nnx && vnr != g.nnx) swrg = 1;
-        if (iz == 1 && vnt != 1) swrg = 1;
-        if (iz == g.nnz && vnb != g.nnz) swrg = 1;
-        if (swrg) { w.S[lin(g, iz, ix)] = 0; go = false; }
-      }
-      if (go) {
-        if (tr && tr->n < tr->max) {
-          tr->ti[3 * tr->n] = urg; tr->ti[3 * tr->n + 1] = lin(g, iz, ix); tr->ti[3 * tr->n + 2] = w.ntr;
-          tr->tt[tr->n] = to_double(w.T[lin(g, iz, ix)], fx); tr->n++;
+  bool live = active && marches;
+  if (t64 < 32) {
+    // ---- heap warp: lanes 0 and 16 hold the solves' heaps
+    for (;;) {
+      if (leader && live) {
+        int st = 0, cur = -1;
+        if (w.overflow) {
+          st = 2;
+        } else if (w.ntr == 0) {
+          st = 1;
+        } else {
+          const int top = w.H[1];
+          const int iz = (top & 255) + 1, ix = (top >> 8) + 1;
+          int swrg = 0;
+          if (urg == 1) {
+            if (ix == 1 && vnl != 1) swrg = 1;
+            if (ix == g.nnx && vnr != g.nnx) swrg = 1;
+            if (iz == 1 && vnt != 1) swrg = 1;
+            if (iz == g.nnz && vnb != g.nnz) swrg = 1;
+          }
+          if (!swrg && tr && tr->n < tr->max) {
+            tr->ti[3 * tr->n] = urg; tr->ti[3 * tr->n + 1] = lin(g, iz, ix); tr->ti[3 * tr->n + 2] = w.ntr;
+            tr->tt[tr->n] = to_double(w.T[lin(g, iz, ix)], fx); tr->n++;
+          }
+          w.S[lin(g, iz, ix)] = 0;
+          if (swrg) {
+            st = 1;
+          } else {
+            downtree(w);
+            cur = top;
+          }
         }
-        w.S[lin(g, iz, ix)] = 0;
-        downtree(w);
-        pk = top;
+        const int root = (st == 0 && w.ntr > 0) ? (int)w.H[1] : -1;
+        mb->cur = cur;
+        mb->root = root;
+        mb->rkey = root >= 0 ? w.T[plin(w, root)] : TT();
+        mb->stop = st;
+        live = st == 0;
       }
-    }
-    pk = __shfl_sync(0xffffffffu, pk, 0);
-    if (pk < 0) break;
-    __syncwarp();
-    const int iz = (pk & 255) + 1, ix = (pk >> 8) + 1;
-    // New times are computed in registers (each reads only accepted nodes),
-    // then written and sifted by lane 0 one neighbour at a time in the
-    // reference's order: a sift compares against the other close nodes'
-    // current times, so the writes must not run ahead of the sifts.
-    int st = 0;
-    bool valid = false, have = false;
-    TT cand = time_inf(TT());
-    if (lane >= 16) {
-      const int nx_ = ix + dqx, nz_ = iz + dqz;
-      valid = nx_ >= 1 && nx_ <= g.nnx && nz_ >= 1 && nz_ <= g.nnz;
-      if (valid) {
-        const int ln = lin(g, nz_, nx_);
-        st = w.S[ln];
-        Stencil sc;
-        if (st != 0 && combo_stencil(w, g, nz_, nx_, cmb, fom, sc)) {
-          have = true;
-          cand = combo_time(w, g, sc, pk == pred ? sl_pred : SL[(nz_ - 1) + (size_t)sld * (nx_ - 1)], fom, fx, K);
-        }
-      }
-    }
-    const unsigned hb = __ballot_sync(0xffffffffu, have);
+      live = __shfl_sync(0xffffffffu, live, hbase);
+      const bool any = __any_sync(0xffffffffu, live);
+      pair_arrive(bar1);
+      if (!any) break;
+      pair_sync(bar2);
+      if (leader && live) {
+        const int cur = mb->cur;
+        const int iz = (cur & 255) + 1, ix = (cur >> 8) + 1;
+        const int qz[4] = {iz, iz, iz - 1, iz + 1}, qx[4] = {ix - 1, ix + 1, ix, ix};
 #pragma unroll
-    for (int m = 1; m <= 2; m <<= 1) {
-      const TT o = shfl_xor_time(cand, m);
-      if (tlt(o, cand)) cand = o;
+        for (int k = 0; k < 4; ++k) {
+          if (mb->cd[k] == 0) continue;
+          const TT t = mb->tn[k];
+          const int l = lin(g, qz[k], qx[k]);
+          w.T[l] = t;
+          if (w.S[l] == -1) addtree(w, g, qz[k], qx[k], t);
+          else updtree(w, g, qz[k], qx[k], t);
+        }
+      }
+      __syncwarp();
     }
-    // a node with no usable combination gets 0, the reference's initial travm
-    if (((hb >> (lane & ~3)) & 0xFu) == 0u) cand = TT();
-    const int code = valid ? (st == -1 ? 1 : (st > 0 ? 2 : 0)) : 0;
-    int cd[4];
+  } else {
+    // ---- update warp: lanes 0-15 and 16-31 evaluate the solves' updates
+    if constexpr (std::is_same<TT, double>::value) {
+      if (live) build_case_tab(w.tab, g, lane & 15);
+      __syncwarp();
+    }
+    int pred = -1;
+    TT tpred = TT();
     TT tn[4];
+    int cd[4];
+    for (;;) {
+      // speculative: the predicted node's neighbours, while the heap warp
+      // sifts the previous node's neighbours and pops
+      if (live && pred >= 0) update_neighbours(w, g, SL, sld, fom, fx, K, lane, pred, tpred, tn, cd);
+      pair_sync(bar1);
+      int st = 1, cur = -1, root = -1;
+      TT rkey = TT();
+      if (live) { st = mb->stop; cur = mb->cur; root = mb->root; rkey = mb->rkey; }
+      if (st != 0) live = false;
+      if (!__any_sync(0xffffffffu, live)) break;
+      if (live && cur != pred) update_neighbours(w, g, SL, sld, fom, fx, K, lane, cur, w.T[plin(w, cur)], tn, cd);
+      pred = -1;
+      if (live) {
+        if (leader) {
 #pragma unroll
-    for (int k = 0; k < 4; ++k) {
-      cd[k] = __shfl_sync(0xffffffffu, code, 16 + 4 * k);
-      tn[k] = shfl_time(cand, 16 + 4 * k);
-    }
-    const int qz[4] = {iz, iz, iz - 1, iz + 1}, qx[4] = {ix - 1, ix + 1, ix, ix};
-    // the next root: the current one unless a sifted neighbour is strictly
-    // earlier (the sifts below move such a node to the top)
-    int nxt = -1;
-    if (lane == 0) {
-      int r = w.ntr > 0 ? w.H[1] : -1;
-      TT rk = r >= 0 ? w.T[plin(w, r)] : TT();
+          for (int k = 0; k < 4; ++k) { mb->tn[k] = tn[k]; mb->cd[k] = cd[k]; }
+        }
+        // the next root: the root left by downtree unless a sifted neighbour
+        // is strictly earlier (or the root itself is updated)
+        const int iz = (cur & 255) + 1, ix = (cur >> 8) + 1;
+        const int qz[4] = {iz, iz, iz - 1, iz + 1}, qx[4] = {ix - 1, ix + 1, ix, ix};
+        int r = root;
+        TT rk = rkey;
 #pragma unroll
-      for (int k = 0; k < 4; ++k) {
-        if (cd[k] == 0) continue;
-        const int pq = (int)pack(qz[k], qx[k]);
-        if (r < 0 || pq == r || tlt(tn[k], rk)) { r = pq; rk = tn[k]; }
+        for (int k = 0; k < 4; ++k) {
+          if (cd[k] == 0) continue;
+          const int pq = (int)pack(qz[k], qx[k]);
+          if (r < 0 || pq == r || tlt(tn[k], rk)) { r = pq; rk = tn[k]; }
+        }
+        pred = r; tpred = rk;
       }
-      nxt = r;
+      __syncwarp();
+      pair_arrive(bar2);
     }
-    nxt = __shfl_sync(0xffffffffu, nxt, 0);
-    if (lane >= 16 && nxt >= 0) {
-      const int nx_ = (nxt >> 8) + 1 + dqx, nz_ = (nxt & 255) + 1 + dqz;
-      pred = nxt;
-      if (nx_ >= 1 && nx_ <= g.nnx && nz_ >= 1 && nz_ <= g.nnz) sl_pred = SL[(nz_ - 1) + (size_t)sld * (nx_ - 1)];
-    }
-    __syncwarp();
-    if (lane == 0) {
-#pragma unroll
-      for (int k = 0; k < 4; ++k) {
-        if (cd[k] == 0) continue;
-        w.T[lin(g, qz[k], qx[k])] = tn[k];
-        if (cd[k] == 1) addtree(w, g, qz[k], qx[k], tn[k]);
-        else updtree(w, g, qz[k], qx[k], tn[k]);
-      }
-    }
-    __syncwarp();
   }
-  __syncwarp();
+  pair_sync(bar2);   // both warps: the solve's times and states are complete
+  return active ? mb->stop : 1;
 }
 
 // Source initialisation of travel (fm2d_ttime.f90:95-127), lane 0. vel(iz, ix)
@@ -936,56 +1032,63 @@ __device__ __forceinline__ WarpStateT<TT> warp_state(unsigned char *base, int no
 // First pass: every solve with a heap of REFINED_HEAP_CAP entries, solves
 // whose band outgrows it listed in job.ovf_list. Overflow pass (redo = 1): the
 // listed solves again with a heap as large as the box.
-template <class TT>
-__global__ void __launch_bounds__(32 * WARPS_PER_BLOCK_MAX)
-fm2d_refined_kernel(Fm2dJob job, int warp_bytes, int heap_cap, int redo) {
+template <class TT, int SPW>
+__global__ void __launch_bounds__(64 * PAIRS_MAX)
+fm2d_refined_kernel(Fm2dJob job, int solve_bytes, int heap_cap, int redo) {
   extern __shared__ __align__(16) unsigned char smem[];
-  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  int solve = blockIdx.x * (blockDim.x >> 5) + warp;
-  if (redo) {
-    if (solve >= *job.ovf_count) return;
-    solve = job.ovf_list[solve];
-  }
-  if (solve >= job.nsolve) return;
+  const int pair = threadIdx.x >> 6, t64 = threadIdx.x & 63, lane = t64 & 31;
+  const int slot = SPW == 2 ? (lane >> 4) : 0;                          // this thread's solve in the pair
+  const int sub = SPW == 2 ? ((t64 >> 5) << 4) + (lane & 15) : t64;   // thread index within the solve
+  constexpr int NSUB = 64 / SPW;
+  const bool leader = t64 < 32 && (lane & 15) == 0 && (SPW == 2 || lane == 0);
+  const int bar1 = 1 + 2 * pair, bar2 = 2 + 2 * pair;
+  int solve = (blockIdx.x * (blockDim.x >> 6) + pair) * SPW + slot;
+  if (redo) solve = solve < *job.ovf_count ? job.ovf_list[solve] : job.nsolve;
   SolveGeom sg;
-  if (!solve_geom(job, solve, sg)) return;   // reported by the coarse stage
-  WarpStateT<TT> w = warp_state<TT>(smem + (size_t)warp * warp_bytes, job.nref_max, heap_cap);
+  const bool active = solve < job.nsolve && solve_geom(job, solve, sg);   // geometry errors: coarse stage
+  if (!__any_sync(0xffffffffu, active)) return;   // the same for both warps of the pair
+  unsigned char *base = smem + ((size_t)pair * SPW + slot) * solve_bytes;
+  WarpStateT<TT> w = warp_state<TT>(base, job.nref_max, heap_cap);
+  Mailbox<TT> *mb = reinterpret_cast<Mailbox<TT> *>(base + solve_bytes - MAILBOX_BYTES);
   const Fx fx = time_scale<TT>(job);
   const int sgdl = job.sgdl;
   const int vnl = sg.vnl, vnr = sg.vnr, vnt = sg.vnt, vnb = sg.vnb;
   const Grid2 &gc = sg.gc;
-  const int nrnx = (vnr - vnl) * sgdl + 1, nrnz = (vnb - vnt) * sgdl + 1;
+  const int nrnx = active ? (vnr - vnl) * sgdl + 1 : 0, nrnz = active ? (vnb - vnt) * sgdl + 1 : 0;
   Grid2 gr{nrnx, nrnz, nrnz, gc.gox + gc.dnx * (double)(vnl - 1), gc.goz + gc.dnz * (double)(vnt - 1),
            job.dvxd / (double)(job.gdx * sgdl), job.dvzd / (double)(job.gdz * sgdl)};
   Trace trace{job.trace_i, job.trace_t, job.trace_max / 2, 0};
-  Trace *tr = (job.trace_i && solve == job.trace_solve && lane == 0) ? &trace : nullptr;
+  Trace *tr = (job.trace_i && active && solve == job.trace_solve && leader) ? &trace : nullptr;
   // the box's nodes in the map's refined slowness field (refine_slowness
   // kernel): refined node (iz, ix) of the box is node (iz + (vnt-1) sgdl,
   // ix + (vnl-1) sgdl) of the whole refined grid, and every node of the box
   // lies inside the box's coarse cells, where bsplrefine gives the same
   // velocity from either numbering
   const int ldv = job.nvz + 2;
-  const RefineBox rb{job.velv + (size_t)sg.map * (job.nvx + 2) * ldv, ldv, (vnl - 1) * sgdl + 1,
+  const RefineBox rb{job.velv + (size_t)(active ? sg.map : 0) * (job.nvx + 2) * ldv, ldv, (vnl - 1) * sgdl + 1,
                      (vnt - 1) * sgdl + 1, job.gdx * sgdl, job.gdz * sgdl, vnl, vnr, vnt, vnb};
   const int nrgz = (job.nvz - 1) * job.gdz * sgdl + 1;
-  const SlowT<TT> *SLr = reinterpret_cast<const SlowT<TT> *>(job.sref) + (size_t)sg.map * job.nref_map +
-                         (size_t)(vnl - 1) * sgdl * nrgz + (size_t)(vnt - 1) * sgdl;
-  for (int q = lane; q < nrnx * nrnz; q += 32) w.S[q] = -1;
+  const SlowT<TT> *SLr = active ? reinterpret_cast<const SlowT<TT> *>(job.sref) + (size_t)sg.map * job.nref_map +
+                                      (size_t)(vnl - 1) * sgdl * nrgz + (size_t)(vnt - 1) * sgdl
+                                : nullptr;
+  for (int q = sub; q < nrnx * nrnz; q += NSUB) w.S[q] = -1;
   w.ld = gr.ld;
-  __syncwarp();
-  if (lane == 0)
+  pair_sync(bar1);
+  if (leader && active)
     init_source(w, gr, [&](int zz, int xx) { return refined_velocity(job, rb, zz, xx); }, sg.x, sg.z, fx);
-  __syncwarp();
-  march(w, gr, SLr, nrgz, job.fom, 1, vnl, vnr, vnt, vnb, fx, tr);
-  if (__shfl_sync(0xffffffffu, (int)w.overflow, 0)) {
-    if (lane == 0) job.ovf_list[atomicAdd(job.ovf_count, 1)] = solve;
+  pair_sync(bar1);
+  const int end = march(w, mb, active, SPW == 2 || lane < 16, gr, SLr, nrgz, job.fom, 1, vnl, vnr, vnt, vnb, fx,
+                        bar1, bar2, tr);
+  if (!active) return;
+  if (end == 2) {
+    if (leader) job.ovf_list[atomicAdd(job.ovf_count, 1)] = solve;
     return;
   }
   // the refined nodes that map onto coarse nodes (fm2dray_cartesian.f90:365-383)
   const int mx = (nrnx - 1) / sgdl + 1, mz = (nrnz - 1) / sgdl + 1;   // = vnr-vnl+1, vnb-vnt+1
   double *tmpT = job.map_tmp_t + (size_t)solve * job.map_tmp_max;
   short *tmpS = job.map_tmp_s + (size_t)solve * job.map_tmp_max;
-  for (int q = lane; q < mx * mz; q += 32) {
+  for (int q = sub; q < mx * mz; q += NSUB) {
     int a = q % mz, b = q / mz;
     int k = a * sgdl + 1, l = b * sgdl + 1;
     int r = lin(gr, k, l);
@@ -997,7 +1100,7 @@ fm2d_refined_kernel(Fm2dJob job, int warp_bytes, int heap_cap, int redo) {
     // uninitialised memory in the reference; 0 here)
     double *rt = job.ref_t + (size_t)solve * job.nref_max;
     short *rs = job.ref_s + (size_t)solve * job.nref_max;
-    for (int q = lane; q < nrnx * nrnz; q += 32) {
+    for (int q = sub; q < nrnx * nrnz; q += NSUB) {
       const short st = w.S[q];
       rs[q] = st;
       rt[q] = st == -1 ? 0.0 : to_double(w.T[q], fx);
@@ -1022,7 +1125,7 @@ __device__ __forceinline__ int floor_idx(double v) { return isnan(v) ? INT_MIN :
 // stores a one-point ray).
 template <class TT>
 __device__ void trace_rays(const Fm2dJob &job, const WarpStateT<TT> &w, const Fx &fx, const SolveGeom &sg, int solve,
-                           int lane) {
+                           int sub, int nsub) {
   const int map = sg.map, src = sg.src;
   const Grid2 &gc = sg.gc;
   const int nnx = gc.nnx, nnz = gc.nnz;
@@ -1053,7 +1156,7 @@ __device__ void trace_rays(const Fm2dJob &job, const WarpStateT<TT> &w, const Fx
   dpl = 0.5 * dpl;
   const int *srs = job.srs + (size_t)(map % job.srs_nmaps) * job.nsrc * job.nrc + (size_t)src * job.nrc;
   const size_t o0 = ((size_t)map * job.nsrc + src) * job.nrc;
-  for (int r = lane; r < job.nrc; r += 32) {
+  for (int r = sub; r < job.nrc; r += nsub) {
     if (srs[r] == 0) continue;
     const double rcx = job.rcx[r], rcz = job.rcz[r];
     int ipx = floor_idx((rcx - gox) / dnx) + 1;
@@ -1153,23 +1256,31 @@ __device__ void trace_rays(const Fm2dJob &job, const WarpStateT<TT> &w, const Fx
 // narrow band repaired and re-heaped, travel with urg = 2 (or, without
 // refinement, the point source and travel with urg = 0); then the optional
 // time field and srtimes.
-template <class TT>
-__global__ void __launch_bounds__(32 * WARPS_PER_BLOCK_MAX)
-fm2d_coarse_kernel(Fm2dJob job, int warp_bytes) {
+template <class TT, int SPW>
+__global__ void __launch_bounds__(64 * PAIRS_MAX)
+fm2d_coarse_kernel(Fm2dJob job, int solve_bytes) {
   extern __shared__ __align__(16) unsigned char smem[];
-  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  const int solve = blockIdx.x * (blockDim.x >> 5) + warp;
-  if (solve >= job.nsolve) return;
+  const int pair = threadIdx.x >> 6, t64 = threadIdx.x & 63, lane = t64 & 31;
+  const int slot = SPW == 2 ? (lane >> 4) : 0;                          // this thread's solve in the pair
+  const int sub = SPW == 2 ? ((t64 >> 5) << 4) + (lane & 15) : t64;   // thread index within the solve
+  constexpr int NSUB = 64 / SPW;
+  const bool leader = t64 < 32 && (lane & 15) == 0 && (SPW == 2 || lane == 0);
+  const int bar1 = 1 + 2 * pair, bar2 = 2 + 2 * pair;
+  const int solve = (blockIdx.x * (blockDim.x >> 6) + pair) * SPW + slot;
   SolveGeom sg;
-  if (!solve_geom(job, solve, sg)) {
-    if (lane == 0) atomicExch(job.status, MCT_ERR_OUTSIDE);
-    return;
+  bool active = solve < job.nsolve;
+  if (active && !solve_geom(job, solve, sg)) {
+    if (leader) atomicExch(job.status, MCT_ERR_OUTSIDE);
+    active = false;
   }
+  if (!__any_sync(0xffffffffu, active)) return;   // the same for both warps of the pair
   const Grid2 gc = sg.gc;
-  const int nnx = gc.nnx, nnz = gc.nnz;
-  WarpStateT<TT> w = warp_state<TT>(smem + (size_t)warp * warp_bytes, nnx * nnz, nnx * nnz);
+  const int nnx = active ? gc.nnx : 0, nnz = active ? gc.nnz : 0;
+  unsigned char *base = smem + ((size_t)pair * SPW + slot) * solve_bytes;
+  WarpStateT<TT> w = warp_state<TT>(base, nnx * nnz, nnx * nnz);
+  Mailbox<TT> *mb = reinterpret_cast<Mailbox<TT> *>(base + solve_bytes - MAILBOX_BYTES);
   const Fx fx = time_scale<TT>(job);
-  const int map = sg.map, src = sg.src;
+  const int map = active ? sg.map : 0, src = active ? sg.src : 0;
   const double x = sg.x, z = sg.z;
   const int sgdl = job.sgdl;
   const int vnl = sg.vnl, vnr = sg.vnr, vnt = sg.vnt, vnb = sg.vnb;
@@ -1177,25 +1288,28 @@ fm2d_coarse_kernel(Fm2dJob job, int warp_bytes) {
   const SlowT<TT> *SLc = reinterpret_cast<const SlowT<TT> *>(job.slon) + (size_t)map * nnx * nnz;
   Trace trace{job.trace_i ? job.trace_i + 3 * (job.trace_max / 2) : nullptr,
               job.trace_t ? job.trace_t + job.trace_max / 2 : nullptr, job.trace_max / 2, 0};
-  Trace *tr = (job.trace_i && solve == job.trace_solve && lane == 0) ? &trace : nullptr;
-  w.ld = gc.ld;
-  for (int q = lane; q < nnx * nnz; q += 32) w.S[q] = -1;
-  __syncwarp();
+  Trace *tr = (job.trace_i && active && solve == job.trace_solve && leader) ? &trace : nullptr;
+  const bool marches = SPW == 2 || lane < 16;
+  w.ld = active ? gc.ld : 1;
+  for (int q = sub; q < nnx * nnz; q += NSUB) w.S[q] = -1;
+  pair_sync(bar1);
   if (job.asgr == 1) {
-    const int nrnx = (vnr - vnl) * sgdl + 1, nrnz = (vnb - vnt) * sgdl + 1;
-    const int mx = (nrnx - 1) / sgdl + 1, mz = (nrnz - 1) / sgdl + 1;
-    const double *tmpT = job.map_tmp_t + (size_t)solve * job.map_tmp_max;
-    const short *tmpS = job.map_tmp_s + (size_t)solve * job.map_tmp_max;
-    for (int q = lane; q < mx * mz; q += 32) {
-      int a = q % mz, b = q / mz;
-      int c = lin(gc, vnt + a, vnl + b);
-      short s = tmpS[q];
-      w.S[c] = s;
-      if (s >= 0) w.T[c] = bit_load<TT>(tmpT[q]);
+    if (active) {
+      const int nrnx = (vnr - vnl) * sgdl + 1, nrnz = (vnb - vnt) * sgdl + 1;
+      const int mx = (nrnx - 1) / sgdl + 1, mz = (nrnz - 1) / sgdl + 1;
+      const double *tmpT = job.map_tmp_t + (size_t)solve * job.map_tmp_max;
+      const short *tmpS = job.map_tmp_s + (size_t)solve * job.map_tmp_max;
+      for (int q = sub; q < mx * mz; q += NSUB) {
+        int a = q % mz, b = q / mz;
+        int c = lin(gc, vnt + a, vnl + b);
+        short s = tmpS[q];
+        w.S[c] = s;
+        if (s >= 0) w.T[c] = bit_load<TT>(tmpT[q]);
+      }
     }
-    __syncwarp();
+    pair_sync(bar1);
     // narrow band repair (fm2dray_cartesian.f90:384-405); order-independent
-    for (int q = lane; q < nnx * nnz; q += 32) {
+    for (int q = sub; q < nnx * nnz; q += NSUB) {
       int l = q % nnz + 1, k = q / nnz + 1;
       if (w.S[q] == 0) {
         bool far = (l - 1 >= 1 && w.S[lin(gc, l - 1, k)] == -1) || (l + 1 <= nnz && w.S[lin(gc, l + 1, k)] == -1) ||
@@ -1203,30 +1317,31 @@ fm2d_coarse_kernel(Fm2dJob job, int warp_bytes) {
         if (far) w.S[q] = 1;
       }
     }
-    __syncwarp();
+    pair_sync(bar1);
     // travel(urg=2): heap from all nodes marked close, i outer, j inner
-    if (lane == 0) {
+    if (leader && active) {
       w.ntr = 0;
       for (int i = 1; i <= nnx; ++i)
         for (int j = 1; j <= nnz; ++j)
           if (w.S[lin(gc, j, i)] > 0) addtree(w, gc, j, i);
     }
-    __syncwarp();
-    march(w, gc, SLc, nnz, job.fom, 2, vnl, vnr, vnt, vnb, fx, tr);
+    pair_sync(bar1);
+    march(w, mb, active, marches, gc, SLc, nnz, job.fom, 2, vnl, vnr, vnt, vnb, fx, bar1, bar2, tr);
   } else {
-    if (lane == 0) init_source(w, gc, [&](int zz, int xx) { return Vc[lin(gc, zz, xx)]; }, x, z, fx);
-    __syncwarp();
-    march(w, gc, SLc, nnz, job.fom, 0, vnl, vnr, vnt, vnb, fx, tr);
+    if (leader && active) init_source(w, gc, [&](int zz, int xx) { return Vc[lin(gc, zz, xx)]; }, x, z, fx);
+    pair_sync(bar1);
+    march(w, mb, active, marches, gc, SLc, nnz, job.fom, 0, vnl, vnr, vnt, vnb, fx, bar1, bar2, tr);
   }
+  if (!active) return;
   // optional travel-time field
   if (job.tfield) {
     double *tf = job.tfield + ((size_t)map * job.nsrc + src) * nnx * nnz;
-    for (int q = lane; q < nnx * nnz; q += 32) tf[q] = to_double(w.T[q], fx);
+    for (int q = sub; q < nnx * nnz; q += NSUB) tf[q] = to_double(w.T[q], fx);
   }
   // srtimes (fm2dray_cartesian.f90:682-797), one receiver per lane
   const int *srs = job.srs + (size_t)(map % job.srs_nmaps) * job.nsrc * job.nrc + (size_t)src * job.nrc;
   double *tt = job.ttime + ((size_t)map * job.nsrc + src) * job.nrc;
-  for (int r = lane; r < job.nrc; r += 32) {
+  for (int r = sub; r < job.nrc; r += NSUB) {
     if (srs[r] == 0) continue;
     const double rx = job.rcx[r], rz = job.rcz[r];
     int irx = (int)floor((rx - gc.gox) / gc.dnx) + 1;
@@ -1275,32 +1390,32 @@ fm2d_coarse_kernel(Fm2dJob job, int warp_bytes) {
     }
     tt[r] = trr;
   }
-  if (job.rays) trace_rays(job, w, fx, sg, solve, lane);
+  if (job.rays) trace_rays(job, w, fx, sg, solve, sub, NSUB);
 }
 
 }  // namespace
 
 namespace {
-// Warps (solves) per block for kernel k with a per-warp shared-memory
-// footprint of wb bytes: the block size that keeps the most solves resident
-// per SM (shared memory, registers and the block limit all counted by the
-// occupancy calculator). Remembered per (kernel, footprint).
+// Warp pairs per block for kernel k with pair_bytes of shared memory per
+// pair: the block size that keeps the most pairs resident per SM (shared
+// memory, registers and the block limit all counted by the occupancy
+// calculator). Remembered per (kernel, footprint).
 template <class K>
-int warps_for(K k, int wb) {
+int pairs_for(K k, int pair_bytes) {
   static std::mutex mu;
   static std::vector<std::pair<std::pair<const void *, int>, int>> memo;
   std::lock_guard<std::mutex> lk(mu);
   for (auto &m : memo)
-    if (m.first.first == (const void *)k && m.first.second == wb) return m.second;
-  int best = 0, best_warps = 0;
-  for (int wpb = 1; wpb <= WARPS_PER_BLOCK_MAX; ++wpb) {
-    const size_t bytes = (size_t)wpb * wb;
+    if (m.first.first == (const void *)k && m.first.second == pair_bytes) return m.second;
+  int best = 0, best_pairs = 0;
+  for (int ppb = 1; ppb <= PAIRS_MAX; ++ppb) {
+    const size_t bytes = (size_t)ppb * pair_bytes;
     if (bytes > 227 * 1024) break;
     int nb = 0;
-    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, k, 32 * wpb, bytes) != cudaSuccess) continue;
-    if (nb * wpb > best_warps) { best_warps = nb * wpb; best = wpb; }
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, k, 64 * ppb, bytes) != cudaSuccess) continue;
+    if (nb * ppb > best_pairs) { best_pairs = nb * ppb; best = ppb; }
   }
-  memo.push_back({{(const void *)k, wb}, best});
+  memo.push_back({{(const void *)k, pair_bytes}, best});
   return best;
 }
 }  // namespace
@@ -1315,6 +1430,24 @@ int g_ref_heap_cap = REFINED_HEAP_CAP;
 extern "C" int mct_debug_fm2d_heap_cap(int cap) {
   g_ref_heap_cap = cap < 4 ? REFINED_HEAP_CAP : cap;
   return MCT_OK;
+}
+
+namespace {
+// Solves per warp pair of the refined and coarse stages. One solve per pair
+// keeps five refined boxes resident per SM (two would share each FP64
+// instruction but fit only four); the coarse stage's ten resident solves
+// share their update warps in twos.
+int g_spw_refined = 1, g_spw_coarse = 2;
+}  // namespace
+
+// Diagnostics (not part of the public header): solves per warp pair (1 or 2)
+// of the refined and coarse stages; 0 keeps a setting. Returns the previous
+// settings as refined * 10 + coarse.
+extern "C" int mct_debug_fm2d_spw(int refined, int coarse) {
+  const int old = g_spw_refined * 10 + g_spw_coarse;
+  if (refined == 1 || refined == 2) g_spw_refined = refined;
+  if (coarse == 1 || coarse == 2) g_spw_coarse = coarse;
+  return old;
 }
 
 namespace {
@@ -1426,36 +1559,51 @@ int fm2d_plan(const Fm2dJob &job, Fm2dPlan *plan) {
 }
 
 namespace {
+template <class TT, int SPW>
+int launch_refined(const Fm2dJob &job, int solve_bytes, int heap_cap, int redo, cudaStream_t s) {
+  auto kern = fm2d_refined_kernel<TT, SPW>;
+  int rc = mct_smem_attr(kern, 227 * 1024);
+  if (rc) return rc;
+  const int ppb = pairs_for(kern, SPW * solve_bytes);
+  if (ppb < 1) return MCT_ERR_ARG;
+  const int per_block = ppb * SPW;
+  const int blocks = (job.nsolve + per_block - 1) / per_block;
+  kern<<<blocks, 64 * ppb, (size_t)per_block * solve_bytes, s>>>(job, solve_bytes, heap_cap, redo);
+  MCT_CUDA_TRY(cudaGetLastError());
+  return MCT_OK;
+}
+
+template <class TT, int SPW>
+int launch_coarse(const Fm2dJob &job, int solve_bytes, cudaStream_t s) {
+  auto kern = fm2d_coarse_kernel<TT, SPW>;
+  int rc = mct_smem_attr(kern, 227 * 1024);
+  if (rc) return rc;
+  const int ppb = pairs_for(kern, SPW * solve_bytes);
+  if (ppb < 1) return MCT_ERR_ARG;
+  const int per_block = ppb * SPW;
+  const int blocks = (job.nsolve + per_block - 1) / per_block;
+  kern<<<blocks, 64 * ppb, (size_t)per_block * solve_bytes, s>>>(job, solve_bytes);
+  MCT_CUDA_TRY(cudaGetLastError());
+  return MCT_OK;
+}
+
 template <class TT>
 int launch_solves(const Fm2dJob &job, const Fm2dPlan &plan, cudaStream_t s) {
-  int rc = mct_smem_attr(fm2d_refined_kernel<TT>, 227 * 1024);
-  if (!rc) rc = mct_smem_attr(fm2d_coarse_kernel<TT>, 227 * 1024);
-  if (rc) return rc;
+  int rc;
   if (job.asgr == 1) {
     if (!job.ovf_list || !job.ovf_count) return MCT_ERR_ARG;
     MCT_CUDA_TRY(cudaMemsetAsync(job.ovf_count, 0, sizeof(int), s));
-    int wpb = warps_for(fm2d_refined_kernel<TT>, plan.ref_warp_bytes);
-    if (wpb < 1) return MCT_ERR_ARG;
-    int blocks = (job.nsolve + wpb - 1) / wpb;
-    fm2d_refined_kernel<TT><<<blocks, 32 * wpb, (size_t)plan.ref_warp_bytes * wpb, s>>>(
-        job, plan.ref_warp_bytes, plan.ref_heap_cap, 0);
-    MCT_CUDA_TRY(cudaGetLastError());
+    rc = g_spw_refined == 2 ? launch_refined<TT, 2>(job, plan.ref_warp_bytes, plan.ref_heap_cap, 0, s)
+                            : launch_refined<TT, 1>(job, plan.ref_warp_bytes, plan.ref_heap_cap, 0, s);
+    if (rc) return rc;
     if (plan.ref_heap_cap < job.nref_max) {
-      // overflow pass: blocks beyond the device-side count exit at once
-      wpb = warps_for(fm2d_refined_kernel<TT>, plan.ref_full_warp_bytes);
-      if (wpb < 1) return MCT_ERR_ARG;
-      blocks = (job.nsolve + wpb - 1) / wpb;
-      fm2d_refined_kernel<TT><<<blocks, 32 * wpb, (size_t)plan.ref_full_warp_bytes * wpb, s>>>(
-          job, plan.ref_full_warp_bytes, job.nref_max, 1);
-      MCT_CUDA_TRY(cudaGetLastError());
+      // overflow pass: solves beyond the device-side count exit at once
+      rc = launch_refined<TT, 1>(job, plan.ref_full_warp_bytes, job.nref_max, 1, s);
+      if (rc) return rc;
     }
   }
-  const int wpb = warps_for(fm2d_coarse_kernel<TT>, plan.warp_bytes);
-  if (wpb < 1) return MCT_ERR_ARG;
-  const int blocks = (job.nsolve + wpb - 1) / wpb;
-  fm2d_coarse_kernel<TT><<<blocks, 32 * wpb, (size_t)plan.warp_bytes * wpb, s>>>(job, plan.warp_bytes);
-  MCT_CUDA_TRY(cudaGetLastError());
-  return MCT_OK;
+  return g_spw_coarse == 2 ? launch_coarse<TT, 2>(job, plan.warp_bytes, s)
+                           : launch_coarse<TT, 1>(job, plan.warp_bytes, s);
 }
 }  // namespace
 

@@ -26,6 +26,20 @@ template <class K> inline int mct_smem_attr(K *kernel, int bytes) {
   return mct_smem_attr_raw(reinterpret_cast<const void *>(kernel), bytes);
 }
 
+// Replaces a context's stream by a new non-blocking stream of the device's
+// highest priority (high != 0) or of normal priority, after the old stream's
+// work has finished.
+inline int mct_restream(cudaStream_t *stream, int high) {
+  int least = 0, greatest = 0;
+  MCT_CUDA_TRY(cudaDeviceGetStreamPriorityRange(&least, &greatest));
+  MCT_CUDA_TRY(cudaStreamSynchronize(*stream));
+  cudaStream_t s = nullptr;
+  MCT_CUDA_TRY(cudaStreamCreateWithPriority(&s, cudaStreamNonBlocking, high ? greatest : least));
+  cudaStreamDestroy(*stream);
+  *stream = s;
+  return MCT_OK;
+}
+
 // Grow-only device buffer (reused across synchronous drop-in calls).
 struct DevBuf {
   void *p = nullptr;

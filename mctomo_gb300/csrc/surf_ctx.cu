@@ -276,6 +276,12 @@ int mct_surf_device_bytes(const mct_grid *g, const mct_surf_settings *st, const 
   return surf_create(g, st, dat, nslots, ncell_max, nullptr, true, bytes);
 }
 
+int mct_surf_set_priority(mct_surf_ctx *c, int high) {
+  if (!c) return MCT_ERR_ARG;
+  if (c->pending) return MCT_ERR_ARG;
+  return mct_restream(&c->stream, high);
+}
+
 int mct_surf_destroy(mct_surf_ctx *c) {
   if (!c) return MCT_OK;
   cudaStreamSynchronize(c->stream);

@@ -511,6 +511,11 @@ int mct_tt2d_create(const mct_grid *g, const mct_tt2d_settings *st, const mct_tt
   return MCT_OK;
 }
 
+int mct_tt2d_set_priority(mct_tt2d_ctx *c, int high) {
+  if (!c) return MCT_ERR_ARG;
+  return mct_restream(&c->stream, high);
+}
+
 int mct_tt2d_destroy(mct_tt2d_ctx *c) {
   if (!c) return MCT_OK;
   cudaStreamSynchronize(c->stream);

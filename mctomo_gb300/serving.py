@@ -237,6 +237,9 @@ class TT2DBackend(_SlotBackend):
         super().__init__(nslots, new_model, propose, single)
         self.ctx, self.n1 = ctx, n1
 
+    def set_priority(self, high):
+        self.ctx.set_priority(high)
+
     def forward(self, slots, models):
         assert not self.single or len(models) == 1
         m, idx, nc, pts, par = self._pack(slots, models)
@@ -285,6 +288,9 @@ class SurfaceBackend(_SlotBackend):
         assert not self.single or len(models) == 1
         return self.ctx.forward(*self._args(slots, models))[:, 0]
 
+    def set_priority(self, high):
+        self.ctx.set_priority(high)
+
     def submit(self, slots, models):
         self.ctx.submit(*self._args(slots, models))
 
@@ -307,6 +313,10 @@ class JointBackend:
     def __init__(self, surface, body):
         self.s, self.b = surface, body
         self.nslots = min(surface.nslots, body.nslots)
+
+    def set_priority(self, high):
+        self.s.set_priority(high)
+        self.b.set_priority(high)
 
     def new_model(self, rng):
         return self.b.new_model(rng)

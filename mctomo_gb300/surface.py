@@ -80,6 +80,11 @@ class SurfaceLikelihood:
                                                        nslots, ncell_max, ctypes.byref(h)))
         self.h = h
 
+    def set_priority(self, high):
+        """Run this context's work on a high-priority (True) or a normal
+        stream of the device."""
+        check("mct_surf_set_priority", lib().mct_surf_set_priority(self.h, 1 if high else 0))
+
     def close(self):
         if self.h:
             lib().mct_surf_destroy(self.h)

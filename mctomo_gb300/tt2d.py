@@ -65,6 +65,11 @@ class TravelTime2DLikelihood:
                                                        nslots, ncell_max, ctypes.byref(h)))
         self.h = h
 
+    def set_priority(self, high):
+        """Run this context's work on a high-priority (True) or a normal
+        stream of the device."""
+        check("mct_tt2d_set_priority", lib().mct_tt2d_set_priority(self.h, 1 if high else 0))
+
     def close(self):
         if self.h:
             lib().mct_tt2d_destroy(self.h)
