@@ -78,6 +78,24 @@ module mctomo_gb300
     integer(c_int) :: ndtime
   end type mct_tt2d_data
 
+  type, bind(C) :: mct_mcmc_set
+    integer(c_int) :: ncell_min, ncell_max, kernel, datatype, sigdep, locate
+    real(c_double) :: xmin, xmax, ymin, ymax, zmin, zmax, vpmin, vpmax, vsmin, vsmax
+    real(c_double) :: sigma_vp, sigma_vs, sigma_vp2, sigma_vs2, pd, pd2
+    real(c_double) :: sigma_bn0, sigma_bn1, bn0_min, bn0_max, bn1_min, bn1_max
+    real(c_double) :: sigma_sn0, sigma_sn1, sn0_min, sn0_max, sn1_min, sn1_max
+  end type
+  type, bind(C) :: mct_mcmc_state
+    integer(c_int) :: ncells
+    type(c_ptr) :: points, parameters
+    integer(c_int) :: nbnoise, nsnoise
+    type(c_ptr) :: bnoise0, bnoise1, snoise0, snoise1
+  end type
+  type, bind(C) :: mct_mcmc_step
+    integer(c_int) :: ptype, index, valid
+    real(c_double) :: prob, random
+  end type
+
   interface
     type(c_ptr) function mct_version() bind(C, name="mct_version")
       import :: c_ptr
@@ -489,6 +507,20 @@ contains
       import :: c_int, c_ptr
       type(c_ptr), value :: ctx
       integer(c_int), value :: high
+    end function
+    integer(c_int) function mct_mcmc_propose(set, rng, iter, redo, state, step) bind(C, name="mct_mcmc_propose")
+      import :: c_int, c_ptr, mct_mcmc_set, mct_mcmc_state, mct_mcmc_step
+      type(mct_mcmc_set), intent(in) :: set
+      type(c_ptr), value :: rng
+      integer(c_int), value :: iter, redo
+      type(mct_mcmc_state), intent(inout) :: state
+      type(mct_mcmc_step), intent(inout) :: step
+    end function
+    integer(c_int) function mct_mcmc_accept(set, step, like_new, like_old) bind(C, name="mct_mcmc_accept")
+      import :: c_int, c_double, mct_mcmc_set, mct_mcmc_step
+      type(mct_mcmc_set), intent(in) :: set
+      type(mct_mcmc_step), intent(in) :: step
+      real(c_double), value :: like_new, like_old
     end function
   end interface
     p = mct_last_error()

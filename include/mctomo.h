@@ -545,6 +545,58 @@ double mct_rng_gasdev(mct_rng *rng);
 unsigned mct_rng_u32(mct_rng *rng);
 long long mct_rng_count(const mct_rng *rng);
 
+/* ------------------------------------------------------------------------
+ * Proposal steps and acceptance test of the reference's Metropolis-Hastings
+ * loop (src/mcmc_loc2.f90:72-687): proposeType2 (:1384-1432), cell_birth
+ * (:1521-1613), cell_death (:1615-1683), cell_move (:1685-1765), vel_change
+ * (:1767-1835), bsigma_change / ssigma_change (:1837-1903). Host only.
+ * mct_mcmc_set holds the T_MCMC_SET fields the steps read; mct_mcmc_state
+ * the chain's RTI%points / RTI%parameters (ncell_max x 3 each, one nucleus
+ * per row: x, y, z and vp, vs, rho) and noise levels. The cell containing a
+ * point (the reference's CGAL locate) is its nearest nucleus, the first in
+ * index order on an exact tie. Source relocation (type 7) is not restated.
+ * ---------------------------------------------------------------------- */
+typedef struct {
+  int ncell_min, ncell_max;
+  int kernel;      /* 0: birth/death values from the local cell (Gaussian), 1: from the prior */
+  int datatype;    /* 0 P, 1 P and S, 2 surface waves, 3 joint */
+  int sigdep;      /* noise levels are sampled */
+  int locate;      /* source locations are sampled (type 7, not supported) */
+  double xmin, xmax, ymin, ymax, zmin, zmax;
+  double vpmin, vpmax, vsmin, vsmax;
+  double sigma_vp, sigma_vs, sigma_vp2, sigma_vs2;   /* value steps (upper, deeper half) */
+  double pd, pd2;                                    /* move steps, percent of the extent */
+  double sigma_bn0, sigma_bn1, bn0_min, bn0_max, bn1_min, bn1_max;
+  double sigma_sn0, sigma_sn1, sn0_min, sn0_max, sn1_min, sn1_max;
+} mct_mcmc_set;
+
+typedef struct {
+  int ncells;
+  double *points;        /* [ncell_max][3] */
+  double *parameters;    /* [ncell_max][3] vp, vs, rho */
+  int nbnoise, nsnoise;  /* periods / phases of the body and surface noise levels */
+  double *bnoise0, *bnoise1, *snoise0, *snoise1;
+} mct_mcmc_state;
+
+typedef struct {
+  int ptype;       /* 1 birth, 2 death, 3 move, 4 value, 5 body noise, 6 surface noise */
+  int index;       /* the cell (1-based) or period changed */
+  int valid;       /* 0: the reference's lerr = .false. (the state is not a proposal) */
+  double prob;     /* the proposal's log-density term of the acceptance ratio */
+  double random;   /* the acceptance draw */
+} mct_mcmc_step;
+
+/* One proposal of iteration iter applied to state in place. Unless redo
+ * (the last proposal's model was invalid and the reference repeats it with
+ * the same type and acceptance draw), first draws step->random and the type
+ * with proposeType2. The caller keeps a copy of the state to restore on
+ * rejection, as the reference does. */
+int mct_mcmc_propose(const mct_mcmc_set *set, mct_rng *rng, int iter, int redo, mct_mcmc_state *state,
+                     mct_mcmc_step *step);
+/* The acceptance test of the step given the proposal's -log L (like_new)
+ * and the current one (like_old): 1 accept, 0 reject. */
+int mct_mcmc_accept(const mct_mcmc_set *set, const mct_mcmc_step *step, double like_new, double like_old);
+
 #ifdef __cplusplus
 }
 #endif

@@ -64,6 +64,8 @@ SIGNATURES = {
     "mct_rng_gasdev": (D, [P]),
     "mct_rng_u32": (ctypes.c_uint, [P]),
     "mct_rng_count": (ctypes.c_longlong, [P]),
+    "mct_mcmc_propose": (I, [P, P, I, I, P, P]),
+    "mct_mcmc_accept": (I, [P, P, D, D]),
     "mct_surf_create": (I, [P, P, P, I, I, P]),
     "mct_surf_destroy": (I, [P]),
     "mct_surf_forward": (I, [P, I, P, P, P, P, P, P, P]),

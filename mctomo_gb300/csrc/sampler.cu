@@ -1,7 +1,8 @@
 // Host side of the reversible-jump sampler: the reference's random number
-// stream (src/mt19937.f90), so that a C or Fortran host can drive the GPU
-// likelihood with the reference's own sequence of random draws. Host code
-// only (no kernels).
+// stream (src/mt19937.f90) and its Metropolis-Hastings proposal steps and
+// acceptance test (src/mcmc_loc2.f90), so that a C or Fortran host can drive
+// the GPU likelihood with the reference's own sequence of random draws and
+// moves. Host code only (no kernels).
 //
 // MT19937 (M. Matsumoto and T. Nishimura, "Mersenne Twister: a
 // 623-dimensionally equidistributed uniform pseudo-random number generator",
@@ -101,5 +102,237 @@ unsigned mct_rng_u32(mct_rng *r) {
 }
 
 long long mct_rng_count(const mct_rng *r) { return r ? r->count : -1; }
+
+}  // extern "C"
+
+// ---------------------------------------------------------------------------
+// Proposal steps of the reference's MCMC loop (src/mcmc_loc2.f90:72-687).
+// The Voronoi model is held as RTI%points / RTI%parameters are; the CGAL
+// triangulation the reference keeps beside them only serves to find the cell
+// containing a point (cgal_delaunay_locate) and the box of grid nodes to
+// recompute. Here the cell containing a point is its nearest nucleus (the
+// first in index order on an exact tie), and the likelihood finds the
+// changed grid columns itself.
+// ---------------------------------------------------------------------------
+namespace {
+
+// REAL*4 literals of the reference, widened to REAL*8 as its expressions do
+const double kPii = (double)3.1415926f;      // mcmc_loc2.f90:49 PII
+const double kPoisson = (double)1.730f;      // utils.f90:95 vs2vp
+const double kRho0 = (double)2.35f, kRho1 = (double)0.036f;   // utils.f90:120 vp2rho (crust)
+const double kVpVs = (double)1.1f;           // the vp >= 1.1 vs test
+
+double vs2vp(double vs) { return vs * kPoisson; }
+double vp2rho(double vp) { return kRho0 + kRho1 * ((vp - 3) * (vp - 3)); }
+
+// Fortran CEILING of a non-negative double, as an index (1-based); 0 -> 1
+int pick_index(double u, long long n) {
+  int i = (int)std::ceil(u * (double)n);
+  return i == 0 ? 1 : i;
+}
+
+int nearest_cell(const mct_mcmc_state *st, double x, double y, double z) {
+  int best = 0;
+  double bd = 0;
+  for (int i = 0; i < st->ncells; ++i) {
+    const double *p = st->points + 3 * (size_t)i;
+    const double dx = p[0] - x, dy = p[1] - y, dz = p[2] - z;
+    const double d = dx * dx + dy * dy + dz * dz;
+    if (i == 0 || d < bd) { bd = d; best = i; }
+  }
+  return best;
+}
+
+// proposeType2 (mcmc_loc2.f90:1384-1432) and proposeSigmaType (:1499-1519);
+// the joint datatype's choice between the two noise types draws from the
+// Fortran intrinsic random_number, which is not the chain's stream and is
+// not reproducible, so it is taken from the chain's stream here.
+int propose_type(const mct_mcmc_set *set, double propose, int iter, mct_rng *r) {
+  auto sigma_type = [&]() {
+    if (set->datatype == 0 || set->datatype == 1) return 5;
+    if (set->datatype == 2) return 6;
+    return mct_rng_unirand(r) < 0.1 ? 5 : 6;
+  };
+  if (iter % 2 == 0) {
+    if (propose < (double)0.333f) return 1;
+    if (propose < (double)0.666f) return 2;
+    return 3;
+  }
+  if (set->sigdep != 0 && set->locate != 0) {
+    if (propose < (double)0.300f) return 4;
+    if (propose < (double)0.8f) return 7;
+    return sigma_type();
+  }
+  if (set->sigdep != 0) return propose < (double)0.800f ? 4 : sigma_type();
+  if (set->locate != 0) return propose < (double)0.500f ? 4 : 7;
+  return 4;
+}
+
+bool in_prior(const mct_mcmc_set *set, double vp, double vs) {
+  return !(vs < set->vsmin || vs > set->vsmax || vp < set->vpmin || vp > set->vpmax || vp < kVpVs * vs);
+}
+
+// cell_birth (mcmc_loc2.f90:1521-1613)
+bool cell_birth(const mct_mcmc_set *set, mct_rng *r, mct_mcmc_state *st, double *prob) {
+  *prob = 0;
+  if (st->ncells == set->ncell_max) return false;
+  const double x = set->xmin + mct_rng_unirand(r) * (set->xmax - set->xmin);
+  const double y = set->ymin + mct_rng_unirand(r) * (set->ymax - set->ymin);
+  const double z = set->zmin + mct_rng_unirand(r) * (set->zmax - set->zmin);
+  double vp, vs, rho;
+  if (set->kernel == 0) {
+    const double *pm = st->parameters + 3 * (size_t)nearest_cell(st, x, y, z);
+    vs = pm[1] + mct_rng_gasdev(r) * set->sigma_vs2;
+    vp = pm[0] + mct_rng_gasdev(r) * set->sigma_vp2;
+    rho = vp2rho(vp);
+    const double gp = std::log(set->sigma_vp2 * std::sqrt(2 * kPii)) +
+                      (vp - pm[0]) * (vp - pm[0]) / (2 * (set->sigma_vp2 * set->sigma_vp2));
+    const double gs = std::log(set->sigma_vs2 * std::sqrt(2 * kPii)) +
+                      (vs - pm[1]) * (vs - pm[1]) / (2 * (set->sigma_vs2 * set->sigma_vs2));
+    *prob = set->datatype == 0 ? gp : (set->datatype == 2 ? gs : gp + gs);
+  } else {
+    vs = set->vsmin + mct_rng_unirand(r) * (set->vsmax - set->vsmin);
+    vp = set->vpmin + mct_rng_unirand(r) * (set->vpmax - set->vpmin);
+    if (set->datatype == 2) vp = vs2vp(vs);
+    rho = vp2rho(vp);
+  }
+  if (!in_prior(set, vp, vs)) { *prob = 0; return false; }
+  double *p = st->points + 3 * (size_t)st->ncells, *q = st->parameters + 3 * (size_t)st->ncells;
+  p[0] = x; p[1] = y; p[2] = z;
+  q[0] = vp; q[1] = vs; q[2] = rho;
+  st->ncells += 1;
+  return true;
+}
+
+// cell_death (mcmc_loc2.f90:1615-1683)
+bool cell_death(const mct_mcmc_set *set, mct_rng *r, mct_mcmc_state *st, int *iremove, double *prob) {
+  *prob = 0;
+  if (st->ncells == set->ncell_min) return false;
+  const int ir = pick_index(mct_rng_unirand(r), st->ncells);
+  *iremove = ir;
+  const double pt[3] = {st->points[3 * (size_t)(ir - 1)], st->points[3 * (size_t)(ir - 1) + 1],
+                        st->points[3 * (size_t)(ir - 1) + 2]};
+  const double pm1[3] = {st->parameters[3 * (size_t)(ir - 1)], st->parameters[3 * (size_t)(ir - 1) + 1],
+                         st->parameters[3 * (size_t)(ir - 1) + 2]};
+  for (int i = ir; i < st->ncells; ++i)
+    for (int k = 0; k < 3; ++k) {
+      st->points[3 * (size_t)(i - 1) + k] = st->points[3 * (size_t)i + k];
+      st->parameters[3 * (size_t)(i - 1) + k] = st->parameters[3 * (size_t)i + k];
+    }
+  st->ncells -= 1;
+  if (set->kernel == 0) {
+    const double *pm2 = st->parameters + 3 * (size_t)nearest_cell(st, pt[0], pt[1], pt[2]);
+    const double gp = std::log(1 / (set->sigma_vp2 * std::sqrt(2 * kPii))) -
+                      (pm2[0] - pm1[0]) * (pm2[0] - pm1[0]) / (2 * (set->sigma_vp2 * set->sigma_vp2));
+    const double gs = std::log(1 / (set->sigma_vs2 * std::sqrt(2 * kPii))) -
+                      (pm2[1] - pm1[1]) * (pm2[1] - pm1[1]) / (2 * (set->sigma_vs2 * set->sigma_vs2));
+    *prob = set->datatype == 0 ? gp : (set->datatype == 2 ? gs : gp + gs);
+  }
+  return true;
+}
+
+// cell_move (mcmc_loc2.f90:1685-1765): one coordinate moves; nuclei in the
+// deeper half of the grid use pd2 (both draws are taken there, as the
+// reference's code does)
+bool cell_move(const mct_mcmc_set *set, mct_rng *r, mct_mcmc_state *st, int *imove) {
+  const int im = pick_index(mct_rng_unirand(r), st->ncells);
+  *imove = im;
+  double *p = st->points + 3 * (size_t)(im - 1);
+  double dst[3] = {p[0], p[1], p[2]};
+  const double propose = mct_rng_unirand(r);
+  const bool deep = p[2] > (set->zmin + set->zmax) / 2;
+  const int axis = propose < (double)0.333f ? 0 : (propose < (double)0.666f ? 1 : 2);
+  const double ext = axis == 0 ? set->xmax - set->xmin : (axis == 1 ? set->ymax - set->ymin : set->zmax - set->zmin);
+  dst[axis] = p[axis] + mct_rng_gasdev(r) * set->pd * ext / 100;
+  if (deep) dst[axis] = p[axis] + mct_rng_gasdev(r) * set->pd2 * ext / 100;
+  if (dst[0] < set->xmin || dst[0] > set->xmax || dst[1] < set->ymin || dst[1] > set->ymax || dst[2] < set->zmin ||
+      dst[2] > set->zmax)
+    return false;
+  p[0] = dst[0]; p[1] = dst[1]; p[2] = dst[2];
+  return true;
+}
+
+// vel_change (mcmc_loc2.f90:1767-1835). The reference's one-line IF guards
+// only the vs redraw for deep nuclei; the vp redraw with sigma_vp2 that
+// follows it runs always, so three or four draws are taken.
+bool vel_change(const mct_mcmc_set *set, mct_rng *r, mct_mcmc_state *st, int *ivalue) {
+  const int iv = pick_index(mct_rng_unirand(r), st->ncells);
+  *ivalue = iv;
+  double *q = st->parameters + 3 * (size_t)(iv - 1);
+  const bool deep = st->points[3 * (size_t)(iv - 1) + 2] > (set->zmin + set->zmax) / 2;
+  double vs = q[1] + mct_rng_gasdev(r) * set->sigma_vs;
+  double vp = q[0] + mct_rng_gasdev(r) * set->sigma_vp;
+  if (deep) vs = q[1] + mct_rng_gasdev(r) * set->sigma_vs2;
+  vp = q[0] + mct_rng_gasdev(r) * set->sigma_vp2;
+  if (set->datatype == 2) vp = vs2vp(vs);
+  const double rho = vp2rho(vp);
+  if (vs < set->vsmin || vs > set->vsmax || vp < set->vpmin || vp > set->vpmax || vp < vs * kVpVs) return false;
+  q[0] = vp; q[1] = vs; q[2] = rho;
+  return true;
+}
+
+// bsigma_change / ssigma_change (mcmc_loc2.f90:1837-1903)
+bool sigma_change(mct_rng *r, int np, double *n0, double *n1, double sig0, double sig1, double n0min, double n0max,
+                  double n1min, double n1max, int *iperiod) {
+  if (np < 1) return false;
+  const int ip = pick_index(mct_rng_unirand(r), np);
+  *iperiod = ip;
+  if (mct_rng_unirand(r) < 0.5) n0[ip - 1] = n0[ip - 1] + mct_rng_gasdev(r) * sig0;
+  else n1[ip - 1] = n1[ip - 1] + mct_rng_gasdev(r) * sig1;
+  return !(n0[ip - 1] < n0min || n0[ip - 1] > n0max || n1[ip - 1] < n1min || n1[ip - 1] > n1max);
+}
+
+}  // namespace
+
+extern "C" {
+
+int mct_mcmc_propose(const mct_mcmc_set *set, mct_rng *rng, int iter, int redo, mct_mcmc_state *st,
+                     mct_mcmc_step *step) {
+  if (!set || !rng || !st || !step || !st->points || !st->parameters || st->ncells < 1 ||
+      st->ncells > set->ncell_max)
+    return MCT_ERR_ARG;
+  // a new proposal draws the acceptance number and the type; a redo (the
+  // previous proposal gave an invalid model) keeps both
+  // (mcmc_loc2.f90:200-205)
+  if (!redo) {
+    step->random = mct_rng_unirand(rng);
+    const double propose = mct_rng_unirand(rng);
+    step->ptype = propose_type(set, propose, iter, rng);
+  }
+  step->index = 0;
+  step->prob = 0;
+  bool ok = false;
+  switch (step->ptype) {
+    case 1: ok = cell_birth(set, rng, st, &step->prob); step->index = st->ncells; break;
+    case 2: ok = cell_death(set, rng, st, &step->index, &step->prob); break;
+    case 3: ok = cell_move(set, rng, st, &step->index); break;
+    case 4: ok = vel_change(set, rng, st, &step->index); break;
+    case 5:
+      ok = sigma_change(rng, st->nbnoise, st->bnoise0, st->bnoise1, set->sigma_bn0, set->sigma_bn1, set->bn0_min,
+                        set->bn0_max, set->bn1_min, set->bn1_max, &step->index);
+      break;
+    case 6:
+      ok = sigma_change(rng, st->nsnoise, st->snoise0, st->snoise1, set->sigma_sn0, set->sigma_sn1, set->sn0_min,
+                        set->sn0_max, set->sn1_min, set->sn1_max, &step->index);
+      break;
+    default:
+      // 7: source relocation (loc_change) is not restated
+      mct_set_error("mct_mcmc_propose", "proposal type 7 (source relocation) is not supported", __FILE__, __LINE__);
+      return MCT_ERR_UNSUPPORTED;
+  }
+  step->valid = ok ? 1 : 0;
+  return MCT_OK;
+}
+
+int mct_mcmc_accept(const mct_mcmc_set *set, const mct_mcmc_step *step, double like_new, double like_old) {
+  if (!set || !step) return MCT_ERR_ARG;
+  // the acceptance ratios of mcmc_loc2.f90:241-246 (birth), :289-294
+  // (death) and the rest (-like + like_copy)
+  double a = -like_new + like_old;
+  if (set->kernel == 0 && step->ptype == 1) a = step->prob - std::log(set->vsmax - set->vsmin) - like_new + like_old;
+  if (set->kernel == 0 && step->ptype == 2) a = step->prob + std::log(set->vsmax - set->vsmin) - like_new + like_old;
+  const double alpha = std::fmin(std::log(1.0), a);
+  return std::log(step->random) < alpha ? 1 : 0;
+}
 
 }  // extern "C"

@@ -1,0 +1,88 @@
+"""The sampler's random stream and proposal steps (C ABI mct_rng_*,
+mct_mcmc_*), mirroring the reference's mt19937 module and the
+Metropolis-Hastings steps of src/mcmc_loc2.f90.
+
+Chain holds one chain's state (RTI%points, RTI%parameters, noise levels)
+and its generator; propose() applies one proposal in place (the caller keeps
+a snapshot to restore on rejection, as the reference does) and accept()
+runs the acceptance test.
+"""
+import ctypes
+
+import numpy as np
+
+from ._lib import check, lib
+
+_D = ctypes.c_double
+_I = ctypes.c_int
+_P = ctypes.c_void_p
+
+
+class McmcSet(ctypes.Structure):
+    """The T_MCMC_SET fields the proposal steps read (include/mctomo.h)."""
+    _fields_ = [(n, _I) for n in ("ncell_min", "ncell_max", "kernel", "datatype", "sigdep", "locate")] + \
+               [(n, _D) for n in ("xmin", "xmax", "ymin", "ymax", "zmin", "zmax", "vpmin", "vpmax", "vsmin", "vsmax",
+                                  "sigma_vp", "sigma_vs", "sigma_vp2", "sigma_vs2", "pd", "pd2",
+                                  "sigma_bn0", "sigma_bn1", "bn0_min", "bn0_max", "bn1_min", "bn1_max",
+                                  "sigma_sn0", "sigma_sn1", "sn0_min", "sn0_max", "sn1_min", "sn1_max")]
+
+
+class McmcState(ctypes.Structure):
+    _fields_ = [("ncells", _I), ("points", _P), ("parameters", _P), ("nbnoise", _I), ("nsnoise", _I),
+                ("bnoise0", _P), ("bnoise1", _P), ("snoise0", _P), ("snoise1", _P)]
+
+
+class McmcStep(ctypes.Structure):
+    _fields_ = [("ptype", _I), ("index", _I), ("valid", _I), ("prob", _D), ("random", _D)]
+
+
+class Chain:
+    """One chain: seed for init_genrand, the initial nuclei (ncells, points
+    (ncell_max, 3), params (ncell_max, 3)) and noise levels."""
+
+    def __init__(self, settings, seed, ncells, points, params, snoise0=(), snoise1=(), bnoise0=(), bnoise1=()):
+        self.set = McmcSet(**settings)
+        self.rng = ctypes.c_void_p()
+        check("mct_rng_create", lib().mct_rng_create(seed, ctypes.byref(self.rng)))
+        nmax = self.set.ncell_max
+        self.ncells = int(ncells)
+        self.points = np.zeros((nmax, 3)); self.points[:ncells] = points[:ncells]
+        self.params = np.zeros((nmax, 3)); self.params[:ncells] = params[:ncells]
+        self.sn0 = np.array(snoise0, np.float64); self.sn1 = np.array(snoise1, np.float64)
+        self.bn0 = np.array(bnoise0, np.float64); self.bn1 = np.array(bnoise1, np.float64)
+
+    def close(self):
+        if self.rng:
+            lib().mct_rng_destroy(self.rng)
+            self.rng = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def snapshot(self):
+        return (self.ncells, self.points.copy(), self.params.copy(), self.sn0.copy(), self.sn1.copy(),
+                self.bn0.copy(), self.bn1.copy())
+
+    def restore(self, snap):
+        self.ncells = snap[0]
+        for dst, src in zip((self.points, self.params, self.sn0, self.sn1, self.bn0, self.bn1), snap[1:]):
+            dst[...] = src
+
+    def propose(self, it, redo=False, step=None):
+        """One proposal of iteration it applied in place; with redo, the type
+        and acceptance draw of step are kept. Returns the step."""
+        step = step if step is not None else McmcStep()
+        ptr = lambda a: a.ctypes.data if a.size else None  # noqa: E731
+        st = McmcState(self.ncells, self.points.ctypes.data, self.params.ctypes.data, self.bn0.size, self.sn0.size,
+                       ptr(self.bn0), ptr(self.bn1), ptr(self.sn0), ptr(self.sn1))
+        check("mct_mcmc_propose", lib().mct_mcmc_propose(ctypes.byref(self.set), self.rng, int(it), 1 if redo else 0,
+                                                        ctypes.byref(st), ctypes.byref(step)))
+        self.ncells = st.ncells
+        return step
+
+    def accept(self, step, like_new, like_old):
+        return lib().mct_mcmc_accept(ctypes.byref(self.set), ctypes.byref(step), float(like_new),
+                                     float(like_old)) == 1
