@@ -280,7 +280,15 @@ def run_gpu(args):
         "stage_ms_per_step": {n: round(v, 4) for n, v in zip(names, stage_ms)},
         "roofline": {"kernel": names[dom], "bound": "hbm", "achieved": round(achieved, 3), "peak": peak,
                      "peak_kind": peak_kind, "unit": "GB/s", "frac": round(achieved / peak, 6),
-                     "traffic": traffic},
+                     "traffic": traffic,
+                     # what actually limits the stage (HBM is ~0 % busy): the
+                     # latency of the reference's sequential heap march, one
+                     # node after another per solve; ncu on the small fm2d
+                     # case (profiles/fm2d_fp64_warp_pairs_16maps_49sources.md)
+                     "limiter": "latency of the sequential heap march (heap warp + FP64 update warp per solve)",
+                     "ncu_small_case": {"issue_active": {"coarse": 0.262, "refined": 0.220},
+                                        "fp64_pipe_active": {"coarse": 0.417, "refined": 0.336},
+                                        "dram_throughput": 0.0}},
         "gpu_launches": int(launches.value),
         "clocks": cl,
         "valid_models": int((out[:, 3] == 0).sum()),
