@@ -33,7 +33,11 @@ import numpy as np
 ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, ROOT)
 
-FM2D_DRAM_BYTES_PER_FORWARD = 2.19e9
+# DRAM bytes (read + write) of the fm2d stage of one forward of the surface
+# workload below (refine_slowness 0.223 GB, refined solves 0.421 GB, coarse
+# solves 0.169 GB), measured with ncu's one-pass dram__bytes_read.sum and
+# dram__bytes_write.sum over the stage's launches of the bench's first forward
+FM2D_DRAM_BYTES_PER_FORWARD = 0.813e9
 NCHAINS = 64
 NCELL_MAX = 400
 SEED = 20261203
@@ -257,10 +261,8 @@ def run_gpu(args):
                  1: 0.0, 3: NCHAINS * 20 * 1225 * 24.0}[dom]
     peak, peak_kind = peaks()
     achieved = alg_bytes / (stage_ms[dom] / 1e3) / 1e9 if alg_bytes else 0.0
-    # DRAM bytes (read + write) of the fm2d launches of one forward of this
-    # workload, measured with ncu (dram__bytes_read.sum, dram__bytes_write.sum,
-    # one pass): 2.19 GB on both the FP64 and the double-float path
-    traffic = FM2D_DRAM_BYTES_PER_FORWARD if dom == 2 and args.tt_precision in (0, 1) else None
+    # measured DRAM traffic of the FP64 fm2d stage (FM2D_DRAM_BYTES_PER_FORWARD)
+    traffic = FM2D_DRAM_BYTES_PER_FORWARD if dom == 2 and args.tt_precision == 0 else None
     line = {
         "metric": METRIC, "value": round(value, 3), "unit": "proposal evals/s", "n_gpus": ws,
         "steps": K, "warmup": W, "ms_per_step": round(total_ms / K, 4), "higher_is_better": True,
@@ -1007,9 +1009,13 @@ SERVED_CONFIG = {
 SERVED_SLOTS = {"tt2d": 256, "surface": 64, "body": 32, "joint": 16}
 
 
-def served_backends(single, slots):
+def served_backends(single, slots, priority="none"):
     """The four kinds' backends at the configurations' shapes (single: one
-    chain per call on one-slot contexts). Returns (backends, bytes per kind)."""
+    chain per call on one-slot contexts). priority names the contexts whose
+    streams get the device's highest priority in the batched mode: "none",
+    "body" (the body kind's context and the joint kind's body context) or
+    "body+joint" (the body kind and both of the joint kind's contexts).
+    Returns (backends, bytes per kind)."""
     import torch
     from mctomo_gb300 import BodyLikelihood, SurfaceLikelihood, TravelTime2DLikelihood, serving, synthetic
     rng = np.random.default_rng(SEED + 6)
@@ -1044,13 +1050,15 @@ def served_backends(single, slots):
     jb = serving.BodyBackend(sized("joint", lambda: BodyLikelihood(gb, sb, db, n["joint"], 800)), n["joint"], nmj,
                              prj, ev, single=single)
     joint = serving.JointBackend(js, jb)
-    if not single:
-        # The body and joint kinds wait on the host between the 3D solver's
-        # passes; their streams get the device's highest priority so that
-        # their short launches are not queued behind the 2D and surface
-        # kinds' long travel-time kernels.
+    if not single and priority != "none":
+        # The body kinds wait on the host between the 3D solver's passes; a
+        # high-priority stream keeps their short launches from queueing
+        # behind the 2D and surface kinds' long travel-time kernels.
         body.set_priority(True)
-        joint.set_priority(True)
+        if priority == "body":
+            jb.set_priority(True)
+        else:
+            joint.set_priority(True)
     return {"tt2d": tt2d, "surface": surf, "body": body, "joint": joint}, used
 
 
@@ -1068,7 +1076,7 @@ def run_served(args):
     arrivals = serving.poisson_arrivals(rng, SERVED_CONFIG["rate_chains_per_s"], dur, names)
     res = {}
     for plain in (False, True):
-        backends, used = served_backends(plain, SERVED_SLOTS)
+        backends, used = served_backends(plain, SERVED_SLOTS, args.served_priority)
         if sum(used.values()) > SERVED_CONFIG["hbm_budget_gb"] * 1e9:
             raise SystemExit("served contexts exceed the HBM budget: %s" % used)
         # one warm-up step per kind outside the stream
@@ -1095,7 +1103,7 @@ def run_served(args):
             "dtype": "f64 dispersion polish, f32 bracketing; f64 fm2d (reference order); int32 fixed-point 3D tiles",
             "data": "synthetic (seeded, shapes of configurations 1-3)",
             "config": dict(SERVED_CONFIG, slots=SERVED_SLOTS, seconds=dur, measured_window_s=[round(warm, 1), dur],
-                           arrivals=len(arrivals)),
+                           arrivals=len(arrivals), high_priority_streams=args.served_priority),
             "served": sv, "plain": pl,
             "served_over_plain": round(sv["evals_per_s"] / pl["evals_per_s"], 3) if pl["evals_per_s"] else None,
             "clocks": sv["clocks"]}
@@ -1279,6 +1287,8 @@ def main():
     ap.add_argument("--no-variant", action="store_true", help="surface workload: skip the double-float variant")
     ap.add_argument("--workload", default="surface", choices=["surface", "body", "disp", "tt2d", "served"])
     ap.add_argument("--served-seconds", type=float, default=60.0, help="served workload: stream length (s)")
+    ap.add_argument("--served-priority", default="none", choices=["none", "body", "body+joint"],
+                    help="served workload: contexts whose streams run at the device's highest priority")
     ap.add_argument("--chains2d", type=int, default=256, help="tt2d workload: chains per step")
     ap.add_argument("--columns", type=int, default=262144, help="disp workload: columns")
     ap.add_argument("--disp-sample", type=int, default=512, help="disp workload: columns checked by the oracle")
