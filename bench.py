@@ -1009,13 +1009,15 @@ SERVED_CONFIG = {
 SERVED_SLOTS = {"tt2d": 256, "surface": 64, "body": 32, "joint": 16}
 
 
-def served_backends(single, slots, priority="none"):
+def served_backends(single, slots, priority="none", share=None):
     """The four kinds' backends at the configurations' shapes (single: one
     chain per call on one-slot contexts). priority names the contexts whose
     streams get the device's highest priority in the batched mode: "none",
     "body" (the body kind's context and the joint kind's body context) or
-    "body+joint" (the body kind and both of the joint kind's contexts).
-    Returns (backends, bytes per kind)."""
+    "body+joint" (the body kind and both of the joint kind's contexts);
+    share maps "tt2d", "surface" and "joint" to the SM share of that kind's
+    2D travel-time launches (the joint kind's surface context) in the
+    batched mode. Returns (backends, bytes per kind)."""
     import torch
     from mctomo_gb300 import BodyLikelihood, SurfaceLikelihood, TravelTime2DLikelihood, serving, synthetic
     rng = np.random.default_rng(SEED + 6)
@@ -1050,6 +1052,12 @@ def served_backends(single, slots, priority="none"):
     jb = serving.BodyBackend(sized("joint", lambda: BodyLikelihood(gb, sb, db, n["joint"], 800)), n["joint"], nmj,
                              prj, ev, single=single)
     joint = serving.JointBackend(js, jb)
+    if not single and share:
+        # 2D travel-time kernels hold their SMs for the whole launch; a share
+        # per kind leaves SMs free for the body kinds' short 3D passes
+        for kind, obj in (("tt2d", tt2d), ("surface", surf), ("joint", js)):
+            if kind in share:
+                obj.set_sm_share(share[kind])
     if not single and priority != "none":
         # The body kinds wait on the host between the 3D solver's passes; a
         # high-priority stream keeps their short launches from queueing
@@ -1060,6 +1068,19 @@ def served_backends(single, slots, priority="none"):
         else:
             joint.set_priority(True)
     return {"tt2d": tt2d, "surface": surf, "body": body, "joint": joint}, used
+
+
+def parse_share(spec):
+    """'kind=share,...' (kinds tt2d, surface, joint) -> dict; 'none' -> {}."""
+    if not spec or spec == "none":
+        return {}
+    out = {}
+    for item in spec.split(","):
+        k, v = item.split("=")
+        if k not in ("tt2d", "surface", "joint"):
+            raise SystemExit("--served-sm-share: unknown kind %r" % k)
+        out[k] = float(v)
+    return out
 
 
 def run_served(args):
@@ -1075,8 +1096,9 @@ def run_served(args):
     dur, warm = args.served_seconds, args.served_seconds / 3.0
     arrivals = serving.poisson_arrivals(rng, SERVED_CONFIG["rate_chains_per_s"], dur, names)
     res = {}
-    for plain in (False, True):
-        backends, used = served_backends(plain, SERVED_SLOTS, args.served_priority)
+    share = parse_share(args.served_sm_share)
+    for plain in (False, True) if not args.served_only else (False,):
+        backends, used = served_backends(plain, SERVED_SLOTS, args.served_priority, share)
         if sum(used.values()) > SERVED_CONFIG["hbm_budget_gb"] * 1e9:
             raise SystemExit("served contexts exceed the HBM budget: %s" % used)
         # one warm-up step per kind outside the stream
@@ -1095,7 +1117,8 @@ def run_served(args):
         res["plain" if plain else "served"] = stats
         del backends, workers
         torch.cuda.synchronize()
-    sv, pl = res["served"], res["plain"]
+    sv = res["served"]
+    pl = res.get("plain", {"evals_per_s": 0.0, "kinds": {}})
     line = {"metric": "served proposal evals/s & p99 proposal latency, mixed stream, 1 GB300",
             "value": round(sv["evals_per_s"], 3), "unit": "proposal evals/s", "n_gpus": 1, "steps": None,
             "warmup": None, "ms_per_step": None, "higher_is_better": True, "scaling": "weak",
@@ -1103,7 +1126,8 @@ def run_served(args):
             "dtype": "f64 dispersion polish, f32 bracketing; f64 fm2d (reference order); int32 fixed-point 3D tiles",
             "data": "synthetic (seeded, shapes of configurations 1-3)",
             "config": dict(SERVED_CONFIG, slots=SERVED_SLOTS, seconds=dur, measured_window_s=[round(warm, 1), dur],
-                           arrivals=len(arrivals), high_priority_streams=args.served_priority),
+                           arrivals=len(arrivals), high_priority_streams=args.served_priority,
+                           sm_share=share or "whole device"),
             "served": sv, "plain": pl,
             "served_over_plain": round(sv["evals_per_s"] / pl["evals_per_s"], 3) if pl["evals_per_s"] else None,
             "clocks": sv["clocks"]}
@@ -1289,6 +1313,10 @@ def main():
     ap.add_argument("--served-seconds", type=float, default=60.0, help="served workload: stream length (s)")
     ap.add_argument("--served-priority", default="none", choices=["none", "body", "body+joint"],
                     help="served workload: contexts whose streams run at the device's highest priority")
+    ap.add_argument("--served-sm-share", default="none",
+                    help="served workload: SM share of the 2D travel-time launches per kind, "
+                         "e.g. tt2d=0.15,surface=0.25,joint=0.2 (none: whole device)")
+    ap.add_argument("--served-only", action="store_true", help="served workload: skip the plain leg")
     ap.add_argument("--chains2d", type=int, default=256, help="tt2d workload: chains per step")
     ap.add_argument("--columns", type=int, default=262144, help="disp workload: columns")
     ap.add_argument("--disp-sample", type=int, default=512, help="disp workload: columns checked by the oracle")

@@ -508,6 +508,16 @@ contains
       type(c_ptr), value :: ctx
       integer(c_int), value :: high
     end function
+    integer(c_int) function mct_surf_set_sm_share(ctx, share) bind(C, name="mct_surf_set_sm_share")
+      import :: c_int, c_ptr, c_double
+      type(c_ptr), value :: ctx
+      real(c_double), value :: share
+    end function
+    integer(c_int) function mct_tt2d_set_sm_share(ctx, share) bind(C, name="mct_tt2d_set_sm_share")
+      import :: c_int, c_ptr, c_double
+      type(c_ptr), value :: ctx
+      real(c_double), value :: share
+    end function
     integer(c_int) function mct_mcmc_propose(set, rng, iter, redo, state, step) bind(C, name="mct_mcmc_propose")
       import :: c_int, c_ptr, mct_mcmc_set, mct_mcmc_state, mct_mcmc_step
       type(mct_mcmc_set), intent(in) :: set

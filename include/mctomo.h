@@ -255,6 +255,13 @@ int mct_surf_destroy(mct_surf_ctx *ctx);
  * No counterpart in the reference: for the served loop, where contexts of
  * different kinds share the GPU. Refused while a submitted batch is pending. */
 int mct_surf_set_priority(mct_surf_ctx *ctx, int high);
+/* Limits the context's 2D travel-time launches to a share of the device's
+ * SMs (share in (0, 1): that share of the SM count times the kernels'
+ * resident blocks per SM; 0 or 1: the whole device, the default), so that
+ * other contexts' kernels on other streams find free SMs while they run.
+ * Results do not depend on it. No counterpart in the reference: for the
+ * served loop. MCT_ERR_ARG outside [0, 1]. */
+int mct_surf_set_sm_share(mct_surf_ctx *ctx, double share);
 
 /* Evaluates one proposal per listed chain against its slot's committed
  * state. points / params: [nchains][ncell_max][3] (x, y, z) and
@@ -498,6 +505,8 @@ int mct_tt2d_destroy(mct_tt2d_ctx *ctx);
  * No counterpart in the reference: for the served loop, where contexts of
  * different kinds share the GPU. */
 int mct_tt2d_set_priority(mct_tt2d_ctx *ctx, int high);
+/* As mct_surf_set_sm_share, for the context's fm2d launches. */
+int mct_tt2d_set_sm_share(mct_tt2d_ctx *ctx, double share);
 /* points [nchains][ncell_max][2] (x, y) = RTI%points, params
  * [nchains][ncell_max][3] (velocity first) = RTI%parameters, n0/n1
  * [nchains][2] = RTI%snoise0/1 (travel times, differential times);

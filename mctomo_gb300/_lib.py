@@ -57,6 +57,8 @@ SIGNATURES = {
     "mct_surf_set_priority": (I, [P, I]),
     "mct_body_set_priority": (I, [P, I]),
     "mct_tt2d_set_priority": (I, [P, I]),
+    "mct_surf_set_sm_share": (I, [P, D]),
+    "mct_tt2d_set_sm_share": (I, [P, D]),
     "mct_rng_create": (I, [ctypes.c_uint, P]),
     "mct_rng_destroy": (None, [P]),
     "mct_rng_seed": (I, [P, ctypes.c_uint]),

@@ -1033,8 +1033,7 @@ __device__ __forceinline__ WarpStateT<TT> warp_state(unsigned char *base, int no
 // whose band outgrows it listed in job.ovf_list. Overflow pass (redo = 1): the
 // listed solves again with a heap as large as the box.
 template <class TT, int SPW>
-__global__ void __launch_bounds__(64 * PAIRS_MAX)
-fm2d_refined_kernel(Fm2dJob job, int solve_bytes, int heap_cap, int redo) {
+__device__ __forceinline__ void refined_block(const Fm2dJob &job, int solve_bytes, int heap_cap, int redo, int blk) {
   extern __shared__ __align__(16) unsigned char smem[];
   const int pair = threadIdx.x >> 6, t64 = threadIdx.x & 63, lane = t64 & 31;
   const int slot = SPW == 2 ? (lane >> 4) : 0;                          // this thread's solve in the pair
@@ -1042,7 +1041,7 @@ fm2d_refined_kernel(Fm2dJob job, int solve_bytes, int heap_cap, int redo) {
   constexpr int NSUB = 64 / SPW;
   const bool leader = t64 < 32 && (lane & 15) == 0 && (SPW == 2 || lane == 0);
   const int bar1 = 1 + 2 * pair, bar2 = 2 + 2 * pair;
-  int solve = (blockIdx.x * (blockDim.x >> 6) + pair) * SPW + slot;
+  int solve = (blk * (blockDim.x >> 6) + pair) * SPW + slot;
   if (redo) solve = solve < *job.ovf_count ? job.ovf_list[solve] : job.nsolve;
   SolveGeom sg;
   const bool active = solve < job.nsolve && solve_geom(job, solve, sg);   // geometry errors: coarse stage
@@ -1105,6 +1104,27 @@ fm2d_refined_kernel(Fm2dJob job, int solve_bytes, int heap_cap, int redo) {
       rs[q] = st;
       rt[q] = st == -1 ? 0.0 : to_double(w.T[q], fx);
     }
+  }
+}
+
+// One logical block per block (WALK false), or (WALK true) a grid of at
+// most nblk blocks, each walking logical blocks blockIdx.x, blockIdx.x +
+// gridDim.x, ... below nblk, so that a grid smaller than nblk keeps the
+// kernel to a share of the SMs. Both warps of a pair meet at the pair's
+// barrier before the next logical block reuses the pair's shared memory. The
+// walk is a separate instantiation: in a loop the compiler keeps more of the
+// job in registers, which costs the single-pass kernel its register budget.
+template <class TT, int SPW, bool WALK>
+__global__ void __launch_bounds__(64 * PAIRS_MAX)
+fm2d_refined_kernel(Fm2dJob job, int solve_bytes, int heap_cap, int redo, int nblk) {
+  if constexpr (WALK) {
+    const int bar1 = 1 + 2 * (threadIdx.x >> 6);
+    for (int blk = blockIdx.x; blk < nblk; blk += gridDim.x) {
+      if (blk != (int)blockIdx.x) { __syncwarp(); pair_sync(bar1); }
+      refined_block<TT, SPW>(job, solve_bytes, heap_cap, redo, blk);
+    }
+  } else {
+    refined_block<TT, SPW>(job, solve_bytes, heap_cap, redo, blockIdx.x);
   }
 }
 
@@ -1257,8 +1277,7 @@ __device__ void trace_rays(const Fm2dJob &job, const WarpStateT<TT> &w, const Fx
 // refinement, the point source and travel with urg = 0); then the optional
 // time field and srtimes.
 template <class TT, int SPW>
-__global__ void __launch_bounds__(64 * PAIRS_MAX)
-fm2d_coarse_kernel(Fm2dJob job, int solve_bytes) {
+__device__ __forceinline__ void coarse_block(const Fm2dJob &job, int solve_bytes, int blk) {
   extern __shared__ __align__(16) unsigned char smem[];
   const int pair = threadIdx.x >> 6, t64 = threadIdx.x & 63, lane = t64 & 31;
   const int slot = SPW == 2 ? (lane >> 4) : 0;                          // this thread's solve in the pair
@@ -1266,7 +1285,7 @@ fm2d_coarse_kernel(Fm2dJob job, int solve_bytes) {
   constexpr int NSUB = 64 / SPW;
   const bool leader = t64 < 32 && (lane & 15) == 0 && (SPW == 2 || lane == 0);
   const int bar1 = 1 + 2 * pair, bar2 = 2 + 2 * pair;
-  const int solve = (blockIdx.x * (blockDim.x >> 6) + pair) * SPW + slot;
+  const int solve = (blk * (blockDim.x >> 6) + pair) * SPW + slot;
   SolveGeom sg;
   bool active = solve < job.nsolve;
   if (active && !solve_geom(job, solve, sg)) {
@@ -1391,6 +1410,21 @@ fm2d_coarse_kernel(Fm2dJob job, int solve_bytes) {
     tt[r] = trr;
   }
   if (job.rays) trace_rays(job, w, fx, sg, solve, sub, NSUB);
+}
+
+// Logical blocks as fm2d_refined_kernel has them.
+template <class TT, int SPW, bool WALK>
+__global__ void __launch_bounds__(64 * PAIRS_MAX)
+fm2d_coarse_kernel(Fm2dJob job, int solve_bytes, int nblk) {
+  if constexpr (WALK) {
+    const int bar1 = 1 + 2 * (threadIdx.x >> 6);
+    for (int blk = blockIdx.x; blk < nblk; blk += gridDim.x) {
+      if (blk != (int)blockIdx.x) { __syncwarp(); pair_sync(bar1); }
+      coarse_block<TT, SPW>(job, solve_bytes, blk);
+    }
+  } else {
+    coarse_block<TT, SPW>(job, solve_bytes, blockIdx.x);
+  }
 }
 
 }  // namespace
@@ -1559,30 +1593,61 @@ int fm2d_plan(const Fm2dJob &job, Fm2dPlan *plan) {
 }
 
 namespace {
+// Blocks to launch for nblk logical blocks of kernel k: with a share in
+// (0, 1) of the device, share x SM count (rounded, at least one) x the
+// kernel's resident blocks per SM, so that the launch leaves the other SMs to
+// other streams' kernels for its whole duration; *grid = nblk when that is
+// not fewer.
+template <class K>
+int grid_for(K k, int nblk, int threads, size_t smem, double share, int *grid) {
+  int dev = 0, sms = 0, occ = 0;
+  MCT_CUDA_TRY(cudaGetDevice(&dev));
+  MCT_CUDA_TRY(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
+  MCT_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k, threads, smem));
+  const int nsm = std::max(1, (int)(share * sms + 0.5));
+  const long cap = (long)nsm * std::max(occ, 1);
+  *grid = cap < nblk ? (int)cap : nblk;
+  return MCT_OK;
+}
+
+bool shared_out(double share) { return share > 0.0 && share < 1.0; }
+
+// The walking instantiations exist for the default warp layouts (refined
+// SPW 1, coarse SPW 2); other layouts run on the whole device.
 template <class TT, int SPW>
-int launch_refined(const Fm2dJob &job, int solve_bytes, int heap_cap, int redo, cudaStream_t s) {
-  auto kern = fm2d_refined_kernel<TT, SPW>;
+int launch_refined(const Fm2dJob &job, int solve_bytes, int heap_cap, int redo, double share, cudaStream_t s) {
+  constexpr bool kWalk = SPW == 1;
+  const bool walk = kWalk && shared_out(share);
+  auto kern = walk ? fm2d_refined_kernel<TT, SPW, kWalk> : fm2d_refined_kernel<TT, SPW, false>;
   int rc = mct_smem_attr(kern, 227 * 1024);
   if (rc) return rc;
   const int ppb = pairs_for(kern, SPW * solve_bytes);
   if (ppb < 1) return MCT_ERR_ARG;
   const int per_block = ppb * SPW;
-  const int blocks = (job.nsolve + per_block - 1) / per_block;
-  kern<<<blocks, 64 * ppb, (size_t)per_block * solve_bytes, s>>>(job, solve_bytes, heap_cap, redo);
+  const int nblk = (job.nsolve + per_block - 1) / per_block;
+  const size_t smem = (size_t)per_block * solve_bytes;
+  int grid = nblk;
+  if (walk && (rc = grid_for(kern, nblk, 64 * ppb, smem, share, &grid))) return rc;
+  kern<<<grid, 64 * ppb, smem, s>>>(job, solve_bytes, heap_cap, redo, nblk);
   MCT_CUDA_TRY(cudaGetLastError());
   return MCT_OK;
 }
 
 template <class TT, int SPW>
-int launch_coarse(const Fm2dJob &job, int solve_bytes, cudaStream_t s) {
-  auto kern = fm2d_coarse_kernel<TT, SPW>;
+int launch_coarse(const Fm2dJob &job, int solve_bytes, double share, cudaStream_t s) {
+  constexpr bool kWalk = SPW == 2;
+  const bool walk = kWalk && shared_out(share);
+  auto kern = walk ? fm2d_coarse_kernel<TT, SPW, kWalk> : fm2d_coarse_kernel<TT, SPW, false>;
   int rc = mct_smem_attr(kern, 227 * 1024);
   if (rc) return rc;
   const int ppb = pairs_for(kern, SPW * solve_bytes);
   if (ppb < 1) return MCT_ERR_ARG;
   const int per_block = ppb * SPW;
-  const int blocks = (job.nsolve + per_block - 1) / per_block;
-  kern<<<blocks, 64 * ppb, (size_t)per_block * solve_bytes, s>>>(job, solve_bytes);
+  const int nblk = (job.nsolve + per_block - 1) / per_block;
+  const size_t smem = (size_t)per_block * solve_bytes;
+  int grid = nblk;
+  if (walk && (rc = grid_for(kern, nblk, 64 * ppb, smem, share, &grid))) return rc;
+  kern<<<grid, 64 * ppb, smem, s>>>(job, solve_bytes, nblk);
   MCT_CUDA_TRY(cudaGetLastError());
   return MCT_OK;
 }
@@ -1590,20 +1655,21 @@ int launch_coarse(const Fm2dJob &job, int solve_bytes, cudaStream_t s) {
 template <class TT>
 int launch_solves(const Fm2dJob &job, const Fm2dPlan &plan, cudaStream_t s) {
   int rc;
+  const double sh = plan.sm_share;
   if (job.asgr == 1) {
     if (!job.ovf_list || !job.ovf_count) return MCT_ERR_ARG;
     MCT_CUDA_TRY(cudaMemsetAsync(job.ovf_count, 0, sizeof(int), s));
-    rc = g_spw_refined == 2 ? launch_refined<TT, 2>(job, plan.ref_warp_bytes, plan.ref_heap_cap, 0, s)
-                            : launch_refined<TT, 1>(job, plan.ref_warp_bytes, plan.ref_heap_cap, 0, s);
+    rc = g_spw_refined == 2 ? launch_refined<TT, 2>(job, plan.ref_warp_bytes, plan.ref_heap_cap, 0, sh, s)
+                            : launch_refined<TT, 1>(job, plan.ref_warp_bytes, plan.ref_heap_cap, 0, sh, s);
     if (rc) return rc;
     if (plan.ref_heap_cap < job.nref_max) {
       // overflow pass: solves beyond the device-side count exit at once
-      rc = launch_refined<TT, 1>(job, plan.ref_full_warp_bytes, job.nref_max, 1, s);
+      rc = launch_refined<TT, 1>(job, plan.ref_full_warp_bytes, job.nref_max, 1, sh, s);
       if (rc) return rc;
     }
   }
-  return g_spw_coarse == 2 ? launch_coarse<TT, 2>(job, plan.warp_bytes, s)
-                           : launch_coarse<TT, 1>(job, plan.warp_bytes, s);
+  return g_spw_coarse == 2 ? launch_coarse<TT, 2>(job, plan.warp_bytes, sh, s)
+                           : launch_coarse<TT, 1>(job, plan.warp_bytes, sh, s);
 }
 }  // namespace
 

@@ -46,6 +46,9 @@ struct Fm2dPlan {
   int ref_heap_cap;          // heap entries of the refined source-box stage (asgr = 1)
   int ref_warp_bytes;        // shared memory per solve of that stage
   int ref_full_warp_bytes;   // the same with a heap as large as the box (overflow pass)
+  // launch policy, not set by fm2d_plan: the share of the device's SMs the
+  // solve kernels may hold at once (0 or >= 1: all)
+  double sm_share = 0.0;
 };
 
 int fm2d_plan(const Fm2dJob &job, Fm2dPlan *plan);

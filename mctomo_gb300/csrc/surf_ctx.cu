@@ -282,6 +282,12 @@ int mct_surf_set_priority(mct_surf_ctx *c, int high) {
   return mct_restream(&c->stream, high);
 }
 
+int mct_surf_set_sm_share(mct_surf_ctx *c, double share) {
+  if (!c || !(share >= 0.0 && share <= 1.0)) return MCT_ERR_ARG;
+  c->plan.fm2d_plan.sm_share = share;
+  return MCT_OK;
+}
+
 int mct_surf_destroy(mct_surf_ctx *c) {
   if (!c) return MCT_OK;
   cudaStreamSynchronize(c->stream);

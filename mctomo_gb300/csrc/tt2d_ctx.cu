@@ -516,6 +516,12 @@ int mct_tt2d_set_priority(mct_tt2d_ctx *c, int high) {
   return mct_restream(&c->stream, high);
 }
 
+int mct_tt2d_set_sm_share(mct_tt2d_ctx *c, double share) {
+  if (!c || !(share >= 0.0 && share <= 1.0)) return MCT_ERR_ARG;
+  c->fp.sm_share = share;
+  return MCT_OK;
+}
+
 int mct_tt2d_destroy(mct_tt2d_ctx *c) {
   if (!c) return MCT_OK;
   cudaStreamSynchronize(c->stream);

@@ -240,6 +240,9 @@ class TT2DBackend(_SlotBackend):
     def set_priority(self, high):
         self.ctx.set_priority(high)
 
+    def set_sm_share(self, share):
+        self.ctx.set_sm_share(share)
+
     def forward(self, slots, models):
         assert not self.single or len(models) == 1
         m, idx, nc, pts, par = self._pack(slots, models)
@@ -290,6 +293,9 @@ class SurfaceBackend(_SlotBackend):
 
     def set_priority(self, high):
         self.ctx.set_priority(high)
+
+    def set_sm_share(self, share):
+        self.ctx.set_sm_share(share)
 
     def submit(self, slots, models):
         self.ctx.submit(*self._args(slots, models))

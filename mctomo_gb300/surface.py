@@ -85,6 +85,11 @@ class SurfaceLikelihood:
         stream of the device."""
         check("mct_surf_set_priority", lib().mct_surf_set_priority(self.h, 1 if high else 0))
 
+    def set_sm_share(self, share):
+        """Keep this context's 2D travel-time kernels to a share (0-1) of the
+        device's SMs (0 or 1: all of them); results do not depend on it."""
+        check("mct_surf_set_sm_share", lib().mct_surf_set_sm_share(self.h, float(share)))
+
     def close(self):
         if self.h:
             lib().mct_surf_destroy(self.h)

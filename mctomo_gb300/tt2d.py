@@ -70,6 +70,11 @@ class TravelTime2DLikelihood:
         stream of the device."""
         check("mct_tt2d_set_priority", lib().mct_tt2d_set_priority(self.h, 1 if high else 0))
 
+    def set_sm_share(self, share):
+        """Keep this context's 2D travel-time kernels to a share (0-1) of the
+        device's SMs (0 or 1: all of them); results do not depend on it."""
+        check("mct_tt2d_set_sm_share", lib().mct_tt2d_set_sm_share(self.h, float(share)))
+
     def close(self):
         if self.h:
             lib().mct_tt2d_destroy(self.h)
