@@ -331,6 +331,34 @@ module mctomo_gb300
       real(c_double), intent(out) :: out(*)
       integer(c_int), intent(out) :: done
     end function
+    integer(c_int) function mct_body_submit(ctx, nchains, ncells, points, params, locations, n0, n1) &
+        bind(C, name="mct_body_submit")
+      import :: c_int, c_double, c_ptr
+      type(c_ptr), value :: ctx
+      integer(c_int), value :: nchains
+      integer(c_int), intent(in) :: ncells(*)
+      real(c_double), intent(in) :: points(*), params(*), locations(*), n0(*), n1(*)
+    end function
+    integer(c_int) function mct_body_poll(ctx, out, done) bind(C, name="mct_body_poll")
+      import :: c_int, c_double, c_ptr
+      type(c_ptr), value :: ctx
+      real(c_double), intent(out) :: out(*)
+      integer(c_int), intent(out) :: done
+    end function
+    integer(c_int) function mct_tt2d_submit(ctx, nchains, ncells, points, params, n0, n1) &
+        bind(C, name="mct_tt2d_submit")
+      import :: c_int, c_double, c_ptr
+      type(c_ptr), value :: ctx
+      integer(c_int), value :: nchains
+      integer(c_int), intent(in) :: ncells(*)
+      real(c_double), intent(in) :: points(*), params(*), n0(*), n1(*)
+    end function
+    integer(c_int) function mct_tt2d_poll(ctx, out, done) bind(C, name="mct_tt2d_poll")
+      import :: c_int, c_double, c_ptr
+      type(c_ptr), value :: ctx
+      real(c_double), intent(out) :: out(*)
+      integer(c_int), intent(out) :: done
+    end function
 
     ! ---- 3D travel times (fastmarching/fastMarching.cpp fastMarching3D)
     integer(c_int) function mct_fast_marching3d(nx, ny, nz, dx, dy, dz, xmin, ymin, zmin, vel, src, rev, nrev, &

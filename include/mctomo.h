@@ -435,6 +435,20 @@ int mct_body_forward(mct_body_ctx *ctx, int nchains, const int *ncells,
                      const double *points, const double *params,
                      const double *locations, const double *n0,
                      const double *n1, double *out);
+/* mct_body_submit: starts the forward of mct_body_forward and returns at
+ * once (the arrays are copied before it returns); the batch runs on a
+ * worker thread of the context, since the 3D solver waits on the host
+ * between its passes. One submitted batch per context at a time; the other
+ * calls on the context return MCT_ERR_ARG until it is polled.
+ * mct_body_poll: *done = 0 while the batch runs; when it has finished, *done
+ * = 1, out (nchains x 4) is filled as by mct_body_forward and the batch's
+ * status is returned; mct_body_commit then applies to it. No counterpart in
+ * the reference: one host thread can keep several contexts busy. */
+int mct_body_submit(mct_body_ctx *ctx, int nchains, const int *ncells,
+                    const double *points, const double *params,
+                    const double *locations, const double *n0,
+                    const double *n1);
+int mct_body_poll(mct_body_ctx *ctx, double *out, int *done);
 /* After the Metropolis test: chains with accept[c] != 0 (and a valid
  * forward) keep the last forward's travel times as their state (the
  * reference keeps the accepted like and restores the backup on reject,
@@ -516,6 +530,15 @@ int mct_tt2d_set_sm_share(mct_tt2d_ctx *ctx, double share);
 int mct_tt2d_forward(mct_tt2d_ctx *ctx, int nchains, const int *ncells,
                      const double *points, const double *params,
                      const double *n0, const double *n1, double *out);
+/* mct_tt2d_submit / mct_tt2d_poll: mct_tt2d_forward split as
+ * mct_surf_submit / mct_surf_poll are (the arrays copied into pinned
+ * staging before submit returns, the batch on the context's stream, poll
+ * without blocking). One submitted batch at a time; the other calls on the
+ * context return MCT_ERR_ARG until it is polled. */
+int mct_tt2d_submit(mct_tt2d_ctx *ctx, int nchains, const int *ncells,
+                    const double *points, const double *params,
+                    const double *n0, const double *n1);
+int mct_tt2d_poll(mct_tt2d_ctx *ctx, double *out, int *done);
 /* After the Metropolis test: chains with accept[c] != 0 (and a valid
  * forward) keep the last forward's times as their state, as the
  * reference keeps the accepted like and restores the backed-up one on

@@ -46,6 +46,8 @@ SIGNATURES = {
     "mct_body_destroy": (I, [P]),
     "mct_body_forward": (I, [P, I, P, P, P, P, P, P, P]),
     "mct_body_phase_time": (I, [P, I, P, P]),
+    "mct_body_submit": (I, [P, I, P, P, P, P, P, P]),
+    "mct_body_poll": (I, [P, P, P]),
     "mct_body_commit": (I, [P, I, P]),
     "mct_body_noise_likelihood": (I, [P, I, P, P, P, P]),
     "mct_tt2d_create": (I, [P, P, P, I, I, P]),
@@ -54,6 +56,8 @@ SIGNATURES = {
     "mct_tt2d_commit": (I, [P, I, P]),
     "mct_tt2d_noise_likelihood": (I, [P, I, P, P, P]),
     "mct_tt2d_phase_time": (I, [P, I, P]),
+    "mct_tt2d_submit": (I, [P, I, P, P, P, P, P]),
+    "mct_tt2d_poll": (I, [P, P, P]),
     "mct_surf_set_priority": (I, [P, I]),
     "mct_body_set_priority": (I, [P, I]),
     "mct_tt2d_set_priority": (I, [P, I]),

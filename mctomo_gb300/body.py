@@ -79,6 +79,27 @@ class BodyLikelihood:
                                                          ptr(locations), ptr(n0), ptr(n1), ptr(out)))
         return out
 
+    def submit(self, ncells, points, params, locations, n0, n1):
+        """Starts forward() on the context's worker thread without waiting;
+        poll() collects it."""
+        ncells = np.ascontiguousarray(ncells, np.int32)
+        nch = ncells.size
+        points = np.ascontiguousarray(points, np.float64)
+        params = np.ascontiguousarray(params, np.float64)
+        locations = np.ascontiguousarray(locations, np.float64).reshape(nch, self.nsrc, 4)
+        n0 = np.ascontiguousarray(n0, np.float64).reshape(nch, self.np)
+        n1 = np.ascontiguousarray(n1, np.float64).reshape(nch, self.np)
+        check("mct_body_submit", lib().mct_body_submit(self.h, nch, ptr(ncells), ptr(points), ptr(params),
+                                                       ptr(locations), ptr(n0), ptr(n1)))
+        self._pending = nch
+
+    def poll(self):
+        """(done, out): out (nchains, 4) once the submitted batch finished."""
+        out = np.zeros((self._pending, 4))
+        done = ctypes.c_int()
+        check("mct_body_poll", lib().mct_body_poll(self.h, ptr(out), ctypes.byref(done)))
+        return bool(done.value), (out if done.value else None)
+
     def commit(self, accept):
         """Chains with accept[c] keep the last forward as their state."""
         accept = np.ascontiguousarray(accept, np.int32)

@@ -17,7 +17,14 @@
 #include <cfloat>
 #include <climits>
 #include <algorithm>
+#include <atomic>
 #include <cmath>
+#include <condition_variable>
+#include <cstring>
+#include <mutex>
+#include <string>
+#include <system_error>
+#include <thread>
 
 namespace {
 
@@ -185,7 +192,52 @@ struct mct_body_ctx {
   double2 *hvn = nullptr; void *hscratch = nullptr;
   int hchunk = 0; int *herr = nullptr;
   int last_nchains = 0, last_passes = 0;
+  // mct_body_submit / mct_body_poll: the forward waits on the host between
+  // the 3D solver's passes, so a submitted batch runs on a worker thread of
+  // the context (started by the first submit) with copies of the caller's
+  // arrays; state 0 idle, 1 submitted, 2 finished (results in sub.out)
+  int device = 0;
+  std::thread worker;
+  std::mutex mu;
+  std::condition_variable cv;
+  bool job_ready = false, quit = false;
+  std::atomic<int> state{0};
+  struct Submitted {
+    int nchains = 0, rc = 0;
+    std::vector<int> ncells;
+    std::vector<double> points, params, loc, n0, n1, out;
+    std::string err;
+  } sub;
 };
+
+namespace {
+int body_forward(mct_body_ctx *c, int nchains, const int *ncells, const double *points, const double *params,
+                 const double *locations, const double *n0, const double *n1, double *out);
+
+void body_worker(mct_body_ctx *c) {
+  cudaSetDevice(c->device);
+  std::unique_lock<std::mutex> lk(c->mu);
+  for (;;) {
+    c->cv.wait(lk, [c] { return c->job_ready || c->quit; });
+    if (c->quit) return;
+    c->job_ready = false;
+    lk.unlock();
+    mct_body_ctx::Submitted &j = c->sub;
+    j.rc = body_forward(c, j.nchains, j.ncells.data(), j.points.data(), j.params.data(), j.loc.data(), j.n0.data(),
+                        j.n1.data(), j.out.data());
+    j.err = j.rc < 0 ? mct_last_error() : "";
+    c->state.store(2, std::memory_order_release);
+    lk.lock();
+  }
+}
+
+// a submitted batch has not been polled: the blocking calls are refused
+bool busy(const mct_body_ctx *c, const char *name) {
+  if (c->state.load(std::memory_order_acquire) == 0) return false;
+  mct_set_error(name, "a submitted batch is not polled yet", __FILE__, __LINE__);
+  return true;
+}
+}  // namespace
 
 extern "C" {
 
@@ -290,17 +342,24 @@ int mct_body_create(const mct_grid *g, const mct_body_settings *st, const mct_bo
   cudaMemcpy(dt + (size_t)np * npairs, hs.data(), sizeof(double) * np * npairs, cudaMemcpyHostToDevice);
   if (cudaDeviceSynchronize() != cudaSuccess) { cudaFree(c->mem); cudaStreamDestroy(c->stream); delete c; return MCT_ERR_CUDA; }
   c->dev = BodyDev{nsrc, nrev, np, dat->nrays, st->sigdep, from_rev, rays, dt, dt + (size_t)np * npairs};
+  cudaGetDevice(&c->device);
   *out = c;
   return MCT_OK;
 }
 
 int mct_body_set_priority(mct_body_ctx *c, int high) {
-  if (!c) return MCT_ERR_ARG;
+  if (!c || busy(c, "mct_body_set_priority")) return MCT_ERR_ARG;
   return mct_restream(&c->stream, high);
 }
 
 int mct_body_destroy(mct_body_ctx *c) {
   if (!c) return MCT_OK;
+  if (c->worker.joinable()) {
+    // the worker finishes a batch in flight before it sees quit
+    { std::lock_guard<std::mutex> lk(c->mu); c->quit = true; }
+    c->cv.notify_one();
+    c->worker.join();
+  }
   cudaStreamSynchronize(c->stream);
   cudaFree(c->mem);
   cudaStreamDestroy(c->stream);
@@ -310,8 +369,63 @@ int mct_body_destroy(mct_body_ctx *c) {
 
 int mct_body_forward(mct_body_ctx *c, int nchains, const int *ncells, const double *points, const double *params,
                      const double *locations, const double *n0, const double *n1, double *out) {
-  if (!c || nchains < 1 || nchains > c->nslots) return MCT_ERR_ARG;
+  if (!c || busy(c, "mct_body_forward") || nchains < 1 || nchains > c->nslots) return MCT_ERR_ARG;
   for (int i = 0; i < nchains; ++i) if (ncells[i] < 1 || ncells[i] > c->ncell_max) return MCT_ERR_ARG;
+  return body_forward(c, nchains, ncells, points, params, locations, n0, n1, out);
+}
+
+int mct_body_submit(mct_body_ctx *c, int nchains, const int *ncells, const double *points, const double *params,
+                    const double *locations, const double *n0, const double *n1) {
+  if (!c || busy(c, "mct_body_submit") || nchains < 1 || nchains > c->nslots || !ncells || !points || !params ||
+      !locations || !n0 || !n1)
+    return MCT_ERR_ARG;
+  for (int i = 0; i < nchains; ++i) if (ncells[i] < 1 || ncells[i] > c->ncell_max) return MCT_ERR_ARG;
+  mct_body_ctx::Submitted &j = c->sub;
+  const size_t pc = (size_t)nchains * c->ncell_max * 3, nl = (size_t)nchains * c->dev.nsrc * 4;
+  const size_t nn = (size_t)nchains * c->dev.np;
+  j.nchains = nchains;
+  j.ncells.assign(ncells, ncells + nchains);
+  j.points.assign(points, points + pc);
+  j.params.assign(params, params + pc);
+  j.loc.assign(locations, locations + nl);
+  j.n0.assign(n0, n0 + nn);
+  j.n1.assign(n1, n1 + nn);
+  j.out.assign((size_t)4 * nchains, 0.0);
+  if (!c->worker.joinable()) {
+    try {
+      c->worker = std::thread(body_worker, c);
+    } catch (const std::system_error &e) {
+      mct_set_error("mct_body_submit", e.what(), __FILE__, __LINE__);
+      return MCT_ERR_INTERNAL;
+    }
+  }
+  {
+    std::lock_guard<std::mutex> lk(c->mu);
+    c->state.store(1, std::memory_order_release);
+    c->job_ready = true;
+  }
+  c->cv.notify_one();
+  return MCT_OK;
+}
+
+int mct_body_poll(mct_body_ctx *c, double *out, int *done) {
+  if (!c || !out || !done || c->state.load(std::memory_order_acquire) == 0) return MCT_ERR_ARG;
+  *done = 0;
+  if (c->state.load(std::memory_order_acquire) != 2) return MCT_OK;
+  mct_body_ctx::Submitted &j = c->sub;
+  std::memcpy(out, j.out.data(), sizeof(double) * 4 * j.nchains);
+  const int rc = j.rc;
+  if (rc < 0) mct_set_error("mct_body_poll", j.err.c_str(), __FILE__, __LINE__);
+  c->state.store(0, std::memory_order_release);
+  *done = 1;
+  return rc;
+}
+
+}  // extern "C"
+
+namespace {
+int body_forward(mct_body_ctx *c, int nchains, const int *ncells, const double *points, const double *params,
+                 const double *locations, const double *n0, const double *n1, double *out) {
   const mct_grid &g = c->g;
   const BodyDev &d = c->dev;
   cudaStream_t s = c->stream;
@@ -390,9 +504,12 @@ int mct_body_forward(mct_body_ctx *c, int nchains, const int *ncells, const doub
   if (gst[0]) return gst[0];
   return MCT_OK;
 }
+}  // namespace
+
+extern "C" {
 
 int mct_body_commit(mct_body_ctx *c, int nchains, const int *accept) {
-  if (!c || nchains < 1 || nchains > c->last_nchains || !accept) return MCT_ERR_ARG;
+  if (!c || busy(c, "mct_body_commit") || nchains < 1 || nchains > c->last_nchains || !accept) return MCT_ERR_ARG;
   cudaStream_t s = c->stream;
   const int n = c->dev.np * c->dev.nsrc * c->dev.nrev;
   MCT_CUDA_TRY(cudaMemcpyAsync(c->accept, accept, sizeof(int) * nchains, cudaMemcpyHostToDevice, s));
@@ -405,7 +522,9 @@ int mct_body_commit(mct_body_ctx *c, int nchains, const int *accept) {
 
 int mct_body_noise_likelihood(mct_body_ctx *c, int nchains, const double *locations, const double *n0,
                               const double *n1, double *out) {
-  if (!c || nchains < 1 || nchains > c->nslots || !locations || !n0 || !n1 || !out) return MCT_ERR_ARG;
+  if (!c || busy(c, "mct_body_noise_likelihood") || nchains < 1 || nchains > c->nslots || !locations || !n0 || !n1 ||
+      !out)
+    return MCT_ERR_ARG;
   cudaStream_t s = c->stream;
   const BodyDev &d = c->dev;
   MCT_CUDA_TRY(cudaMemcpyAsync(c->loc, locations, sizeof(double) * nchains * d.nsrc * 4, cudaMemcpyHostToDevice, s));
@@ -419,7 +538,7 @@ int mct_body_noise_likelihood(mct_body_ctx *c, int nchains, const double *locati
 }
 
 int mct_body_phase_time(mct_body_ctx *c, int index, double *phase_time, int *passes) {
-  if (!c || index < 0 || index >= c->last_nchains) return MCT_ERR_ARG;
+  if (!c || busy(c, "mct_body_phase_time") || index < 0 || index >= c->last_nchains) return MCT_ERR_ARG;
   const size_t n = (size_t)c->dev.np * c->dev.nsrc * c->dev.nrev;
   MCT_CUDA_TRY(cudaStreamSynchronize(c->stream));
   if (phase_time) MCT_CUDA_TRY(cudaMemcpy(phase_time, c->ptime + (size_t)index * n, sizeof(double) * n,

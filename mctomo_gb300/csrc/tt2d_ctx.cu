@@ -38,6 +38,7 @@
 #include <cfloat>
 #include <climits>
 #include <cmath>
+#include <cstring>
 #include <vector>
 
 namespace {
@@ -331,7 +332,17 @@ struct mct_tt2d_ctx {
   double *vel = nullptr, *velv = nullptr, *tt = nullptr;
   double *ctt = nullptr, *cumis = nullptr;     // committed state per slot
   int *committed = nullptr, *accept = nullptr;
+  // mct_tt2d_submit / mct_tt2d_poll: pinned staging (allocated by the first
+  // submit), the completion event and the batch in flight
+  int *h_ints = nullptr;       // [nslots] ncells, [2] device status
+  double *h_dbl = nullptr;     // points [nslots][ncell_max][2], params [..][3], n0, n1 [nslots][2], out [nslots][4]
+  cudaEvent_t done = nullptr;
+  int pending = 0;
 };
+
+namespace {
+bool tt2d_busy(const mct_tt2d_ctx *c, const char *name);
+}
 
 extern "C" {
 
@@ -512,7 +523,7 @@ int mct_tt2d_create(const mct_grid *g, const mct_tt2d_settings *st, const mct_tt
 }
 
 int mct_tt2d_set_priority(mct_tt2d_ctx *c, int high) {
-  if (!c) return MCT_ERR_ARG;
+  if (!c || tt2d_busy(c, "mct_tt2d_set_priority")) return MCT_ERR_ARG;
   return mct_restream(&c->stream, high);
 }
 
@@ -525,23 +536,44 @@ int mct_tt2d_set_sm_share(mct_tt2d_ctx *c, double share) {
 int mct_tt2d_destroy(mct_tt2d_ctx *c) {
   if (!c) return MCT_OK;
   cudaStreamSynchronize(c->stream);
+  if (c->h_ints) cudaFreeHost(c->h_ints);
+  if (c->h_dbl) cudaFreeHost(c->h_dbl);
+  if (c->done) cudaEventDestroy(c->done);
   cudaFree(c->mem);
   cudaStreamDestroy(c->stream);
   delete c;
   return MCT_OK;
 }
 
-int mct_tt2d_forward(mct_tt2d_ctx *c, int nchains, const int *ncells, const double *points, const double *params,
-                     const double *n0, const double *n1, double *out) {
-  if (!c || nchains < 1 || nchains > c->nslots || !ncells || !points || !params || !n0 || !n1 || !out) {
-    mct_set_error("mct_tt2d_forward", "bad arguments", __FILE__, __LINE__);
+}  // extern "C"
+
+namespace {
+bool tt2d_busy(const mct_tt2d_ctx *c, const char *name) {
+  if (!c->pending) return false;
+  mct_set_error(name, "a submitted batch is not polled yet", __FILE__, __LINE__);
+  return true;
+}
+
+int tt2d_check(const mct_tt2d_ctx *c, int nchains, const int *ncells, const double *points, const double *params,
+               const double *n0, const double *n1, const char *name) {
+  if (!c || tt2d_busy(c, name)) return MCT_ERR_ARG;
+  if (nchains < 1 || nchains > c->nslots || !ncells || !points || !params || !n0 || !n1) {
+    mct_set_error(name, "bad arguments", __FILE__, __LINE__);
     return MCT_ERR_ARG;
   }
   for (int i = 0; i < nchains; ++i)
     if (ncells[i] < 1 || ncells[i] > c->ncell_max) {
-      mct_set_error("mct_tt2d_forward", "cell count outside [1, ncell_max]", __FILE__, __LINE__);
+      mct_set_error(name, "cell count outside [1, ncell_max]", __FILE__, __LINE__);
       return MCT_ERR_ARG;
     }
+  return MCT_OK;
+}
+
+// The forward's work on the context's stream: the inputs copied from host
+// arrays, the results and the two device status words copied to out and gst
+// (host arrays; pinned ones make the copies asynchronous).
+int tt2d_enqueue(mct_tt2d_ctx *c, int nchains, const int *ncells, const double *points, const double *params,
+                 const double *n0, const double *n1, double *out, int *gst) {
   const mct_grid &g = c->g;
   const Tt2dDev &d = c->dev;
   cudaStream_t s = c->stream;
@@ -576,22 +608,83 @@ int mct_tt2d_forward(mct_tt2d_ctx *c, int nchains, const int *ncells, const doub
   }
   tt2d_misfit_kernel<<<nchains, 256, 0, s>>>(d, c->tt, c->n0, c->n1, c->out, c->umis);
   MCT_CUDA_TRY(cudaGetLastError());
-  int gst[2] = {0, 0};
   MCT_CUDA_TRY(cudaMemcpyAsync(out, c->out, sizeof(double) * 4 * nchains, cudaMemcpyDeviceToHost, s));
   MCT_CUDA_TRY(cudaMemcpyAsync(gst, c->gstatus, sizeof(int) * 2, cudaMemcpyDeviceToHost, s));
-  MCT_CUDA_TRY(cudaStreamSynchronize(s));
-  c->last_nchains = nchains;
+  return MCT_OK;
+}
+
+// The call's status from the device status words (gridding, fm2d).
+int tt2d_status(const int *gst, const char *name) {
   if (gst[0]) return gst[0];
   if (gst[1]) {
-    mct_set_error("mct_tt2d_forward", gst[1] == MCT_ERR_OUTSIDE ? "ray or source outside the grid" : "fm2d status",
-                  __FILE__, __LINE__);
+    mct_set_error(name, gst[1] == MCT_ERR_OUTSIDE ? "ray or source outside the grid" : "fm2d status", __FILE__,
+                  __LINE__);
     return gst[1] < 0 ? gst[1] : MCT_ERR_INTERNAL;
   }
   return MCT_OK;
 }
+}  // namespace
+
+extern "C" {
+
+int mct_tt2d_forward(mct_tt2d_ctx *c, int nchains, const int *ncells, const double *points, const double *params,
+                     const double *n0, const double *n1, double *out) {
+  int rc = tt2d_check(c, nchains, ncells, points, params, n0, n1, "mct_tt2d_forward");
+  if (rc) return rc;
+  if (!out) return MCT_ERR_ARG;
+  int gst[2] = {0, 0};
+  rc = tt2d_enqueue(c, nchains, ncells, points, params, n0, n1, out, gst);
+  if (rc) return rc;
+  MCT_CUDA_TRY(cudaStreamSynchronize(c->stream));
+  c->last_nchains = nchains;
+  return tt2d_status(gst, "mct_tt2d_forward");
+}
+
+int mct_tt2d_submit(mct_tt2d_ctx *c, int nchains, const int *ncells, const double *points, const double *params,
+                    const double *n0, const double *n1) {
+  int rc = tt2d_check(c, nchains, ncells, points, params, n0, n1, "mct_tt2d_submit");
+  if (rc) return rc;
+  const int ns = c->nslots;
+  const size_t pmax = (size_t)ns * c->ncell_max;
+  if (!c->h_ints) {
+    MCT_CUDA_TRY(cudaHostAlloc(&c->h_ints, sizeof(int) * (ns + 2), cudaHostAllocDefault));
+    MCT_CUDA_TRY(cudaHostAlloc(&c->h_dbl, sizeof(double) * (pmax * 5 + (size_t)ns * 8), cudaHostAllocDefault));
+    MCT_CUDA_TRY(cudaEventCreateWithFlags(&c->done, cudaEventDisableTiming));
+  }
+  const size_t npc = (size_t)nchains * c->ncell_max;
+  int *hn = c->h_ints, *hg = c->h_ints + ns;
+  double *hp = c->h_dbl, *hq = hp + pmax * 2, *h0 = hq + pmax * 3, *h1 = h0 + (size_t)ns * 2, *ho = h1 + (size_t)ns * 2;
+  std::memcpy(hn, ncells, sizeof(int) * nchains);
+  std::memcpy(hp, points, sizeof(double) * npc * 2);
+  std::memcpy(hq, params, sizeof(double) * npc * 3);
+  std::memcpy(h0, n0, sizeof(double) * 2 * nchains);
+  std::memcpy(h1, n1, sizeof(double) * 2 * nchains);
+  rc = tt2d_enqueue(c, nchains, hn, hp, hq, h0, h1, ho, hg);
+  if (rc) return rc;
+  MCT_CUDA_TRY(cudaEventRecord(c->done, c->stream));
+  c->pending = nchains;
+  return MCT_OK;
+}
+
+int mct_tt2d_poll(mct_tt2d_ctx *c, double *out, int *done) {
+  if (!c || !out || !done || !c->pending) return MCT_ERR_ARG;
+  *done = 0;
+  const cudaError_t q = cudaEventQuery(c->done);
+  if (q == cudaErrorNotReady) return MCT_OK;
+  if (q != cudaSuccess) { mct_set_error("cudaEventQuery", cudaGetErrorString(q), __FILE__, __LINE__); return MCT_ERR_CUDA; }
+  const int ns = c->nslots, n = c->pending;
+  const size_t pmax = (size_t)ns * c->ncell_max;
+  const double *ho = c->h_dbl + pmax * 5 + (size_t)ns * 4;
+  std::memcpy(out, ho, sizeof(double) * 4 * n);
+  c->pending = 0;
+  c->last_nchains = n;
+  *done = 1;
+  return tt2d_status(c->h_ints + ns, "mct_tt2d_poll");
+}
 
 int mct_tt2d_commit(mct_tt2d_ctx *c, int nchains, const int *accept) {
-  if (!c || nchains < 1 || nchains > c->last_nchains || !accept) {
+  if (!c || tt2d_busy(c, "mct_tt2d_commit")) return MCT_ERR_ARG;
+  if (nchains < 1 || nchains > c->last_nchains || !accept) {
     mct_set_error("mct_tt2d_commit", "bad arguments (commit follows a forward of at least nchains)", __FILE__,
                   __LINE__);
     return MCT_ERR_ARG;
@@ -607,7 +700,8 @@ int mct_tt2d_commit(mct_tt2d_ctx *c, int nchains, const int *accept) {
 }
 
 int mct_tt2d_noise_likelihood(mct_tt2d_ctx *c, int nchains, const double *n0, const double *n1, double *out) {
-  if (!c || nchains < 1 || nchains > c->nslots || !n0 || !n1 || !out) {
+  if (!c || tt2d_busy(c, "mct_tt2d_noise_likelihood")) return MCT_ERR_ARG;
+  if (nchains < 1 || nchains > c->nslots || !n0 || !n1 || !out) {
     mct_set_error("mct_tt2d_noise_likelihood", "bad arguments", __FILE__, __LINE__);
     return MCT_ERR_ARG;
   }
@@ -623,7 +717,7 @@ int mct_tt2d_noise_likelihood(mct_tt2d_ctx *c, int nchains, const double *n0, co
 }
 
 int mct_tt2d_phase_time(mct_tt2d_ctx *c, int index, double *phase_time) {
-  if (!c || index < 0 || index >= c->last_nchains || !phase_time) return MCT_ERR_ARG;
+  if (!c || tt2d_busy(c, "mct_tt2d_phase_time") || index < 0 || index >= c->last_nchains || !phase_time) return MCT_ERR_ARG;
   const size_t npairs = (size_t)c->dev.nsrc * c->dev.nrev;
   MCT_CUDA_TRY(cudaMemcpyAsync(phase_time, c->tt + (size_t)index * npairs, sizeof(double) * npairs,
                                cudaMemcpyDeviceToHost, c->stream));

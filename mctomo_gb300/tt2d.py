@@ -101,6 +101,25 @@ class TravelTime2DLikelihood:
                                                          ptr(n0), ptr(n1), ptr(out)))
         return out
 
+    def submit(self, ncells, points, params, n0, n1):
+        """Starts forward() without waiting; poll() collects it."""
+        ncells = np.ascontiguousarray(ncells, np.int32)
+        nch = ncells.size
+        points = np.ascontiguousarray(points, np.float64)
+        params = np.ascontiguousarray(params, np.float64)
+        n0 = np.ascontiguousarray(n0, np.float64).reshape(nch, 2)
+        n1 = np.ascontiguousarray(n1, np.float64).reshape(nch, 2)
+        check("mct_tt2d_submit", lib().mct_tt2d_submit(self.h, nch, ptr(ncells), ptr(points), ptr(params),
+                                                       ptr(n0), ptr(n1)))
+        self._pending = nch
+
+    def poll(self):
+        """(done, out): out (nchains, 4) once the submitted batch finished."""
+        out = np.zeros((self._pending, 4))
+        done = ctypes.c_int()
+        check("mct_tt2d_poll", lib().mct_tt2d_poll(self.h, ptr(out), ctypes.byref(done)))
+        return bool(done.value), (out if done.value else None)
+
     def commit(self, accept):
         """Chains with accept[c] keep the last forward as their state."""
         accept = np.ascontiguousarray(accept, np.int32)
