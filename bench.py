@@ -1097,8 +1097,14 @@ def run_served(args):
     arrivals = serving.poisson_arrivals(rng, SERVED_CONFIG["rate_chains_per_s"], dur, names)
     res = {}
     share = parse_share(args.served_sm_share)
+    slots = dict(SERVED_SLOTS)
+    for item in filter(None, args.served_slots.split(",")):
+        k, v = item.split("=")
+        if k not in slots:
+            raise SystemExit("--served-slots: unknown kind %r" % k)
+        slots[k] = int(v)
     for plain in (False, True) if not args.served_only else (False,):
-        backends, used = served_backends(plain, SERVED_SLOTS, args.served_priority, share)
+        backends, used = served_backends(plain, slots, args.served_priority, share)
         if sum(used.values()) > SERVED_CONFIG["hbm_budget_gb"] * 1e9:
             raise SystemExit("served contexts exceed the HBM budget: %s" % used)
         # one warm-up step per kind outside the stream
@@ -1125,7 +1131,7 @@ def run_served(args):
             "vs_baseline": None,
             "dtype": "f64 dispersion polish, f32 bracketing; f64 fm2d (reference order); int32 fixed-point 3D tiles",
             "data": "synthetic (seeded, shapes of configurations 1-3)",
-            "config": dict(SERVED_CONFIG, slots=SERVED_SLOTS, seconds=dur, measured_window_s=[round(warm, 1), dur],
+            "config": dict(SERVED_CONFIG, slots=slots, seconds=dur, measured_window_s=[round(warm, 1), dur],
                            arrivals=len(arrivals), high_priority_streams=args.served_priority,
                            sm_share=share or "whole device"),
             "served": sv, "plain": pl,
@@ -1317,6 +1323,7 @@ def main():
                     help="served workload: SM share of the 2D travel-time launches per kind, "
                          "e.g. tt2d=0.15,surface=0.25,joint=0.2 (none: whole device)")
     ap.add_argument("--served-only", action="store_true", help="served workload: skip the plain leg")
+    ap.add_argument("--served-slots", default="", help="served workload: slots per kind, e.g. body=48,joint=32")
     ap.add_argument("--chains2d", type=int, default=256, help="tt2d workload: chains per step")
     ap.add_argument("--columns", type=int, default=262144, help="disp workload: columns")
     ap.add_argument("--disp-sample", type=int, default=512, help="disp workload: columns checked by the oracle")
