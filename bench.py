@@ -721,10 +721,10 @@ def run_disp(args):
     cnt = torch.zeros(2, dtype=torch.int64, device=dev)
     stream = torch.cuda.current_stream()
 
-    # Rayleigh over all columns; Love over the first LOVE_COLS columns (Love
-    # waves with the first overtone faulted twice at full size; the cause is
-    # not found, so that case is not run again)
-    love_cols = min(ncol, LOVE_COLS)
+    # Rayleigh over all columns; Love over the first --love-cols columns (an
+    # earlier version of the kernel faulted twice on Love with the first
+    # overtone at full size)
+    love_cols = min(ncol, args.love_cols)
     chunk = ncol          # one launch per wave: every column's warp runs at once
 
     def study(precision):
@@ -809,7 +809,7 @@ def disp_oracle_sample(nl, thk, vp, vs, rho, periods, args):
     orc = oracle.load()
     P = lambda a: None if a is None else a.ctypes.data_as(ctypes.c_void_p)  # noqa: E731
     rng = np.random.default_rng(SEED + 4)
-    idx = np.sort(rng.choice(min(len(nl), LOVE_COLS), args.disp_sample, replace=False))
+    idx = np.sort(rng.choice(min(len(nl), args.love_cols), args.disp_sample, replace=False))
     cols = [tuple(np.ascontiguousarray(x[c, :nl[c]]) for x in (thk, vp, vs, rho)) for c in idx]
     lvl = np.array([bool(np.any(np.diff(vs[c, :nl[c]]) < 0)) for c in idx])
     threads = os.cpu_count() or 1
@@ -1327,6 +1327,7 @@ def main():
     ap.add_argument("--chains2d", type=int, default=256, help="tt2d workload: chains per step")
     ap.add_argument("--columns", type=int, default=262144, help="disp workload: columns")
     ap.add_argument("--disp-sample", type=int, default=512, help="disp workload: columns checked by the oracle")
+    ap.add_argument("--love-cols", type=int, default=LOVE_COLS, help="disp workload: columns with Love waves")
     ap.add_argument("--chains", type=int, default=32, help="body workload: chains per step")
     ap.add_argument("--order", type=int, default=0, help="body workload: eikonal order")
     ap.add_argument("--body-sample", type=int, default=2, help="body workload: proposals checked by the oracle")

@@ -421,7 +421,8 @@ int modrays_batch(int nmaps, int nsrc, const double *scx, const double *scz, int
                              rays ? sizeof(double) * 2 * (size_t)nmaps * nsrc * nrc : 0,
                              rays ? sizeof(int) * (size_t)nmaps : 0,
                              rays ? sizeof(double) * (size_t)plan.nref_max * ns : 0,
-                             rays ? sizeof(short) * (size_t)plan.nref_max * ns : 0});
+                             rays ? sizeof(short) * (size_t)plan.nref_max * ns : 0,
+                             fm2d_tws_bytes(plan, (long)ns)});
   rc = td->ws.reserve(bytes); if (rc) return rc;
   Carve cv(td->ws.p);
   double *d_velv = cv.take<double>(nv * nmaps);
@@ -450,6 +451,7 @@ int modrays_batch(int nmaps, int nsrc, const double *scx, const double *scz, int
     job.rays = 1; job.gvel = d_gvel; job.gtime = d_gt; job.raylen = d_gt + (size_t)nmaps * nsrc * nrc;
     job.crazy = d_crazy;
   }
+  fm2d_bind_tws(job, plan, (long)ns, cv.take<char>(fm2d_tws_bytes(plan, (long)ns)));
   cudaStream_t s = td->stream;
   if (rays) {
     MCT_CUDA_TRY(cudaMemcpyAsync(d_gvel, gvel, sizeof(double) * (size_t)nmaps * nvx * nvz, cudaMemcpyHostToDevice, s));

@@ -141,17 +141,21 @@ __device__ void downtree(WarpStateT<TT> &w) {
   w.S[ln] = (short)hole;
 }
 
-// Shared-memory layout of one solve: T [n], S [n], H [cap + 2] (1-based
-// heap of at most cap entries), each array starting on a 16-byte boundary.
+// Shared-memory layout of one solve: S [n], H [cap + 2] (1-based heap of at
+// most cap entries), each array starting on a 16-byte boundary. The solve's
+// time field T [n] lives in global memory (a slot of Fm2dJob::tws_ref / tws
+// per resident solve), where it stays in L1/L2: with 8 of every 10 bytes per
+// node out of shared memory, twice as many solves fit on an SM, and the
+// march is bound by the per-solve latency, which more solves per SM hide.
 __host__ __device__ __forceinline__ int align16(int b) { return (b + 15) & ~15; }
 // ... then the 8 per-case constant records of the FP64 update (CaseTab, 64 B
 // each).
 constexpr int CASE_TAB_BYTES = 8 * 64;
 constexpr int MAILBOX_BYTES = 128;   // ... and the solve's mailbox (last 128 B, see march)
 struct SolveLayout { int offS, offH, offTab, bytes; };
-__host__ __device__ __forceinline__ SolveLayout solve_layout(int tbytes, int n, int cap) {
+__host__ __device__ __forceinline__ SolveLayout solve_layout(int n, int cap) {
   SolveLayout L;
-  L.offS = align16(tbytes * n);
+  L.offS = 0;
   L.offH = L.offS + align16(2 * n);
   L.offTab = L.offH + align16(2 * (cap + 2));
   L.bytes = L.offTab + CASE_TAB_BYTES + MAILBOX_BYTES;
@@ -1010,12 +1014,12 @@ __device__ __forceinline__ Fx time_scale(const Fm2dJob &job) {
 }
 
 template <class TT>
-__device__ __forceinline__ WarpStateT<TT> warp_state(unsigned char *base, int nodes, int cap) {
+__device__ __forceinline__ WarpStateT<TT> warp_state(unsigned char *base, TT *T, int nodes, int cap) {
   WarpStateT<TT> w;
-  const SolveLayout lay = solve_layout((int)sizeof(TT), nodes, cap);
+  const SolveLayout lay = solve_layout(nodes, cap);
   w.cap = cap;
   w.overflow = false;
-  w.T = reinterpret_cast<TT *>(base);
+  w.T = T;
   w.S = reinterpret_cast<short *>(base + lay.offS);
   w.H = reinterpret_cast<unsigned short *>(base + lay.offH);
   w.tab = reinterpret_cast<CaseTab *>(base + lay.offTab);
@@ -1047,7 +1051,10 @@ __device__ __forceinline__ void refined_block(const Fm2dJob &job, int solve_byte
   const bool active = solve < job.nsolve && solve_geom(job, solve, sg);   // geometry errors: coarse stage
   if (!__any_sync(0xffffffffu, active)) return;   // the same for both warps of the pair
   unsigned char *base = smem + ((size_t)pair * SPW + slot) * solve_bytes;
-  WarpStateT<TT> w = warp_state<TT>(base, job.nref_max, heap_cap);
+  // the time-field slot of this solve's place in the grid (block, pair, slot)
+  const size_t tslot = ((size_t)blockIdx.x * (blockDim.x >> 6) + pair) * SPW + slot;
+  WarpStateT<TT> w = warp_state<TT>(base, reinterpret_cast<TT *>(job.tws_ref) + tslot * job.nref_max,
+                                    job.nref_max, heap_cap);
   Mailbox<TT> *mb = reinterpret_cast<Mailbox<TT> *>(base + solve_bytes - MAILBOX_BYTES);
   const Fx fx = time_scale<TT>(job);
   const int sgdl = job.sgdl;
@@ -1107,24 +1114,18 @@ __device__ __forceinline__ void refined_block(const Fm2dJob &job, int solve_byte
   }
 }
 
-// One logical block per block (WALK false), or (WALK true) a grid of at
-// most nblk blocks, each walking logical blocks blockIdx.x, blockIdx.x +
-// gridDim.x, ... below nblk, so that a grid smaller than nblk keeps the
-// kernel to a share of the SMs. Both warps of a pair meet at the pair's
-// barrier before the next logical block reuses the pair's shared memory. The
-// walk is a separate instantiation: in a loop the compiler keeps more of the
-// job in registers, which costs the single-pass kernel its register budget.
-template <class TT, int SPW, bool WALK>
+// A persistent grid: at most as many blocks as are resident at once (fewer
+// with an SM share), each walking logical blocks blockIdx.x, blockIdx.x +
+// gridDim.x, ... below nblk, with the time-field slots of its own place in
+// the grid. Both warps of a pair meet at the pair's barrier before the next
+// logical block reuses the pair's shared memory and slots.
+template <class TT, int SPW>
 __global__ void __launch_bounds__(64 * PAIRS_MAX)
 fm2d_refined_kernel(Fm2dJob job, int solve_bytes, int heap_cap, int redo, int nblk) {
-  if constexpr (WALK) {
-    const int bar1 = 1 + 2 * (threadIdx.x >> 6);
-    for (int blk = blockIdx.x; blk < nblk; blk += gridDim.x) {
-      if (blk != (int)blockIdx.x) { __syncwarp(); pair_sync(bar1); }
-      refined_block<TT, SPW>(job, solve_bytes, heap_cap, redo, blk);
-    }
-  } else {
-    refined_block<TT, SPW>(job, solve_bytes, heap_cap, redo, blockIdx.x);
+  const int bar1 = 1 + 2 * (threadIdx.x >> 6);
+  for (int blk = blockIdx.x; blk < nblk; blk += gridDim.x) {
+    if (blk != (int)blockIdx.x) { __syncwarp(); pair_sync(bar1); }
+    refined_block<TT, SPW>(job, solve_bytes, heap_cap, redo, blk);
   }
 }
 
@@ -1296,7 +1297,9 @@ __device__ __forceinline__ void coarse_block(const Fm2dJob &job, int solve_bytes
   const Grid2 gc = sg.gc;
   const int nnx = active ? gc.nnx : 0, nnz = active ? gc.nnz : 0;
   unsigned char *base = smem + ((size_t)pair * SPW + slot) * solve_bytes;
-  WarpStateT<TT> w = warp_state<TT>(base, nnx * nnz, nnx * nnz);
+  const size_t tslot = ((size_t)blockIdx.x * (blockDim.x >> 6) + pair) * SPW + slot;
+  WarpStateT<TT> w = warp_state<TT>(base, reinterpret_cast<TT *>(job.tws) + tslot * job.nodes_max, nnx * nnz,
+                                    nnx * nnz);
   Mailbox<TT> *mb = reinterpret_cast<Mailbox<TT> *>(base + solve_bytes - MAILBOX_BYTES);
   const Fx fx = time_scale<TT>(job);
   const int map = active ? sg.map : 0, src = active ? sg.src : 0;
@@ -1412,18 +1415,14 @@ __device__ __forceinline__ void coarse_block(const Fm2dJob &job, int solve_bytes
   if (job.rays) trace_rays(job, w, fx, sg, solve, sub, NSUB);
 }
 
-// Logical blocks as fm2d_refined_kernel has them.
-template <class TT, int SPW, bool WALK>
+// The persistent grid of fm2d_refined_kernel.
+template <class TT, int SPW>
 __global__ void __launch_bounds__(64 * PAIRS_MAX)
 fm2d_coarse_kernel(Fm2dJob job, int solve_bytes, int nblk) {
-  if constexpr (WALK) {
-    const int bar1 = 1 + 2 * (threadIdx.x >> 6);
-    for (int blk = blockIdx.x; blk < nblk; blk += gridDim.x) {
-      if (blk != (int)blockIdx.x) { __syncwarp(); pair_sync(bar1); }
-      coarse_block<TT, SPW>(job, solve_bytes, blk);
-    }
-  } else {
-    coarse_block<TT, SPW>(job, solve_bytes, blockIdx.x);
+  const int bar1 = 1 + 2 * (threadIdx.x >> 6);
+  for (int blk = blockIdx.x; blk < nblk; blk += gridDim.x) {
+    if (blk != (int)blockIdx.x) { __syncwarp(); pair_sync(bar1); }
+    coarse_block<TT, SPW>(job, solve_bytes, blk);
   }
 }
 
@@ -1471,7 +1470,7 @@ namespace {
 // keeps five refined boxes resident per SM (two would share each FP64
 // instruction but fit only four); the coarse stage's ten resident solves
 // share their update warps in twos.
-int g_spw_refined = 1, g_spw_coarse = 2;
+int g_spw_refined = 2, g_spw_coarse = 2;
 }  // namespace
 
 // Diagnostics (not part of the public header): solves per warp pair (1 or 2)
@@ -1572,7 +1571,6 @@ int fm2d_plan(const Fm2dJob &job, Fm2dPlan *plan) {
   int nodes_max = nodes > nref ? nodes : nref;
   if (nodes_max > 32000) return MCT_ERR_ARG;   // int16 heap positions / node ids
   if (nnx > 256 || nnz > 256 || (job.asgr == 1 && 2 * job.sgs * job.sgdl + 1 > 256)) return MCT_ERR_ARG;
-  const int tbytes = job.precision == 2 ? (int)sizeof(int) : (int)sizeof(double);
   plan->nodes_max = nodes_max;
   plan->nref_max = nref;
   plan->nref_map = 0;
@@ -1584,41 +1582,65 @@ int fm2d_plan(const Fm2dJob &job, Fm2dPlan *plan) {
     plan->nref_map = (int)(nrx * nrz);
   }
   plan->map_tmp_max = tmp;
-  plan->warp_bytes = solve_layout(tbytes, nodes, nodes).bytes;
+  plan->warp_bytes = solve_layout(nodes, nodes).bytes;
   plan->ref_heap_cap = nref < g_ref_heap_cap ? nref : g_ref_heap_cap;
-  plan->ref_warp_bytes = nref > 0 ? solve_layout(tbytes, nref, plan->ref_heap_cap).bytes : 0;
-  plan->ref_full_warp_bytes = nref > 0 ? solve_layout(tbytes, nref, nref).bytes : 0;
+  plan->ref_warp_bytes = nref > 0 ? solve_layout(nref, plan->ref_heap_cap).bytes : 0;
+  plan->ref_full_warp_bytes = nref > 0 ? solve_layout(nref, nref).bytes : 0;
   if (plan->warp_bytes > 227 * 1024 || plan->ref_full_warp_bytes > 227 * 1024) return MCT_ERR_ARG;
+  plan->tbytes = job.precision == 2 ? (int)sizeof(int) : (int)sizeof(double);
+  // time-field slots: a bound on the solves resident at once, from the
+  // shared memory per solve (228 KB per SM) and the threads per SM (2,048:
+  // 32 warp pairs of at most two solves), times the device's SM count (a
+  // 152-SM GB300 when no device is visible, for sizing without one)
+  int sms = 152, dev = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess || cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) !=
+                                                cudaSuccess) {
+    cudaGetLastError();
+    sms = 152;
+  }
+  auto per_sm = [](int bytes) { return bytes > 0 ? std::min(228 * 1024 / bytes, 64) : 0; };
+  plan->tslots = sms * per_sm(plan->warp_bytes);
+  plan->tslots_ref = nref > 0 ? sms * per_sm(plan->ref_warp_bytes) : 0;
   return MCT_OK;
 }
 
+size_t fm2d_tws_bytes(const Fm2dPlan &plan, long nsolve_max) {
+  const long r = std::min<long>(plan.tslots_ref, nsolve_max + 32), c = std::min<long>(plan.tslots, nsolve_max + 32);
+  const size_t ref = ((size_t)r * plan.nref_max * plan.tbytes + 255) & ~size_t(255);
+  return ref + (size_t)c * plan.nodes_max * plan.tbytes;
+}
+
+void fm2d_bind_tws(Fm2dJob &job, const Fm2dPlan &plan, long nsolve_max, void *mem) {
+  const long r = std::min<long>(plan.tslots_ref, nsolve_max + 32), c = std::min<long>(plan.tslots, nsolve_max + 32);
+  const size_t ref = ((size_t)r * plan.nref_max * plan.tbytes + 255) & ~size_t(255);
+  job.tws_ref = mem;
+  job.tslots_ref = plan.nref_max > 0 ? (int)r : 0;
+  job.tws = static_cast<char *>(mem) + ref;
+  job.tslots = (int)c;
+}
+
 namespace {
-// Blocks to launch for nblk logical blocks of kernel k: with a share in
-// (0, 1) of the device, share x SM count (rounded, at least one) x the
-// kernel's resident blocks per SM, so that the launch leaves the other SMs to
-// other streams' kernels for its whole duration; *grid = nblk when that is
-// not fewer.
+// Blocks to launch for nblk logical blocks of kernel k: the blocks resident
+// at once on the device, or with a share in (0, 1) on share x the SM count
+// (rounded, at least one), so that the launch leaves the other SMs to other
+// streams' kernels for its whole duration; at most nblk.
 template <class K>
 int grid_for(K k, int nblk, int threads, size_t smem, double share, int *grid) {
   int dev = 0, sms = 0, occ = 0;
   MCT_CUDA_TRY(cudaGetDevice(&dev));
   MCT_CUDA_TRY(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
   MCT_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k, threads, smem));
-  const int nsm = std::max(1, (int)(share * sms + 0.5));
+  const int nsm = share > 0.0 && share < 1.0 ? std::max(1, (int)(share * sms + 0.5)) : sms;
   const long cap = (long)nsm * std::max(occ, 1);
   *grid = cap < nblk ? (int)cap : nblk;
   return MCT_OK;
 }
 
-bool shared_out(double share) { return share > 0.0 && share < 1.0; }
-
-// The walking instantiations exist for the default warp layouts (refined
-// SPW 1, coarse SPW 2); other layouts run on the whole device.
+// A launch's blocks also stay within the job's time-field slots (a block
+// uses the slots of its place in the grid).
 template <class TT, int SPW>
 int launch_refined(const Fm2dJob &job, int solve_bytes, int heap_cap, int redo, double share, cudaStream_t s) {
-  constexpr bool kWalk = SPW == 1;
-  const bool walk = kWalk && shared_out(share);
-  auto kern = walk ? fm2d_refined_kernel<TT, SPW, kWalk> : fm2d_refined_kernel<TT, SPW, false>;
+  auto kern = fm2d_refined_kernel<TT, SPW>;
   int rc = mct_smem_attr(kern, 227 * 1024);
   if (rc) return rc;
   const int ppb = pairs_for(kern, SPW * solve_bytes);
@@ -1627,7 +1649,9 @@ int launch_refined(const Fm2dJob &job, int solve_bytes, int heap_cap, int redo, 
   const int nblk = (job.nsolve + per_block - 1) / per_block;
   const size_t smem = (size_t)per_block * solve_bytes;
   int grid = nblk;
-  if (walk && (rc = grid_for(kern, nblk, 64 * ppb, smem, share, &grid))) return rc;
+  if ((rc = grid_for(kern, nblk, 64 * ppb, smem, share, &grid))) return rc;
+  grid = std::min(grid, job.tslots_ref / per_block);
+  if (grid < 1 || !job.tws_ref) return MCT_ERR_ARG;
   kern<<<grid, 64 * ppb, smem, s>>>(job, solve_bytes, heap_cap, redo, nblk);
   MCT_CUDA_TRY(cudaGetLastError());
   return MCT_OK;
@@ -1635,9 +1659,7 @@ int launch_refined(const Fm2dJob &job, int solve_bytes, int heap_cap, int redo, 
 
 template <class TT, int SPW>
 int launch_coarse(const Fm2dJob &job, int solve_bytes, double share, cudaStream_t s) {
-  constexpr bool kWalk = SPW == 2;
-  const bool walk = kWalk && shared_out(share);
-  auto kern = walk ? fm2d_coarse_kernel<TT, SPW, kWalk> : fm2d_coarse_kernel<TT, SPW, false>;
+  auto kern = fm2d_coarse_kernel<TT, SPW>;
   int rc = mct_smem_attr(kern, 227 * 1024);
   if (rc) return rc;
   const int ppb = pairs_for(kern, SPW * solve_bytes);
@@ -1646,7 +1668,9 @@ int launch_coarse(const Fm2dJob &job, int solve_bytes, double share, cudaStream_
   const int nblk = (job.nsolve + per_block - 1) / per_block;
   const size_t smem = (size_t)per_block * solve_bytes;
   int grid = nblk;
-  if (walk && (rc = grid_for(kern, nblk, 64 * ppb, smem, share, &grid))) return rc;
+  if ((rc = grid_for(kern, nblk, 64 * ppb, smem, share, &grid))) return rc;
+  grid = std::min(grid, job.tslots / per_block);
+  if (grid < 1 || !job.tws) return MCT_ERR_ARG;
   kern<<<grid, 64 * ppb, smem, s>>>(job, solve_bytes, nblk);
   MCT_CUDA_TRY(cudaGetLastError());
   return MCT_OK;

@@ -37,6 +37,12 @@ struct Fm2dJob {
   int trace_solve; int *trace_i; double *trace_t; int trace_max;
   // from fm2d_plan
   int nodes_max, nref_max, map_tmp_max, nref_map;
+  // time fields of the solves in flight (fm2d_bind_tws): [tslots_ref][nref_max]
+  // and [tslots][nodes_max] elements of the precision's time type (int for
+  // precision 2, 8 bytes otherwise); a block's solves use the slots of its
+  // place in the grid
+  void *tws_ref, *tws;
+  int tslots_ref, tslots;
 };
 
 struct Fm2dPlan {
@@ -46,10 +52,16 @@ struct Fm2dPlan {
   int ref_heap_cap;          // heap entries of the refined source-box stage (asgr = 1)
   int ref_warp_bytes;        // shared memory per solve of that stage
   int ref_full_warp_bytes;   // the same with a heap as large as the box (overflow pass)
+  int tbytes;                // bytes of one time value
+  int tslots, tslots_ref;    // the most solves resident at once per stage
   // launch policy, not set by fm2d_plan: the share of the device's SMs the
   // solve kernels may hold at once (0 or >= 1: all)
   double sm_share = 0.0;
 };
 
 int fm2d_plan(const Fm2dJob &job, Fm2dPlan *plan);
+// Device memory of the time-field slots for at most nsolve_max solves per
+// launch, and the binding of such a block (256-byte aligned) to a job.
+size_t fm2d_tws_bytes(const Fm2dPlan &plan, long nsolve_max);
+void fm2d_bind_tws(Fm2dJob &job, const Fm2dPlan &plan, long nsolve_max, void *mem);
 int launch_fm2d(const Fm2dJob &job, const Fm2dPlan &plan, cudaStream_t s);

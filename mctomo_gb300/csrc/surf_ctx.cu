@@ -129,7 +129,9 @@ int surf_create(const mct_grid *g, const mct_surf_settings *st, const mct_surf_d
       sizeof(double) * (size_t)nslots * np * npairs,
       (b.igr && !b.straight) ? sizeof(double) * (size_t)fp.nref_max * nsolve : 0,
       (b.igr && !b.straight) ? sizeof(short) * (size_t)fp.nref_max * nsolve : 0,
-      sizeof(int) * (size_t)nslots * ncol};
+      sizeof(int) * (size_t)nslots * ncol,
+      // fm2d time-field slots
+      fm2d_tws_bytes(fp, (long)nsolve)};
   size_t total = 0;
   for (size_t s : sz) total = ((total + 255) & ~size_t(255)) + s;
   total += 256;
@@ -212,6 +214,7 @@ int surf_create(const mct_grid *g, const mct_surf_settings *st, const mct_surf_d
   fj.ref_t = cv.take<double>((b.igr && !b.straight) ? (size_t)fp.nref_max * nsolve : 0);
   fj.ref_s = cv.take<short>((b.igr && !b.straight) ? (size_t)fp.nref_max * nsolve : 0);
   b.lorder = cv.take<int>((size_t)nslots * ncol);
+  fm2d_bind_tws(fj, fp, (long)nsolve, cv.take<char>(fm2d_tws_bytes(fp, (long)nsolve)));
   b.sdist = sdist;
   c->plan.src_xy = sxy; c->plan.rev_xy = sxy + 2 * nsrc;
   {

@@ -415,7 +415,8 @@ int mct_tt2d_create(const mct_grid *g, const mct_tt2d_settings *st, const mct_tt
       fm ? sizeof(int2) * nsolve : 0, fm ? sizeof(double) * (size_t)c->fp.nref_map * nslots : 0,
       fm ? sizeof(double) * (size_t)c->fp.map_tmp_max * nsolve : 0,
       fm ? sizeof(short) * (size_t)c->fp.map_tmp_max * nsolve : 0, sizeof(int) * (nsolve + 1),
-      fm ? sizeof(double) * 2 * (size_t)nnx * nnz * nslots : 0, sizeof(int)};
+      fm ? sizeof(double) * 2 * (size_t)nnx * nnz * nslots : 0, sizeof(int),
+      fm ? fm2d_tws_bytes(c->fp, (long)nsolve) : 0};
   size_t total = 0;
   for (size_t b : sz) total = ((total + 255) & ~size_t(255)) + b;
   total += 256;
@@ -461,6 +462,7 @@ int mct_tt2d_create(const mct_grid *g, const mct_tt2d_settings *st, const mct_tt
   fj.veln = cv.take<double>(fm ? 2 * (size_t)nnx * nnz * nslots : 0);
   fj.slon = fj.veln + (size_t)nnx * nnz * nslots;
   fj.vmin_bits = cv.take<int>(1);
+  if (fm) fm2d_bind_tws(fj, c->fp, (long)nsolve, cv.take<char>(fm2d_tws_bytes(c->fp, (long)nsolve)));
   // data in the reference's layouts
   std::vector<double> pd(5 * (size_t)npairs, 1.0), xy(2 * (size_t)(nsrc + nrev)), sep(2 * (size_t)(nsrc + nrev));
   std::vector<int2> pairs((size_t)std::max(ndd, 1), make_int2(0, 0));
