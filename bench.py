@@ -1006,7 +1006,11 @@ SERVED_CONFIG = {
                 "1,000 proposals per chain, device-resident state, slots sized within a 150 GB budget, "
                 "chains evicted on completion",
     "rate_chains_per_s": 40.0, "proposals_per_chain": 1000, "hbm_budget_gb": 150}
-SERVED_SLOTS = {"tt2d": 256, "surface": 64, "body": 32, "joint": 16}
+SERVED_SLOTS = {"tt2d": 256, "surface": 64, "body": 32, "joint": 32}
+# SM shares of the 2D travel-time launches per kind in the batched mode: the
+# fm2d grids are persistent, so without a share each launch holds every SM
+# until its last block, and the body kinds' 3D passes wait behind it
+SERVED_SM_SHARE = "tt2d=0.15,surface=0.25,joint=0.1"
 
 
 def served_backends(single, slots, priority="none", share=None):
@@ -1319,7 +1323,7 @@ def main():
     ap.add_argument("--served-seconds", type=float, default=60.0, help="served workload: stream length (s)")
     ap.add_argument("--served-priority", default="none", choices=["none", "body", "body+joint"],
                     help="served workload: contexts whose streams run at the device's highest priority")
-    ap.add_argument("--served-sm-share", default="none",
+    ap.add_argument("--served-sm-share", default=SERVED_SM_SHARE,
                     help="served workload: SM share of the 2D travel-time launches per kind, "
                          "e.g. tt2d=0.15,surface=0.25,joint=0.2 (none: whole device)")
     ap.add_argument("--served-only", action="store_true", help="served workload: skip the plain leg")
