@@ -34,10 +34,10 @@ ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, ROOT)
 
 # DRAM bytes (read + write) of the fm2d stage of one forward of the surface
-# workload below (refine_slowness 0.223 GB, refined solves 0.421 GB, coarse
-# solves 0.169 GB), measured with ncu's one-pass dram__bytes_read.sum and
+# workload below (refine_slowness 0.223 GB, refined solves 1.510 GB, coarse
+# solves 0.220 GB), measured with ncu's one-pass dram__bytes_read.sum and
 # dram__bytes_write.sum over the stage's launches of the bench's first forward
-FM2D_DRAM_BYTES_PER_FORWARD = 0.813e9
+FM2D_DRAM_BYTES_PER_FORWARD = 1.953e9
 NCHAINS = 64
 NCELL_MAX = 400
 SEED = 20261203
@@ -285,12 +285,13 @@ def run_gpu(args):
                      "traffic": traffic,
                      # what actually limits the stage (HBM is ~0 % busy): the
                      # latency of the reference's sequential heap march, one
-                     # node after another per solve; ncu on the small fm2d
-                     # case (profiles/fm2d_fp64_warp_pairs_16maps_49sources.md)
+                     # node after another per solve; ncu --set full on the
+                     # small fm2d case (--case fm2d --case-precision 0
+                     # --case-maps 64: 3,136 solves)
                      "limiter": "latency of the sequential heap march (heap warp + FP64 update warp per solve)",
-                     "ncu_small_case": {"issue_active": {"coarse": 0.262, "refined": 0.220},
-                                        "fp64_pipe_active": {"coarse": 0.417, "refined": 0.336},
-                                        "dram_throughput": 0.0}},
+                     "ncu_small_case": {"issue_active": {"coarse": 0.270, "refined": 0.257},
+                                        "fp64_pipe_active": {"coarse": 0.430, "refined": 0.385},
+                                        "resident_solves_per_sm": 16, "dram_throughput": 0.001}},
         "gpu_launches": int(launches.value),
         "clocks": cl,
         "valid_models": int((out[:, 3] == 0).sum()),
