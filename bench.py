@@ -503,6 +503,103 @@ BODY_SOLVERS = {
 }
 
 
+DROPIN_CONFIG = {"workload": "the reference's body-wave loop with the per-solve drop-in: per proposal, "
+                             "kdtree_to_grid (mct_kdtree_to_grid) then one fastMarching3D call "
+                             "(mct_fast_marching3d) per station and phase from a pool of host threads, as the "
+                             "reference's OpenMP loop over stations; 101x101x51 grid over 50x50x25 km, 200 events, "
+                             "60 stations, P and S (120 solves per proposal)",
+                 "grid": [101, 101, 51], "events": 200, "stations": 60, "phases": 2}
+
+
+def run_dropin(args):
+    """Configuration 3 through the literal drop-in (src/likelihood_body.F90:
+    204-224): each proposal grids the chain's model with mct_kdtree_to_grid
+    and makes one mct_fast_marching3d call per station and phase from a pool
+    of args.dropin_threads host threads (each thread has its own stream and
+    workspace in the library). The oracle runs the same proposals on the
+    host cores (the reference's SFMM restated) for the CPU column and the
+    accuracy check."""
+    import concurrent.futures as cf
+    import torch
+    from mctomo_gb300 import fast_marching3d, forward, synthetic
+    rng = np.random.default_rng(SEED + 1)
+    grid, settings, data, ev = synthetic.body_workload(rng)
+    settings["order"] = args.order
+    nx, ny, nz = grid["nx"], grid["ny"], grid["nz"]
+    h = (grid["dx"], grid["dy"], grid["dz"] / grid["scaling"])
+    lo3 = (grid["xmin"], grid["ymin"], grid["zmin"] / grid["scaling"])
+    rev = np.asarray(data["rev"]); locs = np.ascontiguousarray(ev[:, :3])
+    npp = settings["np"]
+    lo = np.zeros(3); hi = np.array([50.0, 50.0, 25.0])
+    ncell_max = 800
+    props = []
+    for _ in range(args.warmup + args.steps):
+        n = int(rng.integers(20, ncell_max + 1))
+        p, q = synthetic.voronoi_model_3d(rng, n, lo, hi, (3.0 / 1.73, 7.5 / 1.73))
+        q[:, 0] = q[:, 1] * 1.73
+        props.append((n, p, q))
+    threads = args.dropin_threads
+    solver = None if args.order == 1 else "tiles"
+
+    def proposal(n, p, q):
+        _, vp, vs, _ = forward.kdtree_to_grid(p, q, nx, ny, nz, (grid["xmin"], grid["ymin"], grid["zmin"]),
+                                              (grid["dx"], grid["dy"], grid["dz"]))
+        vels = (vp, vs)
+        pt = np.zeros((npp, data["nsrc"], len(rev)))
+
+        def solve(job):
+            ph, k = job
+            pt[ph, :, k] = fast_marching3d(vels[ph], h, lo3, rev[k], locs, order=args.order, solver=solver)
+
+        with cf.ThreadPoolExecutor(threads) as ex:
+            list(ex.map(solve, [(ph, k) for ph in range(npp) for k in range(len(rev))]))
+        return pt
+
+    for i in range(args.warmup):
+        proposal(*props[i])
+    torch.cuda.synchronize()
+    clocks = Clocks(0)
+    clocks.start()
+    ms, pts = [], []
+    for i in range(args.warmup, args.warmup + args.steps):
+        t0 = time.perf_counter()
+        pts.append(proposal(*props[i]))
+        ms.append((time.perf_counter() - t0) * 1e3)
+    cl = clocks.stop()
+    value = 1e3 * len(ms) / sum(ms)
+    line = {"metric": "proposal evals/s through the per-solve drop-in (fastMarching3D per station and phase "
+                      "from %d host threads)" % threads,
+            "value": round(value, 4), "unit": "proposal evals/s", "n_gpus": 1, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": round(sum(ms) / len(ms), 3), "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None,
+            "dtype": "f32 local solves on int32 fixed-point times (tile solver)" if args.order == 0 else
+                     "f64 heap march in the reference's operation order",
+            "data": "synthetic (seeded, shapes of the configuration)",
+            "config": dict(DROPIN_CONFIG, order=args.order, host_threads=threads),
+            "e2e": {"value": round(value, 4), "unit": "proposal evals/s",
+                    "h2d_bytes_per_step": int(npp * len(rev) * (nx * ny * nz * 8 + 24 + len(ev) * 24)),
+                    "d2h_bytes_per_step": int(npp * len(rev) * len(ev) * 8)},
+            "p50_ms": round(float(np.percentile(ms, 50)), 3), "p99_ms": round(float(np.percentile(ms, 99)), 3),
+            "gpu_launches": None, "clocks": cl}
+    if not args.no_cpu:
+        k = args.warmup
+        n, p, q = props[k]
+        ept, _, dt = body_oracle_proposal(grid, settings, data, ev, n, p, q, np.zeros(npp), np.full(npp, 0.05),
+                                          os.cpu_count() or 1)
+        line["cpu_baseline"] = {"value": round(1.0 / dt, 4), "unit": "proposal evals/s",
+                                "cores": os.cpu_count() or 1, "kind": "reference",
+                                "sample": "1 proposal: kd-tree gridding + 120 fastMarching3D solves (the "
+                                          "reference's SFMM restated bit-exactly) on a thread pool over all host "
+                                          "cores, misfit"}
+        rays = np.asarray(data["raystat"]).reshape(ept.shape) == 1
+        e = np.abs(pts[0] - ept)[rays]
+        line["accuracy"] = {"proposals_checked": 1, "times_checked": int(e.size), "max_ttime_err_s": float(e.max()),
+                            "p99_ttime_err_s": float(np.quantile(e, 0.99)),
+                            "frac_times_within_1e-4_s": float(np.mean(e <= 1e-4)),
+                            "reference": "oracle restatement of the reference's fastMarching3D (FP64)"}
+    print(json.dumps(line), flush=True)
+
+
 def run_body(args):
     """The body-wave configuration: every step is one full proposal per chain
     (gridding, 120 3D solves, misfit) through the host API."""
@@ -1320,7 +1417,8 @@ def main():
     ap.add_argument("--tt-precision", type=int, default=0,
                     help="surface workload: fm2d arithmetic (0 FP64 exact, 1 double-float, 2 fixed point)")
     ap.add_argument("--no-variant", action="store_true", help="surface workload: skip the double-float variant")
-    ap.add_argument("--workload", default="surface", choices=["surface", "body", "disp", "tt2d", "served"])
+    ap.add_argument("--workload", default="surface",
+                    choices=["surface", "body", "disp", "tt2d", "served", "dropin"])
     ap.add_argument("--served-seconds", type=float, default=60.0, help="served workload: stream length (s)")
     ap.add_argument("--served-priority", default="none", choices=["none", "body", "body+joint"],
                     help="served workload: contexts whose streams run at the device's highest priority")
@@ -1336,6 +1434,7 @@ def main():
     ap.add_argument("--chains", type=int, default=32, help="body workload: chains per step")
     ap.add_argument("--order", type=int, default=0, help="body workload: eikonal order")
     ap.add_argument("--body-sample", type=int, default=2, help="body workload: proposals checked by the oracle")
+    ap.add_argument("--dropin-threads", type=int, default=16, help="dropin workload: host threads")
     ap.add_argument("--solver", default=None, choices=["tiles", "heap"],
                     help="body workload: 3D solver (default: heap march for order 1, tiles for order 0)")
     ap.add_argument("--case", default=None, choices=["fm2d", "eik3", "eik3heap", "disp", "grid", "tiles"],
@@ -1351,11 +1450,13 @@ def main():
     if args.case:
         run_case(args)
         return
-    if args.workload in ("body", "disp", "tt2d", "served"):
+    if args.workload in ("body", "disp", "tt2d", "served", "dropin"):
         if args.impl == "reference":
             print(json.dumps({"impl": "reference", "unavailable": "the reference arm times the surface workload"}))
         elif args.workload == "served":
             run_served(args)
+        elif args.workload == "dropin":
+            run_dropin(args)
         elif args.workload == "body":
             run_body(args)
         elif args.workload == "disp":
