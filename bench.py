@@ -773,7 +773,6 @@ def body_cpu_and_accuracy(lk, grid, settings, data, ev, prop, locs, n0, n1, chai
     return (cpu if with_cpu else None), acc
 
 
-LOVE_COLS = 16384
 # FP64 operations (add, sub, mul, div, sqrt) of one layer iteration of the
 # period equation, counted from the source (surfdisp96.f:1119-1217 with var
 # 1220-1337, dnka 1370-1414, normc 1341-1366 for Rayleigh; dltar1
@@ -819,10 +818,9 @@ def run_disp(args):
     cnt = torch.zeros(2, dtype=torch.int64, device=dev)
     stream = torch.cuda.current_stream()
 
-    # Rayleigh over all columns; Love over the first --love-cols columns (an
-    # earlier version of the kernel faulted twice on Love with the first
-    # overtone at full size)
-    love_cols = min(ncol, args.love_cols)
+    # Rayleigh over all columns; Love over the first --love-cols columns (all
+    # by default)
+    love_cols = min(ncol, args.love_cols) if args.love_cols else ncol
     chunk = ncol          # one launch per wave: every column's warp runs at once
 
     def study(precision):
@@ -907,7 +905,7 @@ def disp_oracle_sample(nl, thk, vp, vs, rho, periods, args):
     orc = oracle.load()
     P = lambda a: None if a is None else a.ctypes.data_as(ctypes.c_void_p)  # noqa: E731
     rng = np.random.default_rng(SEED + 4)
-    idx = np.sort(rng.choice(min(len(nl), args.love_cols), args.disp_sample, replace=False))
+    idx = np.sort(rng.choice(min(len(nl), args.love_cols or len(nl)), args.disp_sample, replace=False))
     cols = [tuple(np.ascontiguousarray(x[c, :nl[c]]) for x in (thk, vp, vs, rho)) for c in idx]
     lvl = np.array([bool(np.any(np.diff(vs[c, :nl[c]]) < 0)) for c in idx])
     threads = os.cpu_count() or 1
@@ -1430,7 +1428,7 @@ def main():
     ap.add_argument("--chains2d", type=int, default=256, help="tt2d workload: chains per step")
     ap.add_argument("--columns", type=int, default=262144, help="disp workload: columns")
     ap.add_argument("--disp-sample", type=int, default=512, help="disp workload: columns checked by the oracle")
-    ap.add_argument("--love-cols", type=int, default=LOVE_COLS, help="disp workload: columns with Love waves")
+    ap.add_argument("--love-cols", type=int, default=0, help="disp workload: columns with Love waves (0: all)")
     ap.add_argument("--chains", type=int, default=32, help="body workload: chains per step")
     ap.add_argument("--order", type=int, default=0, help="body workload: eikonal order")
     ap.add_argument("--body-sample", type=int, default=2, help="body workload: proposals checked by the oracle")
