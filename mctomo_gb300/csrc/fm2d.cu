@@ -153,13 +153,18 @@ __host__ __device__ __forceinline__ int align16(int b) { return (b + 15) & ~15; 
 constexpr int CASE_TAB_BYTES = 8 * 64;
 constexpr int MAILBOX_BYTES = 128;   // ... and the solve's mailbox (last 128 B, see march)
 struct SolveLayout { int offS, offH, offTab, bytes; };
-__host__ __device__ __forceinline__ SolveLayout solve_layout(int n, int cap) {
+__host__ __device__ __forceinline__ SolveLayout solve_layout(int n, int cap, bool sglobal) {
   SolveLayout L;
   L.offS = 0;
-  L.offH = L.offS + align16(2 * n);
+  L.offH = sglobal ? 0 : L.offS + align16(2 * n);
   L.offTab = L.offH + align16(2 * (cap + 2));
   L.bytes = L.offTab + CASE_TAB_BYTES + MAILBOX_BYTES;
   return L;
+}
+// A time-field slot of n nodes: the times (elements of T bytes), then, when
+// the node states are kept in global memory too, the states (int16).
+__host__ __device__ __forceinline__ size_t slot_bytes(int n, int tbytes, bool sglobal) {
+  return (((size_t)n * tbytes + 15) & ~size_t(15)) + (sglobal ? (((size_t)n * 2 + 15) & ~size_t(15)) : 0);
 }
 // Heap capacity of the refined source-box stage. The heap holds the narrow
 // band, a closed front around the source (a few hundred nodes on the largest
@@ -1014,13 +1019,15 @@ __device__ __forceinline__ Fx time_scale(const Fm2dJob &job) {
 }
 
 template <class TT>
-__device__ __forceinline__ WarpStateT<TT> warp_state(unsigned char *base, TT *T, int nodes, int cap) {
+__device__ __forceinline__ WarpStateT<TT> warp_state(unsigned char *base, char *slot, int nmax, bool sglobal,
+                                                     int nodes, int cap) {
   WarpStateT<TT> w;
-  const SolveLayout lay = solve_layout(nodes, cap);
+  const SolveLayout lay = solve_layout(nodes, cap, sglobal);
   w.cap = cap;
   w.overflow = false;
-  w.T = T;
-  w.S = reinterpret_cast<short *>(base + lay.offS);
+  w.T = reinterpret_cast<TT *>(slot);
+  w.S = sglobal ? reinterpret_cast<short *>(slot + slot_bytes(nmax, (int)sizeof(TT), false))
+                : reinterpret_cast<short *>(base + lay.offS);
   w.H = reinterpret_cast<unsigned short *>(base + lay.offH);
   w.tab = reinterpret_cast<CaseTab *>(base + lay.offTab);
   w.ntr = 0;
@@ -1053,8 +1060,9 @@ __device__ __forceinline__ void refined_block(const Fm2dJob &job, int solve_byte
   unsigned char *base = smem + ((size_t)pair * SPW + slot) * solve_bytes;
   // the time-field slot of this solve's place in the grid (block, pair, slot)
   const size_t tslot = ((size_t)blockIdx.x * (blockDim.x >> 6) + pair) * SPW + slot;
-  WarpStateT<TT> w = warp_state<TT>(base, reinterpret_cast<TT *>(job.tws_ref) + tslot * job.nref_max,
-                                    job.nref_max, heap_cap);
+  WarpStateT<TT> w = warp_state<TT>(
+      base, static_cast<char *>(job.tws_ref) + tslot * slot_bytes(job.nref_max, (int)sizeof(TT), job.sglobal_ref),
+      job.nref_max, job.sglobal_ref, job.nref_max, heap_cap);
   Mailbox<TT> *mb = reinterpret_cast<Mailbox<TT> *>(base + solve_bytes - MAILBOX_BYTES);
   const Fx fx = time_scale<TT>(job);
   const int sgdl = job.sgdl;
@@ -1298,8 +1306,9 @@ __device__ __forceinline__ void coarse_block(const Fm2dJob &job, int solve_bytes
   const int nnx = active ? gc.nnx : 0, nnz = active ? gc.nnz : 0;
   unsigned char *base = smem + ((size_t)pair * SPW + slot) * solve_bytes;
   const size_t tslot = ((size_t)blockIdx.x * (blockDim.x >> 6) + pair) * SPW + slot;
-  WarpStateT<TT> w = warp_state<TT>(base, reinterpret_cast<TT *>(job.tws) + tslot * job.nodes_max, nnx * nnz,
-                                    nnx * nnz);
+  WarpStateT<TT> w = warp_state<TT>(
+      base, static_cast<char *>(job.tws) + tslot * slot_bytes(job.nodes_max, (int)sizeof(TT), job.sglobal),
+      job.nodes_max, job.sglobal, nnx * nnz, nnx * nnz);
   Mailbox<TT> *mb = reinterpret_cast<Mailbox<TT> *>(base + solve_bytes - MAILBOX_BYTES);
   const Fx fx = time_scale<TT>(job);
   const int map = active ? sg.map : 0, src = active ? sg.src : 0;
@@ -1582,10 +1591,16 @@ int fm2d_plan(const Fm2dJob &job, Fm2dPlan *plan) {
     plan->nref_map = (int)(nrx * nrz);
   }
   plan->map_tmp_max = tmp;
-  plan->warp_bytes = solve_layout(nodes, nodes).bytes;
+  // node states stay in shared memory when 16 solves (the solve kernels'
+  // register limit per SM) fit beside each other, else they join the times
+  // in the global slot, so that shared memory does not cut the residency
+  const int per_sm_target = 16, smem_sm = 228 * 1024;
+  plan->sglobal = solve_layout(nodes, nodes, false).bytes * per_sm_target > smem_sm;
+  plan->warp_bytes = solve_layout(nodes, nodes, plan->sglobal).bytes;
   plan->ref_heap_cap = nref < g_ref_heap_cap ? nref : g_ref_heap_cap;
-  plan->ref_warp_bytes = nref > 0 ? solve_layout(nref, plan->ref_heap_cap).bytes : 0;
-  plan->ref_full_warp_bytes = nref > 0 ? solve_layout(nref, nref).bytes : 0;
+  plan->sglobal_ref = nref > 0 && solve_layout(nref, plan->ref_heap_cap, false).bytes * per_sm_target > smem_sm;
+  plan->ref_warp_bytes = nref > 0 ? solve_layout(nref, plan->ref_heap_cap, plan->sglobal_ref).bytes : 0;
+  plan->ref_full_warp_bytes = nref > 0 ? solve_layout(nref, nref, plan->sglobal_ref).bytes : 0;
   if (plan->warp_bytes > 227 * 1024 || plan->ref_full_warp_bytes > 227 * 1024) return MCT_ERR_ARG;
   plan->tbytes = job.precision == 2 ? (int)sizeof(int) : (int)sizeof(double);
   // time-field slots: a bound on the solves resident at once, from the
@@ -1598,7 +1613,7 @@ int fm2d_plan(const Fm2dJob &job, Fm2dPlan *plan) {
     cudaGetLastError();
     sms = 152;
   }
-  auto per_sm = [](int bytes) { return bytes > 0 ? std::min(228 * 1024 / bytes, 64) : 0; };
+  auto per_sm = [](int bytes) { return bytes > 0 ? std::min(228 * 1024 / bytes, 32) : 0; };
   plan->tslots = sms * per_sm(plan->warp_bytes);
   plan->tslots_ref = nref > 0 ? sms * per_sm(plan->ref_warp_bytes) : 0;
   return MCT_OK;
@@ -1606,17 +1621,19 @@ int fm2d_plan(const Fm2dJob &job, Fm2dPlan *plan) {
 
 size_t fm2d_tws_bytes(const Fm2dPlan &plan, long nsolve_max) {
   const long r = std::min<long>(plan.tslots_ref, nsolve_max + 32), c = std::min<long>(plan.tslots, nsolve_max + 32);
-  const size_t ref = ((size_t)r * plan.nref_max * plan.tbytes + 255) & ~size_t(255);
-  return ref + (size_t)c * plan.nodes_max * plan.tbytes;
+  const size_t ref = ((size_t)r * slot_bytes(plan.nref_max, plan.tbytes, plan.sglobal_ref) + 255) & ~size_t(255);
+  return ref + (size_t)c * slot_bytes(plan.nodes_max, plan.tbytes, plan.sglobal);
 }
 
 void fm2d_bind_tws(Fm2dJob &job, const Fm2dPlan &plan, long nsolve_max, void *mem) {
   const long r = std::min<long>(plan.tslots_ref, nsolve_max + 32), c = std::min<long>(plan.tslots, nsolve_max + 32);
-  const size_t ref = ((size_t)r * plan.nref_max * plan.tbytes + 255) & ~size_t(255);
+  const size_t ref = ((size_t)r * slot_bytes(plan.nref_max, plan.tbytes, plan.sglobal_ref) + 255) & ~size_t(255);
   job.tws_ref = mem;
   job.tslots_ref = plan.nref_max > 0 ? (int)r : 0;
   job.tws = static_cast<char *>(mem) + ref;
   job.tslots = (int)c;
+  job.sglobal_ref = plan.sglobal_ref;
+  job.sglobal = plan.sglobal;
 }
 
 namespace {

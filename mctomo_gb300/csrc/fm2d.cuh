@@ -37,12 +37,14 @@ struct Fm2dJob {
   int trace_solve; int *trace_i; double *trace_t; int trace_max;
   // from fm2d_plan
   int nodes_max, nref_max, map_tmp_max, nref_map;
-  // time fields of the solves in flight (fm2d_bind_tws): [tslots_ref][nref_max]
-  // and [tslots][nodes_max] elements of the precision's time type (int for
-  // precision 2, 8 bytes otherwise); a block's solves use the slots of its
-  // place in the grid
+  // time fields of the solves in flight (fm2d_bind_tws): [tslots_ref] slots
+  // of nref_max and [tslots] slots of nodes_max nodes, each the times
+  // (the precision's time type: int for precision 2, 8 bytes otherwise)
+  // and, with sglobal(_ref), the node states (int16); a block's solves use
+  // the slots of its place in the grid
   void *tws_ref, *tws;
   int tslots_ref, tslots;
+  int sglobal_ref, sglobal;
 };
 
 struct Fm2dPlan {
@@ -54,6 +56,7 @@ struct Fm2dPlan {
   int ref_full_warp_bytes;   // the same with a heap as large as the box (overflow pass)
   int tbytes;                // bytes of one time value
   int tslots, tslots_ref;    // the most solves resident at once per stage
+  int sglobal, sglobal_ref;  // node states in the global slots (shared memory would cut the residency)
   // launch policy, not set by fm2d_plan: the share of the device's SMs the
   // solve kernels may hold at once (0 or >= 1: all)
   double sm_share = 0.0;
