@@ -1170,6 +1170,37 @@ def served_backends(single, slots, priority="none", share=None):
     return {"tt2d": tt2d, "surface": surf, "body": body, "joint": joint}, used
 
 
+def served_trace_check(traces):
+    """Every chain that ran in both legs has the same seed, so its -log L
+    trace (one value per step: the state after the Metropolis decision) is
+    the same served and plain as long as each evaluation is: the exact kinds
+    (FP64 fm2d) must agree bit for bit; the body kinds' tile solver may move
+    a time by a few fixed-point units with the other chains of a call, which
+    can flip a later decision. Per kind: the steps compared (up to the first
+    step differing by more than 1e-6 relative, where the traces part), the
+    share identical, the largest relative difference before they part, and
+    the chains whose traces parted."""
+    out = {}
+    for cid, (kind, a) in traces["served"].items():
+        if cid not in traces["plain"]:
+            continue
+        b = traces["plain"][cid][1]
+        o = out.setdefault(kind, {"chains_compared": 0, "steps_compared": 0, "identical_steps": 0,
+                                  "max_rel_diff": 0.0, "chains_parted": 0})
+        o["chains_compared"] += 1
+        for x, y in zip(a, b):
+            d = abs(x - y) / max(abs(y), 1e-300)
+            if d > 1e-6:
+                o["chains_parted"] += 1
+                break
+            o["steps_compared"] += 1
+            o["identical_steps"] += int(x == y)
+            o["max_rel_diff"] = max(o["max_rel_diff"], d)
+    for o in out.values():
+        o["identical_frac"] = round(o["identical_steps"] / max(o["steps_compared"], 1), 6)
+    return out
+
+
 def parse_share(spec):
     """'kind=share,...' (kinds tt2d, surface, joint) -> dict; 'none' -> {}."""
     if not spec or spec == "none":
@@ -1195,7 +1226,7 @@ def run_served(args):
     rng = np.random.default_rng(SEED + 7)
     dur, warm = args.served_seconds, args.served_seconds / 3.0
     arrivals = serving.poisson_arrivals(rng, SERVED_CONFIG["rate_chains_per_s"], dur, names)
-    res = {}
+    res, traces = {}, {}
     share = parse_share(args.served_sm_share)
     slots = dict(SERVED_SLOTS)
     for item in filter(None, args.served_slots.split(",")):
@@ -1221,6 +1252,7 @@ def run_served(args):
         stats["clocks"] = clocks.stop()
         stats["device_bytes"] = {k: int(v) for k, v in used.items()}
         res["plain" if plain else "served"] = stats
+        traces["plain" if plain else "served"] = {ch.cid: (ch.kind, list(ch.trace)) for ch in chains if ch.trace}
         del backends, workers
         torch.cuda.synchronize()
     sv = res["served"]
@@ -1236,6 +1268,7 @@ def run_served(args):
                            sm_share=share or "whole device"),
             "served": sv, "plain": pl,
             "served_over_plain": round(sv["evals_per_s"] / pl["evals_per_s"], 3) if pl["evals_per_s"] else None,
+            "accuracy": served_trace_check(traces) if "plain" in traces else None,
             "clocks": sv["clocks"]}
     print(json.dumps(line), flush=True)
 
