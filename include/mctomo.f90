@@ -95,6 +95,11 @@ module mctomo_gb300
     integer(c_int) :: ptype, index, valid
     real(c_double) :: prob, random
   end type
+  type, bind(C) :: mct_pt
+    integer(c_int) :: nchains, number_of_1s, jump_type
+    type(c_ptr) :: values0, values, indices
+    integer(c_long_long) :: accepted, total
+  end type
 
   interface
     type(c_ptr) function mct_version() bind(C, name="mct_version")
@@ -559,6 +564,30 @@ contains
       type(mct_mcmc_set), intent(in) :: set
       type(mct_mcmc_step), intent(in) :: step
       real(c_double), value :: like_new, like_old
+    end function
+    integer(c_int) function mct_mcmc_accept_tempered(set, step, like_new, like_old, temperature) &
+        bind(C, name="mct_mcmc_accept_tempered")
+      import :: c_int, c_double, mct_mcmc_set, mct_mcmc_step
+      type(mct_mcmc_set), intent(in) :: set
+      type(mct_mcmc_step), intent(in) :: step
+      real(c_double), value :: like_new, like_old, temperature
+    end function
+    integer(c_int) function mct_pt_init(pt) bind(C, name="mct_pt_init")
+      import :: c_int, mct_pt
+      type(mct_pt), intent(inout) :: pt
+    end function
+    integer(c_int) function mct_pt_choose(pt, rng, t1_chain, t2_chain) bind(C, name="mct_pt_choose")
+      import :: c_int, c_ptr, mct_pt
+      type(mct_pt), intent(inout) :: pt
+      type(c_ptr), value :: rng
+      integer(c_int), intent(out) :: t1_chain, t2_chain
+    end function
+    integer(c_int) function mct_pt_swap(pt, rng, t1_chain, t2_chain, like_t1, like_t2) bind(C, name="mct_pt_swap")
+      import :: c_int, c_double, c_ptr, mct_pt
+      type(mct_pt), intent(inout) :: pt
+      type(c_ptr), value :: rng
+      integer(c_int), value :: t1_chain, t2_chain
+      real(c_double), value :: like_t1, like_t2
     end function
   end interface
     p = mct_last_error()

@@ -628,6 +628,37 @@ int mct_mcmc_propose(const mct_mcmc_set *set, mct_rng *rng, int iter, int redo, 
 /* The acceptance test of the step given the proposal's -log L (like_new)
  * and the current one (like_old): 1 accept, 0 reject. */
 int mct_mcmc_accept(const mct_mcmc_set *set, const mct_mcmc_step *step, double like_new, double like_old);
+/* The same test in the parallel-tempering loop mcmc_pt
+ * (src/mcmc_loc2.f90:881-886, 933-938, 979-981): the likelihood ratio is
+ * divided by the chain's temperature (> 0). */
+int mct_mcmc_accept_tempered(const mct_mcmc_set *set, const mct_mcmc_step *step, double like_new,
+                             double like_old, double temperature);
+
+/* ------------------------------------------------------------------------
+ * Parallel tempering (mcmc_pt, src/mcmc_loc2.f90:1222-1275): chains
+ * 1..nchains (RTI%number_of_chains) share a temperature ladder values0 of
+ * nchains values (number_of_1s ones, then the temperature file's values,
+ * src/initialise.f90:128-134). values / indices are each chain's current
+ * temperature and its 1-based ladder position (RTI%temperature_values /
+ * _indices); mct_pt_init sets them to the ladder in order. Every
+ * tempering_step iterations from tempering_start, mct_pt_choose picks two
+ * chains as choose_t1 / choose_t2 (:2148-2236; jump_type 0: a random chain
+ * of another temperature, 1: a random ladder neighbour, 2: the nearest
+ * ladder value) and mct_pt_swap offers them a swap given their current
+ * -log L, as do_tempering (:2240-2280): 1 swapped, 0 not. Both draw from
+ * the stream of the reference's first process (its chain 1). Host only. */
+typedef struct {
+  int nchains;
+  int number_of_1s;
+  int jump_type;
+  const double *values0;   /* [nchains] */
+  double *values;          /* [nchains] */
+  int *indices;            /* [nchains] */
+  long long accepted, total;
+} mct_pt;
+int mct_pt_init(mct_pt *pt);
+int mct_pt_choose(mct_pt *pt, mct_rng *rng, int *t1_chain, int *t2_chain);
+int mct_pt_swap(mct_pt *pt, mct_rng *rng, int t1_chain, int t2_chain, double like_t1, double like_t2);
 
 #ifdef __cplusplus
 }

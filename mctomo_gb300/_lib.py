@@ -72,6 +72,10 @@ SIGNATURES = {
     "mct_rng_count": (ctypes.c_longlong, [P]),
     "mct_mcmc_propose": (I, [P, P, I, I, P, P]),
     "mct_mcmc_accept": (I, [P, P, D, D]),
+    "mct_mcmc_accept_tempered": (I, [P, P, D, D, D]),
+    "mct_pt_init": (I, [P]),
+    "mct_pt_choose": (I, [P, P, P, P]),
+    "mct_pt_swap": (I, [P, P, I, I, D, D]),
     "mct_surf_create": (I, [P, P, P, I, I, P]),
     "mct_surf_destroy": (I, [P]),
     "mct_surf_forward": (I, [P, I, P, P, P, P, P, P, P]),

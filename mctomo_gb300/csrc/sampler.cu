@@ -13,7 +13,9 @@
 // (:200-222). Each generator counts its draws as RTI%randcount does.
 #include "mct_common.cuh"
 #include <cmath>
+#include <cstdlib>
 #include <new>
+#include <utility>
 
 struct mct_rng {
   unsigned mt[624];
@@ -333,6 +335,133 @@ int mct_mcmc_accept(const mct_mcmc_set *set, const mct_mcmc_step *step, double l
   if (set->kernel == 0 && step->ptype == 2) a = step->prob + std::log(set->vsmax - set->vsmin) - like_new + like_old;
   const double alpha = std::fmin(std::log(1.0), a);
   return std::log(step->random) < alpha ? 1 : 0;
+}
+
+int mct_mcmc_accept_tempered(const mct_mcmc_set *set, const mct_mcmc_step *step, double like_new, double like_old,
+                             double temperature) {
+  if (!set || !step || !(temperature > 0)) return MCT_ERR_ARG;
+  // mcmc_pt's ratios (mcmc_loc2.f90:881-886 birth, :933-938 death, the rest
+  // e.g. :979-981): the likelihood ratio divided by the chain's temperature
+  const double t = (-like_new + like_old) / temperature;
+  double a = t;
+  if (set->kernel == 0 && step->ptype == 1) a = step->prob - std::log(set->vsmax - set->vsmin) + t;
+  if (set->kernel == 0 && step->ptype == 2) a = step->prob + std::log(set->vsmax - set->vsmin) + t;
+  const double alpha = std::fmin(std::log(1.0), a);
+  return std::log(step->random) < alpha ? 1 : 0;
+}
+
+}  // extern "C"
+
+// ---------------------------------------------------------------------------
+// Parallel tempering of mcmc_pt (src/mcmc_loc2.f90:1222-1275): every
+// tempering_step iterations after tempering_start, the first chain's
+// process picks two chains (choose_t1 :2148-2169, choose_t2 :2171-2236) and
+// offers them a swap of temperatures (do_tempering :2240-2280), drawing
+// from its own random stream. The chains' temperatures are the ladder
+// values0 (number_of_1s ones, then the temperature file's values,
+// initialise.f90:128-134 and run_time_info.f90:186-192) permuted by the
+// accepted swaps.
+// ---------------------------------------------------------------------------
+namespace {
+// mcmc_loc2.f90:51, a REAL*4 literal widened to REAL*8
+const double kEps = (double)1e-8f;
+
+bool in_chains(const mct_pt *pt, int c) { return c >= 1 && c <= pt->nchains; }
+
+// MINLOC(ABS(indices - t2_index), 1): the first chain holding that ladder position
+int chain_of_index(const mct_pt *pt, int index) {
+  int best = 1, bd = -1;
+  for (int c = 1; c <= pt->nchains; ++c) {
+    const int d = std::abs(pt->indices[c - 1] - index);
+    if (bd < 0 || d < bd) { bd = d; best = c; }
+  }
+  return best;
+}
+}  // namespace
+
+extern "C" {
+
+int mct_pt_init(mct_pt *pt) {
+  if (!pt || pt->nchains < 2 || !pt->values0 || !pt->values || !pt->indices || pt->number_of_1s < 1 ||
+      pt->number_of_1s >= pt->nchains || pt->jump_type < 0 || pt->jump_type > 2)
+    return MCT_ERR_ARG;
+  for (int c = 0; c < pt->nchains; ++c) {
+    if (!(pt->values0[c] > 0)) return MCT_ERR_ARG;
+    pt->values[c] = pt->values0[c];
+    pt->indices[c] = c + 1;
+  }
+  pt->accepted = 0;
+  pt->total = 0;
+  return MCT_OK;
+}
+
+int mct_pt_choose(mct_pt *pt, mct_rng *rng, int *t1_chain, int *t2_chain) {
+  if (!pt || !rng || !t1_chain || !t2_chain || pt->nchains < 2) return MCT_ERR_ARG;
+  const int n = pt->nchains, n1 = pt->number_of_1s;
+  // choose_t1
+  int t1 = 0;
+  while (!in_chains(pt, t1)) t1 = pick_index(mct_rng_unirand(rng), n);
+  const double t1v = pt->values[t1 - 1];
+  const int t1i = pt->indices[t1 - 1];
+  // choose_t2
+  int t2 = 0;
+  double t2v = 0;
+  int t2i = 0;
+  if (pt->jump_type == 0) {
+    // a random chain of another temperature (the loop's first test is
+    // decided by t2 = 0 alone); the reference loops for ever when every
+    // chain has t1's temperature, here the draws are bounded
+    long long tries = 0;
+    do {
+      if (++tries > (1LL << 24)) return MCT_ERR_INTERNAL;
+      t2 = pick_index(mct_rng_unirand(rng), n);
+      t2v = pt->values[t2 - 1];
+      t2i = pt->indices[t2 - 1];
+    } while (!in_chains(pt, t2) || std::fabs(t1v - t2v) < kEps);
+  } else {
+    int k;   // 1-based ladder position of the second temperature
+    if (std::fabs(t1v - 1.0) < kEps) {
+      k = n1 + 1;
+    } else if (std::fabs(t1v - pt->values0[n - 1]) < kEps) {
+      k = n - 1;
+    } else if (pt->jump_type == 1) {
+      k = t1i + (mct_rng_unirand(rng) < 0.5 ? -1 : 1);
+    } else {
+      // MINLOC(ABS(values0 - t1v), 1, MASK = ABS(values0 - t1v) > eps)
+      k = 0;
+      double bd = 0;
+      for (int q = 1; q <= n; ++q) {
+        const double d = std::fabs(pt->values0[q - 1] - t1v);
+        if (!(d > kEps)) continue;
+        if (k == 0 || d < bd) { bd = d; k = q; }
+      }
+      if (k == 1) k = pick_index(mct_rng_unirand(rng), n1);
+    }
+    if (k < 1 || k > n) return MCT_ERR_INTERNAL;
+    t2i = k;   // temperature_indices0(k) = k
+    t2 = chain_of_index(pt, t2i);
+  }
+  *t1_chain = t1;
+  *t2_chain = t2;
+  return MCT_OK;
+}
+
+int mct_pt_swap(mct_pt *pt, mct_rng *rng, int t1_chain, int t2_chain, double like_t1, double like_t2) {
+  if (!pt || !rng || !in_chains(pt, t1_chain) || !in_chains(pt, t2_chain)) return MCT_ERR_ARG;
+  const double t1v = pt->values[t1_chain - 1], t2v = pt->values[t2_chain - 1];
+  // do_tempering: alpha_swap = min(0, -L1/T2 + L2/T2 - L2/T1 + L1/T1)
+  const double a = -(like_t1 / t2v) + like_t2 / t2v - like_t2 / t1v + like_t1 / t1v;
+  const double alpha = std::fmin(0.0, a);
+  const double u = mct_rng_unirand(rng);
+  int swapped = 0;
+  if (std::log(u) <= alpha) {
+    std::swap(pt->values[t1_chain - 1], pt->values[t2_chain - 1]);
+    std::swap(pt->indices[t1_chain - 1], pt->indices[t2_chain - 1]);
+    ++pt->accepted;
+    swapped = 1;
+  }
+  ++pt->total;
+  return swapped;
 }
 
 }  // extern "C"

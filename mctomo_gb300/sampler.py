@@ -86,3 +86,49 @@ class Chain:
     def accept(self, step, like_new, like_old):
         return lib().mct_mcmc_accept(ctypes.byref(self.set), ctypes.byref(step), float(like_new),
                                      float(like_old)) == 1
+
+    def accept_tempered(self, step, like_new, like_old, temperature):
+        """The acceptance test of mcmc_pt: the likelihood ratio over the
+        chain's temperature."""
+        rc = lib().mct_mcmc_accept_tempered(ctypes.byref(self.set), ctypes.byref(step), float(like_new),
+                                            float(like_old), float(temperature))
+        return check("mct_mcmc_accept_tempered", rc) == 1
+
+
+class Pt(ctypes.Structure):
+    _fields_ = [("nchains", _I), ("number_of_1s", _I), ("jump_type", _I), ("values0", _P), ("values", _P),
+                ("indices", _P), ("accepted", ctypes.c_longlong), ("total", ctypes.c_longlong)]
+
+
+class Tempering:
+    """Parallel tempering over chains 1..n (mct_pt_*): ladder = number_of_1s
+    ones followed by the temperature file's values; jump_type as in the
+    reference's settings. choose() and swap() draw from the given chain's
+    generator (the reference uses its first process's stream)."""
+
+    def __init__(self, ladder, number_of_1s, jump_type=0):
+        self.values0 = np.ascontiguousarray(ladder, np.float64)
+        n = self.values0.size
+        self.values = np.zeros(n)
+        self.indices = np.zeros(n, np.int32)
+        self.pt = Pt(n, int(number_of_1s), int(jump_type), self.values0.ctypes.data, self.values.ctypes.data,
+                     self.indices.ctypes.data, 0, 0)
+        check("mct_pt_init", lib().mct_pt_init(ctypes.byref(self.pt)))
+
+    def choose(self, chain):
+        t1, t2 = _I(), _I()
+        check("mct_pt_choose", lib().mct_pt_choose(ctypes.byref(self.pt), chain.rng, ctypes.byref(t1),
+                                                   ctypes.byref(t2)))
+        return t1.value, t2.value
+
+    def swap(self, chain, t1, t2, like1, like2):
+        rc = lib().mct_pt_swap(ctypes.byref(self.pt), chain.rng, int(t1), int(t2), float(like1), float(like2))
+        return check("mct_pt_swap", rc) == 1
+
+    @property
+    def accepted(self):
+        return self.pt.accepted
+
+    @property
+    def total(self):
+        return self.pt.total

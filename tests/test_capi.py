@@ -56,8 +56,11 @@ def _c_decls():
             decl = decl.strip()
             if not decl:
                 continue
-            kind = "ptr" if "*" in decl else decl.split()[0]
-            names = decl.replace("*", " ").split(None, 1 if not decl.startswith("const") else 2)[-1]
+            if decl.startswith("long long"):
+                kind, names = "long long", decl[len("long long"):]
+            else:
+                kind = "ptr" if "*" in decl else decl.split()[0]
+                names = decl.replace("*", " ").split(None, 1 if not decl.startswith("const") else 2)[-1]
             fields += [(kind, n.strip()) for n in names.split(",")]
         structs[m.group(2)] = fields
     return funcs, structs
@@ -77,7 +80,8 @@ def test_fortran_module_covers_the_header():
     assert set(ff) == set(funcs)
     for name, args in funcs.items():
         assert len(ff[name]) == len(args), name
-    kinds = {"integer(c_int)": "int", "real(c_double)": "double", "type(c_ptr)": "ptr"}
+    kinds = {"integer(c_int)": "int", "real(c_double)": "double", "type(c_ptr)": "ptr",
+             "integer(c_long_long)": "long long"}
     for m in re.finditer(r"type, bind\(C\) :: (\w+)\n(.*?)end type", f, flags=re.S):
         fields = []
         for line in m.group(2).strip().splitlines():
