@@ -336,6 +336,25 @@ module mctomo_gb300
       real(c_double), intent(out) :: out(*)
       integer(c_int), intent(out) :: done
     end function
+    integer(c_int) function mct_surf_stat_add(ctx, nchains, slots) bind(C, name="mct_surf_stat_add")
+      import :: c_int, c_ptr
+      type(c_ptr), value :: ctx
+      integer(c_int), value :: nchains
+      integer(c_int), intent(in) :: slots(*)
+    end function
+    integer(c_int) function mct_surf_stat_read(ctx, slot, mean_vp, mean_vs, msq_vp, msq_vs, nthin) &
+        bind(C, name="mct_surf_stat_read")
+      import :: c_int, c_double, c_ptr
+      type(c_ptr), value :: ctx
+      integer(c_int), value :: slot
+      real(c_double), intent(out) :: mean_vp(*), mean_vs(*), msq_vp(*), msq_vs(*)
+      integer(c_int), intent(out) :: nthin
+    end function
+    integer(c_int) function mct_surf_stat_reset(ctx, slot) bind(C, name="mct_surf_stat_reset")
+      import :: c_int, c_ptr
+      type(c_ptr), value :: ctx
+      integer(c_int), value :: slot
+    end function
     integer(c_int) function mct_body_submit(ctx, nchains, ncells, points, params, locations, n0, n1) &
         bind(C, name="mct_body_submit")
       import :: c_int, c_double, c_ptr

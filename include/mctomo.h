@@ -332,6 +332,21 @@ int mct_surf_submit(mct_surf_ctx *ctx, int nchains, const int *slots,
                     const double *params, const double *n0,
                     const double *n1);
 int mct_surf_poll(mct_surf_ctx *ctx, double *out, int *done);
+/* Posterior statistics, replaces stat_rti (src/mcmc_loc2.f90:1966-2000) for
+ * the models held on the device: mct_surf_stat_add adds each listed slot's
+ * committed model (after mct_surf_commit) to the slot's sums of vp, vp^2,
+ * vs and vs^2 per grid node, in the reference's order of operations, and
+ * counts it (RTI%nthin); the caller decides when (after burn-in, every
+ * thin-th sample, at temperature 1). The first call allocates the sums
+ * (4 x nodes x nslots doubles). mct_surf_stat_read gives a slot's means and
+ * mean squares, the sums over the count as write_mean / write_var
+ * (src/read_write.f90:223-292) write them (zero when nothing was added),
+ * each (nz, ny, nx) in Fortran order; any output may be NULL.
+ * mct_surf_stat_reset clears a slot (mct_surf_admit does too). */
+int mct_surf_stat_add(mct_surf_ctx *ctx, int nchains, const int *slots);
+int mct_surf_stat_read(mct_surf_ctx *ctx, int slot, double *mean_vp, double *mean_vs, double *msq_vp,
+                       double *msq_vs, int *nthin);
+int mct_surf_stat_reset(mct_surf_ctx *ctx, int slot);
 
 
 /* ------------------------------------------------------------------------

@@ -90,6 +90,9 @@ SIGNATURES = {
     "mct_surf_evict": (I, [P, I]),
     "mct_surf_submit": (I, [P, I, P, P, P, P, P, P]),
     "mct_surf_poll": (I, [P, P, P]),
+    "mct_surf_stat_add": (I, [P, I, P]),
+    "mct_surf_stat_read": (I, [P, I, P, P, P, P, P]),
+    "mct_surf_stat_reset": (I, [P, I]),
     "mct_surf_profile_start": (I, [P, I]),
     "mct_surf_profile_read": (I, [P, P, P, P]),
 }

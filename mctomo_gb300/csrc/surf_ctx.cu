@@ -2,6 +2,7 @@
 // around surf_forward / surf_commit (surf_pipeline.cu).
 #include "mct_common.cuh"
 #include "surf_pipeline.cuh"
+#include <algorithm>
 #include <cmath>
 #include <vector>
 #include <cstring>
@@ -25,7 +26,32 @@ struct mct_surf_ctx {
   cudaEvent_t done = nullptr;
   int pending = 0;
   std::vector<char> in_use;           // slot allocator (mct_surf_admit / mct_surf_evict)
+  // posterior statistics (mct_surf_stat_*), allocated by the first
+  // mct_surf_stat_add: per slot the sums of vs, vs^2, vp, vp^2 over the
+  // committed models added, and their count
+  double *st_sum = nullptr;           // [nslots][4][nodes]
+  int *st_slots = nullptr;            // [nslots] device copy of the call's slots
+  std::vector<int> st_n;
 };
+
+namespace {
+// stat_rti (src/mcmc_loc2.f90:1975-1978): aveS += vs, stdS += vs**2,
+// aveP += vp, stdP += vp**2, node by node, for each listed slot's committed
+// model
+__global__ void stat_add_kernel(int nchains, const int *slots, size_t nodes, const double *cvp, const double *cvs,
+                                double *sum) {
+  const int slot = slots[blockIdx.y];
+  const double *vp = cvp + (size_t)slot * nodes, *vs = cvs + (size_t)slot * nodes;
+  double *s = sum + (size_t)slot * 4 * nodes;
+  for (size_t q = blockIdx.x * (size_t)blockDim.x + threadIdx.x; q < nodes; q += (size_t)gridDim.x * blockDim.x) {
+    const double v = vs[q], p = vp[q];
+    s[q] = s[q] + v;
+    s[nodes + q] = s[nodes + q] + v * v;
+    s[2 * nodes + q] = s[2 * nodes + q] + p;
+    s[3 * nodes + q] = s[3 * nodes + q] + p * p;
+  }
+}
+}  // namespace
 
 namespace {
 std::string &err() { static thread_local std::string e; return e; }
@@ -301,6 +327,8 @@ int mct_surf_destroy(mct_surf_ctx *c) {
     for (int i = 0; i < 5 * c->prof.max_steps; ++i) cudaEventDestroy(c->prof.ev[i]);
     delete[] c->prof.ev;
   }
+  if (c->st_sum) cudaFree(c->st_sum);
+  if (c->st_slots) cudaFree(c->st_slots);
   cudaFree(c->mem);
   cudaStreamDestroy(c->stream);
   delete c;
@@ -442,12 +470,78 @@ int mct_surf_poll(mct_surf_ctx *c, double *out, int *done) {
   return st ? st : MCT_OK;
 }
 
+int mct_surf_stat_add(mct_surf_ctx *c, int nchains, const int *slots) {
+  if (!c || c->pending || nchains < 1 || nchains > c->nslots || !slots) return MCT_ERR_ARG;
+  for (int i = 0; i < nchains; ++i) {
+    if (slots[i] < 0 || slots[i] >= c->nslots) return MCT_ERR_ARG;
+    for (int j = 0; j < i; ++j) if (slots[j] == slots[i]) return MCT_ERR_ARG;
+  }
+  const SurfBatch &b = c->b;
+  const size_t nodes = (size_t)b.nx * b.ny * b.nz;
+  if (!c->st_sum) {
+    MCT_CUDA_TRY(cudaMalloc(&c->st_sum, sizeof(double) * 4 * nodes * c->nslots));
+    MCT_CUDA_TRY(cudaMalloc(&c->st_slots, sizeof(int) * c->nslots));
+    MCT_CUDA_TRY(cudaMemsetAsync(c->st_sum, 0, sizeof(double) * 4 * nodes * c->nslots, c->stream));
+    c->st_n.assign((size_t)c->nslots, 0);
+  }
+  MCT_CUDA_TRY(cudaMemcpyAsync(c->st_slots, slots, sizeof(int) * nchains, cudaMemcpyHostToDevice, c->stream));
+  stat_add_kernel<<<dim3((unsigned)std::min<size_t>((nodes + 255) / 256, 152), nchains), 256, 0, c->stream>>>(
+      nchains, c->st_slots, nodes, b.cvp, b.cvs, c->st_sum);
+  MCT_CUDA_TRY(cudaGetLastError());
+  MCT_CUDA_TRY(cudaStreamSynchronize(c->stream));   // the slots array is the caller's
+  for (int i = 0; i < nchains; ++i) ++c->st_n[(size_t)slots[i]];
+  return MCT_OK;
+}
+
+int mct_surf_stat_read(mct_surf_ctx *c, int slot, double *mean_vp, double *mean_vs, double *msq_vp, double *msq_vs,
+                       int *nthin) {
+  if (!c || c->pending || slot < 0 || slot >= c->nslots) return MCT_ERR_ARG;
+  const SurfBatch &b = c->b;
+  const size_t nodes = (size_t)b.nx * b.ny * b.nz;
+  const int n = c->st_sum ? c->st_n[(size_t)slot] : 0;
+  if (nthin) *nthin = n;
+  double *outs[4] = {mean_vs, msq_vs, mean_vp, msq_vp};
+  std::vector<double> h(nodes);
+  for (int k = 0; k < 4; ++k) {
+    if (!outs[k]) continue;
+    if (n == 0) { std::fill(outs[k], outs[k] + nodes, 0.0); continue; }
+    MCT_CUDA_TRY(cudaMemcpyAsync(h.data(), c->st_sum + ((size_t)slot * 4 + k) * nodes, sizeof(double) * nodes,
+                                 cudaMemcpyDeviceToHost, c->stream));
+    MCT_CUDA_TRY(cudaStreamSynchronize(c->stream));
+    // write_mean / write_var (src/read_write.f90:223-292): sums over nthin
+    for (size_t q = 0; q < nodes; ++q) outs[k][q] = h[q] / n;
+  }
+  return MCT_OK;
+}
+
+}  // extern "C"
+
+namespace {
+int stat_reset_slot(mct_surf_ctx *c, int slot) {
+  if (!c->st_sum) return MCT_OK;
+  const size_t nodes = (size_t)c->b.nx * c->b.ny * c->b.nz;
+  MCT_CUDA_TRY(cudaMemsetAsync(c->st_sum + (size_t)slot * 4 * nodes, 0, sizeof(double) * 4 * nodes, c->stream));
+  c->st_n[(size_t)slot] = 0;
+  return MCT_OK;
+}
+}  // namespace
+
+extern "C" {
+
+int mct_surf_stat_reset(mct_surf_ctx *c, int slot) {
+  if (!c || c->pending || slot < 0 || slot >= c->nslots) return MCT_ERR_ARG;
+  return stat_reset_slot(c, slot);
+}
+
 int mct_surf_admit(mct_surf_ctx *c, int *slot) {
   if (!c || !slot) return MCT_ERR_ARG;
   for (int i = 0; i < c->nslots; ++i) {
     if (c->in_use[(size_t)i]) continue;
-    // a fresh chain: nothing committed, so its first forward computes every column
+    // a fresh chain: nothing committed, so its first forward computes every
+    // column, and no posterior statistics
     MCT_CUDA_TRY(cudaMemsetAsync(c->b.committed + i, 0, sizeof(int), c->stream));
+    int rc = stat_reset_slot(c, i);
+    if (rc) return rc;
     c->in_use[(size_t)i] = 1;
     *slot = i;
     return MCT_OK;

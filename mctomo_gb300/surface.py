@@ -74,7 +74,7 @@ class SurfaceLikelihood:
         self._keep.append(arrs)
         self.nsrc, self.nrev = d.nsrc, d.nrev
         self.nslots, self.ncell_max = nslots, ncell_max
-        self.nx, self.ny = g.nx, g.ny
+        self.nx, self.ny, self.nz = g.nx, g.ny, g.nz
         h = ctypes.c_void_p()
         check("mct_surf_create", lib().mct_surf_create(ctypes.byref(g), ctypes.byref(s), ctypes.byref(d),
                                                        nslots, ncell_max, ctypes.byref(h)))
@@ -136,6 +136,25 @@ class SurfaceLikelihood:
         done = ctypes.c_int()
         check("mct_surf_poll", lib().mct_surf_poll(self.h, ptr(out), ctypes.byref(done)))
         return bool(done.value), (out if done.value else None)
+
+    def stat_add(self, slots):
+        """stat_rti on the device: add each slot's committed model to its
+        posterior sums (vp, vp^2, vs, vs^2 per node)."""
+        slots = np.ascontiguousarray(slots, np.int32)
+        check("mct_surf_stat_add", lib().mct_surf_stat_add(self.h, slots.size, ptr(slots)))
+
+    def stat_read(self, slot):
+        """(mean_vp, mean_vs, msq_vp, msq_vs, nthin): each (nx, ny, nz), the
+        sums over the number of models added (write_mean / write_var)."""
+        shape = (self.nx, self.ny, self.nz)
+        mp, ms, qp, qs = (np.zeros(shape) for _ in range(4))
+        n = ctypes.c_int()
+        check("mct_surf_stat_read", lib().mct_surf_stat_read(self.h, int(slot), ptr(mp), ptr(ms), ptr(qp), ptr(qs),
+                                                             ctypes.byref(n)))
+        return mp, ms, qp, qs, n.value
+
+    def stat_reset(self, slot):
+        check("mct_surf_stat_reset", lib().mct_surf_stat_reset(self.h, int(slot)))
 
     def admit(self):
         """Claims a free chain slot (MctError when none is free)."""
