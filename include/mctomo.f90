@@ -56,7 +56,7 @@ module mctomo_gb300
   end type mct_surf_data
 
   type, bind(C) :: mct_body_settings
-    integer(c_int) :: order, np, sigdep, solver
+    integer(c_int) :: order, np, sigdep, solver, dynamic
   end type mct_body_settings
 
   type, bind(C) :: mct_body_data
@@ -354,6 +354,21 @@ module mctomo_gb300
       import :: c_int, c_ptr
       type(c_ptr), value :: ctx
       integer(c_int), value :: slot
+    end function
+    integer(c_int) function mct_body_location_likelihood(ctx, nchains, locations, n0, n1, out, phase_time) &
+        bind(C, name="mct_body_location_likelihood")
+      import :: c_int, c_double, c_ptr
+      type(c_ptr), value :: ctx
+      integer(c_int), value :: nchains
+      real(c_double), intent(in) :: locations(*), n0(*), n1(*)
+      real(c_double), intent(out) :: out(*)
+      type(c_ptr), value :: phase_time
+    end function
+    integer(c_int) function mct_body_location_commit(ctx, nchains, accept) bind(C, name="mct_body_location_commit")
+      import :: c_int, c_ptr
+      type(c_ptr), value :: ctx
+      integer(c_int), value :: nchains
+      integer(c_int), intent(in) :: accept(*)
     end function
     integer(c_int) function mct_body_submit(ctx, nchains, ncells, points, params, locations, n0, n1) &
         bind(C, name="mct_body_submit")

@@ -420,6 +420,10 @@ typedef struct {
   int sigdep;    /* 0 data sigma, else sigma = n0*time + n1 */
   int solver;    /* 3D solver: 0 default (heap march for order 1, tiles for
                     order 0), MCT_EIK3_TILES or MCT_EIK3_HEAP */
+  int dynamic;   /* LIKE_SET%dynamic: 1 keeps the stations' travel-time fields
+                    (like%field5d, 2 x nslots x np x nrev x nodes FP64) for
+                    mct_body_location_likelihood; the solves then always run
+                    from the stations */
 } mct_body_settings;
 
 typedef struct {
@@ -475,6 +479,19 @@ int mct_body_commit(mct_body_ctx *ctx, int nchains, const int *accept);
  * origin times (locations, nchains x nsrc x 4, the 4th entry used); sigma =
  * n0 * travel time + n1 for every pair. out as mct_body_forward (status 16:
  * nothing committed yet). */
+/* Location step with stored fields, replaces body_location_likelihood
+ * (src/likelihood_body.F90:82-149, settings.dynamic = 1): chains
+ * 0..nchains-1's committed fields (one per station and phase, from their
+ * last accepted forward) read at the proposed event locations
+ * (Interpolate3d, :976-1005) and the misfit with origin times, sigma =
+ * n0 * time + n1; out [nchains][4] as mct_body_forward (status 16: nothing
+ * committed yet); phase_time (optional) [nchains][np][nsrc*nrev] the times.
+ * mct_body_location_commit: the accepted location steps' times become the
+ * chains' committed times. MCT_ERR_UNSUPPORTED without stored fields (the
+ * reference's location step is then a full forward). */
+int mct_body_location_likelihood(mct_body_ctx *ctx, int nchains, const double *locations, const double *n0,
+                                 const double *n1, double *out, double *phase_time);
+int mct_body_location_commit(mct_body_ctx *ctx, int nchains, const int *accept);
 int mct_body_noise_likelihood(mct_body_ctx *ctx, int nchains,
                               const double *locations, const double *n0,
                               const double *n1, double *out);

@@ -47,6 +47,8 @@ SIGNATURES = {
     "mct_body_forward": (I, [P, I, P, P, P, P, P, P, P]),
     "mct_body_phase_time": (I, [P, I, P, P]),
     "mct_body_submit": (I, [P, I, P, P, P, P, P, P]),
+    "mct_body_location_likelihood": (I, [P, I, P, P, P, P, P]),
+    "mct_body_location_commit": (I, [P, I, P]),
     "mct_body_poll": (I, [P, P, P]),
     "mct_body_commit": (I, [P, I, P]),
     "mct_body_noise_likelihood": (I, [P, I, P, P, P, P]),

@@ -16,7 +16,7 @@ class BodySettings(ctypes.Structure):
     travel-time solver (0 default: the exact heap march for order 1, tiles
     for order 0; EIK3_TILES or EIK3_HEAP)."""
     _fields_ = [("order", ctypes.c_int), ("np", ctypes.c_int), ("sigdep", ctypes.c_int),
-                ("solver", ctypes.c_int)]
+                ("solver", ctypes.c_int), ("dynamic", ctypes.c_int)]
 
 
 class BodyData(ctypes.Structure):
@@ -78,6 +78,26 @@ class BodyLikelihood:
         check("mct_body_forward", lib().mct_body_forward(self.h, nch, ptr(ncells), ptr(points), ptr(params),
                                                          ptr(locations), ptr(n0), ptr(n1), ptr(out)))
         return out
+
+    def location_likelihood(self, locations, n0, n1, times=False):
+        """body_location_likelihood on the stored fields (settings dynamic=1):
+        chains 0..nchains-1's committed fields read at the proposed event
+        locations (nchains, nsrc, 4). Returns out (nchains, 4), and with
+        times the interpolated times (nchains, np, nsrc*nrev)."""
+        locations = np.ascontiguousarray(locations, np.float64)
+        nch = locations.shape[0]
+        locations = locations.reshape(nch, self.nsrc, 4)
+        n0 = np.ascontiguousarray(n0, np.float64).reshape(nch, self.np)
+        n1 = np.ascontiguousarray(n1, np.float64).reshape(nch, self.np)
+        out = np.zeros((nch, 4))
+        pt = np.zeros((nch, self.np, self.nsrc * self.nrev)) if times else None
+        check("mct_body_location_likelihood",
+              lib().mct_body_location_likelihood(self.h, nch, ptr(locations), ptr(n0), ptr(n1), ptr(out), ptr(pt)))
+        return (out, pt) if times else out
+
+    def location_commit(self, accept):
+        accept = np.ascontiguousarray(accept, np.int32)
+        check("mct_body_location_commit", lib().mct_body_location_commit(self.h, accept.size, ptr(accept)))
 
     def submit(self, ncells, points, params, locations, n0, n1):
         """Starts forward() on the context's worker thread without waiting;

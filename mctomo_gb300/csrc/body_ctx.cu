@@ -114,6 +114,99 @@ __global__ void body_misfit_kernel(BodyDev d, int nchains, const double *tt, con
   }
 }
 
+// Interpolate3d (src/likelihood_body.F90:976-1005) with point2idx
+// (:1038-1054): the trilinear time of a field (nx, ny, nz; z fastest) at an
+// event location, with the reference's cell clamp and REAL*4 1.0 weights.
+__device__ double interpolate3d(const double *f, int nx, int ny, int nz, double xmin, double ymin, double zmin,
+                                double dx, double dy, double dz, double scaling, const double *pt) {
+  int ix = (int)floor((pt[0] - xmin) / dx) + 1;
+  int iy = (int)floor((pt[1] - ymin) / dy) + 1;
+  int iz = (int)floor((pt[2] - zmin / scaling) / (dz / scaling)) + 1;
+  if (ix < 1) ix = 1;
+  if (iy < 1) iy = 1;
+  if (iz < 1) iz = 1;
+  if (ix >= nx) ix = nx - 1;
+  if (iy >= ny) iy = ny - 1;
+  if (iz >= nz) iz = nz - 1;
+  const double dsx = pt[0] - (xmin + (ix - 1) * dx);
+  const double dsy = pt[1] - (ymin + (iy - 1) * dy);
+  const double dsz = pt[2] - (zmin + (iz - 1) * dz) / scaling;
+  double qv = 0;
+  for (int i = 1; i <= 2; ++i)
+    for (int j = 1; j <= 2; ++j)
+      for (int k = 1; k <= 2; ++k) {
+        const double w = (1.0 - fabs((i - 1) * dx - dsx) / dx) * (1.0 - fabs((j - 1) * dy - dsy) / dy) *
+                         (1.0 - fabs((k - 1) * dz / scaling - dsz) / (dz / scaling));
+        qv = qv + w * f[((size_t)(ix + i - 2) * ny + (iy + j - 2)) * nz + (iz + k - 2)];
+      }
+  return qv;
+}
+
+// body_location_likelihood (src/likelihood_body.F90:82-149): the committed
+// fields of chain c (one per station and phase) read at the events' proposed
+// locations, then the misfit with origin times and sigma = n0 * time + n1
+// for every pair (unused pairs sigma 1); status 16 when nothing is committed.
+__global__ void body_location_kernel(BodyDev d, mct_grid g, const double *cfield, const double *loc,
+                                     const double *n0, const double *n1, const int *committed, double *ptime,
+                                     double *out) {
+  const int c = blockIdx.x;
+  const int npairs = d.nsrc * d.nrev;
+  const size_t nn = (size_t)g.nx * g.ny * g.nz;
+  double like = 0, mis = 0, umis = 0, slog = 0;
+  for (int q = threadIdx.x; q < d.np * npairs; q += blockDim.x) {
+    const int p = q / npairs, r = q % npairs;
+    const int j = r / d.nrev, k = r % d.nrev;       // event j, station k
+    const double *f = cfield + (((size_t)c * d.np + p) * d.nrev + k) * nn;
+    const double t = interpolate3d(f, g.nx, g.ny, g.nz, g.xmin, g.ymin, g.zmin, g.dx, g.dy, g.dz, g.scaling,
+                                   loc + ((size_t)c * d.nsrc + j) * 4);
+    ptime[((size_t)c * d.np + p) * npairs + r] = t;
+    const bool used = d.raystat[(size_t)p * npairs + r] == 1;
+    const double sig = used ? n0[(size_t)c * d.np + p] * t + n1[(size_t)c * d.np + p] : 1.0;
+    if (used) {
+      const double res = t + loc[((size_t)c * d.nsrc + j) * 4 + 3] - d.dtime[(size_t)p * npairs + r];
+      const double r2 = res * res;
+      like += r2 / (2 * (sig * sig));
+      mis += r2 / (sig * sig);
+      umis += r2;
+    }
+    slog += log(sig);
+  }
+  __shared__ double red[4][256];
+  red[0][threadIdx.x] = like; red[1][threadIdx.x] = mis; red[2][threadIdx.x] = umis; red[3][threadIdx.x] = slog;
+  __syncthreads();
+  for (int st = blockDim.x / 2; st > 0; st >>= 1) {
+    if (threadIdx.x < st)
+      for (int m = 0; m < 4; ++m) red[m][threadIdx.x] += red[m][threadIdx.x + st];
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) {
+    const double PI2 = (double)6.283185f;
+    const bool ok = committed[c] != 0;
+    out[(size_t)c * 4 + 0] = ok ? red[0][0] + red[3][0] + (double)((float)d.nrays / 2.0f) * log(PI2) : DBL_MAX;
+    out[(size_t)c * 4 + 1] = red[1][0];
+    out[(size_t)c * 4 + 2] = red[2][0];
+    out[(size_t)c * 4 + 3] = ok ? 0.0 : 16.0;
+  }
+}
+
+// The fields of an accepted forward become its chain's committed fields.
+__global__ void body_field_commit_kernel(size_t n, const int *accept, const double *out, const double *field,
+                                         double *cfield) {
+  const int c = blockIdx.y;
+  if (!accept[c] || out[(size_t)c * 4 + 3] != 0.0) return;
+  for (size_t q = blockIdx.x * (size_t)blockDim.x + threadIdx.x; q < n; q += (size_t)gridDim.x * blockDim.x)
+    cfield[(size_t)c * n + q] = field[(size_t)c * n + q];
+}
+
+// A location step's times become the chain's committed times.
+__global__ void body_loc_commit_kernel(int n, const int *accept, const double *out, const double *lptime,
+                                       double *cptime) {
+  const int c = blockIdx.y;
+  if (!accept[c] || out[(size_t)c * 4 + 3] != 0.0) return;
+  for (int q = blockIdx.x * blockDim.x + threadIdx.x; q < n; q += gridDim.x * blockDim.x)
+    cptime[(size_t)c * n + q] = lptime[(size_t)c * n + q];
+}
+
 }  // namespace
 
 // An accepted proposal becomes its chain's state (what the reference keeps
@@ -192,6 +285,11 @@ struct mct_body_ctx {
   double2 *hvn = nullptr; void *hscratch = nullptr;
   int hchunk = 0; int *herr = nullptr;
   int last_nchains = 0, last_passes = 0;
+  // dynamic (settings.dynamic): the travel-time fields of the last forward
+  // and of each chain's committed model, [nslots][np][nrev][nodes] FP64
+  // (the reference's like%field5d), the location step's times
+  int dynamic = 0;
+  double *field = nullptr, *cfield = nullptr, *lptime = nullptr, *lout = nullptr;
   // mct_body_submit / mct_body_poll: the forward waits on the host between
   // the 3D solver's passes, so a submitted batch runs on a worker thread of
   // the context (started by the first submit) with copies of the caller's
@@ -249,12 +347,15 @@ int mct_body_create(const mct_grid *g, const mct_body_settings *st, const mct_bo
   if (st->np != 1 && st->np != 2) return MCT_ERR_ARG;
   if (st->order != 0 && st->order != 1) return MCT_ERR_ARG;
   if (st->solver != 0 && st->solver != MCT_EIK3_TILES && st->solver != MCT_EIK3_HEAP) return MCT_ERR_ARG;
+  if (st->dynamic != 0 && st->dynamic != 1) return MCT_ERR_ARG;
   if (dat->nsrc < 1 || dat->nrev < 1 || dat->np != st->np) return MCT_ERR_ARG;
   *out = nullptr;
   mct_body_ctx *c = new mct_body_ctx();
   c->g = *g; c->order = st->order; c->np = st->np; c->sigdep = st->sigdep; c->nslots = nslots; c->ncell_max = ncell_max;
   const int nsrc = dat->nsrc, nrev = dat->nrev, np = dat->np, npairs = nsrc * nrev;
-  const int from_rev = nsrc > nrev ? 1 : 0;   // likelihood_body.F90:204,226
+  // likelihood_body.F90:204,226; with stored fields always from the
+  // stations (:251-281), whose fields the location steps read
+  const int from_rev = (nsrc > nrev || st->dynamic) ? 1 : 0;
   const int nsol = from_rev ? nrev : nsrc, nrecv = from_rev ? nsrc : nrev;
   const size_t nn = (size_t)g->nx * g->ny * g->nz;
   const size_t nsolve = (size_t)nslots * np * nsol;
@@ -288,7 +389,9 @@ int mct_body_create(const mct_grid *g, const mct_body_settings *st, const mct_bo
       heap ? sizeof(double2) * 2 * (size_t)nslots * nn : 0,
       eik3_heap_scratch_bytes(g->nx, g->ny, g->nz, (int)hchunk), sizeof(int),
       sizeof(double) * (size_t)nslots * np * npairs, sizeof(int) * 2 * nslots, sizeof(double) * 4 * nslots,
-      sizeof(int) * 2 * nslots};
+      sizeof(int) * 2 * nslots,
+      st->dynamic ? 2 * sizeof(double) * (size_t)nslots * np * nrev * nn : 0,
+      st->dynamic ? sizeof(double) * (size_t)nslots * np * npairs : 0, st->dynamic ? sizeof(double) * 4 * nslots : 0};
   size_t total = 0;
   for (size_t s : sz) total = ((total + 255) & ~size_t(255)) + s;
   total += 256;
@@ -332,6 +435,13 @@ int mct_body_create(const mct_grid *g, const mct_body_settings *st, const mct_bo
   c->accept = c->committed + nslots;
   c->nout = cv.take<double>(4 * (size_t)nslots);
   c->gshift = cv.take<int>(2 * (size_t)nslots);
+  c->dynamic = st->dynamic;
+  if (st->dynamic) {
+    c->field = cv.take<double>(2 * (size_t)nslots * np * nrev * nn);
+    c->cfield = c->field + (size_t)nslots * np * nrev * nn;
+    c->lptime = cv.take<double>((size_t)nslots * np * npairs);
+    c->lout = cv.take<double>(4 * (size_t)nslots);
+  }
   cudaMemset(c->committed, 0, sizeof(int) * 2 * nslots);
   c->hchunk = (int)hchunk;
   std::vector<double> hs((size_t)np * npairs, 1.0);
@@ -492,7 +602,7 @@ int body_forward(mct_body_ctx *c, int nchains, const int *ncells, const double *
   }
   job.nrev = nrecv; job.rev = c->erecv; job.rev_per_solve = 1; job.solve_rev = c->eset; job.ttime = c->ett;
   int passes = 0;
-  rc = launch_eik3(job, s, 100000, &passes, nullptr); if (rc) return rc;
+  rc = launch_eik3(job, s, 100000, &passes, c->dynamic ? c->field : nullptr); if (rc) return rc;
   c->last_passes = passes;
   body_misfit_kernel<<<nchains, 256, 0, s>>>(d, nchains, c->ett, c->loc, c->n0, c->n1, c->ptime, c->out);
   MCT_CUDA_TRY(cudaGetLastError());
@@ -515,6 +625,50 @@ int mct_body_commit(mct_body_ctx *c, int nchains, const int *accept) {
   MCT_CUDA_TRY(cudaMemcpyAsync(c->accept, accept, sizeof(int) * nchains, cudaMemcpyHostToDevice, s));
   body_commit_kernel<<<dim3((n + 255) / 256, nchains), 256, 0, s>>>(n, c->accept, c->out, c->ptime, c->cptime,
                                                                     c->committed);
+  MCT_CUDA_TRY(cudaGetLastError());
+  if (c->dynamic) {
+    const size_t nf = (size_t)c->dev.np * c->dev.nrev * c->g.nx * c->g.ny * c->g.nz;
+    body_field_commit_kernel<<<dim3(1024, nchains), 256, 0, s>>>(nf, c->accept, c->out, c->field, c->cfield);
+    MCT_CUDA_TRY(cudaGetLastError());
+  }
+  MCT_CUDA_TRY(cudaStreamSynchronize(s));
+  return MCT_OK;
+}
+
+int mct_body_location_likelihood(mct_body_ctx *c, int nchains, const double *locations, const double *n0,
+                                 const double *n1, double *out, double *phase_time) {
+  if (!c || busy(c, "mct_body_location_likelihood") || nchains < 1 || nchains > c->nslots || !locations || !n0 ||
+      !n1 || !out)
+    return MCT_ERR_ARG;
+  if (!c->dynamic) {
+    mct_set_error("mct_body_location_likelihood", "the context keeps no fields (settings.dynamic = 0): "
+                  "a location step is a full forward", __FILE__, __LINE__);
+    return MCT_ERR_UNSUPPORTED;
+  }
+  cudaStream_t s = c->stream;
+  const BodyDev &d = c->dev;
+  MCT_CUDA_TRY(cudaMemcpyAsync(c->loc, locations, sizeof(double) * nchains * d.nsrc * 4, cudaMemcpyHostToDevice, s));
+  MCT_CUDA_TRY(cudaMemcpyAsync(c->n0, n0, sizeof(double) * nchains * d.np, cudaMemcpyHostToDevice, s));
+  MCT_CUDA_TRY(cudaMemcpyAsync(c->n1, n1, sizeof(double) * nchains * d.np, cudaMemcpyHostToDevice, s));
+  body_location_kernel<<<nchains, 256, 0, s>>>(d, c->g, c->cfield, c->loc, c->n0, c->n1, c->committed, c->lptime,
+                                              c->lout);
+  MCT_CUDA_TRY(cudaGetLastError());
+  MCT_CUDA_TRY(cudaMemcpyAsync(out, c->lout, sizeof(double) * 4 * nchains, cudaMemcpyDeviceToHost, s));
+  const size_t npt = (size_t)d.np * d.nsrc * d.nrev;
+  if (phase_time)
+    MCT_CUDA_TRY(cudaMemcpyAsync(phase_time, c->lptime, sizeof(double) * npt * nchains, cudaMemcpyDeviceToHost, s));
+  MCT_CUDA_TRY(cudaStreamSynchronize(s));
+  return MCT_OK;
+}
+
+int mct_body_location_commit(mct_body_ctx *c, int nchains, const int *accept) {
+  if (!c || busy(c, "mct_body_location_commit") || nchains < 1 || nchains > c->nslots || !accept) return MCT_ERR_ARG;
+  if (!c->dynamic) return MCT_ERR_UNSUPPORTED;
+  cudaStream_t s = c->stream;
+  const int n = c->dev.np * c->dev.nsrc * c->dev.nrev;
+  MCT_CUDA_TRY(cudaMemcpyAsync(c->accept, accept, sizeof(int) * nchains, cudaMemcpyHostToDevice, s));
+  body_loc_commit_kernel<<<dim3((n + 255) / 256, nchains), 256, 0, s>>>(n, c->accept, c->lout, c->lptime,
+                                                                        c->cptime);
   MCT_CUDA_TRY(cudaGetLastError());
   MCT_CUDA_TRY(cudaStreamSynchronize(s));
   return MCT_OK;
