@@ -617,6 +617,7 @@ def run_body(args):
     settings["order"] = args.order
     solver = args.solver or ("heap" if args.order == 1 else "tiles")
     settings["solver"] = {"tiles": 0x10, "heap": 0x20}[solver]
+    settings["dynamic"] = 1 if args.dynamic else 0
     lo = np.zeros(3); hi = np.array([50.0, 50.0, 25.0])
     ncell_max = 800
     props = []
@@ -657,6 +658,7 @@ def run_body(args):
         one.forward(nc[:1], pp[:1], qq[:1], locs[:1], n0[:1], n1[:1])
         pms.append((time.perf_counter() - t0) * 1e3)
     one.close()
+    location = body_location_steps(lk, grid, settings, data, ev, locs, n0, n1, args) if args.dynamic else None
     desc, err, dtype = BODY_SOLVERS[solver]
     from mctomo_gb300 import lib as _mlib
     # the tile solver's tuned configuration (shape index * 4 + sweeps index)
@@ -677,6 +679,8 @@ def run_body(args):
                       "p50_ms": round(float(np.percentile(pms, 50)), 3),
                       "p99_ms": round(float(np.percentile(pms, 99)), 3)},
             "clocks": cl, "valid_models": int((out[:, 3] == 0).sum())}
+    if location is not None:
+        line["location"] = location
     if rank == 0:
         chains = sorted({0, nch // 3, (2 * nch) // 3})[:args.body_sample]
         try:
@@ -691,6 +695,72 @@ def run_body(args):
     lk.close()
     if ws > 1:
         torch.distributed.destroy_process_group()
+
+
+def body_location_steps(lk, grid, settings, data, ev, locs, n0, n1, args):
+    """Location steps on the stored fields (settings dynamic = 1): the last
+    forward's models are committed, then every step proposes new locations
+    for all events of every chain (Gaussian, 0.2 km) and evaluates them
+    through the host API; the CPU column is the oracle's read-out of the
+    same 120 fields per chain (OpenMP over phases and stations) and the
+    misfit, for one chain."""
+    nch = locs.shape[0]
+    lk.commit(np.ones(nch, np.int32))
+    rng = np.random.default_rng(SEED + 9)
+    ext = np.array([grid["dx"] * (grid["nx"] - 1), grid["dy"] * (grid["ny"] - 1), grid["dz"] * (grid["nz"] - 1)])
+    props = []
+    for _ in range(args.warmup + args.steps):
+        p = locs.copy()
+        p[:, :, :3] = np.clip(p[:, :, :3] + rng.normal(0, 0.2, p[:, :, :3].shape), 0.0, ext)
+        props.append(p)
+    for i in range(args.warmup):
+        lk.location_likelihood(props[i], n0, n1)
+    ms = []
+    for i in range(args.warmup, args.warmup + args.steps):
+        t0 = time.perf_counter()
+        out = lk.location_likelihood(props[i], n0, n1)
+        ms.append((time.perf_counter() - t0) * 1e3)
+    res = {"value": round(nch * len(ms) / (sum(ms) / 1e3), 2), "unit": "location steps/s (chains x steps)",
+           "ms_per_step": round(float(np.mean(ms)), 4), "p50_ms": round(float(np.percentile(ms, 50)), 4),
+           "p99_ms": round(float(np.percentile(ms, 99)), 4), "valid": int((out[:, 3] == 0).sum()),
+           "reads_per_step": int(nch * settings["np"] * data["nsrc"] * len(data["rev"]))}
+    if not args.no_cpu:
+        import oracle
+        orc = oracle.load()
+        P = lambda a: a.ctypes.data_as(ctypes.c_void_p)  # noqa: E731
+        npp, nsrc, nrev = settings["np"], data["nsrc"], len(data["rev"])
+        fields = rng.uniform(0.0, 20.0, (npp, nrev, grid["nx"], grid["ny"], grid["nz"]))
+        ev0 = np.ascontiguousarray(props[-1][0])
+        times = np.zeros((npp, nsrc, nrev))
+        reps = 5
+        t0 = time.perf_counter()
+        for _ in range(reps):
+            orc.orc_location_times(grid["nx"], grid["ny"], grid["nz"], grid["xmin"], grid["ymin"], grid["zmin"],
+                                   grid["dx"], grid["dy"], grid["dz"], grid["scaling"], npp, nsrc, nrev, P(fields),
+                                   P(ev0), P(times))
+            body_location_cpu_misfit(orc, settings, data, ev0, times, n0[0], n1[0])
+        dt = (time.perf_counter() - t0) / reps
+        res["cpu_baseline"] = {"value": round(1.0 / dt, 2), "unit": "location steps/s", "cores": os.cpu_count() or 1,
+                               "kind": "port", "sample": "%d location steps of one chain: the oracle's Interpolate3d "
+                                                         "read-out of its %d stored fields (OpenMP) and misfit"
+                                                         % (reps, npp * nrev)}
+    return res
+
+
+def body_location_cpu_misfit(orc, settings, data, ev, pt, n0, n1):
+    """The oracle's misfit of a location step (sigma = n0 * time + n1)."""
+    P = lambda a: a.ctypes.data_as(ctypes.c_void_p)  # noqa: E731
+    npp, nsrc, nrev = pt.shape
+    npairs = nsrc * nrev
+    dtt = np.zeros((npp, 3, npairs))
+    dtt[:, 0] = np.asarray(data["ttime"]).reshape(npp, npairs)
+    rs = np.zeros((npp, 2, npairs), np.int32); rs[:, 0] = np.asarray(data["raystat"]).reshape(npp, npairs)
+    sig = np.zeros((npp, npairs)); out = np.zeros(3)
+    ptf = np.ascontiguousarray(pt.reshape(npp, npairs))
+    orc.orc_body_misfit(nsrc, nrev, npp, P(ptf), P(np.ascontiguousarray(ev[:, 3])), P(np.ascontiguousarray(dtt)),
+                        P(np.ascontiguousarray(rs)), P(ptf), 1, P(np.ascontiguousarray(n0)),
+                        P(np.ascontiguousarray(n1)), data["nrays"], P(sig), P(out))
+    return out
 
 
 def body_oracle_proposal(grid, settings, data, ev, n, pts, par, n0, n1, threads):
@@ -1466,6 +1536,8 @@ def main():
     ap.add_argument("--order", type=int, default=0, help="body workload: eikonal order")
     ap.add_argument("--body-sample", type=int, default=2, help="body workload: proposals checked by the oracle")
     ap.add_argument("--dropin-threads", type=int, default=16, help="dropin workload: host threads")
+    ap.add_argument("--dynamic", action="store_true",
+                    help="body workload: keep the stations' travel-time fields and time location steps on them")
     ap.add_argument("--solver", default=None, choices=["tiles", "heap"],
                     help="body workload: 3D solver (default: heap march for order 1, tiles for order 0)")
     ap.add_argument("--case", default=None, choices=["fm2d", "eik3", "eik3heap", "disp", "grid", "tiles"],

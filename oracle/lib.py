@@ -75,6 +75,7 @@ def load():
             "orc_convert_to_layer": (_I, [_P, _P, _P, _I, _D, _D, _D, _P, _P, _P, _P]),
             "orc_surf_misfit": (_I, [_I, _I, _I, _P, _P, _P, _P, _I, _P, _P, _I, _P, _P]),
             "orc_body_misfit": (_I, [_I, _I, _I, _P, _P, _P, _P, _P, _I, _P, _P, _I, _P, _P]),
+            "orc_location_times": (_I, [_I, _I, _I, _D, _D, _D, _D, _D, _D, _D, _I, _I, _I, _P, _P, _P]),
             "orc_tt2d_misfit": (_I, [_I, _I, _P, _P, _P, _P, _I, _I, _P, _P, _I, _P, _P, _I, _P]),
             "orc_tt2d_noise": (_I, [_I, _I, _P, _P, _P, _P, _I, _P, _P, _I, _P, _P, _I, _P]),
             "orc_surf_likelihood": (_I, [_P, _P, _P, _D, _D, _I, _P, _P, _I, _P, _I, _P, _I, _P,

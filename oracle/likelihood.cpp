@@ -135,6 +135,46 @@ int orc_surf_misfit(int nsrc, int nrev, int np, const double *phase_time,
   return status;
 }
 
+// Location-step read-out (src/likelihood_body.F90:104-111): phase_time(k, j,
+// p) = Interpolate3d (:976-1005, point2idx :1038-1054) of field (p, k) at
+// event j, fields [np][nrev][nx][ny][nz] (z fastest), events [nsrc][4],
+// times [np][nsrc][nrev]; OpenMP over phases and stations.
+int orc_location_times(int nx, int ny, int nz, double xmin, double ymin, double zmin, double dx, double dy,
+                       double dz, double scaling, int np, int nsrc, int nrev, const double *fields,
+                       const double *events, double *times) {
+  const size_t nn = (size_t)nx * ny * nz;
+#pragma omp parallel for collapse(2) schedule(static)
+  for (int p = 0; p < np; ++p)
+    for (int k = 0; k < nrev; ++k) {
+      const double *f = fields + ((size_t)p * nrev + k) * nn;
+      for (int j = 0; j < nsrc; ++j) {
+        const double *pt = events + 4 * (size_t)j;
+        int ix = (int)std::floor((pt[0] - xmin) / dx) + 1;
+        int iy = (int)std::floor((pt[1] - ymin) / dy) + 1;
+        int iz = (int)std::floor((pt[2] - zmin / scaling) / (dz / scaling)) + 1;
+        if (ix < 1) ix = 1;
+        if (iy < 1) iy = 1;
+        if (iz < 1) iz = 1;
+        if (ix >= nx) ix = nx - 1;
+        if (iy >= ny) iy = ny - 1;
+        if (iz >= nz) iz = nz - 1;
+        const double dsx = pt[0] - (xmin + (ix - 1) * dx);
+        const double dsy = pt[1] - (ymin + (iy - 1) * dy);
+        const double dsz = pt[2] - (zmin + (iz - 1) * dz) / scaling;
+        double qv = 0;
+        for (int i = 1; i <= 2; ++i)
+          for (int jj = 1; jj <= 2; ++jj)
+            for (int kk = 1; kk <= 2; ++kk) {
+              const double w = (1.0 - std::fabs((i - 1) * dx - dsx) / dx) * (1.0 - std::fabs((jj - 1) * dy - dsy) / dy) *
+                               (1.0 - std::fabs((kk - 1) * dz / scaling - dsz) / (dz / scaling));
+              qv = qv + w * f[((size_t)(ix + i - 2) * ny + (iy + jj - 2)) * nz + (iz + kk - 2)];
+            }
+        times[((size_t)p * nsrc + j) * nrev + k] = qv;
+      }
+    }
+  return 0;
+}
+
 // Body-wave misfit (src/likelihood_body.F90:284-333; with sigdep != 0 and
 // srdist = phase_time also body_noise_likelihood, :38-80): residual adds the
 // event origin time t0[j] (locations(4,j)).

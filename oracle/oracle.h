@@ -72,6 +72,9 @@ int orc_tt2d_noise(int nsrc, int nrev, const double *phase_time, const double *d
                    const int *raystat, const double *srdist, int datatype, const double *dtime,
                    const double *dcc, int ndtime, const double *n0, const double *n1, int nrays,
                    double *out);
+int orc_location_times(int nx, int ny, int nz, double xmin, double ymin, double zmin, double dx, double dy,
+                       double dz, double scaling, int np, int nsrc, int nrev, const double *fields,
+                       const double *events, double *times);
 int orc_body_misfit(int nsrc, int nrev, int np, const double *phase_time,
                     const double *t0, const double *dat_ttime,
                     const int *raystat, const double *srdist, int sigdep,

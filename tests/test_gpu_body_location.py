@@ -83,6 +83,13 @@ def test_location_step_reads_the_committed_fields(orc, gpulib):
                 for k in range(nrev):
                     exp[p, j, k] = oloc.interpolate3d(fields[p][k], grid, new[c, j, :3])
         np.testing.assert_array_equal(times[c].reshape(2, nsrc, nrev), exp)
+        # the oracle's C read-out (the CPU path the bench times) agrees
+        ct = np.zeros((2, nsrc, nrev))
+        orc.orc_location_times(grid["nx"], grid["ny"], grid["nz"], grid["xmin"], grid["ymin"], grid["zmin"],
+                               grid["dx"], grid["dy"], grid["dz"], grid["scaling"], 2, nsrc, nrev,
+                               P(np.ascontiguousarray(np.stack([np.stack(f) for f in fields]))),
+                               P(np.ascontiguousarray(new[c])), P(ct))
+        np.testing.assert_array_equal(ct, exp)
         eo = body_misfit(orc, dict(settings, sigdep=1), data, new[c], exp, n0[c], n1[c])
         np.testing.assert_allclose(out[c, :3], eo, rtol=1e-12)
     # chain 0 accepts its location step: its committed times are now the

@@ -235,3 +235,23 @@ def test_kdtree_oracle_on_the_reference_vertices(orc):
             i = orc.orc_kdtree_nearest(3, pts.shape[0], P(pts), P(np.ascontiguousarray(q)))
             dd = ((pts - q) ** 2).sum(1)
             assert dd[i - 1] == dd.min()
+
+
+def test_location_readout_c_matches_the_python_restatement(orc):
+    # orc_location_times (C, OpenMP) against oracle.location.interpolate3d
+    # (plain Python) on random fields, events inside and on the grid's faces
+    from oracle import location as oloc
+    P = lambda a: a.ctypes.data_as(ctypes.c_void_p)  # noqa: E731
+    rng = np.random.default_rng(5)
+    grid = dict(nx=9, ny=7, nz=6, xmin=1.0, ymin=-2.0, zmin=0.5, dx=0.5, dy=0.75, dz=0.4, scaling=2.0)
+    fields = rng.uniform(0, 10, (2, 3, 9, 7, 6))
+    ev = np.zeros((11, 4))
+    ev[:, 0] = rng.uniform(1.0, 5.0, 11); ev[:, 1] = rng.uniform(-2.0, 2.5, 11)
+    ev[:, 2] = rng.uniform(0.25, 1.25, 11)
+    ev[0, :3] = [5.0, 2.5, 1.25]; ev[1, :3] = [1.0, -2.0, 0.25]
+    out = np.zeros((2, 11, 3))
+    orc.orc_location_times(9, 7, 6, 1.0, -2.0, 0.5, 0.5, 0.75, 0.4, 2.0, 2, 11, 3, P(fields), P(ev), P(out))
+    for p in range(2):
+        for j in range(11):
+            for k in range(3):
+                assert out[p, j, k] == oloc.interpolate3d(fields[p, k], grid, ev[j, :3])
