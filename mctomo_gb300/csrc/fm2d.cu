@@ -1054,6 +1054,7 @@ __device__ __forceinline__ void refined_block(const Fm2dJob &job, int solve_byte
   const int bar1 = 1 + 2 * pair, bar2 = 2 + 2 * pair;
   int solve = (blk * (blockDim.x >> 6) + pair) * SPW + slot;
   if (redo) solve = solve < *job.ovf_count ? job.ovf_list[solve] : job.nsolve;
+  else if (job.ref_list) solve = solve < *job.ref_count ? job.ref_list[solve] : job.nsolve;
   SolveGeom sg;
   const bool active = solve < job.nsolve && solve_geom(job, solve, sg);   // geometry errors: coarse stage
   if (!__any_sync(0xffffffffu, active)) return;   // the same for both warps of the pair
@@ -1438,6 +1439,49 @@ fm2d_coarse_kernel(Fm2dJob job, int solve_bytes, int nblk) {
 }  // namespace
 
 namespace {
+// The refined stage's reuse test, one warp per solve: the solve's map and
+// its committed map agree over the padded vertices the box's B-spline
+// velocities read (the box's vertex cells and 3 vertices beyond, which
+// covers the 4-vertex support of every refined node and the source); then
+// the committed box mapping is copied in, else the solve joins the list
+// that marches. The refined result depends on nothing else (the march
+// stops at the box, its update and slowness read only the box).
+__global__ void ref_reuse_kernel(Fm2dJob job) {
+  const int lane = threadIdx.x & 31;
+  const int q = (int)((blockIdx.x * (size_t)blockDim.x + threadIdx.x) >> 5);
+  if (q >= job.nsolve) return;
+  SolveGeom sg;
+  const bool geom = solve_geom(job, q, sg);
+  const int cs = job.csolve[q];
+  const int cm = geom ? job.cmap[sg.map] : -1;
+  bool same = geom && cs >= 0 && cm >= 0;
+  if (same) {
+    const int ldv = job.nvz + 2;
+    const int xl = max((sg.vnl - 1) / job.gdx + 1 - 3, 0), xr = min((sg.vnr - 1) / job.gdx + 1 + 3, job.nvx + 1);
+    const int zl = max((sg.vnt - 1) / job.gdz + 1 - 3, 0), zr = min((sg.vnb - 1) / job.gdz + 1 + 3, job.nvz + 1);
+    const double *a = job.velv + (size_t)sg.map * (job.nvx + 2) * ldv;
+    const double *b = job.cvelv + (size_t)cm * (job.nvx + 2) * ldv;
+    const int w = zr - zl + 1, n = (xr - xl + 1) * w;
+    bool diff = false;
+    for (int i = lane; i < n; i += 32) {
+      const size_t o = (size_t)(xl + i / w) * ldv + zl + i % w;
+      diff |= __double_as_longlong(a[o]) != __double_as_longlong(b[o]);
+    }
+    same = !__any_sync(0xffffffffu, diff);
+  }
+  if (same) {
+    const double *ct = job.cref_t + (size_t)cs * job.map_tmp_max;
+    const short *cs2 = job.cref_s + (size_t)cs * job.map_tmp_max;
+    double *tt = job.map_tmp_t + (size_t)q * job.map_tmp_max;
+    short *ts = job.map_tmp_s + (size_t)q * job.map_tmp_max;
+    for (int i = lane; i < job.map_tmp_max; i += 32) { tt[i] = ct[i]; ts[i] = cs2[i]; }
+  } else if (lane == 0) {
+    job.ref_list[atomicAdd(job.ref_count, 1)] = q;
+  }
+}
+}  // namespace
+
+namespace {
 // Warp pairs per block for kernel k with pair_bytes of shared memory per
 // pair: the block size that keeps the most pairs resident per SM (shared
 // memory, registers and the block limit all counted by the occupancy
@@ -1700,6 +1744,11 @@ int launch_solves(const Fm2dJob &job, const Fm2dPlan &plan, cudaStream_t s) {
   if (job.asgr == 1) {
     if (!job.ovf_list || !job.ovf_count) return MCT_ERR_ARG;
     MCT_CUDA_TRY(cudaMemsetAsync(job.ovf_count, 0, sizeof(int), s));
+    if (job.ref_list) {
+      MCT_CUDA_TRY(cudaMemsetAsync(job.ref_count, 0, sizeof(int), s));
+      ref_reuse_kernel<<<(job.nsolve + 7) / 8, 256, 0, s>>>(job);
+      MCT_CUDA_TRY(cudaGetLastError());
+    }
     rc = g_spw_refined == 2 ? launch_refined<TT, 2>(job, plan.ref_warp_bytes, plan.ref_heap_cap, 0, sh, s)
                             : launch_refined<TT, 1>(job, plan.ref_warp_bytes, plan.ref_heap_cap, 0, sh, s);
     if (rc) return rc;
@@ -1730,6 +1779,9 @@ int launch_fm2d(const Fm2dJob &job, const Fm2dPlan &plan, cudaStream_t s) {
     refine_slowness_kernel<<<dim3(bx, job.nmaps), 256, tab, s>>>(job);
     MCT_CUDA_TRY(cudaGetLastError());
   }
+  if (job.ref_list && (job.asgr != 1 || job.rays || job.precision == 2 || !job.ref_count || !job.cvelv ||
+                        !job.cmap || !job.csolve || !job.cref_t || !job.cref_s))
+    return MCT_ERR_ARG;
   if (job.precision == 2) return launch_solves<int>(job, plan, s);
   if (job.precision == 1) return launch_solves<float2>(job, plan, s);
   return launch_solves<double>(job, plan, s);

@@ -45,6 +45,18 @@ struct Fm2dJob {
   void *tws_ref, *tws;
   int tslots_ref, tslots;
   int sglobal_ref, sglobal;
+  // optional reuse of committed refined-box results (asgr = 1, no rays,
+  // precision 0 or 1): a solve whose map equals its committed map over the
+  // refined box and the B-spline's reach gets the committed box mapping
+  // instead of a march. cmap [nmaps]: the committed map (index into cvelv)
+  // of each map, -1 for none; csolve [nsolve]: the committed solve (index
+  // into cref_t / cref_s) of each solve, -1 for none; ref_list [nsolve] and
+  // ref_count [1]: scratch, the solves that march
+  const double *cvelv;       // [ncommitted maps][nvx+2][nvz+2]
+  const int *cmap, *csolve;
+  const double *cref_t;      // [ncommitted solves][map_tmp_max]
+  const short *cref_s;
+  int *ref_list, *ref_count;
 };
 
 struct Fm2dPlan {

@@ -126,6 +126,8 @@ int surf_create(const mct_grid *g, const mct_surf_settings *st, const mct_surf_d
   const Fm2dPlan &fp = c->plan.fm2d_plan;
   const size_t nsolve = all.size();
   const int nn = (g->nx - 1) * fj.gdx + 1, nz2 = (g->ny - 1) * fj.gdz + 1;
+  // fm2d may reuse a committed refined box whose maps are unchanged
+  const bool reuse = fj.asgr == 1 && !b.igr && !b.straight && fj.precision != 2;
   size_t kd = kd_scratch_bytes(ncell_max);
   std::vector<size_t> sz = {
       sizeof(double) * np, sizeof(int) * np * npairs, sizeof(double) * np * npairs, sizeof(double) * np * npairs,
@@ -157,7 +159,11 @@ int surf_create(const mct_grid *g, const mct_surf_settings *st, const mct_surf_d
       (b.igr && !b.straight) ? sizeof(short) * (size_t)fp.nref_max * nsolve : 0,
       sizeof(int) * (size_t)nslots * ncol,
       // fm2d time-field slots
-      fm2d_tws_bytes(fp, (long)nsolve)};
+      fm2d_tws_bytes(fp, (long)nsolve),
+      // committed refined-box results (reuse)
+      reuse ? sizeof(double) * (size_t)nslots * np * nvv : 0,
+      reuse ? sizeof(double) * nsolve * fp.map_tmp_max : 0, reuse ? sizeof(short) * nsolve * fp.map_tmp_max : 0,
+      reuse ? sizeof(int) * ((size_t)nslots * np + nsolve + nsolve + 1) : 0};
   size_t total = 0;
   for (size_t s : sz) total = ((total + 255) & ~size_t(255)) + s;
   total += 256;
@@ -241,6 +247,18 @@ int surf_create(const mct_grid *g, const mct_surf_settings *st, const mct_surf_d
   fj.ref_s = cv.take<short>((b.igr && !b.straight) ? (size_t)fp.nref_max * nsolve : 0);
   b.lorder = cv.take<int>((size_t)nslots * ncol);
   fm2d_bind_tws(fj, fp, (long)nsolve, cv.take<char>(fm2d_tws_bytes(fp, (long)nsolve)));
+  b.reuse = reuse ? 1 : 0;
+  b.spc = spc;
+  b.map_tmp_max = fp.map_tmp_max;
+  b.map_tmp_t = fj.map_tmp_t;
+  b.map_tmp_s = fj.map_tmp_s;
+  b.cvelv = cv.take<double>(reuse ? (size_t)nslots * np * nvv : 0);
+  b.cref_t = cv.take<double>(reuse ? nsolve * fp.map_tmp_max : 0);
+  b.cref_s = cv.take<short>(reuse ? nsolve * fp.map_tmp_max : 0);
+  b.cmap = cv.take<int>(reuse ? (size_t)nslots * np + 2 * nsolve + 1 : 0);
+  b.csolve = b.cmap + (size_t)nslots * np;
+  b.ref_list = b.csolve + nsolve;
+  b.ref_count = b.ref_list + nsolve;
   b.sdist = sdist;
   c->plan.src_xy = sxy; c->plan.rev_xy = sxy + 2 * nsrc;
   {

@@ -188,6 +188,36 @@ __global__ void misfit_kernel(SurfBatch b) {
 }
 
 // Copy a chain's proposal into its slot's committed state.
+// Committed counterparts of this forward's maps and solves (-1: the slot
+// holds no committed state), for the reuse test of the refined stage.
+__global__ void reuse_index_kernel(SurfBatch b, int nch) {
+  const int stride = gridDim.x * blockDim.x, i0 = blockIdx.x * blockDim.x + threadIdx.x;
+  for (int m = i0; m < nch * b.np; m += stride) {
+    const int slot = b.slots[m / b.np];
+    b.cmap[m] = b.committed[slot] ? slot * b.np + m % b.np : -1;
+  }
+  for (int q = i0; q < nch * b.spc; q += stride) {
+    const int slot = b.slots[q / b.spc];
+    b.csolve[q] = b.committed[slot] ? slot * b.spc + q % b.spc : -1;
+  }
+}
+
+// An accepted forward's padded maps and refined-box mappings become the
+// slot's committed ones (beside commit_kernel's state).
+__global__ void commit_ref_kernel(SurfBatch b, const int *accept) {
+  const int c = blockIdx.y;
+  if (!accept[c] || b.status[c]) return;
+  const int slot = b.slots[c];
+  const size_t nvv = (size_t)(b.nx + 2) * (b.ny + 2) * b.np;
+  for (size_t q = blockIdx.x * blockDim.x + threadIdx.x; q < nvv; q += (size_t)gridDim.x * blockDim.x)
+    b.cvelv[(size_t)slot * nvv + q] = b.velv[(size_t)c * nvv + q];
+  const size_t nt = (size_t)b.spc * b.map_tmp_max;
+  for (size_t q = blockIdx.x * blockDim.x + threadIdx.x; q < nt; q += (size_t)gridDim.x * blockDim.x) {
+    b.cref_t[(size_t)slot * nt + q] = b.map_tmp_t[(size_t)c * nt + q];
+    b.cref_s[(size_t)slot * nt + q] = b.map_tmp_s[(size_t)c * nt + q];
+  }
+}
+
 __global__ void commit_kernel(SurfBatch b, const int *accept) {
   const int c = blockIdx.y;
   if (!accept[c] || b.status[c]) return;
@@ -403,6 +433,12 @@ int surf_forward(SurfBatch &b, const SurfPlan &plan, cudaStream_t s, SurfProfile
       fj.rays = 1; fj.gvel = b.gvel; fj.gtime = b.gtime; fj.raylen = b.raylen; fj.crazy = b.crazy;
       MCT_CUDA_TRY(cudaMemsetAsync(b.crazy, 0, sizeof(int) * (size_t)nch * b.np, s));
     }
+    if (b.reuse) {
+      reuse_index_kernel<<<64, 256, 0, s>>>(b, nch);
+      MCT_CUDA_TRY(cudaGetLastError());
+      fj.cvelv = b.cvelv; fj.cmap = b.cmap; fj.csolve = b.csolve; fj.cref_t = b.cref_t; fj.cref_s = b.cref_s;
+      fj.ref_list = b.ref_list; fj.ref_count = b.ref_count;
+    }
     rc = launch_fm2d(fj, plan.fm2d_plan, s); if (rc) return rc;
   }
   if (ev) MCT_CUDA_TRY(cudaEventRecord(ev[3], s));
@@ -421,6 +457,10 @@ int surf_noise(const SurfBatch &b, int nchains, const int *slots, const double *
 }
 
 int surf_commit(SurfBatch &b, const int *accept_dev, cudaStream_t s) {
+  if (b.reuse) {
+    commit_ref_kernel<<<dim3(64, b.nchains), 256, 0, s>>>(b, accept_dev);
+    MCT_CUDA_TRY(cudaGetLastError());
+  }
   commit_kernel<<<dim3(64, b.nchains), 256, 0, s>>>(b, accept_dev);
   MCT_CUDA_TRY(cudaGetLastError());
   return MCT_OK;

@@ -53,6 +53,16 @@ struct SurfBatch {
   double *cttime;            // [nslots][np][nsrc][nrev] committed phase times
   double *csrd;              // [nslots][np][nsrc][nrev] their srdist (sigma = n0 srdist + n1)
   double *cgvel;             // [nslots][np][nx][ny] committed group maps (igr)
+  // reuse of committed refined-box results in fm2d (reuse = 1: refined
+  // source boxes, no rays, FP64 or double-float times)
+  int reuse, spc, map_tmp_max;
+  double *cvelv;             // [nslots][np][(nx+2)(ny+2)] committed padded phase maps
+  double *cref_t;            // [nslots][spc][map_tmp_max] committed refined-box mappings
+  short *cref_s;
+  int *cmap, *csolve;        // per forward: [nchains*np], [nchains*spc] committed map / solve or -1
+  int *ref_list, *ref_count; // [nslots*spc], [1]
+  const double *map_tmp_t;   // the forward's mappings (fm2d scratch)
+  const short *map_tmp_s;
 };
 
 // Optional per-stage timing: events recorded around the stages of each
