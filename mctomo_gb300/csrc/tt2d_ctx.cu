@@ -314,6 +314,29 @@ __global__ void tt2d_commit_kernel(int npairs, const int *accept, const double *
   if (blockIdx.x == 0 && threadIdx.x == 0) { cumis[c] = umis[c]; committed[c] = 1; }
 }
 
+// Committed counterparts of the forward's maps and solves for fm2d's reuse
+// of refined boxes (chain c is slot c; -1 while nothing is committed).
+__global__ void tt2d_reuse_index_kernel(int nchains, int spc, const int *committed, int *cmap, int *csolve) {
+  const int stride = gridDim.x * blockDim.x, i0 = blockIdx.x * blockDim.x + threadIdx.x;
+  for (int m = i0; m < nchains; m += stride) cmap[m] = committed[m] ? m : -1;
+  for (int q = i0; q < nchains * spc; q += stride) csolve[q] = committed[q / spc] ? q : -1;
+}
+
+// An accepted forward's padded map and refined-box mappings become the
+// chain's committed ones.
+__global__ void tt2d_commit_ref_kernel(const int *accept, const double *out, size_t nvv, const double *velv,
+                                       double *cvelv, size_t nref, const double *map_t, const short *map_s,
+                                       double *cref_t, short *cref_s) {
+  const int c = blockIdx.y;
+  if (!accept[c] || out[(size_t)c * 4 + 3] != 0.0) return;
+  for (size_t q = blockIdx.x * (size_t)blockDim.x + threadIdx.x; q < nvv; q += (size_t)gridDim.x * blockDim.x)
+    cvelv[(size_t)c * nvv + q] = velv[(size_t)c * nvv + q];
+  for (size_t q = blockIdx.x * (size_t)blockDim.x + threadIdx.x; q < nref; q += (size_t)gridDim.x * blockDim.x) {
+    cref_t[(size_t)c * nref + q] = map_t[(size_t)c * nref + q];
+    cref_s[(size_t)c * nref + q] = map_s[(size_t)c * nref + q];
+  }
+}
+
 }  // namespace
 
 struct mct_tt2d_ctx {
@@ -332,6 +355,10 @@ struct mct_tt2d_ctx {
   double *vel = nullptr, *velv = nullptr, *tt = nullptr;
   double *ctt = nullptr, *cumis = nullptr;     // committed state per slot
   int *committed = nullptr, *accept = nullptr;
+  // fm2d's reuse of committed refined boxes (refined source boxes only)
+  int reuse = 0;
+  double *cvelv = nullptr, *cref_t = nullptr; short *cref_s = nullptr;
+  int *cmap = nullptr, *csolve = nullptr, *ref_list = nullptr;
   // mct_tt2d_submit / mct_tt2d_poll: pinned staging (allocated by the first
   // submit), the completion event and the batch in flight
   int *h_ints = nullptr;       // [nslots] ncells, [2] device status
@@ -402,6 +429,8 @@ int mct_tt2d_create(const mct_grid *g, const mct_tt2d_settings *st, const mct_tt
   const int nnx = (nx - 1) * std::max(fj.gdx, 1) + 1, nnz = (ny - 1) * std::max(fj.gdz, 1) + 1;
   const size_t kd = kd_scratch_bytes(ncell_max);
   const bool fm = !st->straight;
+  // fm2d may reuse a committed refined box whose map is unchanged
+  const bool reuse = fm && fj.asgr == 1 && fj.precision != 2;
   std::vector<size_t> sz = {
       sizeof(int) * nslots, sizeof(double) * (size_t)nslots * ncell_max * 5, sizeof(double) * 4 * nslots,
       sizeof(double) * 8 * nslots, sizeof(double) * nslots,
@@ -416,7 +445,10 @@ int mct_tt2d_create(const mct_grid *g, const mct_tt2d_settings *st, const mct_tt
       fm ? sizeof(double) * (size_t)c->fp.map_tmp_max * nsolve : 0,
       fm ? sizeof(short) * (size_t)c->fp.map_tmp_max * nsolve : 0, sizeof(int) * (nsolve + 1),
       fm ? sizeof(double) * 2 * (size_t)nnx * nnz * nslots : 0, sizeof(int),
-      fm ? fm2d_tws_bytes(c->fp, (long)nsolve) : 0};
+      fm ? fm2d_tws_bytes(c->fp, (long)nsolve) : 0,
+      reuse ? sizeof(double) * nslots * nvv : 0, reuse ? sizeof(double) * (size_t)c->fp.map_tmp_max * nsolve : 0,
+      reuse ? sizeof(short) * (size_t)c->fp.map_tmp_max * nsolve : 0,
+      reuse ? sizeof(int) * ((size_t)nslots + 2 * nsolve + 1) : 0};
   size_t total = 0;
   for (size_t b : sz) total = ((total + 255) & ~size_t(255)) + b;
   total += 256;
@@ -463,6 +495,13 @@ int mct_tt2d_create(const mct_grid *g, const mct_tt2d_settings *st, const mct_tt
   fj.slon = fj.veln + (size_t)nnx * nnz * nslots;
   fj.vmin_bits = cv.take<int>(1);
   if (fm) fm2d_bind_tws(fj, c->fp, (long)nsolve, cv.take<char>(fm2d_tws_bytes(c->fp, (long)nsolve)));
+  c->reuse = reuse ? 1 : 0;
+  c->cvelv = cv.take<double>(reuse ? (size_t)nslots * nvv : 0);
+  c->cref_t = cv.take<double>(reuse ? (size_t)c->fp.map_tmp_max * nsolve : 0);
+  c->cref_s = cv.take<short>(reuse ? (size_t)c->fp.map_tmp_max * nsolve : 0);
+  c->cmap = cv.take<int>(reuse ? (size_t)nslots + 2 * nsolve + 1 : 0);
+  c->csolve = c->cmap + nslots;
+  c->ref_list = c->csolve + nsolve;
   // data in the reference's layouts
   std::vector<double> pd(5 * (size_t)npairs, 1.0), xy(2 * (size_t)(nsrc + nrev)), sep(2 * (size_t)(nsrc + nrev));
   std::vector<int2> pairs((size_t)std::max(ndd, 1), make_int2(0, 0));
@@ -606,6 +645,12 @@ int tt2d_enqueue(mct_tt2d_ctx *c, int nchains, const int *ncells, const double *
     Fm2dJob fj = c->fj;
     fj.nmaps = nchains; fj.velv = c->velv; fj.nsolve = c->spc * nchains;
     fj.ttime = c->tt; fj.tfield = nullptr; fj.status = c->gstatus + 1;
+    if (c->reuse) {
+      tt2d_reuse_index_kernel<<<64, 256, 0, s>>>(nchains, c->spc, c->committed, c->cmap, c->csolve);
+      MCT_CUDA_TRY(cudaGetLastError());
+      fj.cvelv = c->cvelv; fj.cmap = c->cmap; fj.csolve = c->csolve; fj.cref_t = c->cref_t; fj.cref_s = c->cref_s;
+      fj.ref_list = c->ref_list; fj.ref_count = c->ref_list + (size_t)c->spc * c->nslots;
+    }
     rc = launch_fm2d(fj, c->fp, s); if (rc) return rc;
   }
   tt2d_misfit_kernel<<<nchains, 256, 0, s>>>(d, c->tt, c->n0, c->n1, c->out, c->umis);
@@ -694,6 +739,13 @@ int mct_tt2d_commit(mct_tt2d_ctx *c, int nchains, const int *accept) {
   cudaStream_t s = c->stream;
   const int npairs = c->dev.nsrc * c->dev.nrev;
   MCT_CUDA_TRY(cudaMemcpyAsync(c->accept, accept, sizeof(int) * nchains, cudaMemcpyHostToDevice, s));
+  if (c->reuse) {
+    // before tt2d_commit_kernel sets the chains' committed flags
+    const size_t nvv = (size_t)(c->g.nx + 2) * (c->g.ny + 2), nref = (size_t)c->spc * c->fp.map_tmp_max;
+    tt2d_commit_ref_kernel<<<dim3(32, nchains), 256, 0, s>>>(c->accept, c->out, nvv, c->velv, c->cvelv, nref,
+                                                            c->fj.map_tmp_t, c->fj.map_tmp_s, c->cref_t, c->cref_s);
+    MCT_CUDA_TRY(cudaGetLastError());
+  }
   tt2d_commit_kernel<<<dim3((npairs + 255) / 256, nchains), 256, 0, s>>>(npairs, c->accept, c->out, c->tt, c->umis,
                                                                          c->ctt, c->cumis, c->committed);
   MCT_CUDA_TRY(cudaGetLastError());
