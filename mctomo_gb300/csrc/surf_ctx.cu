@@ -368,7 +368,7 @@ int mct_surf_forward_device(mct_surf_ctx *c, int nchains, const int *slots, cons
 int mct_surf_commit_device(mct_surf_ctx *c, const int *accept, void *stream) {
   if (!c || c->last_nchains < 1) return MCT_ERR_ARG;
   cudaStream_t s = stream ? static_cast<cudaStream_t>(stream) : c->stream;
-  c->prof.launches += 1;
+  c->prof.launches += c->b.reuse ? 2 : 1;
   return surf_commit(c->b, accept, s);
 }
 

@@ -378,7 +378,18 @@ int surf_forward(SurfBatch &b, const SurfPlan &plan, cudaStream_t s, SurfProfile
   cudaEvent_t *ev = nullptr;
   if (prof && prof->enabled && prof->step < prof->max_steps) ev = prof->ev + 5 * prof->step++;
   if (ev) MCT_CUDA_TRY(cudaEventRecord(ev[0], s));
-  if (prof) prof->launches += 12;
+  if (prof) {
+    // the kernels of one forward: material, gridding (3), layering and
+    // dispersion (4), the committed maps' gather and scatter, the misfit,
+    // and the travel-time stage's
+    const Fm2dJob &f = plan.fm2d;
+    const Fm2dPlan &fp = plan.fm2d_plan;
+    int n = 11;
+    if (b.straight) n += 1;
+    else n += 3 + (f.precision == 2 ? 1 : 0) + (f.asgr == 1 ? 2 + (fp.ref_heap_cap < fp.nref_max ? 1 : 0) : 0) +
+              (b.reuse ? 2 : 0);
+    prof->launches += n;
+  }
   const int ncol = b.nx * b.ny;
   MCT_CUDA_TRY(cudaMemsetAsync(b.status, 0, sizeof(int) * nch, s));
   MCT_CUDA_TRY(cudaMemsetAsync(b.list_count, 0, sizeof(int), s));
