@@ -100,6 +100,13 @@ module mctomo_gb300
     type(c_ptr) :: values0, values, indices
     integer(c_long_long) :: accepted, total
   end type
+  type, bind(C) :: mct_sample
+    integer(c_int) :: step, accepted, vindex
+    integer(c_long_long) :: ncells
+    real(c_double) :: misfit, unweighted_misfit, like
+    real(c_double) :: coord(3), values(3)
+    real(c_double) :: noise0, noise1
+  end type
 
   interface
     type(c_ptr) function mct_version() bind(C, name="mct_version")
@@ -605,6 +612,27 @@ contains
       type(mct_mcmc_set), intent(in) :: set
       type(mct_mcmc_step), intent(in) :: step
       real(c_double), value :: like_new, like_old, temperature
+    end function
+    integer(c_int) function mct_mcmc_record(state, step, accepted, like, misfit, unweighted_misfit, sample) &
+        bind(C, name="mct_mcmc_record")
+      import :: c_int, c_double, mct_mcmc_state, mct_mcmc_step, mct_sample
+      type(mct_mcmc_state), intent(in) :: state
+      type(mct_mcmc_step), intent(in) :: step
+      integer(c_int), value :: accepted
+      real(c_double), value :: like, misfit, unweighted_misfit
+      type(mct_sample), intent(out) :: sample
+    end function
+    integer(c_int) function mct_samples_write(filename, dim, samples, n) bind(C, name="mct_samples_write")
+      import :: c_int, c_char, mct_sample
+      character(kind=c_char), intent(in) :: filename(*)
+      integer(c_int), value :: dim, n
+      type(mct_sample), intent(in) :: samples(*)
+    end function
+    integer(c_int) function mct_samples_read(filename, dim, samples, n) bind(C, name="mct_samples_read")
+      import :: c_int, c_char, mct_sample
+      character(kind=c_char), intent(in) :: filename(*)
+      integer(c_int), value :: dim, n
+      type(mct_sample), intent(out) :: samples(*)
     end function
     integer(c_int) function mct_pt_init(pt) bind(C, name="mct_pt_init")
       import :: c_int, mct_pt

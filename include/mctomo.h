@@ -692,6 +692,35 @@ int mct_pt_init(mct_pt *pt);
 int mct_pt_choose(mct_pt *pt, mct_rng *rng, int *t1_chain, int *t2_chain);
 int mct_pt_swap(mct_pt *pt, mct_rng *rng, int t1_chain, int t2_chain, double like_t1, double like_t2);
 
+/* ------------------------------------------------------------------------
+ * The sample stream (samples_*.out, run_time_sample_*.dat): one T_SAMPLE
+ * (src/run_time_info.f90:62-76) per iteration. mct_mcmc_record fills it as
+ * the MCMC loop does after the acceptance test (src/mcmc_loc2.f90:253-263,
+ * 305-315, 345-355, 425-436, 487-497, 578-582): zeros and the step's type;
+ * for an accepted step the new cell's nucleus and values (birth), the
+ * removed cell (death), the moved nucleus (move), the cell's new values
+ * (value change) or the period's new noise levels (noise steps); then the
+ * chain's current number of cells, -log L, misfit and unweighted misfit.
+ * state is the chain's state after the decision (restored on rejection).
+ * mct_samples_write appends records to a file (creating it) in
+ * write_samples' stream layout (run_time_info.f90:306-340): int32 step,
+ * 1-byte accepted, int32 vindex, int64 ncells, misfit, unweighted misfit,
+ * like, dim coordinates (dim 2 for the 2D code, 3), 3 values, noise0,
+ * noise1, unpadded little-endian. mct_samples_read reads up to n records
+ * and returns how many it read (< 0: error). Host only.
+ * ---------------------------------------------------------------------- */
+typedef struct {
+  int step, accepted, vindex;
+  long long ncells;
+  double misfit, unweighted_misfit, like;
+  double coord[3], values[3];
+  double noise0, noise1;
+} mct_sample;
+int mct_mcmc_record(const mct_mcmc_state *state, const mct_mcmc_step *step, int accepted, double like,
+                    double misfit, double unweighted_misfit, mct_sample *sample);
+int mct_samples_write(const char *filename, int dim, const mct_sample *samples, int n);
+int mct_samples_read(const char *filename, int dim, mct_sample *samples, int n);
+
 #ifdef __cplusplus
 }
 #endif

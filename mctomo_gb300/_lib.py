@@ -76,6 +76,9 @@ SIGNATURES = {
     "mct_mcmc_accept": (I, [P, P, D, D]),
     "mct_mcmc_accept_tempered": (I, [P, P, D, D, D]),
     "mct_pt_init": (I, [P]),
+    "mct_mcmc_record": (I, [P, P, I, D, D, D, P]),
+    "mct_samples_write": (I, [ctypes.c_char_p, I, P, I]),
+    "mct_samples_read": (I, [ctypes.c_char_p, I, P, I]),
     "mct_pt_choose": (I, [P, P, P, P]),
     "mct_pt_swap": (I, [P, P, I, I, D, D]),
     "mct_surf_create": (I, [P, P, P, I, I, P]),

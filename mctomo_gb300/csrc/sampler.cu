@@ -13,7 +13,11 @@
 // (:200-222). Each generator counts its draws as RTI%randcount does.
 #include "mct_common.cuh"
 #include <cmath>
+#include <cstdint>
+#include <cstdio>
 #include <cstdlib>
+#include <cstring>
+#include <vector>
 #include <new>
 #include <utility>
 
@@ -462,6 +466,119 @@ int mct_pt_swap(mct_pt *pt, mct_rng *rng, int t1_chain, int t2_chain, double lik
   }
   ++pt->total;
   return swapped;
+}
+
+}  // extern "C"
+
+// ---------------------------------------------------------------------------
+// The sample stream (samples_*.out and run_time_sample_*.dat): T_SAMPLE
+// (src/run_time_info.f90:62-76) filled as the MCMC loop fills it
+// (src/mcmc_loc2.f90:253-263, 305-315, 345-355, 425-436, 487-497, and
+// :578-582 for every iteration) and written with stream access field by
+// field, unpadded (write_samples, run_time_info.f90:306-340; the reference's
+// plot/plot_point_values.m:46-56 reads the same layout).
+// ---------------------------------------------------------------------------
+namespace {
+size_t sample_bytes(int dim) { return 4 + 1 + 4 + 8 + 3 * 8 + (size_t)dim * 8 + 3 * 8 + 2 * 8; }
+}  // namespace
+
+extern "C" {
+
+int mct_mcmc_record(const mct_mcmc_state *st, const mct_mcmc_step *step, int accepted, double like, double misfit,
+                    double unweighted_misfit, mct_sample *sm) {
+  if (!st || !step || !sm) return MCT_ERR_ARG;
+  *sm = mct_sample{};   // init_sample: zeros
+  sm->step = step->ptype;
+  const bool acc = accepted && step->valid;
+  if (acc) {
+    sm->accepted = 1;
+    const int i = step->index - 1;
+    switch (step->ptype) {
+      case 1:   // birth: the new cell's nucleus and values
+      case 3:   // move: the moved nucleus (vindex), no values
+        if (i < 0 || i >= st->ncells) return MCT_ERR_ARG;
+        sm->vindex = step->ptype == 1 ? 0 : step->index;
+        for (int k = 0; k < 3; ++k) sm->coord[k] = st->points[3 * (size_t)i + k];
+        if (step->ptype == 1)
+          for (int k = 0; k < 3; ++k) sm->values[k] = st->parameters[3 * (size_t)i + k];
+        break;
+      case 2:   // death: the removed cell's index
+        sm->vindex = step->index;
+        break;
+      case 4:   // value change: the cell's new values
+        if (i < 0 || i >= st->ncells) return MCT_ERR_ARG;
+        sm->vindex = step->index;
+        for (int k = 0; k < 3; ++k) sm->values[k] = st->parameters[3 * (size_t)i + k];
+        break;
+      case 5:   // body-wave noise of period index
+      case 6: { // surface-wave noise
+        const int n = step->ptype == 5 ? st->nbnoise : st->nsnoise;
+        const double *a = step->ptype == 5 ? st->bnoise0 : st->snoise0, *b = step->ptype == 5 ? st->bnoise1 : st->snoise1;
+        if (i < 0 || i >= n || !a || !b) return MCT_ERR_ARG;
+        sm->vindex = step->index;
+        sm->noise0 = a[i];
+        sm->noise1 = b[i];
+        break;
+      }
+      default:
+        return MCT_ERR_ARG;
+    }
+  }
+  // every iteration: the chain's current state (mcmc_loc2.f90:578-582)
+  sm->ncells = st->ncells;
+  sm->like = like;
+  sm->misfit = misfit;
+  sm->unweighted_misfit = unweighted_misfit;
+  return MCT_OK;
+}
+
+int mct_samples_write(const char *filename, int dim, const mct_sample *samples, int n) {
+  if (!filename || (dim != 2 && dim != 3) || n < 0 || (n > 0 && !samples)) return MCT_ERR_ARG;
+  if (n == 0) return MCT_OK;
+  FILE *f = std::fopen(filename, "ab");   // appended, created when absent
+  if (!f) { mct_set_error("mct_samples_write", "cannot open the file", __FILE__, __LINE__); return MCT_ERR_ARG; }
+  std::vector<unsigned char> buf(sample_bytes(dim) * (size_t)n);
+  unsigned char *p = buf.data();
+  auto put = [&](const void *v, size_t b) { std::memcpy(p, v, b); p += b; };
+  for (int r = 0; r < n; ++r) {
+    const mct_sample &s = samples[r];
+    const int32_t step = s.step, vindex = s.vindex;
+    const unsigned char acc = s.accepted ? 1 : 0;
+    const int64_t ncells = s.ncells;
+    put(&step, 4); put(&acc, 1); put(&vindex, 4); put(&ncells, 8);
+    put(&s.misfit, 8); put(&s.unweighted_misfit, 8); put(&s.like, 8);
+    put(s.coord, 8 * (size_t)dim); put(s.values, 24); put(&s.noise0, 8); put(&s.noise1, 8);
+  }
+  const size_t w = std::fwrite(buf.data(), 1, buf.size(), f);
+  const int cl = std::fclose(f);
+  if (w != buf.size() || cl != 0) {
+    mct_set_error("mct_samples_write", "short write", __FILE__, __LINE__);
+    return MCT_ERR_INTERNAL;
+  }
+  return MCT_OK;
+}
+
+int mct_samples_read(const char *filename, int dim, mct_sample *samples, int n) {
+  if (!filename || (dim != 2 && dim != 3) || n < 0 || (n > 0 && !samples)) return MCT_ERR_ARG;
+  FILE *f = std::fopen(filename, "rb");
+  if (!f) { mct_set_error("mct_samples_read", "cannot open the file", __FILE__, __LINE__); return MCT_ERR_ARG; }
+  const size_t rb = sample_bytes(dim);
+  std::vector<unsigned char> buf(rb);
+  int got = 0;
+  while (got < n && std::fread(buf.data(), 1, rb, f) == rb) {
+    const unsigned char *p = buf.data();
+    auto take = [&](void *v, size_t b) { std::memcpy(v, p, b); p += b; };
+    mct_sample &s = samples[got];
+    s = mct_sample{};
+    int32_t step, vindex; unsigned char acc; int64_t ncells;
+    take(&step, 4); take(&acc, 1); take(&vindex, 4); take(&ncells, 8);
+    take(&s.misfit, 8); take(&s.unweighted_misfit, 8); take(&s.like, 8);
+    take(s.coord, 8 * (size_t)dim); take(s.values, 24); take(&s.noise0, 8); take(&s.noise1, 8);
+    s.step = step; s.accepted = acc != 0; s.vindex = vindex; s.ncells = ncells;
+    ++got;
+  }
+  std::fclose(f);
+  return got;
 }
 
 }  // extern "C"

@@ -87,12 +87,44 @@ class Chain:
         return lib().mct_mcmc_accept(ctypes.byref(self.set), ctypes.byref(step), float(like_new),
                                      float(like_old)) == 1
 
+    def record(self, step, accepted, like, misfit, unweighted_misfit):
+        """The iteration's T_SAMPLE after the acceptance test (the state as
+        restored on rejection)."""
+        ptr = lambda a: a.ctypes.data if a.size else None  # noqa: E731
+        st = McmcState(self.ncells, self.points.ctypes.data, self.params.ctypes.data, self.bn0.size, self.sn0.size,
+                       ptr(self.bn0), ptr(self.bn1), ptr(self.sn0), ptr(self.sn1))
+        sm = Sample()
+        check("mct_mcmc_record", lib().mct_mcmc_record(ctypes.byref(st), ctypes.byref(step), 1 if accepted else 0,
+                                                       float(like), float(misfit), float(unweighted_misfit),
+                                                       ctypes.byref(sm)))
+        return sm
+
     def accept_tempered(self, step, like_new, like_old, temperature):
         """The acceptance test of mcmc_pt: the likelihood ratio over the
         chain's temperature."""
         rc = lib().mct_mcmc_accept_tempered(ctypes.byref(self.set), ctypes.byref(step), float(like_new),
                                             float(like_old), float(temperature))
         return check("mct_mcmc_accept_tempered", rc) == 1
+
+
+class Sample(ctypes.Structure):
+    """T_SAMPLE (src/run_time_info.f90:62-76): one iteration's record."""
+    _fields_ = [("step", _I), ("accepted", _I), ("vindex", _I), ("ncells", ctypes.c_longlong),
+                ("misfit", _D), ("unweighted_misfit", _D), ("like", _D), ("coord", _D * 3), ("values", _D * 3),
+                ("noise0", _D), ("noise1", _D)]
+
+
+def write_samples(filename, samples, dim=3):
+    """Appends records to a sample stream file (write_samples' layout)."""
+    arr = (Sample * len(samples))(*samples)
+    check("mct_samples_write", lib().mct_samples_write(str(filename).encode(), int(dim), arr, len(samples)))
+
+
+def read_samples(filename, n, dim=3):
+    """Up to n records of a sample stream file."""
+    arr = (Sample * n)()
+    got = check("mct_samples_read", lib().mct_samples_read(str(filename).encode(), int(dim), arr, n))
+    return list(arr[:got])
 
 
 class Pt(ctypes.Structure):

@@ -61,7 +61,7 @@ def _c_decls():
             else:
                 kind = "ptr" if "*" in decl else decl.split()[0]
                 names = decl.replace("*", " ").split(None, 1 if not decl.startswith("const") else 2)[-1]
-            fields += [(kind, n.strip()) for n in names.split(",")]
+            fields += [(kind, n.strip().replace("[", "(").replace("]", ")")) for n in names.split(",")]
         structs[m.group(2)] = fields
     return funcs, structs
 
