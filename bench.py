@@ -1478,7 +1478,7 @@ def case_tiles(chains=32):
     lk = BodyLikelihood(grid, settings, data, nslots=chains, ncell_max=ncell_max)
     old = L.mct_eik3_tile_config(-1, 0, 0, 0, 0)
     ref = None
-    for cfg in list(range(44)) + [-1]:
+    for cfg in list(range(48)) + [-1]:
         L.mct_eik3_tile_config(cfg, 0, 0, 0, 0)
         lk.forward(ncells, pts, par, locs, n0, n1)
         t0 = time.perf_counter()

@@ -252,7 +252,8 @@ __device__ __forceinline__ int relax(const int *sT, int x, int y, int z, float s
 
 template <int TX, int TY, int TZ>
 __global__ void __launch_bounds__(512) tile_kernel(Eik3Job job, const int *list, int nlocal) {
-  static_assert(TX * TY * TZ == 512 || TX * TY * TZ == 256 || TX * TY * TZ == 128, "one thread per tile node");
+  static_assert(TX * TY * TZ == 512 || TX * TY * TZ == 256 || TX * TY * TZ == 128 || TX * TY * TZ == 64,
+                "one thread per tile node");
   constexpr int SX = TX + 2 * HALO, SY = TY + 2 * HALO, SZ = TZ + 2 * HALO;
   __shared__ int sT[SX * SY * SZ];
   __shared__ int s_face[6];
@@ -375,7 +376,7 @@ int run_tiles(const Eik3Job &job, cudaStream_t s, int max_passes, int nlocal, in
 // Tile shapes (512, 256 or 128 nodes) and local sweeps per visit the tuner tries.
 struct TileShape { int tx, ty, tz; };
 constexpr TileShape kShapes[] = {{8, 8, 8}, {4, 8, 16}, {8, 4, 16}, {16, 8, 4}, {8, 16, 4},
-                                 {8, 8, 4}, {8, 4, 8}, {4, 8, 8}, {4, 4, 8}, {4, 8, 4}, {8, 4, 4}};
+                                 {8, 8, 4}, {8, 4, 8}, {4, 8, 8}, {4, 4, 8}, {4, 8, 4}, {8, 4, 4}, {4, 4, 4}};
 constexpr int kNShapes = sizeof(kShapes) / sizeof(kShapes[0]);
 constexpr int kSweeps[] = {12, 24, 48, 96};
 constexpr int kNSweeps = sizeof(kSweeps) / sizeof(kSweeps[0]);
@@ -394,7 +395,8 @@ int run_config(int cfg, const Eik3Job &job, cudaStream_t s, int max_passes, int 
     case 7: return run_tiles<4, 8, 8>(job, s, max_passes, nl, err);
     case 8: return run_tiles<4, 4, 8>(job, s, max_passes, nl, err);
     case 9: return run_tiles<4, 8, 4>(job, s, max_passes, nl, err);
-    default: return run_tiles<8, 4, 4>(job, s, max_passes, nl, err);
+    case 10: return run_tiles<8, 4, 4>(job, s, max_passes, nl, err);
+    default: return run_tiles<4, 4, 4>(job, s, max_passes, nl, err);
   }
 }
 

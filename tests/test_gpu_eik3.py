@@ -229,7 +229,7 @@ def test_tile_solver_configurations_all_match_reference(orc, gpulib):
     old = gpulib.mct_eik3_tile_config(-1, 0, 0, 0, 0)
     try:
         results = []
-        for cfg in range(44):
+        for cfg in range(48):
             gpulib.mct_eik3_tile_config(cfg, 0, 0, 0, 0)
             got, _, _ = eikonal3d_batch(vel, h, lo, grid_of, srcs, rev, order=0, solver="tiles")
             for i in range(3):
@@ -240,6 +240,6 @@ def test_tile_solver_configurations_all_match_reference(orc, gpulib):
             assert np.max(np.abs(got - results[0])) <= 1e-6
         gpulib.mct_eik3_tile_config(-1, 0, 0, 0, 0)
         eikonal3d_batch(vel, h, lo, grid_of, srcs, rev, order=0, solver="tiles")
-        assert 0 <= gpulib.mct_eik3_tile_config(-2, *shape, 0) < 44
+        assert 0 <= gpulib.mct_eik3_tile_config(-2, *shape, 0) < 48
     finally:
         gpulib.mct_eik3_tile_config(old, 0, 0, 0, 0)
