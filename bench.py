@@ -1176,7 +1176,7 @@ SERVED_SLOTS = {"tt2d": 256, "surface": 64, "body": 32, "joint": 32}
 # SM shares of the 2D travel-time launches per kind in the batched mode: the
 # fm2d grids are persistent, so without a share each launch holds every SM
 # until its last block, and the body kinds' 3D passes wait behind it
-SERVED_SM_SHARE = "tt2d=0.05,surface=0.1,joint=0.1"
+SERVED_SM_SHARE = "tt2d=0.05,surface=0.15,joint=0.2"
 
 
 def served_backends(single, slots, priority="none", share=None):
