@@ -39,6 +39,12 @@ module mctomo_gb300
   end type mct_grid
 
   ! surface-wave settings (T_LIKE_SET fields the surface likelihood reads)
+  type, bind(C) :: mct_modes_para
+    integer(c_int) :: modetype, nmodes, phase_group
+    real(c_double) :: tolmin, tolmax, smin_min, smin_max
+    real(c_double) :: dc, dcm, dc1, dc2
+  end type
+
   type, bind(C) :: mct_surf_settings
     integer(c_int) :: raylov, phase_group
     real(c_double) :: dphase
@@ -178,6 +184,33 @@ module mctomo_gb300
       real(c_double), value :: dc
       real(c_double), intent(out) :: phase(*), group(*)
       integer(c_int), intent(out) :: ierr
+    end function
+    integer(c_int) function mct_surfmodes_para(thick, vp, vs, rho, nlayers, freqs, np, paras, phase, group, &
+        ierr) bind(C, name="mct_surfmodes_para")
+      import :: c_int, c_double, mct_modes_para
+      real(c_double), intent(in) :: thick(*), vp(*), vs(*), rho(*), freqs(*)
+      integer(c_int), value :: nlayers, np
+      type(mct_modes_para), intent(in) :: paras
+      real(c_double), intent(out) :: phase(*), group(*)
+      integer(c_int), intent(out) :: ierr
+    end function
+    integer(c_int) function mct_grt_batch(ncol, nl_max, nl, thk, vp, vs, rho, np, freqs, paras, phase, group, &
+        ierr, nevals) bind(C, name="mct_grt_batch")
+      import :: c_int, c_double, c_long_long, mct_modes_para
+      integer(c_int), value :: ncol, nl_max, np
+      integer(c_int), intent(in) :: nl(*)
+      real(c_double), intent(in) :: thk(*), vp(*), vs(*), rho(*), freqs(*)
+      type(mct_modes_para), intent(in) :: paras
+      real(c_double), intent(out) :: phase(*), group(*)
+      integer(c_int), intent(out) :: ierr(*)
+      integer(c_long_long), intent(out) :: nevals
+    end function
+    integer(c_int) function mct_grt_batch_device(ncol, nl_max, nl, thk, vp, vs, rho, np, freqs, paras, phase, &
+        group, ierr, nevals, stream) bind(C, name="mct_grt_batch_device")
+      import :: c_int, c_ptr, mct_modes_para
+      integer(c_int), value :: ncol, nl_max, np
+      type(c_ptr), value :: nl, thk, vp, vs, rho, freqs, phase, group, ierr, nevals, stream
+      type(mct_modes_para), intent(in) :: paras
     end function
     integer(c_int) function mct_surfdisp_batch(ncol, nl_max, nl, thk, vp, vs, rho, np, periods, iwave, mode, igr, &
         dphase, multimode, precision, cp, cg, ierr, ndltar) bind(C, name="mct_surfdisp_batch")

@@ -115,14 +115,59 @@ int mct_surfdisp_mmodes(const float *thkm, const float *vpm, const float *vsm,
                         int mode, int igr, int kmax, const double *t,
                         double dphase, double *cp, double *cg, int *ierr);
 
-/* surfmodes (surfmodes/surfmodes.f90:39-108): FP64 layer model cast to
- * REAL*4, freqs[np] in Hz, modetype 1 Rayleigh / 0 Love, phase_group 0/1.
- * A column with a low-velocity layer that the reference routes to its
- * generalized R/T solver returns MCT_ERR_UNSUPPORTED. */
+/* The surface-mode search parameters, T_MODES_PARA
+ * (surfmodes/surfmodes.f90:23-30). The reference's surface likelihood sets
+ * tolmin = tol, tolmax = 10 tol, smin_min = 1e-3f, smin_max = 5e-3f and
+ * dc = dcm = dc1 = dc2 = dPhaseVel (src/likelihood_surf.F90:173-182). */
+typedef struct {
+  int modetype;      /* 1 Rayleigh, 0 Love */
+  int nmodes;        /* modes (the generalized R/T path computes the fundamental) */
+  int phase_group;   /* 0 phase only, 1 phase and group */
+  double tolmin, tolmax, smin_min, smin_max;
+  double dc, dcm, dc1, dc2;
+} mct_modes_para;
+
+/* surfmodes (surfmodes/surfmodes.f90:39-108) with the reference's routing:
+ * a column without a low-velocity layer slower than the top layer
+ * (setup_grt's nlvls1 = 0, :320-450) goes to surfdisp96 with the model cast
+ * to REAL*4; a column with one goes to the generalized R/T fundamental-mode
+ * search (RayleighModes / LoveModes, :185-303), FP64 throughout. freqs[np]
+ * in Hz (np <= 60). Fluid layers (vs = 0) return MCT_ERR_UNSUPPORTED. */
+int mct_surfmodes_para(const double *thick, const double *vp, const double *vs,
+                       const double *rho, int nlayers, const double *freqs, int np,
+                       const mct_modes_para *paras, double *phase, double *group,
+                       int *ierr);
+
+/* surfmodes with the example decks' tolerance (LIKE_SET%TOL = 1e-6,
+ * examples/example1/MCTomo.inp:55): mct_surfmodes_para with tolmin 1e-6,
+ * tolmax 1e-5, smin 1e-3f / 5e-3f and dc for every increment. */
 int mct_surfmodes(const double *thick, const double *vp, const double *vs,
                   const double *rho, int nlayers, const double *freqs, int np,
                   int modetype, int phase_group, double dc, double *phase,
                   double *group, int *ierr);
+
+/* The generalized R/T fundamental-mode search (RayleighModes / LoveModes,
+ * surfmodes/surfmodes.f90:185-303, allmodes 0) for many columns, whatever
+ * their layering: layer arrays [ncol][nl_max] FP64 (last layer of each
+ * column the half-space), nl[ncol]; freqs[np] in Hz; phase / group
+ * [ncol][np] (entries after a frequency without a root stay 0); ierr[ncol]:
+ * 0, 1 (no root, the reference's ierr), 2 (the trial-velocity list would
+ * exceed the reference's 20,000 entries), -1 (a layer count outside
+ * 2..nl_max), -2 (a fluid layer, not built).
+ * nevals (optional) receives the secular-function evaluations. */
+int mct_grt_batch(int ncol, int nl_max, const int *nl, const double *thk,
+                  const double *vp, const double *vs, const double *rho, int np,
+                  const double *freqs, const mct_modes_para *paras, double *phase,
+                  double *group, int *ierr, unsigned long long *nevals);
+
+/* Device-pointer variant on the caller's stream (asynchronous; scratch is
+ * allocated and freed in stream order). nevals, if given, is a device
+ * counter that the kernel adds to. */
+int mct_grt_batch_device(int ncol, int nl_max, const int *nl, const double *thk,
+                         const double *vp, const double *vs, const double *rho,
+                         int np, const double *freqs, const mct_modes_para *paras,
+                         double *phase, double *group, int *ierr,
+                         unsigned long long *nevals, void *stream);
 
 /* Many columns at once (host buffers): layer arrays [ncol][nl_max] REAL*4,
  * nl[ncol]; cp/cg [ncol][mode][np]; ierr[ncol]. precision 0 = FP64 root

@@ -22,6 +22,14 @@ I = ctypes.c_int
 D = ctypes.c_double
 ULLP = ctypes.POINTER(ctypes.c_ulonglong)
 
+class ModesPara(ctypes.Structure):
+    """mct_modes_para: the reference's T_MODES_PARA (surfmodes/surfmodes.f90:23-30)."""
+    _fields_ = [("modetype", ctypes.c_int), ("nmodes", ctypes.c_int), ("phase_group", ctypes.c_int),
+                ("tolmin", ctypes.c_double), ("tolmax", ctypes.c_double), ("smin_min", ctypes.c_double),
+                ("smin_max", ctypes.c_double), ("dc", ctypes.c_double), ("dcm", ctypes.c_double),
+                ("dc1", ctypes.c_double), ("dc2", ctypes.c_double)]
+
+
 # name -> (restype, argtypes); must list every symbol declared in include/mctomo.h
 SIGNATURES = {
     "mct_version": (ctypes.c_char_p, []),
@@ -33,6 +41,9 @@ SIGNATURES = {
     "mct_surfdisp96": (I, [P, P, P, P, I, I, I, I, I, I, P, D, P, P, P]),
     "mct_surfdisp_mmodes": (I, [P, P, P, P, I, I, I, I, I, I, P, D, P, P, P]),
     "mct_surfmodes": (I, [P, P, P, P, I, P, I, I, I, D, P, P, P]),
+    "mct_surfmodes_para": (I, [P, P, P, P, I, P, I, P, P, P, P]),
+    "mct_grt_batch": (I, [I, I, P, P, P, P, P, I, P, P, P, P, P, ULLP]),
+    "mct_grt_batch_device": (I, [I, I, P, P, P, P, P, I, P, P, P, P, P, P, P]),
     "mct_surfdisp_batch": (I, [I, I, P, P, P, P, P, I, P, I, I, I, D, I, I, P, P, P, P]),
     "mct_surfdisp_batch_device": (I, [I, I, P, P, P, P, P, I, P, I, I, I, D, I, I, P, P, P, P, P]),
     "mct_modrays": (I, [I, P, P, I, P, P, P, I, I, I, D, D, D, D, P, I, I, I, I, I, D, I, D, P, I, P, P]),

@@ -3,6 +3,7 @@
 // the library's own stream and wait for the result; _device calls launch on
 // the caller's stream.
 #include "mct_common.cuh"
+#include "grt.cuh"
 #include "fm2d.cuh"
 #include "eikonal3d.cuh"
 #include <cstring>
@@ -344,14 +345,93 @@ static int count_lvl(const double *vp, const double *vs, int nl, int modetype) {
   return n;
 }
 
-int mct_surfmodes(const double *thick, const double *vp, const double *vs, const double *rho,
-                  int nlayers, const double *freqs, int np, int modetype, int phase_group,
-                  double dc, double *phase, double *group, int *ierr) {
-  if (nlayers < 1 || nlayers > 200 || np < 1 || np > 60) return arg_error("mct_surfmodes: sizes");
-  if (modetype != 0 && modetype != 1) return arg_error("mct_surfmodes: modetype must be 0 or 1");
-  if (count_lvl(vp, vs, nlayers, modetype) > 0) {
-    g_last_error = "column has a low-velocity layer (generalized R/T path)";
-    return MCT_ERR_UNSUPPORTED;
+static bool modes_para_ok(const mct_modes_para *p) {
+  return p && (p->modetype == 0 || p->modetype == 1) && (p->phase_group == 0 || p->phase_group == 1) &&
+         p->tolmin > 0 && p->tolmax > 0 && p->smin_min > 0 && p->smin_max > 0 && p->dc > 0;
+}
+
+int mct_grt_batch_device(int ncol, int nl_max, const int *nl, const double *thk, const double *vp,
+                         const double *vs, const double *rho, int np, const double *freqs,
+                         const mct_modes_para *paras, double *phase, double *group, int *ierr,
+                         unsigned long long *nevals, void *stream) {
+  if (ncol < 0 || nl_max < 2 || nl_max > 200 || np < 1 || np > 100 || !modes_para_ok(paras) ||
+      (ncol > 0 && (!nl || !thk || !vp || !vs || !rho || !freqs || !phase || !group || !ierr)))
+    return arg_error("mct_grt_batch_device: bad arguments");
+  if (ncol == 0) return MCT_OK;
+  cudaStream_t s = static_cast<cudaStream_t>(stream);
+  const size_t lay = (size_t)ncol * nl_max;
+  const size_t nscr = grt_scratch_doubles(ncol, paras->modetype);
+  double *w = nullptr;
+  MCT_CUDA_TRY(cudaMallocAsync(&w, sizeof(double) * (7 * lay + nscr), s));
+  GrtJob J{};
+  J.ncol = ncol; J.nl_max = nl_max; J.np = np; J.modetype = paras->modetype; J.phase_group = paras->phase_group;
+  J.nl = nl; J.freqs = freqs;
+  J.tolmin = paras->tolmin; J.tolmax = paras->tolmax; J.smin_min = paras->smin_min; J.smin_max = paras->smin_max;
+  J.dc = paras->dc;
+  J.mu = w + 4 * lay; J.v = w + 5 * lay; J.scratch = w + 7 * lay;
+  J.cols = nullptr; J.n = ncol;
+  J.phase = phase; J.group = group; J.ierr = ierr; J.nevals = nevals;
+  const double *rows[4] = {thk, vp, vs, rho};
+  const int rc = launch_grt(J, rows, w, s);
+  cudaFreeAsync(w, s);
+  return rc;
+}
+
+int mct_grt_batch(int ncol, int nl_max, const int *nl, const double *thk, const double *vp, const double *vs,
+                  const double *rho, int np, const double *freqs, const mct_modes_para *paras, double *phase,
+                  double *group, int *ierr, unsigned long long *nevals) {
+  if (ncol < 0 || nl_max < 2 || nl_max > 200 || np < 1 || np > 100 || !modes_para_ok(paras))
+    return arg_error("mct_grt_batch: bad arguments");
+  for (int c = 0; c < ncol; ++c)
+    if (nl[c] < 2 || nl[c] > nl_max) return arg_error("mct_grt_batch: layer count outside 2..nl_max");
+  if (ncol == 0) return MCT_OK;
+  ThreadDev *td = nullptr;
+  int rc = thread_dev(&td); if (rc) return rc;
+  const size_t lay = (size_t)ncol * nl_max, outn = (size_t)ncol * np;
+  size_t bytes = carve_size({sizeof(int) * ncol, 4 * sizeof(double) * lay, sizeof(double) * np,
+                             2 * sizeof(double) * outn, sizeof(int) * ncol, sizeof(unsigned long long)});
+  rc = td->ws.reserve(bytes); if (rc) return rc;
+  Carve cv(td->ws.p);
+  int *d_nl = cv.take<int>(ncol);
+  double *d_lay = cv.take<double>(4 * lay);
+  double *d_f = cv.take<double>(np);
+  double *d_out = cv.take<double>(2 * outn);
+  int *d_ierr = cv.take<int>(ncol);
+  unsigned long long *d_cnt = cv.take<unsigned long long>(1);
+  cudaStream_t s = td->stream;
+  MCT_CUDA_TRY(cudaMemcpyAsync(d_nl, nl, sizeof(int) * ncol, cudaMemcpyHostToDevice, s));
+  const double *src[4] = {thk, vp, vs, rho};
+  for (int a = 0; a < 4; ++a)
+    MCT_CUDA_TRY(cudaMemcpyAsync(d_lay + a * lay, src[a], sizeof(double) * lay, cudaMemcpyHostToDevice, s));
+  MCT_CUDA_TRY(cudaMemcpyAsync(d_f, freqs, sizeof(double) * np, cudaMemcpyHostToDevice, s));
+  MCT_CUDA_TRY(cudaMemsetAsync(d_cnt, 0, sizeof(unsigned long long), s));
+  rc = mct_grt_batch_device(ncol, nl_max, d_nl, d_lay, d_lay + lay, d_lay + 2 * lay, d_lay + 3 * lay, np, d_f,
+                            paras, d_out, d_out + outn, d_ierr, d_cnt, s);
+  if (rc) return rc;
+  MCT_CUDA_TRY(cudaMemcpyAsync(phase, d_out, sizeof(double) * outn, cudaMemcpyDeviceToHost, s));
+  MCT_CUDA_TRY(cudaMemcpyAsync(group, d_out + outn, sizeof(double) * outn, cudaMemcpyDeviceToHost, s));
+  MCT_CUDA_TRY(cudaMemcpyAsync(ierr, d_ierr, sizeof(int) * ncol, cudaMemcpyDeviceToHost, s));
+  unsigned long long cnt = 0;
+  MCT_CUDA_TRY(cudaMemcpyAsync(&cnt, d_cnt, sizeof(cnt), cudaMemcpyDeviceToHost, s));
+  rc = sync_and_check(s, nullptr);
+  if (nevals) *nevals = cnt;
+  return rc;
+}
+
+int mct_surfmodes_para(const double *thick, const double *vp, const double *vs, const double *rho,
+                       int nlayers, const double *freqs, int np, const mct_modes_para *paras, double *phase,
+                       double *group, int *ierr) {
+  if (nlayers < 1 || nlayers > 200 || np < 1 || np > 60 || !modes_para_ok(paras))
+    return arg_error("mct_surfmodes_para: bad arguments");
+  if (count_lvl(vp, vs, nlayers, paras->modetype) > 0) {
+    for (int i = 0; i < nlayers; ++i)
+      if (!(std::fabs(vs[i]) > (double)1e-6f)) {
+        g_last_error = "low-velocity layer under a fluid layer (the Stoneley-mode path)";
+        return MCT_ERR_UNSUPPORTED;
+      }
+    if (nlayers < 2) return arg_error("mct_surfmodes_para: one layer");
+    int nl = nlayers;
+    return mct_grt_batch(1, nlayers, &nl, thick, vp, vs, rho, np, freqs, paras, phase, group, ierr, nullptr);
   }
   std::vector<float> t4(nlayers), a4(nlayers), b4(nlayers), r4(nlayers);
   std::vector<double> per(np);
@@ -359,8 +439,19 @@ int mct_surfmodes(const double *thick, const double *vp, const double *vs, const
     t4[i] = (float)thick[i]; a4[i] = (float)vp[i]; b4[i] = (float)vs[i]; r4[i] = (float)rho[i];
   }
   for (int i = 0; i < np; ++i) per[i] = 1.0 / freqs[i];
-  return mct_surfdisp96(t4.data(), a4.data(), b4.data(), r4.data(), nlayers, 0, modetype == 1 ? 2 : 1,
-                        1, phase_group, np, per.data(), dc, phase, group, ierr);
+  return mct_surfdisp96(t4.data(), a4.data(), b4.data(), r4.data(), nlayers, 0, paras->modetype == 1 ? 2 : 1,
+                        1, paras->phase_group, np, per.data(), paras->dc, phase, group, ierr);
+}
+
+int mct_surfmodes(const double *thick, const double *vp, const double *vs, const double *rho,
+                  int nlayers, const double *freqs, int np, int modetype, int phase_group,
+                  double dc, double *phase, double *group, int *ierr) {
+  mct_modes_para p{};
+  p.modetype = modetype; p.nmodes = 1; p.phase_group = phase_group;
+  p.tolmin = 1e-6; p.tolmax = 1e-5; p.smin_min = (double)1e-3f; p.smin_max = (double)5e-3f;
+  p.dc = p.dcm = p.dc1 = p.dc2 = dc;
+  if (modetype != 0 && modetype != 1) return arg_error("mct_surfmodes: modetype must be 0 or 1");
+  return mct_surfmodes_para(thick, vp, vs, rho, nlayers, freqs, np, &p, phase, group, ierr);
 }
 
 

@@ -84,6 +84,47 @@ def surfmodes(thick, vp, vs, rho, freqs, modetype, phase_group, dc):
     return phase, group, ierr.value
 
 
+def modes_para(modetype, phase_group, tol=1e-6, dc=1e-3):
+    """The reference surface likelihood's mode-search parameters
+    (src/likelihood_surf.F90:173-182): tolmin = tol, tolmax = 10 tol, smin
+    1e-3 / 5e-3 (single-precision literals) and every increment dc."""
+    from ._lib import ModesPara
+    return ModesPara(modetype, 1, phase_group, tol, 10 * tol, float(np.float32(1e-3)), float(np.float32(5e-3)),
+                     dc, dc, dc, dc)
+
+
+def surfmodes_para(thick, vp, vs, rho, freqs, paras):
+    """surfmodes with explicit T_MODES_PARA (mct_surfmodes_para): columns with
+    a low-velocity layer go to the generalized R/T search. Returns (phase,
+    group, ierr)."""
+    thick, vp, vs, rho, freqs = _f64(thick), _f64(vp), _f64(vs), _f64(rho), _f64(freqs)
+    np_ = freqs.size
+    phase = np.zeros(np_); group = np.zeros(np_)
+    ierr = ctypes.c_int(0)
+    rc = lib().mct_surfmodes_para(ptr(thick), ptr(vp), ptr(vs), ptr(rho), thick.size, ptr(freqs), np_,
+                                  ctypes.byref(paras), ptr(phase), ptr(group), ctypes.byref(ierr))
+    check("mct_surfmodes_para", rc)
+    return phase, group, ierr.value
+
+
+def grt_batch(nl, thk, vp, vs, rho, freqs, paras):
+    """The generalized R/T fundamental-mode search (RayleighModes / LoveModes,
+    surfmodes/surfmodes.f90:185-303) for many FP64 columns: thk/vp/vs/rho
+    (ncol, nl_max), nl (ncol,). Returns (phase, group, ierr, nevals) with
+    phase/group shaped (ncol, np)."""
+    nl = np.ascontiguousarray(nl, dtype=np.int32)
+    thk, vp, vs, rho, freqs = _f64(thk), _f64(vp), _f64(vs), _f64(rho), _f64(freqs)
+    ncol, nl_max = thk.shape
+    np_ = freqs.size
+    phase = np.zeros((ncol, np_)); group = np.zeros((ncol, np_))
+    ierr = np.zeros(ncol, np.int32)
+    cnt = ctypes.c_ulonglong(0)
+    rc = lib().mct_grt_batch(ncol, nl_max, ptr(nl), ptr(thk), ptr(vp), ptr(vs), ptr(rho), np_, ptr(freqs),
+                             ctypes.byref(paras), ptr(phase), ptr(group), ptr(ierr), ctypes.byref(cnt))
+    check("mct_grt_batch", rc)
+    return phase, group, ierr, cnt.value
+
+
 def surfdisp_batch(nl, thk, vp, vs, rho, periods, iwave, igr, dphase, mode=1, multimode=False,
                    precision=0):
     """Many columns at once. thk/vp/vs/rho: (ncol, nl_max) REAL*4 models, nl:

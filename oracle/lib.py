@@ -4,7 +4,8 @@ import os
 import subprocess
 
 HERE = os.path.dirname(os.path.abspath(__file__))
-SOURCES = ["kdgrid.cpp", "surfdisp.cpp", "fm2d.cpp", "sfmm3d.cpp", "likelihood.cpp", "surf_pipeline.cpp"]
+SOURCES = ["kdgrid.cpp", "surfdisp.cpp", "fm2d.cpp", "sfmm3d.cpp", "likelihood.cpp", "surf_pipeline.cpp",
+           "grt.cpp"]
 LIB = os.path.join(HERE, "liboracle.so")
 REF_LIB = os.path.join(HERE, "_ref", "libfmm_ref.so")
 
@@ -55,6 +56,9 @@ def load():
                                         _I, _I, _I, _I, _I, _I, _P, _P, _P, _P]),
             "orc_kdtree_nearest": (_I, [_I, _I, _P, _P]),
             "orc_surfdisp96": (_I, [_P, _P, _P, _P, _I, _I, _I, _I, _I, _P, _D, _P, _P, _P]),
+            "orc_grt_modes": (_I, [_I, _P, _P, _P, _P, _I, _P, _I, _I, _D, _D, _D, _D, _D, _D, _D, _P, _P, _P]),
+            "orc_grt_nlvls1": (_I, [_I, _P, _P, _P, _P, _I]),
+            "orc_grt_secfun": (_D, [_I, _P, _P, _P, _P, _I, _D, _D, _P]),
             "orc_surfdisp_mmodes": (_I, [_P, _P, _P, _P, _I, _I, _I, _I, _I, _P, _D, _P, _P, _P]),
             "orc_dltar": (_D, [_D, _D, _I, _P, _P, _P, _P, _I]),
             "orc_gtsolh": (_F, [_F, _F]),
