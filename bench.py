@@ -1027,6 +1027,168 @@ TT2D_CONFIG = {"workload": "plain 2D travel-time likelihood (the 2D code's path)
                "grid": [51, 51], "stations": 16, "times": 240}
 
 
+GRT_CONFIG = {"workload": "generalized R/T fundamental-mode dispersion (the reference's single-mode surfmodes path "
+                         "for low-velocity-layer columns): layered columns drawn as the dispersion study's (12-40 "
+                         "layers, h U[0.05,0.5] km, Vs U[0.2,3.5] km/s with a 10% low-velocity-layer chance, "
+                         "Vp = 1.73 Vs, rho = 1.74 Vp^0.25), routed as surfmodes routes them (setup_grt's nlvls1 > "
+                         "0), Rayleigh and Love, phase and group, 60 periods 0.2-20 s (ascending), tol 1e-6, "
+                         "dc 1e-3",
+              "periods": 60, "inputs": "larger than L2 (per-lane trial-velocity scratch of GBs)"}
+
+
+def run_grt(args):
+    """Generalized R/T fundamental-mode dispersion curves of the columns that
+    surfmodes routes to RayleighModes / LoveModes (surfmodes.f90:39-108,
+    185-303): device path timed with CUDA events, host-buffer path end to
+    end, the oracle on a sample of the same columns on all host cores."""
+    import torch
+    from mctomo_gb300 import _lib, forward, synthetic
+    dev = torch.device("cuda", 0)
+    torch.cuda.set_device(dev)
+    L = _lib.lib()
+    rng = np.random.default_rng(SEED + 7)
+    nl, thk, vp, vs, rho = synthetic.layered_columns(rng, args.grt_cols, nl_range=(12, 40), lvl_prob=0.1)
+    thk, vp, vs, rho = (np.ascontiguousarray(x, np.float64) for x in (thk, vp, vs, rho))
+    periods = np.geomspace(0.2, 20.0, 60)
+    freqs = np.ascontiguousarray(1.0 / periods)
+    waves = {}
+    for mt in (1, 0):
+        route = forward.surfmodes_route(nl, vp, vs, mt)
+        sel = np.where(route == 1)[0]
+        waves[mt] = sel
+    streams = {1: torch.cuda.Stream(dev), 0: torch.cuda.Stream(dev)}
+    dbuf = {}
+    for mt, sel in waves.items():
+        t = lambda a: torch.from_numpy(np.ascontiguousarray(a)).to(dev)  # noqa: E731
+        dbuf[mt] = dict(nl=t(nl[sel].astype(np.int32)), thk=t(thk[sel]), vp=t(vp[sel]), vs=t(vs[sel]),
+                        rho=t(rho[sel]), ph=torch.zeros((len(sel), 60), dtype=torch.float64, device=dev),
+                        gr=torch.zeros((len(sel), 60), dtype=torch.float64, device=dev),
+                        ierr=torch.zeros(len(sel), dtype=torch.int32, device=dev),
+                        cnt=torch.zeros(1, dtype=torch.int64, device=dev))
+    d_f = torch.from_numpy(freqs).to(dev)
+    paras = {mt: forward.modes_para(mt, 1, tol=1e-6, dc=1e-3) for mt in (1, 0)}
+    nl_max = thk.shape[1]
+
+    def launch(mt, ncols):
+        b = dbuf[mt]
+        rc = L.mct_grt_batch_device(ncols, nl_max, b["nl"].data_ptr(), b["thk"].data_ptr(),
+                                    b["vp"].data_ptr(), b["vs"].data_ptr(), b["rho"].data_ptr(), 60,
+                                    d_f.data_ptr(), ctypes.byref(paras[mt]), b["ph"].data_ptr(),
+                                    b["gr"].data_ptr(), b["ierr"].data_ptr(), b["cnt"].data_ptr(),
+                                    ctypes.c_void_p(streams[mt].cuda_stream))
+        _lib.check("mct_grt_batch_device", rc)
+
+    # warm-up: the kernels' first launches on a few columns of each wave
+    for _ in range(args.warmup):
+        for mt in (1, 0):
+            launch(mt, min(64, len(waves[mt])))
+    torch.cuda.synchronize()
+    for mt in (1, 0):
+        dbuf[mt]["cnt"].zero_()
+    torch.cuda.synchronize()
+    # the two wave types run on their own streams, side by side
+    clocks = Clocks(0)
+    clocks.start()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    done0 = torch.cuda.Event()
+    s1, s0 = streams[1], streams[0]
+    e0.record(s1)
+    s0.wait_event(e0)
+    for _ in range(args.steps):
+        launch(1, len(waves[1]))
+        launch(0, len(waves[0]))
+    done0.record(s0)
+    s1.wait_event(done0)
+    e1.record(s1)
+    torch.cuda.synchronize()
+    cl = clocks.stop()
+    ms = e0.elapsed_time(e1) / args.steps
+    curves = sum(len(v) for v in waves.values())
+    value = curves / (ms / 1e3)
+    evals = {mt: int(dbuf[mt]["cnt"].item()) // args.steps for mt in (1, 0)}
+    # end to end through the host API, one host thread per wave type (each
+    # gets its own stream in the library)
+    host = {}
+
+    def host_call(mt):
+        sel = waves[mt]
+        host[mt] = forward.grt_batch(nl[sel], thk[sel], vp[sel], vs[sel], rho[sel], freqs, paras[mt])
+    t0 = time.perf_counter()
+    ths = [threading.Thread(target=host_call, args=(mt,)) for mt in (1, 0)]
+    for th in ths:
+        th.start()
+    for th in ths:
+        th.join()
+    e2e_s = time.perf_counter() - t0
+    lay_b = sum(int(len(v)) * nl_max * 8 * 4 + int(len(v)) * 4 for v in waves.values()) + 60 * 8
+    out_b = sum(int(len(v)) * (2 * 60 * 8 + 4) for v in waves.values())
+    acc, cpu = grt_oracle_sample(nl, thk, vp, vs, rho, freqs, waves, host, args)
+    line = {"metric": "generalized R/T dispersion curves/s (low-velocity-layer columns, fundamental mode, phase + "
+                      "group, Rayleigh and Love), 1 GB300",
+            "value": round(value, 2), "unit": "curves/s", "n_gpus": 1, "steps": args.steps, "warmup": args.warmup,
+            "ms_per_step": round(ms, 1), "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+            "dtype": "f64 (complex FP64, no fused multiply-add, the reference's operation order)",
+            "data": "synthetic (seeded, shapes of the dispersion study)",
+            "config": dict(GRT_CONFIG, columns=int(args.grt_cols), rayleigh_columns=int(len(waves[1])),
+                           love_columns=int(len(waves[0]))),
+            "secular_evaluations_per_step": evals,
+            "secular_evaluations_per_s": round(sum(evals.values()) / (ms / 1e3)),
+            "e2e": {"value": round(curves / e2e_s, 2), "unit": "curves/s", "h2d_bytes_per_step": int(lay_b),
+                    "d2h_bytes_per_step": int(out_b)},
+            "accuracy": acc, "clocks": cl,
+            "gpu_launches": args.steps * 2 * 6,
+            "timing": "the two wave types on two streams; warm-up launches on 64 columns of each"}
+    if not args.no_cpu:
+        line["cpu_baseline"] = cpu
+    print(json.dumps(line), flush=True)
+
+
+def grt_oracle_sample(nl, thk, vp, vs, rho, freqs, waves, host, args):
+    """The oracle (orc_grt_modes, the reference's RayleighModes / LoveModes
+    restated) on the first args.grt_sample routed columns of each wave, on a
+    thread pool over all host cores; agreement of the GPU's curves there."""
+    import concurrent.futures as cf
+    import oracle
+    orc = oracle.load()
+    P = lambda a: None if a is None else a.ctypes.data_as(ctypes.c_void_p)  # noqa: E731
+    threads = os.cpu_count() or 1
+    acc = {}
+    t0 = time.perf_counter()
+    res = {}
+    for mt in (1, 0):
+        sel = waves[mt][:args.grt_sample]
+
+        def one(c, mt=mt):
+            n = int(nl[c])
+            a = [np.ascontiguousarray(x[c, :n]) for x in (thk, vp, vs, rho)]
+            ph, gr, ne = np.zeros(60), np.zeros(60), np.zeros(1, np.int64)
+            e = orc.orc_grt_modes(n, P(a[0]), P(a[1]), P(a[2]), P(a[3]), 60, P(freqs), mt, 1, 1e-6, 1e-5,
+                                  float(np.float32(1e-3)), float(np.float32(5e-3)), 1e-3, 1e-3, 1e-3, P(ph), P(gr),
+                                  P(ne))
+            return e, ph, gr, int(ne[0])
+        with cf.ThreadPoolExecutor(threads) as ex:
+            res[mt] = list(ex.map(one, sel))
+    cpu_s = time.perf_counter() - t0
+    ncurves = 0
+    for mt, name in ((1, "rayleigh"), (0, "love")):
+        ph, gr, ierr, _ = host[mt]
+        same = tot = ierr_diff = 0
+        worst = 0.0
+        for k, (e, eph, egr, _) in enumerate(res[mt]):
+            ncurves += 1
+            ierr_diff += int(ierr[k] != e)
+            d = np.maximum(np.abs(ph[k] - eph), np.abs(gr[k] - egr))
+            same += int(np.sum(d <= 1e-9)); tot += d.size
+            worst = max(worst, float(np.max(d)))
+        acc[name] = {"columns_checked": len(res[mt]), "ierr_mismatches": ierr_diff,
+                     "frac_within_1e-9_kms": round(same / max(tot, 1), 5), "max_abs_diff_kms": worst}
+    acc["reference"] = "oracle restatement of RayleighModes / LoveModes (FP64)"
+    cpu = {"value": round(ncurves / cpu_s, 3), "unit": "curves/s", "cores": threads, "kind": "port",
+           "sample": "%d Rayleigh + %d Love routed columns of the same workload, phase + group, 60 periods, "
+                     "oracle restatement on a thread pool" % (len(res[1]), len(res[0]))}
+    return acc, cpu
+
+
 def run_tt2d(args):
     """The plain 2D configuration: every step is one value-change proposal
     per chain through the host API (2D gridding, 16 fm2d solves, misfit),
@@ -1519,7 +1681,7 @@ def main():
                     help="surface workload: fm2d arithmetic (0 FP64 exact, 1 double-float, 2 fixed point)")
     ap.add_argument("--no-variant", action="store_true", help="surface workload: skip the double-float variant")
     ap.add_argument("--workload", default="surface",
-                    choices=["surface", "body", "disp", "tt2d", "served", "dropin"])
+                    choices=["surface", "body", "disp", "tt2d", "served", "dropin", "grt"])
     ap.add_argument("--served-seconds", type=float, default=60.0, help="served workload: stream length (s)")
     ap.add_argument("--served-priority", default="none", choices=["none", "body", "body+joint"],
                     help="served workload: contexts whose streams run at the device's highest priority")
@@ -1532,6 +1694,8 @@ def main():
     ap.add_argument("--columns", type=int, default=262144, help="disp workload: columns")
     ap.add_argument("--disp-sample", type=int, default=512, help="disp workload: columns checked by the oracle")
     ap.add_argument("--love-cols", type=int, default=0, help="disp workload: columns with Love waves (0: all)")
+    ap.add_argument("--grt-cols", type=int, default=262144, help="grt workload: columns drawn (about 10%% routed)")
+    ap.add_argument("--grt-sample", type=int, default=128, help="grt workload: routed columns per wave the oracle checks")
     ap.add_argument("--chains", type=int, default=32, help="body workload: chains per step")
     ap.add_argument("--order", type=int, default=0, help="body workload: eikonal order")
     ap.add_argument("--body-sample", type=int, default=2, help="body workload: proposals checked by the oracle")
@@ -1553,7 +1717,7 @@ def main():
     if args.case:
         run_case(args)
         return
-    if args.workload in ("body", "disp", "tt2d", "served", "dropin"):
+    if args.workload in ("body", "disp", "tt2d", "served", "dropin", "grt"):
         if args.impl == "reference":
             print(json.dumps({"impl": "reference", "unavailable": "the reference arm times the surface workload"}))
         elif args.workload == "served":
@@ -1564,6 +1728,8 @@ def main():
             run_body(args)
         elif args.workload == "disp":
             run_disp(args)
+        elif args.workload == "grt":
+            run_grt(args)
         else:
             run_tt2d(args)
     elif args.impl == "reference":

@@ -194,6 +194,14 @@ module mctomo_gb300
       real(c_double), intent(out) :: phase(*), group(*)
       integer(c_int), intent(out) :: ierr
     end function
+    integer(c_int) function mct_surfmodes_route(ncol, nl_max, nl, vp, vs, modetype, route) &
+        bind(C, name="mct_surfmodes_route")
+      import :: c_int, c_double
+      integer(c_int), value :: ncol, nl_max, modetype
+      integer(c_int), intent(in) :: nl(*)
+      real(c_double), intent(in) :: vp(*), vs(*)
+      integer(c_int), intent(out) :: route(*)
+    end function
     integer(c_int) function mct_grt_batch(ncol, nl_max, nl, thk, vp, vs, rho, np, freqs, paras, phase, group, &
         ierr, nevals) bind(C, name="mct_grt_batch")
       import :: c_int, c_double, c_long_long, mct_modes_para

@@ -146,6 +146,14 @@ int mct_surfmodes(const double *thick, const double *vp, const double *vs,
                   int modetype, int phase_group, double dc, double *phase,
                   double *group, int *ierr);
 
+/* surfmodes' routing for many columns (host only): route[c] = 1 where
+ * setup_grt counts a low-velocity layer slower than the top layer (nlvls1 >
+ * 0, surfmodes/surfmodes.f90:320-450; the generalized R/T search), 0 where
+ * not (surfdisp96), -2 where such a column has a fluid layer (the
+ * Stoneley-mode path, not built). Layer arrays [ncol][nl_max] FP64. */
+int mct_surfmodes_route(int ncol, int nl_max, const int *nl, const double *vp,
+                        const double *vs, int modetype, int *route);
+
 /* The generalized R/T fundamental-mode search (RayleighModes / LoveModes,
  * surfmodes/surfmodes.f90:185-303, allmodes 0) for many columns, whatever
  * their layering: layer arrays [ncol][nl_max] FP64 (last layer of each

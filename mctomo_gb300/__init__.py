@@ -11,7 +11,8 @@ from .surface import SurfaceLikelihood  # noqa: F401
 from .body import BodyLikelihood  # noqa: F401
 from .tt2d import TravelTime2DLikelihood  # noqa: F401
 from .forward import (  # noqa: F401
-    kdtree_to_grid, surfdisp96, surfdisp_mmodes, surfmodes, surfmodes_para, modes_para, grt_batch, surfdisp_batch,
+    kdtree_to_grid, surfdisp96, surfdisp_mmodes, surfmodes, surfmodes_para, modes_para, grt_batch, surfmodes_route,
+    surfdisp_batch,
     modrays, modrays_batch,
     modrays_group_batch, fast_marching3d, eikonal3d_batch,
 )

@@ -43,6 +43,7 @@ SIGNATURES = {
     "mct_surfmodes": (I, [P, P, P, P, I, P, I, I, I, D, P, P, P]),
     "mct_surfmodes_para": (I, [P, P, P, P, I, P, I, P, P, P, P]),
     "mct_grt_batch": (I, [I, I, P, P, P, P, P, I, P, P, P, P, P, ULLP]),
+    "mct_surfmodes_route": (I, [I, I, P, P, P, I, P]),
     "mct_grt_batch_device": (I, [I, I, P, P, P, P, P, I, P, P, P, P, P, P, P]),
     "mct_surfdisp_batch": (I, [I, I, P, P, P, P, P, I, P, I, I, I, D, I, I, P, P, P, P]),
     "mct_surfdisp_batch_device": (I, [I, I, P, P, P, P, P, I, P, I, I, I, D, I, I, P, P, P, P, P]),

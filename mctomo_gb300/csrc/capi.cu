@@ -362,7 +362,7 @@ int mct_grt_batch_device(int ncol, int nl_max, const int *nl, const double *thk,
   const size_t lay = (size_t)ncol * nl_max;
   const size_t nscr = grt_scratch_doubles(ncol, paras->modetype);
   double *w = nullptr;
-  MCT_CUDA_TRY(cudaMallocAsync(&w, sizeof(double) * (7 * lay + nscr), s));
+  MCT_CUDA_TRY(cudaMallocAsync(&w, sizeof(double) * (7 * lay + nscr + 1), s));
   GrtJob J{};
   J.ncol = ncol; J.nl_max = nl_max; J.np = np; J.modetype = paras->modetype; J.phase_group = paras->phase_group;
   J.nl = nl; J.freqs = freqs;
@@ -370,6 +370,7 @@ int mct_grt_batch_device(int ncol, int nl_max, const int *nl, const double *thk,
   J.dc = paras->dc;
   J.mu = w + 4 * lay; J.v = w + 5 * lay; J.scratch = w + 7 * lay;
   J.cols = nullptr; J.n = ncol;
+  J.next = reinterpret_cast<unsigned *>(w + 7 * lay + nscr);
   J.phase = phase; J.group = group; J.ierr = ierr; J.nevals = nevals;
   const double *rows[4] = {thk, vp, vs, rho};
   const int rc = launch_grt(J, rows, w, s);
@@ -416,6 +417,24 @@ int mct_grt_batch(int ncol, int nl_max, const int *nl, const double *thk, const 
   rc = sync_and_check(s, nullptr);
   if (nevals) *nevals = cnt;
   return rc;
+}
+
+int mct_surfmodes_route(int ncol, int nl_max, const int *nl, const double *vp, const double *vs, int modetype,
+                        int *route) {
+  if (ncol < 0 || nl_max < 1 || nl_max > 200 || (modetype != 0 && modetype != 1) ||
+      (ncol > 0 && (!nl || !vp || !vs || !route)))
+    return arg_error("mct_surfmodes_route: bad arguments");
+  for (int c = 0; c < ncol; ++c) {
+    const int n = nl[c];
+    if (n < 1 || n > nl_max) return arg_error("mct_surfmodes_route: layer count outside 1..nl_max");
+    const double *a = vp + (size_t)c * nl_max, *b = vs + (size_t)c * nl_max;
+    int r = count_lvl(a, b, n, modetype) > 0 ? 1 : 0;
+    if (r)
+      for (int i = 0; i < n; ++i)
+        if (!(std::fabs(b[i]) > (double)1e-6f)) { r = -2; break; }
+    route[c] = r;
+  }
+  return MCT_OK;
 }
 
 int mct_surfmodes_para(const double *thick, const double *vp, const double *vs, const double *rho,

@@ -29,6 +29,7 @@
 #include <algorithm>
 #include <cmath>
 #include <cfloat>
+#include <cstdlib>
 
 namespace {
 
@@ -58,7 +59,7 @@ __device__ __forceinline__ cx cexp_(cx z) {
   double s, c;
   if (fabs(z.im) > DBL_MIN) sincos(z.im, &s, &c);
   else { s = z.im; c = 1.0; }
-  const double e = exp(z.re);
+  const double e = z.re == 0.0 ? 1.0 : exp(z.re);   // exp(+-0) = 1 exactly
   return {e * c, e * s};
 }
 __device__ __forceinline__ cx csqrt_real(double x) {
@@ -107,65 +108,13 @@ __device__ void startl(double c, Col &g) {
 
 __device__ __forceinline__ cx decay(double d, double vk, cx q) { return cexp_(neg(rmul(d * vk, q))); }
 
-// The distinct entries of EinvE's two factors at interface j (1-based):
-// b44 (E^-1 of the layer above, divided by 2(1 - xi)) and a44 (E of the
-// layer below), Rayleigh.f90:404-440.
+// The distinct entries of EinvE's two factors (Rayleigh.f90:404-440): b44
+// (E^-1 of the layer above, divided by 2(1 - xi)) and a44 (E of the layer
+// below).
 struct Ev {
   cx P[6];      // b44: P0 = 1/den, P1..P5 the other entries / den
   cx A[6];      // a44: 1, cs1, cp1, n1, n2, n3
-  cx cp0, cs0, cp1, cs1;
 };
-__device__ void einve_vals(const Col &g, int j, double c, Ev &e) {
-  {  // the layer below (k = 1)
-    const int L = j;
-    const double am = g.MU(L), b = g.VS(L);
-    e.cp1 = csq(c, g.VP(L)); e.cs1 = csq(c, b);
-    const double t = c / b;
-    const cx xi = C(1.0 - t * t / 2.0);
-    e.A[0] = C(1.0); e.A[1] = e.cs1; e.A[2] = e.cp1;
-    e.A[3] = neg(rmul(am, e.cp1)); e.A[4] = neg(rmul(am, xi)); e.A[5] = neg(rmul(am, e.cs1));
-  }
-  {  // the layer above (k = 0)
-    const int L = j - 1;
-    const double am = g.MU(L), b = g.VS(L);
-    e.cp0 = csq(c, g.VP(L)); e.cs0 = csq(c, b);
-    const double t = c / b;
-    const cx xi = C(1.0 - t * t / 2.0);
-    const cx den = rmul(2.0, sub(C(1.0), xi));
-    e.P[0] = cdiv(C(1.0), den);
-    e.P[1] = cdiv(neg(cdiv(xi, e.cp0)), den);
-    e.P[2] = cdiv(neg(cdiv(C(1.0), rmul(am, e.cp0))), den);
-    e.P[3] = cdiv(cdiv(C(1.0), C(am)), den);
-    e.P[4] = cdiv(neg(cdiv(xi, e.cs0)), den);
-    e.P[5] = cdiv(neg(cdiv(C(1.0), rmul(am, e.cs0))), den);
-  }
-}
-// a44 only, for the interface above the top layer (EinvE(0, c, 1))
-__device__ void einve_top(const Col &g, double c, Ev &e) {
-  const double am = g.MU(0), b = g.VS(0);
-  e.cp1 = csq(c, g.VP(0)); e.cs1 = csq(c, b);
-  const double t = c / b;
-  const cx xi = C(1.0 - t * t / 2.0);
-  e.A[0] = C(1.0); e.A[1] = e.cs1; e.A[2] = e.cp1;
-  e.A[3] = neg(rmul(am, e.cp1)); e.A[4] = neg(rmul(am, xi)); e.A[5] = neg(rmul(am, e.cs1));
-}
-
-// Entry (R, Q) of b44 @ a44: b44 rows (P0 P1 P2 P3), (P4 P0 P3 P5), (P0 -P1
-// -P2 P3), (P4 -P0 -P3 P5); a44 columns (1 cp1 n1 n2), (cs1 1 n2 n3),
-// (1 -cp1 -n1 n2), (cs1 -1 -n2 n3).
-template <int R, int Q> __device__ __forceinline__ cx eent(const Ev &e) {
-  constexpr int bi[4][4] = {{0, 1, 2, 3}, {4, 0, 3, 5}, {0, 1, 2, 3}, {4, 0, 3, 5}};
-  constexpr int bs[4][4] = {{1, 1, 1, 1}, {1, 1, 1, 1}, {1, -1, -1, 1}, {1, -1, -1, 1}};
-  constexpr int ai[4][4] = {{0, 1, 0, 1}, {2, 0, 2, 0}, {3, 4, 3, 4}, {4, 5, 4, 5}};
-  constexpr int as[4][4] = {{1, 1, 1, 1}, {1, 1, -1, -1}, {1, 1, -1, -1}, {1, 1, 1, 1}};
-  cx s = C(0.0);
-#pragma unroll
-  for (int k = 0; k < 4; ++k) {
-    const cx p = mul(e.P[bi[R][k]], e.A[ai[k][Q]]);
-    s = (bs[R][k] * as[k][Q] > 0) ? add(s, p) : sub(s, p);
-  }
-  return s;
-}
 // Entry (R, Q) of a44 alone
 template <int R, int Q> __device__ __forceinline__ cx aent(const Ev &e) {
   constexpr int ai[4][4] = {{0, 1, 0, 1}, {2, 0, 2, 0}, {3, 4, 3, 4}, {4, 5, 4, 5}};
@@ -188,35 +137,134 @@ __device__ __forceinline__ M2 inv2(const M2 &x) {
   return {cdiv(x.d, det), cdiv(neg(x.b), det), cdiv(neg(x.c), det), cdiv(x.a, det)};
 }
 
-// SecFunSurf (Rayleigh.f90:92-125) after propup (Rayleigh.f90:455-491)
+// A layer's quantities at phase velocity c: the vertical slownesses cp, cs
+// (csq of a real argument: real, or imaginary when c exceeds the velocity;
+// zero when c equals it), xi = 1 - (c/vs)^2/2 and the normalised modulus.
+struct Lay {
+  cx cp, cs;
+  double xi, am;
+  bool cpi, csi, zero;           // cp / cs imaginary; either exactly zero
+};
+__device__ __forceinline__ Lay layer_at(const Col &g, int L, double c) {
+  Lay q;
+  q.am = g.MU(L);
+  const double b = g.VS(L);
+  q.cp = csq(c, g.VP(L)); q.cs = csq(c, b);
+  const double t = c / b;
+  q.xi = 1.0 - t * t / 2.0;
+  q.cpi = q.cp.re == 0.0; q.csi = q.cs.re == 0.0;
+  q.zero = (q.cp.re == 0.0 && q.cp.im == 0.0) || (q.cs.re == 0.0 && q.cs.im == 0.0);
+  return q;
+}
+__device__ __forceinline__ double nz(const cx &v, bool imag) { return imag ? v.im : v.re; }
+
+// E^-1 E of interface j from the layer above (u) and below (w), as EinvE
+// (Rayleigh.f90:404-440) evaluates it. Every entry of both factors is exactly
+// real or exactly imaginary (the other part an exact zero), so each product
+// term is one multiplication of the nonzero parts, added to the real or the
+// imaginary sum; the values are those of the full complex arithmetic. A
+// layer whose slowness is exactly zero takes the general path.
+struct E44 { cx e[4][4]; };
+__device__ void einve_pair(const Lay &u, const Lay &w, E44 &E) {
+  constexpr int bi[4][4] = {{0, 1, 2, 3}, {4, 0, 3, 5}, {0, 1, 2, 3}, {4, 0, 3, 5}};
+  constexpr int bs[4][4] = {{1, 1, 1, 1}, {1, 1, 1, 1}, {1, -1, -1, 1}, {1, -1, -1, 1}};
+  constexpr int ai[4][4] = {{0, 1, 0, 1}, {2, 0, 2, 0}, {3, 4, 3, 4}, {4, 5, 4, 5}};
+  constexpr int as[4][4] = {{1, 1, 1, 1}, {1, 1, -1, -1}, {1, 1, -1, -1}, {1, 1, 1, 1}};
+  if (u.zero || w.zero) {
+    Ev e;
+    e.A[0] = C(1.0); e.A[1] = w.cs; e.A[2] = w.cp;
+    e.A[3] = neg(rmul(w.am, w.cp)); e.A[4] = neg(rmul(w.am, C(w.xi))); e.A[5] = neg(rmul(w.am, w.cs));
+    const cx xi = C(u.xi);
+    const cx den = rmul(2.0, sub(C(1.0), xi));
+    e.P[0] = cdiv(C(1.0), den);
+    e.P[1] = cdiv(neg(cdiv(xi, u.cp)), den);
+    e.P[2] = cdiv(neg(cdiv(C(1.0), rmul(u.am, u.cp))), den);
+    e.P[3] = cdiv(cdiv(C(1.0), C(u.am)), den);
+    e.P[4] = cdiv(neg(cdiv(xi, u.cs)), den);
+    e.P[5] = cdiv(neg(cdiv(C(1.0), rmul(u.am, u.cs))), den);
+#pragma unroll
+    for (int r = 0; r < 4; ++r)
+#pragma unroll
+      for (int q = 0; q < 4; ++q) {
+        cx sm = C(0.0);
+#pragma unroll
+        for (int k = 0; k < 4; ++k) {
+          const cx pr = mul(e.P[bi[r][k]], e.A[ai[k][q]]);
+          sm = (bs[r][k] * as[k][q] > 0) ? add(sm, pr) : sub(sm, pr);
+        }
+        E.e[r][q] = sm;
+      }
+    return;
+  }
+  // b44's distinct entries (the layer above), Smith's quotients by the real
+  // 2(1 - xi) reduced to their nonzero parts
+  const double D = 2.0 * (1.0 - u.xi);
+  const double cpv = nz(u.cp, u.cpi), csv = nz(u.cs, u.csi);
+  double Pv[6];
+  bool Pi[6];
+  Pv[0] = 1.0 / D; Pi[0] = false;
+  Pv[3] = (1.0 / u.am) / D; Pi[3] = false;
+  Pv[1] = u.cpi ? (u.xi / cpv) / D : (-(u.xi / cpv)) / D; Pi[1] = u.cpi;
+  Pv[2] = u.cpi ? (1.0 / (u.am * cpv)) / D : (-(1.0 / (u.am * cpv))) / D; Pi[2] = u.cpi;
+  Pv[4] = u.csi ? (u.xi / csv) / D : (-(u.xi / csv)) / D; Pi[4] = u.csi;
+  Pv[5] = u.csi ? (1.0 / (u.am * csv)) / D : (-(1.0 / (u.am * csv))) / D; Pi[5] = u.csi;
+  // a44's distinct entries (the layer below)
+  const double wcp = nz(w.cp, w.cpi), wcs = nz(w.cs, w.csi);
+  const double Av[6] = {1.0, wcs, wcp, -(w.am * wcp), -(w.am * w.xi), -(w.am * wcs)};
+  const bool Ai[6] = {false, w.csi, w.cpi, w.cpi, false, w.csi};
+#pragma unroll
+  for (int r = 0; r < 4; ++r)
+#pragma unroll
+    for (int q = 0; q < 4; ++q) {
+      double re = 0.0, im = 0.0;
+#pragma unroll
+      for (int k = 0; k < 4; ++k) {
+        const bool pim = Pi[bi[r][k]], aim = Ai[ai[k][q]];
+        double pr = Pv[bi[r][k]] * Av[ai[k][q]];
+        if (pim && aim) pr = -pr;                    // i * i
+        const bool plus = bs[r][k] * as[k][q] > 0;
+        if (pim != aim) im = plus ? im + pr : im - pr;
+        else re = plus ? re + pr : re - pr;
+      }
+      E.e[r][q] = cx{re, im};
+    }
+}
+
+// SecFunSurf (Rayleigh.f90:92-125) after propup (Rayleigh.f90:455-491). The
+// layer below one interface is the layer above the previous one: its
+// slownesses and its decay exp(-d vk [cp, cs]) carry over (the same values
+// the reference recomputes).
 __device__ double secfun_surf(Col &g, double c, double *imf) {
   g.evals++;
   const double vk = g.w / c;
   const int j2 = g.ll - 1;
-  Ev e;
-  einve_vals(g, j2, c, e);
-  M2 a22 = inv2(M2{eent<0, 0>(e), eent<0, 1>(e), eent<1, 0>(e), eent<1, 1>(e)});
-  cx la0 = decay(g.D(j2 - 1), vk, e.cp0), la1 = decay(g.D(j2 - 1), vk, e.cs0);
+  Lay w = layer_at(g, j2, c), u = layer_at(g, j2 - 1, c);
+  E44 E;
+  einve_pair(u, w, E);
+  M2 a22 = inv2(M2{E.e[0][0], E.e[0][1], E.e[1][0], E.e[1][1]});
+  cx la0 = decay(g.D(j2 - 1), vk, u.cp), la1 = decay(g.D(j2 - 1), vk, u.cs);
   a22.a = mul(a22.a, la0); a22.c = mul(a22.c, la0);
   a22.b = mul(a22.b, la1); a22.d = mul(a22.d, la1);
-  M2 rdu = mm2(M2{eent<2, 0>(e), eent<2, 1>(e), eent<3, 0>(e), eent<3, 1>(e)}, a22);
+  M2 rdu = mm2(M2{E.e[2][0], E.e[2][1], E.e[3][0], E.e[3][1]}, a22);
   for (int j = j2 - 1; j >= 1; --j) {
-    einve_vals(g, j, c, e);
-    const cx lb0 = decay(g.D(j), vk, e.cp1), lb1 = decay(g.D(j), vk, e.cs1);
+    w = u;
+    u = layer_at(g, j - 1, c);
+    einve_pair(u, w, E);
+    const cx lb0 = la0, lb1 = la1;                  // decay(D(j), vk, [cp, cs] of layer j)
     M2 b22{mul(rdu.a, lb0), mul(rdu.b, lb0), mul(rdu.c, lb1), mul(rdu.d, lb1)};
-    M2 t = mm2(M2{eent<0, 2>(e), eent<0, 3>(e), eent<1, 2>(e), eent<1, 3>(e)}, b22);
-    a22 = inv2(M2{add(eent<0, 0>(e), t.a), add(eent<0, 1>(e), t.b), add(eent<1, 0>(e), t.c),
-                  add(eent<1, 1>(e), t.d)});
-    la0 = decay(g.D(j - 1), vk, e.cp0); la1 = decay(g.D(j - 1), vk, e.cs0);
+    M2 t = mm2(M2{E.e[0][2], E.e[0][3], E.e[1][2], E.e[1][3]}, b22);
+    a22 = inv2(M2{add(E.e[0][0], t.a), add(E.e[0][1], t.b), add(E.e[1][0], t.c), add(E.e[1][1], t.d)});
+    la0 = decay(g.D(j - 1), vk, u.cp); la1 = decay(g.D(j - 1), vk, u.cs);
     a22.a = mul(a22.a, la0); a22.c = mul(a22.c, la0);
     a22.b = mul(a22.b, la1); a22.d = mul(a22.d, la1);
-    t = mm2(M2{eent<2, 2>(e), eent<2, 3>(e), eent<3, 2>(e), eent<3, 3>(e)}, b22);
-    b22 = M2{add(eent<2, 0>(e), t.a), add(eent<2, 1>(e), t.b), add(eent<3, 0>(e), t.c), add(eent<3, 1>(e), t.d)};
+    t = mm2(M2{E.e[2][2], E.e[2][3], E.e[3][2], E.e[3][3]}, b22);
+    b22 = M2{add(E.e[2][0], t.a), add(E.e[2][1], t.b), add(E.e[3][0], t.c), add(E.e[3][1], t.d)};
     rdu = mm2(b22, a22);
   }
-  // la now holds layer 1's decays
+  // la now holds layer 1's decays; u is layer 1
   Ev top;
-  einve_top(g, c, top);
+  top.A[0] = C(1.0); top.A[1] = u.cs; top.A[2] = u.cp;
+  top.A[3] = neg(rmul(u.am, u.cp)); top.A[4] = neg(rmul(u.am, C(u.xi))); top.A[5] = neg(rmul(u.am, u.cs));
   M2 b22{mul(aent<2, 2>(top), la0), mul(aent<2, 3>(top), la1), mul(aent<3, 2>(top), la0),
          mul(aent<3, 3>(top), la1)};
   const M2 t = mm2(b22, rdu);
@@ -241,27 +289,33 @@ __device__ double secfun_love(Col &g, double c, double *imf) {
     rud0 = neg(cdiv(mul(a22_22, la2), a22_21));
   }
   // EinvE_L(j, c, 0) = b22 @ a22 with a22 = [[1, 1], [-m1 cs1, m1 cs1]] (the
-  // layer below) and b22 = [[m0 cs0, -1], [m0 cs0, 1]] / (2 m0 cs0) (above)
-  auto einve_l = [&](int j, cx &cs0, cx &cs1, M2 &E) {
+  // layer below) and b22 = [[m0 cs0, -1], [m0 cs0, 1]] / (2 m0 cs0) (above);
+  // the layer below one interface is the layer above the previous one, so
+  // its slowness and decay carry over
+  auto einve_l = [&](int j, const cx &cs0, const cx &cs1, M2 &E) {
     const double am1 = g.MU(j), am0 = g.MU(j - 1);
-    cs1 = csq(c, g.VS(j)); cs0 = csq(c, g.VS(j - 1));
     const cx a12 = rmul(am1, cs1);
     const M2 a{C(1.0), C(1.0), neg(a12), a12};
     const cx b0 = rmul(am0, cs0);
     const cx den = rmul(2.0, b0);
-    const M2 b{cdiv(b0, den), cdiv(C(-1.0), den), cdiv(b0, den), cdiv(C(1.0), den)};
+    const cx h = cdiv(b0, den);
+    const M2 b{h, cdiv(C(-1.0), den), h, cdiv(C(1.0), den)};
     E = mm2(b, a);
   };
   const int j2 = g.ll - 1;
-  cx cs0, cs1;
+  cx cs1 = csq(c, g.VS(j2)), cs0 = csq(c, g.VS(j2 - 1));
   M2 E;
   einve_l(j2, cs0, cs1, E);
-  cx td = cdiv(decay(g.D(j2 - 1), vk, cs0), E.a);
+  cx dec0 = decay(g.D(j2 - 1), vk, cs0);
+  cx td = cdiv(dec0, E.a);
   cx rdu = mul(E.c, td);
   for (int j = j2 - 1; j >= 1; --j) {
+    cs1 = cs0;
+    cs0 = csq(c, g.VS(j - 1));
     einve_l(j, cs0, cs1, E);
-    const cx r = mul(decay(g.D(j), vk, cs1), rdu);
-    td = cdiv(decay(g.D(j - 1), vk, cs0), add(E.a, mul(E.b, r)));
+    const cx r = mul(dec0, rdu);                    // decay(D(j), vk, cs of layer j)
+    dec0 = decay(g.D(j - 1), vk, cs0);
+    td = cdiv(dec0, add(E.a, mul(E.b, r)));
     rdu = mul(add(E.c, mul(E.d, r)), td);
   }
   const cx dsp = sub(C(1.0), mul(rud0, rdu));
@@ -700,22 +754,21 @@ __device__ void advance(Search &S, Col &g, const GrtJob &J, const double *buf) {
 }
 #undef REQUEST
 
-// Persistent grid over the columns (each thread walks q = tid, tid +
-// threads, ...); redo runs only the columns a previous pass left with ierr 2
+// Persistent grid over the columns: a lane whose column is done takes the
+// next one from the pool counter J.next; redo runs only the columns a
+// previous pass left with ierr 2
 // (trial list over that pass's room). Every round, each lane advances its
 // search to its next request; lanes wanting a trial list build it, then all
 // lanes wanting an evaluation evaluate together.
 template <int W>
-__global__ void __launch_bounds__(128) grt_kernel(GrtJob J, int cap, int redo) {
+__global__ void __launch_bounds__(128, W == 1 ? 3 : 4) grt_kernel(GrtJob J, int cap, int redo) {
   const long long tid = blockIdx.x * (long long)blockDim.x + threadIdx.x;
-  const long long nthreads = (long long)gridDim.x * blockDim.x;
   double *buf = J.scratch + (size_t)tid * (cap + 1);
   unsigned long long evals = 0;
   Search S;
   S.s = S_COLUMN_DONE; S.req = REQ_NONE; S.e = 0;
   Col g;
   g.evals = 0;
-  long long q = tid - nthreads;
   int c = -1;
   bool active = true;
   for (;;) {
@@ -726,8 +779,8 @@ __global__ void __launch_bounds__(128) grt_kernel(GrtJob J, int cap, int redo) {
           if (!(S.e == 2 && !redo)) evals += g.evals;   // a column redone in the next pass counts there
           c = -1;
         }
-        q += nthreads;
-        if (q >= J.n) { active = false; break; }
+        const unsigned q = atomicAdd(J.next, 1u);          // the next column of the pool
+        if (q >= (unsigned)J.n) { active = false; break; }
         const int cc = J.cols ? J.cols[q] : (int)q;
         if (redo && J.ierr[cc] != 2) continue;
         c = cc;
@@ -771,7 +824,19 @@ int grt_threads(int n, int pass, int modetype) {
     if (e != cudaSuccess || occ < 1) occ = 1;
   }
   const long want = (long)sms * (pass == 0 ? occ * 128 : 32);
-  long t = n < want ? n : want;
+  // columns per lane: one. Each lane's search is a chain of dependent FP64
+  // work, so the kernel's rate grows with the lanes in flight; two per lane
+  // balance a warp's lanes better only when the columns are several times
+  // the resident lanes (Rayleigh curves of 27,049 columns: 51 s with two,
+  // 61 s with one; of 6,700: four times slower with two).
+  // MCT_GRT_COLS_PER_LANE overrides it for tuning.
+  static const int per = [] {
+    const char *e = getenv("MCT_GRT_COLS_PER_LANE");
+    const int v = e ? atoi(e) : 1;
+    return v >= 1 ? v : 1;
+  }();
+  const long byn = (n + per - 1) / per;
+  long t = byn < want ? byn : want;
   t = (t + 127) / 128 * 128;
   return (int)(t > 0 ? t : 128);
 }
@@ -795,6 +860,7 @@ int launch_grt(const GrtJob &J, const double *const rows[4], double *cols4, cuda
   MCT_CUDA_TRY(cudaGetLastError());
   K.thk = dst[0]; K.vp = dst[1]; K.vs = dst[2]; K.rho = dst[3];
   for (int pass = 0; pass < 2; ++pass) {
+    MCT_CUDA_TRY(cudaMemsetAsync(K.next, 0, sizeof(unsigned), s));
     const int threads = grt_threads(J.n, pass, J.modetype);
     if (J.modetype == 1) grt_kernel<1><<<threads / 128, 128, 0, s>>>(K, pass == 0 ? kGrtCap0 : kGrtCap1, pass);
     else grt_kernel<0><<<threads / 128, 128, 0, s>>>(K, pass == 0 ? kGrtCap0 : kGrtCap1, pass);

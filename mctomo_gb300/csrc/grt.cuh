@@ -13,6 +13,7 @@ struct GrtJob {
   double *scratch;                        // grt_scratch_doubles(n) trial velocities
   const int *cols;                        // optional list of the n columns to run (else 0..ncol-1)
   int n;                                  // columns to run
+  unsigned *next;                         // pool counter (device, one word)
   double *phase, *group;                  // [ncol][np]
   int *ierr;                              // [ncol]: 0, 1 (no root), 2 (trial list over 20,000),
                                           // -1 (layer count), -2 (fluid layer)

@@ -107,6 +107,18 @@ def surfmodes_para(thick, vp, vs, rho, freqs, paras):
     return phase, group, ierr.value
 
 
+def surfmodes_route(nl, vp, vs, modetype):
+    """surfmodes' routing per column (mct_surfmodes_route): 1 generalized
+    R/T, 0 surfdisp96, -2 low-velocity layer under a fluid layer."""
+    nl = np.ascontiguousarray(nl, dtype=np.int32)
+    vp, vs = _f64(vp), _f64(vs)
+    ncol, nl_max = vp.shape
+    route = np.zeros(ncol, np.int32)
+    check("mct_surfmodes_route", lib().mct_surfmodes_route(ncol, nl_max, ptr(nl), ptr(vp), ptr(vs), modetype,
+                                                           ptr(route)))
+    return route
+
+
 def grt_batch(nl, thk, vp, vs, rho, freqs, paras):
     """The generalized R/T fundamental-mode search (RayleighModes / LoveModes,
     surfmodes/surfmodes.f90:185-303) for many FP64 columns: thk/vp/vs/rho

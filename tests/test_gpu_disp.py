@@ -92,15 +92,25 @@ def test_mmodes_and_single_column_entry_points(orc, gpulib):
         assert np.max(np.abs(mcp[good] - e2[0][0][good]), initial=0) <= PHASE_TOL
 
 
-def test_surfmodes_routes_lvl_columns_to_unsupported(gpulib):
+def test_surfmodes_routes_lvl_columns_to_grt(orc, gpulib):
+    # a layer slower than the top layer: the generalized R/T search, as the
+    # reference's surfmodes routes it (surfmodes.f90:39-108); under a fluid
+    # layer that path (the Stoneley mode) is not built and is refused
+    from test_grt_oracle import grt
     thick = np.array([1.0, 1.0, 1.0, 0.0])
     vs = np.array([1.0, 0.6, 1.5, 2.0])
     vp = vs * 1.73
     rho = np.full(4, 2.0)
+    freqs = 1.0 / np.geomspace(0.5, 5, 5)
+    ph, gr, ierr = surfmodes(thick, vp, vs, rho, freqs, 1, 0, 0.001)
+    e, eph, _, _ = grt(orc, thick, vp, vs, rho, freqs, 1, pg=0)
+    assert ierr == e
+    np.testing.assert_allclose(ph, eph, rtol=0, atol=1e-9)
+    # water over a solid whose second layer is slower than the first
     with pytest.raises(MctError) as ei:
-        surfmodes(thick, vp, vs, rho, 1.0 / np.geomspace(0.5, 5, 5), 1, 0, 0.001)
+        surfmodes(thick, np.array([1.5, 1.73, 1.04, 3.46]), np.array([0.0, 1.0, 0.6, 2.0]), rho, freqs, 1, 0, 0.001)
     assert ei.value.code == -5
-    ph, gr, ierr = surfmodes(thick, vp, np.array([1.0, 1.2, 1.5, 2.0]), rho, 1.0 / np.geomspace(0.5, 5, 5), 1, 0, 0.001)
+    ph, gr, ierr = surfmodes(thick, vp, np.array([1.0, 1.2, 1.5, 2.0]), rho, freqs, 1, 0, 0.001)
     assert ierr == 0 and np.all(ph > 0.8) and np.all(ph < 2.0)
 
 

@@ -121,3 +121,20 @@ def test_routing_count(orc):
     assert orc.orc_grt_nlvls1(4, P(d), P(vs2 * 1.73), P(vs2), P(rho), 1) == 0
     vs3 = np.array([0.0, 1.5, 2.0, 3.0])     # fluid top: the Stoneley path is not restated
     assert orc.orc_grt_nlvls1(4, P(d), P(np.array([1.5, 2.6, 3.4, 5.2])), P(vs3), P(rho), 1) == -2
+
+
+def test_route_matches_setup_grt(orc, gpulib):
+    # mct_surfmodes_route (host code of the library) against the oracle's
+    # setup_grt count, on synthetic study columns
+    from mctomo_gb300 import forward, synthetic
+    rng = np.random.default_rng(5)
+    nl, thk, vp, vs, rho = synthetic.layered_columns(rng, 400, nl_range=(12, 40), lvl_prob=0.1)
+    thk, vp, vs, rho = (np.ascontiguousarray(x, np.float64) for x in (thk, vp, vs, rho))
+    for mt in (1, 0):
+        route = forward.surfmodes_route(nl, vp, vs, mt)
+        for c in range(len(nl)):
+            k = int(nl[c])
+            n = orc.orc_grt_nlvls1(k, P(np.ascontiguousarray(thk[c, :k])), P(np.ascontiguousarray(vp[c, :k])),
+                                   P(np.ascontiguousarray(vs[c, :k])), P(np.ascontiguousarray(rho[c, :k])), mt)
+            assert route[c] == (1 if n > 0 else 0), (c, route[c], n)
+        assert 0 < np.sum(route == 1) < len(nl)
