@@ -1607,6 +1607,23 @@ def case_disp(precision=1, columns=4096, study=False):
           f"evals_fp64={cnt[0]} evals_fp32={cnt[1]} cp00={cp[0, 0, 0]:.6f}")
 
 
+def case_grt(modetype=1, columns=20, periods=4):
+    """A small generalized R/T case for ncu: the first columns of a seeded
+    draw that route to the generalized R/T search, a few periods."""
+    forward, synthetic = _case_modules()
+    rng = np.random.default_rng(11)
+    nl, thk, vp, vs, rho = synthetic.layered_columns(rng, 64 * columns, nl_range=(12, 40), lvl_prob=0.1)
+    thk, vp, vs, rho = (np.ascontiguousarray(x, np.float64) for x in (thk, vp, vs, rho))
+    sel = np.where(forward.surfmodes_route(nl, vp, vs, modetype) == 1)[0][:columns]
+    freqs = 1.0 / np.geomspace(0.2, 20.0, 60)[::max(1, 60 // periods)][:periods]
+    t0 = time.perf_counter()
+    ph, gr, ierr, nev = forward.grt_batch(nl[sel], thk[sel], vp[sel], vs[sel], rho[sel], freqs,
+                                          forward.modes_para(modetype, 1))
+    dt = time.perf_counter() - t0
+    print(f"grt modetype={modetype} columns={len(sel)} periods={len(freqs)} call_s={dt:.4f} evals={nev} "
+          f"ierr={int((ierr != 0).sum())} ph00={ph[0, 0]:.6f}")
+
+
 def case_grid():
     forward, synthetic = _case_modules()
     rng = np.random.default_rng(3)
@@ -1665,6 +1682,8 @@ def run_case(a):
         case_disp(a.case_precision, a.case_columns, a.case_study)
     elif a.case == "tiles":
         case_tiles(a.chains)
+    elif a.case == "grt":
+        case_grt(1 if a.case_order is None else a.case_order, min(a.case_columns, 128))
     else:
         case_grid()
 
@@ -1704,7 +1723,7 @@ def main():
                     help="body workload: keep the stations' travel-time fields and time location steps on them")
     ap.add_argument("--solver", default=None, choices=["tiles", "heap"],
                     help="body workload: 3D solver (default: heap march for order 1, tiles for order 0)")
-    ap.add_argument("--case", default=None, choices=["fm2d", "eik3", "eik3heap", "disp", "grid", "tiles"],
+    ap.add_argument("--case", default=None, choices=["fm2d", "eik3", "eik3heap", "disp", "grid", "tiles", "grt"],
                     help="run one small fixed case of a hot kernel (for profilers) instead of a workload")
     ap.add_argument("--case-precision", type=int, default=1)
     ap.add_argument("--case-maps", type=int, default=16)

@@ -552,6 +552,7 @@ enum : int { REQ_NONE = 0, REQ_EVAL = 1, REQ_CI = 2 };
 
 struct Search {
   int s, ret, req;
+  int sl;                      // run startl(rc) before the requested evaluation
   double rc;                   // requested phase velocity
   double f, imf;               // delivered secular-function value
   int index0, start, im1;      // delivered trial list
@@ -570,7 +571,9 @@ __device__ __forceinline__ void bis_begin(Search &S, double x1, double x2, doubl
   S.xt1 = (S.xa + S.xb) / 2.0; S.ret = ret; S.s = B_ITER;
 }
 
-#define REQUEST(c, next) do { S.rc = (c); S.req = REQ_EVAL; S.s = (next); return; } while (0)
+#define REQUEST(c, next) do { S.rc = (c); S.sl = 0; S.req = REQ_EVAL; S.s = (next); return; } while (0)
+// an evaluation at a scan point, which the reference precedes by startl at it
+#define REQUEST_SL(c, next) do { S.rc = (c); S.sl = 1; S.req = REQ_EVAL; S.s = (next); return; } while (0)
 
 template <int W>
 __device__ void advance(Search &S, Col &g, const GrtJob &J, const double *buf) {
@@ -643,15 +646,15 @@ __device__ void advance(Search &S, Col &g, const GrtJob &J, const double *buf) {
       if (g.nlvl1 == 0) {
         while (ccc[im2] < S.cray - 2.0 * g.dc) { im2++; if (im2 == S.index0) break; }
       }
-      S.k2 = ccc[im2]; startl(S.k2, g); S.ip = im2 + 1;
-      REQUEST(S.k2, R_FB_FIRST);
+      S.k2 = ccc[im2]; S.ip = im2 + 1;
+      REQUEST_SL(S.k2, R_FB_FIRST);
     }
     case R_FB_FIRST: S.f2 = S.f; S.s = R_FB_NEXT; break;
     case R_FB_NEXT: {
       if (S.ip > S.index0) { S.s = R_END; break; }
       const double *ccc = buf + S.start - 1;
-      S.k1 = S.k2; S.f1 = S.f2; S.k2 = ccc[S.ip]; startl(S.k2, g); S.iq = -1;
-      REQUEST(S.k2, R_FB_GOT);
+      S.k1 = S.k2; S.f1 = S.f2; S.k2 = ccc[S.ip]; S.iq = -1;
+      REQUEST_SL(S.k2, R_FB_GOT);
     }
     case R_FB_GOT:
       S.f2 = S.f;
@@ -669,15 +672,15 @@ __device__ void advance(Search &S, Col &g, const GrtJob &J, const double *buf) {
       if (S.index0 < 0) { S.e = 2; S.s = S_DONE_SEARCH; break; }
       S.ierr = 1; S.iq = -1; S.c0l = S.cray;
       const double *ccc = buf + S.start - 1;
-      S.k2 = ccc[1]; startl(S.k2, g); S.ip = 2;
-      REQUEST(S.k2, L_FIRST);
+      S.k2 = ccc[1]; S.ip = 2;
+      REQUEST_SL(S.k2, L_FIRST);
     }
     case L_FIRST: S.f2 = S.f; S.s = L_NEXT; break;
     case L_NEXT: {
       if (S.ip > S.index0) { S.s = L_FB_BEGIN; break; }
       const double *ccc = buf + S.start - 1;
-      S.k1 = S.k2; S.f1 = S.f2; S.k2 = ccc[S.ip]; startl(S.k2, g); S.iq = -1;
-      REQUEST(S.k2, L_GOT);
+      S.k1 = S.k2; S.f1 = S.f2; S.k2 = ccc[S.ip]; S.iq = -1;
+      REQUEST_SL(S.k2, L_GOT);
     }
     case L_GOT:
       S.f2 = S.f;
@@ -690,8 +693,8 @@ __device__ void advance(Search &S, Col &g, const GrtJob &J, const double *buf) {
       break;
     case L_FB_BEGIN:
       if (S.ierr == 1 && isfinite(S.c0l)) {
-        S.k2 = (double)1.1f * S.c0l; startl(S.k2, g);
-        REQUEST(S.k2, L_FB_FIRST);
+        S.k2 = (double)1.1f * S.c0l;
+        REQUEST_SL(S.k2, L_FB_FIRST);
       }
       S.s = L_END;
       break;
@@ -699,8 +702,7 @@ __device__ void advance(Search &S, Col &g, const GrtJob &J, const double *buf) {
     case L_FB_NEXT:
       S.k1 = S.k2 - g.dc;
       if (S.k1 < g.vsm) { S.s = L_END; break; }
-      startl(S.k1, g);
-      REQUEST(S.k1, L_FB_GOT);
+      REQUEST_SL(S.k1, L_FB_GOT);
     case L_FB_GOT:
       S.f1 = S.f; S.iq = -1;
       if (S.f1 * S.f2 < 0.) { bis_begin(S, S.k1, S.k2, S.f1, S.f2, L_FB_BIS); break; }
@@ -753,6 +755,7 @@ __device__ void advance(Search &S, Col &g, const GrtJob &J, const double *buf) {
   }
 }
 #undef REQUEST
+#undef REQUEST_SL
 
 // Persistent grid over the columns: a lane whose column is done takes the
 // next one from the pool counter J.next; redo runs only the columns a
@@ -794,10 +797,14 @@ __global__ void __launch_bounds__(128, W == 1 ? 3 : 4) grt_kernel(GrtJob J, int 
       advance<W>(S, g, J, buf);
     }
     if (!__any_sync(0xffffffffu, active)) break;
+    __syncwarp();                                       // the lanes take the requests together
     if (active && S.req == REQ_CI) {
       S.index0 = c_interval<W>(g, buf, cap, &S.start, &S.im1);
       S.req = REQ_NONE;
-    } else if (active && S.req == REQ_EVAL) {
+    }
+    __syncwarp();
+    if (active && S.req == REQ_EVAL) {
+      if (S.sl) startl(S.rc, g);
       S.f = secfun<W>(g, S.rc, &S.imf);
       S.req = REQ_NONE;
     }
