@@ -449,14 +449,14 @@ int mct_eikonal3d_batch(int nsolve, int nx, int ny, int nz, double dx,
                         double *tfield, int *passes);
 
 /* The tile solver's configuration (tile shape index * 4 + local sweeps
- * index, 0..43: shapes 8x8x8, 4x8x16, 8x4x16, 16x8x4, 8x16x4, 8x8x4, 8x4x8,
- * 4x8x8, 4x4x8, 4x8x4, 8x4x4; 12, 24, 48 or 96 sweeps per visit). No counterpart in the
+ * index, 0..47: shapes 8x8x8, 4x8x16, 8x4x16, 16x8x4, 8x16x4, 8x8x4, 8x4x8,
+ * 4x8x8, 4x4x8, 4x8x4, 8x4x4, 4x4x4; 12, 24, 48 or 96 sweeps per visit). No counterpart in the
  * reference, whose solver has no tuning.
  * cfg = -1: tuned per (device, grid shape, order), the default; the tuner
  * times every configuration on the first call for a key. Configurations
  * differ in the last units of the fixed-point times (2^-shift s), so times
  * can differ by that much between processes whose tuners chose differently:
- * pin one (0..43) for reproducible times. Returns the previous setting. With
+ * pin one (0..47) for reproducible times. Returns the previous setting. With
  * cfg < -1, returns the configuration tuned on the current device for
  * (nx, ny, nz, order), or -1 if none yet, and changes nothing. */
 int mct_eik3_tile_config(int cfg, int nx, int ny, int nz, int order);

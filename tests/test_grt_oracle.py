@@ -138,3 +138,41 @@ def test_route_matches_setup_grt(orc, gpulib):
                                    P(np.ascontiguousarray(vs[c, :k])), P(np.ascontiguousarray(rho[c, :k])), mt)
             assert route[c] == (1 if n > 0 else 0), (c, route[c], n)
         assert 0 < np.sum(route == 1) < len(nl)
+
+
+def test_roots_are_roots_of_the_surfdisp96_period_equations(orc):
+    # On study columns with a low-velocity layer, the generalized R/T roots are
+    # zeros of the Haskell-Thomson / Dunkin period equations that the
+    # surfdisp96 oracle evaluates (dltar1 for Love, dltar4 for Rayleigh; an
+    # independent formulation): a sign change within 4 tol. For Rayleigh this
+    # holds below the top layer's shear velocity; above it the reference
+    # brackets sign changes of the real part of its determinant and also
+    # accepts points where that part is merely small, which are often not
+    # roots (kept as the reference does; counted, not asserted).
+    from mctomo_gb300 import synthetic
+    rng = np.random.default_rng(21)
+    nl, thk, vp, vs, rho = synthetic.layered_columns(rng, 300, nl_range=(12, 40), lvl_prob=0.1)
+    freqs = 1.0 / np.geomspace(0.2, 20.0, 20)
+    for mt, kk in ((0, 1), (1, 2)):
+        hit = miss = cols = 0
+        for c in range(len(nl)):
+            n = int(nl[c])
+            m4 = [np.ascontiguousarray(x[c, :n], np.float32) for x in (thk, vp, vs, rho)]
+            m8 = [x.astype(np.float64) for x in m4]
+            if orc.orc_grt_nlvls1(n, *[P(x) for x in m8], mt) <= 0:
+                continue
+            cols += 1
+            if cols > 12:
+                break
+            _, ph, _, _ = grt(orc, *m8, freqs, mt)
+            for i, (f, cv) in enumerate(zip(freqs, ph)):
+                if cv <= 0 or (mt == 1 and cv >= m8[2][0]):
+                    continue
+                tol = 1e-6 + (len(freqs) - i) * 9e-6 / len(freqs)
+                om = 2 * np.pi * f
+                d = [orc.orc_dltar(om / x, om, kk, *[P(a) for a in m4], n) for x in (cv - 4 * tol, cv + 4 * tol)]
+                if d[0] * d[1] <= 0:
+                    hit += 1
+                else:
+                    miss += 1
+        assert hit > 50 and miss <= 0.01 * (hit + miss), (mt, hit, miss)
