@@ -1027,6 +1027,12 @@ TT2D_CONFIG = {"workload": "plain 2D travel-time likelihood (the 2D code's path)
                "grid": [51, 51], "stations": 16, "times": 240}
 
 
+# FP64 operations per secular evaluation of the generalized R/T search as the
+# kernel executes them (DADD + DMUL + 2 x DFMA thread instructions over the
+# evaluations of the small ncu case, search logic included):
+# profiles/grt_study_27041_columns.md
+GRT_FP64_FLOPS_PER_EVAL = {1: (21567665 + 22925835 + 2 * 31357386) / 4276,
+                           0: (24931182 + 46682971 + 2 * 149068957) / 13014}
 GRT_CONFIG = {"workload": "generalized R/T fundamental-mode dispersion (the reference's single-mode surfmodes path "
                          "for low-velocity-layer columns): layered columns drawn as the dispersion study's (12-40 "
                          "layers, h U[0.05,0.5] km, Vs U[0.2,3.5] km/s with a 10% low-velocity-layer chance, "
@@ -1135,12 +1141,27 @@ def run_grt(args):
             "secular_evaluations_per_s": round(sum(evals.values()) / (ms / 1e3)),
             "e2e": {"value": round(curves / e2e_s, 2), "unit": "curves/s", "h2d_bytes_per_step": int(lay_b),
                     "d2h_bytes_per_step": int(out_b)},
-            "accuracy": acc, "clocks": cl,
+            "accuracy": acc, "clocks": cl, "roofline": grt_roofline(evals, ms),
             "gpu_launches": args.steps * 2 * 6,
             "timing": "the two wave types on two streams; warm-up launches on 64 columns of each"}
     if not args.no_cpu:
         line["cpu_baseline"] = cpu
     print(json.dumps(line), flush=True)
+
+
+def grt_roofline(evals, ms):
+    """FP64 roofline of the generalized R/T step: the executed FP64
+    operations per secular evaluation (ncu) times the evaluations, over the
+    step's time, against the FP64 peak."""
+    flops = sum(GRT_FP64_FLOPS_PER_EVAL[mt] * evals[mt] for mt in (1, 0))
+    achieved = flops / (ms / 1e3) / 1e12
+    return {"kernel": "grt_kernel (Rayleigh and Love on two streams)", "bound": "fp64",
+            "achieved": round(achieved, 4), "peak": round(FP64_PEAK_TFLOPS, 4),
+            "peak_kind": "rated (2 DFMA/cycle/SM x 152 SMs x 2.07 GHz); MEASURED_PEAKS.json has no FP64 figure",
+            "unit": "TFLOP/s", "frac": round(achieved / FP64_PEAK_TFLOPS, 4), "traffic": None,
+            "fp64_flops_per_evaluation": {"rayleigh": round(GRT_FP64_FLOPS_PER_EVAL[1]),
+                                          "love": round(GRT_FP64_FLOPS_PER_EVAL[0])},
+            "limiter": "latency of dependent FP64 chains per lane (ncu: dominant stall 'wait'); lanes in flight"}
 
 
 def grt_oracle_sample(nl, thk, vp, vs, rho, freqs, waves, host, args):
