@@ -176,3 +176,17 @@ def test_roots_are_roots_of_the_surfdisp96_period_equations(orc):
                 else:
                     miss += 1
         assert hit > 50 and miss <= 0.01 * (hit + miss), (mt, hit, miss)
+
+
+def test_trial_list_beyond_the_reference_arrays(orc):
+    # Two 200 km layers at 0.1 Hz: C_Interval_L would place (NN + 1) * 512
+    # trial velocities, more than the reference's 20,000-entry arrays hold
+    # (surfmodes/C_interval_L.f90:24-30); the column gets ierr 2 at once and
+    # no secular evaluation. The Rayleigh search finds its root in the window
+    # below vs1 and never builds the list.
+    thk, vs = np.array([200.0, 200.0, 0.0]), np.array([1.5, 1.0, 3.0])
+    vp, rho = vs * 1.73, np.full(3, 2.5)
+    e, ph, gr, ne = grt(orc, thk, vp, vs, rho, np.array([0.1]), 0)
+    assert e == 2 and ph[0] == 0 and ne == 0
+    e, ph, gr, ne = grt(orc, thk, vp, vs, rho, np.array([0.1]), 1)
+    assert e == 0 and ph[0] > 0
