@@ -1028,9 +1028,9 @@ TT2D_CONFIG = {"workload": "plain 2D travel-time likelihood (the 2D code's path)
 
 
 # FP64 operations per secular evaluation of the generalized R/T search as the
-# kernel executes them (DADD + DMUL + 2 x DFMA thread instructions over the
-# evaluations of the small ncu case, search logic included):
-# profiles/grt_study_27041_columns.md
+# kernel executes them: DADD + DMUL + 2 x DFMA thread instructions (ncu
+# counters) over the evaluations of `bench.py --case grt --case-columns 20`
+# (Rayleigh, then --case-order 0 for Love), search logic included
 GRT_FP64_FLOPS_PER_EVAL = {1: (21567665 + 22925835 + 2 * 31357386) / 4276,
                            0: (24931182 + 46682971 + 2 * 149068957) / 13014}
 GRT_CONFIG = {"workload": "generalized R/T fundamental-mode dispersion (the reference's single-mode surfmodes path "
